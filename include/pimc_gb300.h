@@ -1,0 +1,248 @@
+/*
+ * pimc_gb300.h -- C ABI of the GB300-native WA-PIMC hot path.
+ *
+ * The library owns its device memory and one CUDA stream per context.  Every
+ * entry point returns 0 on success or a negative PGB_E* code; the message of
+ * the last failure is available from pgb_last_error().  No entry point aborts,
+ * throws across the ABI or falls back to a CPU path: when the CUDA device or
+ * the kernels are unavailable the call fails with PGB_ECUDA.
+ *
+ * Each group below names the reference interface it replaces (file:line in
+ * the DelMaestroGroup/pimc tree).  Arrays follow the reference's own layouts:
+ *   positions  AoS FP64 [M][Ne][3]     (Path::beads, include/path.h:164)
+ *   links      int32   [M][Ne][2]      (Path::nextLink/prevLink, path.h:165)
+ *   on flags   uint8   [M][Ne]         (Worm::beads, include/worm.h:153)
+ *   beads      int32   [k][2]          (beadLocator = {slice, ptcl})
+ *   worm       int32   [8]             head, tail, special1, special2
+ * A context is used from one host thread at a time; calls on one context are
+ * serialised on its stream and are synchronous from the caller's view unless
+ * the name says "_async".
+ */
+#ifndef PIMC_GB300_H
+#define PIMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGB_OK        0
+#define PGB_EINVAL   -1   /* bad argument or size */
+#define PGB_ECUDA    -2   /* CUDA runtime / launch failure or no device */
+#define PGB_ENOMEM   -3   /* device allocation refused */
+#define PGB_ESTATE   -4   /* call out of order (e.g. no path loaded) */
+#define PGB_ETIMEOUT -5   /* a bounded device wait ran out */
+
+/* precision of the pair sums */
+#define PGB_FP64   0      /* plain form: FP64 direct-lookup Aziz tables */
+#define PGB_MIXED  1      /* FP32 analytic Aziz pairs, FP64 accumulation */
+
+/* modes of pgb_bead_actions */
+#define PGB_ACTION_FULL 0 /* LocalAction::potentialAction(bead)     action.cpp:487 */
+#define PGB_ACTION_BARE 1 /* LocalAction::barePotentialAction(bead) action.cpp:628 */
+#define PGB_ACTION_CORR 2 /* LocalAction::potentialActionCorrection action.cpp:696 */
+
+typedef struct pgb_ctx pgb_ctx;
+
+/* Physical and numerical parameters of one path (constants.cpp:120-166,
+ * setup.cpp:1216-1266, container.cpp:84-113). */
+typedef struct {
+    double side[3];         /* periodic box sides, A */
+    int    num_slices;      /* M (the reference forces it even) */
+    int    num_ptcl_ext;    /* Ne, bead-array extent per slice */
+    double tau;             /* imaginary time step, 1/K */
+    double lambda;          /* hbar^2/2m, K A^2 (24.24/mass) */
+    double rc;              /* cutoff; LookupTable list uses |sep|^2 < rc^2 */
+    double vfactor[2];      /* even/odd VFactor (primitive 1,1; gsf 2/3,4/3) */
+    double gradvfactor[2];  /* even/odd gradVFactor (gsf 0,2/9) */
+    int    period;          /* action period (1 primitive, 2 gsf) */
+    int    aziz_year;       /* 1979 (HFDHE2), 1987 or 1995 */
+    int    virial_window;   /* centroid virial window, reference default 5 */
+    int    precision;       /* PGB_FP64 or PGB_MIXED */
+    double mu;              /* chemical potential for E_mu columns */
+} pgb_params;
+
+/* ---- context: replaces the construction in pdrive.cpp:84-150 ---------- */
+int         pgb_create(const pgb_params* p, pgb_ctx** out);
+int         pgb_destroy(pgb_ctx* ctx);
+const char* pgb_last_error(const pgb_ctx* ctx);   /* ctx may be NULL */
+int         pgb_device_info(char* name, int cap, int* sm_count, int* cc);
+
+/* ---- Aziz potential: AzizPotential (potential.h:933-1017,
+ *      potential.cpp:1741-1907).  Tables are built on the device from the
+ *      host-accumulated r_k = r_{k-1} + dr sequence (potential.h:176-183). -- */
+int pgb_table_info(pgb_ctx* ctx, int* length, double* dr, double* tailV);
+int pgb_copy_tables(pgb_ctx* ctx, double* V, double* dV, double* d2V);
+/* PotentialBase::V(const dVec*, double*, int), potential.h:86 / potential.cpp:127:
+ * batched V(sep) for n separation vectors (AoS [n][3]). */
+int pgb_potential_batch(pgb_ctx* ctx, const double* sep, double* out, int n);
+/* gradV (potential.h:997) and grad2V (potential.h:1010) batched */
+int pgb_gradv_batch(pgb_ctx* ctx, const double* sep, double* out3, int n);
+int pgb_grad2v_batch(pgb_ctx* ctx, const double* sep, double* out, int n);
+
+/* ---- worldline state: Path/Worm/LookupTable updates (path.cpp:197-420,
+ *      lookuptable.cpp:314-458).  The device mirror must follow every bead
+ *      change the caller makes, as the reference mutates before it asks. -- */
+int pgb_load_path(pgb_ctx* ctx, const double* pos, const int32_t* next,
+                  const int32_t* prev, const uint8_t* on, const int32_t* worm8);
+int pgb_update_beads(pgb_ctx* ctx, const int32_t* beads, const double* pos, int k);
+int pgb_get_positions(pgb_ctx* ctx, double* pos);
+
+/* ---- potential action: LocalAction (action.cpp:456-740) --------------
+ * Per-bead U_b for k beads at imaginary-time shift `shift` (bisection level
+ * spacing, ActionBase::setShift action.h:119).  out_per_bead may be NULL;
+ * out_sum receives the sum over beads in list order (ActionBase list and
+ * range forms, action.cpp:384-405, 572-620).  Inactive beads give 0. */
+int pgb_bead_actions(pgb_ctx* ctx, const int32_t* beads, int k, int shift,
+                     int mode, double* out_per_bead, double* out_sum);
+/* potentialAction(startBead, endBead), action.cpp:522-570: follows next links */
+int pgb_range_action(pgb_ctx* ctx, int s0, int p0, int s1, int p1, int shift,
+                     double* out);
+/* potentialAction() over the whole path, action.cpp:456-472 */
+int pgb_full_action(pgb_ctx* ctx, double* out);
+/* kineticAction(), action.cpp:345-369 */
+int pgb_kinetic_action(pgb_ctx* ctx, double* out);
+
+/* Per-slice sums behind the estimator-facing ActionBase virtuals
+ * (action.cpp:751-806, 902-947, 1188-1223, 1446-1803).  Arrays of length M:
+ *  vint[t]  sum_{i<j} factor V(r_j - r_i)              (V(slice)[1])
+ *  g2[t]    sum_i |sum_{j!=i} gradV(r_i - r_j)|^2      (gradVSquared(slice))
+ *  r1[t]    sum_i gradV_i . r_i                        (rDOTgradUterm1 / (VF tau))
+ *  r2[t]    sum_i (T_i gradV_i) . r_i                  (rDOTgradUterm2 / (2 gF tau^3 lambda))
+ *  d1[t]    sum_i gradV_i . delta_i                    (deltaDOTgradUterm1 / (VF tau))
+ *  d2[t]    sum_i (T_i gradV_i) . delta_i              (deltaDOTgradUterm2 / (...))
+ *  kin[t]   sum_i |r_{t+1} - r_t|^2 on the next link    (getVelocity, path.h:189)
+ *  xch[t]   sum_i (r_{t+W} - r_t) . (r_{t+1} - r_t)      (virial T2 term)
+ * Any pointer may be NULL.  r2/d2 need the T-matrix and are computed only
+ * when non-NULL. */
+typedef struct {
+    double *vint, *g2, *r1, *r2, *d1, *d2, *kin, *xch;
+} pgb_slice_terms;
+int pgb_slice_terms_compute(pgb_ctx* ctx, pgb_slice_terms* out);
+
+/* ---- estimators (estimator.cpp:917-1252, 3661-4236) -------------------
+ * One accumulate() of EnergyEstimator: K, V, V_ext, V_int, E, E_mu, K/N,
+ * V/N, E/N (estimator.cpp:940-1029). */
+int pgb_energy(pgb_ctx* ctx, double out9[9]);
+/* One accumulate() of VirialEnergyEstimator, 19 columns
+ * (estimator.cpp:1086-1252).  cvcov2_quirk = 1 keeps the reference's
+ * misspelt "cVCov2" key, which adds totEcv*beta*dEdB into column 0. */
+int pgb_virial(pgb_ctx* ctx, int cvcov2_quirk, double out19[19]);
+/* EstimatorBase::getQVectors (estimator.cpp:439-570).  Returns the number
+ * of q-vectors through *count; fills at most cap of them into q[3*i]. */
+int pgb_qvectors(const char* type, const char* input, const double side[3],
+                 double* q, int cap, int* count);
+/* S(q): StaticStructureFactor(GPU)Estimator::accumulate
+ * (estimator.cpp:3705-3737, 3824-3861), per-sample value already divided by
+ * N M (the reference's norm 1/M applied), via rho_q. */
+int pgb_ssf(pgb_ctx* ctx, const double* q, int nq, double* out);
+/* F(q,tau): IntermediateScatteringFunctionEstimatorGpu::accumulate
+ * (estimator.cpp:4063-4100, gpu_isf estimator_gpu.cu:67-165): layout
+ * [q][M/2+1], value (1/(N M)) sum_{t,i,j} cos(q.(r_j(t+tau) - r_i(t))).
+ * mode 0: CUDA-core correlation; mode 1: tensor-core (tcgen05, split-BF16)
+ * DFT correlation.  PGB_FP64 contexts always use the FP64 direct form. */
+int pgb_isf(pgb_ctx* ctx, const double* q, int nq, int mode, double* out);
+/* rho_q(t) of the loaded path, layout [q][M][2] (FP64 values) */
+int pgb_rhoq(pgb_ctx* ctx, const double* q, int nq, double* out);
+
+/* ---- device-resident variants for timing: inputs already in device
+ *      memory, results left on the device (no host copies, no syncs). ---- */
+int pgb_isf_device_async(pgb_ctx* ctx, const double* d_q, int nq, int mode,
+                         double* d_out);
+int pgb_load_positions_device_async(pgb_ctx* ctx, const double* d_pos);
+void* pgb_stream(pgb_ctx* ctx);   /* the context's cudaStream_t */
+
+/* ---- batched walkers: many independent canonical chains in one
+ *      persistent kernel (no reference counterpart; replaces running many
+ *      pimc.e processes with offset seeds, setup.cpp:921-923). ---------- */
+typedef struct pgb_walkers pgb_walkers;
+typedef struct {
+    int           num_walkers;
+    const int*    num_ptcl;     /* N_w */
+    const int*    num_slices;   /* M_w (even) */
+    const double* temperature;  /* T_w = 1/(M_w tau) */
+    const double* side;         /* cube side L_w */
+    const int*    mbar;         /* staging length Mbar_w (even, >= 2) */
+    double        tau, lambda;
+    double        p_com;        /* centre-of-mass move probability */
+    uint64_t      seed;         /* Philox key; walker w uses stream w */
+    int           aziz_year;
+    int           threads_per_walker; /* 0: autotune */
+    int           var_updates;  /* 1: stage length 2 + U{0..Mbar-2} */
+} pgb_walkers_params;
+
+typedef struct {
+    double    energy_sum;      /* sum of E/N samples */
+    double    energy_sumsq;
+    long long samples;
+    long long bead_updates;
+    long long attempted[2];    /* com, staging */
+    long long accepted[2];
+} pgb_walker_stats;
+
+int pgb_walkers_create(const pgb_walkers_params* p, pgb_walkers** out);
+int pgb_walkers_destroy(pgb_walkers* w);
+/* Initialise worldlines on the device (uniform + N(0, 2 lambda tau) jitter,
+ * identity permutation) from the Philox streams. */
+int pgb_walkers_init(pgb_walkers* w);
+/* Upload one walker's positions (AoS FP64 [M][N][3]) */
+int pgb_walkers_set_positions(pgb_walkers* w, int walker, const double* pos);
+int pgb_walkers_get_positions(pgb_walkers* w, int walker, double* pos);
+/* Upload every walker's positions at once from one host buffer: walker w's
+ * AoS FP64 [M_w][N_w][3] block follows walker w-1's (total sum M_w N_w 3
+ * doubles).  Pinned host memory gives the full C2C copy bandwidth. */
+int pgb_walkers_set_all_positions(pgb_walkers* w, const double* pos);
+/* bytes of the host buffer pgb_walkers_set_all_positions reads */
+size_t pgb_walkers_state_bytes(pgb_walkers* w);
+/* Run `sweeps` MC steps for every walker (numUpdates moves per step,
+ * pimc.cpp:62-65, then one energy sample), asynchronously on the stream. */
+int pgb_walkers_run_async(pgb_walkers* w, int sweeps, int measure);
+int pgb_walkers_sync(pgb_walkers* w);
+int pgb_walkers_stats(pgb_walkers* w, pgb_walker_stats* per_walker);
+int pgb_walkers_reset_stats(pgb_walkers* w);
+/* launches of walker kernels issued so far */
+long long pgb_walkers_launch_count(pgb_walkers* w);
+/* threads per walker chosen by the autotuner (or set) */
+int pgb_walkers_threads(pgb_walkers* w);
+/* Energy per particle (thermodynamic estimator, primitive action) of each
+ * walker's current configuration, FP64 pair sums (plain form) or mixed. */
+int pgb_walkers_energy(pgb_walkers* w, int precision, double* en_per_walker);
+void* pgb_walkers_stream(pgb_walkers* w);
+const char* pgb_walkers_last_error(const pgb_walkers* w);
+
+/* ---- plain form: the reference move loop driven from the host with one
+ *      FP64 device action call per move (move.cpp:1124-1707 semantics,
+ *      MT19937 stream as include/MersenneTwister.h). --------------------- */
+typedef struct {
+    int    mbar;
+    int    diagonal_move;   /* 0 bisection, 1 staging */
+    int    var_updates;
+    int    max_wind;
+    double temperature;
+    double p_com;
+    int    num_updates;     /* <= 0: max(100, ceil(N M / Mbar)) */
+} pgb_move_params;
+
+typedef struct {
+    long long attempted[3]; /* com, staging, bisection */
+    long long accepted[3];
+    long long bead_updates;
+} pgb_move_stats;
+
+/* Seed the context's MT19937 stream (MTRand(seed), MersenneTwister.h:170-206) */
+int pgb_plain_seed(pgb_ctx* ctx, uint32_t seed);
+/* Run nsteps PathIntegralMonteCarlo::step() loops (pimc.cpp:724-741) of
+ * centre-of-mass + diagonal moves on the loaded closed path, continuing the
+ * context's MT19937 stream.  trace (optional) receives (move, accepted) int32
+ * pairs of attempted moves (0 com, 1 staging, 2 bisection); energies
+ * (optional) receives E/N of each step's EnergyEstimator sample. */
+int pgb_plain_run(pgb_ctx* ctx, const pgb_move_params* mp, int nsteps,
+                  int32_t* trace, int trace_cap, int* trace_len,
+                  double* energies, pgb_move_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

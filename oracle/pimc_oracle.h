@@ -1,0 +1,161 @@
+/*
+ * pimc_oracle.h -- C interface of the FP64 CPU oracle.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GB300 hot
+ * path: it restates, in plain C++ and FP64, the reference WA-PIMC CPU code
+ * for the pair action (Aziz table, LookupTable cutoff semantics, LocalAction),
+ * the path-wide estimators (thermodynamic / virial energy, S(q), F(q,tau)),
+ * the MT19937 generator and the diagonal moves (centre of mass, staging,
+ * bisection).  Only tests/, __graft_entry__.smoke() and the CPU-baseline legs
+ * of bench.py load it.  The product library (pimc_gb300) never links it.
+ *
+ * Parity status: the reference cannot be built in this image (it needs Boost
+ * and <mdspan>), and it ships no golden vectors, so this restatement is
+ * "parity unpinned": it is checked against the reference's own invariants
+ * (batched-vs-scalar potential check, checkMove full-vs-local action
+ * identity, pairwise-vs-rho_q structure factors) rather than against outputs
+ * of the reference binary.
+ *
+ * Conventions: beads are addressed as (slice, ptcl); positions are AoS FP64
+ * [M][Ne][3]; links are [M][Ne][2] int32 (slice, ptcl), -1 for "no link";
+ * worm locators are int32[8] = head, tail, special1, special2.
+ */
+#ifndef PIMC_ORACLE_H
+#define PIMC_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_sys orc_sys;
+
+typedef struct {
+    double side[3];        /* box sides (periodic prism) */
+    int    num_slices;     /* M */
+    int    num_ptcl_ext;   /* Ne, array extent */
+    double tau;            /* imaginary time step */
+    double lambda;         /* hbar^2/2m in K A^2 */
+    double rc;             /* interaction cutoff (reference default: box side) */
+    double vfactor[2];     /* even/odd potential factors */
+    double gradvfactor[2]; /* even/odd |grad V|^2 factors */
+    int    aziz_year;      /* 1979, 1987 or 1995 */
+    int    virial_window;  /* centroid virial window (reference default 5) */
+    double mu;             /* chemical potential (for E_mu columns) */
+} orc_params;
+
+/* ---- Aziz potential (src/potential.cpp:1741-1907) ---- */
+void   orc_aziz_values(int year, double r, double out3[3]);
+
+/* ---- system ---- */
+orc_sys* orc_create(const orc_params* p);
+void     orc_destroy(orc_sys* s);
+int      orc_table_length(orc_sys* s);
+double   orc_table_dr(orc_sys* s);
+double   orc_tailV(orc_sys* s);
+void     orc_copy_tables(orc_sys* s, double* V, double* dV, double* d2V);
+double   orc_V(orc_sys* s, const double sep[3]);
+void     orc_gradV(orc_sys* s, const double sep[3], double out[3]);
+double   orc_grad2V(orc_sys* s, const double sep[3]);
+void     orc_load_path(orc_sys* s, const double* pos, const int32_t* next,
+                       const int32_t* prev, const uint8_t* on,
+                       const int32_t* worm8);
+void     orc_get_positions(orc_sys* s, double* pos);
+void     orc_update_bead(orc_sys* s, int slice, int ptcl, const double pos[3]);
+void     orc_set_shift(orc_sys* s, int shift);
+
+/* ---- action (src/action.cpp) ---- */
+double orc_potential_action_bead(orc_sys* s, int slice, int ptcl);
+double orc_bare_potential_action(orc_sys* s, int slice, int ptcl);
+double orc_potential_action_correction(orc_sys* s, int slice, int ptcl);
+double orc_potential_action_range(orc_sys* s, int s0, int p0, int s1, int p1);
+double orc_potential_action_list(orc_sys* s, const int32_t* beads, int k);
+double orc_potential_action_full(orc_sys* s);
+double orc_kinetic_action_full(orc_sys* s);
+double orc_Vnn(orc_sys* s, int slice, int ptcl);
+double orc_gradVnnSquared(orc_sys* s, int slice, int ptcl);
+void   orc_V_slice(orc_sys* s, int slice, double out2[2]);
+double orc_gradVSquared_slice(orc_sys* s, int slice);
+double orc_gradVSquared_bead(orc_sys* s, int slice, int ptcl);
+double orc_deriv_tau(orc_sys* s, int slice);
+double orc_deriv_lambda(orc_sys* s, int slice);
+double orc_second_deriv_tau(orc_sys* s, int slice);
+double orc_rdotgradU1(orc_sys* s, int slice);
+double orc_rdotgradU2(orc_sys* s, int slice);
+double orc_deltadotgradU1(orc_sys* s, int slice);
+double orc_deltadotgradU2(orc_sys* s, int slice);
+double orc_virial_kin_corr(orc_sys* s, int slice);
+
+/* ---- estimators (src/estimator.cpp) ---- */
+/* one accumulate() of EnergyEstimator: K,V,V_ext,V_int,E,E_mu,K/N,V/N,E/N */
+void orc_energy(orc_sys* s, double out9[9]);
+/* one accumulate() of VirialEnergyEstimator (19 columns); cvcov2_quirk=1
+ * reproduces the reference's misspelt "cVCov2" key (adds into column 0). */
+void orc_virial(orc_sys* s, int cvcov2_quirk, double out19[19]);
+/* q-vector list (EstimatorBase::getQVectors); returns count, fills up to cap */
+int  orc_qvectors(const char* type, const char* input, const double side[3],
+                  double* q, int cap);
+/* S(q) pairwise CPU form, per-sample value already normalised by 1/(N M) */
+void orc_ssf_pairwise(orc_sys* s, const double* q, int nq, double* out);
+/* S(q) by rho_q in FP64 */
+void orc_ssf_rhoq(orc_sys* s, const double* q, int nq, double* out);
+/* F(q,tau): reference CPU form, tau in [0,M), layout [q][M] */
+void orc_isf_cpu_form(orc_sys* s, const double* q, int nq, double* out);
+/* F(q,tau): reference GPU form (raw q.(r_j - r_i) sum), tau in [0,M/2], layout [q][M/2+1] */
+void orc_isf_gpu_form(orc_sys* s, const double* q, int nq, double* out);
+/* F(q,tau) by rho_q in FP64, tau in [0,M/2], layout [q][M/2+1]; nthreads>=1 */
+void orc_isf_rhoq(orc_sys* s, const double* q, int nq, int nthreads, double* out);
+/* rho_q(t) FP64, layout [q][M][2] */
+void orc_rhoq(orc_sys* s, const double* q, int nq, double* out);
+
+/* ---- MT19937 (include/MersenneTwister.h) ---- */
+typedef struct orc_mt orc_mt;
+orc_mt*  orc_mt_create(uint32_t seed);
+void     orc_mt_destroy(orc_mt* m);
+uint32_t orc_mt_randint(orc_mt* m);
+uint32_t orc_mt_randint_n(orc_mt* m, uint32_t n);
+double   orc_mt_rand(orc_mt* m);
+double   orc_mt_randexc(orc_mt* m);
+double   orc_mt_randnorm(orc_mt* m, double mean, double sd);
+
+/* ---- diagonal moves + driver (src/move.cpp, src/pimc.cpp) ---- */
+typedef struct {
+    int    mbar;          /* update length Mbar (even) */
+    int    diagonal_move; /* 0 = bisection, 1 = staging */
+    int    var_updates;   /* reference default: 1 (see constants.cpp:96) */
+    int    max_wind;      /* winding sectors sampled by staging, default 1 */
+    double temperature;   /* for comDelta = 0.04 * lambda_dB */
+    double p_com;         /* probability of a centre-of-mass move */
+    int    num_updates;   /* moves per step; <=0 -> max(100, ceil(N M / Mbar)) */
+} orc_move_params;
+
+typedef struct {
+    long long attempted[3];   /* com, staging, bisection */
+    long long accepted[3];
+    long long bead_updates;   /* beads proposed and Metropolis-tested */
+} orc_move_stats;
+
+/* Run nsteps MC steps on the loaded path using MT19937(seed-state owned by
+ * mt).  If trace != NULL, each attempted move appends (move, accepted) pairs
+ * as int32 [2] up to trace_cap entries; returns number of trace entries.
+ * energies (may be NULL) receives E/N of each step's energy sample. */
+int orc_run_steps(orc_sys* s, orc_mt* mt, const orc_move_params* mp, int nsteps,
+                  int32_t* trace, int trace_cap, double* energies,
+                  orc_move_stats* stats);
+
+/* CPU baseline: run W independent canonical walkers (each its own system,
+ * MT19937 seed seeds[w]) for nsteps each, on nthreads threads.  Each walker
+ * w has N[w] particles, M[w] slices, temperature T[w], box side L[w];
+ * initial worldlines are generated by the oracle's lattice-free generator
+ * from the same seed.  Returns wall seconds; fills per-walker mean E/N and
+ * bead-update counts. */
+double orc_walkers_cpu(int W, const int* N, const int* M, const double* T,
+                       const double* L, const uint32_t* seeds, double tau,
+                       double lambda, int nsteps, int nthreads,
+                       double* mean_en, long long* bead_updates);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

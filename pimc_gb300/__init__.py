@@ -1,0 +1,310 @@
+"""pimc_gb300 -- GB300-native WA-PIMC hot path (pair action + path-wide estimators).
+
+Python mirror of the reference plugin surface for this path, over the C ABI
+of libpimc_gb300.so (include/pimc_gb300.h):
+
+  * ``Action``   -- AzizPotential + LocalAction + the estimator-facing
+                    ActionBase virtuals (include/action.h:30-145) for one path
+  * ``qvectors`` -- EstimatorBase::getQVectors (estimator.cpp:439-570)
+  * ``Walkers``  -- many independent canonical chains in one persistent kernel
+
+Every call runs on the GPU; a missing library or device raises.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import (PGB_FP64, PGB_MIXED, PGB_ACTION_FULL, PGB_ACTION_BARE, PGB_ACTION_CORR,
+                   PgbError, dptr, iptr, u8ptr)
+from . import worldlines
+
+__all__ = ["Action", "Walkers", "qvectors", "device_info", "PGB_FP64", "PGB_MIXED",
+           "PGB_ACTION_FULL", "PGB_ACTION_BARE", "PGB_ACTION_CORR", "PgbError", "worldlines",
+           "action_factors"]
+
+
+def action_factors(kind):
+    """VFactor, gradVFactor, period of Setup::action (src/setup.cpp:1230-1253)."""
+    if kind == "gsf":
+        return (2.0 / 3.0, 4.0 / 3.0), (0.0, 2.0 / 9.0), 2
+    if kind == "li_broughton":
+        return (1.0, 1.0), (1.0 / 12.0, 1.0 / 12.0), 2
+    return (1.0, 1.0), (0.0, 0.0), 1
+
+
+def device_info():
+    lib = _lib.load()
+    name = C.create_string_buffer(256)
+    sm, cc = C.c_int(), C.c_int()
+    _lib.check(lib.pgb_device_info(name, 256, C.byref(sm), C.byref(cc)))
+    return dict(name=name.value.decode(), sm_count=sm.value, cc=cc.value)
+
+
+def qvectors(kind, text, side):
+    lib = _lib.load()
+    side = np.ascontiguousarray(np.broadcast_to(np.asarray(side, dtype=np.float64), (3,)))
+    n = C.c_int()
+    _lib.check(lib.pgb_qvectors(kind.encode(), text.encode(), dptr(side), None, 0, C.byref(n)))
+    q = np.zeros((max(n.value, 1), 3))
+    _lib.check(lib.pgb_qvectors(kind.encode(), text.encode(), dptr(side), dptr(q), n.value,
+                                C.byref(n)))
+    return q[:n.value]
+
+
+class Action:
+    """One path on the device with its Aziz tables and LocalAction factors."""
+
+    def __init__(self, side, num_slices, num_ptcl_ext, tau, lam, rc=None, action="primitive",
+                 precision=PGB_FP64, aziz_year=1979, virial_window=5, mu=0.0):
+        self.lib = _lib.load()
+        side = np.broadcast_to(np.asarray(side, dtype=np.float64), (3,))
+        vf, gf, period = action_factors(action)
+        p = _lib.PgbParams()
+        for i in range(3):
+            p.side[i] = side[i]
+        p.num_slices, p.num_ptcl_ext = int(num_slices), int(num_ptcl_ext)
+        p.tau, p.lambda_ = float(tau), float(lam)
+        p.rc = float(side[2] if rc is None else rc)
+        p.vfactor[0], p.vfactor[1] = vf
+        p.gradvfactor[0], p.gradvfactor[1] = gf
+        p.period, p.aziz_year, p.virial_window = period, aziz_year, virial_window
+        p.precision, p.mu = precision, mu
+        self.params = p
+        self.M, self.Ne = int(num_slices), int(num_ptcl_ext)
+        h = C.c_void_p()
+        rc_ = self.lib.pgb_create(C.byref(p), C.byref(h))
+        if rc_ != 0:
+            raise PgbError(rc_, (self.lib.pgb_last_error(None) or b"").decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        return _lib.check(rc, self.h)
+
+    # ---- potential ----
+    def table_info(self):
+        n, dr, tail = C.c_int(), C.c_double(), C.c_double()
+        self._chk(self.lib.pgb_table_info(self.h, C.byref(n), C.byref(dr), C.byref(tail)))
+        return n.value, dr.value, tail.value
+
+    def tables(self):
+        n, _, _ = self.table_info()
+        V, dV, d2V = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._chk(self.lib.pgb_copy_tables(self.h, dptr(V), dptr(dV), dptr(d2V)))
+        return V, dV, d2V
+
+    def V_batch(self, sep):
+        sep = np.ascontiguousarray(sep, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(sep))
+        self._chk(self.lib.pgb_potential_batch(self.h, dptr(sep), dptr(out), len(sep)))
+        return out
+
+    def gradV_batch(self, sep):
+        sep = np.ascontiguousarray(sep, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((len(sep), 3))
+        self._chk(self.lib.pgb_gradv_batch(self.h, dptr(sep), dptr(out), len(sep)))
+        return out
+
+    def grad2V_batch(self, sep):
+        sep = np.ascontiguousarray(sep, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(sep))
+        self._chk(self.lib.pgb_grad2v_batch(self.h, dptr(sep), dptr(out), len(sep)))
+        return out
+
+    # ---- worldlines ----
+    def load(self, cfg):
+        pos = np.ascontiguousarray(cfg["pos"], dtype=np.float64)
+        nxt = np.ascontiguousarray(cfg["next"], dtype=np.int32)
+        prv = np.ascontiguousarray(cfg["prev"], dtype=np.int32)
+        on = np.ascontiguousarray(cfg["on"], dtype=np.uint8)
+        worm = np.ascontiguousarray(cfg.get("worm", np.full(8, -1)), dtype=np.int32)
+        self._chk(self.lib.pgb_load_path(self.h, dptr(pos), iptr(nxt), iptr(prv), u8ptr(on),
+                                         iptr(worm)))
+
+    def update_beads(self, beads, pos):
+        beads = np.ascontiguousarray(beads, dtype=np.int32).reshape(-1, 2)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        self._chk(self.lib.pgb_update_beads(self.h, iptr(beads), dptr(pos), len(beads)))
+
+    def positions(self):
+        out = np.zeros((self.M, self.Ne, 3))
+        self._chk(self.lib.pgb_get_positions(self.h, dptr(out)))
+        return out
+
+    # ---- action ----
+    def bead_actions(self, beads, shift=1, mode=PGB_ACTION_FULL):
+        beads = np.ascontiguousarray(beads, dtype=np.int32).reshape(-1, 2)
+        per = np.zeros(len(beads))
+        tot = C.c_double()
+        self._chk(self.lib.pgb_bead_actions(self.h, iptr(beads), len(beads), shift, mode,
+                                            dptr(per), C.byref(tot)))
+        return per, tot.value
+
+    def range_action(self, start, end, shift=1):
+        out = C.c_double()
+        self._chk(self.lib.pgb_range_action(self.h, start[0], start[1], end[0], end[1], shift,
+                                            C.byref(out)))
+        return out.value
+
+    def full_action(self):
+        out = C.c_double()
+        self._chk(self.lib.pgb_full_action(self.h, C.byref(out)))
+        return out.value
+
+    def kinetic_action(self):
+        out = C.c_double()
+        self._chk(self.lib.pgb_kinetic_action(self.h, C.byref(out)))
+        return out.value
+
+    def slice_terms(self, tmatrix=True):
+        arrs = {k: np.zeros(self.M) for k in ("vint", "g2", "r1", "r2", "d1", "d2", "kin", "xch")}
+        st = _lib.PgbSliceTerms()
+        for k, a in arrs.items():
+            if tmatrix or k not in ("r2", "d2"):
+                setattr(st, k, dptr(a))
+        self._chk(self.lib.pgb_slice_terms_compute(self.h, C.byref(st)))
+        return arrs
+
+    # ---- estimators ----
+    def energy(self):
+        out = np.zeros(9)
+        self._chk(self.lib.pgb_energy(self.h, dptr(out)))
+        return out
+
+    def virial(self, cvcov2_quirk=True):
+        out = np.zeros(19)
+        self._chk(self.lib.pgb_virial(self.h, 1 if cvcov2_quirk else 0, dptr(out)))
+        return out
+
+    def ssf(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(q))
+        self._chk(self.lib.pgb_ssf(self.h, dptr(q), len(q), dptr(out)))
+        return out
+
+    def isf(self, q, mode=0):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((len(q), self.M // 2 + 1))
+        self._chk(self.lib.pgb_isf(self.h, dptr(q), len(q), mode, dptr(out)))
+        return out
+
+    def rhoq(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((len(q), self.M, 2))
+        self._chk(self.lib.pgb_rhoq(self.h, dptr(q), len(q), dptr(out)))
+        return out
+
+    # ---- plain form (host-driven moves, FP64 device actions) ----
+    def plain_seed(self, seed):
+        self._chk(self.lib.pgb_plain_seed(self.h, seed))
+
+    def plain_run(self, nsteps, mbar, temperature, diagonal_move=1, var_updates=1, max_wind=1,
+                  p_com=0.05, num_updates=0, trace_cap=0):
+        mp = _lib.PgbMoveParams(mbar, diagonal_move, var_updates, max_wind, temperature, p_com,
+                                num_updates)
+        trace = np.zeros((max(trace_cap, 1), 2), dtype=np.int32)
+        ntr = C.c_int()
+        en = np.zeros(max(nsteps, 1))
+        st = _lib.PgbMoveStats()
+        self._chk(self.lib.pgb_plain_run(self.h, C.byref(mp), nsteps, iptr(trace), trace_cap,
+                                         C.byref(ntr), dptr(en), C.byref(st)))
+        return dict(trace=trace[:ntr.value], energies=en[:nsteps],
+                    attempted=list(st.attempted), accepted=list(st.accepted),
+                    bead_updates=st.bead_updates)
+
+
+class Walkers:
+    """Independent canonical walkers advanced together on the device."""
+
+    def __init__(self, n, m, temperature, side, mbar, tau, lam, seed=0, p_com=0.05,
+                 threads_per_walker=0, var_updates=1, aziz_year=1979):
+        self.lib = _lib.load()
+        self.n = np.ascontiguousarray(n, dtype=np.int32)
+        self.m = np.ascontiguousarray(m, dtype=np.int32)
+        self.t = np.ascontiguousarray(temperature, dtype=np.float64)
+        self.side = np.ascontiguousarray(side, dtype=np.float64)
+        self.mbar = np.ascontiguousarray(mbar, dtype=np.int32)
+        p = _lib.PgbWalkersParams()
+        p.num_walkers = len(self.n)
+        p.num_ptcl = self.n.ctypes.data_as(C.POINTER(C.c_int))
+        p.num_slices = self.m.ctypes.data_as(C.POINTER(C.c_int))
+        p.temperature = dptr(self.t)
+        p.side = dptr(self.side)
+        p.mbar = self.mbar.ctypes.data_as(C.POINTER(C.c_int))
+        p.tau, p.lambda_, p.p_com, p.seed = tau, lam, p_com, seed
+        p.aziz_year, p.threads_per_walker, p.var_updates = aziz_year, threads_per_walker, var_updates
+        h = C.c_void_p()
+        rc = self.lib.pgb_walkers_create(C.byref(p), C.byref(h))
+        if rc != 0:
+            raise PgbError(rc, (self.lib.pgb_walkers_last_error(None) or b"").decode())
+        self.h = h
+        self.W = len(self.n)
+
+    def _chk(self, rc):
+        return _lib.check(rc, self.h, walkers=True)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pgb_walkers_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self):
+        self._chk(self.lib.pgb_walkers_init(self.h))
+
+    def set_positions(self, w, pos):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        self._chk(self.lib.pgb_walkers_set_positions(self.h, w, dptr(pos)))
+
+    def positions(self, w):
+        out = np.zeros((int(self.m[w]), int(self.n[w]), 3))
+        self._chk(self.lib.pgb_walkers_get_positions(self.h, w, dptr(out)))
+        return out
+
+    def run(self, sweeps, measure=1, sync=True):
+        self._chk(self.lib.pgb_walkers_run_async(self.h, sweeps, measure))
+        if sync:
+            self._chk(self.lib.pgb_walkers_sync(self.h))
+
+    def sync(self):
+        self._chk(self.lib.pgb_walkers_sync(self.h))
+
+    def stats(self):
+        st = (_lib.PgbWalkerStats * self.W)()
+        self._chk(self.lib.pgb_walkers_stats(self.h, st))
+        return [dict(energy_sum=s.energy_sum, energy_sumsq=s.energy_sumsq, samples=s.samples,
+                     bead_updates=s.bead_updates, attempted=list(s.attempted),
+                     accepted=list(s.accepted)) for s in st]
+
+    def reset_stats(self):
+        self._chk(self.lib.pgb_walkers_reset_stats(self.h))
+
+    def energy(self, precision=PGB_MIXED):
+        out = np.zeros(self.W)
+        self._chk(self.lib.pgb_walkers_energy(self.h, precision, dptr(out)))
+        return out
+
+    def launch_count(self):
+        return self.lib.pgb_walkers_launch_count(self.h)
+
+    def threads(self):
+        return self.lib.pgb_walkers_threads(self.h)
+
+    def stream(self):
+        return self.lib.pgb_walkers_stream(self.h)

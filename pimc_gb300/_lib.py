@@ -1,0 +1,162 @@
+"""ctypes binding of libpimc_gb300.so (the C ABI declared in include/pimc_gb300.h).
+
+The shared library is built in-tree by pimc_gb300/build.py.  Loading fails
+loudly when it is missing: there is no CPU fallback for any entry point.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpimc_gb300.so")
+
+PGB_OK, PGB_EINVAL, PGB_ECUDA, PGB_ENOMEM, PGB_ESTATE, PGB_ETIMEOUT = 0, -1, -2, -3, -4, -5
+PGB_FP64, PGB_MIXED = 0, 1
+PGB_ACTION_FULL, PGB_ACTION_BARE, PGB_ACTION_CORR = 0, 1, 2
+
+
+class PgbParams(C.Structure):
+    _fields_ = [("side", C.c_double * 3), ("num_slices", C.c_int), ("num_ptcl_ext", C.c_int),
+                ("tau", C.c_double), ("lambda_", C.c_double), ("rc", C.c_double),
+                ("vfactor", C.c_double * 2), ("gradvfactor", C.c_double * 2),
+                ("period", C.c_int), ("aziz_year", C.c_int), ("virial_window", C.c_int),
+                ("precision", C.c_int), ("mu", C.c_double)]
+
+
+class PgbSliceTerms(C.Structure):
+    _fields_ = [(n, C.POINTER(C.c_double)) for n in
+                ("vint", "g2", "r1", "r2", "d1", "d2", "kin", "xch")]
+
+
+class PgbWalkersParams(C.Structure):
+    _fields_ = [("num_walkers", C.c_int), ("num_ptcl", C.POINTER(C.c_int)),
+                ("num_slices", C.POINTER(C.c_int)), ("temperature", C.POINTER(C.c_double)),
+                ("side", C.POINTER(C.c_double)), ("mbar", C.POINTER(C.c_int)),
+                ("tau", C.c_double), ("lambda_", C.c_double), ("p_com", C.c_double),
+                ("seed", C.c_uint64), ("aziz_year", C.c_int),
+                ("threads_per_walker", C.c_int), ("var_updates", C.c_int)]
+
+
+class PgbWalkerStats(C.Structure):
+    _fields_ = [("energy_sum", C.c_double), ("energy_sumsq", C.c_double),
+                ("samples", C.c_longlong), ("bead_updates", C.c_longlong),
+                ("attempted", C.c_longlong * 2), ("accepted", C.c_longlong * 2)]
+
+
+class PgbMoveParams(C.Structure):
+    _fields_ = [("mbar", C.c_int), ("diagonal_move", C.c_int), ("var_updates", C.c_int),
+                ("max_wind", C.c_int), ("temperature", C.c_double), ("p_com", C.c_double),
+                ("num_updates", C.c_int)]
+
+
+class PgbMoveStats(C.Structure):
+    _fields_ = [("attempted", C.c_longlong * 3), ("accepted", C.c_longlong * 3),
+                ("bead_updates", C.c_longlong)]
+
+
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int32)
+_U8 = C.POINTER(C.c_uint8)
+_VP = C.c_void_p
+
+_SIGS = {
+    "pgb_create": (C.c_int, [C.POINTER(PgbParams), C.POINTER(_VP)]),
+    "pgb_destroy": (C.c_int, [_VP]),
+    "pgb_last_error": (C.c_char_p, [_VP]),
+    "pgb_device_info": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "pgb_table_info": (C.c_int, [_VP, C.POINTER(C.c_int), _DP, _DP]),
+    "pgb_copy_tables": (C.c_int, [_VP, _DP, _DP, _DP]),
+    "pgb_potential_batch": (C.c_int, [_VP, _DP, _DP, C.c_int]),
+    "pgb_gradv_batch": (C.c_int, [_VP, _DP, _DP, C.c_int]),
+    "pgb_grad2v_batch": (C.c_int, [_VP, _DP, _DP, C.c_int]),
+    "pgb_load_path": (C.c_int, [_VP, _DP, _IP, _IP, _U8, _IP]),
+    "pgb_update_beads": (C.c_int, [_VP, _IP, _DP, C.c_int]),
+    "pgb_get_positions": (C.c_int, [_VP, _DP]),
+    "pgb_bead_actions": (C.c_int, [_VP, _IP, C.c_int, C.c_int, C.c_int, _DP, _DP]),
+    "pgb_range_action": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
+    "pgb_full_action": (C.c_int, [_VP, _DP]),
+    "pgb_kinetic_action": (C.c_int, [_VP, _DP]),
+    "pgb_slice_terms_compute": (C.c_int, [_VP, C.POINTER(PgbSliceTerms)]),
+    "pgb_energy": (C.c_int, [_VP, _DP]),
+    "pgb_virial": (C.c_int, [_VP, C.c_int, _DP]),
+    "pgb_qvectors": (C.c_int, [C.c_char_p, C.c_char_p, _DP, _DP, C.c_int, C.POINTER(C.c_int)]),
+    "pgb_ssf": (C.c_int, [_VP, _DP, C.c_int, _DP]),
+    "pgb_isf": (C.c_int, [_VP, _DP, C.c_int, C.c_int, _DP]),
+    "pgb_rhoq": (C.c_int, [_VP, _DP, C.c_int, _DP]),
+    "pgb_isf_device_async": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP]),
+    "pgb_load_positions_device_async": (C.c_int, [_VP, _VP]),
+    "pgb_stream": (_VP, [_VP]),
+    "pgb_walkers_create": (C.c_int, [C.POINTER(PgbWalkersParams), C.POINTER(_VP)]),
+    "pgb_walkers_destroy": (C.c_int, [_VP]),
+    "pgb_walkers_init": (C.c_int, [_VP]),
+    "pgb_walkers_set_positions": (C.c_int, [_VP, C.c_int, _DP]),
+    "pgb_walkers_get_positions": (C.c_int, [_VP, C.c_int, _DP]),
+    "pgb_walkers_set_all_positions": (C.c_int, [_VP, _DP]),
+    "pgb_walkers_state_bytes": (C.c_size_t, [_VP]),
+    "pgb_walkers_run_async": (C.c_int, [_VP, C.c_int, C.c_int]),
+    "pgb_walkers_sync": (C.c_int, [_VP]),
+    "pgb_walkers_stats": (C.c_int, [_VP, C.POINTER(PgbWalkerStats)]),
+    "pgb_walkers_reset_stats": (C.c_int, [_VP]),
+    "pgb_walkers_launch_count": (C.c_longlong, [_VP]),
+    "pgb_walkers_threads": (C.c_int, [_VP]),
+    "pgb_walkers_energy": (C.c_int, [_VP, C.c_int, _DP]),
+    "pgb_walkers_stream": (_VP, [_VP]),
+    "pgb_walkers_last_error": (C.c_char_p, [_VP]),
+    "pgb_plain_seed": (C.c_int, [_VP, C.c_uint32]),
+    "pgb_plain_run": (C.c_int, [_VP, C.POINTER(PgbMoveParams), C.c_int, _IP, C.c_int,
+                                C.POINTER(C.c_int), _DP, C.POINTER(PgbMoveStats)]),
+}
+
+_lib = None
+
+
+def exported_symbols():
+    """Names of every entry point the C ABI header declares."""
+    return sorted(_SIGS)
+
+
+def load():
+    """Load the in-tree library (raises OSError if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OSError("libpimc_gb300.so not found at %s: run "
+                      "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class PgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("pgb error %d: %s" % (code, msg))
+        self.code = code
+
+
+def dptr(a):
+    return a.ctypes.data_as(_DP)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_IP)
+
+
+def u8ptr(a):
+    return a.ctypes.data_as(_U8)
+
+
+def check(rc, handle=None, walkers=False):
+    if rc != PGB_OK:
+        lib = load()
+        if walkers:
+            msg = lib.pgb_walkers_last_error(handle)
+        else:
+            msg = lib.pgb_last_error(handle)
+        raise PgbError(rc, (msg or b"").decode())
+    return rc

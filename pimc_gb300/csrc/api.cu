@@ -1,0 +1,763 @@
+// api.cu -- host side of the C ABI: context, tables, worldline mirror,
+// actions and estimator assembly.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "pgb_device.cuh"
+
+namespace pgb {
+
+AzizParams aziz_params(int year) {
+    // src/potential.cpp:1749-1788
+    if (year == 1987)
+        return {2.9673, 1.8443101E5, 10.948, 10.43329537, -2.27965105, 1.4826,
+                1.36745214, 0.42123807, 0.17473318};
+    if (year == 1995)
+        return {2.9683, 1.86924404E5, 10.956, 10.5717543, -2.07758779, 1.438,
+                1.35186623, 0.4149514, 0.17151143};
+    return {2.9673, 0.5448504E6, 10.8, 13.353384, 0.0, 1.241314, 1.3732412, 0.4253785, 0.1781};
+}
+
+PathView Ctx::view() const {
+    PathView v;
+    v.M = M; v.Ne = Ne;
+    for (int i = 0; i < 3; ++i) { v.side[i] = p.side[i]; v.sideInv[i] = 1.0 / p.side[i]; }
+    v.rc2 = p.rc * p.rc;
+    v.pos = d_pos; v.pos32 = d_pos32; v.next = d_next; v.prev = d_prev; v.on = d_on;
+    v.nbs = d_nbs;
+    for (int i = 0; i < 8; ++i) v.worm[i] = worm[i];
+    v.tV = d_tV; v.tdV = d_tdV; v.td2V = d_td2V; v.dr = dr; v.tableLength = tableLength;
+    return v;
+}
+
+int Ctx::cuda_fail(cudaError_t e, const char* where) {
+    err = std::string("CUDA error ") + cudaGetErrorString(e) + " at " + where;
+    return e == cudaErrorMemoryAllocation ? PGB_ENOMEM : PGB_ECUDA;
+}
+
+int Ctx::ensure_scratch(size_t bytes) {
+    if (bytes <= scratch_bytes) return PGB_OK;
+    if (d_scratch) cudaFree(d_scratch);
+    d_scratch = nullptr; scratch_bytes = 0;
+    size_t b = std::max(bytes, (size_t)1 << 20);
+    cudaError_t e = cudaMalloc(&d_scratch, b);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
+    scratch_bytes = b;
+    return PGB_OK;
+}
+
+int Ctx::ensure_pinned(size_t bytes) {
+    if (bytes <= pinned_bytes) return PGB_OK;
+    if (h_pinned) cudaFreeHost(h_pinned);
+    h_pinned = nullptr; pinned_bytes = 0;
+    size_t b = std::max(bytes, (size_t)1 << 20);
+    cudaError_t e = cudaMallocHost(&h_pinned, b);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost(staging)");
+    pinned_bytes = b;
+    return PGB_OK;
+}
+
+// scatter (bead, position) updates into the SoA FP64 array and FP32 mirror
+__global__ void k_update_beads(double* pos, float4* pos32, int Ne, const int2* beads,
+                               const double* p, int k) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    int2 b = beads[i];
+    double* X = pos + (size_t)b.x * 3 * Ne;
+    X[b.y] = p[3*i]; X[Ne + b.y] = p[3*i+1]; X[2 * Ne + b.y] = p[3*i+2];
+    pos32[(size_t)b.x * Ne + b.y] = make_float4((float)p[3*i], (float)p[3*i+1], (float)p[3*i+2], 0.f);
+}
+
+}  // namespace pgb
+
+using namespace pgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int check_ctx(pgb_ctx* c) { return c ? PGB_OK : PGB_EINVAL; }
+
+int need_path(Ctx& c) {
+    if (!c.loaded) return c.fail(PGB_ESTATE, "no path loaded (call pgb_load_path first)");
+    return PGB_OK;
+}
+
+// per-slice terms, internal layout [9][M]: vint g2 r1 r2 d1 d2 kin xch kinprev
+int compute_terms(Ctx& c, std::vector<double>& h, bool want_tmat) {
+    int rc = need_path(c); if (rc) return rc;
+    size_t bytes = (size_t)8 * c.M * sizeof(double);
+    rc = c.ensure_scratch(bytes); if (rc) return rc;
+    double* d = static_cast<double*>(c.d_scratch);
+    PathView v = c.view();
+    int window = c.p.virial_window > 0 ? c.p.virial_window : 5;
+    cudaError_t e = (c.p.precision == PGB_MIXED)
+        ? launch_slice_terms32(v, c.az, window, d, c.stream)
+        : launch_slice_terms64(v, window, want_tmat ? 1 : 0, d, c.stream);
+    if (e != cudaSuccess) return c.cuda_fail(e, "slice terms launch");
+    h.assign((size_t)8 * c.M, 0.0);
+    PGB_CUDA(&c, cudaMemcpyAsync(h.data(), d, bytes, cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    return PGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pgb_last_error(const pgb_ctx* ctx) {
+    if (ctx) return ctx->c.err.c_str();
+    return g_last_error.c_str();
+}
+
+int pgb_device_info(char* name, int cap, int* sm_count, int* cc) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        g_last_error = "no CUDA device available";
+        return PGB_ECUDA;
+    }
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, 0);
+    if (e != cudaSuccess) { g_last_error = cudaGetErrorString(e); return PGB_ECUDA; }
+    if (name && cap > 0) { std::strncpy(name, prop.name, cap - 1); name[cap - 1] = 0; }
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    if (cc) *cc = prop.major * 10 + prop.minor;
+    return PGB_OK;
+}
+
+int pgb_create(const pgb_params* p, pgb_ctx** out) {
+    if (!p || !out) { g_last_error = "null argument"; return PGB_EINVAL; }
+    *out = nullptr;
+    if (p->num_slices <= 0 || p->num_ptcl_ext <= 0 || p->tau <= 0 || p->lambda <= 0 ||
+        p->rc <= 0 || p->side[0] <= 0 || p->side[1] <= 0 || p->side[2] <= 0) {
+        g_last_error = "invalid parameters (sizes, tau, lambda, rc and sides must be > 0)";
+        return PGB_EINVAL;
+    }
+    if (p->precision != PGB_FP64 && p->precision != PGB_MIXED) {
+        g_last_error = "precision must be PGB_FP64 or PGB_MIXED"; return PGB_EINVAL;
+    }
+    if (p->num_ptcl_ext > 8192) { g_last_error = "num_ptcl_ext > 8192 not supported"; return PGB_EINVAL; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        g_last_error = "no CUDA device available"; return PGB_ECUDA;
+    }
+    pgb_ctx* h = new pgb_ctx();
+    Ctx& c = h->c;
+    c.p = *p;
+    c.M = p->num_slices; c.Ne = p->num_ptcl_ext;
+    c.az = aziz_params(p->aziz_year);
+    cudaError_t e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { g_last_error = cudaGetErrorString(e); delete h; return PGB_ECUDA; }
+    // table sizes (potential.cpp:1793-1796, container.cpp:100-103)
+    double hx = p->side[0] / 2.0, hy = p->side[1] / 2.0, hz = p->side[2] / 2.0;
+    double d2 = 0.0; d2 += hx * hx; d2 += hy * hy; d2 += hz * hz;
+    c.maxSep = std::sqrt(d2);
+    c.dr = (1.0E-6) * c.az.rm;
+    c.tableLength = int(c.maxSep / c.dr);
+    // tail correction (potential.cpp:1801-1806)
+    double rmorc = c.az.rm / p->rc;
+    double t2 = c.az.C6 * std::pow(rmorc, 3.0) / 3.0;
+    double t3 = c.az.C8 * std::pow(rmorc, 5.0) / 5.0;
+    double t4 = c.az.C10 * std::pow(rmorc, 7.0) / 7.0;
+    c.tailV = 2.0 * M_PI * c.az.epsilon * (-c.az.rm * c.az.rm * c.az.rm * (t2 + t3 + t4));
+    int rc = PGB_OK;
+    size_t tb = (size_t)c.tableLength * sizeof(double);
+    size_t nb = (size_t)c.M * c.Ne;
+    do {
+        if ((e = cudaMalloc(&c.d_tV, tb)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&c.d_tdV, tb)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&c.d_td2V, tb)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&c.d_pos, nb * 3 * sizeof(double))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&c.d_pos32, nb * sizeof(float4))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&c.d_next, nb * sizeof(int2))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&c.d_prev, nb * sizeof(int2))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&c.d_on, nb)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&c.d_nbs, c.M * sizeof(int))) != cudaSuccess) break;
+    } while (0);
+    if (e != cudaSuccess) { rc = c.cuda_fail(e, "cudaMalloc(context)"); g_last_error = c.err; pgb_destroy(h); return rc; }
+    // The table abscissae accumulate r += dr sequentially (potential.h:176-183);
+    // that sequence is formed here and the V, dV/dr, d2V/dr2 values are
+    // evaluated on the device.
+    rc = c.ensure_pinned(tb);
+    if (rc) { g_last_error = c.err; pgb_destroy(h); return rc; }
+    double* r = static_cast<double*>(c.h_pinned);
+    double acc = 0.0;
+    for (int n = 0; n < c.tableLength; ++n) { r[n] = acc; acc += c.dr; }
+    rc = c.ensure_scratch(tb);
+    if (rc) { g_last_error = c.err; pgb_destroy(h); return rc; }
+    e = cudaMemcpyAsync(c.d_scratch, r, tb, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess)
+        e = launch_build_tables(static_cast<double*>(c.d_scratch), c.tableLength, c.az,
+                                c.d_tV, c.d_tdV, c.d_td2V, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) { rc = c.cuda_fail(e, "table build"); g_last_error = c.err; pgb_destroy(h); return rc; }
+    c.h_nbs.assign(c.M, 0);
+    *out = h;
+    return PGB_OK;
+}
+
+int pgb_destroy(pgb_ctx* h) {
+    if (!h) return PGB_OK;
+    Ctx& c = h->c;
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    cudaFree(c.d_tV); cudaFree(c.d_tdV); cudaFree(c.d_td2V);
+    cudaFree(c.d_pos); cudaFree(c.d_pos32); cudaFree(c.d_next); cudaFree(c.d_prev);
+    cudaFree(c.d_on); cudaFree(c.d_nbs);
+    if (c.d_scratch) cudaFree(c.d_scratch);
+    if (c.h_pinned) cudaFreeHost(c.h_pinned);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete h;
+    return PGB_OK;
+}
+
+void* pgb_stream(pgb_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
+
+int pgb_table_info(pgb_ctx* h, int* length, double* dr, double* tailV) {
+    if (check_ctx(h)) return PGB_EINVAL;
+    if (length) *length = h->c.tableLength;
+    if (dr) *dr = h->c.dr;
+    if (tailV) *tailV = h->c.tailV;
+    return PGB_OK;
+}
+
+int pgb_copy_tables(pgb_ctx* h, double* V, double* dV, double* d2V) {
+    if (check_ctx(h)) return PGB_EINVAL;
+    Ctx& c = h->c;
+    size_t tb = (size_t)c.tableLength * sizeof(double);
+    if (V) PGB_CUDA(&c, cudaMemcpyAsync(V, c.d_tV, tb, cudaMemcpyDeviceToHost, c.stream));
+    if (dV) PGB_CUDA(&c, cudaMemcpyAsync(dV, c.d_tdV, tb, cudaMemcpyDeviceToHost, c.stream));
+    if (d2V) PGB_CUDA(&c, cudaMemcpyAsync(d2V, c.d_td2V, tb, cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    return PGB_OK;
+}
+
+static int potential_batch(pgb_ctx* h, const double* sep, double* out, int n, int what) {
+    if (check_ctx(h) || (n > 0 && (!sep || !out)) || n < 0) {
+        if (h) h->c.err = "potential batch: bad arguments (count must be non-negative)";
+        return PGB_EINVAL;
+    }
+    if (n == 0) return PGB_OK;
+    Ctx& c = h->c;
+    int outw = (what == 1) ? 3 : 1;
+    size_t in_b = (size_t)n * 3 * sizeof(double), out_b = (size_t)n * outw * sizeof(double);
+    int rc = c.ensure_scratch(in_b + out_b); if (rc) return rc;
+    double* d_in = static_cast<double*>(c.d_scratch);
+    double* d_out = d_in + (size_t)n * 3;
+    PGB_CUDA(&c, cudaMemcpyAsync(d_in, sep, in_b, cudaMemcpyHostToDevice, c.stream));
+    PGB_CUDA(&c, launch_potential_batch64(c.view(), d_in, d_out, n, what, c.stream));
+    PGB_CUDA(&c, cudaMemcpyAsync(out, d_out, out_b, cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    return PGB_OK;
+}
+
+int pgb_potential_batch(pgb_ctx* h, const double* sep, double* out, int n) { return potential_batch(h, sep, out, n, 0); }
+int pgb_gradv_batch(pgb_ctx* h, const double* sep, double* out3, int n) { return potential_batch(h, sep, out3, n, 1); }
+int pgb_grad2v_batch(pgb_ctx* h, const double* sep, double* out, int n) { return potential_batch(h, sep, out, n, 2); }
+
+int pgb_load_path(pgb_ctx* h, const double* pos, const int32_t* next, const int32_t* prev,
+                  const uint8_t* on, const int32_t* worm8) {
+    if (check_ctx(h) || !pos || !next || !prev || !on) {
+        if (h) h->c.err = "load_path: null array";
+        return PGB_EINVAL;
+    }
+    Ctx& c = h->c;
+    size_t nb = (size_t)c.M * c.Ne;
+    for (size_t i = 0; i < nb * 2; i += 2) {
+        int s = next[i], p = next[i + 1];
+        if (!((s == kXXX && p == kXXX) || (s >= 0 && s < c.M && p >= 0 && p < c.Ne)))
+            return c.fail(PGB_EINVAL, "load_path: next link out of range");
+        s = prev[i]; p = prev[i + 1];
+        if (!((s == kXXX && p == kXXX) || (s >= 0 && s < c.M && p >= 0 && p < c.Ne)))
+            return c.fail(PGB_EINVAL, "load_path: prev link out of range");
+    }
+    int rc = c.ensure_pinned(nb * 3 * sizeof(double)); if (rc) return rc;
+    double* soa = static_cast<double*>(c.h_pinned);
+    for (int s = 0; s < c.M; ++s)
+        for (int p = 0; p < c.Ne; ++p)
+            for (int d = 0; d < 3; ++d)
+                soa[((size_t)s * 3 + d) * c.Ne + p] = pos[((size_t)s * c.Ne + p) * 3 + d];
+    PGB_CUDA(&c, cudaMemcpyAsync(c.d_pos, soa, nb * 3 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    c.h_next.assign(next, next + nb * 2);
+    c.h_prev.assign(prev, prev + nb * 2);
+    c.h_on.assign(on, on + nb);
+    PGB_CUDA(&c, cudaMemcpyAsync(c.d_next, c.h_next.data(), nb * sizeof(int2), cudaMemcpyHostToDevice, c.stream));
+    PGB_CUDA(&c, cudaMemcpyAsync(c.d_prev, c.h_prev.data(), nb * sizeof(int2), cudaMemcpyHostToDevice, c.stream));
+    PGB_CUDA(&c, cudaMemcpyAsync(c.d_on, c.h_on.data(), nb, cudaMemcpyHostToDevice, c.stream));
+    c.numBeadsOn = 0;
+    for (int s = 0; s < c.M; ++s) {
+        int cnt = 0;
+        for (int p = 0; p < c.Ne; ++p) cnt += c.h_on[(size_t)s * c.Ne + p] ? 1 : 0;
+        c.h_nbs[s] = cnt;
+        c.numBeadsOn += cnt;
+    }
+    PGB_CUDA(&c, cudaMemcpyAsync(c.d_nbs, c.h_nbs.data(), c.M * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    for (int i = 0; i < 8; ++i) c.worm[i] = worm8 ? worm8[i] : kXXX;
+    PGB_CUDA(&c, launch_pos32_from64(c.view(), c.d_pos32, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    c.loaded = true;
+    return PGB_OK;
+}
+
+int pgb_load_positions_device_async(pgb_ctx* h, const double* d_pos) {
+    if (check_ctx(h) || !d_pos) return PGB_EINVAL;
+    Ctx& c = h->c;
+    size_t nb = (size_t)c.M * c.Ne;
+    PGB_CUDA(&c, cudaMemcpyAsync(c.d_pos, d_pos, nb * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    PGB_CUDA(&c, launch_pos32_from64(c.view(), c.d_pos32, c.stream));
+    return PGB_OK;
+}
+
+int pgb_update_beads(pgb_ctx* h, const int32_t* beads, const double* pos, int k) {
+    if (check_ctx(h) || k < 0 || (k > 0 && (!beads || !pos))) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    if (k == 0) return PGB_OK;
+    for (int i = 0; i < k; ++i)
+        if (beads[2*i] < 0 || beads[2*i] >= c.M || beads[2*i+1] < 0 || beads[2*i+1] >= c.Ne)
+            return c.fail(PGB_EINVAL, "update_beads: bead out of range");
+    size_t bb = (size_t)k * sizeof(int2), pb = (size_t)k * 3 * sizeof(double);
+    rc = c.ensure_scratch(bb + pb + 64); if (rc) return rc;
+    rc = c.ensure_pinned(bb + pb + 64); if (rc) return rc;
+    char* hp = static_cast<char*>(c.h_pinned);
+    std::memcpy(hp, beads, bb);
+    std::memcpy(hp + bb, pos, pb);
+    char* dp = static_cast<char*>(c.d_scratch);
+    PGB_CUDA(&c, cudaMemcpyAsync(dp, hp, bb + pb, cudaMemcpyHostToDevice, c.stream));
+    k_update_beads<<<(k + 127) / 128, 128, 0, c.stream>>>(c.d_pos, c.d_pos32, c.Ne,
+        reinterpret_cast<const int2*>(dp), reinterpret_cast<const double*>(dp + bb), k);
+    PGB_CUDA(&c, cudaGetLastError());
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    return PGB_OK;
+}
+
+int pgb_get_positions(pgb_ctx* h, double* pos) {
+    if (check_ctx(h) || !pos) return PGB_EINVAL;
+    Ctx& c = h->c;
+    size_t nb = (size_t)c.M * c.Ne;
+    int rc = c.ensure_pinned(nb * 3 * sizeof(double)); if (rc) return rc;
+    double* soa = static_cast<double*>(c.h_pinned);
+    PGB_CUDA(&c, cudaMemcpyAsync(soa, c.d_pos, nb * 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    for (int s = 0; s < c.M; ++s)
+        for (int p = 0; p < c.Ne; ++p)
+            for (int d = 0; d < 3; ++d)
+                pos[((size_t)s * c.Ne + p) * 3 + d] = soa[((size_t)s * 3 + d) * c.Ne + p];
+    return PGB_OK;
+}
+
+int pgb_bead_actions(pgb_ctx* h, const int32_t* beads, int k, int shift, int mode,
+                     double* out_per_bead, double* out_sum) {
+    if (check_ctx(h)) return PGB_EINVAL;
+    Ctx& c = h->c;
+    if (k < 0 || (k > 0 && !beads) || shift < 1 || mode < 0 || mode > 2)
+        return c.fail(PGB_EINVAL, "bead_actions: bad arguments");
+    int rc = need_path(c); if (rc) return rc;
+    if (k == 0) { if (out_sum) *out_sum = 0.0; return PGB_OK; }
+    for (int i = 0; i < k; ++i)
+        if (beads[2*i] < 0 || beads[2*i] >= c.M || beads[2*i+1] < 0 || beads[2*i+1] >= c.Ne)
+            return c.fail(PGB_EINVAL, "bead_actions: bead out of range");
+    size_t bb = (size_t)k * sizeof(int2), ob = (size_t)k * sizeof(double);
+    rc = c.ensure_scratch(bb + ob + 64); if (rc) return rc;
+    rc = c.ensure_pinned(bb + ob + 64); if (rc) return rc;
+    char* hp = static_cast<char*>(c.h_pinned);
+    std::memcpy(hp, beads, bb);
+    char* dp = static_cast<char*>(c.d_scratch);
+    int2* d_b = reinterpret_cast<int2*>(dp);
+    double* d_o = reinterpret_cast<double*>(dp + ((bb + 15) & ~(size_t)15));
+    PGB_CUDA(&c, cudaMemcpyAsync(dp, hp, bb, cudaMemcpyHostToDevice, c.stream));
+    PathView v = c.view();
+    cudaError_t e = (c.p.precision == PGB_MIXED)
+        ? launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda,
+                                c.p.vfactor, c.p.gradvfactor, d_o, c.stream)
+        : launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda,
+                                c.p.vfactor, c.p.gradvfactor, d_o, c.stream);
+    if (e != cudaSuccess) return c.cuda_fail(e, "bead actions launch");
+    double* ho = reinterpret_cast<double*>(hp + ((bb + 15) & ~(size_t)15));
+    PGB_CUDA(&c, cudaMemcpyAsync(ho, d_o, ob, cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    double tot = 0.0;
+    for (int i = 0; i < k; ++i) tot += ho[i];
+    if (out_per_bead) std::memcpy(out_per_bead, ho, ob);
+    if (out_sum) *out_sum = tot;
+    return PGB_OK;
+}
+
+int pgb_range_action(pgb_ctx* h, int s0, int p0, int s1, int p1, int shift, double* out) {
+    if (check_ctx(h) || !out) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    if (s0 < 0 || s0 >= c.M || p0 < 0 || p0 >= c.Ne || s1 < 0 || s1 >= c.M || p1 < 0 || p1 >= c.Ne)
+        return c.fail(PGB_EINVAL, "range_action: bead out of range");
+    // walk next links from start to end inclusive (action.cpp:532-541)
+    size_t ie = ((size_t)s1 * c.Ne + p1) * 2;
+    int stop_s = c.h_next[ie], stop_p = c.h_next[ie + 1];
+    std::vector<int32_t> list;
+    int s = s0, p = p0;
+    long long guard = 0, lim = (long long)c.M * c.Ne + 1;
+    do {
+        if (s < 0 || p < 0) return c.fail(PGB_EINVAL, "range_action: broken link inside range");
+        if (c.h_on[(size_t)s * c.Ne + p]) { list.push_back(s); list.push_back(p); }
+        size_t i = ((size_t)s * c.Ne + p) * 2;
+        s = c.h_next[i]; p = c.h_next[i + 1];
+        if (++guard > lim) return c.fail(PGB_EINVAL, "range_action: end bead not reachable");
+    } while (!(s == stop_s && p == stop_p));
+    return pgb_bead_actions(h, list.data(), (int)list.size() / 2, shift, PGB_ACTION_FULL, nullptr, out);
+}
+
+int pgb_full_action(pgb_ctx* h, double* out) {
+    if (check_ctx(h) || !out) return PGB_EINVAL;
+    Ctx& c = h->c;
+    std::vector<double> t;
+    int rc = compute_terms(c, t, false); if (rc) return rc;
+    double totU = 0.0, tt = c.p.tau;
+    for (int s = 0; s < c.M; ++s) {
+        int eo = s % 2;
+        totU += c.p.vfactor[eo] * tt * (0.0 + 0.0 + t[s]);
+        if (c.p.gradvfactor[eo] > kEPS)
+            totU += c.p.gradvfactor[eo] * tt * tt * tt * c.p.lambda * t[(size_t)c.M + s];
+    }
+    *out = totU;
+    return PGB_OK;
+}
+
+int pgb_kinetic_action(pgb_ctx* h, double* out) {
+    if (check_ctx(h) || !out) return PGB_EINVAL;
+    Ctx& c = h->c;
+    std::vector<double> t;
+    int rc = compute_terms(c, t, false); if (rc) return rc;
+    // each link is counted from both of its beads (action.cpp:306-323)
+    double totK = 0.0;
+    for (int s = 0; s < c.M; ++s) totK += 2.0 * t[(size_t)6 * c.M + s];
+    *out = totK / (4.0 * c.p.lambda * c.p.tau);
+    return PGB_OK;
+}
+
+int pgb_slice_terms_compute(pgb_ctx* h, pgb_slice_terms* o) {
+    if (check_ctx(h) || !o) return PGB_EINVAL;
+    Ctx& c = h->c;
+    std::vector<double> t;
+    bool tm = (o->r2 || o->d2);
+    int rc = compute_terms(c, t, tm); if (rc) return rc;
+    double* dst[8] = {o->vint, o->g2, o->r1, o->r2, o->d1, o->d2, o->kin, o->xch};
+    for (int q = 0; q < 8; ++q)
+        if (dst[q]) std::memcpy(dst[q], t.data() + (size_t)q * c.M, c.M * sizeof(double));
+    return PGB_OK;
+}
+
+// EnergyEstimator::accumulate (estimator.cpp:940-1029) from per-slice sums.
+int pgb_energy(pgb_ctx* h, double out[9]) {
+    if (check_ctx(h) || !out) return PGB_EINVAL;
+    Ctx& c = h->c;
+    std::vector<double> t;
+    int rc = compute_terms(c, t, false); if (rc) return rc;
+    const int M = c.M;
+    const double tau = c.p.tau, lambda = c.p.lambda;
+    const double* vint = t.data();
+    const double* g2 = t.data() + M;
+    const double* kin = t.data() + 6 * (size_t)M;
+    int numParticles = c.numBeadsOn / M;
+    double volume = c.p.side[0] * c.p.side[1] * c.p.side[2];
+    double tailV = (1.0 * numParticles * numParticles / volume) * c.tailV;
+    double kinNorm = (0.25 / (lambda * tau)) / (tau * M);
+    double classicalKinetic = (0.5 * 3 / tau) * numParticles;
+    double totK = 0.0;
+    for (int s = 0; s < M; ++s) totK -= kin[s];
+    totK *= kinNorm;
+    double t1 = 0.0, t2 = 0.0, vop0 = 0.0, vop1 = 0.0;
+    int period = c.p.period > 0 ? c.p.period : 1;
+    for (int s = 0; s < M; ++s) {
+        int eo = s % 2;
+        double dl = (c.p.gradvfactor[eo] > kEPS) ? c.p.gradvfactor[eo] * tau * tau * tau * g2[s] : 0.0;
+        double dt = c.p.vfactor[eo] * (0.0 + 0.0 + vint[s]);
+        if (c.p.gradvfactor[eo] > kEPS) dt += 3.0 * c.p.gradvfactor[eo] * tau * tau * lambda * g2[s];
+        t1 += 1.0 * dl;
+        t2 += 1.0 * dt;
+        if (!(s % period)) { vop0 += 1.0 * 0.0; vop1 += 1.0 * vint[s]; }
+    }
+    t1 *= lambda / (tau * M);
+    t2 /= 1.0 * M;
+    int nper = M / period;
+    vop0 /= nper; vop1 /= nper;
+    totK += (classicalKinetic + t1);
+    double totV = t2 - t1 + tailV;
+    vop1 += tailV;
+    out[0] = totK; out[1] = totV; out[2] = vop0; out[3] = vop1;
+    out[4] = totK + totV; out[5] = totK + totV - c.p.mu * numParticles;
+    if (numParticles > 0) {
+        out[6] = totK / (1.0 * numParticles); out[7] = totV / (1.0 * numParticles);
+        out[8] = (totK + totV) / (1.0 * numParticles);
+    } else out[6] = out[7] = out[8] = 0.0;
+    return PGB_OK;
+}
+
+// VirialEnergyEstimator::accumulate (estimator.cpp:1086-1252)
+int pgb_virial(pgb_ctx* h, int quirk, double est[19]) {
+    if (check_ctx(h) || !est) return PGB_EINVAL;
+    Ctx& c = h->c;
+    std::vector<double> t;
+    int rc = compute_terms(c, t, true); if (rc) return rc;
+    const int M = c.M;
+    const double* vint = t.data();
+    const double* g2 = t.data() + M;
+    const double* r1 = t.data() + 2 * (size_t)M;
+    const double* r2 = t.data() + 3 * (size_t)M;
+    const double* d1 = t.data() + 4 * (size_t)M;
+    const double* d2 = t.data() + 5 * (size_t)M;
+    const double* kin = t.data() + 6 * (size_t)M;
+    const double* xch = t.data() + 7 * (size_t)M;
+    const double tau = c.p.tau, lambda = c.p.lambda;
+    const double* VF = c.p.vfactor;
+    const double* gF = c.p.gradvfactor;
+    for (int i = 0; i < 19; ++i) est[i] = 0.0;
+    int numParticles = c.numBeadsOn / M;
+    double beta = 1.0 * M * tau;
+    int W = c.p.virial_window > 0 ? c.p.virial_window : 5;
+    double volume = c.p.side[0] * c.p.side[1] * c.p.side[2];
+    double tailV = (1.0 * numParticles * numParticles / volume) * c.tailV;
+    double thermTerm1 = (0.5 * 3 / tau) * numParticles;
+    double T1 = 0.5 * 3 * numParticles / (1.0 * W * tau);
+    double exchangeNorm = 1.0 / (4.0 * W * std::pow(tau, 2) * lambda * M);
+    double Pressure = 3 * numParticles;
+    double T2 = 0.0, thermE = 0.0;
+    for (int s = 0; s < M; ++s) { T2 -= xch[s]; thermE -= kin[s]; }
+    double P2 = thermE;
+    T2 *= exchangeNorm;
+    P2 /= (2.0 * lambda * tau * M);
+    Pressure += P2;
+    double T3 = 0.0, T4 = 0.0, T5 = 0.0, virKinTerm = 0.0, totVop = 0.0, P3 = 0.0;
+    for (int s = 0; s < M; ++s) {
+        int eo = s % 2;
+        bool cor = gF[eo] > kEPS;
+        double t3 = std::pow(tau, 3);
+        T3 += VF[eo] * tau * d1[s];
+        T4 += cor ? d2[s] * (2.0 * gF[eo] * t3 * lambda) : 0.0;
+        double dt = VF[eo] * (0.0 + 0.0 + vint[s]);
+        if (cor) dt += 3.0 * gF[eo] * tau * tau * lambda * g2[s];
+        T5 += dt;
+        virKinTerm += cor ? (0.0 + g2[s]) * (gF[eo] * t3 * lambda) : 0.0;
+        if (eo == 0) totVop += (0.0 + 0.0 + vint[s]);
+        P3 += VF[eo] * tau * r1[s] + (cor ? r2[s] * (2.0 * gF[eo] * t3 * lambda) : 0.0);
+    }
+    P3 *= (1.0 / (2.0 * M));
+    Pressure -= P3;
+    Pressure /= (3 * tau * volume);
+    totVop /= (0.5 * M);
+    totVop += tailV;
+    T3 /= (2.0 * beta);
+    T4 /= (1.0 * beta);
+    T5 /= (1.0 * M);
+    virKinTerm /= (0.5 * beta);
+    thermE *= (0.25 / (lambda * tau)) / (tau * M);
+    thermE += thermTerm1;
+    thermE += T5;
+    thermE += tailV;
+    double totEcv = T1 + T2 + T3 + T4 + T5 + tailV;
+    double Kcv = T1 + T2 + T3 + T4 + virKinTerm;
+    double dEdB = (-1.0 * T1 - 2.0 * T2 + 2.0 * T4) / tau;
+    for (int s = 0; s < M; s++) {
+        int eo = s % 2;
+        double d2U = 0.0;
+        if (gF[eo] > kEPS) d2U += 6.0 * gF[eo] * tau * lambda * g2[s];
+        dEdB += d2U / (1.0 * M);
+    }
+    dEdB *= beta * beta / (1.0 * M);
+    est[0] += totEcv - totVop;
+    est[1] += Kcv;
+    est[2] += totVop;
+    est[3] += totEcv - Kcv;
+    est[4] += totEcv;
+    est[5] += totEcv - c.p.mu * numParticles;
+    if (numParticles > 0) {
+        est[6] += (totEcv - totVop) / (1.0 * numParticles);
+        est[7] += Kcv / (1.0 * numParticles);
+        est[8] += totVop / (1.0 * numParticles);
+        est[9] += (totEcv - Kcv) / (1.0 * numParticles);
+        est[10] += totEcv / (1.0 * numParticles);
+    }
+    est[11] += totEcv * thermE * beta * beta;
+    est[12] += totEcv * beta;
+    est[13] += dEdB;
+    est[14] += totEcv * thermE * beta * beta * totEcv * beta;
+    // estimator.cpp:1244 writes estIndex["cVCov2"]; the map has no such key, so
+    // operator[] inserts index 0 and the term is added into K_op.
+    est[quirk ? 0 : 15] += totEcv * beta * dEdB;
+    est[16] += totEcv * thermE * beta * beta * dEdB;
+    est[17] += thermE;
+    est[18] += Pressure;
+    return PGB_OK;
+}
+
+// EstimatorBase::getQVectors (estimator.cpp:439-570)
+int pgb_qvectors(const char* type, const char* input, const double side[3], double* qout,
+                 int cap, int* count) {
+    if (!type || !input || !side || !count) { g_last_error = "qvectors: null argument"; return PGB_EINVAL; }
+    std::string inputType(type), in(input);
+    std::vector<std::array<double,3>> qv;
+    std::istringstream iss(in);
+    std::vector<std::string> tok;
+    std::string w;
+    while (iss >> w) tok.push_back(w);
+    auto norm = [](const std::array<double,3>& q) { double r = 0.0; for (int i = 0; i < 3; ++i) r += q[i]*q[i]; return std::sqrt(r); };
+    try {
+        if (inputType == "int" || inputType == "float") {
+            if (tok.empty() || tok.size() % 3) { g_last_error = "qvectors: need a multiple of 3 components"; return PGB_EINVAL; }
+            for (size_t i = 0; i + 2 < tok.size(); i += 3) {
+                std::array<double,3> q;
+                for (int j = 0; j < 3; ++j)
+                    q[j] = (inputType == "int") ? (2.0 * M_PI / side[j]) * std::stoi(tok[i + j])
+                                                : (double)std::stof(tok[i + j]);
+                qv.push_back(q);
+            }
+        } else if (inputType == "max_int" || inputType == "max_float") {
+            if (tok.size() < 3) { g_last_error = "qvectors: need 3 components"; return PGB_EINVAL; }
+            int qmi[3], qi[3];
+            std::array<double,3> qmax{}, q{};
+            for (int i = 0; i < 3; ++i) {
+                if (inputType == "max_int") { qmi[i] = std::abs(std::stoi(tok[i])); qmax[i] = qmi[i] * 2.0 * M_PI / side[i]; }
+                else qmax[i] = std::stof(tok[i]);
+            }
+            double qmm = norm(qmax);
+            if (inputType == "max_float")
+                for (int i = 0; i < 3; ++i) qmi[i] = 1 + static_cast<int>(qmm * side[i] / 2.0 / M_PI);
+            int n_q = 1;
+            for (int i = 0; i < 3; ++i) { n_q *= 2 * qmi[i] + 1; qi[i] = -qmi[i]; q[i] = qi[i] * 2.0 * M_PI / side[i]; }
+            if (norm(q) <= qmm) qv.push_back(q);
+            int pos = 2, cnt = 0;
+            while (cnt < n_q - 1) {
+                if (qi[pos] == qmi[pos]) { qi[pos] = -qmi[pos]; pos -= 1; }
+                else {
+                    qi[pos] += 1;
+                    for (int i = 0; i < 3; ++i) q[i] = qi[i] * 2.0 * M_PI / side[i];
+                    if (norm(q) <= qmm) qv.push_back(q);
+                    cnt += 1; pos = 2;
+                }
+            }
+        } else if (inputType == "file_int" || inputType == "file_float") {
+            FILE* f = std::fopen(in.c_str(), "r");
+            if (!f) { g_last_error = "qvectors: cannot open " + in; return PGB_EINVAL; }
+            char line[4096];
+            while (std::fgets(line, sizeof line, f)) {
+                std::istringstream ls(line);
+                std::array<double,3> q;
+                if (inputType == "file_int") {
+                    int a[3];
+                    if (!(ls >> a[0] >> a[1] >> a[2])) continue;
+                    for (int i = 0; i < 3; ++i) q[i] = (2.0 * M_PI / side[i]) * a[i];
+                } else {
+                    float a[3];
+                    if (!(ls >> a[0] >> a[1] >> a[2])) continue;
+                    for (int i = 0; i < 3; ++i) q[i] = a[i];
+                }
+                qv.push_back(q);
+            }
+            std::fclose(f);
+        } else {
+            g_last_error = "qvectors: unknown wavevector type " + inputType; return PGB_EINVAL;
+        }
+    } catch (...) {
+        g_last_error = "qvectors: cannot parse input"; return PGB_EINVAL;
+    }
+    *count = (int)qv.size();
+    if (qout)
+        for (int i = 0; i < (int)qv.size() && i < cap; ++i)
+            for (int j = 0; j < 3; ++j) qout[3 * i + j] = qv[i][j];
+    return PGB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Structure factors
+// ---------------------------------------------------------------------------
+namespace {
+
+int scatter_common(Ctx& c, const double* d_q, int nq, int what, int mode, double* d_out,
+                   void* d_work) {
+    // what: 0 ssf, 1 isf, 2 rho (FP64 values)
+    PathView v = c.view();
+    int N = c.numBeadsOn / c.M;
+    if (N <= 0) return c.fail(PGB_ESTATE, "structure factor needs at least one particle");
+    double norm = 1.0 / (1.0 * N * c.M);
+    cudaError_t e;
+    if (c.p.precision == PGB_FP64 || what == 2) {
+        double* d_rho = static_cast<double*>(d_work);
+        e = launch_rhoq64(v, d_q, nq, d_rho, c.stream);
+        if (e == cudaSuccess) {
+            if (what == 0) e = launch_ssf_from_rho64(d_rho, nq, c.M, norm, d_out, c.stream);
+            else if (what == 1) e = launch_isf_direct64(d_rho, nq, c.M, norm, d_out, c.stream);
+            else e = cudaMemcpyAsync(d_out, d_rho, (size_t)nq * c.M * 2 * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, c.stream);
+        }
+    } else {
+        float2* d_rho = static_cast<float2*>(d_work);
+        e = launch_rhoq32(v, d_q, nq, d_rho, c.stream);
+        if (e == cudaSuccess) {
+            if (what == 0) e = launch_ssf_from_rho32(d_rho, nq, c.M, norm, d_out, c.stream);
+            else if (mode == 1) {
+                if (!isf_tc_supported(c.M))
+                    return c.fail(PGB_EINVAL, "tensor-core F(q,tau) needs M a multiple of 128 and <= 1024");
+                void* tc = static_cast<char*>(d_work) + (((size_t)nq * c.M * sizeof(float2) + 255) & ~(size_t)255);
+                e = launch_isf_tc(d_rho, nq, c.M, norm, d_out, tc, c.stream);
+            } else e = launch_isf_direct32(d_rho, nq, c.M, norm, d_out, c.stream);
+        }
+    }
+    if (e != cudaSuccess) return c.cuda_fail(e, "structure factor launch");
+    return PGB_OK;
+}
+
+size_t scatter_work_bytes(const Ctx& c, int nq, int what, int mode) {
+    size_t rho = (size_t)nq * c.M * 2 * sizeof(double);
+    size_t extra = (c.p.precision == PGB_MIXED && what == 1 && mode == 1)
+                       ? isf_tc_scratch_bytes(nq, c.M) : 0;
+    return ((rho + 255) & ~(size_t)255) + extra;
+}
+
+int scatter_host(pgb_ctx* h, const double* q, int nq, int what, int mode, double* out) {
+    if (!h || !q || !out || nq < 0) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    if (nq == 0) return PGB_OK;
+    if (mode != 0 && mode != 1) return c.fail(PGB_EINVAL, "isf mode must be 0 or 1");
+    size_t nout = (what == 0) ? (size_t)nq : (what == 1) ? (size_t)nq * (c.M / 2 + 1)
+                                                         : (size_t)nq * c.M * 2;
+    size_t qb = (size_t)nq * 3 * sizeof(double);
+    size_t ob = nout * sizeof(double);
+    size_t wb = scatter_work_bytes(c, nq, what, mode);
+    size_t off_o = (qb + 255) & ~(size_t)255;
+    size_t off_w = (off_o + ob + 255) & ~(size_t)255;
+    rc = c.ensure_scratch(off_w + wb); if (rc) return rc;
+    char* base = static_cast<char*>(c.d_scratch);
+    PGB_CUDA(&c, cudaMemcpyAsync(base, q, qb, cudaMemcpyHostToDevice, c.stream));
+    rc = scatter_common(c, reinterpret_cast<double*>(base), nq, what, mode,
+                        reinterpret_cast<double*>(base + off_o), base + off_w);
+    if (rc) return rc;
+    PGB_CUDA(&c, cudaMemcpyAsync(out, base + off_o, ob, cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    return PGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pgb_ssf(pgb_ctx* h, const double* q, int nq, double* out) { return scatter_host(h, q, nq, 0, 0, out); }
+int pgb_isf(pgb_ctx* h, const double* q, int nq, int mode, double* out) { return scatter_host(h, q, nq, 1, mode, out); }
+int pgb_rhoq(pgb_ctx* h, const double* q, int nq, double* out) { return scatter_host(h, q, nq, 2, 0, out); }
+
+int pgb_isf_device_async(pgb_ctx* h, const double* d_q, int nq, int mode, double* d_out) {
+    if (!h || !d_q || !d_out || nq <= 0) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    if (mode != 0 && mode != 1) return c.fail(PGB_EINVAL, "isf mode must be 0 or 1");
+    rc = c.ensure_scratch(scatter_work_bytes(c, nq, 1, mode)); if (rc) return rc;
+    return scatter_common(c, d_q, nq, 1, mode, d_out, c.d_scratch);
+}
+
+}  // extern "C"

@@ -1,0 +1,149 @@
+// scatter.cu -- rho_q(t) in FP32 and the CUDA-core S(q) / F(q,tau) kernels.
+//
+// S(q) and F(q,tau) of the reference (estimator.cpp:3705-3737, 3923-3961 and
+// gpu_ssf/gpu_isf, estimator_gpu.cu:67-165, 288-380) are pair sums over beads;
+// both equal correlations of the collective density
+//     rho_q(t) = sum_j exp(i q . r_j(t)):
+//     S(q)     = 1/(N M) sum_t |rho_q(t)|^2
+//     F(q,tau) = 1/(N M) sum_t Re[rho_q(t) conj(rho_q(t+tau))]
+// which turns O(Q M N^2) (S) and O(Q M^2 N^2) (F) into O(Q M N) + O(Q M^2).
+#include "pgb_device.cuh"
+
+namespace pgb {
+
+// One CTA = one slice t x 256 q-vectors; each thread owns one q and streams
+// the slice's beads from shared memory (broadcast reads).  The phase is
+// reduced in turns, per dimension, with an exact FMA remainder:
+//     q . r / 2pi = sum_d n_d u_d,   n_d = q_d L_d / 2pi,  u_d = r_d / L_d,
+//     frac_d = fma(n_d, u_d, -rint(n_d u_d))
+// so that __sincosf always sees |angle| <= pi.
+constexpr int kRhoBlock = 256;
+
+__global__ void __launch_bounds__(kRhoBlock)
+k_rhoq32(PathView v, const double* __restrict__ q, int nq, float2* __restrict__ rho) {
+    extern __shared__ float4 su[];
+    const int t = blockIdx.y;
+    const int n = v.nbs[t];
+    const double* X = v.pos + (size_t)t * 3 * v.Ne;
+    for (int j = threadIdx.x; j < n; j += blockDim.x)
+        su[j] = make_float4((float)(X[j] * v.sideInv[0]), (float)(X[v.Ne + j] * v.sideInv[1]),
+                            (float)(X[2 * v.Ne + j] * v.sideInv[2]), 0.f);
+    __syncthreads();
+    const int iq = blockIdx.x * kRhoBlock + threadIdx.x;
+    if (iq >= nq) return;
+    const double inv2pi = 0.15915494309189533577;
+    const float nx = (float)(q[3*iq] * v.side[0] * inv2pi);
+    const float ny = (float)(q[3*iq+1] * v.side[1] * inv2pi);
+    const float nz = (float)(q[3*iq+2] * v.side[2] * inv2pi);
+    double re = 0.0, im = 0.0;
+    int j = 0;
+    while (j < n) {
+        float cr = 0.f, ci = 0.f;
+        int jend = min(n, j + 32);
+        for (; j < jend; ++j) {
+            float4 u = su[j];
+            float fx = fmaf(nx, u.x, -rintf(nx * u.x));
+            float fy = fmaf(ny, u.y, -rintf(ny * u.y));
+            float fz = fmaf(nz, u.z, -rintf(nz * u.z));
+            float f = fx + fy + fz;
+            f -= rintf(f);
+            float sn, cs;
+            __sincosf(6.28318530717958647692f * f, &sn, &cs);
+            cr += cs; ci += sn;
+        }
+        re += cr; im += ci;
+    }
+    rho[(size_t)iq * v.M + t] = make_float2((float)re, (float)im);
+}
+
+cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* d_rho,
+                          cudaStream_t s) {
+    if (nq <= 0) return cudaSuccess;
+    dim3 grid((nq + kRhoBlock - 1) / kRhoBlock, v.M);
+    size_t smem = (size_t)v.Ne * sizeof(float4);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_rhoq32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    k_rhoq32<<<grid, kRhoBlock, smem, s>>>(v, d_q, nq, d_rho);
+    return cudaGetLastError();
+}
+
+__global__ void k_ssf_from_rho32(const float2* __restrict__ rho, int nq, int M, double norm,
+                                 double* __restrict__ out) {
+    __shared__ double red[8];
+    int iq = blockIdx.x;
+    double acc = 0.0;
+    for (int t = threadIdx.x; t < M; t += blockDim.x) {
+        float2 r = rho[(size_t)iq * M + t];
+        acc += (double)r.x * r.x + (double)r.y * r.y;
+    }
+    double s = block_sum(acc, red);
+    if (threadIdx.x == 0) out[iq] = s * norm;
+}
+
+cudaError_t launch_ssf_from_rho32(const float2* d_rho, int nq, int M, double norm,
+                                  double* d_out, cudaStream_t s) {
+    if (nq <= 0) return cudaSuccess;
+    k_ssf_from_rho32<<<nq, 256, 0, s>>>(d_rho, nq, M, norm, d_out);
+    return cudaGetLastError();
+}
+
+// CUDA-core circular correlation: one CTA per q, rho_q staged in shared
+// memory, each thread owns kTauPerThread consecutive tau and slides a
+// register window along t (one new shared load per kTauPerThread FMAs pairs).
+constexpr int kTauPerThread = 8;
+
+__global__ void k_isf_direct32(const float2* __restrict__ rho, int nq, int M, double norm,
+                               double* __restrict__ out) {
+    extern __shared__ float2 sr[];
+    const int iq = blockIdx.x;
+    const int nt = M / 2 + 1;
+    for (int t = threadIdx.x; t < M; t += blockDim.x) sr[t] = rho[(size_t)iq * M + t];
+    __syncthreads();
+    for (int tau0 = threadIdx.x * kTauPerThread; tau0 < nt; tau0 += blockDim.x * kTauPerThread) {
+        double acc[kTauPerThread];
+        float win_r[kTauPerThread], win_i[kTauPerThread];
+        #pragma unroll
+        for (int k = 0; k < kTauPerThread; ++k) {
+            acc[k] = 0.0;
+            int t2 = (tau0 + k) % M;
+            win_r[k] = sr[t2].x; win_i[k] = sr[t2].y;
+        }
+        int t = 0;
+        while (t < M) {
+            float c[kTauPerThread];
+            #pragma unroll
+            for (int k = 0; k < kTauPerThread; ++k) c[k] = 0.f;
+            int tend = min(M, t + 64);
+            for (; t < tend; ++t) {
+                float2 a = sr[t];
+                #pragma unroll
+                for (int k = 0; k < kTauPerThread; ++k) c[k] = fmaf(a.x, win_r[k], fmaf(a.y, win_i[k], c[k]));
+                #pragma unroll
+                for (int k = 0; k < kTauPerThread - 1; ++k) { win_r[k] = win_r[k+1]; win_i[k] = win_i[k+1]; }
+                int tn = (t + 1 + tau0 + kTauPerThread - 1) % M;
+                win_r[kTauPerThread - 1] = sr[tn].x; win_i[kTauPerThread - 1] = sr[tn].y;
+            }
+            #pragma unroll
+            for (int k = 0; k < kTauPerThread; ++k) acc[k] += c[k];
+        }
+        #pragma unroll
+        for (int k = 0; k < kTauPerThread; ++k)
+            if (tau0 + k < nt) out[(size_t)iq * nt + tau0 + k] = acc[k] * norm;
+    }
+}
+
+cudaError_t launch_isf_direct32(const float2* d_rho, int nq, int M, double norm, double* d_out,
+                                cudaStream_t s) {
+    if (nq <= 0) return cudaSuccess;
+    int nt = M / 2 + 1;
+    int threads = (nt + kTauPerThread - 1) / kTauPerThread;
+    threads = ((threads + 31) / 32) * 32;
+    if (threads > 256) threads = 256;
+    k_isf_direct32<<<nq, threads, (size_t)M * sizeof(float2), s>>>(d_rho, nq, M, norm, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace pgb
