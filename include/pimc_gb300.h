@@ -154,6 +154,24 @@ int pgb_isf_device_async(pgb_ctx* ctx, const double* d_q, int nq, int mode,
 int pgb_load_positions_device_async(pgb_ctx* ctx, const double* d_pos);
 void* pgb_stream(pgb_ctx* ctx);   /* the context's cudaStream_t */
 
+/* F(q,tau) that allocates nothing, for callers that cannot call cudaMalloc
+ * when they measure (their device memory is reserved up front by a pool they
+ * do not own, or they may only launch work once set-up is over).  No
+ * counterpart in the reference.  The caller passes device buffers: d_beads,
+ * AoS FP64 [num_slices][ptcl_extent][3] of which the first num_ptcl beads per
+ * slice are used; d_qvecs [nq][3]; d_isf [nq][num_slices/2+1], the same values
+ * as pgb_isf mode 0 on a PGB_MIXED context.  The densities rho_q(t) go to a
+ * static 16 MiB device array held by every GPU that loads the library, so
+ * nq * num_slices must not exceed 2^21 (PGB_EINVAL otherwise).  Work is
+ * queued on `stream` (a cudaStream_t, NULL for the default stream) and the
+ * call returns without waiting.  The first call on a device looks up the
+ * array's device address with that device current; make that first call
+ * before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race, so order them.  Errors are reported by pgb_last_error(NULL). */
+int pgb_isf_static(const double* d_beads, int num_slices, int num_ptcl,
+                   int ptcl_extent, const double side[3], const double* d_qvecs,
+                   int nq, double* d_isf, void* stream);
+
 /* ---- batched walkers: many independent canonical chains in one
  *      persistent kernel (no reference counterpart; replaces running many
  *      pimc.e processes with offset seeds, setup.cpp:921-923). ---------- */

@@ -87,6 +87,7 @@ _SIGS = {
     "pgb_isf_device_async": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP]),
     "pgb_load_positions_device_async": (C.c_int, [_VP, _VP]),
     "pgb_stream": (_VP, [_VP]),
+    "pgb_isf_static": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, _DP, _VP, C.c_int, _VP, _VP]),
     "pgb_walkers_create": (C.c_int, [C.POINTER(PgbWalkersParams), C.POINTER(_VP)]),
     "pgb_walkers_destroy": (C.c_int, [_VP]),
     "pgb_walkers_init": (C.c_int, [_VP]),

@@ -23,7 +23,7 @@ PER_FILE = {
     "fp64_kernels.cu": ["-fmad=false"],
 }
 SOURCES = ["api.cu", "fp64_kernels.cu", "mixed_kernels.cu", "scatter.cu",
-           "isf_tc.cu", "walkers.cu", "plain_moves.cu"]
+           "isf_tc.cu", "walkers.cu", "plain_moves.cu", "isf_static.cu"]
 
 
 def nvcc():

@@ -108,6 +108,8 @@ int compute_terms(Ctx& c, std::vector<double>& h, bool want_tmat) {
 
 }  // namespace
 
+void pgb::set_global_error(const std::string& msg) { g_last_error = msg; }
+
 extern "C" {
 
 const char* pgb_last_error(const pgb_ctx* ctx) {

@@ -20,6 +20,8 @@ struct AzizParams {
     double rm, A, epsilon, alpha, beta, D, C6, C8, C10;
 };
 AzizParams aziz_params(int year);
+// message returned by pgb_last_error(NULL) on this host thread
+void set_global_error(const std::string& msg);
 
 // Read-only view of one path handed to kernels by value.
 struct PathView {
