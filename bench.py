@@ -203,6 +203,26 @@ def cpu_baseline(w, threads, budget_s=15.0):
                        % (len(idx), int(sel["n"].min()), int(sel["n"].max()), reps, threads))
 
 
+def plain_form_rate(pgb, n=64, t=2.0, tau=0.004, steps=1):
+    """The plain FP64 GPU form: the reference's move loop on the host (MT19937,
+    staging + centre of mass) with one FP64 device action call per Metropolis
+    decision, on one walker of the workload's mean size."""
+    from pimc_gb300 import worldlines as wl
+    m = wl.even_slices(t, tau)
+    L = wl.box_side(n)
+    mbar = wl.default_mbar(n, L ** 3, wl.LAMBDA_HE4, tau, m)
+    a = pgb.Action(L, m, n, tau, wl.LAMBDA_HE4, precision=pgb.PGB_FP64)
+    a.load(wl.seeded_worldlines(n, m, L, wl.LAMBDA_HE4, tau, 5))
+    a.plain_seed(139853)
+    a.plain_run(1, mbar=mbar, temperature=1.0 / (m * tau), num_updates=50)   # warm-up
+    t0 = time.perf_counter()
+    r = a.plain_run(steps, mbar=mbar, temperature=1.0 / (m * tau))
+    dt = time.perf_counter() - t0
+    return dict(value=r["bead_updates"] / dt, unit="bead-updates/s",
+                walker="N=%d M=%d T=%.3f Mbar=%d, %d step(s), energy sampled per step" % (n, m, 1.0 / (m * tau), mbar, steps),
+                accepted=r["accepted"], attempted=r["attempted"])
+
+
 def run_reference(args):
     rank, ws = dist_init()
     if rank != 0:
@@ -306,7 +326,8 @@ def main():
                                   "T~U[1,4] K, tau=0.004, M even, Aziz HFDHE2, rho=0.02186, "
                                   "staging (Mbar 32) + COM moves, energy sampled every sweep"
                                   % W.W,
-                      "threads_per_walker": W.threads(), "l2": "flushed between timed steps",
+                      "schedule": W.threads(), "autotune_ms": W.tuning(),
+                      "l2": "flushed between timed steps",
                       "parallelism": "replicas" if ws > 1 else "single"},
            "e2e": {"value": e2e_val, "unit": "bead-updates/s", "h2d_bytes_per_step": state_bytes,
                    "d2h_bytes_per_step": stats_bytes},
@@ -319,6 +340,8 @@ def main():
            "clocks": clocks}
     if rank == 0 and not args.no_baseline:
         out["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
+        out["plain_fp64"] = plain_form_rate(pgb)
+        out["plain_fp64"]["batched_over_plain"] = value / out["plain_fp64"]["value"]
     if rank == 0:
         print(json.dumps(out))
 

@@ -187,7 +187,7 @@ typedef struct {
     double        p_com;        /* centre-of-mass move probability */
     uint64_t      seed;         /* Philox key; walker w uses stream w */
     int           aziz_year;
-    int           threads_per_walker; /* 0: autotune */
+    int           threads_per_walker; /* schedule (pgb_walkers_threads); 0: autotune */
     int           var_updates;  /* 1: stage length 2 + U{0..Mbar-2} */
 } pgb_walkers_params;
 
@@ -217,13 +217,24 @@ size_t pgb_walkers_state_bytes(pgb_walkers* w);
 /* Run `sweeps` MC steps for every walker (numUpdates moves per step,
  * pimc.cpp:62-65, then one energy sample), asynchronously on the stream. */
 int pgb_walkers_run_async(pgb_walkers* w, int sweeps, int measure);
+/* waits for the stream; PGB_ETIMEOUT if a walker's bounded device wait ran
+ * out (the walker's chain stopped; its state is left as it was) */
 int pgb_walkers_sync(pgb_walkers* w);
 int pgb_walkers_stats(pgb_walkers* w, pgb_walker_stats* per_walker);
 int pgb_walkers_reset_stats(pgb_walkers* w);
 /* launches of walker kernels issued so far */
 long long pgb_walkers_launch_count(pgb_walkers* w);
-/* threads per walker chosen by the autotuner (or set) */
+/* schedule chosen by the autotuner (or set): 64/128/256 = one CTA of that
+ * size per walker; 1004/1008/1016 (2004/2008/2016) = walkers packed as thread
+ * teams of 1-8 warps into 256-thread CTAs sized for 4/8/16 pair evaluations
+ * per thread per move, 3 (2) CTAs per SM; 3003 (3002) = one warp per
+ * imaginary-time window, up to min(8, M/(Mbar+1)) concurrent staging moves
+ * per walker on disjoint windows, 3 (2) CTAs per SM; 4004/4008/4016 = packed
+ * teams whose slab rows are staged in shared memory by bulk copies */
 int pgb_walkers_threads(pgb_walkers* w);
+/* the autotuner's record: schedules tried and one-sweep time (ms) of each;
+ * returns the number of candidates, fills at most cap */
+int pgb_walkers_tuning(pgb_walkers* w, int* scheds, float* ms, int cap);
 /* Energy per particle (thermodynamic estimator, primitive action) of each
  * walker's current configuration, FP64 pair sums (plain form) or mixed. */
 int pgb_walkers_energy(pgb_walkers* w, int precision, double* en_per_walker);

@@ -1346,7 +1346,7 @@ int orc_run_steps(orc_sys* h, orc_mt* mt, const orc_move_params* mp, int nsteps,
 
 double orc_walkers_cpu(int W, const int* N, const int* M, const double* T,
                        const double* L, const uint32_t* seeds, double tau,
-                       double lambda, int nsteps, int nthreads,
+                       double lambda, int nequil, int nsteps, int nthreads,
                        double* mean_en, long long* bead_updates) {
     if (nthreads < 1) nthreads = 1;
     std::atomic<int> nextw(0);
@@ -1391,6 +1391,8 @@ double orc_walkers_cpu(int W, const int* N, const int* M, const double* T,
             mp.temperature = T[w]; mp.p_com = 0.05; mp.num_updates = 0;
             std::vector<double> en(nsteps);
             orc_move_stats st{};
+            if (nequil > 0) run_steps(s, &mt, &mp, nequil, nullptr, 0, nullptr, &st);
+            st = orc_move_stats{};
             run_steps(s, &mt, &mp, nsteps, nullptr, 0, en.data(), &st);
             double acc = 0.0;
             for (double e : en) acc += e;

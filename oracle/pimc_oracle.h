@@ -148,11 +148,12 @@ int orc_run_steps(orc_sys* s, orc_mt* mt, const orc_move_params* mp, int nsteps,
  * MT19937 seed seeds[w]) for nsteps each, on nthreads threads.  Each walker
  * w has N[w] particles, M[w] slices, temperature T[w], box side L[w];
  * initial worldlines are generated by the oracle's lattice-free generator
- * from the same seed.  Returns wall seconds; fills per-walker mean E/N and
- * bead-update counts. */
+ * from the same seed.  The first nequil steps are not sampled.  Returns wall
+ * seconds; fills per-walker mean E/N over the nsteps sampled steps and the
+ * bead-update counts of the sampled steps. */
 double orc_walkers_cpu(int W, const int* N, const int* M, const double* T,
                        const double* L, const uint32_t* seeds, double tau,
-                       double lambda, int nsteps, int nthreads,
+                       double lambda, int nequil, int nsteps, int nthreads,
                        double* mean_en, long long* bead_updates);
 
 #ifdef __cplusplus

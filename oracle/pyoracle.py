@@ -103,7 +103,7 @@ def load():
         "orc_run_steps": (C.c_int, [_VP, _VP, C.POINTER(OrcMoveParams), C.c_int, _IP, C.c_int,
                                     _DP, C.POINTER(OrcMoveStats)]),
         "orc_walkers_cpu": (C.c_double, [C.c_int, _IP, _IP, _DP, _DP, C.POINTER(C.c_uint32),
-                                         C.c_double, C.c_double, C.c_int, C.c_int, _DP,
+                                         C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _DP,
                                          C.POINTER(C.c_longlong)]),
     }
     for name, (res, args) in sig.items():
@@ -330,7 +330,7 @@ class MT:
         return self.lib.orc_mt_randnorm(self.h, mean, sd)
 
 
-def walkers_cpu(n, m, temperature, side, seeds, tau, lam, nsteps, threads):
+def walkers_cpu(n, m, temperature, side, seeds, tau, lam, nsteps, threads, nequil=0):
     lib = load()
     n = np.ascontiguousarray(n, dtype=np.int32)
     m = np.ascontiguousarray(m, dtype=np.int32)
@@ -340,6 +340,7 @@ def walkers_cpu(n, m, temperature, side, seeds, tau, lam, nsteps, threads):
     en = np.zeros(len(n))
     bu = np.zeros(len(n), dtype=np.int64)
     sec = lib.orc_walkers_cpu(len(n), _i(n), _i(m), _d(t), _d(L),
-                              s.ctypes.data_as(C.POINTER(C.c_uint32)), tau, lam, nsteps, threads,
+                              s.ctypes.data_as(C.POINTER(C.c_uint32)), tau, lam, nequil, nsteps,
+                              threads,
                               _d(en), bu.ctypes.data_as(C.POINTER(C.c_longlong)))
     return sec, en, bu

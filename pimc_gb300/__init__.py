@@ -306,5 +306,12 @@ class Walkers:
     def threads(self):
         return self.lib.pgb_walkers_threads(self.h)
 
+    def tuning(self):
+        n = self.lib.pgb_walkers_tuning(self.h, None, None, 0)
+        sc = (C.c_int * max(n, 1))()
+        ms = (C.c_float * max(n, 1))()
+        self.lib.pgb_walkers_tuning(self.h, sc, ms, n)
+        return {int(sc[i]): float(ms[i]) for i in range(n)}
+
     def stream(self):
         return self.lib.pgb_walkers_stream(self.h)

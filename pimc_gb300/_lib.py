@@ -101,6 +101,7 @@ _SIGS = {
     "pgb_walkers_reset_stats": (C.c_int, [_VP]),
     "pgb_walkers_launch_count": (C.c_longlong, [_VP]),
     "pgb_walkers_threads": (C.c_int, [_VP]),
+    "pgb_walkers_tuning": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int]),
     "pgb_walkers_energy": (C.c_int, [_VP, C.c_int, _DP]),
     "pgb_walkers_stream": (_VP, [_VP]),
     "pgb_walkers_last_error": (C.c_char_p, [_VP]),

@@ -248,6 +248,850 @@ k_walkers_run(const WalkerMeta* __restrict__ meta, const int* __restrict__ order
     }
 }
 
+// ---------------------------------------------------------------------------
+// Packed-team schedule.  Each walker gets a team of 1, 2, 4 or 8 warps, sized
+// to its per-move pair count (about 2 N Mbar/2 pairs), and up to 8 warps of
+// teams share one 256-thread CTA.  A team synchronises on its own named
+// barrier (bar.sync id, count) -- or __syncwarp for one-warp teams -- so small
+// walkers never wait on large ones.  The staging path is drawn as a Brownian
+// bridge built by one warp with shuffle scans (the same free-particle
+// distribution as the sequential staging construction, move.cpp:263-292).
+// ---------------------------------------------------------------------------
+constexpr int kTeamCta = 256;
+
+__device__ __forceinline__ void team_sync(int slot, int nthreads) {
+    if (nthreads == 32) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" :: "r"(slot + 1), "r"(nthreads) : "memory");
+}
+
+__device__ __forceinline__ float warp_scan_incl(float x, int lane) {
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        float y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    return x;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kTeamCta, MINB)
+k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
+               float4* __restrict__ pos, WalkerAcc* __restrict__ accs,
+               unsigned long long* __restrict__ ctr, int sweeps, int measure, AzizF az,
+               double tau, double lambda, float p_com, int var_updates, uint64_t seed) {
+    __shared__ float4 s_new[8][2][kMaxStage];
+    __shared__ float4 s_old[8][2][kMaxStage];
+    __shared__ double s_red[8][8];
+    __shared__ int s_acc[8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int4 tm = make_int4(-1, 0, 0, 0);
+    #pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        int4 t = teams[blockIdx.x * 8 + k];
+        if (t.w && warp >= t.y && warp < t.y + t.z) tm = t;
+    }
+    if (tm.x < 0) return;                       // warp not in any team
+    const int w = tm.x, slot = tm.y, nw = tm.z, T = nw * 32;
+    const int tt = threadIdx.x - slot * 32;     // thread index in the team
+    const int wi = warp - slot;                 // warp index in the team
+    const WalkerMeta m = meta[w];
+    float4* P = pos + m.off;
+    const int N = m.N, M = m.M;
+    double* red = s_red[slot];
+    const unsigned long long sweep0 = ctr[w];
+    double esum = 0.0, esumsq = 0.0;
+    long long nsamp = 0, nbu = 0, att0 = 0, att1 = 0, acc0 = 0, acc1 = 0;
+    int buf = 0;
+    // pair-loop mapping: G threads per partner j when the team has at least N
+    // threads (thread tt -> j = tt % N, moved beads k = tt / N, +G, ...), else
+    // one thread per partner and a loop over partners
+    const int G = (T >= N) ? T / N : 1;
+    const int j0 = (T >= N) ? ((tt < G * N) ? tt % N : N) : tt;
+    const int kb0 = (T >= N) ? tt / N : 0;
+    const int jstep = (T >= N) ? N : T;
+
+    for (int sw = 0; sw < sweeps; ++sw) {
+        const unsigned long long gs = sweep0 + sw;
+        const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
+        for (int u = 0; u < m.num_updates; ++u) {
+            uint4 r0 = wrand(seed, w, (uint32_t)u, g0, g1, 0u);
+            const bool com = u01f(r0.x) < p_com;
+            const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
+            if (!com) {
+                const int s0 = (int)(((unsigned long long)r0.y * (unsigned)M) >> 32);
+                const int len = var_updates
+                    ? 2 + (int)(((unsigned long long)r0.w * (unsigned)(m.mbar - 1)) >> 32)
+                    : m.mbar;
+                const int nmove = len - 1;
+                float4* sn = s_new[slot][buf];
+                float4* so = s_old[slot][buf];
+                if (wi == 0) {
+                    // Brownian bridge between the fixed beads at s0 and s0+len:
+                    // W_j = sum_{i<=j} sigma z_i, x_j = x0 + (j/len)(xe - x0) + W_j - (j/len) W_len
+                    int se = s0 + len; if (se >= M) se -= M;
+                    const float4 x0 = P[(size_t)s0 * N + i], xe = P[(size_t)se * N + i];
+                    float4 ob0 = make_float4(0, 0, 0, 0), ob1 = ob0;
+                    {
+                        int sl = s0 + 1 + lane; if (sl >= M) sl -= M;
+                        if (lane < nmove) ob0 = P[(size_t)sl * N + i];
+                        sl = s0 + 33 + lane; if (sl >= M) sl -= M;
+                        if (lane + 32 < nmove) ob1 = P[(size_t)sl * N + i];
+                    }
+                    float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
+                    const int j1 = lane + 1, j2 = lane + 33;
+                    if (j1 <= len) {
+                        uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)j1);
+                        float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+                        a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
+                    }
+                    if (j2 <= len) {
+                        uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)j2);
+                        float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+                        a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
+                    }
+                    float W1x = warp_scan_incl(a1x, lane), W1y = warp_scan_incl(a1y, lane),
+                          W1z = warp_scan_incl(a1z, lane);
+                    float W2x = warp_scan_incl(a2x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
+                    float W2y = warp_scan_incl(a2y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
+                    float W2z = warp_scan_incl(a2z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
+                    const int src = (len <= 32) ? len - 1 : len - 33;
+                    float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
+                    float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
+                    float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
+                    const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
+                    const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
+                    const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
+                    const float il = 1.0f / (float)len;
+                    #pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = lane + 32 * h;            // bead k <-> j = k + 1
+                        if (k < nmove) {
+                            const float f = (float)(k + 1) * il;
+                            const float Wx = h ? W2x : W1x, Wy = h ? W2y : W1y, Wz = h ? W2z : W1z;
+                            so[k] = h ? ob1 : ob0;
+                            sn[k] = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
+                                                put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
+                                                put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
+                        }
+                    }
+                }
+                team_sync(slot, T);
+                KahanF acc;
+                // thread <-> partner j (G threads per partner share the moved beads)
+                for (int j = j0; j < N; j += jstep) {
+                    if (j == i) continue;
+                    #pragma unroll 4
+                    for (int k = kb0; k < nmove; k += G) {
+                        int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                        const float4 pj = P[(size_t)sl * N + j];
+                        const float4 a = sn[k], b = so[k];
+                        const float ax = min_image32(a.x - pj.x, m.L, m.Linv);
+                        const float ay = min_image32(a.y - pj.y, m.L, m.Linv);
+                        const float az_ = min_image32(a.z - pj.z, m.L, m.Linv);
+                        const float bx = min_image32(b.x - pj.x, m.L, m.Linv);
+                        const float by = min_image32(b.y - pj.y, m.L, m.Linv);
+                        const float bz = min_image32(b.z - pj.z, m.L, m.Linv);
+                        const float vn = aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az);
+                        const float vo = aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az);
+                        acc.add(vn - vo);
+                    }
+                }
+                double part = warp_sum(acc.value());
+                if (lane == 0) red[wi] = part;
+                team_sync(slot, T);
+                if (tt == 0) {
+                    double dV = 0.0;
+                    for (int q = 0; q < nw; ++q) dV += red[q];
+                    uint4 ra = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFFu);
+                    const double x = u01d(ra.x, ra.y);
+                    const double a = -(tau * dV);
+                    s_acc[slot] = (a >= 0.0 || x < exp(a)) ? 1 : 0;
+                }
+                team_sync(slot, T);
+                const int ok = s_acc[slot];
+                if (wi == 0 && ok) {
+                    for (int k2 = lane; k2 < nmove; k2 += 32) {
+                        int sl = s0 + 1 + k2; if (sl >= M) sl -= M;
+                        P[(size_t)sl * N + i] = sn[k2];
+                    }
+                    __syncwarp();
+                }
+                att1 += 1; acc1 += ok; nbu += nmove;
+                buf ^= 1;
+            } else {
+                const float sx = m.com_delta * (u01f(r0.y) - 0.5f);
+                const float sy = m.com_delta * (u01f(r0.w) - 0.5f);
+                const uint4 r1 = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFEu);
+                const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
+                KahanF acc;
+                for (int j = j0; j < N; j += jstep) {
+                    if (j == i) continue;
+                    #pragma unroll 4
+                    for (int t = kb0; t < M; t += G) {
+                        const float4 pi = P[(size_t)t * N + i];
+                        const float4 pj = P[(size_t)t * N + j];
+                        const float bx = min_image32(pi.x - pj.x, m.L, m.Linv);
+                        const float by = min_image32(pi.y - pj.y, m.L, m.Linv);
+                        const float bz = min_image32(pi.z - pj.z, m.L, m.Linv);
+                        const float ax = min_image32(bx + sx, m.L, m.Linv);
+                        const float ay = min_image32(by + sy, m.L, m.Linv);
+                        const float az_ = min_image32(bz + sz, m.L, m.Linv);
+                        const float vn = aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az);
+                        const float vo = aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az);
+                        acc.add(vn - vo);
+                    }
+                }
+                double part = warp_sum(acc.value());
+                if (lane == 0) red[wi] = part;
+                team_sync(slot, T);
+                if (tt == 0) {
+                    double dV = 0.0;
+                    for (int q = 0; q < nw; ++q) dV += red[q];
+                    const double x = u01d(r1.y, r1.z);
+                    const double a = -(tau * dV);
+                    s_acc[slot] = (a >= 0.0 || x < exp(a)) ? 1 : 0;
+                }
+                team_sync(slot, T);
+                const int ok = s_acc[slot];
+                if (ok)
+                    for (int t2 = tt; t2 < M; t2 += T) {
+                        float4 pi = P[(size_t)t2 * N + i];
+                        pi.x = put_inside(pi.x + sx, m.L, m.Linv);
+                        pi.y = put_inside(pi.y + sy, m.L, m.Linv);
+                        pi.z = put_inside(pi.z + sz, m.L, m.Linv);
+                        P[(size_t)t2 * N + i] = pi;
+                    }
+                team_sync(slot, T);
+                att0 += 1; acc0 += ok; nbu += M;
+            }
+        }
+        if (measure > 0 && ((gs + 1) % (unsigned long long)measure) == 0) {
+            team_sync(slot, T);
+            KahanF pot, kin;
+            const int half = (N - 1) / 2;
+            const bool even = (N % 2) == 0;
+            for (int idx = tt; idx < M * N; idx += T) {
+                const int t = idx / N, ii = idx - t * N;
+                const float4 ri = P[(size_t)t * N + ii];
+                const int cnt = half + ((even && ii < N / 2) ? 1 : 0);
+                for (int d = 1; d <= cnt; ++d) {
+                    int jj = ii + d; if (jj >= N) jj -= N;
+                    const float4 rj = P[(size_t)t * N + jj];
+                    const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
+                    const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
+                    const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
+                    pot.add(aziz_v32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+                }
+                const int tn = (t + 1 == M) ? 0 : t + 1;
+                const float4 rn = P[(size_t)tn * N + ii];
+                const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
+                const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
+                const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
+                kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+            }
+            double pv = warp_sum(pot.value()), kv = warp_sum(kin.value());
+            if (lane == 0) { red[wi] = pv; }
+            team_sync(slot, T);
+            double V = 0.0;
+            if (tt == 0) for (int q = 0; q < nw; ++q) V += red[q];
+            team_sync(slot, T);
+            if (lane == 0) red[wi] = kv;
+            team_sync(slot, T);
+            if (tt == 0) {
+                double K2 = 0.0;
+                for (int q = 0; q < nw; ++q) K2 += red[q];
+                const double totK = 1.5 * N / tau - K2 * ((0.25 / (lambda * tau)) / (tau * M));
+                const double e = (totK + V / M + m.tailV) / N;
+                esum += e; esumsq += e * e; nsamp += 1;
+            }
+            team_sync(slot, T);
+        }
+    }
+    if (tt == 0) {
+        WalkerAcc& A = accs[w];
+        A.esum += esum; A.esumsq += esumsq; A.samples += nsamp; A.bead_updates += nbu;
+        A.att[0] += att0; A.att[1] += att1; A.acc[0] += acc0; A.acc[1] += acc1;
+        ctr[w] = sweep0 + sweeps;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Time-window schedule.  Staging moves whose closed segments [s0, s0+len] lie
+// in disjoint imaginary-time windows touch disjoint sets of beads and read no
+// bead another one writes, so they commute: applying them at once equals
+// applying them one after another.  A walker with M slices gets P =
+// min(8, M / (Mbar + 1)) warps; every round draws a random offset phi, cuts
+// the slices into P windows of S = M / P slices starting at phi, and each warp
+// makes one complete staging move inside its window (bridge, pair sums,
+// Metropolis test, write-back) with warp-level synchronisation only.  The
+// selection of particle, window position and stage length never depends on
+// the configuration, so every move keeps the staging acceptance
+// min(1, exp(-dU)) and detailed balance; a sweep makes the same number of
+// staging and centre-of-mass moves as the sequential loop in expectation.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool metropolis(double dV, double tau, uint32_t hi, uint32_t lo) {
+    const double x = u01d(hi, lo);
+    const double a = -(tau * dV);
+    if (a >= 0.0) return true;
+    if (x > 0.0) {
+        // FP32 screen; exact FP64 test only near the boundary
+        const float d = (float)a - __logf((float)x);
+        if (d > 1e-3f) return true;
+        if (d < -1e-3f) return false;
+    }
+    return x < exp(a);
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kTeamCta, MINB)
+k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
+                  float4* __restrict__ pos, WalkerAcc* __restrict__ accs,
+                  unsigned long long* __restrict__ ctr, int sweeps, int measure, AzizF az,
+                  double tau, double lambda, float p_com, int var_updates, uint64_t seed) {
+    __shared__ float4 s_new[8][kMaxStage];
+    __shared__ float4 s_old[8][kMaxStage];
+    __shared__ double s_red[8][8];
+    __shared__ int s_acc[8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int4 tm = make_int4(-1, 0, 0, 0);
+    #pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        int4 t = teams[blockIdx.x * 8 + k];
+        if (t.w && warp >= t.y && warp < t.y + t.z) tm = t;
+    }
+    if (tm.x < 0) return;
+    const int w = tm.x, slot = tm.y, P = tm.z, T = P * 32;
+    float4* so = s_old[warp];
+    const int tt = threadIdx.x - slot * 32, wi = warp - slot;
+    const WalkerMeta m = meta[w];
+    float4* Pp = pos + m.off;
+    const int N = m.N, M = m.M;
+    const int S = M / P;                         // window length (>= Mbar + 1)
+    float4* sn = s_new[warp];
+    double* red = s_red[slot];
+    const unsigned long long sweep0 = ctr[w];
+    double esum = 0.0, esumsq = 0.0;
+    long long nsamp = 0, nbu = 0, nbu_com = 0, att0 = 0, att1 = 0, acc0 = 0, acc1 = 0;
+
+    for (int sw = 0; sw < sweeps; ++sw) {
+        const unsigned long long gs = sweep0 + sw;
+        const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
+        // split of the sweep's numUpdates moves into staging and COM moves
+        const uint4 rs = wrand(seed, w, 0xC0000000u, g0, g1, 0u);
+        const float ncom_f = p_com * (float)m.num_updates;
+        const int n_com = (int)ncom_f + ((u01f(rs.x) < ncom_f - floorf(ncom_f)) ? 1 : 0);
+        const int n_stage = m.num_updates - n_com;
+        const int rounds = (n_stage + P - 1) / P;
+        for (int r = 0; r < rounds; ++r) {
+            const uint4 rphi = wrand(seed, w, 0x80000000u | (uint32_t)r, g0, g1, 0u);
+            const int phi = (int)(((unsigned long long)rphi.x * (unsigned)M) >> 32);
+            const bool active = (r * P + wi) < n_stage;
+            if (active) {
+                const uint32_t c0 = (uint32_t)r | ((uint32_t)wi << 24);
+                const uint4 r0 = wrand(seed, w, c0, g0, g1, 0u);
+                const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
+                const int len = var_updates
+                    ? 2 + (int)(((unsigned long long)r0.w * (unsigned)(m.mbar - 1)) >> 32)
+                    : m.mbar;
+                const int nmove = len - 1;
+                const int span = S - len;                                  // >= 1
+                int s0 = phi + wi * S + (int)(((unsigned long long)r0.y * (unsigned)span) >> 32);
+                s0 %= M;
+                // bridge (as in the team schedule), this warp only
+                int se = s0 + len; if (se >= M) se -= M;
+                const float4 x0 = Pp[(size_t)s0 * N + i], xe = Pp[(size_t)se * N + i];
+                float4 ob0 = make_float4(0, 0, 0, 0), ob1 = ob0;
+                {
+                    int sl = s0 + 1 + lane; if (sl >= M) sl -= M;
+                    if (lane < nmove) ob0 = Pp[(size_t)sl * N + i];
+                    sl = s0 + 33 + lane; if (sl >= M) sl -= M;
+                    if (lane + 32 < nmove) ob1 = Pp[(size_t)sl * N + i];
+                }
+                float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
+                if (lane + 1 <= len) {
+                    const uint4 a = wrand(seed, w, c0, g0, g1, (uint32_t)(lane + 1));
+                    const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+                    a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
+                }
+                if (lane + 33 <= len) {
+                    const uint4 a = wrand(seed, w, c0, g0, g1, (uint32_t)(lane + 33));
+                    const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+                    a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
+                }
+                const float W1x = warp_scan_incl(a1x, lane), W1y = warp_scan_incl(a1y, lane),
+                            W1z = warp_scan_incl(a1z, lane);
+                const float W2x = warp_scan_incl(a2x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
+                const float W2y = warp_scan_incl(a2y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
+                const float W2z = warp_scan_incl(a2z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
+                const int src = (len <= 32) ? len - 1 : len - 33;
+                const float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
+                const float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
+                const float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
+                const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
+                const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
+                const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
+                const float il = 1.0f / (float)len;
+                float4 mine0 = make_float4(0, 0, 0, 0), mine1 = mine0;
+                #pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int k = lane + 32 * h;
+                    if (k < nmove) {
+                        const float f = (float)(k + 1) * il;
+                        const float Wx = h ? W2x : W1x, Wy = h ? W2y : W1y, Wz = h ? W2z : W1z;
+                        const float4 nv = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
+                                                      put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
+                                                      put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
+                        sn[k] = nv;
+                        so[k] = h ? ob1 : ob0;
+                        if (h) mine1 = nv; else mine0 = nv;
+                    }
+                }
+                __syncwarp();
+                // pair sums: lane <-> partner j, loop over moved beads k
+                KahanF acc;
+                for (int j = lane; j < N; j += 32) {
+                    if (j == i) continue;
+                    #pragma unroll 4
+                    for (int k = 0; k < nmove; ++k) {
+                        int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                        const float4 pj = Pp[(size_t)sl * N + j];
+                        const float4 a = sn[k], b = so[k];
+                        const float ax = min_image32(a.x - pj.x, m.L, m.Linv);
+                        const float ay = min_image32(a.y - pj.y, m.L, m.Linv);
+                        const float az_ = min_image32(a.z - pj.z, m.L, m.Linv);
+                        const float bx = min_image32(b.x - pj.x, m.L, m.Linv);
+                        const float by = min_image32(b.y - pj.y, m.L, m.Linv);
+                        const float bz = min_image32(b.z - pj.z, m.L, m.Linv);
+                        acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                                aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+                    }
+                }
+                const double dV = warp_sum(acc.value());
+                int ok = 0;
+                if (lane == 0) {
+                    const uint4 ra = wrand(seed, w, c0, g0, g1, 0xFFFFu);
+                    ok = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
+                }
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (ok) {
+                    for (int k = lane; k < nmove; k += 32) {
+                        int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                        Pp[(size_t)sl * N + i] = (k < 32) ? mine0 : mine1;
+                    }
+                }
+                att1 += 1; acc1 += ok; nbu += nmove;
+            }
+            team_sync(slot, T);
+        }
+        // centre-of-mass moves, whole team
+        for (int c = 0; c < n_com; ++c) {
+            const uint4 r0 = wrand(seed, w, 0x40000000u | (uint32_t)c, g0, g1, 0u);
+            const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
+            const float sx = m.com_delta * (u01f(r0.y) - 0.5f);
+            const float sy = m.com_delta * (u01f(r0.w) - 0.5f);
+            const float sz = m.com_delta * (u01f(r0.x) - 0.5f);
+            KahanF acc;
+            for (int idx = tt; idx < M * N; idx += T) {
+                const int t = idx / N, j = idx - t * N;
+                if (j == i) continue;
+                const float4 pi = Pp[(size_t)t * N + i];
+                const float4 pj = Pp[(size_t)t * N + j];
+                const float bx = min_image32(pi.x - pj.x, m.L, m.Linv);
+                const float by = min_image32(pi.y - pj.y, m.L, m.Linv);
+                const float bz = min_image32(pi.z - pj.z, m.L, m.Linv);
+                const float ax = min_image32(bx + sx, m.L, m.Linv);
+                const float ay = min_image32(by + sy, m.L, m.Linv);
+                const float az_ = min_image32(bz + sz, m.L, m.Linv);
+                acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                        aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+            }
+            const double part = warp_sum(acc.value());
+            if (lane == 0) red[wi] = part;
+            team_sync(slot, T);
+            if (tt == 0) {
+                double dV = 0.0;
+                for (int q = 0; q < P; ++q) dV += red[q];
+                const uint4 ra = wrand(seed, w, 0x40000000u | (uint32_t)c, g0, g1, 0xFFFEu);
+                s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
+            }
+            team_sync(slot, T);
+            const int ok = s_acc[slot];
+            if (ok)
+                for (int t = tt; t < M; t += T) {
+                    float4 pi = Pp[(size_t)t * N + i];
+                    pi.x = put_inside(pi.x + sx, m.L, m.Linv);
+                    pi.y = put_inside(pi.y + sy, m.L, m.Linv);
+                    pi.z = put_inside(pi.z + sz, m.L, m.Linv);
+                    Pp[(size_t)t * N + i] = pi;
+                }
+            team_sync(slot, T);
+            att0 += 1; acc0 += ok; nbu_com += M;
+        }
+        if (measure > 0 && ((gs + 1) % (unsigned long long)measure) == 0) {
+            KahanF pot, kin;
+            const int half = (N - 1) / 2;
+            const bool even = (N % 2) == 0;
+            for (int idx = tt; idx < M * N; idx += T) {
+                const int t = idx / N, ii = idx - t * N;
+                const float4 ri = Pp[(size_t)t * N + ii];
+                const int cnt = half + ((even && ii < N / 2) ? 1 : 0);
+                for (int d = 1; d <= cnt; ++d) {
+                    int jj = ii + d; if (jj >= N) jj -= N;
+                    const float4 rj = Pp[(size_t)t * N + jj];
+                    const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
+                    const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
+                    const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
+                    pot.add(aziz_v32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+                }
+                const int tn = (t + 1 == M) ? 0 : t + 1;
+                const float4 rn = Pp[(size_t)tn * N + ii];
+                const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
+                const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
+                const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
+                kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+            }
+            const double pv = warp_sum(pot.value()), kv = warp_sum(kin.value());
+            if (lane == 0) red[wi] = pv;
+            team_sync(slot, T);
+            double V = 0.0;
+            if (tt == 0) for (int q = 0; q < P; ++q) V += red[q];
+            team_sync(slot, T);
+            if (lane == 0) red[wi] = kv;
+            team_sync(slot, T);
+            if (tt == 0) {
+                double K2 = 0.0;
+                for (int q = 0; q < P; ++q) K2 += red[q];
+                const double totK = 1.5 * N / tau - K2 * ((0.25 / (lambda * tau)) / (tau * M));
+                const double e = (totK + V / M + m.tailV) / N;
+                esum += e; esumsq += e * e; nsamp += 1;
+            }
+            team_sync(slot, T);
+        }
+    }
+    if (tt == 0) {
+        WalkerAcc& A = accs[w];
+        A.esum += esum; A.esumsq += esumsq; A.samples += nsamp;
+        A.att[0] += att0; A.acc[0] += acc0;
+        atomicAdd(reinterpret_cast<unsigned long long*>(&A.bead_updates), (unsigned long long)nbu_com);
+        ctr[w] = sweep0 + sweeps;
+    }
+    // staging counters are per warp (each warp moves in its own window)
+    if (lane == 0) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].att[1]), (unsigned long long)att1);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].acc[1]), (unsigned long long)acc1);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].bead_updates), (unsigned long long)nbu);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged team schedule.  Same teams as the packed-team schedule, but the
+// rows of the walker slab a move needs -- the moved slices for staging, the
+// slices in chunks of Mbar for centre-of-mass moves and energy samples -- are
+// copied into the team's shared-memory buffer with one or two bulk copies
+// (cp.async.bulk, completion on an mbarrier) issued by one thread as soon as
+// the move is drawn.  The copy overlaps the bridge construction; the pair
+// sums then read only shared memory.  Every wait is bounded: a copy that does
+// not land within the limit sets the walker's error word and the team exits
+// together.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                 :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+constexpr long long kWaitLimit = 1LL << 22;   // try_wait polls before giving up
+
+// Copy rows [r0, r0 + nrows) (mod M) of a walker slab into buf; returns bytes.
+__device__ __forceinline__ uint32_t issue_rows(float4* buf, const float4* P, int N, int M, int r0,
+                                               int nrows, uint64_t* bar) {
+    const int first = min(nrows, M - r0);
+    const uint32_t b1 = (uint32_t)first * N * 16u, b2 = (uint32_t)(nrows - first) * N * 16u;
+    mbar_expect_tx(bar, b1 + b2);
+    bulk_load(buf, P + (size_t)r0 * N, b1, bar);
+    if (b2) bulk_load(buf + (size_t)first * N, P, b2, bar);
+    return b1 + b2;
+}
+
+// Bounded wait by every team thread; returns false (team-wide) on timeout.
+__device__ __forceinline__ bool team_wait(uint64_t* bar, uint32_t parity, int slot, int T,
+                                          int* s_fail, int* err_word) {
+    long long n = 0;
+    bool ok = true;
+    while (!mbar_try_wait(bar, parity)) {
+        if (++n > kWaitLimit) { ok = false; break; }
+    }
+    if (!ok) { atomicExch(s_fail, 1); if (err_word) atomicExch(err_word, 1); }
+    team_sync(slot, T);
+    return *(volatile int*)s_fail == 0;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kTeamCta, MINB)
+k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
+              float4* __restrict__ pos, WalkerAcc* __restrict__ accs,
+              unsigned long long* __restrict__ ctr, int* __restrict__ err, int sweeps, int measure,
+              AzizF az, double tau, double lambda, float p_com, int var_updates, uint64_t seed) {
+    extern __shared__ float4 dyn[];
+    __shared__ float4 s_new[8][kMaxStage];
+    __shared__ double s_red[8][8];
+    __shared__ int s_acc[8];
+    __shared__ int s_fail[8];
+    __shared__ __align__(8) uint64_t s_bar[8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int4 tm = make_int4(-1, 0, 0, 0);
+    #pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        int4 t = teams[blockIdx.x * 8 + k];
+        if (t.w && warp >= t.y && warp < t.y + t.z) tm = t;
+    }
+    if (tm.x < 0) return;
+    const int w = tm.x, slot = tm.y, nw = tm.z, T = nw * 32;
+    const int tt = threadIdx.x - slot * 32, wi = warp - slot;
+    const WalkerMeta m = meta[w];
+    float4* P = pos + m.off;
+    float4* buf = dyn + (tm.w - 1);              // team buffer: Mbar rows of N beads
+    const int N = m.N, M = m.M, C = m.mbar;
+    double* red = s_red[slot];
+    float4* sn = s_new[slot];
+    uint64_t* bar = &s_bar[slot];
+    int* fail = &s_fail[slot];
+    if (tt == 0) { mbar_init(bar, 1); *fail = 0; }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    team_sync(slot, T);
+    uint32_t phase = 0;
+    const unsigned long long sweep0 = ctr[w];
+    double esum = 0.0, esumsq = 0.0;
+    long long nsamp = 0, nbu = 0, att0 = 0, att1 = 0, acc0 = 0, acc1 = 0;
+    const int G = (T >= N) ? T / N : 1;
+    const int j0 = (T >= N) ? ((tt < G * N) ? tt % N : N) : tt;
+    const int kb0 = (T >= N) ? tt / N : 0;
+    const int jstep = (T >= N) ? N : T;
+
+    for (int sw = 0; sw < sweeps; ++sw) {
+        const unsigned long long gs = sweep0 + sw;
+        const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
+        for (int u = 0; u < m.num_updates; ++u) {
+            const uint4 r0 = wrand(seed, w, (uint32_t)u, g0, g1, 0u);
+            const bool com = u01f(r0.x) < p_com;
+            const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
+            if (!com) {
+                const int s0 = (int)(((unsigned long long)r0.y * (unsigned)M) >> 32);
+                const int len = var_updates
+                    ? 2 + (int)(((unsigned long long)r0.w * (unsigned)(m.mbar - 1)) >> 32)
+                    : m.mbar;
+                const int nmove = len - 1;
+                int rs = s0 + 1; if (rs >= M) rs -= M;
+                if (tt == 0) issue_rows(buf, P, N, M, rs, nmove, bar);
+                if (wi == 0) {
+                    int se = s0 + len; if (se >= M) se -= M;
+                    const float4 x0 = P[(size_t)s0 * N + i], xe = P[(size_t)se * N + i];
+                    float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
+                    if (lane + 1 <= len) {
+                        const uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)(lane + 1));
+                        const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+                        a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
+                    }
+                    if (lane + 33 <= len) {
+                        const uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)(lane + 33));
+                        const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+                        a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
+                    }
+                    const float W1x = warp_scan_incl(a1x, lane), W1y = warp_scan_incl(a1y, lane),
+                                W1z = warp_scan_incl(a1z, lane);
+                    const float W2x = warp_scan_incl(a2x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
+                    const float W2y = warp_scan_incl(a2y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
+                    const float W2z = warp_scan_incl(a2z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
+                    const int src = (len <= 32) ? len - 1 : len - 33;
+                    const float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
+                    const float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
+                    const float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
+                    const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
+                    const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
+                    const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
+                    const float il = 1.0f / (float)len;
+                    #pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = lane + 32 * h;
+                        if (k < nmove) {
+                            const float f = (float)(k + 1) * il;
+                            const float Wx = h ? W2x : W1x, Wy = h ? W2y : W1y, Wz = h ? W2z : W1z;
+                            sn[k] = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
+                                                put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
+                                                put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
+                        }
+                    }
+                }
+                if (!team_wait(bar, phase, slot, T, fail, err + w)) return;
+                phase ^= 1;
+                KahanF acc;
+                for (int j = j0; j < N; j += jstep) {
+                    if (j == i) continue;
+                    #pragma unroll 4
+                    for (int k = kb0; k < nmove; k += G) {
+                        const float4 pj = buf[k * N + j];
+                        const float4 a = sn[k], b = buf[k * N + i];
+                        const float ax = min_image32(a.x - pj.x, m.L, m.Linv);
+                        const float ay = min_image32(a.y - pj.y, m.L, m.Linv);
+                        const float az_ = min_image32(a.z - pj.z, m.L, m.Linv);
+                        const float bx = min_image32(b.x - pj.x, m.L, m.Linv);
+                        const float by = min_image32(b.y - pj.y, m.L, m.Linv);
+                        const float bz = min_image32(b.z - pj.z, m.L, m.Linv);
+                        acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                                aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+                    }
+                }
+                const double part = warp_sum(acc.value());
+                if (lane == 0) red[wi] = part;
+                team_sync(slot, T);
+                if (tt == 0) {
+                    double dV = 0.0;
+                    for (int q = 0; q < nw; ++q) dV += red[q];
+                    const uint4 ra = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFFu);
+                    s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
+                }
+                team_sync(slot, T);
+                const int ok = s_acc[slot];
+                if (wi == 0) {
+                    if (ok) {
+                        for (int k = lane; k < nmove; k += 32) {
+                            int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                            P[(size_t)sl * N + i] = sn[k];
+                        }
+                        fence_proxy_async_global();
+                    }
+                    __syncwarp();
+                }
+                att1 += 1; acc1 += ok; nbu += nmove;
+            } else {
+                const float sx = m.com_delta * (u01f(r0.y) - 0.5f);
+                const float sy = m.com_delta * (u01f(r0.w) - 0.5f);
+                const uint4 r1 = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFEu);
+                const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
+                KahanF acc;
+                for (int c0 = 0; c0 < M; c0 += C) {
+                    const int nr = min(C, M - c0);
+                    if (tt == 0) issue_rows(buf, P, N, M, c0, nr, bar);
+                    if (!team_wait(bar, phase, slot, T, fail, err + w)) return;
+                    phase ^= 1;
+                    for (int j = j0; j < N; j += jstep) {
+                        if (j == i) continue;
+                        #pragma unroll 4
+                        for (int t = kb0; t < nr; t += G) {
+                            const float4 pi = buf[t * N + i], pj = buf[t * N + j];
+                            const float bx = min_image32(pi.x - pj.x, m.L, m.Linv);
+                            const float by = min_image32(pi.y - pj.y, m.L, m.Linv);
+                            const float bz = min_image32(pi.z - pj.z, m.L, m.Linv);
+                            const float ax = min_image32(bx + sx, m.L, m.Linv);
+                            const float ay = min_image32(by + sy, m.L, m.Linv);
+                            const float az_ = min_image32(bz + sz, m.L, m.Linv);
+                            acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                                    aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+                        }
+                    }
+                    team_sync(slot, T);            // buffer free for the next chunk
+                }
+                const double part = warp_sum(acc.value());
+                if (lane == 0) red[wi] = part;
+                team_sync(slot, T);
+                if (tt == 0) {
+                    double dV = 0.0;
+                    for (int q = 0; q < nw; ++q) dV += red[q];
+                    s_acc[slot] = metropolis(dV, tau, r1.y, r1.z) ? 1 : 0;
+                }
+                team_sync(slot, T);
+                const int ok = s_acc[slot];
+                if (ok) {
+                    for (int t2 = tt; t2 < M; t2 += T) {
+                        float4 pi = P[(size_t)t2 * N + i];
+                        pi.x = put_inside(pi.x + sx, m.L, m.Linv);
+                        pi.y = put_inside(pi.y + sy, m.L, m.Linv);
+                        pi.z = put_inside(pi.z + sz, m.L, m.Linv);
+                        P[(size_t)t2 * N + i] = pi;
+                    }
+                    fence_proxy_async_global();
+                }
+                team_sync(slot, T);
+                att0 += 1; acc0 += ok; nbu += M;
+            }
+        }
+        if (measure > 0 && ((gs + 1) % (unsigned long long)measure) == 0) {
+            KahanF pot, kin;
+            const int half = (N - 1) / 2;
+            const bool even = (N % 2) == 0;
+            for (int c0 = 0; c0 < M; c0 += C) {
+                const int nr = min(C, M - c0);
+                if (tt == 0) issue_rows(buf, P, N, M, c0, nr, bar);
+                if (!team_wait(bar, phase, slot, T, fail, err + w)) return;
+                phase ^= 1;
+                for (int idx = tt; idx < nr * N; idx += T) {
+                    const int t = idx / N, ii = idx - t * N;
+                    const float4 ri = buf[t * N + ii];
+                    const int cnt = half + ((even && ii < N / 2) ? 1 : 0);
+                    for (int d = 1; d <= cnt; ++d) {
+                        int jj = ii + d; if (jj >= N) jj -= N;
+                        const float4 rj = buf[t * N + jj];
+                        const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
+                        const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
+                        const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
+                        pot.add(aziz_v32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+                    }
+                }
+                team_sync(slot, T);
+            }
+            for (int idx = tt; idx < M * N; idx += T) {
+                const int t = idx / N, ii = idx - t * N;
+                const int tn = (t + 1 == M) ? 0 : t + 1;
+                const float4 ri = P[(size_t)t * N + ii], rn = P[(size_t)tn * N + ii];
+                const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
+                const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
+                const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
+                kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+            }
+            const double pv = warp_sum(pot.value()), kv = warp_sum(kin.value());
+            if (lane == 0) red[wi] = pv;
+            team_sync(slot, T);
+            double V = 0.0;
+            if (tt == 0) for (int q = 0; q < nw; ++q) V += red[q];
+            team_sync(slot, T);
+            if (lane == 0) red[wi] = kv;
+            team_sync(slot, T);
+            if (tt == 0) {
+                double K2 = 0.0;
+                for (int q = 0; q < nw; ++q) K2 += red[q];
+                const double totK = 1.5 * N / tau - K2 * ((0.25 / (lambda * tau)) / (tau * M));
+                const double e = (totK + V / M + m.tailV) / N;
+                esum += e; esumsq += e * e; nsamp += 1;
+            }
+            team_sync(slot, T);
+        }
+    }
+    if (tt == 0) {
+        WalkerAcc& A = accs[w];
+        A.esum += esum; A.esumsq += esumsq; A.samples += nsamp; A.bead_updates += nbu;
+        A.att[0] += att0; A.att[1] += att1; A.acc[0] += acc0; A.acc[1] += acc1;
+        ctr[w] = sweep0 + sweeps;
+    }
+}
+
 __global__ void k_walkers_init(const WalkerMeta* __restrict__ meta, float4* __restrict__ pos,
                                uint64_t seed) {
     const int w = blockIdx.x;
@@ -341,6 +1185,14 @@ struct pgb_walkers {
     unsigned long long* d_ctr = nullptr;
     double* d_en = nullptr;
     double* d_stage = nullptr;
+    int* d_err = nullptr;                 // per-walker error word (bounded waits)
+    // packed-team schedules, one per pairs-per-thread target
+    int4* d_teams[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int team_ctas[7] = {0, 0, 0, 0, 0, 0, 0};   // 3 team targets, windows, 3 TMA targets
+    size_t team_smem[7] = {0, 0, 0, 0, 0, 0, 0};
+    // autotuner record: schedule and one-sweep time of each candidate
+    std::vector<int> tune_sched;
+    std::vector<float> tune_ms;
     cudaStream_t stream = nullptr;
     long long launches = 0;
     std::string err;
@@ -354,9 +1206,151 @@ struct pgb_walkers {
 namespace {
 thread_local std::string g_werr;
 
-cudaError_t launch_run(pgb_walkers* h, int tpw, int sweeps, int measure) {
+// Schedules: 64/128/256 = one CTA of that many threads per walker;
+// 1004/1008/1016 = packed teams sized for about 4/8/16 pair evaluations per
+// thread per staging move.
+constexpr int kTeamScheds[3] = {1004, 1008, 1016};
+
+// Team warps per walker (1, 2, 4 or 8) and their packing into 8-warp CTAs:
+// walkers sorted by team size, then by cost N^2 M; CTAs issued by decreasing
+// cost so the longest chains start first.
+// Pack walkers with tw[w] warps each into 8-warp CTAs (first fit, walkers
+// sorted by team size then cost); CTAs are issued by decreasing cost.
+cudaError_t pack_teams(pgb_walkers* h, int k, const std::vector<int>& tw, bool with_buffers = false) {
+    std::vector<int> idx(h->W);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+        if (tw[a] != tw[b]) return tw[a] > tw[b];
+        return (double)h->N[a] * h->N[a] * h->M[a] > (double)h->N[b] * h->N[b] * h->M[b];
+    });
+    std::vector<std::vector<int4>> ctas;
+    std::vector<int> used;
+    std::vector<double> cost;
+    for (int w : idx) {
+        int c = -1;
+        for (int q = (int)ctas.size() - 1; q >= 0 && q >= (int)ctas.size() - 4; --q)
+            if (used[q] + tw[w] <= 8) { c = q; break; }
+        if (c < 0) { ctas.emplace_back(); used.push_back(0); cost.push_back(0.0); c = (int)ctas.size() - 1; }
+        ctas[c].push_back(make_int4(w, used[c], tw[w], 1));
+        cost[c] = std::max(cost[c], (double)h->N[w] * h->N[w] * h->M[w] / tw[w]);
+        used[c] += tw[w];
+    }
+    std::vector<int> order(ctas.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<int4> flat(ctas.size() * 8, make_int4(-1, 0, 0, 0));
+    size_t max_smem = 0;
+    for (size_t c = 0; c < order.size(); ++c) {
+        size_t off = 0;     // float4 units
+        for (size_t e = 0; e < ctas[order[c]].size(); ++e) {
+            int4 t = ctas[order[c]][e];
+            if (with_buffers) {
+                t.w = (int)off + 1;
+                off += (size_t)h->mbar[t.x] * h->N[t.x];
+            }
+            flat[c * 8 + e] = t;
+        }
+        max_smem = std::max(max_smem, off * sizeof(float4));
+    }
+    h->team_smem[k] = max_smem;
+    cudaError_t e = cudaMalloc(&h->d_teams[k], flat.size() * sizeof(int4));
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(h->d_teams[k], flat.data(), flat.size() * sizeof(int4), cudaMemcpyHostToDevice);
+    h->team_ctas[k] = (int)ctas.size();
+    return e;
+}
+
+// Team warps per walker (1, 2, 4 or 8) for the packed-team schedule, sized
+// for about ppt pair evaluations per thread per staging move.
+cudaError_t build_teams(pgb_walkers* h, int k) {
+    if (h->d_teams[k]) return cudaSuccess;
+    const int ppt = kTeamScheds[k] % 1000;
+    std::vector<int> tw(h->W);
+    for (int w = 0; w < h->W; ++w) {
+        double pairs = (double)h->mbar[w] / 2.0 * h->N[w] * 2.0;     // old + new
+        int need = (int)std::ceil(pairs / (32.0 * ppt));
+        int t = 1;
+        while (t < need && t < 8) t <<= 1;
+        tw[w] = t;
+    }
+    return pack_teams(h, k, tw);
+}
+
+// TMA-staged teams: same sizing as build_teams, plus a shared-memory buffer
+// of Mbar rows per walker.
+cudaError_t build_tma_teams(pgb_walkers* h, int ppt) {
+    const int k = 4 + ((ppt == 4) ? 0 : (ppt == 16) ? 2 : 1);
+    if (h->d_teams[k]) return cudaSuccess;
+    std::vector<int> tw(h->W);
+    for (int w = 0; w < h->W; ++w) {
+        double pairs = (double)h->mbar[w] / 2.0 * h->N[w] * 2.0;
+        int need = (int)std::ceil(pairs / (32.0 * ppt));
+        int t = 1;
+        while (t < need && t < 8) t <<= 1;
+        tw[w] = t;
+    }
+    return pack_teams(h, k, tw, true);
+}
+
+// One warp per imaginary-time window: P = min(8, M / (Mbar + 1)) windows.
+cudaError_t build_windows(pgb_walkers* h) {
+    if (h->d_teams[3]) return cudaSuccess;
+    std::vector<int> tw(h->W);
+    for (int w = 0; w < h->W; ++w) tw[w] = std::max(1, std::min(8, h->M[w] / (h->mbar[w] + 1)));
+    return pack_teams(h, 3, tw);
+}
+
+cudaError_t launch_run(pgb_walkers* h, int sched, int sweeps, int measure) {
     AzizF af = make_aziz_f(h->az);
-    switch (tpw) {
+    if (sched >= 4000) {
+        const int ppt = sched % 1000;
+        const int k = 4 + ((ppt == 4) ? 0 : (ppt == 16) ? 2 : 1);
+        cudaError_t e = build_tma_teams(h, ppt);
+        if (e != cudaSuccess) return e;
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_walkers_tma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            attr = true;
+        }
+        if (h->team_smem[k] > 160 * 1024) return cudaErrorInvalidValue;
+        k_walkers_tma<2><<<h->team_ctas[k], kTeamCta, h->team_smem[k], h->stream>>>(h->d_meta,
+            h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
+            h->lambda, (float)h->p_com, h->var_updates, h->seed);
+        h->launches += 1;
+        return cudaGetLastError();
+    }
+    if (sched >= 3000) {
+        cudaError_t e = build_windows(h);
+        if (e != cudaSuccess) return e;
+        if (sched == 3002)
+            k_walkers_windows<2><<<h->team_ctas[3], kTeamCta, 0, h->stream>>>(h->d_meta, h->d_teams[3],
+                h->d_pos, h->d_acc, h->d_ctr, sweeps, measure, af, h->tau, h->lambda,
+                (float)h->p_com, h->var_updates, h->seed);
+        else
+            k_walkers_windows<3><<<h->team_ctas[3], kTeamCta, 0, h->stream>>>(h->d_meta, h->d_teams[3],
+                h->d_pos, h->d_acc, h->d_ctr, sweeps, measure, af, h->tau, h->lambda,
+                (float)h->p_com, h->var_updates, h->seed);
+        h->launches += 1;
+        return cudaGetLastError();
+    }
+    if (sched > 1000) {
+        // 1xxx: 3 CTAs per SM (80 registers), 2xxx: 2 CTAs per SM (128 registers)
+        const int ppt = sched % 1000;
+        int k = (ppt == 4) ? 0 : (ppt == 16) ? 2 : 1;
+        cudaError_t e = build_teams(h, k);
+        if (e != cudaSuccess) return e;
+        if (sched >= 2000)
+            k_walkers_team<2><<<h->team_ctas[k], kTeamCta, 0, h->stream>>>(h->d_meta, h->d_teams[k],
+                h->d_pos, h->d_acc, h->d_ctr, sweeps, measure, af, h->tau, h->lambda,
+                (float)h->p_com, h->var_updates, h->seed);
+        else
+            k_walkers_team<3><<<h->team_ctas[k], kTeamCta, 0, h->stream>>>(h->d_meta, h->d_teams[k],
+                h->d_pos, h->d_acc, h->d_ctr, sweeps, measure, af, h->tau, h->lambda,
+                (float)h->p_com, h->var_updates, h->seed);
+        h->launches += 1;
+        return cudaGetLastError();
+    }
+    switch (sched) {
     case 64:
         k_walkers_run<64><<<h->W, 64, 0, h->stream>>>(h->d_meta, h->d_order, h->d_pos, h->d_acc, h->d_ctr,
             sweeps, measure, af, h->tau, h->lambda, (float)h->p_com, h->var_updates, h->seed);
@@ -388,17 +1382,26 @@ int autotune(pgb_walkers* h) {
     cudaMemcpyAsync(save_ctr, h->d_ctr, h->W * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream);
     cudaEvent_t a, b;
     cudaEventCreate(&a); cudaEventCreate(&b);
-    const int cand[3] = {64, 128, 256};
-    float best = 1e30f; int best_t = 128;
-    for (int c = 0; c < 3; ++c) {
+    const int cand[8] = {128, 2004, 2008, 2016, 3002, 4004, 4008, 4016};
+    float best = 1e30f; int best_t = 4008;
+    for (int c = 0; c < 8; ++c) {
         cudaMemcpyAsync(h->d_pos, save, pb, cudaMemcpyDeviceToDevice, h->stream);
         cudaMemcpyAsync(h->d_ctr, save_ctr, h->W * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream);
         cudaEventRecord(a, h->stream);
         e = launch_run(h, cand[c], 1, 0);
         cudaEventRecord(b, h->stream);
-        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        if (e != cudaSuccess) {
+            // a schedule that does not fit this workload (e.g. shared memory) is skipped
+            cudaGetLastError();
+            e = cudaEventSynchronize(b);
+            if (e != cudaSuccess) break;
+            continue;
+        }
+        e = cudaEventSynchronize(b);
         if (e != cudaSuccess) break;
         float ms = 0; cudaEventElapsedTime(&ms, a, b);
+        h->tune_sched.push_back(cand[c]);
+        h->tune_ms.push_back(ms);
         if (ms < best) { best = ms; best_t = cand[c]; }
     }
     cudaMemcpyAsync(h->d_pos, save, pb, cudaMemcpyDeviceToDevice, h->stream);
@@ -426,8 +1429,18 @@ int pgb_walkers_create(const pgb_walkers_params* p, pgb_walkers** out) {
     *out = nullptr;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { g_werr = "no CUDA device available"; return PGB_ECUDA; }
-    if (p->threads_per_walker != 0 && p->threads_per_walker != 64 && p->threads_per_walker != 128 &&
-        p->threads_per_walker != 256) { g_werr = "threads_per_walker must be 0, 64, 128 or 256"; return PGB_EINVAL; }
+    {
+        const int t = p->threads_per_walker;
+        const bool team = (t / 1000 == 1 || t / 1000 == 2) && (t % 1000 == 4 || t % 1000 == 8 || t % 1000 == 16);
+        const bool win = (t == 3002 || t == 3003 || t == 4004 || t == 4008 || t == 4016);
+        if (!(t == 0 || t == 64 || t == 128 || t == 256 || team || win)) {
+            g_werr = "threads_per_walker must be 0 (autotune), 64/128/256 (one CTA per walker), "
+                     "1004/1008/1016 / 2004/2008/2016 (packed teams, 4/8/16 pairs per thread, "
+                     "3 or 2 CTAs per SM), 3002/3003 (time windows, 2 or 3 CTAs per SM) or "
+                     "4004/4008/4016 (packed teams with TMA-staged rows)";
+            return PGB_EINVAL;
+        }
+    }
     pgb_walkers* h = new pgb_walkers();
     h->W = p->num_walkers;
     h->tau = p->tau; h->lambda = p->lambda; h->p_com = p->p_com; h->seed = p->seed;
@@ -474,6 +1487,8 @@ int pgb_walkers_create(const pgb_walkers_params* p, pgb_walkers** out) {
         if ((e = cudaMalloc(&h->d_acc, h->W * sizeof(WalkerAcc))) != cudaSuccess) break;
         if ((e = cudaMalloc(&h->d_ctr, h->W * sizeof(unsigned long long))) != cudaSuccess) break;
         if ((e = cudaMalloc(&h->d_en, h->W * sizeof(double))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&h->d_err, h->W * sizeof(int))) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(h->d_err, 0, h->W * sizeof(int), h->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(h->d_meta, h->meta.data(), h->W * sizeof(WalkerMeta), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(h->d_order, h->order.data(), h->W * sizeof(int), cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) break;
         if ((e = cudaMemsetAsync(h->d_acc, 0, h->W * sizeof(WalkerAcc), h->stream)) != cudaSuccess) break;
@@ -496,6 +1511,8 @@ int pgb_walkers_destroy(pgb_walkers* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->d_meta); cudaFree(h->d_order); cudaFree(h->d_pos); cudaFree(h->d_acc);
     cudaFree(h->d_ctr); cudaFree(h->d_en); cudaFree(h->d_stage);
+    for (int k = 0; k < 7; ++k) cudaFree(h->d_teams[k]);
+    cudaFree(h->d_err);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return PGB_OK;
@@ -504,6 +1521,16 @@ int pgb_walkers_destroy(pgb_walkers* h) {
 void* pgb_walkers_stream(pgb_walkers* h) { return h ? (void*)h->stream : nullptr; }
 long long pgb_walkers_launch_count(pgb_walkers* h) { return h ? h->launches : 0; }
 int pgb_walkers_threads(pgb_walkers* h) { return h ? h->tpw : 0; }
+
+int pgb_walkers_tuning(pgb_walkers* h, int* scheds, float* ms, int cap) {
+    if (!h) return 0;
+    int n = (int)h->tune_sched.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        if (scheds) scheds[i] = h->tune_sched[i];
+        if (ms) ms[i] = h->tune_ms[i];
+    }
+    return n;
+}
 
 int pgb_walkers_init(pgb_walkers* h) {
     if (!h) return PGB_EINVAL;
@@ -570,7 +1597,7 @@ int pgb_walkers_set_all_positions(pgb_walkers* h, const double* pos) {
 
 int pgb_walkers_run_async(pgb_walkers* h, int sweeps, int measure) {
     if (!h || sweeps < 0 || measure < 0) return PGB_EINVAL;
-    if (h->tpw == 0) h->tpw = 128;
+    if (h->tpw == 0) h->tpw = 4008;
     // bounded launches: at most 64 sweeps per kernel
     int left = sweeps;
     while (left > 0) {
@@ -586,6 +1613,12 @@ int pgb_walkers_sync(pgb_walkers* h) {
     if (!h) return PGB_EINVAL;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return h->cfail(e, "walkers sync");
+    std::vector<int> flags(h->W);
+    e = cudaMemcpy(flags.data(), h->d_err, h->W * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cfail(e, "walkers error words");
+    for (int w = 0; w < h->W; ++w)
+        if (flags[w]) return h->fail(PGB_ETIMEOUT, "walker " + std::to_string(w) +
+                                     ": a staged copy did not complete within the wait limit");
     return PGB_OK;
 }
 
