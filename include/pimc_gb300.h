@@ -230,7 +230,11 @@ long long pgb_walkers_launch_count(pgb_walkers* w);
  * per thread per move, 3 (2) CTAs per SM; 3003 (3002) = one warp per
  * imaginary-time window, up to min(8, M/(Mbar+1)) concurrent staging moves
  * per walker on disjoint windows, 3 (2) CTAs per SM; 4004/4008/4016 = packed
- * teams whose slab rows are staged in shared memory by bulk copies */
+ * teams whose slab rows are staged in shared memory by bulk copies;
+ * 5008/5016 (6008/6016) = the same with the next move's rows prefetched into
+ * a second buffer, 256 (512)-thread CTAs, teams of up to 8 (16) warps;
+ * 5000 (6000) = the same with team warps proportional to each walker's cost
+ * N^2 M, the costliest walker getting all 8 (16) */
 int pgb_walkers_threads(pgb_walkers* w);
 /* the autotuner's record: schedules tried and one-sweep time (ms) of each;
  * returns the number of candidates, fills at most cap */

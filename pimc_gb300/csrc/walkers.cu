@@ -1092,6 +1092,323 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined TMA schedule.  Teams of up to CTA/32 warps; each team owns two
+// shared-memory buffers of Mbar slab rows.  Move descriptions come from the
+// counter-based generator, so the rows of the next staging move are known
+// before the current move is decided: they are copied into the other buffer
+// while the current move runs.  If the current move is accepted and shares
+// slices with the prefetched rows, the team's own write-back also patches the
+// prefetched copy (after its copy has landed), so every move reads the
+// configuration its predecessor left.  Centre-of-mass moves and energy
+// samples stream the slab through the two buffers in Mbar-row chunks.
+// ---------------------------------------------------------------------------
+struct MoveDesc {
+    int com, i, s0, len, nmove, rs;
+    float sx, sy, sz;
+};
+
+__device__ __forceinline__ MoveDesc draw_move(uint64_t seed, int w, int u, uint32_t g0, uint32_t g1,
+                                              const WalkerMeta& m, float p_com, int var_updates) {
+    MoveDesc d;
+    const uint4 r0 = wrand(seed, w, (uint32_t)u, g0, g1, 0u);
+    d.com = u01f(r0.x) < p_com;
+    d.i = (int)(((unsigned long long)r0.z * (unsigned)m.N) >> 32);
+    d.s0 = (int)(((unsigned long long)r0.y * (unsigned)m.M) >> 32);
+    d.len = var_updates ? 2 + (int)(((unsigned long long)r0.w * (unsigned)(m.mbar - 1)) >> 32) : m.mbar;
+    d.nmove = d.len - 1;
+    d.rs = d.s0 + 1; if (d.rs >= m.M) d.rs -= m.M;
+    d.sx = m.com_delta * (u01f(r0.y) - 0.5f);
+    d.sy = m.com_delta * (u01f(r0.w) - 0.5f);
+    d.sz = 0.f;
+    return d;
+}
+
+template <int CTA, int MINB>
+__global__ void __launch_bounds__(CTA, MINB)
+k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
+               float4* __restrict__ pos, WalkerAcc* __restrict__ accs,
+               unsigned long long* __restrict__ ctr, int* __restrict__ err, int sweeps, int measure,
+               AzizF az, double tau, double lambda, float p_com, int var_updates, uint64_t seed) {
+    constexpr int NW = CTA / 32;
+    extern __shared__ float4 dyn[];
+    __shared__ float4 s_new[NW][kMaxStage];
+    __shared__ double s_red[NW][NW];
+    __shared__ int s_acc[NW];
+    __shared__ int s_fail[NW];
+    __shared__ __align__(8) uint64_t s_bar[NW][2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int4 tm = make_int4(-1, 0, 0, 0);
+    for (int k = 0; k < NW; ++k) {
+        int4 t = teams[blockIdx.x * NW + k];
+        if (t.w && warp >= t.y && warp < t.y + t.z) tm = t;
+    }
+    if (tm.x < 0) return;
+    const int w = tm.x, slot = tm.y, nw = tm.z, T = nw * 32;
+    const int tt = threadIdx.x - slot * 32, wi = warp - slot;
+    const WalkerMeta m = meta[w];
+    float4* P = pos + m.off;
+    const int N = m.N, M = m.M, C = m.mbar;
+    float4* const B0 = dyn + (tm.w - 1);
+    float4* const B1 = B0 + (size_t)C * N;
+    uint64_t* const bar0 = &s_bar[slot][0];
+    uint64_t* const bar1 = &s_bar[slot][1];
+    auto Bsel = [&](int x) { return x ? B1 : B0; };
+    auto barsel = [&](int x) { return x ? bar1 : bar0; };
+    double* red = s_red[slot];
+    float4* sn = s_new[slot];
+    int* fail = &s_fail[slot];
+    if (tt == 0) { mbar_init(bar0, 1); mbar_init(bar1, 1); *fail = 0; }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    team_sync(slot, T);
+    uint32_t ph0 = 0u, ph1 = 0u;
+    auto phsel = [&](int x) { return x ? ph1 : ph0; };
+    auto phflip = [&](int x) { if (x) ph1 ^= 1u; else ph0 ^= 1u; };
+    const unsigned long long sweep0 = ctr[w];
+    double esum = 0.0, esumsq = 0.0;
+    long long nsamp = 0, nbu = 0, att0 = 0, att1 = 0, acc0 = 0, acc1 = 0;
+    const int G = (T >= N) ? T / N : 1;
+    const int j0 = (T >= N) ? ((tt < G * N) ? tt % N : N) : tt;
+    const int kb0 = (T >= N) ? tt / N : 0;
+    const int jstep = (T >= N) ? N : T;
+    int cur = 0;
+
+    for (int sw = 0; sw < sweeps; ++sw) {
+        const unsigned long long gs = sweep0 + sw;
+        const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
+        bool have = false;                        // rows of the current move already in Bsel(cur)
+        MoveDesc D = draw_move(seed, w, 0, g0, g1, m, p_com, var_updates);
+        for (int u = 0; u < m.num_updates; ++u) {
+            const bool last = (u + 1 == m.num_updates);
+            MoveDesc Dn = D;
+            if (!last) Dn = draw_move(seed, w, u + 1, g0, g1, m, p_com, var_updates);
+            if (!D.com) {
+                const bool pre = !last && !Dn.com;
+                if (tt == 0) {
+                    if (!have) issue_rows(Bsel(cur), P, N, M, D.rs, D.nmove, barsel(cur));
+                    if (pre) issue_rows(Bsel(cur ^ 1), P, N, M, Dn.rs, Dn.nmove, barsel(cur ^ 1));
+                }
+                const int i = D.i, s0 = D.s0, len = D.len, nmove = D.nmove;
+                if (wi == 0) {
+                    int se = s0 + len; if (se >= M) se -= M;
+                    const float4 x0 = P[(size_t)s0 * N + i], xe = P[(size_t)se * N + i];
+                    float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
+                    if (lane + 1 <= len) {
+                        const uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)(lane + 1));
+                        const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+                        a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
+                    }
+                    if (lane + 33 <= len) {
+                        const uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)(lane + 33));
+                        const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+                        a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
+                    }
+                    const float W1x = warp_scan_incl(a1x, lane), W1y = warp_scan_incl(a1y, lane),
+                                W1z = warp_scan_incl(a1z, lane);
+                    const float W2x = warp_scan_incl(a2x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
+                    const float W2y = warp_scan_incl(a2y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
+                    const float W2z = warp_scan_incl(a2z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
+                    const int src = (len <= 32) ? len - 1 : len - 33;
+                    const float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
+                    const float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
+                    const float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
+                    const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
+                    const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
+                    const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
+                    const float il = 1.0f / (float)len;
+                    #pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = lane + 32 * h;
+                        if (k < nmove) {
+                            const float f = (float)(k + 1) * il;
+                            const float Wx = h ? W2x : W1x, Wy = h ? W2y : W1y, Wz = h ? W2z : W1z;
+                            sn[k] = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
+                                                put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
+                                                put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
+                        }
+                    }
+                }
+                if (!team_wait(barsel(cur), phsel(cur), slot, T, fail, err + w)) return;
+                phflip(cur);
+                const float4* buf = Bsel(cur);
+                KahanF acc;
+                for (int j = j0; j < N; j += jstep) {
+                    if (j == i) continue;
+                    #pragma unroll 4
+                    for (int k = kb0; k < nmove; k += G) {
+                        const float4 pj = buf[k * N + j];
+                        const float4 a = sn[k], b = buf[k * N + i];
+                        const float ax = min_image32(a.x - pj.x, m.L, m.Linv);
+                        const float ay = min_image32(a.y - pj.y, m.L, m.Linv);
+                        const float az_ = min_image32(a.z - pj.z, m.L, m.Linv);
+                        const float bx = min_image32(b.x - pj.x, m.L, m.Linv);
+                        const float by = min_image32(b.y - pj.y, m.L, m.Linv);
+                        const float bz = min_image32(b.z - pj.z, m.L, m.Linv);
+                        acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                                aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+                    }
+                }
+                const double part = warp_sum(acc.value());
+                if (lane == 0) red[wi] = part;
+                team_sync(slot, T);
+                if (tt == 0) {
+                    double dV = 0.0;
+                    for (int q = 0; q < nw; ++q) dV += red[q];
+                    const uint4 ra = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFFu);
+                    s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
+                }
+                team_sync(slot, T);
+                const int ok = s_acc[slot];
+                if (wi == 0 && ok) {
+                    for (int k = lane; k < nmove; k += 32) {
+                        int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                        P[(size_t)sl * N + i] = sn[k];
+                    }
+                    fence_proxy_async_global();
+                    if (pre) {
+                        // the prefetched rows must have landed before they are patched
+                        long long n = 0;
+                        bool landed = true;
+                        while (!mbar_try_wait(barsel(cur ^ 1), phsel(cur ^ 1)))
+                            if (++n > kWaitLimit) { landed = false; break; }
+                        if (!landed) { atomicExch(fail, 1); atomicExch(err + w, 1); }
+                        else {
+                            float4* nb = Bsel(cur ^ 1);
+                            for (int k = lane; k < nmove; k += 32) {
+                                int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                                int q = sl - Dn.rs; if (q < 0) q += M;
+                                if (q < Dn.nmove) nb[q * N + i] = sn[k];
+                            }
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        }
+                    }
+                }
+                if (wi == 0) __syncwarp();
+                att1 += 1; acc1 += ok; nbu += nmove;
+                if (pre) { cur ^= 1; have = true; } else { have = false; }
+            } else {
+                const int i = D.i;
+                const float sx = D.sx, sy = D.sy;
+                const uint4 r1 = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFEu);
+                const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
+                KahanF acc;
+                int b = cur;
+                if (tt == 0) issue_rows(Bsel(b), P, N, M, 0, min(C, M), barsel(b));
+                for (int c0 = 0; c0 < M; c0 += C) {
+                    const int nr = min(C, M - c0), nb0 = c0 + C;
+                    if (nb0 < M && tt == 0) issue_rows(Bsel(b ^ 1), P, N, M, nb0, min(C, M - nb0), barsel(b ^ 1));
+                    if (!team_wait(barsel(b), phsel(b), slot, T, fail, err + w)) return;
+                    phflip(b);
+                    const float4* buf = Bsel(b);
+                    for (int j = j0; j < N; j += jstep) {
+                        if (j == i) continue;
+                        #pragma unroll 4
+                        for (int t = kb0; t < nr; t += G) {
+                            const float4 pi = buf[t * N + i], pj = buf[t * N + j];
+                            const float bx = min_image32(pi.x - pj.x, m.L, m.Linv);
+                            const float by = min_image32(pi.y - pj.y, m.L, m.Linv);
+                            const float bz = min_image32(pi.z - pj.z, m.L, m.Linv);
+                            const float ax = min_image32(bx + sx, m.L, m.Linv);
+                            const float ay = min_image32(by + sy, m.L, m.Linv);
+                            const float az_ = min_image32(bz + sz, m.L, m.Linv);
+                            acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                                    aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+                        }
+                    }
+                    team_sync(slot, T);
+                    b ^= 1;
+                }
+                cur = b;
+                const double part = warp_sum(acc.value());
+                if (lane == 0) red[wi] = part;
+                team_sync(slot, T);
+                if (tt == 0) {
+                    double dV = 0.0;
+                    for (int q = 0; q < nw; ++q) dV += red[q];
+                    s_acc[slot] = metropolis(dV, tau, r1.y, r1.z) ? 1 : 0;
+                }
+                team_sync(slot, T);
+                const int ok = s_acc[slot];
+                if (ok) {
+                    for (int t2 = tt; t2 < M; t2 += T) {
+                        float4 pi = P[(size_t)t2 * N + i];
+                        pi.x = put_inside(pi.x + sx, m.L, m.Linv);
+                        pi.y = put_inside(pi.y + sy, m.L, m.Linv);
+                        pi.z = put_inside(pi.z + sz, m.L, m.Linv);
+                        P[(size_t)t2 * N + i] = pi;
+                    }
+                    fence_proxy_async_global();
+                }
+                team_sync(slot, T);
+                att0 += 1; acc0 += ok; nbu += M;
+                have = false;
+            }
+            D = Dn;
+        }
+        if (measure > 0 && ((gs + 1) % (unsigned long long)measure) == 0) {
+            KahanF pot, kin;
+            const int half = (N - 1) / 2;
+            const bool even = (N % 2) == 0;
+            int b = cur;
+            if (tt == 0) issue_rows(Bsel(b), P, N, M, 0, min(C, M), barsel(b));
+            for (int c0 = 0; c0 < M; c0 += C) {
+                const int nr = min(C, M - c0), nb0 = c0 + C;
+                if (nb0 < M && tt == 0) issue_rows(Bsel(b ^ 1), P, N, M, nb0, min(C, M - nb0), barsel(b ^ 1));
+                if (!team_wait(barsel(b), phsel(b), slot, T, fail, err + w)) return;
+                phflip(b);
+                const float4* buf = Bsel(b);
+                for (int idx = tt; idx < nr * N; idx += T) {
+                    const int t = idx / N, ii = idx - t * N;
+                    const float4 ri = buf[t * N + ii];
+                    const int cnt = half + ((even && ii < N / 2) ? 1 : 0);
+                    for (int d = 1; d <= cnt; ++d) {
+                        int jj = ii + d; if (jj >= N) jj -= N;
+                        const float4 rj = buf[t * N + jj];
+                        const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
+                        const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
+                        const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
+                        pot.add(aziz_v32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+                    }
+                }
+                team_sync(slot, T);
+                b ^= 1;
+            }
+            cur = b;
+            for (int idx = tt; idx < M * N; idx += T) {
+                const int t = idx / N, ii = idx - t * N;
+                const int tn = (t + 1 == M) ? 0 : t + 1;
+                const float4 ri = P[(size_t)t * N + ii], rn = P[(size_t)tn * N + ii];
+                const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
+                const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
+                const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
+                kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+            }
+            const double pv = warp_sum(pot.value()), kv = warp_sum(kin.value());
+            if (lane == 0) red[wi] = pv;
+            team_sync(slot, T);
+            double V = 0.0;
+            if (tt == 0) for (int q = 0; q < nw; ++q) V += red[q];
+            team_sync(slot, T);
+            if (lane == 0) red[wi] = kv;
+            team_sync(slot, T);
+            if (tt == 0) {
+                double K2 = 0.0;
+                for (int q = 0; q < nw; ++q) K2 += red[q];
+                const double totK = 1.5 * N / tau - K2 * ((0.25 / (lambda * tau)) / (tau * M));
+                const double e = (totK + V / M + m.tailV) / N;
+                esum += e; esumsq += e * e; nsamp += 1;
+            }
+            team_sync(slot, T);
+        }
+    }
+    if (tt == 0) {
+        WalkerAcc& A = accs[w];
+        A.esum += esum; A.esumsq += esumsq; A.samples += nsamp; A.bead_updates += nbu;
+        A.att[0] += att0; A.att[1] += att1; A.acc[0] += acc0; A.acc[1] += acc1;
+        ctr[w] = sweep0 + sweeps;
+    }
+}
+
 __global__ void k_walkers_init(const WalkerMeta* __restrict__ meta, float4* __restrict__ pos,
                                uint64_t seed) {
     const int w = blockIdx.x;
@@ -1187,9 +1504,10 @@ struct pgb_walkers {
     double* d_stage = nullptr;
     int* d_err = nullptr;                 // per-walker error word (bounded waits)
     // packed-team schedules, one per pairs-per-thread target
-    int4* d_teams[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    int team_ctas[7] = {0, 0, 0, 0, 0, 0, 0};   // 3 team targets, windows, 3 TMA targets
-    size_t team_smem[7] = {0, 0, 0, 0, 0, 0, 0};
+    // 0-2 team targets, 3 windows, 4-6 TMA targets, 7-10 pipelined (256/8, 256/16, 512/8, 512/16)
+    int4* d_teams[13] = {nullptr};
+    int team_ctas[13] = {0};
+    size_t team_smem[13] = {0};
     // autotuner record: schedule and one-sweep time of each candidate
     std::vector<int> tune_sched;
     std::vector<float> tune_ms;
@@ -1216,7 +1534,8 @@ constexpr int kTeamScheds[3] = {1004, 1008, 1016};
 // cost so the longest chains start first.
 // Pack walkers with tw[w] warps each into 8-warp CTAs (first fit, walkers
 // sorted by team size then cost); CTAs are issued by decreasing cost.
-cudaError_t pack_teams(pgb_walkers* h, int k, const std::vector<int>& tw, bool with_buffers = false) {
+cudaError_t pack_teams(pgb_walkers* h, int k, const std::vector<int>& tw, bool with_buffers = false,
+                       int cta_warps = 8, int nbuf = 1, size_t smem_budget = 160 * 1024) {
     std::vector<int> idx(h->W);
     std::iota(idx.begin(), idx.end(), 0);
     std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
@@ -1226,19 +1545,26 @@ cudaError_t pack_teams(pgb_walkers* h, int k, const std::vector<int>& tw, bool w
     std::vector<std::vector<int4>> ctas;
     std::vector<int> used;
     std::vector<double> cost;
+    std::vector<size_t> bytes;
     for (int w : idx) {
+        const size_t need = with_buffers ? (size_t)nbuf * h->mbar[w] * h->N[w] * sizeof(float4) : 0;
+        if (need > smem_budget) return cudaErrorInvalidValue;
         int c = -1;
         for (int q = (int)ctas.size() - 1; q >= 0 && q >= (int)ctas.size() - 4; --q)
-            if (used[q] + tw[w] <= 8) { c = q; break; }
-        if (c < 0) { ctas.emplace_back(); used.push_back(0); cost.push_back(0.0); c = (int)ctas.size() - 1; }
+            if (used[q] + tw[w] <= cta_warps && bytes[q] + need <= smem_budget) { c = q; break; }
+        if (c < 0) {
+            ctas.emplace_back(); used.push_back(0); cost.push_back(0.0); bytes.push_back(0);
+            c = (int)ctas.size() - 1;
+        }
         ctas[c].push_back(make_int4(w, used[c], tw[w], 1));
         cost[c] = std::max(cost[c], (double)h->N[w] * h->N[w] * h->M[w] / tw[w]);
         used[c] += tw[w];
+        bytes[c] += need;
     }
     std::vector<int> order(ctas.size());
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-    std::vector<int4> flat(ctas.size() * 8, make_int4(-1, 0, 0, 0));
+    std::vector<int4> flat(ctas.size() * cta_warps, make_int4(-1, 0, 0, 0));
     size_t max_smem = 0;
     for (size_t c = 0; c < order.size(); ++c) {
         size_t off = 0;     // float4 units
@@ -1246,9 +1572,9 @@ cudaError_t pack_teams(pgb_walkers* h, int k, const std::vector<int>& tw, bool w
             int4 t = ctas[order[c]][e];
             if (with_buffers) {
                 t.w = (int)off + 1;
-                off += (size_t)h->mbar[t.x] * h->N[t.x];
+                off += (size_t)nbuf * h->mbar[t.x] * h->N[t.x];
             }
-            flat[c * 8 + e] = t;
+            flat[c * cta_warps + e] = t;
         }
         max_smem = std::max(max_smem, off * sizeof(float4));
     }
@@ -1292,6 +1618,31 @@ cudaError_t build_tma_teams(pgb_walkers* h, int ppt) {
     return pack_teams(h, k, tw, true);
 }
 
+// Pipelined TMA teams: cta = 256 (teams of <= 8 warps, 2 CTAs per SM) or
+// 512 (<= 16 warps, 1 CTA per SM); two buffers of Mbar rows per walker.
+cudaError_t build_pipe_teams(pgb_walkers* h, int k, int cta, int ppt) {
+    if (h->d_teams[k]) return cudaSuccess;
+    const int cap = cta / 32;
+    std::vector<int> tw(h->W);
+    double wmax = 0.0;
+    for (int w = 0; w < h->W; ++w) wmax = std::max(wmax, (double)h->N[w] * h->N[w] * h->M[w]);
+    for (int w = 0; w < h->W; ++w) {
+        int need;
+        if (ppt == 0) {
+            // balanced: warps in proportion to the walker's cost N^2 M, so every
+            // chain needs about the same time as the largest one with `cap` warps
+            need = (int)std::ceil(cap * (double)h->N[w] * h->N[w] * h->M[w] / wmax);
+        } else {
+            double pairs = (double)h->mbar[w] / 2.0 * h->N[w] * 2.0;
+            need = (int)std::ceil(pairs / (32.0 * ppt));
+        }
+        int t = 1;
+        while (t < need && t < cap) t <<= 1;
+        tw[w] = t;
+    }
+    return pack_teams(h, k, tw, true, cap, 2, cta == 512 ? 200 * 1024 : 100 * 1024);
+}
+
 // One warp per imaginary-time window: P = min(8, M / (Mbar + 1)) windows.
 cudaError_t build_windows(pgb_walkers* h) {
     if (h->d_teams[3]) return cudaSuccess;
@@ -1302,6 +1653,29 @@ cudaError_t build_windows(pgb_walkers* h) {
 
 cudaError_t launch_run(pgb_walkers* h, int sched, int sweeps, int measure) {
     AzizF af = make_aziz_f(h->az);
+    if (sched >= 5000) {
+        const int ppt = sched % 1000;
+        const int cta = (sched >= 6000) ? 512 : 256;
+        const int k = (ppt == 0) ? (cta == 512 ? 12 : 11) : 7 + (cta == 512 ? 2 : 0) + (ppt == 16 ? 1 : 0);
+        cudaError_t e = build_pipe_teams(h, k, cta, ppt);
+        if (e != cudaSuccess) return e;
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_walkers_pipe<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+            cudaFuncSetAttribute(k_walkers_pipe<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            attr = true;
+        }
+        if (cta == 512)
+            k_walkers_pipe<512, 1><<<h->team_ctas[k], 512, h->team_smem[k], h->stream>>>(h->d_meta,
+                h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
+                h->lambda, (float)h->p_com, h->var_updates, h->seed);
+        else
+            k_walkers_pipe<256, 2><<<h->team_ctas[k], 256, h->team_smem[k], h->stream>>>(h->d_meta,
+                h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
+                h->lambda, (float)h->p_com, h->var_updates, h->seed);
+        h->launches += 1;
+        return cudaGetLastError();
+    }
     if (sched >= 4000) {
         const int ppt = sched % 1000;
         const int k = 4 + ((ppt == 4) ? 0 : (ppt == 16) ? 2 : 1);
@@ -1382,9 +1756,9 @@ int autotune(pgb_walkers* h) {
     cudaMemcpyAsync(save_ctr, h->d_ctr, h->W * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream);
     cudaEvent_t a, b;
     cudaEventCreate(&a); cudaEventCreate(&b);
-    const int cand[8] = {128, 2004, 2008, 2016, 3002, 4004, 4008, 4016};
-    float best = 1e30f; int best_t = 4008;
-    for (int c = 0; c < 8; ++c) {
+    const int cand[9] = {2008, 4008, 5000, 5008, 5016, 6000, 6008, 6016, 3002};
+    float best = 1e30f; int best_t = 6000;
+    for (int c = 0; c < 9; ++c) {
         cudaMemcpyAsync(h->d_pos, save, pb, cudaMemcpyDeviceToDevice, h->stream);
         cudaMemcpyAsync(h->d_ctr, save_ctr, h->W * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream);
         cudaEventRecord(a, h->stream);
@@ -1432,12 +1806,14 @@ int pgb_walkers_create(const pgb_walkers_params* p, pgb_walkers** out) {
     {
         const int t = p->threads_per_walker;
         const bool team = (t / 1000 == 1 || t / 1000 == 2) && (t % 1000 == 4 || t % 1000 == 8 || t % 1000 == 16);
-        const bool win = (t == 3002 || t == 3003 || t == 4004 || t == 4008 || t == 4016);
+        const bool win = (t == 3002 || t == 3003 || t == 4004 || t == 4008 || t == 4016 ||
+                          t == 5000 || t == 5008 || t == 5016 || t == 6000 || t == 6008 || t == 6016);
         if (!(t == 0 || t == 64 || t == 128 || t == 256 || team || win)) {
             g_werr = "threads_per_walker must be 0 (autotune), 64/128/256 (one CTA per walker), "
                      "1004/1008/1016 / 2004/2008/2016 (packed teams, 4/8/16 pairs per thread, "
                      "3 or 2 CTAs per SM), 3002/3003 (time windows, 2 or 3 CTAs per SM) or "
-                     "4004/4008/4016 (packed teams with TMA-staged rows)";
+                     "4004/4008/4016 (packed teams with TMA-staged rows) or 5000/5008/5016/6000/6008/"
+                     "6016 (pipelined TMA teams in 256/512-thread CTAs; x000 = cost-balanced teams)";
             return PGB_EINVAL;
         }
     }
@@ -1511,7 +1887,7 @@ int pgb_walkers_destroy(pgb_walkers* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->d_meta); cudaFree(h->d_order); cudaFree(h->d_pos); cudaFree(h->d_acc);
     cudaFree(h->d_ctr); cudaFree(h->d_en); cudaFree(h->d_stage);
-    for (int k = 0; k < 7; ++k) cudaFree(h->d_teams[k]);
+    for (int k = 0; k < 13; ++k) cudaFree(h->d_teams[k]);
     cudaFree(h->d_err);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -1597,7 +1973,7 @@ int pgb_walkers_set_all_positions(pgb_walkers* h, const double* pos) {
 
 int pgb_walkers_run_async(pgb_walkers* h, int sweeps, int measure) {
     if (!h || sweeps < 0 || measure < 0) return PGB_EINVAL;
-    if (h->tpw == 0) h->tpw = 4008;
+    if (h->tpw == 0) h->tpw = 6000;
     // bounded launches: at most 64 sweeps per kernel
     int left = sweeps;
     while (left > 0) {

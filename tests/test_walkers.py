@@ -25,9 +25,12 @@ def _walkers(pgb, num, seed, sched, n=8, t=4.0, tau=0.004):
     return W, dict(n=n, m=m, L=L, mbar=mbar, t=1.0 / (m * tau), tau=tau)
 
 
-@pytest.mark.parametrize("sched", [128, 1004, 1008, 1016, 2008, 3002, 3003, 4004, 4008, 4016])
+@pytest.mark.parametrize("sched", [128, 1004, 1008, 1016, 2008, 3002, 3003, 4004, 4008, 4016,
+                                   5000, 5008, 5016, 6000, 6008, 6016])
 def test_schedule_runs_and_is_deterministic(pgb, sched):
-    w = pgb.worldlines.workload_walkers(num=40, seed=2)
+    # N <= 90 keeps two Mbar-row buffers of every walker within the 100 KB
+    # budget of the 256-thread pipelined schedules (5008/5016)
+    w = pgb.worldlines.workload_walkers(num=40, seed=2, nmax=90)
     runs = []
     for _ in range(2):
         W = pgb.Walkers(w["n"], w["m"], w["temperature"], w["side"], w["mbar"], w["tau"], w["lam"],
@@ -44,7 +47,7 @@ def test_schedule_runs_and_is_deterministic(pgb, sched):
     assert np.all(np.abs(runs[0][1]) <= L / 2 + 1e-5)
 
 
-@pytest.mark.parametrize("sched", [128, 3002, 4008])
+@pytest.mark.parametrize("sched", [128, 3002, 5008, 6000])
 def test_matched_energy_vs_oracle_walkers(pgb, oracle_lib, sched):
     num, equil, prod = 256, 60, 200
     W, p = _walkers(pgb, num, 11, sched)
@@ -64,3 +67,33 @@ def test_matched_energy_vs_oracle_walkers(pgb, oracle_lib, sched):
     o_mean, o_err = en.mean(), en.std(ddof=1) / math.sqrt(nw)
     diff = abs(g_mean - o_mean)
     assert diff <= 3.0 * math.hypot(g_err, o_err), (g_mean, g_err, o_mean, o_err)
+
+
+def test_prefetch_pipeline_matches_unpipelined(pgb):
+    """The pipelined schedule (next move's rows prefetched and patched after an
+    accepted move) must leave exactly the configuration the unpipelined TMA
+    schedule leaves: same teams, same draws, same arithmetic."""
+    w = pgb.worldlines.workload_walkers(num=48, seed=9, nmax=90)
+    out = []
+    for sched in (4008, 5008):
+        W = pgb.Walkers(w["n"], w["m"], w["temperature"], w["side"], w["mbar"], w["tau"], w["lam"],
+                        seed=21, threads_per_walker=sched)
+        W.init()
+        W.run(3, measure=1)
+        out.append((W.stats(), [W.positions(k) for k in (0, 5, 17, 40)]))
+    (s1, p1), (s2, p2) = out
+    assert [x["accepted"] for x in s1] == [x["accepted"] for x in s2]
+    assert [x["energy_sum"] for x in s1] == [x["energy_sum"] for x in s2]
+    for a, b in zip(p1, p2):
+        assert np.array_equal(a, b)
+
+
+def test_infeasible_schedule_is_an_error(pgb):
+    """A schedule whose shared-memory buffers cannot hold a walker fails with a
+    message instead of running something else."""
+    w = pgb.worldlines.workload_walkers(num=4, seed=1, nmin=128, nmax=128)
+    W = pgb.Walkers(w["n"], w["m"], w["temperature"], w["side"], w["mbar"], w["tau"], w["lam"],
+                    seed=1, threads_per_walker=5008)
+    W.init()
+    with pytest.raises(pgb.PgbError):
+        W.run(1)
