@@ -49,7 +49,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--walkers", type=int, default=1024)
+    ap.add_argument("--schedule", type=int, default=0,
+                    help="walker schedule code (0: autotune)")
     ap.add_argument("--no-baseline", action="store_true")
+    ap.add_argument("--workload", default="walkers",
+                    choices=["walkers", "serving", "isf", "pair", "plain"])
+    ap.add_argument("--serve-seconds", type=float, default=12.0)
     return ap.parse_args()
 
 
@@ -223,6 +228,277 @@ def plain_form_rate(pgb, n=64, t=2.0, tau=0.004, steps=1):
                 accepted=r["accepted"], attempted=r["attempted"])
 
 
+# ---------------------------------------------------------------------------
+# Serving leg: Poisson job stream (50 jobs/s, seeded), each job N0 log-uniform
+# in [8, 512], T uniform in [0.5, 4] K, mu uniform in [-10, 0] K, sweeps
+# log-uniform in [1e3, 1e5], admitted under a 150 GB HBM budget.  Offered
+# load far exceeds capacity, so the window is bounded and the report states
+# how many jobs reached a first bin / completed (the rest are censored).
+# ---------------------------------------------------------------------------
+def serving_run(pgb, seconds=12.0, rate=50.0, seed=0):
+    rng = np.random.Generator(np.random.Philox(seed))
+    arrivals = []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > 0.6 * seconds:
+            break
+        arrivals.append(t)
+    srv = pgb.Server(150e9, max_active=1024, sweeps_per_round=10, bin_sweeps=100)
+    ids = []
+    for k, ta in enumerate(arrivals):
+        n = int(round(math.exp(rng.uniform(math.log(8), math.log(512)))))
+        T = float(rng.uniform(0.5, 4.0))
+        mu = float(rng.uniform(-10.0, 0.0))
+        sweeps = int(round(math.exp(rng.uniform(math.log(1e3), math.log(1e5)))))
+        ids.append(srv.submit(n=n, temperature=T, sweeps=sweeps, seed=seed * 100000 + k,
+                              arrival=srv.clock() + ta, mu=mu))
+    t0 = time.perf_counter()
+    rounds = 0
+    nbins = 0
+    peak_active = 0
+    while time.perf_counter() - t0 < seconds:
+        a, q = srv.step()
+        rounds += 1
+        peak_active = max(peak_active, a)
+        nbins += len(srv.bins())
+    elapsed = time.perf_counter() - t0
+    bu = srv.bead_updates()
+    infos = [srv.job(j) for j in ids]
+    arrived = [i for i in infos if i["state"] >= 1]
+    ttfb = [i["first_bin"] - i["arrival"] for i in arrived if i["first_bin"] >= 0]
+    done = [i["completed"] - i["arrival"] for i in arrived if i["completed"] >= 0]
+    pct = lambda v, p: float(np.percentile(v, p)) if v else None
+    srv.close()
+    return {"bead_updates_per_s": bu / elapsed, "window_s": round(elapsed, 2), "rounds": rounds,
+            "jobs_arrived": len(arrived), "jobs_admitted": sum(1 for i in arrived if i["admitted"] >= 0),
+            "jobs_with_first_bin": len(ttfb), "jobs_completed": len(done), "bins": nbins,
+            "peak_active": peak_active,
+            "ttfb_p50_s": pct(ttfb, 50), "ttfb_p99_s": pct(ttfb, 99),
+            "completion_p50_s": pct(done, 50), "completion_p99_s": pct(done, 99),
+            "note": "Poisson 50 jobs/s for %.1f s of a %.1f s window; percentiles over jobs that "
+                    "reached the event inside the window (the others are censored); canonical "
+                    "chains (staging + COM), bins of 100 sweeps" % (0.6 * seconds, seconds)}
+
+
+def run_serving(args, pgb):
+    r = serving_run(pgb, seconds=args.serve_seconds)
+    out = {"metric": "serving p99 time-to-first-bin", "value": r["ttfb_p99_s"], "unit": "s",
+           "n_gpus": 1, "steps": r["rounds"], "warmup": 0, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
+           "config": {"workload": "serving: Poisson 50 jobs/s, N0 log-U[8,512], T U[0.5,4], "
+                                  "mu U[-10,0], sweeps log-U[1e3,1e5], 150 GB HBM budget"},
+           "serving": r}
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+# F(q,tau) leg: N=512, M=512 (T = 1/(M tau)), 2048 lattice q with |q| <= 4/A.
+# ---------------------------------------------------------------------------
+def run_isf(args, pgb):
+    import torch
+    from pimc_gb300 import worldlines as wl
+    w = wl.workload_isf()
+    n, m = w["n"], w["m"]
+    L = w["side"]
+    q, _ = wl.isf_qvectors(L, count=2048, seed=0)
+    nq = len(q)
+    cfg = wl.seeded_worldlines(n, m, L, w["lam"], w["tau"], 0)
+    a = pgb.Action(L, m, n, w["tau"], w["lam"], precision=pgb.PGB_MIXED)
+    a.load(cfg)
+    stream = torch.cuda.ExternalStream(pgb._lib.load().pgb_stream(a.h))
+    d_q = torch.from_numpy(q).cuda()
+    d_out = torch.empty((nq, m // 2 + 1), dtype=torch.float64, device="cuda")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    res = {}
+    for mode in (0, 1):
+        for _ in range(args.warmup):
+            a._chk(a.lib.pgb_isf_device_async(a.h, d_q.data_ptr(), nq, mode, d_out.data_ptr()))
+        torch.cuda.synchronize()
+        ms = []
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                a._chk(a.lib.pgb_isf_device_async(a.h, d_q.data_ptr(), nq, mode, d_out.data_ptr()))
+                e1.record(stream)
+            ms.append((e0, e1))
+        torch.cuda.synchronize()
+        res[mode] = sum(x.elapsed_time(y) for x, y in ms) / len(ms)
+    # e2e through the C ABI with host buffers: positions uploaded each step
+    # (the reference copies its bead array to the device every sample)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a.load(cfg)
+        a.isf(q, mode=1)
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    # split-BF16 GEMM FLOPs (3 products): [Qp x 2M x 2M] + [Qp x M x colpad]
+    qp = ((nq + 127) // 128) * 128
+    colpad = ((m // 2 + 1 + 255) // 256) * 256
+    flops = 3 * (2.0 * qp * 2 * m * 2 * m + 2.0 * qp * m * colpad)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"bf16_tflops": 1900.0}
+    out = {"metric": "F(q,tau) configurations/s", "value": 1e3 / res[1], "unit": "configurations/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res[1],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+bf16x3",
+           "data": "synthetic",
+           "config": {"workload": "F(q,tau): N=512, M=512, 2048 lattice q |q|<=4/A, tau in [0,M/2]",
+                      "l2": "flushed between timed steps",
+                      "ms_cuda_core_correlation": res[0], "ms_tensor_core_correlation": res[1],
+                      "phase_evaluations_per_s": nq * m * n / (res[1] / 1e3)},
+           "e2e": {"value": 1.0 / t_e2e, "unit": "configurations/s",
+                   "h2d_bytes_per_step": int(cfg["pos"].nbytes + q.nbytes + cfg["next"].nbytes * 2),
+                   "d2h_bytes_per_step": int(nq * (m // 2 + 1) * 8)},
+           "roofline": {"bound": "tensor", "kernel": "k_gemm_split_bf16 (whole F(q,tau) call timed)",
+                        "achieved": flops / (res[1] / 1e3) / 1e12,
+                        "peak": peaks.get("bf16_tflops", 1900.0), "unit": "TFLOP/s",
+                        "frac": flops / (res[1] / 1e3) / 1e12 / peaks.get("bf16_tflops", 1900.0),
+                        "traffic": None, "note": "achieved counts the GEMM FLOPs over the whole call "
+                        "(rho_q included), so it is a lower bound for the GEMM kernel"}}
+    if not args.no_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        o = pyoracle.Oracle(L, m, n, w["tau"], w["lam"])
+        o.load(cfg)
+        thr = os.cpu_count() or 1
+        sub = q[:max(thr * 4, 32)]
+        t0 = time.perf_counter()
+        o.isf_rhoq(sub, threads=thr)
+        dt = time.perf_counter() - t0
+        per_cfg = dt * nq / len(sub)
+        out["cpu_baseline"] = {"value": 1.0 / per_cfg, "unit": "configurations/s", "cores": thr,
+                               "kind": "port", "sample": "FP64 rho_q form for %d of the %d q-vectors, "
+                               "scaled to all of them" % (len(sub), nq)}
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+# Pair-action leg: N=256, M=250, GSF, rc = L: full-path potential action per
+# configuration and 10^6 single-bead trial displacements, FP64 and mixed.
+# ---------------------------------------------------------------------------
+def run_pair(args, pgb):
+    import torch
+    from pimc_gb300 import worldlines as wl
+    w = wl.workload_pair_action()
+    n, m, L = w["n"], w["m"], w["side"]
+    cfg = wl.seeded_worldlines(n, m, L, w["lam"], w["tau"], 0)
+    v_pairs = m * n * (n - 1) / 2.0
+    g_pairs = (m / 2) * n * (n - 1.0)
+    res = {}
+    ntrial = 1000000
+    rng = np.random.default_rng(0)
+    lam_db = 2 * math.sqrt(math.pi * w["lam"] / w["temperature"])
+    beads = np.stack([rng.integers(0, m, ntrial), rng.integers(0, n, ntrial)], 1).astype(np.int32)
+    disp = rng.uniform(-0.04 * lam_db, 0.04 * lam_db, (ntrial, 3))
+    for prec in (pgb.PGB_FP64, pgb.PGB_MIXED):
+        a = pgb.Action(L, m, n, w["tau"], w["lam"], action="gsf", precision=prec)
+        a.load(cfg)
+        for _ in range(2):
+            a.full_action()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            a.full_action()
+        t_full = (time.perf_counter() - t0) / args.steps
+        pos = cfg["pos"][beads[:, 0], beads[:, 1]] + disp
+        pos -= L * np.floor(pos / L + 0.5)
+        d_b = torch.from_numpy(beads).cuda()
+        d_p = torch.from_numpy(np.ascontiguousarray(pos)).cuda()
+        d_o = torch.empty(ntrial, dtype=torch.float64, device="cuda")
+        d_w = torch.empty(2 * ntrial, dtype=torch.float64, device="cuda")
+        stream = torch.cuda.ExternalStream(a.lib.pgb_stream(a.h))
+        k = ntrial if prec == pgb.PGB_MIXED else 20000
+        a._chk(a.lib.pgb_trial_actions_device_async(a.h, d_b.data_ptr(), d_p.data_ptr(), 1000, 1, 0,
+                                                    d_o.data_ptr(), d_w.data_ptr()))
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            a._chk(a.lib.pgb_trial_actions_device_async(a.h, d_b.data_ptr(), d_p.data_ptr(), k, 1, 0,
+                                                        d_o.data_ptr(), d_w.data_ptr()))
+            e1.record(stream)
+        torch.cuda.synchronize()
+        t_trial = e0.elapsed_time(e1) / 1e3
+        # pair evaluations of a trial, counted as the reference's checkMove does
+        # them: 2 (old, new) x [(n-1) V terms + on odd (gradV) slices the
+        # n(n-1)/2 pair forces of the slice]
+        odd = (beads[:k, 0] % 2 == 1).mean()
+        trial_pairs = k * 2 * ((n - 1) + odd * n * (n - 1) / 2)
+        res["fp64" if prec == pgb.PGB_FP64 else "mixed"] = {
+            "full_action_ms": 1e3 * t_full, "full_action_pairs_per_s": (v_pairs + g_pairs) / t_full,
+            "trials": k, "trial_ms": 1e3 * t_trial, "trial_pairs_per_s": trial_pairs / t_trial,
+            "trial_moves_per_s": k / t_trial}
+    out = {"metric": "pair evaluations/s (single-bead trial moves, mixed)",
+           "value": res["mixed"]["trial_pairs_per_s"], "unit": "pair-evaluations/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": 2, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
+           "config": {"workload": "pair action: N=256, M=250, GSF, rc=L, 10^6 trial displacements "
+                                  "uniform in [-0.04 lambda_dB, 0.04 lambda_dB]^3", "results": res}}
+    if not args.no_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        o = pyoracle.Oracle(L, m, n, w["tau"], w["lam"], action="gsf")
+        o.load(cfg)
+        t0 = time.perf_counter()
+        cnt = 0
+        while time.perf_counter() - t0 < 5.0:
+            s_, p_ = int(beads[cnt, 0]), int(beads[cnt, 1])
+            o.bead_action(s_, p_)
+            cnt += 1
+        dt = time.perf_counter() - t0
+        odd = (beads[:cnt, 0] % 2 == 1).mean()
+        pairs = cnt * ((n - 1) + odd * n * (n - 1) / 2)
+        out["cpu_baseline"] = {"value": pairs / dt, "unit": "pair-evaluations/s", "cores": 1,
+                               "kind": "port", "sample": "%d per-bead GSF actions (FP64 oracle, 1 "
+                               "thread, rc=L) in %.1f s" % (cnt, dt)}
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+# Plain worm-PIMC leg (N=16, T=2 K -> M=124, tau=1/248): the plain FP64 GPU
+# form (host-driven moves, MT19937) against the oracle on one host thread,
+# with the energy and S(q) (|q| <= 4/A) estimators sampled every step.
+# ---------------------------------------------------------------------------
+def run_plain(args, pgb):
+    from pimc_gb300 import worldlines as wl
+    w = wl.workload_plain_small()
+    n, m, L = w["n"], w["m"], w["side"]
+    cfg = wl.seeded_worldlines(n, m, L, w["lam"], w["tau"], 0)
+    mbar = wl.default_mbar(n, L ** 3, w["lam"], 0.004, m)
+    q = pgb.qvectors("max_float", "4 0 0", [L, L, L])
+    a = pgb.Action(L, m, n, w["tau"], w["lam"])
+    a.load(cfg)
+    a.plain_seed(139853)
+    a.plain_run(1, mbar=mbar, temperature=w["temperature"])
+    t0 = time.perf_counter()
+    bu = 0
+    for _ in range(args.steps):
+        r = a.plain_run(1, mbar=mbar, temperature=w["temperature"])
+        bu += r["bead_updates"]
+        a.ssf(q)
+    dt = time.perf_counter() - t0
+    out = {"metric": "bead-updates/s (plain FP64 GPU form)", "value": bu / dt,
+           "unit": "bead-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": 1,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic",
+           "config": {"workload": "plain PIMC N=16, T=2 K, M=124 (tau=1/248), Mbar=%d, staging + COM, "
+                                  "energy + S(q) (%d q) every step" % (mbar, len(q))}}
+    if not args.no_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        o = pyoracle.Oracle(L, m, n, w["tau"], w["lam"])
+        o.load(cfg)
+        mt = pyoracle.MT(139853)
+        t0 = time.perf_counter()
+        r = o.run_steps(mt, args.steps, mbar=mbar, temperature=w["temperature"])
+        for _ in range(args.steps):
+            o.ssf_pairwise(q)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": r["bead_updates"] / dt, "unit": "bead-updates/s", "cores": 1,
+                               "kind": "port", "sample": "%d steps of the oracle on one thread" % args.steps}
+    print(json.dumps(out))
+
+
 def run_reference(args):
     rank, ws = dist_init()
     if rank != 0:
@@ -251,11 +527,16 @@ def main():
     rank, ws = dist_init()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     import pimc_gb300 as pgb
+    if args.workload != "walkers":
+        if rank == 0:
+            {"serving": run_serving, "isf": run_isf, "pair": run_pair,
+             "plain": run_plain}[args.workload](args, pgb)
+        return
 
     w = workload(args.walkers, seed=rank)
     W = pgb.Walkers(w["n"], w["m"], w["temperature"], w["side"], w["mbar"], w["tau"], w["lam"],
-                    seed=1000 + rank)
-    W.init()                                   # autotunes threads per walker
+                    seed=1000 + rank, threads_per_walker=args.schedule)
+    W.init()                                   # autotunes the schedule when 0
     stream = torch.cuda.ExternalStream(W.stream())
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
     pair_per_step, bu_nominal = pair_evals_per_sweep(w)
@@ -342,6 +623,7 @@ def main():
         out["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
         out["plain_fp64"] = plain_form_rate(pgb)
         out["plain_fp64"]["batched_over_plain"] = value / out["plain_fp64"]["value"]
+        out["serving"] = serving_run(pgb, seconds=args.serve_seconds)
     if rank == 0:
         print(json.dumps(out))
 

@@ -84,7 +84,8 @@ int pgb_grad2v_batch(pgb_ctx* ctx, const double* sep, double* out, int n);
 
 /* ---- worldline state: Path/Worm/LookupTable updates (path.cpp:197-420,
  *      lookuptable.cpp:314-458).  The device mirror must follow every bead
- *      change the caller makes, as the reference mutates before it asks. -- */
+ *      change the caller makes, as the reference mutates before it asks.
+ *      worm8 may be NULL: no worm (all eight locators XXX = -1). -------- */
 int pgb_load_path(pgb_ctx* ctx, const double* pos, const int32_t* next,
                   const int32_t* prev, const uint8_t* on, const int32_t* worm8);
 int pgb_update_beads(pgb_ctx* ctx, const int32_t* beads, const double* pos, int k);
@@ -97,6 +98,16 @@ int pgb_get_positions(pgb_ctx* ctx, double* pos);
  * range forms, action.cpp:384-405, 572-620).  Inactive beads give 0. */
 int pgb_bead_actions(pgb_ctx* ctx, const int32_t* beads, int k, int shift,
                      int mode, double* out_per_bead, double* out_sum);
+/* Trial displacements: delta[i] = U_b(pos[i]) - U_b(current) for bead i alone
+ * moved to pos[i] (AoS [k][3]); the trials are independent of one another.
+ * This is the quantity of every single-bead Metropolis test
+ * (potentialAction(bead) after minus before, action.cpp:487-514). */
+int pgb_trial_actions(pgb_ctx* ctx, const int32_t* beads, const double* pos, int k,
+                      int shift, int mode, double* out_delta);
+/* the same on device buffers, asynchronous on the context stream; d_work
+ * holds 2k doubles */
+int pgb_trial_actions_device_async(pgb_ctx* ctx, const int32_t* d_beads, const double* d_pos,
+                                   int k, int shift, int mode, double* d_delta, double* d_work);
 /* potentialAction(startBead, endBead), action.cpp:522-570: follows next links */
 int pgb_range_action(pgb_ctx* ctx, int s0, int p0, int s1, int p1, int shift,
                      double* out);
@@ -244,6 +255,59 @@ int pgb_walkers_tuning(pgb_walkers* w, int* scheds, float* ms, int cap);
 int pgb_walkers_energy(pgb_walkers* w, int precision, double* en_per_walker);
 void* pgb_walkers_stream(pgb_walkers* w);
 const char* pgb_walkers_last_error(const pgb_walkers* w);
+
+/* ---- serving: continuous batching of simulation jobs (no reference
+ *      counterpart; replaces queueing independent pimc.e runs).  Jobs are
+ *      canonical chains of the batched-walker engine (staging + centre-of-mass
+ *      moves, energy sampled every sweep); mu is carried for the E_mu column
+ *      only. ------------------------------------------------------------- */
+typedef struct pgb_server pgb_server;
+typedef struct {
+    double hbm_budget_bytes;   /* device memory for worldline slabs */
+    int    max_active;         /* jobs on the device at once */
+    int    sweeps_per_round;   /* sweeps per round of a 64-particle, 125-slice job;
+                                  a job of cost N^2 M makes this times 64^2 125/(N^2 M),
+                                  at least 1 and at most sweeps_per_round */
+    int    bin_sweeps;         /* a bin closes at the first round end after this many sweeps */
+    double tau, lambda;
+    double p_com;
+    int    aziz_year;
+} pgb_server_params;
+typedef struct {
+    int       n;               /* particles N0 */
+    double    temperature;     /* K; M = even round(1/(T tau)) */
+    double    mu;              /* chemical potential (reported, canonical run) */
+    double    density;         /* initial box: L = (n/density)^(1/3) */
+    long long sweeps;          /* Monte Carlo steps to run */
+    uint64_t  seed;            /* the job's own random streams */
+    double    arrival;         /* server-clock seconds at which the job arrives */
+} pgb_job_spec;
+typedef struct {
+    int       job, bin;
+    double    energy_per_particle;  /* mean E/N over the bin */
+    long long samples;
+    double    time;            /* server clock when the bin became available */
+} pgb_bin;
+typedef struct {
+    int       state;           /* 0 submitted, 1 queued, 2 on the device, 3 done */
+    double    arrival, admitted, first_bin, completed;  /* -1 when not yet */
+    long long sweeps_done;
+    int       n, m;
+    size_t    bytes;           /* device footprint of the worldline slab */
+} pgb_job_info;
+
+int         pgb_server_create(const pgb_server_params* p, pgb_server** out);
+int         pgb_server_destroy(pgb_server* s);
+int         pgb_server_submit(pgb_server* s, const pgb_job_spec* job, int* job_id);
+/* one round: admit arrived jobs that fit, advance every active job, emit bins,
+ * retire finished jobs */
+int         pgb_server_step(pgb_server* s, int* n_active, int* n_queued);
+int         pgb_server_poll_bins(pgb_server* s, pgb_bin* out, int cap, int* n);
+int         pgb_server_job_info(pgb_server* s, int job, pgb_job_info* out);
+double      pgb_server_clock(pgb_server* s);
+long long   pgb_server_bead_updates(pgb_server* s);   /* of retired jobs */
+int         pgb_server_active_bead_updates(pgb_server* s, long long* total);
+const char* pgb_server_last_error(const pgb_server* s);
 
 /* ---- plain form: the reference move loop driven from the host with one
  *      FP64 device action call per move (move.cpp:1124-1707 semantics,

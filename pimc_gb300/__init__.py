@@ -19,7 +19,7 @@ from ._lib import (PGB_FP64, PGB_MIXED, PGB_ACTION_FULL, PGB_ACTION_BARE, PGB_AC
                    PgbError, dptr, iptr, u8ptr)
 from . import worldlines
 
-__all__ = ["Action", "Walkers", "qvectors", "device_info", "PGB_FP64", "PGB_MIXED",
+__all__ = ["Action", "Walkers", "Server", "qvectors", "device_info", "PGB_FP64", "PGB_MIXED",
            "PGB_ACTION_FULL", "PGB_ACTION_BARE", "PGB_ACTION_CORR", "PgbError", "worldlines",
            "action_factors"]
 
@@ -150,6 +150,14 @@ class Action:
         self._chk(self.lib.pgb_bead_actions(self.h, iptr(beads), len(beads), shift, mode,
                                             dptr(per), C.byref(tot)))
         return per, tot.value
+
+    def trial_actions(self, beads, pos, shift=1, mode=PGB_ACTION_FULL):
+        beads = np.ascontiguousarray(beads, dtype=np.int32).reshape(-1, 2)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(beads))
+        self._chk(self.lib.pgb_trial_actions(self.h, iptr(beads), dptr(pos), len(beads), shift, mode,
+                                             dptr(out)))
+        return out
 
     def range_action(self, start, end, shift=1):
         out = C.c_double()
@@ -315,3 +323,73 @@ class Walkers:
 
     def stream(self):
         return self.lib.pgb_walkers_stream(self.h)
+
+
+class Server:
+    """Continuous-batching job server: jobs arrive, are admitted when their
+    worldlines fit the HBM budget, run together in shared launches and stream
+    estimator bins back."""
+
+    def __init__(self, hbm_budget_bytes, max_active=1024, sweeps_per_round=10, bin_sweeps=100,
+                 tau=0.004, lam=None, p_com=0.05, aziz_year=1979):
+        self.lib = _lib.load()
+        lam = worldlines.LAMBDA_HE4 if lam is None else lam
+        p = _lib.PgbServerParams(float(hbm_budget_bytes), max_active, sweeps_per_round, bin_sweeps,
+                                 tau, lam, p_com, aziz_year)
+        h = C.c_void_p()
+        rc = self.lib.pgb_server_create(C.byref(p), C.byref(h))
+        if rc != 0:
+            raise PgbError(rc, (self.lib.pgb_server_last_error(None) or b"").decode())
+        self.h = h
+
+    def _chk(self, rc):
+        return _lib.check(rc, self.h, server=True)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pgb_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, n, temperature, sweeps, seed, arrival=0.0, mu=0.0,
+               density=worldlines.DENSITY):
+        spec = _lib.PgbJobSpec(int(n), float(temperature), float(mu), float(density), int(sweeps),
+                               int(seed), float(arrival))
+        jid = C.c_int()
+        self._chk(self.lib.pgb_server_submit(self.h, C.byref(spec), C.byref(jid)))
+        return jid.value
+
+    def step(self):
+        a, q = C.c_int(), C.c_int()
+        self._chk(self.lib.pgb_server_step(self.h, C.byref(a), C.byref(q)))
+        return a.value, q.value
+
+    def bins(self):
+        out = []
+        buf = (_lib.PgbBin * 1024)()
+        while True:
+            n = C.c_int()
+            self._chk(self.lib.pgb_server_poll_bins(self.h, buf, 1024, C.byref(n)))
+            out += [dict(job=b.job, bin=b.bin, energy=b.energy_per_particle, samples=b.samples,
+                         time=b.time) for b in buf[:n.value]]
+            if n.value < 1024:
+                return out
+
+    def job(self, jid):
+        i = _lib.PgbJobInfo()
+        self._chk(self.lib.pgb_server_job_info(self.h, jid, C.byref(i)))
+        return dict(state=i.state, arrival=i.arrival, admitted=i.admitted, first_bin=i.first_bin,
+                    completed=i.completed, sweeps_done=i.sweeps_done, n=i.n, m=i.m, bytes=i.bytes)
+
+    def clock(self):
+        return self.lib.pgb_server_clock(self.h)
+
+    def bead_updates(self):
+        t = C.c_longlong()
+        self._chk(self.lib.pgb_server_active_bead_updates(self.h, C.byref(t)))
+        return t.value

@@ -55,6 +55,29 @@ class PgbMoveStats(C.Structure):
                 ("bead_updates", C.c_longlong)]
 
 
+class PgbServerParams(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int),
+                ("sweeps_per_round", C.c_int), ("bin_sweeps", C.c_int), ("tau", C.c_double),
+                ("lambda_", C.c_double), ("p_com", C.c_double), ("aziz_year", C.c_int)]
+
+
+class PgbJobSpec(C.Structure):
+    _fields_ = [("n", C.c_int), ("temperature", C.c_double), ("mu", C.c_double),
+                ("density", C.c_double), ("sweeps", C.c_longlong), ("seed", C.c_uint64),
+                ("arrival", C.c_double)]
+
+
+class PgbBin(C.Structure):
+    _fields_ = [("job", C.c_int), ("bin", C.c_int), ("energy_per_particle", C.c_double),
+                ("samples", C.c_longlong), ("time", C.c_double)]
+
+
+class PgbJobInfo(C.Structure):
+    _fields_ = [("state", C.c_int), ("arrival", C.c_double), ("admitted", C.c_double),
+                ("first_bin", C.c_double), ("completed", C.c_double), ("sweeps_done", C.c_longlong),
+                ("n", C.c_int), ("m", C.c_int), ("bytes", C.c_size_t)]
+
+
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int32)
 _U8 = C.POINTER(C.c_uint8)
@@ -74,6 +97,8 @@ _SIGS = {
     "pgb_update_beads": (C.c_int, [_VP, _IP, _DP, C.c_int]),
     "pgb_get_positions": (C.c_int, [_VP, _DP]),
     "pgb_bead_actions": (C.c_int, [_VP, _IP, C.c_int, C.c_int, C.c_int, _DP, _DP]),
+    "pgb_trial_actions": (C.c_int, [_VP, _IP, _DP, C.c_int, C.c_int, C.c_int, _DP]),
+    "pgb_trial_actions_device_async": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, _VP, _VP]),
     "pgb_range_action": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _DP]),
     "pgb_full_action": (C.c_int, [_VP, _DP]),
     "pgb_kinetic_action": (C.c_int, [_VP, _DP]),
@@ -105,6 +130,16 @@ _SIGS = {
     "pgb_walkers_energy": (C.c_int, [_VP, C.c_int, _DP]),
     "pgb_walkers_stream": (_VP, [_VP]),
     "pgb_walkers_last_error": (C.c_char_p, [_VP]),
+    "pgb_server_create": (C.c_int, [C.POINTER(PgbServerParams), C.POINTER(_VP)]),
+    "pgb_server_destroy": (C.c_int, [_VP]),
+    "pgb_server_submit": (C.c_int, [_VP, C.POINTER(PgbJobSpec), C.POINTER(C.c_int)]),
+    "pgb_server_step": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "pgb_server_poll_bins": (C.c_int, [_VP, C.POINTER(PgbBin), C.c_int, C.POINTER(C.c_int)]),
+    "pgb_server_job_info": (C.c_int, [_VP, C.c_int, C.POINTER(PgbJobInfo)]),
+    "pgb_server_clock": (C.c_double, [_VP]),
+    "pgb_server_bead_updates": (C.c_longlong, [_VP]),
+    "pgb_server_active_bead_updates": (C.c_int, [_VP, C.POINTER(C.c_longlong)]),
+    "pgb_server_last_error": (C.c_char_p, [_VP]),
     "pgb_plain_seed": (C.c_int, [_VP, C.c_uint32]),
     "pgb_plain_run": (C.c_int, [_VP, C.POINTER(PgbMoveParams), C.c_int, _IP, C.c_int,
                                 C.POINTER(C.c_int), _DP, C.POINTER(PgbMoveStats)]),
@@ -153,10 +188,12 @@ def u8ptr(a):
     return a.ctypes.data_as(_U8)
 
 
-def check(rc, handle=None, walkers=False):
+def check(rc, handle=None, walkers=False, server=False):
     if rc != PGB_OK:
         lib = load()
-        if walkers:
+        if server:
+            msg = lib.pgb_server_last_error(handle)
+        elif walkers:
             msg = lib.pgb_walkers_last_error(handle)
         else:
             msg = lib.pgb_last_error(handle)

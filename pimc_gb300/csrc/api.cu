@@ -377,9 +377,9 @@ int pgb_bead_actions(pgb_ctx* h, const int32_t* beads, int k, int shift, int mod
     PathView v = c.view();
     cudaError_t e = (c.p.precision == PGB_MIXED)
         ? launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda,
-                                c.p.vfactor, c.p.gradvfactor, d_o, c.stream)
+                                c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream)
         : launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda,
-                                c.p.vfactor, c.p.gradvfactor, d_o, c.stream);
+                                c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream);
     if (e != cudaSuccess) return c.cuda_fail(e, "bead actions launch");
     double* ho = reinterpret_cast<double*>(hp + ((bb + 15) & ~(size_t)15));
     PGB_CUDA(&c, cudaMemcpyAsync(ho, d_o, ob, cudaMemcpyDeviceToHost, c.stream));
@@ -760,6 +760,88 @@ int pgb_isf_device_async(pgb_ctx* h, const double* d_q, int nq, int mode, double
     if (mode != 0 && mode != 1) return c.fail(PGB_EINVAL, "isf mode must be 0 or 1");
     rc = c.ensure_scratch(scatter_work_bytes(c, nq, 1, mode)); if (rc) return rc;
     return scatter_common(c, d_q, nq, 1, mode, d_out, c.d_scratch);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Trial displacements: for each (bead, trial position) the change of the
+// bead's potential action if only that bead moved there -- the quantity every
+// single-bead Metropolis test needs (potentialAction(bead) after minus
+// before, action.cpp:487-514), for many independent trials in one launch.
+// ---------------------------------------------------------------------------
+namespace pgb {
+__global__ void k_delta(const double* __restrict__ a, const double* __restrict__ b, double* out, int k) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < k) out[i] = a[i] - b[i];
+}
+}  // namespace pgb
+
+namespace {
+int trial_launch(Ctx& c, const int2* d_b, const double* d_pos, int k, int shift, int mode,
+                 double* d_new, double* d_old, double* d_delta) {
+    PathView v = c.view();
+    cudaError_t e;
+    if (c.p.precision == PGB_MIXED) {
+        e = launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
+                                  c.p.gradvfactor, d_pos, d_new, c.stream);
+        if (e == cudaSuccess)
+            e = launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
+                                      c.p.gradvfactor, nullptr, d_old, c.stream);
+    } else {
+        e = launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
+                                  c.p.gradvfactor, d_pos, d_new, c.stream);
+        if (e == cudaSuccess)
+            e = launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
+                                      c.p.gradvfactor, nullptr, d_old, c.stream);
+    }
+    if (e == cudaSuccess) {
+        pgb::k_delta<<<(k + 255) / 256, 256, 0, c.stream>>>(d_new, d_old, d_delta, k);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return c.cuda_fail(e, "trial actions launch");
+    return PGB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int pgb_trial_actions(pgb_ctx* h, const int32_t* beads, const double* pos, int k, int shift,
+                      int mode, double* out_delta) {
+    if (!h || k < 0 || (k > 0 && (!beads || !pos || !out_delta)) || shift < 1 || mode < 0 || mode > 2)
+        return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    if (k == 0) return PGB_OK;
+    for (int i = 0; i < k; ++i)
+        if (beads[2*i] < 0 || beads[2*i] >= c.M || beads[2*i+1] < 0 || beads[2*i+1] >= c.Ne)
+            return c.fail(PGB_EINVAL, "trial_actions: bead out of range");
+    size_t bb = ((size_t)k * sizeof(int2) + 255) & ~(size_t)255;
+    size_t pb = ((size_t)k * 3 * sizeof(double) + 255) & ~(size_t)255;
+    size_t ob = ((size_t)k * sizeof(double) + 255) & ~(size_t)255;
+    rc = c.ensure_scratch(bb + pb + 3 * ob); if (rc) return rc;
+    char* d = static_cast<char*>(c.d_scratch);
+    PGB_CUDA(&c, cudaMemcpyAsync(d, beads, (size_t)k * sizeof(int2), cudaMemcpyHostToDevice, c.stream));
+    PGB_CUDA(&c, cudaMemcpyAsync(d + bb, pos, (size_t)k * 3 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    double* d_new = reinterpret_cast<double*>(d + bb + pb);
+    double* d_old = reinterpret_cast<double*>(d + bb + pb + ob);
+    double* d_del = reinterpret_cast<double*>(d + bb + pb + 2 * ob);
+    rc = trial_launch(c, reinterpret_cast<int2*>(d), reinterpret_cast<double*>(d + bb), k, shift, mode,
+                      d_new, d_old, d_del);
+    if (rc) return rc;
+    PGB_CUDA(&c, cudaMemcpyAsync(out_delta, d_del, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    return PGB_OK;
+}
+
+int pgb_trial_actions_device_async(pgb_ctx* h, const int32_t* d_beads, const double* d_pos, int k,
+                                   int shift, int mode, double* d_delta, double* d_work) {
+    if (!h || !d_beads || !d_pos || !d_delta || !d_work || k <= 0 || shift < 1 || mode < 0 || mode > 2)
+        return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    return trial_launch(c, reinterpret_cast<const int2*>(d_beads), d_pos, k, shift, mode, d_work,
+                        d_work + k, d_delta);
 }
 
 }  // extern "C"

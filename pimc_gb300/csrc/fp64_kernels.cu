@@ -131,7 +131,7 @@ constexpr int kBeadBlock = 256;
 __global__ void __launch_bounds__(kBeadBlock)
 k_bead_actions64(PathView v, const int2* __restrict__ beads, int k, int shift, int mode,
                  double tau, double lambda, double vf0, double vf1, double gf0,
-                 double gf1, double* __restrict__ out) {
+                 double gf1, const double* __restrict__ over, double* __restrict__ out) {
     extern __shared__ double smem[];
     const int Ne = v.Ne;
     double* lx = smem;
@@ -158,7 +158,10 @@ k_bead_actions64(PathView v, const int2* __restrict__ beads, int k, int shift, i
                       : (mode == PGB_ACTION_FULL) ? (shift == 1 && gf > kEPS) : false;
 
     const double* X = v.pos + (size_t)s * 3 * Ne;
-    const double x1 = X[p], y1 = X[Ne + p], z1 = X[2 * Ne + p];
+    // `over` (trial positions) replaces the bead's stored position
+    const double x1 = over ? over[3 * b] : X[p];
+    const double y1 = over ? over[3 * b + 1] : X[Ne + p];
+    const double z1 = over ? over[3 * b + 2] : X[2 * Ne + p];
     const int st1 = bead_state(v, s, p);
     if (tid == 0) s_total = 0;
     __syncthreads();
@@ -238,7 +241,8 @@ k_bead_actions64(PathView v, const int2* __restrict__ beads, int k, int shift, i
 
 cudaError_t launch_bead_actions64(const PathView& v, const int2* d_beads, int k, int shift,
                                   int mode, double tau, double lambda, const double vf[2],
-                                  const double gf[2], double* d_out, cudaStream_t s) {
+                                  const double gf[2], const double* d_over, double* d_out,
+                                  cudaStream_t s) {
     if (k <= 0) return cudaSuccess;
     size_t smem = (size_t)v.Ne * (3 * sizeof(double) + sizeof(int));
     static bool attr_set = false;
@@ -247,7 +251,7 @@ cudaError_t launch_bead_actions64(const PathView& v, const int2* d_beads, int k,
         attr_set = true;
     }
     k_bead_actions64<<<k, kBeadBlock, smem, s>>>(v, d_beads, k, shift, mode, tau, lambda,
-                                                 vf[0], vf[1], gf[0], gf[1], d_out);
+                                                 vf[0], vf[1], gf[0], gf[1], d_over, d_out);
     return cudaGetLastError();
 }
 

@@ -52,7 +52,7 @@ constexpr int kBeadBlock32 = 256;
 __global__ void __launch_bounds__(kBeadBlock32)
 k_bead_actions32(PathView v, AzizF az, const int2* __restrict__ beads, int k, int shift,
                  int mode, double tau, double lambda, double vf0, double vf1, double gf0,
-                 double gf1, double* __restrict__ out) {
+                 double gf1, const double* __restrict__ over, double* __restrict__ out) {
     extern __shared__ float4 lpos[];
     __shared__ double red[kBeadBlock32 / 32];
     __shared__ int wcount[kBeadBlock32 / 32];
@@ -75,7 +75,9 @@ k_bead_actions32(PathView v, AzizF az, const int2* __restrict__ beads, int k, in
     const float I0 = (float)v.sideInv[0], I1 = (float)v.sideInv[1], I2 = (float)v.sideInv[2];
     const float rc2 = (float)v.rc2;
     const float4* P = v.pos32 + (size_t)s * Ne;
-    const float4 r1 = P[p];
+    const float4 r1 = over ? make_float4((float)over[3 * b], (float)over[3 * b + 1],
+                                         (float)over[3 * b + 2], 0.f)
+                           : P[p];
     const int st1 = bead_state(v, s, p);
     if (tid == 0) s_total = 0;
     __syncthreads();
@@ -147,8 +149,8 @@ k_bead_actions32(PathView v, AzizF az, const int2* __restrict__ beads, int k, in
 
 cudaError_t launch_bead_actions32(const PathView& v, AzizParams a, const int2* d_beads, int k,
                                   int shift, int mode, double tau, double lambda,
-                                  const double vf[2], const double gf[2], double* d_out,
-                                  cudaStream_t s) {
+                                  const double vf[2], const double gf[2], const double* d_over,
+                                  double* d_out, cudaStream_t s) {
     if (k <= 0) return cudaSuccess;
     size_t smem = (size_t)v.Ne * sizeof(float4);
     static bool attr_set = false;
@@ -157,7 +159,8 @@ cudaError_t launch_bead_actions32(const PathView& v, AzizParams a, const int2* d
         attr_set = true;
     }
     k_bead_actions32<<<k, kBeadBlock32, smem, s>>>(v, make_aziz_f(a), d_beads, k, shift, mode,
-                                                   tau, lambda, vf[0], vf[1], gf[0], gf[1], d_out);
+                                                   tau, lambda, vf[0], vf[1], gf[0], gf[1], d_over,
+                                                   d_out);
     return cudaGetLastError();
 }
 

@@ -98,7 +98,7 @@ cudaError_t launch_potential_batch64(const PathView& v, const double* d_sep,
 cudaError_t launch_bead_actions64(const PathView& v, const int2* d_beads, int k,
                                   int shift, int mode, double tau, double lambda,
                                   const double vf[2], const double gf[2],
-                                  double* d_out, cudaStream_t s);
+                                  const double* d_over, double* d_out, cudaStream_t s);
 cudaError_t launch_slice_terms64(const PathView& v, int window, int want_tmat,
                                  double* d_terms /* [8][M] */, cudaStream_t s);
 cudaError_t launch_rhoq64(const PathView& v, const double* d_q, int nq,
@@ -109,7 +109,7 @@ cudaError_t launch_isf_direct64(const double* d_rho, int nq, int M, double norm,
 cudaError_t launch_bead_actions32(const PathView& v, AzizParams az,
                                   const int2* d_beads, int k, int shift, int mode,
                                   double tau, double lambda, const double vf[2],
-                                  const double gf[2], double* d_out,
+                                  const double gf[2], const double* d_over, double* d_out,
                                   cudaStream_t s);
 cudaError_t launch_slice_terms32(const PathView& v, AzizParams az, int window,
                                  double* d_terms, cudaStream_t s);

@@ -21,8 +21,11 @@
 // folded to FP64 across the CTA; the acceptance exp(-dU) test is FP64.
 // Random numbers come from Philox4x32-10 keyed by (seed, walker).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -36,6 +39,9 @@ constexpr int kMaxStage = 64;        // Mbar <= 64
 struct WalkerMeta {
     int N, M, mbar, num_updates;
     long long off;                   // float4 offset of the walker's slab
+    unsigned long long key;          // Philox key of the walker's streams
+    int max_sweeps;                  // sweeps this walker may still make (per launch cap)
+    int pad_;
     float L, Linv;
     float sig2lt;                    // sqrt(2 lambda tau)
     float com_delta;
@@ -48,11 +54,16 @@ struct WalkerAcc {
     long long att[2], acc[2];
 };
 
-__device__ __forceinline__ uint4 wrand(uint64_t seed, int w, uint32_t c0, uint32_t c1,
+// Streams are keyed per walker (WalkerMeta::key), so a walker's trajectory
+// does not depend on its slot or on the other walkers in the launch.
+__device__ __forceinline__ uint4 wrand(unsigned long long key, uint32_t c0, uint32_t c1,
                                        uint32_t c2, uint32_t c3) {
-    uint2 key = make_uint2((uint32_t)seed ^ (uint32_t)w * 0x9E3779B9u,
-                           (uint32_t)(seed >> 32) + (uint32_t)w);
-    return philox4x32(make_uint4(c0, c1, c2, c3), key);
+    return philox4x32(make_uint4(c0, c1, c2, c3), make_uint2((uint32_t)key, (uint32_t)(key >> 32)));
+}
+
+inline unsigned long long walker_key(uint64_t seed, int w) {
+    return (((unsigned long long)((uint32_t)(seed >> 32) + (uint32_t)w)) << 32) |
+           (unsigned long long)((uint32_t)seed ^ ((uint32_t)w * 0x9E3779B9u));
 }
 
 __device__ __forceinline__ float put_inside(float x, float L, float Linv) {
@@ -113,11 +124,11 @@ k_walkers_run(const WalkerMeta* __restrict__ meta, const int* __restrict__ order
     double esum = 0.0, esumsq = 0.0;
     long long nsamp = 0, nbu = 0, att0 = 0, att1 = 0, acc0 = 0, acc1 = 0;
 
-    for (int sw = 0; sw < sweeps; ++sw) {
+    for (int sw = 0; sw < min(sweeps, m.max_sweeps); ++sw) {
         const unsigned long long gs = sweep0 + sw;
         for (int u = 0; u < m.num_updates; ++u) {
             // every thread draws the same move description
-            uint4 r0 = wrand(seed, w, (uint32_t)u, (uint32_t)gs, (uint32_t)(gs >> 32), 0u);
+            uint4 r0 = wrand(m.key, (uint32_t)u, (uint32_t)gs, (uint32_t)(gs >> 32), 0u);
             const bool com = u01f(r0.x) < p_com;
             const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
             double dV;
@@ -130,7 +141,7 @@ k_walkers_run(const WalkerMeta* __restrict__ meta, const int* __restrict__ order
                 nmove = len - 1;
                 // normals for the stage: 3 per moved bead
                 for (int k = tid; k < nmove; k += TPW) {
-                    uint4 a = wrand(seed, w, (uint32_t)u, (uint32_t)gs, (uint32_t)(gs >> 32), 1u + k);
+                    uint4 a = wrand(m.key, (uint32_t)u, (uint32_t)gs, (uint32_t)(gs >> 32), 1u + k);
                     float2 z01 = box_muller(a.x, a.y);
                     float2 z2 = box_muller(a.z, a.w);
                     s_z[k][0] = z01.x; s_z[k][1] = z01.y; s_z[k][2] = z2.x;
@@ -177,7 +188,7 @@ k_walkers_run(const WalkerMeta* __restrict__ meta, const int* __restrict__ order
                 }
                 dV = block_sum(acc.value(), red);
                 if (tid == 0) {
-                    uint4 ra = wrand(seed, w, (uint32_t)u, (uint32_t)gs, (uint32_t)(gs >> 32), 0xFFFFu);
+                    uint4 ra = wrand(m.key, (uint32_t)u, (uint32_t)gs, (uint32_t)(gs >> 32), 0xFFFFu);
                     double x = u01d(ra.x, ra.y);
                     s_acc = (x < exp(-(tau * dV))) ? 1 : 0;
                 }
@@ -195,7 +206,7 @@ k_walkers_run(const WalkerMeta* __restrict__ meta, const int* __restrict__ order
                 nmove = M;
                 const float sx = m.com_delta * (u01f(r0.y) - 0.5f);
                 const float sy = m.com_delta * (u01f(r0.w) - 0.5f);
-                uint4 r1 = wrand(seed, w, (uint32_t)u, (uint32_t)gs, (uint32_t)(gs >> 32), 0xFFFEu);
+                uint4 r1 = wrand(m.key, (uint32_t)u, (uint32_t)gs, (uint32_t)(gs >> 32), 0xFFFEu);
                 const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
                 KahanF acc;
                 const int npairs = M * N;
@@ -244,7 +255,7 @@ k_walkers_run(const WalkerMeta* __restrict__ meta, const int* __restrict__ order
         WalkerAcc& A = accs[w];
         A.esum += esum; A.esumsq += esumsq; A.samples += nsamp; A.bead_updates += nbu;
         A.att[0] += att0; A.att[1] += att1; A.acc[0] += acc0; A.acc[1] += acc1;
-        ctr[w] = sweep0 + sweeps;
+        ctr[w] = sweep0 + min(sweeps, m.max_sweeps);
     }
 }
 
@@ -310,11 +321,11 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
     const int kb0 = (T >= N) ? tt / N : 0;
     const int jstep = (T >= N) ? N : T;
 
-    for (int sw = 0; sw < sweeps; ++sw) {
+    for (int sw = 0; sw < min(sweeps, m.max_sweeps); ++sw) {
         const unsigned long long gs = sweep0 + sw;
         const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
         for (int u = 0; u < m.num_updates; ++u) {
-            uint4 r0 = wrand(seed, w, (uint32_t)u, g0, g1, 0u);
+            uint4 r0 = wrand(m.key, (uint32_t)u, g0, g1, 0u);
             const bool com = u01f(r0.x) < p_com;
             const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
             if (!com) {
@@ -340,12 +351,12 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                     float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
                     const int j1 = lane + 1, j2 = lane + 33;
                     if (j1 <= len) {
-                        uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)j1);
+                        uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)j1);
                         float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
                         a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
                     }
                     if (j2 <= len) {
-                        uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)j2);
+                        uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)j2);
                         float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
                         a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
                     }
@@ -402,7 +413,7 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 if (tt == 0) {
                     double dV = 0.0;
                     for (int q = 0; q < nw; ++q) dV += red[q];
-                    uint4 ra = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFFu);
+                    uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
                     const double x = u01d(ra.x, ra.y);
                     const double a = -(tau * dV);
                     s_acc[slot] = (a >= 0.0 || x < exp(a)) ? 1 : 0;
@@ -421,7 +432,7 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
             } else {
                 const float sx = m.com_delta * (u01f(r0.y) - 0.5f);
                 const float sy = m.com_delta * (u01f(r0.w) - 0.5f);
-                const uint4 r1 = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFEu);
+                const uint4 r1 = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFEu);
                 const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
                 KahanF acc;
                 for (int j = j0; j < N; j += jstep) {
@@ -511,7 +522,7 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
         WalkerAcc& A = accs[w];
         A.esum += esum; A.esumsq += esumsq; A.samples += nsamp; A.bead_updates += nbu;
         A.att[0] += att0; A.att[1] += att1; A.acc[0] += acc0; A.acc[1] += acc1;
-        ctr[w] = sweep0 + sweeps;
+        ctr[w] = sweep0 + min(sweeps, m.max_sweeps);
     }
 }
 
@@ -573,22 +584,22 @@ k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ 
     double esum = 0.0, esumsq = 0.0;
     long long nsamp = 0, nbu = 0, nbu_com = 0, att0 = 0, att1 = 0, acc0 = 0, acc1 = 0;
 
-    for (int sw = 0; sw < sweeps; ++sw) {
+    for (int sw = 0; sw < min(sweeps, m.max_sweeps); ++sw) {
         const unsigned long long gs = sweep0 + sw;
         const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
         // split of the sweep's numUpdates moves into staging and COM moves
-        const uint4 rs = wrand(seed, w, 0xC0000000u, g0, g1, 0u);
+        const uint4 rs = wrand(m.key, 0xC0000000u, g0, g1, 0u);
         const float ncom_f = p_com * (float)m.num_updates;
         const int n_com = (int)ncom_f + ((u01f(rs.x) < ncom_f - floorf(ncom_f)) ? 1 : 0);
         const int n_stage = m.num_updates - n_com;
         const int rounds = (n_stage + P - 1) / P;
         for (int r = 0; r < rounds; ++r) {
-            const uint4 rphi = wrand(seed, w, 0x80000000u | (uint32_t)r, g0, g1, 0u);
+            const uint4 rphi = wrand(m.key, 0x80000000u | (uint32_t)r, g0, g1, 0u);
             const int phi = (int)(((unsigned long long)rphi.x * (unsigned)M) >> 32);
             const bool active = (r * P + wi) < n_stage;
             if (active) {
                 const uint32_t c0 = (uint32_t)r | ((uint32_t)wi << 24);
-                const uint4 r0 = wrand(seed, w, c0, g0, g1, 0u);
+                const uint4 r0 = wrand(m.key, c0, g0, g1, 0u);
                 const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
                 const int len = var_updates
                     ? 2 + (int)(((unsigned long long)r0.w * (unsigned)(m.mbar - 1)) >> 32)
@@ -609,12 +620,12 @@ k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ 
                 }
                 float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
                 if (lane + 1 <= len) {
-                    const uint4 a = wrand(seed, w, c0, g0, g1, (uint32_t)(lane + 1));
+                    const uint4 a = wrand(m.key, c0, g0, g1, (uint32_t)(lane + 1));
                     const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
                     a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
                 }
                 if (lane + 33 <= len) {
-                    const uint4 a = wrand(seed, w, c0, g0, g1, (uint32_t)(lane + 33));
+                    const uint4 a = wrand(m.key, c0, g0, g1, (uint32_t)(lane + 33));
                     const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
                     a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
                 }
@@ -669,7 +680,7 @@ k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ 
                 const double dV = warp_sum(acc.value());
                 int ok = 0;
                 if (lane == 0) {
-                    const uint4 ra = wrand(seed, w, c0, g0, g1, 0xFFFFu);
+                    const uint4 ra = wrand(m.key, c0, g0, g1, 0xFFFFu);
                     ok = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
                 }
                 ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -685,7 +696,7 @@ k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ 
         }
         // centre-of-mass moves, whole team
         for (int c = 0; c < n_com; ++c) {
-            const uint4 r0 = wrand(seed, w, 0x40000000u | (uint32_t)c, g0, g1, 0u);
+            const uint4 r0 = wrand(m.key, 0x40000000u | (uint32_t)c, g0, g1, 0u);
             const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
             const float sx = m.com_delta * (u01f(r0.y) - 0.5f);
             const float sy = m.com_delta * (u01f(r0.w) - 0.5f);
@@ -711,7 +722,7 @@ k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ 
             if (tt == 0) {
                 double dV = 0.0;
                 for (int q = 0; q < P; ++q) dV += red[q];
-                const uint4 ra = wrand(seed, w, 0x40000000u | (uint32_t)c, g0, g1, 0xFFFEu);
+                const uint4 ra = wrand(m.key, 0x40000000u | (uint32_t)c, g0, g1, 0xFFFEu);
                 s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
             }
             team_sync(slot, T);
@@ -773,7 +784,7 @@ k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ 
         A.esum += esum; A.esumsq += esumsq; A.samples += nsamp;
         A.att[0] += att0; A.acc[0] += acc0;
         atomicAdd(reinterpret_cast<unsigned long long*>(&A.bead_updates), (unsigned long long)nbu_com);
-        ctr[w] = sweep0 + sweeps;
+        ctr[w] = sweep0 + min(sweeps, m.max_sweeps);
     }
     // staging counters are per warp (each warp moves in its own window)
     if (lane == 0) {
@@ -886,11 +897,11 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
     const int kb0 = (T >= N) ? tt / N : 0;
     const int jstep = (T >= N) ? N : T;
 
-    for (int sw = 0; sw < sweeps; ++sw) {
+    for (int sw = 0; sw < min(sweeps, m.max_sweeps); ++sw) {
         const unsigned long long gs = sweep0 + sw;
         const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
         for (int u = 0; u < m.num_updates; ++u) {
-            const uint4 r0 = wrand(seed, w, (uint32_t)u, g0, g1, 0u);
+            const uint4 r0 = wrand(m.key, (uint32_t)u, g0, g1, 0u);
             const bool com = u01f(r0.x) < p_com;
             const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
             if (!com) {
@@ -906,12 +917,12 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
                     const float4 x0 = P[(size_t)s0 * N + i], xe = P[(size_t)se * N + i];
                     float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
                     if (lane + 1 <= len) {
-                        const uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)(lane + 1));
+                        const uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)(lane + 1));
                         const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
                         a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
                     }
                     if (lane + 33 <= len) {
-                        const uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)(lane + 33));
+                        const uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)(lane + 33));
                         const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
                         a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
                     }
@@ -965,7 +976,7 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
                 if (tt == 0) {
                     double dV = 0.0;
                     for (int q = 0; q < nw; ++q) dV += red[q];
-                    const uint4 ra = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFFu);
+                    const uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
                     s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
                 }
                 team_sync(slot, T);
@@ -984,7 +995,7 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
             } else {
                 const float sx = m.com_delta * (u01f(r0.y) - 0.5f);
                 const float sy = m.com_delta * (u01f(r0.w) - 0.5f);
-                const uint4 r1 = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFEu);
+                const uint4 r1 = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFEu);
                 const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
                 KahanF acc;
                 for (int c0 = 0; c0 < M; c0 += C) {
@@ -1088,7 +1099,7 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
         WalkerAcc& A = accs[w];
         A.esum += esum; A.esumsq += esumsq; A.samples += nsamp; A.bead_updates += nbu;
         A.att[0] += att0; A.att[1] += att1; A.acc[0] += acc0; A.acc[1] += acc1;
-        ctr[w] = sweep0 + sweeps;
+        ctr[w] = sweep0 + min(sweeps, m.max_sweeps);
     }
 }
 
@@ -1108,10 +1119,10 @@ struct MoveDesc {
     float sx, sy, sz;
 };
 
-__device__ __forceinline__ MoveDesc draw_move(uint64_t seed, int w, int u, uint32_t g0, uint32_t g1,
+__device__ __forceinline__ MoveDesc draw_move(int u, uint32_t g0, uint32_t g1,
                                               const WalkerMeta& m, float p_com, int var_updates) {
     MoveDesc d;
-    const uint4 r0 = wrand(seed, w, (uint32_t)u, g0, g1, 0u);
+    const uint4 r0 = wrand(m.key, (uint32_t)u, g0, g1, 0u);
     d.com = u01f(r0.x) < p_com;
     d.i = (int)(((unsigned long long)r0.z * (unsigned)m.N) >> 32);
     d.s0 = (int)(((unsigned long long)r0.y * (unsigned)m.M) >> 32);
@@ -1173,15 +1184,15 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
     const int jstep = (T >= N) ? N : T;
     int cur = 0;
 
-    for (int sw = 0; sw < sweeps; ++sw) {
+    for (int sw = 0; sw < min(sweeps, m.max_sweeps); ++sw) {
         const unsigned long long gs = sweep0 + sw;
         const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
         bool have = false;                        // rows of the current move already in Bsel(cur)
-        MoveDesc D = draw_move(seed, w, 0, g0, g1, m, p_com, var_updates);
+        MoveDesc D = draw_move(0, g0, g1, m, p_com, var_updates);
         for (int u = 0; u < m.num_updates; ++u) {
             const bool last = (u + 1 == m.num_updates);
             MoveDesc Dn = D;
-            if (!last) Dn = draw_move(seed, w, u + 1, g0, g1, m, p_com, var_updates);
+            if (!last) Dn = draw_move(u + 1, g0, g1, m, p_com, var_updates);
             if (!D.com) {
                 const bool pre = !last && !Dn.com;
                 if (tt == 0) {
@@ -1194,12 +1205,12 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                     const float4 x0 = P[(size_t)s0 * N + i], xe = P[(size_t)se * N + i];
                     float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
                     if (lane + 1 <= len) {
-                        const uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)(lane + 1));
+                        const uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)(lane + 1));
                         const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
                         a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
                     }
                     if (lane + 33 <= len) {
-                        const uint4 a = wrand(seed, w, (uint32_t)u, g0, g1, (uint32_t)(lane + 33));
+                        const uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)(lane + 33));
                         const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
                         a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
                     }
@@ -1254,7 +1265,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 if (tt == 0) {
                     double dV = 0.0;
                     for (int q = 0; q < nw; ++q) dV += red[q];
-                    const uint4 ra = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFFu);
+                    const uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
                     s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
                 }
                 team_sync(slot, T);
@@ -1289,7 +1300,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
             } else {
                 const int i = D.i;
                 const float sx = D.sx, sy = D.sy;
-                const uint4 r1 = wrand(seed, w, (uint32_t)u, g0, g1, 0xFFFEu);
+                const uint4 r1 = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFEu);
                 const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
                 KahanF acc;
                 int b = cur;
@@ -1405,20 +1416,20 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
         WalkerAcc& A = accs[w];
         A.esum += esum; A.esumsq += esumsq; A.samples += nsamp; A.bead_updates += nbu;
         A.att[0] += att0; A.att[1] += att1; A.acc[0] += acc0; A.acc[1] += acc1;
-        ctr[w] = sweep0 + sweeps;
+        ctr[w] = sweep0 + min(sweeps, m.max_sweeps);
     }
 }
 
 __global__ void k_walkers_init(const WalkerMeta* __restrict__ meta, float4* __restrict__ pos,
-                               uint64_t seed) {
-    const int w = blockIdx.x;
+                               const int* __restrict__ list) {
+    const int w = list ? list[blockIdx.x] : blockIdx.x;
     const WalkerMeta m = meta[w];
     float4* P = pos + m.off;
     for (int i = threadIdx.x; i < m.N; i += blockDim.x) {
-        uint4 a = wrand(seed, w, (uint32_t)i, 0u, 0u, 0xA0000000u);
+        uint4 a = wrand(m.key, (uint32_t)i, 0u, 0u, 0xA0000000u);
         float cx = m.L * (u01f(a.x) - 0.5f), cy = m.L * (u01f(a.y) - 0.5f), cz = m.L * (u01f(a.z) - 0.5f);
         for (int t = 0; t < m.M; ++t) {
-            uint4 b = wrand(seed, w, (uint32_t)i, (uint32_t)t, 0u, 0xB0000000u);
+            uint4 b = wrand(m.key, (uint32_t)i, (uint32_t)t, 0u, 0xB0000000u);
             float2 z01 = box_muller(b.x, b.y);
             float2 z2 = box_muller(b.z, b.w);
             P[(size_t)t * m.N + i] = make_float4(put_inside(fmaf(m.sig2lt, z01.x, cx), m.L, m.Linv),
@@ -1844,6 +1855,8 @@ int pgb_walkers_create(const pgb_walkers_params* p, pgb_walkers** out) {
                t4 = h->az.C10 * std::pow(rmorc, 7.0) / 7.0;
         double tailV = 2.0 * M_PI * h->az.epsilon * (-h->az.rm * h->az.rm * h->az.rm * (t2 + t3 + t4));
         m.tailV = (1.0 * N * N / (L * L * L)) * tailV;
+        m.key = walker_key(p->seed, w);
+        m.max_sweeps = 0x7fffffff;
         h->meta.push_back(m);
         off += (long long)N * M;
     }
@@ -1910,7 +1923,7 @@ int pgb_walkers_tuning(pgb_walkers* h, int* scheds, float* ms, int cap) {
 
 int pgb_walkers_init(pgb_walkers* h) {
     if (!h) return PGB_EINVAL;
-    k_walkers_init<<<h->W, 128, 0, h->stream>>>(h->d_meta, h->d_pos, h->seed);
+    k_walkers_init<<<h->W, 128, 0, h->stream>>>(h->d_meta, h->d_pos, nullptr);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemsetAsync(h->d_ctr, 0, h->W * sizeof(unsigned long long), h->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->d_acc, 0, h->W * sizeof(WalkerAcc), h->stream);
@@ -2031,6 +2044,363 @@ int pgb_walkers_energy(pgb_walkers* h, int precision, double* out) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return h->cfail(e, "walkers energy");
     h->launches += 1;
+    return PGB_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Serving: continuous batching of simulation jobs.
+//
+// Jobs (N, T, mu, density, sweeps, seed, arrival time) are submitted as they
+// come.  Each round the server (1) moves arrived jobs into a FIFO queue,
+// (2) admits queued jobs while their worldline slab fits the HBM budget and a
+// slot is free, initialises them on the device, (3) advances every active job
+// by up to `sweeps_per_round` sweeps in ONE launch of the packed-team kernel
+// (jobs of all sizes share the launch), (4) reads the per-job accumulators,
+// emits an estimator bin (mean E/N over `bin_sweeps` sweeps) whenever a job
+// completes one, and retires finished jobs, freeing their memory and slot for
+// the next round.  A job's random streams are keyed by its own seed and its
+// team size depends only on its own N and Mbar, so its results are the same
+// alone and in any mix.
+// ===========================================================================
+namespace {
+
+struct ServerJob {
+    pgb_job_spec spec;
+    int state = 0;                 // 0 submitted, 1 queued, 2 active, 3 done
+    double t_admit = -1, t_first_bin = -1, t_done = -1;
+    int slot = -1, N = 0, M = 0, mbar = 0;
+    long long off = -1, beads = 0;
+    long long sweeps_done = 0, samples_bin_start = 0;
+    double esum_bin_start = 0.0;
+    int bins = 0;
+    int sweeps_per_round = 1;      // from the job's own cost only
+    WalkerMeta meta{};
+};
+
+}  // namespace
+
+struct pgb_server {
+    pgb_server_params p{};
+    AzizParams az{};
+    cudaStream_t stream = nullptr;
+    float4* d_arena = nullptr;
+    long long arena_beads = 0;
+    std::map<long long, long long> free_blocks;      // offset -> length (beads)
+    int max_slots = 0;
+    WalkerMeta* d_meta = nullptr;
+    WalkerAcc* d_acc = nullptr;
+    unsigned long long* d_ctr = nullptr;
+    int* d_err = nullptr;
+    int4* d_teams = nullptr;
+    int teams_cap = 0;
+    int* d_list = nullptr;
+    std::vector<WalkerMeta> h_meta;
+    std::vector<int> free_slots;
+    std::vector<int> slot_job;
+    std::vector<ServerJob> jobs;
+    std::deque<int> queue;
+    std::vector<pgb_bin> bins;
+    std::chrono::steady_clock::time_point t0;
+    long long bead_updates = 0, rounds = 0;
+    std::string err;
+    int fail(int code, const std::string& m) { err = m; return code; }
+    int cfail(cudaError_t e, const char* where) {
+        err = std::string("CUDA error ") + cudaGetErrorString(e) + " at " + where;
+        return e == cudaErrorMemoryAllocation ? PGB_ENOMEM : PGB_ECUDA;
+    }
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+    long long alloc(long long n) {
+        for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it) {
+            if (it->second >= n) {
+                long long off = it->first, len = it->second;
+                free_blocks.erase(it);
+                if (len > n) free_blocks[off + n] = len - n;
+                return off;
+            }
+        }
+        return -1;
+    }
+    void release(long long off, long long n) {
+        auto it = free_blocks.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_blocks.end() && it->first + it->second == nx->first) {
+            it->second += nx->second; free_blocks.erase(nx);
+        }
+        if (it != free_blocks.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) { pv->second += it->second; free_blocks.erase(it); }
+        }
+    }
+};
+
+namespace {
+thread_local std::string g_serr;
+}
+
+extern "C" {
+
+const char* pgb_server_last_error(const pgb_server* s) { return s ? s->err.c_str() : g_serr.c_str(); }
+
+int pgb_server_create(const pgb_server_params* p, pgb_server** out) {
+    if (!p || !out || p->hbm_budget_bytes < 1e6 || p->max_active <= 0 || p->sweeps_per_round <= 0 ||
+        p->bin_sweeps <= 0 || p->tau <= 0 || p->lambda <= 0) {
+        g_serr = "server_create: need budget >= 1 MB, max_active > 0, sweeps_per_round > 0, bin_sweeps > 0";
+        return PGB_EINVAL;
+    }
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { g_serr = "no CUDA device available"; return PGB_ECUDA; }
+    pgb_server* s = new pgb_server();
+    s->p = *p;
+    s->az = aziz_params(p->aziz_year);
+    s->max_slots = p->max_active;
+    s->arena_beads = (long long)(p->hbm_budget_bytes / sizeof(float4));
+    s->t0 = std::chrono::steady_clock::now();
+    cudaError_t e;
+    do {
+        if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_arena, (size_t)s->arena_beads * sizeof(float4))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_meta, s->max_slots * sizeof(WalkerMeta))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_acc, s->max_slots * sizeof(WalkerAcc))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_ctr, s->max_slots * sizeof(unsigned long long))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_err, s->max_slots * sizeof(int))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_list, s->max_slots * sizeof(int))) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(s->d_err, 0, s->max_slots * sizeof(int), s->stream)) != cudaSuccess) break;
+        e = cudaStreamSynchronize(s->stream);
+    } while (0);
+    if (e != cudaSuccess) {
+        g_serr = std::string("server_create: ") + cudaGetErrorString(e);
+        pgb_server_destroy(s);
+        return e == cudaErrorMemoryAllocation ? PGB_ENOMEM : PGB_ECUDA;
+    }
+    s->free_blocks[0] = s->arena_beads;
+    s->h_meta.assign(s->max_slots, WalkerMeta{});
+    s->slot_job.assign(s->max_slots, -1);
+    for (int k = s->max_slots - 1; k >= 0; --k) s->free_slots.push_back(k);
+    *out = s;
+    return PGB_OK;
+}
+
+int pgb_server_destroy(pgb_server* s) {
+    if (!s) return PGB_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    cudaFree(s->d_arena); cudaFree(s->d_meta); cudaFree(s->d_acc); cudaFree(s->d_ctr);
+    cudaFree(s->d_err); cudaFree(s->d_teams); cudaFree(s->d_list);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return PGB_OK;
+}
+
+double pgb_server_clock(pgb_server* s) { return s ? s->now() : 0.0; }
+long long pgb_server_bead_updates(pgb_server* s) { return s ? s->bead_updates : 0; }
+
+int pgb_server_submit(pgb_server* s, const pgb_job_spec* j, int* job_id) {
+    if (!s || !j) return PGB_EINVAL;
+    if (j->n < 2 || j->n > 4096 || j->temperature <= 0 || j->density <= 0 || j->sweeps <= 0)
+        return s->fail(PGB_EINVAL, "job: need 2 <= n <= 4096, temperature > 0, density > 0, sweeps > 0");
+    ServerJob job;
+    job.spec = *j;
+    job.N = j->n;
+    const double L = std::pow(1.0 * j->n / j->density, 1.0 / 3.0);
+    // even M from T and tau (setup.cpp:995-1003), Mbar from setup.cpp:1079-1104
+    job.M = 2 * (int)std::lround(1.0 / (2.0 * j->temperature * s->p.tau));
+    if (job.M < 4) return s->fail(PGB_EINVAL, "job: temperature too high for tau (fewer than 4 slices)");
+    const double ell = std::pow(1.0 * j->n / (L * L * L), -1.0 / 3.0);
+    int mb = (int)(ell * ell / (16 * s->p.lambda * s->p.tau));
+    if (mb < 2) mb = 2; else if (mb > job.M) mb = job.M / 2;
+    if (mb % 2) mb++;
+    if (mb >= job.M) mb = job.M - 2;
+    if (mb > kMaxStage) mb = kMaxStage;
+    job.mbar = mb;
+    job.beads = (long long)job.N * job.M;
+    if (job.beads > s->arena_beads)
+        return s->fail(PGB_EINVAL, "job: worldline slab larger than the whole HBM budget");
+    WalkerMeta& m = job.meta;
+    m.N = job.N; m.M = job.M; m.mbar = job.mbar;
+    const int nu = (int)std::ceil(1.0 * job.N * job.M / (1.0 * job.mbar));
+    m.num_updates = nu < 100 ? 100 : nu;
+    m.L = (float)L; m.Linv = (float)(1.0 / L);
+    m.sig2lt = (float)std::sqrt(2.0 * s->p.lambda * s->p.tau);
+    const double T = 1.0 / (job.M * s->p.tau);
+    m.com_delta = (float)(0.04 * 2.0 * std::sqrt(M_PI * s->p.lambda / T));
+    const double rmorc = s->az.rm / L;
+    const double tV = 2.0 * M_PI * s->az.epsilon *
+        (-s->az.rm * s->az.rm * s->az.rm * (s->az.C6 * std::pow(rmorc, 3.0) / 3.0 +
+                                            s->az.C8 * std::pow(rmorc, 5.0) / 5.0 +
+                                            s->az.C10 * std::pow(rmorc, 7.0) / 7.0));
+    m.tailV = (1.0 * job.N * job.N / (L * L * L)) * tV;
+    m.key = (unsigned long long)j->seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    m.max_sweeps = 0;
+    // sweeps per round in inverse proportion to the job's cost N^2 M (a
+    // 64-particle, 125-slice job makes sweeps_per_round), so one large job
+    // does not stretch every round
+    {
+        const double ref = 64.0 * 64.0 * 125.0, cost = (double)job.N * job.N * job.M;
+        job.sweeps_per_round = (int)std::max(1.0, std::min((double)s->p.sweeps_per_round,
+                                                           std::floor(s->p.sweeps_per_round * ref / cost)));
+    }
+    const int id = (int)s->jobs.size();
+    s->jobs.push_back(job);
+    if (job_id) *job_id = id;
+    return PGB_OK;
+}
+
+int pgb_server_step(pgb_server* s, int* n_active, int* n_queued) {
+    if (!s) return PGB_EINVAL;
+    const double now = s->now();
+    for (size_t k = 0; k < s->jobs.size(); ++k)
+        if (s->jobs[k].state == 0 && s->jobs[k].spec.arrival <= now) { s->jobs[k].state = 1; s->queue.push_back((int)k); }
+    // admission: FIFO while a slot and slab memory are free
+    std::vector<int> admitted;
+    while (!s->queue.empty() && !s->free_slots.empty()) {
+        ServerJob& job = s->jobs[s->queue.front()];
+        const long long off = s->alloc(job.beads);
+        if (off < 0) break;
+        job.off = off;
+        job.slot = s->free_slots.back();
+        s->free_slots.pop_back();
+        job.state = 2;
+        job.t_admit = now;
+        job.meta.off = off;
+        s->slot_job[job.slot] = s->queue.front();
+        s->h_meta[job.slot] = job.meta;
+        admitted.push_back(job.slot);
+        s->queue.pop_front();
+    }
+    std::vector<int> active;
+    for (int k = 0; k < s->max_slots; ++k)
+        if (s->slot_job[k] >= 0) {
+            ServerJob& job = s->jobs[s->slot_job[k]];
+            const long long left = job.spec.sweeps - job.sweeps_done;
+            s->h_meta[k].max_sweeps = (int)std::min<long long>(left, job.sweeps_per_round);
+            active.push_back(k);
+        } else {
+            s->h_meta[k].max_sweeps = 0;
+        }
+    cudaError_t e = cudaMemcpyAsync(s->d_meta, s->h_meta.data(), s->max_slots * sizeof(WalkerMeta),
+                                    cudaMemcpyHostToDevice, s->stream);
+    if (e != cudaSuccess) return s->cfail(e, "server meta upload");
+    if (!admitted.empty()) {
+        for (int k : admitted) {
+            cudaMemsetAsync(s->d_acc + k, 0, sizeof(WalkerAcc), s->stream);
+            cudaMemsetAsync(s->d_ctr + k, 0, sizeof(unsigned long long), s->stream);
+        }
+        e = cudaMemcpyAsync(s->d_list, admitted.data(), admitted.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, s->stream);
+        if (e != cudaSuccess) return s->cfail(e, "server admit list");
+        k_walkers_init<<<(int)admitted.size(), 128, 0, s->stream>>>(s->d_meta, s->d_arena, s->d_list);
+        if ((e = cudaGetLastError()) != cudaSuccess) return s->cfail(e, "server init launch");
+    }
+    if (!active.empty()) {
+        // team sizes from each job's own per-move pair count (8 pairs per thread)
+        std::vector<int> idx = active;
+        std::vector<int> tw(s->max_slots, 1);
+        for (int k : active) {
+            const WalkerMeta& m = s->h_meta[k];
+            const double pairs = (double)m.mbar / 2.0 * m.N * 2.0;
+            const int need = (int)std::ceil(pairs / (32.0 * 8));
+            int t = 1;
+            while (t < need && t < 8) t <<= 1;
+            tw[k] = t;
+        }
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+            if (tw[a] != tw[b]) return tw[a] > tw[b];
+            const WalkerMeta &x = s->h_meta[a], &y = s->h_meta[b];
+            return (double)x.N * x.N * x.M > (double)y.N * y.N * y.M;
+        });
+        std::vector<int4> flat;
+        int used = 8;
+        for (int k : idx) {
+            if (used + tw[k] > 8) { flat.resize(flat.size() + 8, make_int4(-1, 0, 0, 0)); used = 0; }
+            // place the team descriptor in the next free entry of this CTA
+            int e8 = 0;
+            while (flat[flat.size() - 8 + e8].w) ++e8;
+            flat[flat.size() - 8 + e8] = make_int4(k, used, tw[k], 1);
+            used += tw[k];
+        }
+        const int nctas = (int)(flat.size() / 8);
+        if ((int)flat.size() > s->teams_cap) {
+            cudaFree(s->d_teams);
+            s->teams_cap = (int)flat.size() * 2;
+            if ((e = cudaMalloc(&s->d_teams, s->teams_cap * sizeof(int4))) != cudaSuccess)
+                return s->cfail(e, "server teams");
+        }
+        if ((e = cudaMemcpyAsync(s->d_teams, flat.data(), flat.size() * sizeof(int4),
+                                 cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+            return s->cfail(e, "server teams upload");
+        k_walkers_team<2><<<nctas, kTeamCta, 0, s->stream>>>(s->d_meta, s->d_teams, s->d_arena,
+            s->d_acc, s->d_ctr, s->p.sweeps_per_round, 1, make_aziz_f(s->az), s->p.tau, s->p.lambda,
+            (float)s->p.p_com, 1, 0);
+        if ((e = cudaGetLastError()) != cudaSuccess) return s->cfail(e, "server round launch");
+    }
+    std::vector<WalkerAcc> acc(s->max_slots);
+    e = cudaMemcpyAsync(acc.data(), s->d_acc, s->max_slots * sizeof(WalkerAcc), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return s->cfail(e, "server round");
+    s->rounds += 1;
+    const double t_end = s->now();
+    for (int k : active) {
+        ServerJob& job = s->jobs[s->slot_job[k]];
+        const long long before = job.sweeps_done;
+        job.sweeps_done = acc[k].samples;       // one energy sample per sweep
+        (void)before;
+        while (acc[k].samples - job.samples_bin_start >= s->p.bin_sweeps) {
+            pgb_bin b;
+            b.job = s->slot_job[k];
+            b.bin = job.bins;
+            b.samples = acc[k].samples - job.samples_bin_start;
+            b.energy_per_particle = (acc[k].esum - job.esum_bin_start) / (double)b.samples;
+            b.time = t_end;
+            s->bins.push_back(b);
+            if (job.bins == 0) job.t_first_bin = t_end;
+            job.bins += 1;
+            job.samples_bin_start = acc[k].samples;
+            job.esum_bin_start = acc[k].esum;
+        }
+        if (job.sweeps_done >= job.spec.sweeps) {
+            job.state = 3;
+            job.t_done = t_end;
+            s->bead_updates += acc[k].bead_updates;
+            s->release(job.off, job.beads);
+            s->free_slots.push_back(k);
+            s->slot_job[k] = -1;
+        }
+    }
+    // bead updates of active jobs so far are counted when they retire; add the
+    // running total of still-active jobs for throughput reports
+    if (n_active) { int c = 0; for (int k = 0; k < s->max_slots; ++k) c += (s->slot_job[k] >= 0); *n_active = c; }
+    if (n_queued) *n_queued = (int)s->queue.size();
+    return PGB_OK;
+}
+
+int pgb_server_poll_bins(pgb_server* s, pgb_bin* out, int cap, int* n) {
+    if (!s || !n) return PGB_EINVAL;
+    const int k = std::min<int>(cap, (int)s->bins.size());
+    if (out) for (int i = 0; i < k; ++i) out[i] = s->bins[i];
+    s->bins.erase(s->bins.begin(), s->bins.begin() + k);
+    *n = k;
+    return PGB_OK;
+}
+
+int pgb_server_job_info(pgb_server* s, int id, pgb_job_info* out) {
+    if (!s || !out || id < 0 || id >= (int)s->jobs.size()) return PGB_EINVAL;
+    const ServerJob& j = s->jobs[id];
+    out->state = j.state; out->arrival = j.spec.arrival; out->admitted = j.t_admit;
+    out->first_bin = j.t_first_bin; out->completed = j.t_done; out->sweeps_done = j.sweeps_done;
+    out->n = j.N; out->m = j.M; out->bytes = (size_t)j.beads * sizeof(float4);
+    return PGB_OK;
+}
+
+int pgb_server_active_bead_updates(pgb_server* s, long long* total) {
+    if (!s || !total) return PGB_EINVAL;
+    std::vector<WalkerAcc> acc(s->max_slots);
+    cudaError_t e = cudaMemcpy(acc.data(), s->d_acc, s->max_slots * sizeof(WalkerAcc), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return s->cfail(e, "server accumulators");
+    long long t = s->bead_updates;
+    for (int k = 0; k < s->max_slots; ++k) if (s->slot_job[k] >= 0) t += acc[k].bead_updates;
+    *total = t;
     return PGB_OK;
 }
 

@@ -237,3 +237,29 @@ def test_walkers_run_and_energy(pgb):
     W2.run(2, measure=1)
     assert [s["accepted"] for s in W2.stats()] == [s["accepted"] for s in st]
     assert np.array_equal(W2.positions(0), W.positions(0))
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (1, 2e-4)])
+def test_trial_displacements(pgb, oracle_lib, small, precision, tol):
+    """Independent single-bead trial moves: delta U against the oracle's
+    before/after potentialAction(bead)."""
+    d = small
+    a, o = make_pair(pgb, oracle_lib, d["cfg"], d["L"], d["m"], d["n"], d["tau"], d["lam"],
+                     action="gsf", precision=precision)
+    rng = np.random.default_rng(11)
+    beads = random_beads(rng, d["m"], d["n"], 30)
+    pos = d["cfg"]["pos"][beads[:, 0], beads[:, 1]] + rng.uniform(-0.3, 0.3, (30, 3))
+    pos -= d["L"] * np.floor(pos / d["L"] + 0.5)
+    got = a.trial_actions(beads, pos)
+    want, scale = [], []
+    for (s_, p_), r in zip(beads, pos):
+        u0 = o.bead_action(int(s_), int(p_))
+        old = d["cfg"]["pos"][s_, p_].copy()
+        o.update_bead(int(s_), int(p_), r)
+        u1 = o.bead_action(int(s_), int(p_))
+        want.append(u1 - u0)
+        o.update_bead(int(s_), int(p_), old)
+        # the error of a difference is relative to the larger of its terms
+        scale.append(max(abs(u0), abs(u1), 1.0))
+    want = np.array(want)
+    assert np.max(np.abs(got - want) / np.array(scale)) <= tol

@@ -1,0 +1,69 @@
+"""Continuous-batching server: admission by HBM footprint, overlapping jobs in
+shared launches, bins streamed back, and each job's results identical alone
+and in a mix (its streams are keyed by its own seed and its team size depends
+only on its own N and Mbar, so the comparison is exact)."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(server, ids, timeout=120.0):
+    t0 = time.time()
+    bins = []
+    while time.time() - t0 < timeout:
+        server.step()
+        bins += server.bins()
+        if all(server.job(j)["state"] == 3 for j in ids):
+            return bins
+    raise AssertionError("jobs did not finish")
+
+
+def test_job_same_alone_and_in_mix(pgb):
+    X = dict(n=24, temperature=2.0, sweeps=60, seed=5)
+    alone = pgb.Server(2e9, sweeps_per_round=10, bin_sweeps=20)
+    jx = alone.submit(**X)
+    b_alone = [b for b in _run(alone, [jx]) if b["job"] == jx]
+    assert len(b_alone) == 3
+
+    mix = pgb.Server(2e9, sweeps_per_round=10, bin_sweeps=20)
+    rng = np.random.default_rng(0)
+    others = []
+    for k in range(6):
+        others.append(mix.submit(n=int(rng.integers(8, 64)), temperature=float(rng.uniform(1, 4)),
+                                 sweeps=int(rng.integers(20, 90)), seed=100 + k))
+    jm = mix.submit(**X)
+    for k in range(6):   # late arrivals join while the others run
+        others.append(mix.submit(n=int(rng.integers(8, 96)), temperature=float(rng.uniform(1, 4)),
+                                 sweeps=40, seed=200 + k, arrival=0.02 * (k + 1)))
+    bins = _run(mix, others + [jm])
+    b_mix = [b for b in bins if b["job"] == jm]
+    assert [b["energy"] for b in b_mix] == [b["energy"] for b in b_alone]
+    assert all(np.isfinite(b["energy"]) for b in bins)
+
+
+def test_admission_by_memory_budget(pgb):
+    # each job: N=128, T=1 -> M=250 -> 128*250*16 B = 512 KB; the budget holds two
+    s = pgb.Server(1.2e6, max_active=16, sweeps_per_round=5, bin_sweeps=10)
+    ids = [s.submit(n=128, temperature=1.0, sweeps=10, seed=k) for k in range(5)]
+    peak = 0
+    t0 = time.time()
+    while time.time() - t0 < 120:
+        active, queued = s.step()
+        peak = max(peak, active)
+        if all(s.job(j)["state"] == 3 for j in ids):
+            break
+    assert peak == 2
+    for j in ids:
+        info = s.job(j)
+        assert info["state"] == 3 and info["sweeps_done"] == 10
+        assert info["arrival"] <= info["admitted"] <= info["first_bin"] <= info["completed"]
+    assert s.bead_updates() > 0
+
+
+def test_oversized_job_rejected(pgb):
+    s = pgb.Server(1e6, sweeps_per_round=5, bin_sweeps=10)
+    with pytest.raises(pgb.PgbError):
+        s.submit(n=512, temperature=0.5, sweeps=10, seed=1)
