@@ -235,7 +235,7 @@ def plain_form_rate(pgb, n=64, t=2.0, tau=0.004, steps=1):
 # load far exceeds capacity, so the window is bounded and the report states
 # how many jobs reached a first bin / completed (the rest are censored).
 # ---------------------------------------------------------------------------
-def serving_run(pgb, seconds=12.0, rate=50.0, seed=0):
+def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02):
     rng = np.random.Generator(np.random.Philox(seed))
     arrivals = []
     t = 0.0
@@ -244,7 +244,7 @@ def serving_run(pgb, seconds=12.0, rate=50.0, seed=0):
         if t > 0.6 * seconds:
             break
         arrivals.append(t)
-    srv = pgb.Server(150e9, max_active=1024, sweeps_per_round=10, bin_sweeps=100)
+    srv = pgb.Server(150e9, max_active=1024, bin_sweeps=100, round_seconds=round_seconds)
     ids = []
     for k, ta in enumerate(arrivals):
         n = int(round(math.exp(rng.uniform(math.log(8), math.log(512)))))
@@ -278,7 +278,8 @@ def serving_run(pgb, seconds=12.0, rate=50.0, seed=0):
             "completion_p50_s": pct(done, 50), "completion_p99_s": pct(done, 99),
             "note": "Poisson 50 jobs/s for %.1f s of a %.1f s window; percentiles over jobs that "
                     "reached the event inside the window (the others are censored); canonical "
-                    "chains (staging + COM), bins of 100 sweeps" % (0.6 * seconds, seconds)}
+                    "chains (staging + COM), bins of 100 sweeps, rounds of %g s of device time"
+                    % (0.6 * seconds, seconds, round_seconds)}
 
 
 def run_serving(args, pgb):

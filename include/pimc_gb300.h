@@ -268,10 +268,13 @@ typedef struct {
     int    sweeps_per_round;   /* sweeps per round of a 64-particle, 125-slice job;
                                   a job of cost N^2 M makes this times 64^2 125/(N^2 M),
                                   at least 1 and at most sweeps_per_round */
-    int    bin_sweeps;         /* a bin closes at the first round end after this many sweeps */
+    int    bin_sweeps;         /* sweeps per estimator bin (the last bin holds the remainder) */
     double tau, lambda;
     double p_com;
     int    aziz_year;
+    double round_seconds;      /* > 0: every job runs for this much device time per round,
+                                  stopping and resuming between moves (sweeps_per_round
+                                  then unused); 0: sweeps_per_round as above */
 } pgb_server_params;
 typedef struct {
     int       n;               /* particles N0 */

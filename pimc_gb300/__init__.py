@@ -331,11 +331,11 @@ class Server:
     estimator bins back."""
 
     def __init__(self, hbm_budget_bytes, max_active=1024, sweeps_per_round=10, bin_sweeps=100,
-                 tau=0.004, lam=None, p_com=0.05, aziz_year=1979):
+                 tau=0.004, lam=None, p_com=0.05, aziz_year=1979, round_seconds=0.0):
         self.lib = _lib.load()
         lam = worldlines.LAMBDA_HE4 if lam is None else lam
         p = _lib.PgbServerParams(float(hbm_budget_bytes), max_active, sweeps_per_round, bin_sweeps,
-                                 tau, lam, p_com, aziz_year)
+                                 tau, lam, p_com, aziz_year, float(round_seconds))
         h = C.c_void_p()
         rc = self.lib.pgb_server_create(C.byref(p), C.byref(h))
         if rc != 0:

@@ -58,7 +58,8 @@ class PgbMoveStats(C.Structure):
 class PgbServerParams(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int),
                 ("sweeps_per_round", C.c_int), ("bin_sweeps", C.c_int), ("tau", C.c_double),
-                ("lambda_", C.c_double), ("p_com", C.c_double), ("aziz_year", C.c_int)]
+                ("lambda_", C.c_double), ("p_com", C.c_double), ("aziz_year", C.c_int),
+                ("round_seconds", C.c_double)]
 
 
 class PgbJobSpec(C.Structure):

@@ -212,6 +212,7 @@ int pgb_destroy(pgb_ctx* h) {
     cudaFree(c.d_pos); cudaFree(c.d_pos32); cudaFree(c.d_next); cudaFree(c.d_prev);
     cudaFree(c.d_on); cudaFree(c.d_nbs);
     if (c.d_scratch) cudaFree(c.d_scratch);
+    if (c.d_tc_tables) cudaFree(c.d_tc_tables);
     if (c.h_pinned) cudaFreeHost(c.h_pinned);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
@@ -704,9 +705,15 @@ int scatter_common(Ctx& c, const double* d_q, int nq, int what, int mode, double
             if (what == 0) e = launch_ssf_from_rho32(d_rho, nq, c.M, norm, d_out, c.stream);
             else if (mode == 1) {
                 if (!isf_tc_supported(c.M))
-                    return c.fail(PGB_EINVAL, "tensor-core F(q,tau) needs M a multiple of 128 and <= 1024");
+                    return c.fail(PGB_EINVAL, "tensor-core F(q,tau) needs M a multiple of 128 and <= 2048");
+                if (!c.d_tc_tables) {
+                    e = cudaMalloc(&c.d_tc_tables, isf_tc_table_bytes(c.M));
+                    if (e != cudaSuccess) { c.d_tc_tables = nullptr; return c.cuda_fail(e, "cudaMalloc(F(q,tau) tables)"); }
+                    e = isf_tc_build_tables(c.M, c.d_tc_tables, c.stream);
+                    if (e != cudaSuccess) return c.cuda_fail(e, "F(q,tau) tables");
+                }
                 void* tc = static_cast<char*>(d_work) + (((size_t)nq * c.M * sizeof(float2) + 255) & ~(size_t)255);
-                e = launch_isf_tc(d_rho, nq, c.M, norm, d_out, tc, c.stream);
+                e = launch_isf_tc(d_rho, nq, c.M, norm, d_out, tc, c.d_tc_tables, c.stream);
             } else e = launch_isf_direct32(d_rho, nq, c.M, norm, d_out, c.stream);
         }
     }

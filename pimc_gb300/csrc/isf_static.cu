@@ -70,25 +70,7 @@ k_rhoq32_aos(const double* __restrict__ beads, int M, int N, int Ne, double3 sid
     const float nx = (float)(q[3 * iq] * side.x * inv2pi);
     const float ny = (float)(q[3 * iq + 1] * side.y * inv2pi);
     const float nz = (float)(q[3 * iq + 2] * side.z * inv2pi);
-    double re = 0.0, im = 0.0;
-    int j = 0;
-    while (j < N) {
-        float cr = 0.f, ci = 0.f;
-        int jend = min(N, j + 32);
-        for (; j < jend; ++j) {
-            float4 u = su[j];
-            float fx = fmaf(nx, u.x, -rintf(nx * u.x));
-            float fy = fmaf(ny, u.y, -rintf(ny * u.y));
-            float fz = fmaf(nz, u.z, -rintf(nz * u.z));
-            float f = fx + fy + fz;
-            f -= rintf(f);
-            float sn, cs;
-            __sincosf(6.28318530717958647692f * f, &sn, &cs);
-            cr += cs; ci += sn;
-        }
-        re += cr; im += ci;
-    }
-    rho[(size_t)iq * M + t] = make_float2((float)re, (float)im);
+    rho[(size_t)iq * M + t] = rho_partial(su, N, nx, ny, nz);
 }
 
 }  // namespace

@@ -265,9 +265,10 @@ __global__ void k_prep_cos(int M, int colpad, __nv_bfloat16* Bh, __nv_bfloat16* 
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// per-call scratch: the split rho matrix, P and its split, the error flag
 struct Layout {
     int qpad, colpad2;
-    size_t a1, b1, p, a2, b2, err, total;
+    size_t a1, p, a2, err, total;
 };
 
 Layout layout(int nq, int M) {
@@ -276,13 +277,27 @@ Layout layout(int nq, int M) {
     L.colpad2 = ((M / 2 + 1 + kTN - 1) / kTN) * kTN;
     size_t off = 0;
     L.a1 = off; off = align256(off + (size_t)L.qpad * 2 * M * 2 * sizeof(__nv_bfloat16));
-    L.b1 = off; off = align256(off + (size_t)4 * M * M * 2 * sizeof(__nv_bfloat16));
     L.p = off;  off = align256(off + (size_t)L.qpad * M * sizeof(float));
     L.a2 = off; off = align256(off + (size_t)L.qpad * M * 2 * sizeof(__nv_bfloat16));
-    L.b2 = off; off = align256(off + (size_t)L.colpad2 * M * 2 * sizeof(__nv_bfloat16));
     L.err = off; off = align256(off + sizeof(int));
     L.total = off;
     return L;
+}
+
+// fixed matrices of one M: the DFT (B1) and the cosines (B2), each split
+struct Tables {
+    int colpad2;
+    size_t b1, b2, total;
+};
+
+Tables tables(int M) {
+    Tables T;
+    T.colpad2 = ((M / 2 + 1 + kTN - 1) / kTN) * kTN;
+    size_t off = 0;
+    T.b1 = off; off = align256(off + (size_t)4 * M * M * 2 * sizeof(__nv_bfloat16));
+    T.b2 = off; off = align256(off + (size_t)T.colpad2 * M * 2 * sizeof(__nv_bfloat16));
+    T.total = off;
+    return T;
 }
 
 }  // namespace
@@ -291,20 +306,39 @@ bool isf_tc_supported(int M) { return M >= 128 && M <= 2048 && (M % 128) == 0; }
 
 size_t isf_tc_scratch_bytes(int nq, int M) { return layout(nq, M).total; }
 
+size_t isf_tc_table_bytes(int M) { return tables(M).total; }
+
+// The DFT and cosine matrices depend on M alone: a context builds them once
+// (FP64 sincospi, then split to BF16 pairs) and every F(q,tau) reuses them.
+cudaError_t isf_tc_build_tables(int M, void* d_tables, cudaStream_t s) {
+    if (!isf_tc_supported(M)) return cudaErrorInvalidValue;
+    const Tables T = tables(M);
+    char* base = static_cast<char*>(d_tables);
+    auto* b1h = reinterpret_cast<__nv_bfloat16*>(base + T.b1);
+    auto* b1l = b1h + (size_t)4 * M * M;
+    auto* b2h = reinterpret_cast<__nv_bfloat16*>(base + T.b2);
+    auto* b2l = b2h + (size_t)T.colpad2 * M;
+    k_prep_dft<<<152 * 4, 256, 0, s>>>(M, b1h, b1l);
+    k_prep_cos<<<152 * 2, 256, 0, s>>>(M, T.colpad2, b2h, b2l);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_isf_tc(const float2* d_rho, int nq, int M, double norm, double* d_out,
-                          void* d_scratch, cudaStream_t s) {
-    if (!isf_tc_supported(M) || nq <= 0) return cudaErrorInvalidValue;
+                          void* d_scratch, const void* d_tables, cudaStream_t s) {
+    if (!isf_tc_supported(M) || nq <= 0 || !d_tables) return cudaErrorInvalidValue;
     const Layout L = layout(nq, M);
+    const Tables T = tables(M);
     char* base = static_cast<char*>(d_scratch);
     auto* a1h = reinterpret_cast<__nv_bfloat16*>(base + L.a1);
     auto* a1l = a1h + (size_t)L.qpad * 2 * M;
-    auto* b1h = reinterpret_cast<__nv_bfloat16*>(base + L.b1);
+    const char* tb = static_cast<const char*>(d_tables);
+    auto* b1h = reinterpret_cast<const __nv_bfloat16*>(tb + T.b1);
     auto* b1l = b1h + (size_t)4 * M * M;
     auto* P = reinterpret_cast<float*>(base + L.p);
     auto* a2h = reinterpret_cast<__nv_bfloat16*>(base + L.a2);
     auto* a2l = a2h + (size_t)L.qpad * M;
-    auto* b2h = reinterpret_cast<__nv_bfloat16*>(base + L.b2);
-    auto* b2l = b2h + (size_t)L.colpad2 * M;
+    auto* b2h = reinterpret_cast<const __nv_bfloat16*>(tb + T.b2);
+    auto* b2l = b2h + (size_t)T.colpad2 * M;
     int* err = reinterpret_cast<int*>(base + L.err);
     static bool attr = false;
     if (!attr) {
@@ -314,8 +348,6 @@ cudaError_t launch_isf_tc(const float2* d_rho, int nq, int M, double norm, doubl
     }
     cudaMemsetAsync(err, 0, sizeof(int), s);
     k_prep_rho<<<152 * 4, 256, 0, s>>>(d_rho, nq, M, L.qpad, a1h, a1l);
-    k_prep_dft<<<152 * 4, 256, 0, s>>>(M, b1h, b1l);
-    k_prep_cos<<<152 * 2, 256, 0, s>>>(M, L.colpad2, b2h, b2l);
     // GEMM 1: [qpad x 2M] x [2M x 2M] -> P [qpad x M]
     dim3 g1(2 * M / kTN, L.qpad / kTM);
     k_gemm_split_bf16<<<g1, kThreads, kSmem, s>>>(a1h, a1l, b1h, b1l, 2 * M, 0, P, M, nullptr, 0,

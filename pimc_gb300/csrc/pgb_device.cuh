@@ -177,6 +177,27 @@ struct KahanF {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// Sum over the warp of the lanes' Kahan accumulators without the FP64 pipe:
+// each butterfly step adds the leading parts with an error-free TwoSum
+// (Knuth) and carries the error with the trailing parts, so the pair
+// (hi, lo) keeps about 48 bits; it is rounded to FP64 once.  TwoSum's error
+// term is exact whichever operand comes first, so every lane ends with the
+// same bits.
+__device__ __forceinline__ double warp_sum_ff(const KahanF& k) {
+    float hi = k.s, lo = -k.c;
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+        const float sum = hi + h2;
+        const float bp = sum - hi;
+        const float err = (hi - (sum - bp)) + (h2 - bp);
+        hi = sum;
+        lo = (lo + l2) + err;
+    }
+    return (double)hi + (double)lo;
+}
+
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based RNG.
 // ---------------------------------------------------------------------------
@@ -190,6 +211,53 @@ __device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
     }
     return c;
 }
+// Round to nearest (ties to even) for |x| < 2^22 with two FP32 adds: adding
+// and removing 1.5 * 2^23 drops the fraction bits.  Unlike rintf this stays
+// on the FMA/ALU pipes; __fadd_rn/__fsub_rn are never contracted or
+// reassociated.
+__device__ __forceinline__ float rint_add(float x) {
+    return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
+}
+
+// sum_j exp(2 pi i n . u_j) over the n beads su[0..n) (u = r / L per
+// dimension, turns), for one wave vector n = q L / 2 pi.  The phase is
+// reduced in turns per dimension with an exact FMA remainder,
+//     frac_d = fma(n_d, u_d, -rint(n_d u_d)),
+// then once more after the sum, so __sincosf always sees |angle| <= pi.
+// 32-bead partial sums are added with Kahan compensation.
+__device__ __forceinline__ float2 rho_partial(const float4* __restrict__ su, int n, float nx,
+                                              float ny, float nz) {
+    KahanF re, im;
+    int j = 0;
+    while (j < n) {
+        float cr = 0.f, ci = 0.f;
+        const int jend = min(n, j + 32);
+        #pragma unroll 4
+        for (; j < jend; ++j) {
+            const float4 u = su[j];
+            const float fx = fmaf(nx, u.x, -rint_add(nx * u.x));
+            const float fy = fmaf(ny, u.y, -rint_add(ny * u.y));
+            const float fz = fmaf(nz, u.z, -rint_add(nz * u.z));
+            float f = fx + fy + fz;
+            f -= rint_add(f);
+            float sn, cs;
+            __sincosf(6.28318530717958647692f * f, &sn, &cs);
+            cr += cs;
+            ci += sn;
+        }
+        re.add(cr);
+        im.add(ci);
+    }
+    return make_float2(re.s - re.c, im.s - im.c);
+}
+
+// Nanoseconds of the GPU's global timer (PTX %globaltimer).
+__device__ __forceinline__ unsigned long long gtimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ float u01f(uint32_t x) {          // [0,1)
     return (float)(x >> 8) * (1.0f / 16777216.0f);
 }

@@ -68,6 +68,7 @@ struct Ctx {
     bool loaded = false;
     // scratch (grown on demand)
     void* d_scratch = nullptr; size_t scratch_bytes = 0;
+    void* d_tc_tables = nullptr;   // split-BF16 DFT and cosine matrices of this M (built once)
     void* h_pinned = nullptr; size_t pinned_bytes = 0;
     // plain-form generator state (MT19937)
     std::vector<uint32_t> mt_state;
@@ -126,8 +127,10 @@ cudaError_t launch_isf_direct32(const float2* d_rho, int nq, int M, double norm,
                                 double* d_out, cudaStream_t s);
 // isf_tc.cu (tcgen05 split-BF16 DFT correlation)
 size_t isf_tc_scratch_bytes(int nq, int M);
+size_t isf_tc_table_bytes(int M);
+cudaError_t isf_tc_build_tables(int M, void* d_tables, cudaStream_t s);
 cudaError_t launch_isf_tc(const float2* d_rho, int nq, int M, double norm,
-                          double* d_out, void* d_scratch, cudaStream_t s);
+                          double* d_out, void* d_scratch, const void* d_tables, cudaStream_t s);
 bool isf_tc_supported(int M);
 
 }  // namespace pgb

@@ -12,11 +12,11 @@
 namespace pgb {
 
 // One CTA = one slice t x 256 q-vectors; each thread owns one q and streams
-// the slice's beads from shared memory (broadcast reads).  The phase is
-// reduced in turns, per dimension, with an exact FMA remainder:
-//     q . r / 2pi = sum_d n_d u_d,   n_d = q_d L_d / 2pi,  u_d = r_d / L_d,
-//     frac_d = fma(n_d, u_d, -rint(n_d u_d))
-// so that __sincosf always sees |angle| <= pi.
+// the slice's beads from shared memory (broadcast reads) through
+// rho_partial: q . r / 2pi = sum_d n_d u_d with n_d = q_d L_d / 2pi and
+// u_d = r_d / L_d, reduced in turns so that __sincosf sees |angle| <= pi.
+// Rounding runs on the FP32 add pipe, leaving the special-function pipe to
+// the sine and cosine alone.
 constexpr int kRhoBlock = 256;
 
 __global__ void __launch_bounds__(kRhoBlock)
@@ -35,25 +35,7 @@ k_rhoq32(PathView v, const double* __restrict__ q, int nq, float2* __restrict__ 
     const float nx = (float)(q[3*iq] * v.side[0] * inv2pi);
     const float ny = (float)(q[3*iq+1] * v.side[1] * inv2pi);
     const float nz = (float)(q[3*iq+2] * v.side[2] * inv2pi);
-    double re = 0.0, im = 0.0;
-    int j = 0;
-    while (j < n) {
-        float cr = 0.f, ci = 0.f;
-        int jend = min(n, j + 32);
-        for (; j < jend; ++j) {
-            float4 u = su[j];
-            float fx = fmaf(nx, u.x, -rintf(nx * u.x));
-            float fy = fmaf(ny, u.y, -rintf(ny * u.y));
-            float fz = fmaf(nz, u.z, -rintf(nz * u.z));
-            float f = fx + fy + fz;
-            f -= rintf(f);
-            float sn, cs;
-            __sincosf(6.28318530717958647692f * f, &sn, &cs);
-            cr += cs; ci += sn;
-        }
-        re += cr; im += ci;
-    }
-    rho[(size_t)iq * v.M + t] = make_float2((float)re, (float)im);
+    rho[(size_t)iq * v.M + t] = rho_partial(su, n, nx, ny, nz);
 }
 
 cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* d_rho,

@@ -268,6 +268,25 @@ k_walkers_run(const WalkerMeta* __restrict__ meta, const int* __restrict__ order
 // bridge built by one warp with shuffle scans (the same free-particle
 // distribution as the sequential staging construction, move.cpp:263-292).
 // ---------------------------------------------------------------------------
+// Metropolis test of the FP64 log acceptance ratio a = -tau dV against a
+// uniform x in [0,1): accept when a >= 0 or x < exp(a).  An FP32 screen on
+// a - log(x) decides every case farther than 1e-3 from the boundary (the
+// screen's own error is at most about 1e-5 there, as |a| <= 37), and
+// the exact FP64 comparison decides the rest, so the outcome is that of the
+// FP64 test.
+__device__ __forceinline__ bool metropolis(double dV, double tau, uint32_t hi, uint32_t lo) {
+    const double x = u01d(hi, lo);
+    const double a = -(tau * dV);
+    if (a >= 0.0) return true;
+    if (x > 0.0) {
+        // FP32 screen; exact FP64 test only near the boundary
+        const float d = (float)a - __logf((float)x);
+        if (d > 1e-3f) return true;
+        if (d < -1e-3f) return false;
+    }
+    return x < exp(a);
+}
+
 constexpr int kTeamCta = 256;
 
 __device__ __forceinline__ void team_sync(int slot, int nthreads) {
@@ -289,11 +308,13 @@ __global__ void __launch_bounds__(kTeamCta, MINB)
 k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
                float4* __restrict__ pos, WalkerAcc* __restrict__ accs,
                unsigned long long* __restrict__ ctr, int sweeps, int measure, AzizF az,
-               double tau, double lambda, float p_com, int var_updates, uint64_t seed) {
+               double tau, double lambda, float p_com, int var_updates, uint64_t seed,
+               unsigned long long budget_ns, int* __restrict__ upos) {
     __shared__ float4 s_new[8][2][kMaxStage];
     __shared__ float4 s_old[8][2][kMaxStage];
     __shared__ double s_red[8][8];
     __shared__ int s_acc[8];
+    __shared__ int s_stop[8];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int4 tm = make_int4(-1, 0, 0, 0);
     #pragma unroll
@@ -320,11 +341,21 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
     const int j0 = (T >= N) ? ((tt < G * N) ? tt % N : N) : tt;
     const int kb0 = (T >= N) ? tt / N : 0;
     const int jstep = (T >= N) ? N : T;
-
-    for (int sw = 0; sw < min(sweeps, m.max_sweeps); ++sw) {
+    // Resumable rounds (upos != null): the walker continues from move upos[w]
+    // of sweep ctr[w], and with budget_ns > 0 the team stops after the first
+    // move that ends later than budget_ns after the team started.  Draws are
+    // indexed by (sweep, move), so a chain is the same however its moves are
+    // split over launches, and each energy sample is added to the
+    // accumulator in sample order.
+    const unsigned long long t_start = (tt == 0 && budget_ns) ? gtimer_ns() : 0ull;
+    const int nsw = min(sweeps, m.max_sweeps);
+    int u = upos ? upos[w] : 0;
+    int sw = 0;
+    while (sw < nsw) {
         const unsigned long long gs = sweep0 + sw;
         const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
-        for (int u = 0; u < m.num_updates; ++u) {
+        int stop = 0;
+        for (; u < m.num_updates; ++u) {
             uint4 r0 = wrand(m.key, (uint32_t)u, g0, g1, 0u);
             const bool com = u01f(r0.x) < p_com;
             const int i = (int)(((unsigned long long)r0.z * (unsigned)N) >> 32);
@@ -407,19 +438,19 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                         acc.add(vn - vo);
                     }
                 }
-                double part = warp_sum(acc.value());
+                double part = warp_sum_ff(acc);
                 if (lane == 0) red[wi] = part;
                 team_sync(slot, T);
                 if (tt == 0) {
                     double dV = 0.0;
                     for (int q = 0; q < nw; ++q) dV += red[q];
                     uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
-                    const double x = u01d(ra.x, ra.y);
-                    const double a = -(tau * dV);
-                    s_acc[slot] = (a >= 0.0 || x < exp(a)) ? 1 : 0;
+                    s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
+                    s_stop[slot] = (budget_ns && gtimer_ns() - t_start > budget_ns) ? 1 : 0;
                 }
                 team_sync(slot, T);
                 const int ok = s_acc[slot];
+                stop = s_stop[slot];
                 if (wi == 0 && ok) {
                     for (int k2 = lane; k2 < nmove; k2 += 32) {
                         int sl = s0 + 1 + k2; if (sl >= M) sl -= M;
@@ -452,18 +483,18 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                         acc.add(vn - vo);
                     }
                 }
-                double part = warp_sum(acc.value());
+                double part = warp_sum_ff(acc);
                 if (lane == 0) red[wi] = part;
                 team_sync(slot, T);
                 if (tt == 0) {
                     double dV = 0.0;
                     for (int q = 0; q < nw; ++q) dV += red[q];
-                    const double x = u01d(r1.y, r1.z);
-                    const double a = -(tau * dV);
-                    s_acc[slot] = (a >= 0.0 || x < exp(a)) ? 1 : 0;
+                    s_acc[slot] = metropolis(dV, tau, r1.y, r1.z) ? 1 : 0;
+                    s_stop[slot] = (budget_ns && gtimer_ns() - t_start > budget_ns) ? 1 : 0;
                 }
                 team_sync(slot, T);
                 const int ok = s_acc[slot];
+                stop = s_stop[slot];
                 if (ok)
                     for (int t2 = tt; t2 < M; t2 += T) {
                         float4 pi = P[(size_t)t2 * N + i];
@@ -475,7 +506,9 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 team_sync(slot, T);
                 att0 += 1; acc0 += ok; nbu += M;
             }
+            if (stop) { ++u; break; }
         }
+        if (u < m.num_updates) break;               // stopped inside the sweep
         if (measure > 0 && ((gs + 1) % (unsigned long long)measure) == 0) {
             team_sync(slot, T);
             KahanF pot, kin;
@@ -513,16 +546,25 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 for (int q = 0; q < nw; ++q) K2 += red[q];
                 const double totK = 1.5 * N / tau - K2 * ((0.25 / (lambda * tau)) / (tau * M));
                 const double e = (totK + V / M + m.tailV) / N;
-                esum += e; esumsq += e * e; nsamp += 1;
+                if (upos) {
+                    WalkerAcc& A = accs[w];
+                    A.esum += e; A.esumsq += e * e; A.samples += 1;
+                } else {
+                    esum += e; esumsq += e * e; nsamp += 1;
+                }
             }
             team_sync(slot, T);
         }
+        ++sw;
+        u = 0;
+        if (stop) break;
     }
     if (tt == 0) {
         WalkerAcc& A = accs[w];
         A.esum += esum; A.esumsq += esumsq; A.samples += nsamp; A.bead_updates += nbu;
         A.att[0] += att0; A.att[1] += att1; A.acc[0] += acc0; A.acc[1] += acc1;
-        ctr[w] = sweep0 + min(sweeps, m.max_sweeps);
+        ctr[w] = sweep0 + sw;
+        if (upos) upos[w] = u;
     }
 }
 
@@ -540,18 +582,6 @@ k_walkers_team(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
 // min(1, exp(-dU)) and detailed balance; a sweep makes the same number of
 // staging and centre-of-mass moves as the sequential loop in expectation.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool metropolis(double dV, double tau, uint32_t hi, uint32_t lo) {
-    const double x = u01d(hi, lo);
-    const double a = -(tau * dV);
-    if (a >= 0.0) return true;
-    if (x > 0.0) {
-        // FP32 screen; exact FP64 test only near the boundary
-        const float d = (float)a - __logf((float)x);
-        if (d > 1e-3f) return true;
-        if (d < -1e-3f) return false;
-    }
-    return x < exp(a);
-}
 
 template <int MINB>
 __global__ void __launch_bounds__(kTeamCta, MINB)
@@ -677,7 +707,7 @@ k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ 
                                 aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
                     }
                 }
-                const double dV = warp_sum(acc.value());
+                const double dV = warp_sum_ff(acc);
                 int ok = 0;
                 if (lane == 0) {
                     const uint4 ra = wrand(m.key, c0, g0, g1, 0xFFFFu);
@@ -716,7 +746,7 @@ k_walkers_windows(const WalkerMeta* __restrict__ meta, const int4* __restrict__ 
                 acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
                         aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
             }
-            const double part = warp_sum(acc.value());
+            const double part = warp_sum_ff(acc);
             if (lane == 0) red[wi] = part;
             team_sync(slot, T);
             if (tt == 0) {
@@ -970,7 +1000,7 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
                                 aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
                     }
                 }
-                const double part = warp_sum(acc.value());
+                const double part = warp_sum_ff(acc);
                 if (lane == 0) red[wi] = part;
                 team_sync(slot, T);
                 if (tt == 0) {
@@ -1020,7 +1050,7 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
                     }
                     team_sync(slot, T);            // buffer free for the next chunk
                 }
-                const double part = warp_sum(acc.value());
+                const double part = warp_sum_ff(acc);
                 if (lane == 0) red[wi] = part;
                 team_sync(slot, T);
                 if (tt == 0) {
@@ -1259,7 +1289,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                                 aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
                     }
                 }
-                const double part = warp_sum(acc.value());
+                const double part = warp_sum_ff(acc);
                 if (lane == 0) red[wi] = part;
                 team_sync(slot, T);
                 if (tt == 0) {
@@ -1330,7 +1360,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                     b ^= 1;
                 }
                 cur = b;
-                const double part = warp_sum(acc.value());
+                const double part = warp_sum_ff(acc);
                 if (lane == 0) red[wi] = part;
                 team_sync(slot, T);
                 if (tt == 0) {
@@ -1727,11 +1757,11 @@ cudaError_t launch_run(pgb_walkers* h, int sched, int sweeps, int measure) {
         if (sched >= 2000)
             k_walkers_team<2><<<h->team_ctas[k], kTeamCta, 0, h->stream>>>(h->d_meta, h->d_teams[k],
                 h->d_pos, h->d_acc, h->d_ctr, sweeps, measure, af, h->tau, h->lambda,
-                (float)h->p_com, h->var_updates, h->seed);
+                (float)h->p_com, h->var_updates, h->seed, 0ull, nullptr);
         else
             k_walkers_team<3><<<h->team_ctas[k], kTeamCta, 0, h->stream>>>(h->d_meta, h->d_teams[k],
                 h->d_pos, h->d_acc, h->d_ctr, sweeps, measure, af, h->tau, h->lambda,
-                (float)h->p_com, h->var_updates, h->seed);
+                (float)h->p_com, h->var_updates, h->seed, 0ull, nullptr);
         h->launches += 1;
         return cudaGetLastError();
     }
@@ -2056,13 +2086,16 @@ int pgb_walkers_energy(pgb_walkers* h, int precision, double* out) {
 // come.  Each round the server (1) moves arrived jobs into a FIFO queue,
 // (2) admits queued jobs while their worldline slab fits the HBM budget and a
 // slot is free, initialises them on the device, (3) advances every active job
-// by up to `sweeps_per_round` sweeps in ONE launch of the packed-team kernel
-// (jobs of all sizes share the launch), (4) reads the per-job accumulators,
-// emits an estimator bin (mean E/N over `bin_sweeps` sweeps) whenever a job
+// in ONE launch of the packed-team kernel (jobs of all sizes share the
+// launch): for `round_seconds` of device time, stopping between two moves and
+// resuming there next round, or by a cost-scaled number of sweeps, never past
+// the end of the job's current bin, (4) reads the per-job accumulators, emits
+// an estimator bin (mean E/N over `bin_sweeps` sweeps) whenever a job
 // completes one, and retires finished jobs, freeing their memory and slot for
-// the next round.  A job's random streams are keyed by its own seed and its
-// team size depends only on its own N and Mbar, so its results are the same
-// alone and in any mix.
+// the next round.  A job's random streams are keyed by its own seed and
+// indexed by (sweep, move), its team size depends only on its own N and Mbar,
+// and its energy samples are summed in sample order, so its results are the
+// same alone and in any mix, however its moves fall into rounds.
 // ===========================================================================
 namespace {
 
@@ -2092,6 +2125,7 @@ struct pgb_server {
     WalkerMeta* d_meta = nullptr;
     WalkerAcc* d_acc = nullptr;
     unsigned long long* d_ctr = nullptr;
+    int* d_upos = nullptr;                           // next move inside the current sweep
     int* d_err = nullptr;
     int4* d_teams = nullptr;
     int teams_cap = 0;
@@ -2145,8 +2179,10 @@ const char* pgb_server_last_error(const pgb_server* s) { return s ? s->err.c_str
 
 int pgb_server_create(const pgb_server_params* p, pgb_server** out) {
     if (!p || !out || p->hbm_budget_bytes < 1e6 || p->max_active <= 0 || p->sweeps_per_round <= 0 ||
-        p->bin_sweeps <= 0 || p->tau <= 0 || p->lambda <= 0) {
-        g_serr = "server_create: need budget >= 1 MB, max_active > 0, sweeps_per_round > 0, bin_sweeps > 0";
+        p->bin_sweeps <= 0 || p->tau <= 0 || p->lambda <= 0 || !(p->round_seconds >= 0.0) ||
+        p->round_seconds > 10.0) {
+        g_serr = "server_create: need budget >= 1 MB, max_active > 0, sweeps_per_round > 0, "
+                 "bin_sweeps > 0, 0 <= round_seconds <= 10";
         return PGB_EINVAL;
     }
     *out = nullptr;
@@ -2165,6 +2201,7 @@ int pgb_server_create(const pgb_server_params* p, pgb_server** out) {
         if ((e = cudaMalloc(&s->d_meta, s->max_slots * sizeof(WalkerMeta))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_acc, s->max_slots * sizeof(WalkerAcc))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_ctr, s->max_slots * sizeof(unsigned long long))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_upos, s->max_slots * sizeof(int))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_err, s->max_slots * sizeof(int))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_list, s->max_slots * sizeof(int))) != cudaSuccess) break;
         if ((e = cudaMemsetAsync(s->d_err, 0, s->max_slots * sizeof(int), s->stream)) != cudaSuccess) break;
@@ -2187,7 +2224,7 @@ int pgb_server_destroy(pgb_server* s) {
     if (!s) return PGB_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     cudaFree(s->d_arena); cudaFree(s->d_meta); cudaFree(s->d_acc); cudaFree(s->d_ctr);
-    cudaFree(s->d_err); cudaFree(s->d_teams); cudaFree(s->d_list);
+    cudaFree(s->d_upos); cudaFree(s->d_err); cudaFree(s->d_teams); cudaFree(s->d_list);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PGB_OK;
@@ -2273,8 +2310,13 @@ int pgb_server_step(pgb_server* s, int* n_active, int* n_queued) {
     for (int k = 0; k < s->max_slots; ++k)
         if (s->slot_job[k] >= 0) {
             ServerJob& job = s->jobs[s->slot_job[k]];
+            // never past the job's end or its current bin, so every bin holds
+            // exactly bin_sweeps samples (the last one the remainder)
             const long long left = job.spec.sweeps - job.sweeps_done;
-            s->h_meta[k].max_sweeps = (int)std::min<long long>(left, job.sweeps_per_round);
+            const long long bin_left = s->p.bin_sweeps - (job.sweeps_done - job.samples_bin_start);
+            long long cap = std::min(left, bin_left);
+            if (s->p.round_seconds <= 0.0) cap = std::min<long long>(cap, job.sweeps_per_round);
+            s->h_meta[k].max_sweeps = (int)std::max<long long>(cap, 1);
             active.push_back(k);
         } else {
             s->h_meta[k].max_sweeps = 0;
@@ -2286,6 +2328,7 @@ int pgb_server_step(pgb_server* s, int* n_active, int* n_queued) {
         for (int k : admitted) {
             cudaMemsetAsync(s->d_acc + k, 0, sizeof(WalkerAcc), s->stream);
             cudaMemsetAsync(s->d_ctr + k, 0, sizeof(unsigned long long), s->stream);
+            cudaMemsetAsync(s->d_upos + k, 0, sizeof(int), s->stream);
         }
         e = cudaMemcpyAsync(s->d_list, admitted.data(), admitted.size() * sizeof(int),
                             cudaMemcpyHostToDevice, s->stream);
@@ -2330,9 +2373,11 @@ int pgb_server_step(pgb_server* s, int* n_active, int* n_queued) {
         if ((e = cudaMemcpyAsync(s->d_teams, flat.data(), flat.size() * sizeof(int4),
                                  cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
             return s->cfail(e, "server teams upload");
+        const bool timed = s->p.round_seconds > 0.0;
         k_walkers_team<2><<<nctas, kTeamCta, 0, s->stream>>>(s->d_meta, s->d_teams, s->d_arena,
-            s->d_acc, s->d_ctr, s->p.sweeps_per_round, 1, make_aziz_f(s->az), s->p.tau, s->p.lambda,
-            (float)s->p.p_com, 1, 0);
+            s->d_acc, s->d_ctr, timed ? (1 << 30) : s->p.sweeps_per_round, 1, make_aziz_f(s->az),
+            s->p.tau, s->p.lambda, (float)s->p.p_com, 1, 0,
+            timed ? (unsigned long long)(s->p.round_seconds * 1e9) : 0ull, s->d_upos);
         if ((e = cudaGetLastError()) != cudaSuccess) return s->cfail(e, "server round launch");
     }
     std::vector<WalkerAcc> acc(s->max_slots);
@@ -2346,7 +2391,9 @@ int pgb_server_step(pgb_server* s, int* n_active, int* n_queued) {
         const long long before = job.sweeps_done;
         job.sweeps_done = acc[k].samples;       // one energy sample per sweep
         (void)before;
-        while (acc[k].samples - job.samples_bin_start >= s->p.bin_sweeps) {
+        const bool finished = job.sweeps_done >= job.spec.sweeps;
+        while (acc[k].samples - job.samples_bin_start >= s->p.bin_sweeps ||
+               (finished && acc[k].samples > job.samples_bin_start)) {
             pgb_bin b;
             b.job = s->slot_job[k];
             b.bin = job.bins;
@@ -2359,7 +2406,7 @@ int pgb_server_step(pgb_server* s, int* n_active, int* n_queued) {
             job.samples_bin_start = acc[k].samples;
             job.esum_bin_start = acc[k].esum;
         }
-        if (job.sweeps_done >= job.spec.sweeps) {
+        if (finished) {
             job.state = 3;
             job.t_done = t_end;
             s->bead_updates += acc[k].bead_updates;

@@ -44,6 +44,24 @@ def test_job_same_alone_and_in_mix(pgb):
     assert all(np.isfinite(b["energy"]) for b in bins)
 
 
+@pytest.mark.parametrize("round_seconds", [0.0, 0.0004, 0.003])
+def test_bins_do_not_depend_on_round_length(pgb, round_seconds):
+    """Timed rounds stop a job between two moves and resume it there; its
+    draws are indexed by (sweep, move) and its samples summed in order, so
+    the bins equal those of whole-sweep rounds bit for bit."""
+    X = dict(n=40, temperature=1.5, sweeps=45, seed=9)
+    ref = pgb.Server(2e9, sweeps_per_round=7, bin_sweeps=20)
+    jr = ref.submit(**X)
+    want = [b["energy"] for b in _run(ref, [jr])]
+    assert len(want) == 3                       # 20 + 20 + the remaining 5
+    s = pgb.Server(2e9, sweeps_per_round=7, bin_sweeps=20, round_seconds=round_seconds)
+    j = s.submit(**X)
+    others = [s.submit(n=96, temperature=1.0, sweeps=30, seed=77)]
+    bins = _run(s, [j] + others)
+    assert [b["energy"] for b in bins if b["job"] == j] == want
+    assert s.job(j)["sweeps_done"] == 45
+
+
 def test_admission_by_memory_budget(pgb):
     # each job: N=128, T=1 -> M=250 -> 128*250*16 B = 512 KB; the budget holds two
     s = pgb.Server(1.2e6, max_active=16, sweeps_per_round=5, bin_sweeps=10)
