@@ -11,13 +11,17 @@
 // Both run as split-BF16 products, A = Ah + Al, B = Bh + Bl,
 // A B ~ Ah Bh + Ah Bl + Al Bh, accumulated in FP32 in tensor memory.
 //
-// Kernel: one CTA of 128 threads per 128 x 256 output tile.  Operand chunks of
-// K = 64 are staged in shared memory in the canonical K-major layout without
-// swizzle (8 x 16-byte core matrices; LBO = 128 B between core matrices along
-// K, SBO = 1024 B between 8-row groups), one thread issues the
-// tcgen05.mma.kind::f16 instructions (M = 128, N = 256, K = 16), tcgen05.commit
-// signals an mbarrier, and every wait on it is bounded.  The accumulator
-// (128 lanes x 256 FP32 columns of TMEM) is read back with tcgen05.ld.
+// Kernel: one CTA of 128 threads per 128 x 256 output tile.  The prep
+// kernels write every operand in tile order: the 64-wide K chunk of a tile is
+// one contiguous block already in the canonical K-major core-matrix layout
+// without swizzle (8 x 16-byte core matrices; LBO = 128 B between core
+// matrices along K, SBO = 1024 B between 8-row groups), so one bulk copy
+// (cp.async.bulk, completion counted on an mbarrier) moves it into shared
+// memory.  Warp 0 lane 0 produces chunks into a two-stage ring, warp 1 lane 0
+// issues the tcgen05.mma.kind::f16 instructions (M = 128, N = 256, K = 16)
+// and releases each stage with tcgen05.commit; every wait is bounded.  The
+// accumulator (128 lanes x 256 FP32 columns of TMEM) is read back with
+// tcgen05.ld by all four warps.
 #include <cuda_bf16.h>
 #include <cstdint>
 
@@ -33,8 +37,20 @@ constexpr int kTK = 64;           // K per staged chunk
 constexpr int kThreads = 128;
 constexpr uint32_t kTileA = kTM * kTK * 2;     // bytes of one bf16 A chunk
 constexpr uint32_t kTileB = kTN * kTK * 2;     // bytes of one bf16 B chunk
-constexpr uint32_t kSmem = 2 * kTileA + 2 * kTileB + 1024;
+constexpr int kStages = 2;
+constexpr uint32_t kStageBytes = 2 * kTileA + 2 * kTileB;     // Ah, Al, Bh, Bl of one chunk
+constexpr uint32_t kSmem = kStages * kStageBytes + 1024;
 constexpr long long kMmaWaitLimit = 1LL << 24;
+
+// Element index of (r, k) in a tile-ordered [rows x K] bf16 operand whose
+// tiles are TR rows x 64 K: tile (r / TR, k / 64) is one contiguous block of
+// TR * 64 elements in core-matrix order (8-row groups of 1024 B, 16-byte core
+// rows, 128 B between core matrices along K).
+__host__ __device__ __forceinline__ size_t tiled_index(int r, int k, int K, int TR) {
+    const int rt = r / TR, rr = r - rt * TR, kc = k >> 6, kk = k & 63;
+    return ((size_t)rt * (size_t)(K >> 6) + (size_t)kc) * (size_t)(TR * 64) +
+           (size_t)((rr >> 3) * 512 + (kk >> 3) * 64 + (rr & 7) * 8 + (kk & 7));
+}
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -92,8 +108,34 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Split-BF16 GEMM  C[rows x cols] = A[rows x K] B[K x cols], A row-major
-// (K contiguous), B given transposed [cols x K] (K contiguous), hi/lo parts.
+__device__ __forceinline__ void bar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(su32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void bar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                 :: "r"(su32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bar_arrive(uint64_t* bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}"
+                 :: "r"(su32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(su32(dst)), "l"(src), "r"(bytes), "r"(su32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool bar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    long long n = 0;
+    while (!bar_try_wait(bar, parity))
+        if (++n > kMmaWaitLimit) return false;
+    return true;
+}
+
+// Split-BF16 GEMM  C[rows x cols] = A[rows x K] B[K x cols]; A and B^T
+// [cols x K] tile-ordered (tiled_index with TR = 128 and 256), hi/lo parts.
 // mode 0: interleaved (re, im) columns -> P[row][col/2] = re^2 + im^2
 // mode 1: out[row][col] = scale * C  (FP64), for row < rows_valid, col < cols_valid
 __global__ void __launch_bounds__(kThreads, 1)
@@ -102,74 +144,94 @@ k_gemm_split_bf16(const __nv_bfloat16* __restrict__ Ah, const __nv_bfloat16* __r
                   int K, int mode, float* __restrict__ P, int ldp, double* __restrict__ out,
                   int ldo, int rows_valid, int cols_valid, double scale, int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* sAh = smem;
-    unsigned char* sAl = sAh + kTileA;
-    unsigned char* sBh = sAl + kTileA;
-    unsigned char* sBl = sBh + kTileB;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sBl + kTileB);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sBl + kTileB + 64);
-    int* s_fail = reinterpret_cast<int*>(sBl + kTileB + 128);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
+    uint64_t* empty = full + kStages;
+    uint64_t* done = empty + kStages;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+    int* s_fail = reinterpret_cast<int*>(tmem_slot + 1);
+    int* s_count = s_fail + 1;                 // [0] chunks issued, [1] chunks consumed
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int row0 = blockIdx.y * kTM, col0 = blockIdx.x * kTN;
+    const int nk = K / kTK;
+    const char* gAh = reinterpret_cast<const char*>(Ah) + (size_t)blockIdx.y * nk * kTileA;
+    const char* gAl = reinterpret_cast<const char*>(Al) + (size_t)blockIdx.y * nk * kTileA;
+    const char* gBh = reinterpret_cast<const char*>(Bh) + (size_t)blockIdx.x * nk * kTileB;
+    const char* gBl = reinterpret_cast<const char*>(Bl) + (size_t)blockIdx.x * nk * kTileB;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                      :: "r"(su32(tmem_slot)), "r"((uint32_t)kTN) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(su32(bar)) : "memory");
+    if (tid == 32) {
+        for (int st = 0; st < kStages; ++st) { bar_init(full + st, 1); bar_init(empty + st, 1); }
+        bar_init(done, 1);
         *s_fail = 0;
+        s_count[0] = s_count[1] = 0;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    uint32_t phase = 0;
-    bool failed = false;
 
-    const int nchunks = K / kTK;
-    for (int c = 0; c < nchunks; ++c) {
-        const int k0 = c * kTK;
-        // stage A (128 rows) and B (256 rows) chunks, 16-byte vectors
-        for (int v = tid; v < kTM * 8; v += kThreads) {
-            const int r = v >> 3, g = v & 7;
-            const size_t src = (size_t)(row0 + r) * K + k0 + 8 * g;
-            const uint32_t dst = cm_offset(r, g);
-            *reinterpret_cast<uint4*>(sAh + dst) = *reinterpret_cast<const uint4*>(Ah + src);
-            *reinterpret_cast<uint4*>(sAl + dst) = *reinterpret_cast<const uint4*>(Al + src);
-        }
-        for (int v = tid; v < kTN * 8; v += kThreads) {
-            const int r = v >> 3, g = v & 7;
-            const size_t src = (size_t)(col0 + r) * K + k0 + 8 * g;
-            const uint32_t dst = cm_offset(r, g);
-            *reinterpret_cast<uint4*>(sBh + dst) = *reinterpret_cast<const uint4*>(Bh + src);
-            *reinterpret_cast<uint4*>(sBl + dst) = *reinterpret_cast<const uint4*>(Bl + src);
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            #pragma unroll
-            for (int s = 0; s < kTK / 16; ++s) {
-                const uint32_t ko = (uint32_t)(2 * s) * 128u;
-                const uint64_t ah = smem_desc(su32(sAh) + ko), al = smem_desc(su32(sAl) + ko);
-                const uint64_t bh = smem_desc(su32(sBh) + ko), bl = smem_desc(su32(sBl) + ko);
-                mma_bf16(tmem, ah, bh, (c > 0 || s > 0) ? 1u : 0u);
-                mma_bf16(tmem, ah, bl, 1u);
-                mma_bf16(tmem, al, bh, 1u);
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer: chunk c goes to stage c % kStages once the MMAs that
+            // read the chunk before it there have completed
+            int c = 0;
+            for (; c < nk; ++c) {
+                const int st = c % kStages;
+                if (c >= kStages && !bar_wait_bounded(empty + st, (uint32_t)((c / kStages - 1) & 1))) {
+                    atomicExch(s_fail, 1);
+                    break;
+                }
+                unsigned char* sA = smem + (size_t)st * kStageBytes;
+                bar_expect_tx(full + st, kStageBytes);
+                bulk_g2s(sA, gAh + (size_t)c * kTileA, kTileA, full + st);
+                bulk_g2s(sA + kTileA, gAl + (size_t)c * kTileA, kTileA, full + st);
+                bulk_g2s(sA + 2 * kTileA, gBh + (size_t)c * kTileB, kTileB, full + st);
+                bulk_g2s(sA + 2 * kTileA + kTileB, gBl + (size_t)c * kTileB, kTileB, full + st);
             }
-            mma_commit(bar);
+            s_count[0] = c;
         }
-        // every thread waits (bounded) for the MMAs before the chunk is overwritten
-        long long n = 0;
-        while (!bar_try_wait(bar, phase)) {
-            if (++n > kMmaWaitLimit) { failed = true; break; }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int c = 0;
+            for (; c < nk; ++c) {
+                const int st = c % kStages;
+                if (!bar_wait_bounded(full + st, (uint32_t)((c / kStages) & 1))) {
+                    atomicExch(s_fail, 1);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t base = su32(smem + (size_t)st * kStageBytes);
+                #pragma unroll
+                for (int ks = 0; ks < kTK / 16; ++ks) {
+                    const uint32_t ko = (uint32_t)(2 * ks) * 128u;
+                    const uint64_t ah = smem_desc(base + ko), al = smem_desc(base + kTileA + ko);
+                    const uint64_t bh = smem_desc(base + 2 * kTileA + ko);
+                    const uint64_t bl = smem_desc(base + 2 * kTileA + kTileB + ko);
+                    mma_bf16(tmem, ah, bh, (c > 0 || ks > 0) ? 1u : 0u);
+                    mma_bf16(tmem, ah, bl, 1u);
+                    mma_bf16(tmem, al, bh, 1u);
+                }
+                mma_commit(empty + st);        // the stage is free once these MMAs are done
+            }
+            s_count[1] = c;
+            mma_commit(done);                  // tracks every MMA this thread issued
         }
-        phase ^= 1u;
-        if (failed) atomicExch(s_fail, 1);
-        __syncthreads();
-        if (*(volatile int*)s_fail) break;
+        __syncwarp();
+    }
+    // everyone: the accumulator is complete (or the pipeline gave up)
+    const bool landed = bar_wait_bounded(done, 0u);
+    if (!landed) atomicExch(s_fail, 1);
+    __syncthreads();
+    if (tid == 0) {
+        // copies issued but never consumed must land before the CTA exits
+        for (int c = s_count[1]; c < s_count[0]; ++c)
+            if (!bar_wait_bounded(full + (c % kStages), (uint32_t)((c / kStages) & 1))) break;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const bool ok = (*(volatile int*)s_fail == 0);
@@ -220,7 +282,8 @@ __global__ void k_prep_rho(const float2* __restrict__ rho, int nq, int M, int qp
         const int q = (int)(i / (2 * M)), k = (int)(i % (2 * M));
         float x = 0.f;
         if (q < nq) { const float2 r = rho[(size_t)q * M + (k % M)]; x = (k < M) ? r.x : r.y; }
-        split_bf16(x, Ah[i], Al[i]);
+        const size_t o = tiled_index(q, k, 2 * M, kTM);
+        split_bf16(x, Ah[o], Al[o]);
     }
 }
 
@@ -237,14 +300,21 @@ __global__ void k_prep_dft(int M, __nv_bfloat16* Bh, __nv_bfloat16* Bl) {
         double val;
         if ((c & 1) == 0) val = (k < M) ? cs : sn;      // Re X = sum Re(rho) cos + Im(rho) sin
         else              val = (k < M) ? -sn : cs;     // Im X = sum -Re(rho) sin + Im(rho) cos
-        split_bf16((float)val, Bh[i], Bl[i]);
+        const size_t o = tiled_index(c, k, 2 * M, kTN);
+        split_bf16((float)val, Bh[o], Bl[o]);
     }
 }
 
-__global__ void k_prep_p(const float* __restrict__ P, long long n, __nv_bfloat16* Ah, __nv_bfloat16* Al) {
+// A2 = P [qpad x M] (row-major) -> tile order
+__global__ void k_prep_p(const float* __restrict__ P, int qpad, int M, __nv_bfloat16* Ah,
+                         __nv_bfloat16* Al) {
+    const long long n = (long long)qpad * M;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        split_bf16(P[i], Ah[i], Al[i]);
+         i += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(i / M), w = (int)(i % M);
+        const size_t o = tiled_index(q, w, M, kTM);
+        split_bf16(P[i], Ah[o], Al[o]);
+    }
 }
 
 // B2^T [colpad][M]: col tau -> cos(2 pi w tau / M), zero beyond M/2
@@ -259,7 +329,8 @@ __global__ void k_prep_cos(int M, int colpad, __nv_bfloat16* Bh, __nv_bfloat16* 
             const long long ph = ((long long)tau * w) % M;
             val = cospi(2.0 * (double)ph / (double)M);
         }
-        split_bf16((float)val, Bh[i], Bl[i]);
+        const size_t o = tiled_index(tau, w, M, kTN);
+        split_bf16((float)val, Bh[o], Bl[o]);
     }
 }
 
@@ -352,7 +423,7 @@ cudaError_t launch_isf_tc(const float2* d_rho, int nq, int M, double norm, doubl
     dim3 g1(2 * M / kTN, L.qpad / kTM);
     k_gemm_split_bf16<<<g1, kThreads, kSmem, s>>>(a1h, a1l, b1h, b1l, 2 * M, 0, P, M, nullptr, 0,
                                                   L.qpad, 2 * M, 0.0, err);
-    k_prep_p<<<152 * 4, 256, 0, s>>>(P, (long long)L.qpad * M, a2h, a2l);
+    k_prep_p<<<152 * 4, 256, 0, s>>>(P, L.qpad, M, a2h, a2l);
     // GEMM 2: [qpad x M] x [M x colpad2] -> F [nq x (M/2+1)]
     dim3 g2(L.colpad2 / kTN, L.qpad / kTM);
     k_gemm_split_bf16<<<g2, kThreads, kSmem, s>>>(a2h, a2l, b2h, b2l, M, 1, nullptr, 0, d_out,

@@ -92,6 +92,14 @@ __device__ __forceinline__ T block_sum(T x, T* red) {
     return t;
 }
 
+// Round to nearest (ties to even) for |x| < 2^22 with two FP32 adds: adding
+// and removing 1.5 * 2^23 drops the fraction bits.  Unlike rintf this stays
+// on the FMA/ALU pipes; __fadd_rn/__fsub_rn are never contracted or
+// reassociated.
+__device__ __forceinline__ float rint_add(float x) {
+    return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
+}
+
 // ---------------------------------------------------------------------------
 // FP32 Aziz pair evaluation (mixed precision).  Analytic form of
 // AzizPotential::valueV / valuedVdr (potential.cpp:1821-1870) with the
@@ -162,7 +170,7 @@ __device__ __forceinline__ void aziz_vg32(float r2, const AzizF& a, float& V, fl
 }
 
 __device__ __forceinline__ float min_image32(float x, float L, float Linv) {
-    return fmaf(-L, rintf(x * Linv), x);
+    return fmaf(-L, rint_add(x * Linv), x);
 }
 
 // Kahan-compensated FP32 accumulator, folded into FP64 at the end.
@@ -177,14 +185,12 @@ struct KahanF {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-// Sum over the warp of the lanes' Kahan accumulators without the FP64 pipe:
-// each butterfly step adds the leading parts with an error-free TwoSum
-// (Knuth) and carries the error with the trailing parts, so the pair
-// (hi, lo) keeps about 48 bits; it is rounded to FP64 once.  TwoSum's error
-// term is exact whichever operand comes first, so every lane ends with the
-// same bits.
-__device__ __forceinline__ double warp_sum_ff(const KahanF& k) {
-    float hi = k.s, lo = -k.c;
+// Sums over the warp without the FP64 pipe.  Each butterfly step adds the
+// leading parts with an error-free TwoSum (Knuth) and carries the error with
+// the trailing parts, so the pair (hi, lo) keeps about 48 bits.  TwoSum's
+// error term is exact whichever operand comes first, so every lane ends with
+// the same bits.
+__device__ __forceinline__ float2 ff_butterfly(float hi, float lo) {
     #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
@@ -195,7 +201,16 @@ __device__ __forceinline__ double warp_sum_ff(const KahanF& k) {
         hi = sum;
         lo = (lo + l2) + err;
     }
-    return (double)hi + (double)lo;
+    return make_float2(hi, lo);
+}
+
+// the lanes' Kahan accumulators (value s - c) summed as a (hi, lo) pair
+__device__ __forceinline__ float2 warp_ff(const KahanF& k) { return ff_butterfly(k.s, -k.c); }
+
+// the same rounded to FP64 once
+__device__ __forceinline__ double warp_sum_ff(const KahanF& k) {
+    const float2 v = warp_ff(k);
+    return (double)v.x + (double)v.y;
 }
 
 // ---------------------------------------------------------------------------
@@ -210,13 +225,6 @@ __device__ __forceinline__ uint4 philox4x32(uint4 c, uint2 k) {
         k.x += 0x9E3779B9u; k.y += 0xBB67AE85u;
     }
     return c;
-}
-// Round to nearest (ties to even) for |x| < 2^22 with two FP32 adds: adding
-// and removing 1.5 * 2^23 drops the fraction bits.  Unlike rintf this stays
-// on the FMA/ALU pipes; __fadd_rn/__fsub_rn are never contracted or
-// reassociated.
-__device__ __forceinline__ float rint_add(float x) {
-    return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
 }
 
 // sum_j exp(2 pi i n . u_j) over the n beads su[0..n) (u = r / L per

@@ -894,6 +894,7 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
     extern __shared__ float4 dyn[];
     __shared__ float4 s_new[8][kMaxStage];
     __shared__ double s_red[8][8];
+    __shared__ float2 s_ff[8][8];
     __shared__ int s_acc[8];
     __shared__ int s_fail[8];
     __shared__ __align__(8) uint64_t s_bar[8];
@@ -1000,14 +1001,18 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
                                 aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
                     }
                 }
-                const double part = warp_sum_ff(acc);
-                if (lane == 0) red[wi] = part;
+                // the team total as a (hi, lo) pair: per-warp sums, then one
+                // butterfly over the warps (the pipelined schedule does the same)
+                const float2 part = warp_ff(acc);
+                if (lane == 0) s_ff[slot][wi] = part;
                 team_sync(slot, T);
-                if (tt == 0) {
-                    double dV = 0.0;
-                    for (int q = 0; q < nw; ++q) dV += red[q];
-                    const uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
-                    s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
+                if (wi == 0) {
+                    const float2 v = ff_butterfly(lane < nw ? s_ff[slot][lane].x : 0.f,
+                                                  lane < nw ? s_ff[slot][lane].y : 0.f);
+                    if (lane == 0) {
+                        const uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
+                        s_acc[slot] = metropolis((double)v.x + (double)v.y, tau, ra.x, ra.y) ? 1 : 0;
+                    }
                 }
                 team_sync(slot, T);
                 const int ok = s_acc[slot];
@@ -1050,13 +1055,13 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
                     }
                     team_sync(slot, T);            // buffer free for the next chunk
                 }
-                const double part = warp_sum_ff(acc);
-                if (lane == 0) red[wi] = part;
+                const float2 part = warp_ff(acc);
+                if (lane == 0) s_ff[slot][wi] = part;
                 team_sync(slot, T);
-                if (tt == 0) {
-                    double dV = 0.0;
-                    for (int q = 0; q < nw; ++q) dV += red[q];
-                    s_acc[slot] = metropolis(dV, tau, r1.y, r1.z) ? 1 : 0;
+                if (wi == 0) {
+                    const float2 v = ff_butterfly(lane < nw ? s_ff[slot][lane].x : 0.f,
+                                                  lane < nw ? s_ff[slot][lane].y : 0.f);
+                    if (lane == 0) s_acc[slot] = metropolis((double)v.x + (double)v.y, tau, r1.y, r1.z) ? 1 : 0;
                 }
                 team_sync(slot, T);
                 const int ok = s_acc[slot];
@@ -1135,18 +1140,22 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
 
 // ---------------------------------------------------------------------------
 // Pipelined TMA schedule.  Teams of up to CTA/32 warps; each team owns two
-// shared-memory buffers of Mbar slab rows.  Move descriptions come from the
-// counter-based generator, so the rows of the next staging move are known
-// before the current move is decided: they are copied into the other buffer
-// while the current move runs.  If the current move is accepted and shares
-// slices with the prefetched rows, the team's own write-back also patches the
-// prefetched copy (after its copy has landed), so every move reads the
-// configuration its predecessor left.  Centre-of-mass moves and energy
-// samples stream the slab through the two buffers in Mbar-row chunks.
+// shared-memory buffers of Mbar + 1 slab rows and two sets of bridge
+// increments.  Move descriptions come from the counter-based generator, so
+// the next staging move is known before the current one is decided: its rows
+// (both fixed ends and the moved slices) are copied into the other buffer and
+// its Gaussian increments drawn while the current move sums its pairs.  If
+// the current move is accepted and shares beads with the prefetched rows, the
+// deciding warp's write-back also patches the prefetched copy (after its copy
+// has landed), so every move reads the configuration its predecessor left.
+// A staging move costs two team barriers: one after the bridge, one before
+// the decision; warp 0 alone decides, writes back and patches while the other
+// warps wait at the next move's first barrier.  Centre-of-mass moves and
+// energy samples stream the slab through the two buffers in Mbar-row chunks.
 // ---------------------------------------------------------------------------
 struct MoveDesc {
-    int com, i, s0, len, nmove, rs;
-    float sx, sy, sz;
+    int com, i, s0, len, nmove;
+    float sx, sy;
 };
 
 __device__ __forceinline__ MoveDesc draw_move(int u, uint32_t g0, uint32_t g1,
@@ -1158,11 +1167,21 @@ __device__ __forceinline__ MoveDesc draw_move(int u, uint32_t g0, uint32_t g1,
     d.s0 = (int)(((unsigned long long)r0.y * (unsigned)m.M) >> 32);
     d.len = var_updates ? 2 + (int)(((unsigned long long)r0.w * (unsigned)(m.mbar - 1)) >> 32) : m.mbar;
     d.nmove = d.len - 1;
-    d.rs = d.s0 + 1; if (d.rs >= m.M) d.rs -= m.M;
     d.sx = m.com_delta * (u01f(r0.y) - 0.5f);
     d.sy = m.com_delta * (u01f(r0.w) - 0.5f);
-    d.sz = 0.f;
     return d;
+}
+
+// Gaussian increments sigma z of the Brownian bridge of staging move u
+// (beads k + 1 = 1 .. len), the same draws and arithmetic as the bridge of
+// the one-warp construction, spread over the team's threads.
+__device__ __forceinline__ void stage_increments(float4* inc, const WalkerMeta& m, int u, uint32_t g0,
+                                                 uint32_t g1, int len, int tt, int T) {
+    for (int k = tt; k < len; k += T) {
+        const uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)(k + 1));
+        const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
+        inc[k] = make_float4(m.sig2lt * z01.x, m.sig2lt * z01.y, m.sig2lt * z2.x, 0.f);
+    }
 }
 
 template <int CTA, int MINB>
@@ -1174,6 +1193,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
     constexpr int NW = CTA / 32;
     extern __shared__ float4 dyn[];
     __shared__ float4 s_new[NW][kMaxStage];
+    __shared__ float2 s_ff[NW][NW];
     __shared__ double s_red[NW][NW];
     __shared__ int s_acc[NW];
     __shared__ int s_fail[NW];
@@ -1189,14 +1209,19 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
     const int tt = threadIdx.x - slot * 32, wi = warp - slot;
     const WalkerMeta m = meta[w];
     float4* P = pos + m.off;
-    const int N = m.N, M = m.M, C = m.mbar;
+    const int N = m.N, M = m.M, C = m.mbar, R = C + 1;
+    // two row buffers of Mbar + 1 slab rows, then two sets of bridge increments
     float4* const B0 = dyn + (tm.w - 1);
-    float4* const B1 = B0 + (size_t)C * N;
+    float4* const B1 = B0 + (size_t)R * N;
+    float4* const I0 = B1 + (size_t)R * N;
+    float4* const I1 = I0 + kMaxStage;
     uint64_t* const bar0 = &s_bar[slot][0];
     uint64_t* const bar1 = &s_bar[slot][1];
     auto Bsel = [&](int x) { return x ? B1 : B0; };
     auto barsel = [&](int x) { return x ? bar1 : bar0; };
+    auto Isel = [&](int x) { return x ? I1 : I0; };
     double* red = s_red[slot];
+    float2* ffr = s_ff[slot];
     float4* sn = s_new[slot];
     int* fail = &s_fail[slot];
     if (tt == 0) { mbar_init(bar0, 1); mbar_init(bar1, 1); *fail = 0; }
@@ -1213,72 +1238,98 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
     const int kb0 = (T >= N) ? tt / N : 0;
     const int jstep = (T >= N) ? N : T;
     int cur = 0;
+    // bounded wait for a copy this team issued and will not read (error path)
+    auto drain = [&](int b) {
+        long long n = 0;
+        while (!mbar_try_wait(barsel(b), phsel(b)))
+            if (++n > kWaitLimit) break;
+    };
 
     for (int sw = 0; sw < min(sweeps, m.max_sweeps); ++sw) {
         const unsigned long long gs = sweep0 + sw;
         const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
         bool have = false;                        // rows of the current move already in Bsel(cur)
         MoveDesc D = draw_move(0, g0, g1, m, p_com, var_updates);
+        MoveDesc Dn = D;
+        if (m.num_updates > 1) Dn = draw_move(1, g0, g1, m, p_com, var_updates);
+        // the bridge increments of a staging move depend on the draws alone:
+        // those of move u + 1 are made while move u sums its pairs
+        if (!D.com) stage_increments(Isel(0), m, 0, g0, g1, D.len, tt, T);
+        team_sync(slot, T);
         for (int u = 0; u < m.num_updates; ++u) {
             const bool last = (u + 1 == m.num_updates);
-            MoveDesc Dn = D;
-            if (!last) Dn = draw_move(u + 1, g0, g1, m, p_com, var_updates);
+            const bool has_nn = (u + 2 < m.num_updates);
             if (!D.com) {
                 const bool pre = !last && !Dn.com;
-                if (tt == 0) {
-                    if (!have) issue_rows(Bsel(cur), P, N, M, D.rs, D.nmove, barsel(cur));
-                    if (pre) issue_rows(Bsel(cur ^ 1), P, N, M, Dn.rs, Dn.nmove, barsel(cur ^ 1));
-                }
                 const int i = D.i, s0 = D.s0, len = D.len, nmove = D.nmove;
+                // rows s0 .. s0 + len: the two fixed ends and the moved slices
+                if (tt == 0) {
+                    if (!have) issue_rows(Bsel(cur), P, N, M, s0, len + 1, barsel(cur));
+                    if (pre) issue_rows(Bsel(cur ^ 1), P, N, M, Dn.s0, Dn.len + 1, barsel(cur ^ 1));
+                }
+                const float4* buf = Bsel(cur);
                 if (wi == 0) {
-                    int se = s0 + len; if (se >= M) se -= M;
-                    const float4 x0 = P[(size_t)s0 * N + i], xe = P[(size_t)se * N + i];
-                    float a1x = 0.f, a1y = 0.f, a1z = 0.f, a2x = 0.f, a2y = 0.f, a2z = 0.f;
-                    if (lane + 1 <= len) {
-                        const uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)(lane + 1));
-                        const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
-                        a1x = m.sig2lt * z01.x; a1y = m.sig2lt * z01.y; a1z = m.sig2lt * z2.x;
-                    }
-                    if (lane + 33 <= len) {
-                        const uint4 a = wrand(m.key, (uint32_t)u, g0, g1, (uint32_t)(lane + 33));
-                        const float2 z01 = box_muller(a.x, a.y), z2 = box_muller(a.z, a.w);
-                        a2x = m.sig2lt * z01.x; a2y = m.sig2lt * z01.y; a2z = m.sig2lt * z2.x;
-                    }
-                    const float W1x = warp_scan_incl(a1x, lane), W1y = warp_scan_incl(a1y, lane),
-                                W1z = warp_scan_incl(a1z, lane);
-                    const float W2x = warp_scan_incl(a2x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
-                    const float W2y = warp_scan_incl(a2y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
-                    const float W2z = warp_scan_incl(a2z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
-                    const int src = (len <= 32) ? len - 1 : len - 33;
-                    const float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
-                    const float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
-                    const float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
-                    const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
-                    const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
-                    const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
-                    const float il = 1.0f / (float)len;
-                    #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int k = lane + 32 * h;
-                        if (k < nmove) {
-                            const float f = (float)(k + 1) * il;
-                            const float Wx = h ? W2x : W1x, Wy = h ? W2y : W1y, Wz = h ? W2z : W1z;
-                            sn[k] = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
-                                                put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
-                                                put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
+                    // one warp waits for the rows and builds the Brownian bridge
+                    // W_j = sum_{i<=j} sigma z_i, x_j = x0 + (j/len)(xe - x0) + W_j - (j/len) W_len
+                    long long nwait = 0;
+                    bool landed = true;
+                    while (!mbar_try_wait(barsel(cur), phsel(cur)))
+                        if (++nwait > kWaitLimit) { landed = false; break; }
+                    landed = __all_sync(0xffffffffu, landed);
+                    if (!landed) {
+                        if (lane == 0) { atomicExch(fail, 1); atomicExch(err + w, 1); }
+                    } else {
+                        const float4 x0 = buf[i], xe = buf[(size_t)len * N + i];
+                        const float4* inc = Isel(u & 1);
+                        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+                        const float4 i1 = (lane < len) ? inc[lane] : zero;
+                        const float4 i2 = (lane + 32 < len) ? inc[lane + 32] : zero;
+                        const float W1x = warp_scan_incl(i1.x, lane), W1y = warp_scan_incl(i1.y, lane),
+                                    W1z = warp_scan_incl(i1.z, lane);
+                        const float W2x = warp_scan_incl(i2.x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
+                        const float W2y = warp_scan_incl(i2.y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
+                        const float W2z = warp_scan_incl(i2.z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
+                        const int src = (len <= 32) ? len - 1 : len - 33;
+                        const float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
+                        const float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
+                        const float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
+                        const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
+                        const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
+                        const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
+                        const float il = 1.0f / (float)len;
+                        #pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int k = lane + 32 * h;
+                            if (k < nmove) {
+                                const float f = (float)(k + 1) * il;
+                                const float Wx = h ? W2x : W1x, Wy = h ? W2y : W1y, Wz = h ? W2z : W1z;
+                                sn[k] = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
+                                                    put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
+                                                    put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
+                            }
                         }
                     }
                 }
-                if (!team_wait(barsel(cur), phsel(cur), slot, T, fail, err + w)) return;
                 phflip(cur);
-                const float4* buf = Bsel(cur);
+                team_sync(slot, T);
+                if (*(volatile int*)fail) {
+                    if (tt == 0 && pre) drain(cur ^ 1);
+                    return;
+                }
+                // while the pairs are summed: the next move's increments, the
+                // move after it, and this move's acceptance draw
+                if (pre) stage_increments(Isel((u + 1) & 1), m, u + 1, g0, g1, Dn.len, tt, T);
+                MoveDesc Dnn = Dn;
+                if (has_nn) Dnn = draw_move(u + 2, g0, g1, m, p_com, var_updates);
+                uint4 ra = make_uint4(0u, 0u, 0u, 0u);
+                if (tt == 0) ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
                 KahanF acc;
                 for (int j = j0; j < N; j += jstep) {
                     if (j == i) continue;
                     #pragma unroll 4
                     for (int k = kb0; k < nmove; k += G) {
-                        const float4 pj = buf[k * N + j];
-                        const float4 a = sn[k], b = buf[k * N + i];
+                        const float4 pj = buf[(size_t)(k + 1) * N + j];
+                        const float4 a = sn[k], b = buf[(size_t)(k + 1) * N + i];
                         const float ax = min_image32(a.x - pj.x, m.L, m.Linv);
                         const float ay = min_image32(a.y - pj.y, m.L, m.Linv);
                         const float az_ = min_image32(a.z - pj.z, m.L, m.Linv);
@@ -1289,56 +1340,68 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                                 aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
                     }
                 }
-                const double part = warp_sum_ff(acc);
-                if (lane == 0) red[wi] = part;
+                const float2 part = warp_ff(acc);
+                if (lane == 0) ffr[wi] = part;
                 team_sync(slot, T);
-                if (tt == 0) {
-                    double dV = 0.0;
-                    for (int q = 0; q < nw; ++q) dV += red[q];
-                    const uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
-                    s_acc[slot] = metropolis(dV, tau, ra.x, ra.y) ? 1 : 0;
-                }
-                team_sync(slot, T);
-                const int ok = s_acc[slot];
-                if (wi == 0 && ok) {
-                    for (int k = lane; k < nmove; k += 32) {
-                        int sl = s0 + 1 + k; if (sl >= M) sl -= M;
-                        P[(size_t)sl * N + i] = sn[k];
+                if (wi == 0) {
+                    // the decision, the write-back and the patch belong to one warp;
+                    // the others go on to the next move's barrier
+                    const float2 v = ff_butterfly(lane < nw ? ffr[lane].x : 0.f, lane < nw ? ffr[lane].y : 0.f);
+                    int ok = 0;
+                    if (lane == 0) {
+                        ok = metropolis((double)v.x + (double)v.y, tau, ra.x, ra.y) ? 1 : 0;
+                        att1 += 1; acc1 += ok; nbu += nmove;
                     }
-                    fence_proxy_async_global();
-                    if (pre) {
-                        // the prefetched rows must have landed before they are patched
-                        long long n = 0;
-                        bool landed = true;
-                        while (!mbar_try_wait(barsel(cur ^ 1), phsel(cur ^ 1)))
-                            if (++n > kWaitLimit) { landed = false; break; }
-                        if (!landed) { atomicExch(fail, 1); atomicExch(err + w, 1); }
-                        else {
-                            float4* nb = Bsel(cur ^ 1);
-                            for (int k = lane; k < nmove; k += 32) {
-                                int sl = s0 + 1 + k; if (sl >= M) sl -= M;
-                                int q = sl - Dn.rs; if (q < 0) q += M;
-                                if (q < Dn.nmove) nb[q * N + i] = sn[k];
+                    ok = __shfl_sync(0xffffffffu, ok, 0);
+                    if (ok) {
+                        for (int k = lane; k < nmove; k += 32) {
+                            int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                            P[(size_t)sl * N + i] = sn[k];
+                        }
+                        fence_proxy_async_global();
+                        if (pre) {
+                            // the prefetched rows must have landed before they are patched
+                            long long n = 0;
+                            bool landed = true;
+                            while (!mbar_try_wait(barsel(cur ^ 1), phsel(cur ^ 1)))
+                                if (++n > kWaitLimit) { landed = false; break; }
+                            landed = __all_sync(0xffffffffu, landed);
+                            if (!landed) {
+                                if (lane == 0) { atomicExch(fail, 1); atomicExch(err + w, 1); }
+                            } else {
+                                float4* nb = Bsel(cur ^ 1);
+                                for (int k = lane; k < nmove; k += 32) {
+                                    int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                                    int q = sl - Dn.s0; if (q < 0) q += M;
+                                    if (q <= Dn.len) nb[(size_t)q * N + i] = sn[k];
+                                }
+                                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                             }
-                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                         }
                     }
+                    __syncwarp();
                 }
-                if (wi == 0) __syncwarp();
-                att1 += 1; acc1 += ok; nbu += nmove;
                 if (pre) { cur ^= 1; have = true; } else { have = false; }
+                D = Dn;
+                Dn = Dnn;
             } else {
                 const int i = D.i;
                 const float sx = D.sx, sy = D.sy;
                 const uint4 r1 = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFEu);
                 const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
+                if (!last && !Dn.com) stage_increments(Isel((u + 1) & 1), m, u + 1, g0, g1, Dn.len, tt, T);
+                MoveDesc Dnn = Dn;
+                if (has_nn) Dnn = draw_move(u + 2, g0, g1, m, p_com, var_updates);
                 KahanF acc;
                 int b = cur;
                 if (tt == 0) issue_rows(Bsel(b), P, N, M, 0, min(C, M), barsel(b));
                 for (int c0 = 0; c0 < M; c0 += C) {
                     const int nr = min(C, M - c0), nb0 = c0 + C;
                     if (nb0 < M && tt == 0) issue_rows(Bsel(b ^ 1), P, N, M, nb0, min(C, M - nb0), barsel(b ^ 1));
-                    if (!team_wait(barsel(b), phsel(b), slot, T, fail, err + w)) return;
+                    if (!team_wait(barsel(b), phsel(b), slot, T, fail, err + w)) {
+                        if (tt == 0 && nb0 < M) drain(b ^ 1);
+                        return;
+                    }
                     phflip(b);
                     const float4* buf = Bsel(b);
                     for (int j = j0; j < N; j += jstep) {
@@ -1360,13 +1423,12 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                     b ^= 1;
                 }
                 cur = b;
-                const double part = warp_sum_ff(acc);
-                if (lane == 0) red[wi] = part;
+                const float2 part = warp_ff(acc);
+                if (lane == 0) ffr[wi] = part;
                 team_sync(slot, T);
-                if (tt == 0) {
-                    double dV = 0.0;
-                    for (int q = 0; q < nw; ++q) dV += red[q];
-                    s_acc[slot] = metropolis(dV, tau, r1.y, r1.z) ? 1 : 0;
+                if (wi == 0) {
+                    const float2 v = ff_butterfly(lane < nw ? ffr[lane].x : 0.f, lane < nw ? ffr[lane].y : 0.f);
+                    if (lane == 0) s_acc[slot] = metropolis((double)v.x + (double)v.y, tau, r1.y, r1.z) ? 1 : 0;
                 }
                 team_sync(slot, T);
                 const int ok = s_acc[slot];
@@ -1383,8 +1445,9 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 team_sync(slot, T);
                 att0 += 1; acc0 += ok; nbu += M;
                 have = false;
+                D = Dn;
+                Dn = Dnn;
             }
-            D = Dn;
         }
         if (measure > 0 && ((gs + 1) % (unsigned long long)measure) == 0) {
             KahanF pot, kin;
@@ -1575,8 +1638,11 @@ constexpr int kTeamScheds[3] = {1004, 1008, 1016};
 // cost so the longest chains start first.
 // Pack walkers with tw[w] warps each into 8-warp CTAs (first fit, walkers
 // sorted by team size then cost); CTAs are issued by decreasing cost.
+// with_buffers: each team gets nbuf buffers of (Mbar + extra_rows) slab rows
+// and extra_f4 more float4 of shared memory
 cudaError_t pack_teams(pgb_walkers* h, int k, const std::vector<int>& tw, bool with_buffers = false,
-                       int cta_warps = 8, int nbuf = 1, size_t smem_budget = 160 * 1024) {
+                       int cta_warps = 8, int nbuf = 1, size_t smem_budget = 160 * 1024,
+                       int extra_rows = 0, int extra_f4 = 0) {
     std::vector<int> idx(h->W);
     std::iota(idx.begin(), idx.end(), 0);
     std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
@@ -1588,7 +1654,8 @@ cudaError_t pack_teams(pgb_walkers* h, int k, const std::vector<int>& tw, bool w
     std::vector<double> cost;
     std::vector<size_t> bytes;
     for (int w : idx) {
-        const size_t need = with_buffers ? (size_t)nbuf * h->mbar[w] * h->N[w] * sizeof(float4) : 0;
+        const size_t need = with_buffers
+            ? ((size_t)nbuf * (h->mbar[w] + extra_rows) * h->N[w] + extra_f4) * sizeof(float4) : 0;
         if (need > smem_budget) return cudaErrorInvalidValue;
         int c = -1;
         for (int q = (int)ctas.size() - 1; q >= 0 && q >= (int)ctas.size() - 4; --q)
@@ -1613,7 +1680,7 @@ cudaError_t pack_teams(pgb_walkers* h, int k, const std::vector<int>& tw, bool w
             int4 t = ctas[order[c]][e];
             if (with_buffers) {
                 t.w = (int)off + 1;
-                off += (size_t)nbuf * h->mbar[t.x] * h->N[t.x];
+                off += (size_t)nbuf * (h->mbar[t.x] + extra_rows) * h->N[t.x] + extra_f4;
             }
             flat[c * cta_warps + e] = t;
         }
@@ -1681,7 +1748,8 @@ cudaError_t build_pipe_teams(pgb_walkers* h, int k, int cta, int ppt) {
         while (t < need && t < cap) t <<= 1;
         tw[w] = t;
     }
-    return pack_teams(h, k, tw, true, cap, 2, cta == 512 ? 200 * 1024 : 100 * 1024);
+    // two buffers of Mbar + 1 rows and two sets of kMaxStage bridge increments
+    return pack_teams(h, k, tw, true, cap, 2, cta == 512 ? 200 * 1024 : 100 * 1024, 1, 2 * kMaxStage);
 }
 
 // One warp per imaginary-time window: P = min(8, M / (Mbar + 1)) windows.
