@@ -38,7 +38,17 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-PAIR_FLOP = 40          # nominal FP32 FLOP per Aziz pair evaluation (plus 3-4 SFU ops)
+# Algorithmic cost of one pair evaluation (minimum image, r^2, Aziz V):
+# 40 FP32 FLOP and 4 special-function ops; V and gradV together: 52 FLOP and
+# 4 special-function ops.  The kernels issue 3 special-function ops for V
+# (rsqrt and two ex2), so the SFU fractions below overstate their use by 4/3.
+PAIR_FLOP = 40
+PAIR_SFU = 4
+PAIR_FLOP_VG = 52
+SFU_PER_SM_CLK = 16     # nominal special-function results per SM per clock
+# DRAM bytes (read + write) per launch from one ncu capture of each kernel on
+# the workload its bench leg runs (profiles/ holds the summaries)
+NCU_TRAFFIC = {"k_walkers_pipe": 160.0e6}
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -139,6 +149,44 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
                 "samples": len(rows)}
+
+
+def walker_kernel(sched):
+    """Kernel that runs a walker schedule code."""
+    if sched >= 5000:
+        return "k_walkers_pipe"
+    if sched >= 4000:
+        return "k_walkers_tma"
+    if sched >= 3000:
+        return "k_walkers_windows"
+    if sched >= 1000:
+        return "k_walkers_team"
+    return "k_walkers_run"
+
+
+def sfu_peak(sm_mhz):
+    """Nominal special-function throughput at the sampled SM clock (ops/s)."""
+    import pimc_gb300 as pgb
+    sms = pgb.device_info()["sm_count"]
+    mhz = sm_mhz or 2070.0
+    return SFU_PER_SM_CLK * sms * mhz * 1e6
+
+
+def pair_roofline(pairs, pairs_vg, seconds, kernel, peak_fp32, sm_mhz, traffic=None):
+    """FP32 and SFU fractions of a pair-sum kernel; frac is the larger, as the
+    binding pipe."""
+    flops = (pairs * PAIR_FLOP + pairs_vg * PAIR_FLOP_VG) / seconds / 1e12
+    sfu = (pairs + pairs_vg) * PAIR_SFU / seconds
+    sfu_pk = sfu_peak(sm_mhz)
+    f_fp32, f_sfu = flops / peak_fp32, sfu / sfu_pk
+    return {"bound": "fp32" if f_fp32 >= f_sfu else "sfu", "achieved": flops, "peak": peak_fp32,
+            "unit": "TFLOP/s", "frac": max(f_fp32, f_sfu), "fp32_frac": f_fp32,
+            "sfu": {"achieved_gops": sfu / 1e9, "peak_gops": sfu_pk / 1e9, "frac": f_sfu},
+            "traffic": traffic, "kernel": kernel,
+            "note": "achieved = pair evaluations x %d FLOP (%d for V+gradV) / kernel time; FP32 "
+                    "peak = measured cuBLAS SGEMM (no TF32) on this GPU; SFU peak = nominal %d/clk/SM "
+                    "x SMs x median SM clock, %d SFU ops per pair; frac = the larger fraction"
+                    % (PAIR_FLOP, PAIR_FLOP_VG, SFU_PER_SM_CLK, PAIR_SFU)}
 
 
 def workload(num, seed=0):
@@ -310,11 +358,16 @@ def run_isf(args, pgb):
     stream = torch.cuda.ExternalStream(pgb._lib.load().pgb_stream(a.h))
     d_q = torch.from_numpy(q).cuda()
     d_out = torch.empty((nq, m // 2 + 1), dtype=torch.float64, device="cuda")
+    d_s = torch.empty(nq, dtype=torch.float64, device="cuda")
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
     res = {}
-    for mode in (0, 1):
+    clk = Clocks()
+    calls = {0: lambda: a.lib.pgb_isf_device_async(a.h, d_q.data_ptr(), nq, 0, d_out.data_ptr()),
+             1: lambda: a.lib.pgb_isf_device_async(a.h, d_q.data_ptr(), nq, 1, d_out.data_ptr()),
+             "ssf": lambda: a.lib.pgb_ssf_device_async(a.h, d_q.data_ptr(), nq, d_s.data_ptr())}
+    for mode, call in calls.items():
         for _ in range(args.warmup):
-            a._chk(a.lib.pgb_isf_device_async(a.h, d_q.data_ptr(), nq, mode, d_out.data_ptr()))
+            a._chk(call())
         torch.cuda.synchronize()
         ms = []
         for k in range(args.steps):
@@ -322,11 +375,12 @@ def run_isf(args, pgb):
                 flush.fill_(float(k))
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                a._chk(a.lib.pgb_isf_device_async(a.h, d_q.data_ptr(), nq, mode, d_out.data_ptr()))
+                a._chk(call())
                 e1.record(stream)
             ms.append((e0, e1))
         torch.cuda.synchronize()
         res[mode] = sum(x.elapsed_time(y) for x, y in ms) / len(ms)
+    clocks = clk.stop()
     # e2e through the C ABI with host buffers: positions uploaded each step
     # (the reference copies its bead array to the device every sample)
     t0 = time.perf_counter()
@@ -334,12 +388,19 @@ def run_isf(args, pgb):
         a.load(cfg)
         a.isf(q, mode=1)
     t_e2e = (time.perf_counter() - t0) / args.steps
-    # split-BF16 GEMM FLOPs (3 products): [Qp x 2M x 2M] + [Qp x M x colpad]
-    qp = ((nq + 127) // 128) * 128
-    colpad = ((m // 2 + 1 + 255) // 256) * 256
-    flops = 3 * (2.0 * qp * 2 * m * 2 * m + 2.0 * qp * m * colpad)
+    # rho_q (the dominant kernel): Q M N phase evaluations, 2 special-function
+    # ops (sin, cos) each; S(q) = rho_q plus an O(Q M) reduction, so its time
+    # stands for the rho_q kernel.  Correlation (the GEMM part): the
+    # algorithmic 2 M^2 2Q FLOP of the slice-correlation contraction, over the
+    # F(q,tau) time less the S(q) time.
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"bf16_tflops": 1900.0}
+    t_rho = res["ssf"] / 1e3
+    sfu = 2.0 * nq * m * n / t_rho
+    sfu_pk = sfu_peak(clocks.get("sm_mhz"))
+    t_corr = max(res[1] - res["ssf"], 1e-6) / 1e3
+    corr_flops = 2.0 * m * m * 2 * nq
+    bf16 = peaks.get("bf16_tflops", 1900.0)
     out = {"metric": "F(q,tau) configurations/s", "value": 1e3 / res[1], "unit": "configurations/s",
            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res[1],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+bf16x3",
@@ -347,16 +408,24 @@ def run_isf(args, pgb):
            "config": {"workload": "F(q,tau): N=512, M=512, 2048 lattice q |q|<=4/A, tau in [0,M/2]",
                       "l2": "flushed between timed steps",
                       "ms_cuda_core_correlation": res[0], "ms_tensor_core_correlation": res[1],
-                      "phase_evaluations_per_s": nq * m * n / (res[1] / 1e3)},
+                      "ms_ssf": res["ssf"],
+                      "phase_evaluations_per_s": nq * m * n / t_rho},
            "e2e": {"value": 1.0 / t_e2e, "unit": "configurations/s",
                    "h2d_bytes_per_step": int(cfg["pos"].nbytes + q.nbytes + cfg["next"].nbytes * 2),
                    "d2h_bytes_per_step": int(nq * (m // 2 + 1) * 8)},
-           "roofline": {"bound": "tensor", "kernel": "k_gemm_split_bf16 (whole F(q,tau) call timed)",
-                        "achieved": flops / (res[1] / 1e3) / 1e12,
-                        "peak": peaks.get("bf16_tflops", 1900.0), "unit": "TFLOP/s",
-                        "frac": flops / (res[1] / 1e3) / 1e12 / peaks.get("bf16_tflops", 1900.0),
-                        "traffic": None, "note": "achieved counts the GEMM FLOPs over the whole call "
-                        "(rho_q included), so it is a lower bound for the GEMM kernel"}}
+           "roofline": {"bound": "sfu", "kernel": "k_rhoq32", "achieved": sfu / 1e9,
+                        "peak": sfu_pk / 1e9, "unit": "Gop/s", "frac": sfu / sfu_pk, "traffic": None,
+                        "note": "2 special-function ops (sin, cos) per phase evaluation, Q M N of "
+                                "them, over the S(q) call time (rho_q + an O(Q M) reduction); peak "
+                                "= nominal %d/clk/SM x SMs x median SM clock" % SFU_PER_SM_CLK},
+           "roofline_correlation": {"bound": "tensor", "kernel": "k_gemm_split_bf16 + split/prep kernels",
+                                    "achieved": corr_flops / t_corr / 1e12, "peak": bf16,
+                                    "unit": "TFLOP/s", "frac": corr_flops / t_corr / 1e12 / bf16,
+                                    "note": "algorithmic 2 M^2 2Q FLOP of the correlation over "
+                                            "(F(q,tau) time - S(q) time); the split-BF16 DFT form "
+                                            "executes more (3 products, DFT then cosine GEMM); peak "
+                                            "= MEASURED_PEAKS bf16 burst"},
+           "clocks": clocks}
     if not args.no_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
@@ -392,6 +461,7 @@ def run_pair(args, pgb):
     lam_db = 2 * math.sqrt(math.pi * w["lam"] / w["temperature"])
     beads = np.stack([rng.integers(0, m, ntrial), rng.integers(0, n, ntrial)], 1).astype(np.int32)
     disp = rng.uniform(-0.04 * lam_db, 0.04 * lam_db, (ntrial, 3))
+    clk = Clocks()
     for prec in (pgb.PGB_FP64, pgb.PGB_MIXED):
         a = pgb.Action(L, m, n, w["tau"], w["lam"], action="gsf", precision=prec)
         a.load(cfg)
@@ -420,21 +490,31 @@ def run_pair(args, pgb):
             e1.record(stream)
         torch.cuda.synchronize()
         t_trial = e0.elapsed_time(e1) / 1e3
-        # pair evaluations of a trial, counted as the reference's checkMove does
-        # them: 2 (old, new) x [(n-1) V terms + on odd (gradV) slices the
-        # n(n-1)/2 pair forces of the slice]
+        # pair evaluations of a trial as the reference's per-bead action makes
+        # them, old and new: 2 (n-1) V pairs, and on odd (gradV) slices
+        # 2 (n-1)^2 gradV pairs (gradVnnSquared over the bead's list)
         odd = (beads[:k, 0] % 2 == 1).mean()
-        trial_pairs = k * 2 * ((n - 1) + odd * n * (n - 1) / 2)
+        tp_v = k * 2.0 * (n - 1)
+        tp_vg = k * odd * 2.0 * (n - 1) ** 2
+        trial_pairs = tp_v + tp_vg
         res["fp64" if prec == pgb.PGB_FP64 else "mixed"] = {
             "full_action_ms": 1e3 * t_full, "full_action_pairs_per_s": (v_pairs + g_pairs) / t_full,
             "trials": k, "trial_ms": 1e3 * t_trial, "trial_pairs_per_s": trial_pairs / t_trial,
-            "trial_moves_per_s": k / t_trial}
+            "trial_moves_per_s": k / t_trial, "_pv": tp_v, "_pvg": tp_vg, "_t": t_trial}
+    clocks = clk.stop()
+    mx = res["mixed"]
+    roof = pair_roofline(mx.pop("_pv"), mx.pop("_pvg"), mx.pop("_t"), "k_bead_actions32",
+                         measured_fp32_peak(), clocks.get("sm_mhz"))
+    for r in res.values():
+        for key in ("_pv", "_pvg", "_t"):
+            r.pop(key, None)
     out = {"metric": "pair evaluations/s (single-bead trial moves, mixed)",
-           "value": res["mixed"]["trial_pairs_per_s"], "unit": "pair-evaluations/s", "n_gpus": 1,
+           "value": mx["trial_pairs_per_s"], "unit": "pair-evaluations/s", "n_gpus": 1,
            "steps": args.steps, "warmup": 2, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
            "config": {"workload": "pair action: N=256, M=250, GSF, rc=L, 10^6 trial displacements "
-                                  "uniform in [-0.04 lambda_dB, 0.04 lambda_dB]^3", "results": res}}
+                                  "uniform in [-0.04 lambda_dB, 0.04 lambda_dB]^3", "results": res},
+           "roofline": roof, "clocks": clocks}
     if not args.no_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
@@ -448,7 +528,7 @@ def run_pair(args, pgb):
             cnt += 1
         dt = time.perf_counter() - t0
         odd = (beads[:cnt, 0] % 2 == 1).mean()
-        pairs = cnt * ((n - 1) + odd * n * (n - 1) / 2)
+        pairs = cnt * ((n - 1) + odd * (n - 1) ** 2)
         out["cpu_baseline"] = {"value": pairs / dt, "unit": "pair-evaluations/s", "cores": 1,
                                "kind": "port", "sample": "%d per-bead GSF actions (FP64 oracle, 1 "
                                "thread, rc=L) in %.1f s" % (cnt, dt)}
@@ -595,10 +675,12 @@ def main():
     t_e2e = max_over_ranks(t_e2e, ws)
     e2e_val = sum_over_ranks(float(bu_e2e), ws) / t_e2e
 
-    # roofline of the walker kernel: pair evaluations x nominal FLOP
+    # roofline of the walker kernel: pair evaluations x nominal FLOP / SFU ops
     peak_fp32 = measured_fp32_peak()
     pairs = pair_per_step * args.steps
-    achieved = pairs * PAIR_FLOP / t_dev / 1e12
+    kname = walker_kernel(W.threads())
+    roof = pair_roofline(pairs, 0.0, t_dev, kname, peak_fp32, clocks.get("sm_mhz"),
+                         NCU_TRAFFIC.get(kname))
 
     out = {"metric": "bead-updates/s", "value": value, "unit": "bead-updates/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
@@ -614,11 +696,7 @@ def main():
            "e2e": {"value": e2e_val, "unit": "bead-updates/s", "h2d_bytes_per_step": state_bytes,
                    "d2h_bytes_per_step": stats_bytes},
            "gpu_launches": int(launches),
-           "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32,
-                        "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": None,
-                        "kernel": "k_walkers_run",
-                        "note": "pair evaluations x %d FLOP; peak = measured cuBLAS SGEMM "
-                                "(no TF32) on this GPU" % PAIR_FLOP},
+           "roofline": roof,
            "clocks": clocks}
     if rank == 0 and not args.no_baseline:
         out["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)

@@ -162,6 +162,7 @@ int pgb_rhoq(pgb_ctx* ctx, const double* q, int nq, double* out);
  *      memory, results left on the device (no host copies, no syncs). ---- */
 int pgb_isf_device_async(pgb_ctx* ctx, const double* d_q, int nq, int mode,
                          double* d_out);
+int pgb_ssf_device_async(pgb_ctx* ctx, const double* d_q, int nq, double* d_out);
 int pgb_load_positions_device_async(pgb_ctx* ctx, const double* d_pos);
 void* pgb_stream(pgb_ctx* ctx);   /* the context's cudaStream_t */
 

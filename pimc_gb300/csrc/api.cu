@@ -769,6 +769,14 @@ int pgb_isf_device_async(pgb_ctx* h, const double* d_q, int nq, int mode, double
     return scatter_common(c, d_q, nq, 1, mode, d_out, c.d_scratch);
 }
 
+int pgb_ssf_device_async(pgb_ctx* h, const double* d_q, int nq, double* d_out) {
+    if (!h || !d_q || !d_out || nq <= 0) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    rc = c.ensure_scratch(scatter_work_bytes(c, nq, 0, 0)); if (rc) return rc;
+    return scatter_common(c, d_q, nq, 0, 0, d_out, c.d_scratch);
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

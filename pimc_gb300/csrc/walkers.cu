@@ -287,6 +287,35 @@ __device__ __forceinline__ bool metropolis(double dV, double tau, uint32_t hi, u
     return x < exp(a);
 }
 
+// The same test split in two so that the part that depends only on the
+// draw (x and an FP32 log x) runs before the pair sums end.  The screen then
+// takes the team total as its (hi, lo) FP32 pair: a32 = -tau (hi + lo) is
+// within about 1e-5 of a wherever |a| <= 37, far inside the 1e-3 band; the
+// band and x = 0 go to the exact FP64 comparison, so the outcome equals
+// metropolis() on dV = (double)hi + (double)lo.
+struct MetroDraw {
+    double x;
+    float lx;
+};
+
+__device__ __forceinline__ MetroDraw metropolis_draw(uint32_t hi, uint32_t lo) {
+    MetroDraw d;
+    d.x = u01d(hi, lo);
+    d.lx = (d.x > 0.0) ? __logf((float)d.x) : 0.f;
+    return d;
+}
+
+__device__ __forceinline__ bool metropolis_ff(float hi, float lo, double tau, float tauf,
+                                              const MetroDraw& d) {
+    if (d.x > 0.0) {
+        const float diff = -(tauf * (hi + lo)) - d.lx;
+        if (diff > 1e-3f) return true;
+        if (diff < -1e-3f) return false;
+    }
+    const double a = -(tau * ((double)hi + (double)lo));
+    return a >= 0.0 || d.x < exp(a);
+}
+
 constexpr int kTeamCta = 256;
 
 __device__ __forceinline__ void team_sync(int slot, int nthreads) {
@@ -1321,8 +1350,11 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 if (pre) stage_increments(Isel((u + 1) & 1), m, u + 1, g0, g1, Dn.len, tt, T);
                 MoveDesc Dnn = Dn;
                 if (has_nn) Dnn = draw_move(u + 2, g0, g1, m, p_com, var_updates);
-                uint4 ra = make_uint4(0u, 0u, 0u, 0u);
-                if (tt == 0) ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
+                MetroDraw md{0.0, 0.f};
+                if (tt == 0) {
+                    const uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
+                    md = metropolis_draw(ra.x, ra.y);
+                }
                 KahanF acc;
                 for (int j = j0; j < N; j += jstep) {
                     if (j == i) continue;
@@ -1349,7 +1381,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                     const float2 v = ff_butterfly(lane < nw ? ffr[lane].x : 0.f, lane < nw ? ffr[lane].y : 0.f);
                     int ok = 0;
                     if (lane == 0) {
-                        ok = metropolis((double)v.x + (double)v.y, tau, ra.x, ra.y) ? 1 : 0;
+                        ok = metropolis_ff(v.x, v.y, tau, (float)tau, md) ? 1 : 0;
                         att1 += 1; acc1 += ok; nbu += nmove;
                     }
                     ok = __shfl_sync(0xffffffffu, ok, 0);
