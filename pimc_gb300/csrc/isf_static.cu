@@ -58,19 +58,26 @@ __global__ void __launch_bounds__(kBlock)
 k_rhoq32_aos(const double* __restrict__ beads, int M, int N, int Ne, double3 side,
              double3 sideInv, const double* __restrict__ q, int nq, float2* __restrict__ rho) {
     extern __shared__ float4 su[];
+    int4* si = reinterpret_cast<int4*>(su + N);
     const int t = blockIdx.y;
     const double* X = beads + (size_t)t * Ne * 3;
-    for (int j = threadIdx.x; j < N; j += blockDim.x)
-        su[j] = make_float4((float)(X[3 * j] * sideInv.x), (float)(X[3 * j + 1] * sideInv.y),
-                            (float)(X[3 * j + 2] * sideInv.z), 0.f);
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const double ux = X[3 * j] * sideInv.x, uy = X[3 * j + 1] * sideInv.y, uz = X[3 * j + 2] * sideInv.z;
+        su[j] = make_float4((float)ux, (float)uy, (float)uz, 0.f);
+        si[j] = make_int4(fixed_turns(ux), fixed_turns(uy), fixed_turns(uz), 0);
+    }
     __syncthreads();
     const int iq = blockIdx.x * kBlock + threadIdx.x;
     if (iq >= nq) return;
     const double inv2pi = 0.15915494309189533577;
-    const float nx = (float)(q[3 * iq] * side.x * inv2pi);
-    const float ny = (float)(q[3 * iq + 1] * side.y * inv2pi);
-    const float nz = (float)(q[3 * iq + 2] * side.z * inv2pi);
-    rho[(size_t)iq * M + t] = rho_partial(su, N, nx, ny, nz);
+    const double dx = q[3 * iq] * side.x * inv2pi, dy = q[3 * iq + 1] * side.y * inv2pi,
+                 dz = q[3 * iq + 2] * side.z * inv2pi;
+    const double rx = rint(dx), ry = rint(dy), rz = rint(dz);
+    const bool lattice = fabs(dx - rx) < 1e-6 && fabs(dy - ry) < 1e-6 && fabs(dz - rz) < 1e-6 &&
+                         fabs(rx) < 1048576.0 && fabs(ry) < 1048576.0 && fabs(rz) < 1048576.0;
+    rho[(size_t)iq * M + t] = lattice
+        ? rho_partial_lattice(si, N, (int)rx, (int)ry, (int)rz)
+        : rho_partial(su, N, (float)dx, (float)dy, (float)dz);
 }
 
 }  // namespace
@@ -91,7 +98,7 @@ extern "C" int pgb_isf_static(const double* d_beads, int num_slices, int num_ptc
                          " densities (16 MiB); split the q-vectors over several calls");
         return PGB_EINVAL;
     }
-    if ((size_t)num_ptcl * sizeof(float4) > 200 * 1024) {
+    if ((size_t)num_ptcl * (sizeof(float4) + sizeof(int4)) > 200 * 1024) {
         set_global_error("isf_static: num_ptcl too large for one slice in shared memory");
         return PGB_EINVAL;
     }
@@ -110,7 +117,7 @@ extern "C" int pgb_isf_static(const double* d_beads, int num_slices, int num_ptc
     dim3 grid((nq + kBlock - 1) / kBlock, num_slices);
     double3 sd = make_double3(side[0], side[1], side[2]);
     double3 si = make_double3(1.0 / side[0], 1.0 / side[1], 1.0 / side[2]);
-    k_rhoq32_aos<<<grid, kBlock, (size_t)num_ptcl * sizeof(float4), s>>>(
+    k_rhoq32_aos<<<grid, kBlock, (size_t)num_ptcl * (sizeof(float4) + sizeof(int4)), s>>>(
         d_beads, num_slices, num_ptcl, ptcl_extent, sd, si, d_qvecs, nq, rho);
     e = cudaGetLastError();
     if (e == cudaSuccess)

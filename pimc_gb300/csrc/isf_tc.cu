@@ -54,11 +54,6 @@ __host__ __device__ __forceinline__ size_t tiled_index(int r, int k, int K, int 
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// byte offset of element (r, k) of a [rows x 64] bf16 chunk in core-matrix layout
-__device__ __forceinline__ uint32_t cm_offset(int r, int kg) {
-    return (uint32_t)((r >> 3) * 1024 + kg * 128 + (r & 7) * 16);
-}
-
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);          // start address
@@ -117,10 +112,6 @@ __device__ __forceinline__ void bar_expect_tx(uint64_t* bar, uint32_t bytes) {
                  :: "r"(su32(bar)), "r"(bytes) : "memory");
 }
 
-__device__ __forceinline__ void bar_arrive(uint64_t* bar) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}"
-                 :: "r"(su32(bar)) : "memory");
-}
 
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
@@ -237,6 +228,7 @@ k_gemm_split_bf16(const __nv_bfloat16* __restrict__ Ah, const __nv_bfloat16* __r
     const bool ok = (*(volatile int*)s_fail == 0);
     if (!ok && tid == 0 && err) atomicExch(err, 1);
     if (ok) {
+        const float scalef = (float)scale;
         // epilogue: warp w owns TMEM lanes 32w..32w+31 (rows)
         const int r = 32 * warp + lane;
         const int row = row0 + r;
@@ -251,11 +243,12 @@ k_gemm_split_bf16(const __nv_bfloat16* __restrict__ Ah, const __nv_bfloat16* __r
                         P[(size_t)row * ldp + w0 + j] = fmaf(v[2 * j], v[2 * j], v[2 * j + 1] * v[2 * j + 1]);
                 }
             } else {
+                // FP32 scale, FP64 result formed on the integer pipes
                 if (row < rows_valid) {
                     #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         const int col = col0 + 32 * cc + j;
-                        if (col < cols_valid) out[(size_t)row * ldo + col] = scale * (double)v[j];
+                        if (col < cols_valid) out[(size_t)row * ldo + col] = f32_to_f64_alu(scalef * v[j]);
                     }
                 }
             }

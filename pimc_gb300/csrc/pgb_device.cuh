@@ -259,6 +259,54 @@ __device__ __forceinline__ float2 rho_partial(const float4* __restrict__ su, int
     return make_float2(re.s - re.c, im.s - im.c);
 }
 
+// Fixed-point form of the phase for lattice wave vectors q = 2 pi n / L
+// (integer n_d).  With positions as 32-bit fractions of the box,
+// U_d = round(r_d / L_d 2^32) mod 2^32, the phase in turns is
+// n . U / 2^32, and the 32-bit integer multiply-adds wrap exactly modulo one
+// turn: no rounding, no range reduction.  The top 23 bits (rounded) become an
+// angle in [-pi, pi) through an exponent trick on the add pipe.
+__device__ __forceinline__ int fixed_turns(double u) {
+    // u = r / L; |u| <= 1 for positions inside the box
+    return (int)(unsigned int)(long long)rint(u * 4294967296.0);
+}
+
+__device__ __forceinline__ float2 rho_partial_lattice(const int4* __restrict__ su, int n, int nx,
+                                                      int ny, int nz) {
+    KahanF re, im;
+    int j = 0;
+    while (j < n) {
+        float cr = 0.f, ci = 0.f;
+        const int jend = min(n, j + 32);
+        #pragma unroll 4
+        for (; j < jend; ++j) {
+            const int4 u = su[j];
+            // unsigned arithmetic: the products wrap modulo 2^32 by definition
+            const unsigned int p = (unsigned int)nx * (unsigned int)u.x + (unsigned int)ny * (unsigned int)u.y +
+                                   (unsigned int)nz * (unsigned int)u.z + 0x80000100u;
+            const float t = __uint_as_float(0x4B000000u | (p >> 9)) - 8388608.0f;   // [0, 2^23)
+            float sn, cs;
+            __sincosf(fmaf(t, 7.490140565847857e-07f, -3.14159265358979f), &sn, &cs);   // 2 pi / 2^23
+            cr += cs;
+            ci += sn;
+        }
+        re.add(cr);
+        im.add(ci);
+    }
+    return make_float2(re.s - re.c, im.s - im.c);
+}
+
+// FP32 -> FP64 with integer operations: exact for normal numbers, zero,
+// infinities and NaN; FP32 subnormals become signed zero.  For epilogues that
+// would otherwise queue one conversion per output on the narrow FP64 pipe.
+__device__ __forceinline__ double f32_to_f64_alu(float f) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int e = (b >> 23) & 0xFFu;
+    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+    const unsigned long long ex = (e == 0u) ? 0ull : (e == 0xFFu) ? 0x7FFull : (unsigned long long)(e + 896u);
+    const unsigned long long mant = (e == 0u) ? 0ull : (unsigned long long)(b & 0x7FFFFFu) << 29;
+    return __longlong_as_double((long long)(sign | (ex << 52) | mant));
+}
+
 // Nanoseconds of the GPU's global timer (PTX %globaltimer).
 __device__ __forceinline__ unsigned long long gtimer_ns() {
     unsigned long long t;

@@ -12,37 +12,49 @@
 namespace pgb {
 
 // One CTA = one slice t x 256 q-vectors; each thread owns one q and streams
-// the slice's beads from shared memory (broadcast reads) through
-// rho_partial: q . r / 2pi = sum_d n_d u_d with n_d = q_d L_d / 2pi and
-// u_d = r_d / L_d, reduced in turns so that __sincosf sees |angle| <= pi.
-// Rounding runs on the FP32 add pipe, leaving the special-function pipe to
-// the sine and cosine alone.
+// the slice's beads from shared memory (broadcast reads).  q . r / 2pi =
+// sum_d n_d u_d with n_d = q_d L_d / 2pi and u_d = r_d / L_d.  Lattice q
+// (integer n_d) use the fixed-point phase (rho_partial_lattice: three integer
+// multiply-adds, no rounding); others the FP32 turn reduction (rho_partial).
+// Either way __sincosf sees |angle| <= pi and the special-function pipe does
+// only the sine and cosine.
 constexpr int kRhoBlock = 256;
 
 __global__ void __launch_bounds__(kRhoBlock)
 k_rhoq32(PathView v, const double* __restrict__ q, int nq, float2* __restrict__ rho) {
     extern __shared__ float4 su[];
+    int4* si = reinterpret_cast<int4*>(su + v.Ne);
     const int t = blockIdx.y;
     const int n = v.nbs[t];
     const double* X = v.pos + (size_t)t * 3 * v.Ne;
-    for (int j = threadIdx.x; j < n; j += blockDim.x)
-        su[j] = make_float4((float)(X[j] * v.sideInv[0]), (float)(X[v.Ne + j] * v.sideInv[1]),
-                            (float)(X[2 * v.Ne + j] * v.sideInv[2]), 0.f);
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double ux = X[j] * v.sideInv[0], uy = X[v.Ne + j] * v.sideInv[1],
+                     uz = X[2 * v.Ne + j] * v.sideInv[2];
+        su[j] = make_float4((float)ux, (float)uy, (float)uz, 0.f);
+        si[j] = make_int4(fixed_turns(ux), fixed_turns(uy), fixed_turns(uz), 0);
+    }
     __syncthreads();
     const int iq = blockIdx.x * kRhoBlock + threadIdx.x;
     if (iq >= nq) return;
     const double inv2pi = 0.15915494309189533577;
-    const float nx = (float)(q[3*iq] * v.side[0] * inv2pi);
-    const float ny = (float)(q[3*iq+1] * v.side[1] * inv2pi);
-    const float nz = (float)(q[3*iq+2] * v.side[2] * inv2pi);
-    rho[(size_t)iq * v.M + t] = rho_partial(su, n, nx, ny, nz);
+    const double dx = q[3*iq] * v.side[0] * inv2pi, dy = q[3*iq+1] * v.side[1] * inv2pi,
+                 dz = q[3*iq+2] * v.side[2] * inv2pi;
+    const double rx = rint(dx), ry = rint(dy), rz = rint(dz);
+    // lattice wave vectors (the reference's q lists of lattice type) take the
+    // exact fixed-point phase; any other q the FP32 turn reduction
+    const bool lattice = fabs(dx - rx) < 1e-6 && fabs(dy - ry) < 1e-6 && fabs(dz - rz) < 1e-6 &&
+                         fabs(rx) < 1048576.0 && fabs(ry) < 1048576.0 && fabs(rz) < 1048576.0;
+    rho[(size_t)iq * v.M + t] = lattice
+        ? rho_partial_lattice(si, n, (int)rx, (int)ry, (int)rz)
+        : rho_partial(su, n, (float)dx, (float)dy, (float)dz);
 }
 
 cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* d_rho,
                           cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
     dim3 grid((nq + kRhoBlock - 1) / kRhoBlock, v.M);
-    size_t smem = (size_t)v.Ne * sizeof(float4);
+    size_t smem = (size_t)v.Ne * (sizeof(float4) + sizeof(int4));
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;   // one slice must fit in shared memory
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_rhoq32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
