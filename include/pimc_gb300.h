@@ -246,7 +246,10 @@ long long pgb_walkers_launch_count(pgb_walkers* w);
  * 5008/5016 (6008/6016) = the same with the next move's rows prefetched into
  * a second buffer, 256 (512)-thread CTAs, teams of up to 8 (16) warps;
  * 5000 (6000) = the same with team warps proportional to each walker's cost
- * N^2 M, the costliest walker getting all 8 (16) */
+ * N^2 M, the costliest walker getting all 8 (16); 7000/7008/7016 = teams
+ * sized as 6000/6008/6016 that split in two halves to make two consecutive
+ * staging moves at once when their imaginary-time intervals are disjoint
+ * (such moves commute, so the chain is that of making them in turn) */
 int pgb_walkers_threads(pgb_walkers* w);
 /* the autotuner's record: schedules tried and one-sweep time (ms) of each;
  * returns the number of candidates, fills at most cap */

@@ -1545,6 +1545,347 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
     }
 }
 
+// ---------------------------------------------------------------------------
+// Two-move schedule.  Consecutive staging moves whose closed imaginary-time
+// intervals [s0, s0 + len] (mod M) are disjoint read and write disjoint rows
+// of the slab, so they commute: running them at once gives the chain of
+// running them one after the other.  A team of nw >= 2 warps splits into two
+// halves; when moves u and u + 1 are such a pair, half 0 makes move u and
+// half 1 move u + 1, each with its own row buffer, bridge, pair sums and
+// decision; otherwise the whole team makes move u alone.  Centre-of-mass
+// moves and energy samples use the whole team as in the pipelined schedule.
+// One half's serial work (copy wait, bridge, decision, write-back) overlaps
+// the other half's pair sums.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool stage_disjoint(const MoveDesc& a, const MoveDesc& b, int M) {
+    int d1 = b.s0 - a.s0; if (d1 < 0) d1 += M;
+    int d2 = a.s0 - b.s0; if (d2 < 0) d2 += M;
+    return d1 > a.len && d2 > b.len;
+}
+
+// named barrier of half h of a team starting at warp `slot` (ids slot + 2,
+// slot + 3 lie inside the team's own range slot + 1 .. slot + nw)
+__device__ __forceinline__ void half_sync(int slot, int h, int HT) {
+    if (HT == 32) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" :: "r"(slot + 2 + h), "r"(HT) : "memory");
+}
+
+template <int CTA, int MINB>
+__global__ void __launch_bounds__(CTA, MINB)
+k_walkers_pair2(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
+                float4* __restrict__ pos, WalkerAcc* __restrict__ accs,
+                unsigned long long* __restrict__ ctr, int* __restrict__ err, int sweeps, int measure,
+                AzizF az, double tau, double lambda, float p_com, int var_updates, uint64_t seed) {
+    constexpr int NW = CTA / 32;
+    extern __shared__ float4 dyn[];
+    __shared__ float4 s_new[NW][kMaxStage];
+    __shared__ float2 s_ff[NW][NW];
+    __shared__ double s_red[NW][NW];
+    __shared__ int s_acc[NW];
+    __shared__ int s_fail[NW];
+    __shared__ __align__(8) uint64_t s_bar[NW][2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int4 tm = make_int4(-1, 0, 0, 0);
+    for (int k = 0; k < NW; ++k) {
+        int4 t = teams[blockIdx.x * NW + k];
+        if (t.w && warp >= t.y && warp < t.y + t.z) tm = t;
+    }
+    if (tm.x < 0) return;
+    const int w = tm.x, slot = tm.y, nw = tm.z, T = nw * 32;
+    const int tt = threadIdx.x - slot * 32, wi = warp - slot;
+    const int hw = nw / 2;                       // warps per half (0: no split)
+    const WalkerMeta m = meta[w];
+    float4* P = pos + m.off;
+    const int N = m.N, M = m.M, C = m.mbar, R = C + 1;
+    float4* const B0 = dyn + (tm.w - 1);
+    float4* const B1 = B0 + (size_t)R * N;
+    float4* const I0 = B1 + (size_t)R * N;
+    float4* const I1 = I0 + kMaxStage;
+    uint64_t* const bar0 = &s_bar[slot][0];
+    uint64_t* const bar1 = &s_bar[slot][1];
+    auto Bsel = [&](int x) { return x ? B1 : B0; };
+    auto barsel = [&](int x) { return x ? bar1 : bar0; };
+    double* red = s_red[slot];
+    int* fail = &s_fail[slot];
+    if (tt == 0) { mbar_init(bar0, 1); mbar_init(bar1, 1); *fail = 0; }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    team_sync(slot, T);
+    uint32_t ph0 = 0u, ph1 = 0u;
+    auto phsel = [&](int x) { return x ? ph1 : ph0; };
+    auto phflip = [&](int x) { if (x) ph1 ^= 1u; else ph0 ^= 1u; };
+    const unsigned long long sweep0 = ctr[w];
+    double esum = 0.0, esumsq = 0.0;
+    long long nsamp = 0, nbu = 0, att0 = 0, att1 = 0, acc0 = 0, acc1 = 0;
+    const int Gt = (T >= N) ? T / N : 1;
+    const int j0t = (T >= N) ? ((tt < Gt * N) ? tt % N : N) : tt;
+    const int kb0t = (T >= N) ? tt / N : 0;
+    const int jstept = (T >= N) ? N : T;
+    auto drain = [&](int b) {
+        long long n = 0;
+        while (!mbar_try_wait(barsel(b), phsel(b)))
+            if (++n > kWaitLimit) break;
+    };
+
+    for (int sw = 0; sw < min(sweeps, m.max_sweeps); ++sw) {
+        const unsigned long long gs = sweep0 + sw;
+        const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
+        int u = 0;
+        while (u < m.num_updates) {
+            const MoveDesc D0 = draw_move(u, g0, g1, m, p_com, var_updates);
+            if (!D0.com) {
+                bool two = false;
+                MoveDesc D1 = D0;
+                if (hw > 0 && u + 1 < m.num_updates) {
+                    D1 = draw_move(u + 1, g0, g1, m, p_com, var_updates);
+                    two = !D1.com && stage_disjoint(D0, D1, M);
+                }
+                // this thread's group: the whole team, or its half
+                const int h = (two && wi >= hw) ? 1 : 0;
+                const int HT = two ? hw * 32 : T;
+                const int ht = tt - h * hw * 32, wih = wi - h * hw;
+                const int nwg = two ? hw : nw;
+                const MoveDesc D = h ? D1 : D0;
+                const int uh = u + h;
+                const int i = D.i, s0 = D.s0, len = D.len, nmove = D.nmove;
+                float4* const buf = Bsel(h);
+                float4* const inc = h ? I1 : I0;
+                float4* const sn = s_new[slot + h * hw];
+                float2* const ffr = s_ff[slot + h * hw];
+                auto gsync = [&]() { if (two) half_sync(slot, h, HT); else team_sync(slot, T); };
+                // rows s0 .. s0 + len, increments and the acceptance draw
+                if (ht == 0) issue_rows(buf, P, N, M, s0, len + 1, barsel(h));
+                stage_increments(inc, m, uh, g0, g1, len, ht, HT);
+                MetroDraw md{0.0, 0.f};
+                if (ht == 0) {
+                    const uint4 ra = wrand(m.key, (uint32_t)uh, g0, g1, 0xFFFFu);
+                    md = metropolis_draw(ra.x, ra.y);
+                }
+                gsync();
+                if (wih == 0) {
+                    long long nwait = 0;
+                    bool landed = true;
+                    while (!mbar_try_wait(barsel(h), phsel(h)))
+                        if (++nwait > kWaitLimit) { landed = false; break; }
+                    landed = __all_sync(0xffffffffu, landed);
+                    if (!landed) {
+                        // give the copy one more bounded wait before the team leaves
+                        if (lane == 0) { atomicExch(fail, 1); atomicExch(err + w, 1); drain(h); }
+                    } else {
+                        const float4 x0 = buf[i], xe = buf[(size_t)len * N + i];
+                        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+                        const float4 i1 = (lane < len) ? inc[lane] : zero;
+                        const float4 i2 = (lane + 32 < len) ? inc[lane + 32] : zero;
+                        const float W1x = warp_scan_incl(i1.x, lane), W1y = warp_scan_incl(i1.y, lane),
+                                    W1z = warp_scan_incl(i1.z, lane);
+                        const float W2x = warp_scan_incl(i2.x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
+                        const float W2y = warp_scan_incl(i2.y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
+                        const float W2z = warp_scan_incl(i2.z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
+                        const int src = (len <= 32) ? len - 1 : len - 33;
+                        const float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
+                        const float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
+                        const float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
+                        const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
+                        const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
+                        const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
+                        const float il = 1.0f / (float)len;
+                        #pragma unroll
+                        for (int hh = 0; hh < 2; ++hh) {
+                            const int k = lane + 32 * hh;
+                            if (k < nmove) {
+                                const float f = (float)(k + 1) * il;
+                                const float Wx = hh ? W2x : W1x, Wy = hh ? W2y : W1y, Wz = hh ? W2z : W1z;
+                                sn[k] = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
+                                                    put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
+                                                    put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
+                            }
+                        }
+                    }
+                }
+                gsync();
+                if (!*(volatile int*)fail) {
+                    const int G = (HT >= N) ? HT / N : 1;
+                    const int j0 = (HT >= N) ? ((ht < G * N) ? ht % N : N) : ht;
+                    const int kb0 = (HT >= N) ? ht / N : 0;
+                    const int jstep = (HT >= N) ? N : HT;
+                    KahanF acc;
+                    for (int j = j0; j < N; j += jstep) {
+                        if (j == i) continue;
+                        #pragma unroll 4
+                        for (int k = kb0; k < nmove; k += G) {
+                            const float4 pj = buf[(size_t)(k + 1) * N + j];
+                            const float4 a = sn[k], b = buf[(size_t)(k + 1) * N + i];
+                            const float ax = min_image32(a.x - pj.x, m.L, m.Linv);
+                            const float ay = min_image32(a.y - pj.y, m.L, m.Linv);
+                            const float az_ = min_image32(a.z - pj.z, m.L, m.Linv);
+                            const float bx = min_image32(b.x - pj.x, m.L, m.Linv);
+                            const float by = min_image32(b.y - pj.y, m.L, m.Linv);
+                            const float bz = min_image32(b.z - pj.z, m.L, m.Linv);
+                            acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                                    aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+                        }
+                    }
+                    const float2 part = warp_ff(acc);
+                    if (lane == 0) ffr[wih] = part;
+                    gsync();
+                    if (wih == 0) {
+                        const float2 v = ff_butterfly(lane < nwg ? ffr[lane].x : 0.f,
+                                                      lane < nwg ? ffr[lane].y : 0.f);
+                        int ok = 0;
+                        if (lane == 0) {
+                            ok = metropolis_ff(v.x, v.y, tau, (float)tau, md) ? 1 : 0;
+                            att1 += 1; acc1 += ok; nbu += nmove;
+                        }
+                        ok = __shfl_sync(0xffffffffu, ok, 0);
+                        if (ok) {
+                            for (int k = lane; k < nmove; k += 32) {
+                                int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                                P[(size_t)sl * N + i] = sn[k];
+                            }
+                            fence_proxy_async_global();
+                        }
+                        __syncwarp();
+                    }
+                }
+                phflip(0);
+                if (two) phflip(1);
+                // both moves written back (and visible to later copies) before
+                // the buffers and the slab rows are reused
+                team_sync(slot, T);
+                if (*(volatile int*)fail) return;
+                u += two ? 2 : 1;
+            } else {
+                const int i = D0.i;
+                const float sx = D0.sx, sy = D0.sy;
+                const uint4 r1 = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFEu);
+                const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
+                KahanF acc;
+                int b = 0;
+                if (tt == 0) issue_rows(Bsel(b), P, N, M, 0, min(C, M), barsel(b));
+                for (int c0 = 0; c0 < M; c0 += C) {
+                    const int nr = min(C, M - c0), nb0 = c0 + C;
+                    if (nb0 < M && tt == 0) issue_rows(Bsel(b ^ 1), P, N, M, nb0, min(C, M - nb0), barsel(b ^ 1));
+                    if (!team_wait(barsel(b), phsel(b), slot, T, fail, err + w)) {
+                        if (tt == 0 && nb0 < M) drain(b ^ 1);
+                        return;
+                    }
+                    phflip(b);
+                    const float4* buf = Bsel(b);
+                    for (int j = j0t; j < N; j += jstept) {
+                        if (j == i) continue;
+                        #pragma unroll 4
+                        for (int t = kb0t; t < nr; t += Gt) {
+                            const float4 pi = buf[t * N + i], pj = buf[t * N + j];
+                            const float bx = min_image32(pi.x - pj.x, m.L, m.Linv);
+                            const float by = min_image32(pi.y - pj.y, m.L, m.Linv);
+                            const float bz = min_image32(pi.z - pj.z, m.L, m.Linv);
+                            const float ax = min_image32(bx + sx, m.L, m.Linv);
+                            const float ay = min_image32(by + sy, m.L, m.Linv);
+                            const float az_ = min_image32(bz + sz, m.L, m.Linv);
+                            acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                                    aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+                        }
+                    }
+                    team_sync(slot, T);
+                    b ^= 1;
+                }
+                const float2 part = warp_ff(acc);
+                if (lane == 0) s_ff[slot][wi] = part;
+                team_sync(slot, T);
+                if (wi == 0) {
+                    const float2 v = ff_butterfly(lane < nw ? s_ff[slot][lane].x : 0.f,
+                                                  lane < nw ? s_ff[slot][lane].y : 0.f);
+                    if (lane == 0) s_acc[slot] = metropolis((double)v.x + (double)v.y, tau, r1.y, r1.z) ? 1 : 0;
+                }
+                team_sync(slot, T);
+                const int ok = s_acc[slot];
+                if (ok) {
+                    for (int t2 = tt; t2 < M; t2 += T) {
+                        float4 pi = P[(size_t)t2 * N + i];
+                        pi.x = put_inside(pi.x + sx, m.L, m.Linv);
+                        pi.y = put_inside(pi.y + sy, m.L, m.Linv);
+                        pi.z = put_inside(pi.z + sz, m.L, m.Linv);
+                        P[(size_t)t2 * N + i] = pi;
+                    }
+                    fence_proxy_async_global();
+                }
+                team_sync(slot, T);
+                if (tt == 0) { att0 += 1; acc0 += ok; nbu += M; }
+                u += 1;
+            }
+        }
+        if (measure > 0 && ((gs + 1) % (unsigned long long)measure) == 0) {
+            KahanF pot, kin;
+            const int half = (N - 1) / 2;
+            const bool even = (N % 2) == 0;
+            int b = 0;
+            if (tt == 0) issue_rows(Bsel(b), P, N, M, 0, min(C, M), barsel(b));
+            for (int c0 = 0; c0 < M; c0 += C) {
+                const int nr = min(C, M - c0), nb0 = c0 + C;
+                if (nb0 < M && tt == 0) issue_rows(Bsel(b ^ 1), P, N, M, nb0, min(C, M - nb0), barsel(b ^ 1));
+                if (!team_wait(barsel(b), phsel(b), slot, T, fail, err + w)) {
+                    if (tt == 0 && nb0 < M) drain(b ^ 1);
+                    return;
+                }
+                phflip(b);
+                const float4* buf = Bsel(b);
+                for (int idx = tt; idx < nr * N; idx += T) {
+                    const int t = idx / N, ii = idx - t * N;
+                    const float4 ri = buf[t * N + ii];
+                    const int cnt = half + ((even && ii < N / 2) ? 1 : 0);
+                    for (int d = 1; d <= cnt; ++d) {
+                        int jj = ii + d; if (jj >= N) jj -= N;
+                        const float4 rj = buf[t * N + jj];
+                        const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
+                        const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
+                        const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
+                        pot.add(aziz_v32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+                    }
+                }
+                team_sync(slot, T);
+                b ^= 1;
+            }
+            for (int idx = tt; idx < M * N; idx += T) {
+                const int t = idx / N, ii = idx - t * N;
+                const int tn = (t + 1 == M) ? 0 : t + 1;
+                const float4 ri = P[(size_t)t * N + ii], rn = P[(size_t)tn * N + ii];
+                const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
+                const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
+                const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
+                kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+            }
+            const double pv = warp_sum(pot.value()), kv = warp_sum(kin.value());
+            if (lane == 0) red[wi] = pv;
+            team_sync(slot, T);
+            double V = 0.0;
+            if (tt == 0) for (int q = 0; q < nw; ++q) V += red[q];
+            team_sync(slot, T);
+            if (lane == 0) red[wi] = kv;
+            team_sync(slot, T);
+            if (tt == 0) {
+                double K2 = 0.0;
+                for (int q = 0; q < nw; ++q) K2 += red[q];
+                const double totK = 1.5 * N / tau - K2 * ((0.25 / (lambda * tau)) / (tau * M));
+                const double e = (totK + V / M + m.tailV) / N;
+                esum += e; esumsq += e * e; nsamp += 1;
+            }
+            team_sync(slot, T);
+        }
+    }
+    if (tt == 0) {
+        WalkerAcc& A = accs[w];
+        A.esum += esum; A.esumsq += esumsq; A.samples += nsamp;
+        A.att[0] += att0; A.acc[0] += acc0;
+        ctr[w] = sweep0 + min(sweeps, m.max_sweeps);
+    }
+    // staging counters live with each group's deciding thread (team thread 0
+    // and the second half's thread 0)
+    if (tt == 0 || (hw > 0 && tt == hw * 32)) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].att[1]), (unsigned long long)att1);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].acc[1]), (unsigned long long)acc1);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].bead_updates), (unsigned long long)nbu);
+    }
+}
+
 __global__ void k_walkers_init(const WalkerMeta* __restrict__ meta, float4* __restrict__ pos,
                                const int* __restrict__ list) {
     const int w = list ? list[blockIdx.x] : blockIdx.x;
@@ -1641,9 +1982,9 @@ struct pgb_walkers {
     int* d_err = nullptr;                 // per-walker error word (bounded waits)
     // packed-team schedules, one per pairs-per-thread target
     // 0-2 team targets, 3 windows, 4-6 TMA targets, 7-10 pipelined (256/8, 256/16, 512/8, 512/16)
-    int4* d_teams[13] = {nullptr};
-    int team_ctas[13] = {0};
-    size_t team_smem[13] = {0};
+    int4* d_teams[16] = {nullptr};
+    int team_ctas[16] = {0};
+    size_t team_smem[16] = {0};
     // autotuner record: schedule and one-sweep time of each candidate
     std::vector<int> tune_sched;
     std::vector<float> tune_ms;
@@ -1794,6 +2135,22 @@ cudaError_t build_windows(pgb_walkers* h) {
 
 cudaError_t launch_run(pgb_walkers* h, int sched, int sweeps, int measure) {
     AzizF af = make_aziz_f(h->az);
+    if (sched >= 7000) {
+        const int ppt = sched % 1000;
+        const int k = 13 + (ppt == 0 ? 0 : ppt == 8 ? 1 : 2);
+        cudaError_t e = build_pipe_teams(h, k, 512, ppt);
+        if (e != cudaSuccess) return e;
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_walkers_pair2<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            attr = true;
+        }
+        k_walkers_pair2<512, 1><<<h->team_ctas[k], 512, h->team_smem[k], h->stream>>>(h->d_meta,
+            h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
+            h->lambda, (float)h->p_com, h->var_updates, h->seed);
+        h->launches += 1;
+        return cudaGetLastError();
+    }
     if (sched >= 5000) {
         const int ppt = sched % 1000;
         const int cta = (sched >= 6000) ? 512 : 256;
@@ -1897,9 +2254,9 @@ int autotune(pgb_walkers* h) {
     cudaMemcpyAsync(save_ctr, h->d_ctr, h->W * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream);
     cudaEvent_t a, b;
     cudaEventCreate(&a); cudaEventCreate(&b);
-    const int cand[9] = {2008, 4008, 5000, 5008, 5016, 6000, 6008, 6016, 3002};
+    const int cand[12] = {2008, 4008, 5000, 5008, 5016, 6000, 6008, 6016, 3002, 7000, 7008, 7016};
     float best = 1e30f; int best_t = 6000;
-    for (int c = 0; c < 9; ++c) {
+    for (int c = 0; c < 12; ++c) {
         cudaMemcpyAsync(h->d_pos, save, pb, cudaMemcpyDeviceToDevice, h->stream);
         cudaMemcpyAsync(h->d_ctr, save_ctr, h->W * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream);
         cudaEventRecord(a, h->stream);
@@ -1948,13 +2305,15 @@ int pgb_walkers_create(const pgb_walkers_params* p, pgb_walkers** out) {
         const int t = p->threads_per_walker;
         const bool team = (t / 1000 == 1 || t / 1000 == 2) && (t % 1000 == 4 || t % 1000 == 8 || t % 1000 == 16);
         const bool win = (t == 3002 || t == 3003 || t == 4004 || t == 4008 || t == 4016 ||
-                          t == 5000 || t == 5008 || t == 5016 || t == 6000 || t == 6008 || t == 6016);
+                          t == 5000 || t == 5008 || t == 5016 || t == 6000 || t == 6008 || t == 6016 ||
+                          t == 7000 || t == 7008 || t == 7016);
         if (!(t == 0 || t == 64 || t == 128 || t == 256 || team || win)) {
             g_werr = "threads_per_walker must be 0 (autotune), 64/128/256 (one CTA per walker), "
                      "1004/1008/1016 / 2004/2008/2016 (packed teams, 4/8/16 pairs per thread, "
                      "3 or 2 CTAs per SM), 3002/3003 (time windows, 2 or 3 CTAs per SM) or "
                      "4004/4008/4016 (packed teams with TMA-staged rows) or 5000/5008/5016/6000/6008/"
-                     "6016 (pipelined TMA teams in 256/512-thread CTAs; x000 = cost-balanced teams)";
+                     "6016 (pipelined TMA teams in 256/512-thread CTAs; x000 = cost-balanced teams) "
+                     "or 7000/7008/7016 (two commuting moves at once in half-teams)";
             return PGB_EINVAL;
         }
     }

@@ -26,7 +26,7 @@ def _walkers(pgb, num, seed, sched, n=8, t=4.0, tau=0.004):
 
 
 @pytest.mark.parametrize("sched", [128, 1004, 1008, 1016, 2008, 3002, 3003, 4004, 4008, 4016,
-                                   5000, 5008, 5016, 6000, 6008, 6016])
+                                   5000, 5008, 5016, 6000, 6008, 6016, 7000, 7008, 7016])
 def test_schedule_runs_and_is_deterministic(pgb, sched):
     # N <= 90 keeps two Mbar-row buffers of every walker within the 100 KB
     # budget of the 256-thread pipelined schedules (5008/5016)
@@ -47,7 +47,7 @@ def test_schedule_runs_and_is_deterministic(pgb, sched):
     assert np.all(np.abs(runs[0][1]) <= L / 2 + 1e-5)
 
 
-@pytest.mark.parametrize("sched", [128, 3002, 5008, 6000])
+@pytest.mark.parametrize("sched", [128, 3002, 5008, 6000, 7016])
 def test_matched_energy_vs_oracle_walkers(pgb, oracle_lib, sched):
     num, equil, prod = 256, 60, 200
     W, p = _walkers(pgb, num, 11, sched)
