@@ -300,6 +300,22 @@ class Walkers:
                      bead_updates=s.bead_updates, attempted=list(s.attempted),
                      accepted=list(s.accepted)) for s in st]
 
+    # numpy view of pgb_walker_stats, one record per walker
+    STATS_DTYPE = np.dtype([("energy_sum", "<f8"), ("energy_sumsq", "<f8"), ("samples", "<i8"),
+                            ("bead_updates", "<i8"), ("attempted", "<i8", (2,)),
+                            ("accepted", "<i8", (2,))])
+
+    def stats_array(self, out=None):
+        """The per-walker accumulators as a structured array (columns
+        energy_sum, energy_sumsq, samples, bead_updates, attempted[2],
+        accepted[2]); `out` (from a previous call) is filled in place."""
+        if out is None:
+            out = np.zeros(self.W, dtype=self.STATS_DTYPE)
+        assert out.dtype == self.STATS_DTYPE and out.itemsize == C.sizeof(_lib.PgbWalkerStats)
+        self._chk(self.lib.pgb_walkers_stats(self.h, C.cast(out.ctypes.data,
+                                                            C.POINTER(_lib.PgbWalkerStats))))
+        return out
+
     def reset_stats(self):
         self._chk(self.lib.pgb_walkers_reset_stats(self.h))
 

@@ -88,6 +88,29 @@ int need_path(Ctx& c) {
     return PGB_OK;
 }
 
+// Same-slice forces for the O(n) gradient correction of the mixed form.  They
+// apply when the cutoff takes in every minimum-image separation, so that each
+// bead's list is its whole slice.  Returns the forces (valid until the next
+// position change) when they apply, nullptr otherwise.
+const float4* slice_forces(Ctx& c, int* rc) {
+    *rc = PGB_OK;
+    if (c.p.precision != PGB_MIXED) return nullptr;
+    if (!(c.p.gradvfactor[0] > kEPS || c.p.gradvfactor[1] > kEPS)) return nullptr;
+    const double far2 = 0.25 * (c.p.side[0] * c.p.side[0] + c.p.side[1] * c.p.side[1] +
+                                c.p.side[2] * c.p.side[2]);
+    if (!(c.p.rc * c.p.rc > far2)) return nullptr;
+    if (!c.d_force32) {
+        cudaError_t e = cudaMalloc(&c.d_force32, (size_t)c.M * c.Ne * sizeof(float4));
+        if (e != cudaSuccess) { c.d_force32 = nullptr; *rc = c.cuda_fail(e, "cudaMalloc(slice forces)"); return nullptr; }
+    }
+    if (!c.force_valid) {
+        cudaError_t e = launch_slice_forces32(c.view(), c.az, c.d_force32, c.stream);
+        if (e != cudaSuccess) { *rc = c.cuda_fail(e, "slice forces launch"); return nullptr; }
+        c.force_valid = true;
+    }
+    return c.d_force32;
+}
+
 // per-slice terms, internal layout [9][M]: vint g2 r1 r2 d1 d2 kin xch kinprev
 int compute_terms(Ctx& c, std::vector<double>& h, bool want_tmat) {
     int rc = need_path(c); if (rc) return rc;
@@ -213,6 +236,7 @@ int pgb_destroy(pgb_ctx* h) {
     cudaFree(c.d_on); cudaFree(c.d_nbs);
     if (c.d_scratch) cudaFree(c.d_scratch);
     if (c.d_tc_tables) cudaFree(c.d_tc_tables);
+    if (c.d_force32) cudaFree(c.d_force32);
     if (c.h_pinned) cudaFreeHost(c.h_pinned);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
@@ -305,6 +329,7 @@ int pgb_load_path(pgb_ctx* h, const double* pos, const int32_t* next, const int3
     PGB_CUDA(&c, launch_pos32_from64(c.view(), c.d_pos32, c.stream));
     PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
     c.loaded = true;
+    c.force_valid = false;
     return PGB_OK;
 }
 
@@ -314,6 +339,7 @@ int pgb_load_positions_device_async(pgb_ctx* h, const double* d_pos) {
     size_t nb = (size_t)c.M * c.Ne;
     PGB_CUDA(&c, cudaMemcpyAsync(c.d_pos, d_pos, nb * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
     PGB_CUDA(&c, launch_pos32_from64(c.view(), c.d_pos32, c.stream));
+    c.force_valid = false;
     return PGB_OK;
 }
 
@@ -337,6 +363,7 @@ int pgb_update_beads(pgb_ctx* h, const int32_t* beads, const double* pos, int k)
         reinterpret_cast<const int2*>(dp), reinterpret_cast<const double*>(dp + bb), k);
     PGB_CUDA(&c, cudaGetLastError());
     PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    c.force_valid = false;
     return PGB_OK;
 }
 
@@ -376,9 +403,11 @@ int pgb_bead_actions(pgb_ctx* h, const int32_t* beads, int k, int shift, int mod
     double* d_o = reinterpret_cast<double*>(dp + ((bb + 15) & ~(size_t)15));
     PGB_CUDA(&c, cudaMemcpyAsync(dp, hp, bb, cudaMemcpyHostToDevice, c.stream));
     PathView v = c.view();
+    const float4* fall = slice_forces(c, &rc);
+    if (rc) return rc;
     cudaError_t e = (c.p.precision == PGB_MIXED)
         ? launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda,
-                                c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream)
+                                c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream, fall)
         : launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda,
                                 c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream);
     if (e != cudaSuccess) return c.cuda_fail(e, "bead actions launch");
@@ -798,11 +827,14 @@ int trial_launch(Ctx& c, const int2* d_b, const double* d_pos, int k, int shift,
     PathView v = c.view();
     cudaError_t e;
     if (c.p.precision == PGB_MIXED) {
+        int rc = PGB_OK;
+        const float4* fall = slice_forces(c, &rc);
+        if (rc) return rc;
         e = launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
-                                  c.p.gradvfactor, d_pos, d_new, c.stream);
+                                  c.p.gradvfactor, d_pos, d_new, c.stream, fall);
         if (e == cudaSuccess)
             e = launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
-                                      c.p.gradvfactor, nullptr, d_old, c.stream);
+                                      c.p.gradvfactor, nullptr, d_old, c.stream, fall);
     } else {
         e = launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
                                   c.p.gradvfactor, d_pos, d_new, c.stream);

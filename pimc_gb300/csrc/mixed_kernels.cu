@@ -52,8 +52,10 @@ constexpr int kBeadBlock32 = 256;
 __global__ void __launch_bounds__(kBeadBlock32)
 k_bead_actions32(PathView v, AzizF az, const int2* __restrict__ beads, int k, int shift,
                  int mode, double tau, double lambda, double vf0, double vf1, double gf0,
-                 double gf1, const double* __restrict__ over, double* __restrict__ out) {
+                 double gf1, const double* __restrict__ over, double* __restrict__ out,
+                 const float4* __restrict__ fall) {
     extern __shared__ float4 lpos[];
+    int* lidx = reinterpret_cast<int*>(lpos + v.Ne);
     __shared__ double red[kBeadBlock32 / 32];
     __shared__ int wcount[kBeadBlock32 / 32];
     __shared__ int s_total;
@@ -102,7 +104,11 @@ k_bead_actions32(PathView v, AzizF az, const int2* __restrict__ beads, int k, in
         __syncthreads();
         int off = s_total;
         for (int i = 0; i < w; ++i) off += wcount[i];
-        if (in) lpos[off + __popc(m & ((1u << lane) - 1u))] = rj;
+        if (in) {
+            const int slot_ = off + __popc(m & ((1u << lane) - 1u));
+            lpos[slot_] = rj;
+            lidx[slot_] = j;
+        }
         __syncthreads();
         if (tid == 0) { int tot = 0; for (int i = 0; i < kBeadBlock32 / 32; ++i) tot += wcount[i]; s_total += tot; }
         __syncthreads();
@@ -110,7 +116,42 @@ k_bead_actions32(PathView v, AzizF az, const int2* __restrict__ beads, int k, in
     const int nlist = s_total;
     double Vnn = need_v ? block_sum(vs.value(), red) : 0.0;
     double corr_g = 0.0;
-    if (need_c) {
+    if (need_c && fall) {
+        // Every active same-slice bead is in the list (rc covers the box), so
+        // the inner sum of gradVnnSquared, F3(b2) = sum over b3 != p, b2 of
+        // gradV(r_b2 - r_b3), does not depend on where p is: it is the slice
+        // force on b2 less p's own term at p's current position.  O(n) per bead.
+        const float4 rpo = P[p];
+        KahanF ts;
+        float f1x = 0.f, f1y = 0.f, f1z = 0.f;
+        const float4* Fs = fall + (size_t)s * Ne;
+        for (int n = tid; n < nlist; n += kBeadBlock32) {
+            const float4 r2v = lpos[n];
+            const float dx = min_image32(r2v.x - r1.x, L0, I0);
+            const float dy = min_image32(r2v.y - r1.y, L1, I1);
+            const float dz = min_image32(r2v.z - r1.z, L2, I2);
+            const float g = aziz_g32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az);
+            const float F2x = g * dx, F2y = g * dy, F2z = g * dz;
+            f1x -= F2x; f1y -= F2y; f1z -= F2z;
+            float Fox = F2x, Foy = F2y, Foz = F2z;
+            if (over) {
+                const float ox = min_image32(r2v.x - rpo.x, L0, I0);
+                const float oy = min_image32(r2v.y - rpo.y, L1, I1);
+                const float oz = min_image32(r2v.z - rpo.z, L2, I2);
+                const float go = aziz_g32(fmaf(ox, ox, fmaf(oy, oy, oz * oz)), az);
+                Fox = go * ox; Foy = go * oy; Foz = go * oz;
+            }
+            const float4 fa = Fs[lidx[n]];
+            const float F3x = fa.x - Fox, F3y = fa.y - Foy, F3z = fa.z - Foz;
+            const float d22 = fmaf(F2x, F2x, fmaf(F2y, F2y, F2z * F2z));
+            const float d23 = fmaf(F2x, F3x, fmaf(F2y, F3y, F2z * F3z));
+            ts.add(fmaf(2.0f, d23, d22));
+        }
+        double T = block_sum(ts.value(), red);
+        double Fx = block_sum((double)f1x, red), Fy = block_sum((double)f1y, red),
+               Fz = block_sum((double)f1z, red);
+        corr_g = T + (Fx * Fx + Fy * Fy + Fz * Fz);
+    } else if (need_c) {
         KahanF ts;
         float f1x = 0.f, f1y = 0.f, f1z = 0.f;
         for (int n = tid; n < nlist; n += kBeadBlock32) {
@@ -150,9 +191,10 @@ k_bead_actions32(PathView v, AzizF az, const int2* __restrict__ beads, int k, in
 cudaError_t launch_bead_actions32(const PathView& v, AzizParams a, const int2* d_beads, int k,
                                   int shift, int mode, double tau, double lambda,
                                   const double vf[2], const double gf[2], const double* d_over,
-                                  double* d_out, cudaStream_t s) {
+                                  double* d_out, cudaStream_t s, const float4* d_force) {
     if (k <= 0) return cudaSuccess;
-    size_t smem = (size_t)v.Ne * sizeof(float4);
+    size_t smem = (size_t)v.Ne * (sizeof(float4) + sizeof(int));
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;     // one slice's list in shared memory
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_bead_actions32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -160,7 +202,54 @@ cudaError_t launch_bead_actions32(const PathView& v, AzizParams a, const int2* d
     }
     k_bead_actions32<<<k, kBeadBlock32, smem, s>>>(v, make_aziz_f(a), d_beads, k, shift, mode,
                                                    tau, lambda, vf[0], vf[1], gf[0], gf[1], d_over,
-                                                   d_out);
+                                                   d_out, d_force);
+    return cudaGetLastError();
+}
+
+// Same-slice forces of every active bead: F[t][b] = sum over active b3 != b
+// of gradV(r_b - r_b3), FP32 with Kahan sums per component.  One CTA per
+// slice, O(N^2).
+constexpr int kForceBlock = 256;
+
+__global__ void __launch_bounds__(kForceBlock)
+k_slice_forces32(PathView v, AzizF az, float4* __restrict__ force) {
+    extern __shared__ float4 sp[];
+    const int s = blockIdx.x, Ne = v.Ne;
+    const float L0 = (float)v.side[0], L1 = (float)v.side[1], L2 = (float)v.side[2];
+    const float I0 = (float)v.sideInv[0], I1 = (float)v.sideInv[1], I2 = (float)v.sideInv[2];
+    for (int j = threadIdx.x; j < Ne; j += blockDim.x) {
+        float4 r = v.pos32[(size_t)s * Ne + j];
+        r.w = v.on[(size_t)s * Ne + j] ? 1.f : 0.f;
+        sp[j] = r;
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < Ne; b += blockDim.x) {
+        const float4 rb = sp[b];
+        KahanF fx, fy, fz;
+        if (rb.w != 0.f) {
+            for (int b3 = 0; b3 < Ne; ++b3) {
+                const float4 r3 = sp[b3];
+                if (b3 == b || r3.w == 0.f) continue;
+                const float ex = min_image32(rb.x - r3.x, L0, I0);
+                const float ey = min_image32(rb.y - r3.y, L1, I1);
+                const float ez = min_image32(rb.z - r3.z, L2, I2);
+                const float g = aziz_g32(fmaf(ex, ex, fmaf(ey, ey, ez * ez)), az);
+                fx.add(g * ex); fy.add(g * ey); fz.add(g * ez);
+            }
+        }
+        force[(size_t)s * Ne + b] = make_float4(fx.s - fx.c, fy.s - fy.c, fz.s - fz.c, 0.f);
+    }
+}
+
+cudaError_t launch_slice_forces32(const PathView& v, AzizParams a, float4* d_force, cudaStream_t s) {
+    size_t smem = (size_t)v.Ne * sizeof(float4);
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_slice_forces32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    k_slice_forces32<<<v.M, kForceBlock, smem, s>>>(v, make_aziz_f(a), d_force);
     return cudaGetLastError();
 }
 

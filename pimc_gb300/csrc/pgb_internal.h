@@ -69,6 +69,8 @@ struct Ctx {
     // scratch (grown on demand)
     void* d_scratch = nullptr; size_t scratch_bytes = 0;
     void* d_tc_tables = nullptr;   // split-BF16 DFT and cosine matrices of this M (built once)
+    float4* d_force32 = nullptr;   // per-bead same-slice forces of the current configuration
+    bool force_valid = false;      // cleared by every position change
     void* h_pinned = nullptr; size_t pinned_bytes = 0;
     // plain-form generator state (MT19937)
     std::vector<uint32_t> mt_state;
@@ -111,7 +113,9 @@ cudaError_t launch_bead_actions32(const PathView& v, AzizParams az,
                                   const int2* d_beads, int k, int shift, int mode,
                                   double tau, double lambda, const double vf[2],
                                   const double gf[2], const double* d_over, double* d_out,
-                                  cudaStream_t s);
+                                  cudaStream_t s, const float4* d_force = nullptr);
+// F[t][b] = sum over active b3 != b of gradV(r_b - r_b3) on slice t, FP32 [M][Ne]
+cudaError_t launch_slice_forces32(const PathView& v, AzizParams az, float4* d_force, cudaStream_t s);
 cudaError_t launch_slice_terms32(const PathView& v, AzizParams az, int window,
                                  double* d_terms, cudaStream_t s);
 cudaError_t launch_pos32_from64(const PathView& v, float4* d_pos32,

@@ -263,3 +263,30 @@ def test_trial_displacements(pgb, oracle_lib, small, precision, tol):
         scale.append(max(abs(u0), abs(u1), 1.0))
     want = np.array(want)
     assert np.max(np.abs(got - want) / np.array(scale)) <= tol
+
+
+def test_mixed_correction_follows_updates(pgb, oracle_lib, small):
+    """Mixed GSF actions with rc covering the box take the O(n) correction
+    through cached slice forces; the cache must follow every bead update and
+    the on/off state of an open worm."""
+    d = small
+    for worm in (False, True):
+        cfg = pgb.worldlines.open_worm(d["cfg"], head=(3, 2), tail=(9, 2)) if worm else d["cfg"]
+        o = oracle_lib.Oracle(d["L"], d["m"], d["n"], d["tau"], d["lam"], action="gsf")
+        o.load(cfg)
+        a = pgb.Action(d["L"], d["m"], d["n"], d["tau"], d["lam"], action="gsf",
+                       precision=pgb.PGB_MIXED)
+        a.load(cfg)
+        rng = np.random.default_rng(21)
+        beads = random_beads(rng, d["m"], d["n"], 30)
+        for step in range(3):
+            want = np.array([o.bead_action(int(s), int(p)) for s, p in beads])
+            got, _ = a.bead_actions(beads)
+            scale = np.maximum(np.abs(want), 1.0)
+            assert np.max(np.abs(got - want) / scale) <= 2e-4, (worm, step)
+            # move a bead on an odd (gradient) slice that the next check reads
+            s, p = int(beads[step, 0]) | 1, int(beads[step, 1])
+            r = a.positions()[s, p] + rng.normal(0, 0.15, 3)
+            r -= d["L"] * np.floor(r / d["L"] + 0.5)
+            a.update_beads([[s, p]], [r])
+            o.update_bead(s, p, r)

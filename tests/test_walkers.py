@@ -97,3 +97,15 @@ def test_infeasible_schedule_is_an_error(pgb):
     W.init()
     with pytest.raises(pgb.PgbError):
         W.run(1)
+
+
+def test_stats_array_matches_stats(pgb):
+    w = pgb.worldlines.workload_walkers(num=20, seed=4, nmax=40)
+    W = pgb.Walkers(w["n"], w["m"], w["temperature"], w["side"], w["mbar"], w["tau"], w["lam"],
+                    seed=2, threads_per_walker=6016)
+    W.init()
+    W.run(2, measure=1)
+    st, arr = W.stats(), W.stats_array()
+    assert list(arr["bead_updates"]) == [s["bead_updates"] for s in st]
+    assert list(arr["energy_sum"]) == [s["energy_sum"] for s in st]
+    assert [list(a) for a in arr["accepted"]] == [s["accepted"] for s in st]
