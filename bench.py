@@ -444,8 +444,9 @@ def run_isf(args, pgb):
 
 
 # ---------------------------------------------------------------------------
-# Pair-action leg: N=256, M=250, GSF, rc = L: full-path potential action per
-# configuration and 10^6 single-bead trial displacements, FP64 and mixed.
+# Pair-action leg: N=256, M=250, GSF, rc = L: full-path potential action and
+# virial energy per configuration (host call, synchronous) and 10^6
+# single-bead trial displacements, FP64 and mixed.
 # ---------------------------------------------------------------------------
 def run_pair(args, pgb):
     import torch
@@ -471,6 +472,11 @@ def run_pair(args, pgb):
         for _ in range(args.steps):
             a.full_action()
         t_full = (time.perf_counter() - t0) / args.steps
+        a.virial()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            a.virial()
+        t_vir = (time.perf_counter() - t0) / args.steps
         pos = cfg["pos"][beads[:, 0], beads[:, 1]] + disp
         pos -= L * np.floor(pos / L + 0.5)
         d_b = torch.from_numpy(beads).cuda()
@@ -494,21 +500,23 @@ def run_pair(args, pgb):
         # them, old and new: 2 (n-1) V pairs, and on odd (gradV) slices
         # 2 (n-1)^2 gradV pairs (gradVnnSquared over the bead's list).  With
         # rc covering the box the mixed form gets the inner gradient sums from
-        # cached slice forces and evaluates 3 (n-1) gradV pairs instead; the
-        # roofline counts the pairs it evaluates.
+        # cached slice forces and evaluates 2 (n-1) gradV pairs instead (trial
+        # and current position, one fused launch); the roofline counts the
+        # pairs it evaluates.
         odd = (beads[:k, 0] % 2 == 1).mean()
         tp_v = k * 2.0 * (n - 1)
         tp_vg_ref = k * odd * 2.0 * (n - 1) ** 2
-        tp_vg = tp_vg_ref if prec == pgb.PGB_FP64 else k * odd * 3.0 * (n - 1)
+        tp_vg = tp_vg_ref if prec == pgb.PGB_FP64 else k * odd * 2.0 * (n - 1)
         trial_pairs = tp_v + tp_vg_ref
         res["fp64" if prec == pgb.PGB_FP64 else "mixed"] = {
             "full_action_ms": 1e3 * t_full, "full_action_pairs_per_s": (v_pairs + g_pairs) / t_full,
+            "virial_ms": 1e3 * t_vir,
             "trials": k, "trial_ms": 1e3 * t_trial,
             "reference_equivalent_pairs_per_s": trial_pairs / t_trial,
             "trial_moves_per_s": k / t_trial, "_pv": tp_v, "_pvg": tp_vg, "_t": t_trial}
     clocks = clk.stop()
     mx = res["mixed"]
-    roof = pair_roofline(mx.pop("_pv"), mx.pop("_pvg"), mx.pop("_t"), "k_bead_actions32",
+    roof = pair_roofline(mx.pop("_pv"), mx.pop("_pvg"), mx.pop("_t"), "k_bead_actions32_full",
                          measured_fp32_peak(), clocks.get("sm_mhz"))
     for r in res.values():
         for key in ("_pv", "_pvg", "_t"):

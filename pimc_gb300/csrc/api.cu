@@ -88,17 +88,22 @@ int need_path(Ctx& c) {
     return PGB_OK;
 }
 
-// Same-slice forces for the O(n) gradient correction of the mixed form.  They
-// apply when the cutoff takes in every minimum-image separation, so that each
-// bead's list is its whole slice.  Returns the forces (valid until the next
-// position change) when they apply, nullptr otherwise.
+// True when the cutoff takes in every minimum-image separation, so that each
+// bead's list is its whole slice (the reference default rc = L does).
+bool full_list(const Ctx& c) {
+    const double far2 = 0.25 * (c.p.side[0] * c.p.side[0] + c.p.side[1] * c.p.side[1] +
+                                c.p.side[2] * c.p.side[2]);
+    return c.p.rc * c.p.rc > far2;
+}
+
+// Same-slice forces for the O(n) gradient correction of the mixed form with
+// full lists.  Returns the forces (valid until the next position change), or
+// nullptr when the action has no gradient term or the lists are cut.
 const float4* slice_forces(Ctx& c, int* rc) {
     *rc = PGB_OK;
     if (c.p.precision != PGB_MIXED) return nullptr;
     if (!(c.p.gradvfactor[0] > kEPS || c.p.gradvfactor[1] > kEPS)) return nullptr;
-    const double far2 = 0.25 * (c.p.side[0] * c.p.side[0] + c.p.side[1] * c.p.side[1] +
-                                c.p.side[2] * c.p.side[2]);
-    if (!(c.p.rc * c.p.rc > far2)) return nullptr;
+    if (!full_list(c)) return nullptr;
     if (!c.d_force32) {
         cudaError_t e = cudaMalloc(&c.d_force32, (size_t)c.M * c.Ne * sizeof(float4));
         if (e != cudaSuccess) { c.d_force32 = nullptr; *rc = c.cuda_fail(e, "cudaMalloc(slice forces)"); return nullptr; }
@@ -405,11 +410,14 @@ int pgb_bead_actions(pgb_ctx* h, const int32_t* beads, int k, int shift, int mod
     PathView v = c.view();
     const float4* fall = slice_forces(c, &rc);
     if (rc) return rc;
-    cudaError_t e = (c.p.precision == PGB_MIXED)
-        ? launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda,
-                                c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream, fall)
-        : launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda,
-                                c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream);
+    cudaError_t e = (c.p.precision != PGB_MIXED)
+        ? launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda,
+                                c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream)
+        : full_list(c)
+        ? launch_bead_actions32_full(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda,
+                                     c.p.vfactor, c.p.gradvfactor, nullptr, fall, 0, d_o, c.stream)
+        : launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda,
+                                c.p.vfactor, c.p.gradvfactor, nullptr, d_o, c.stream, fall);
     if (e != cudaSuccess) return c.cuda_fail(e, "bead actions launch");
     double* ho = reinterpret_cast<double*>(hp + ((bb + 15) & ~(size_t)15));
     PGB_CUDA(&c, cudaMemcpyAsync(ho, d_o, ob, cudaMemcpyDeviceToHost, c.stream));
@@ -826,15 +834,22 @@ int trial_launch(Ctx& c, const int2* d_b, const double* d_pos, int k, int shift,
                  double* d_new, double* d_old, double* d_delta) {
     PathView v = c.view();
     cudaError_t e;
-    if (c.p.precision == PGB_MIXED) {
+    if (c.p.precision == PGB_MIXED && full_list(c)) {
+        // one fused launch: U(trial) - U(current) per trial
         int rc = PGB_OK;
         const float4* fall = slice_forces(c, &rc);
         if (rc) return rc;
+        e = launch_bead_actions32_full(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda,
+                                       c.p.vfactor, c.p.gradvfactor, d_pos, fall, 1, d_delta, c.stream);
+        if (e != cudaSuccess) return c.cuda_fail(e, "trial actions launch");
+        return PGB_OK;
+    }
+    if (c.p.precision == PGB_MIXED) {
         e = launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
-                                  c.p.gradvfactor, d_pos, d_new, c.stream, fall);
+                                  c.p.gradvfactor, d_pos, d_new, c.stream);
         if (e == cudaSuccess)
             e = launch_bead_actions32(v, c.az, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
-                                      c.p.gradvfactor, nullptr, d_old, c.stream, fall);
+                                      c.p.gradvfactor, nullptr, d_old, c.stream);
     } else {
         e = launch_bead_actions64(v, d_b, k, shift, mode, c.p.tau, c.p.lambda, c.p.vfactor,
                                   c.p.gradvfactor, d_pos, d_new, c.stream);

@@ -114,6 +114,13 @@ cudaError_t launch_bead_actions32(const PathView& v, AzizParams az,
                                   double tau, double lambda, const double vf[2],
                                   const double gf[2], const double* d_over, double* d_out,
                                   cudaStream_t s, const float4* d_force = nullptr);
+// one warp per bead, every active same-slice bead in the list; delta = 1 with
+// d_over writes U(trial) - U(current)
+cudaError_t launch_bead_actions32_full(const PathView& v, AzizParams az, const int2* d_beads, int k,
+                                       int shift, int mode, double tau, double lambda,
+                                       const double vf[2], const double gf[2], const double* d_over,
+                                       const float4* d_force, int delta, double* d_out,
+                                       cudaStream_t s);
 // F[t][b] = sum over active b3 != b of gradV(r_b - r_b3) on slice t, FP32 [M][Ne]
 cudaError_t launch_slice_forces32(const PathView& v, AzizParams az, float4* d_force, cudaStream_t s);
 cudaError_t launch_slice_terms32(const PathView& v, AzizParams az, int window,
