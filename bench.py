@@ -680,11 +680,14 @@ def main():
     torch.cuda.synchronize()
     barrier(ws)
     st = W.stats_array()
+    upload = lambda: W._chk(W.lib.pgb_walkers_set_all_positions(W.h, host_np.ctypes.data_as(
+        pgb._lib._DP)))
     t0 = time.perf_counter()
+    upload()                                    # step 0's state
     for k in range(args.steps):
-        W._chk(W.lib.pgb_walkers_set_all_positions(W.h, host_np.ctypes.data_as(
-            pgb._lib._DP)))
         W.run(1, measure=1, sync=False)
+        if k + 1 < args.steps:
+            upload()                            # step k+1's state: its copy overlaps sweep k
         W.stats_array(st)                       # synchronous D2H of the accumulators
     t_e2e = time.perf_counter() - t0
     bu_e2e = int(st["bead_updates"].sum())

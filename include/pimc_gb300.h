@@ -222,7 +222,11 @@ int pgb_walkers_set_positions(pgb_walkers* w, int walker, const double* pos);
 int pgb_walkers_get_positions(pgb_walkers* w, int walker, double* pos);
 /* Upload every walker's positions at once from one host buffer: walker w's
  * AoS FP64 [M_w][N_w][3] block follows walker w-1's (total sum M_w N_w 3
- * doubles).  Pinned host memory gives the full C2C copy bandwidth. */
+ * doubles).  Pinned host memory gives the full C2C copy bandwidth.  The copy
+ * runs on a second stream into one of two staging buffers, so it overlaps
+ * work already queued (the previous sweep); the new state takes effect in
+ * stream order.  The host buffer must stay unchanged until the next
+ * synchronizing call (pgb_walkers_sync, pgb_walkers_stats). */
 int pgb_walkers_set_all_positions(pgb_walkers* w, const double* pos);
 /* bytes of the host buffer pgb_walkers_set_all_positions reads */
 size_t pgb_walkers_state_bytes(pgb_walkers* w);
@@ -247,9 +251,10 @@ long long pgb_walkers_launch_count(pgb_walkers* w);
  * a second buffer, 256 (512)-thread CTAs, teams of up to 8 (16) warps;
  * 5000 (6000) = the same with team warps proportional to each walker's cost
  * N^2 M, the costliest walker getting all 8 (16); 7000/7008/7016 = teams
- * sized as 6000/6008/6016 that split in two halves to make two consecutive
- * staging moves at once when their imaginary-time intervals are disjoint
- * (such moves commute, so the chain is that of making them in turn) */
+ * sized as 6000/6008/6016 that split into sub-teams to make a run of up to
+ * two (8000/8008/8016: four) consecutive staging moves at once when their
+ * imaginary-time intervals are pairwise disjoint (such moves commute, so the
+ * chain is that of making them in turn) */
 int pgb_walkers_threads(pgb_walkers* w);
 /* the autotuner's record: schedules tried and one-sweep time (ms) of each;
  * returns the number of candidates, fills at most cap */

@@ -914,6 +914,39 @@ __device__ __forceinline__ bool team_wait(uint64_t* bar, uint32_t parity, int sl
     return *(volatile int*)s_fail == 0;
 }
 
+// Energy samples: bead ii's pairs with its cnt successors (cyclic) on one
+// buffered slice row.  Two interleaved Kahan sums let consecutive pair
+// evaluations overlap; they are folded into `pot` at the end.
+__device__ __forceinline__ void row_potential(const float4* __restrict__ row, int ii, int cnt, int N,
+                                              float4 ri, const WalkerMeta& m, const AzizF& az,
+                                              KahanF& pot) {
+    KahanF pa, pb;
+    int d = 1;
+    for (; d + 1 <= cnt; d += 2) {
+        int j1 = ii + d; if (j1 >= N) j1 -= N;
+        int j2 = j1 + 1; if (j2 >= N) j2 -= N;
+        const float4 r1 = row[j1], r2 = row[j2];
+        const float ax = min_image32(ri.x - r1.x, m.L, m.Linv);
+        const float ay = min_image32(ri.y - r1.y, m.L, m.Linv);
+        const float az_ = min_image32(ri.z - r1.z, m.L, m.Linv);
+        const float bx = min_image32(ri.x - r2.x, m.L, m.Linv);
+        const float by = min_image32(ri.y - r2.y, m.L, m.Linv);
+        const float bz = min_image32(ri.z - r2.z, m.L, m.Linv);
+        pa.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az));
+        pb.add(aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+    }
+    if (d <= cnt) {
+        int j1 = ii + d; if (j1 >= N) j1 -= N;
+        const float4 r1 = row[j1];
+        const float ax = min_image32(ri.x - r1.x, m.L, m.Linv);
+        const float ay = min_image32(ri.y - r1.y, m.L, m.Linv);
+        const float az_ = min_image32(ri.z - r1.z, m.L, m.Linv);
+        pa.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az));
+    }
+    pot.add(pa.s - pa.c);
+    pot.add(pb.s - pb.c);
+}
+
 template <int MINB>
 __global__ void __launch_bounds__(kTeamCta, MINB)
 k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
@@ -1121,14 +1154,7 @@ k_walkers_tma(const WalkerMeta* __restrict__ meta, const int4* __restrict__ team
                     const int t = idx / N, ii = idx - t * N;
                     const float4 ri = buf[t * N + ii];
                     const int cnt = half + ((even && ii < N / 2) ? 1 : 0);
-                    for (int d = 1; d <= cnt; ++d) {
-                        int jj = ii + d; if (jj >= N) jj -= N;
-                        const float4 rj = buf[t * N + jj];
-                        const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
-                        const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
-                        const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
-                        pot.add(aziz_v32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
-                    }
+                    row_potential(buf + (size_t)t * N, ii, cnt, N, ri, m, az, pot);
                 }
                 team_sync(slot, T);
             }
@@ -1227,6 +1253,9 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
     __shared__ int s_acc[NW];
     __shared__ int s_fail[NW];
     __shared__ __align__(8) uint64_t s_bar[NW][2];
+    // move descriptors: one warp draws them and the team reads them, a ring
+    // of three per team (move u + 2 is written while u + 1 is being read)
+    __shared__ MoveDesc s_mv[NW][3];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int4 tm = make_int4(-1, 0, 0, 0);
     for (int k = 0; k < NW; ++k) {
@@ -1278,9 +1307,16 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
         const unsigned long long gs = sweep0 + sw;
         const uint32_t g0 = (uint32_t)gs, g1 = (uint32_t)(gs >> 32);
         bool have = false;                        // rows of the current move already in Bsel(cur)
-        MoveDesc D = draw_move(0, g0, g1, m, p_com, var_updates);
-        MoveDesc Dn = D;
-        if (m.num_updates > 1) Dn = draw_move(1, g0, g1, m, p_com, var_updates);
+        // warp 0 alone runs the generator for the move descriptors; the other
+        // warps read them from shared memory once a barrier has ordered them
+        MoveDesc D, Dn;
+        if (wi == 0) {
+            D = draw_move(0, g0, g1, m, p_com, var_updates);
+            Dn = (m.num_updates > 1) ? draw_move(1, g0, g1, m, p_com, var_updates) : D;
+            if (lane == 0) { s_mv[slot][0] = D; s_mv[slot][1] = Dn; }
+        }
+        team_sync(slot, T);
+        if (wi != 0) { D = s_mv[slot][0]; Dn = s_mv[slot][1]; }
         // the bridge increments of a staging move depend on the draws alone:
         // those of move u + 1 are made while move u sums its pairs
         if (!D.com) stage_increments(Isel(0), m, 0, g0, g1, D.len, tt, T);
@@ -1289,7 +1325,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
             const bool last = (u + 1 == m.num_updates);
             const bool has_nn = (u + 2 < m.num_updates);
             if (!D.com) {
-                const bool pre = !last && !Dn.com;
+                bool pre = !last && !Dn.com;             // exact in warp 0, which issues the copies
                 const int i = D.i, s0 = D.s0, len = D.len, nmove = D.nmove;
                 // rows s0 .. s0 + len: the two fixed ends and the moved slices
                 if (tt == 0) {
@@ -1341,15 +1377,24 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 }
                 phflip(cur);
                 team_sync(slot, T);
+                // move u + 1 was written by warp 0 during move u - 1 (or at the
+                // start of the sweep); the barrier above orders it
+                if (wi != 0) Dn = s_mv[slot][(u + 1) % 3];
+                pre = !last && !Dn.com;
                 if (*(volatile int*)fail) {
                     if (tt == 0 && pre) drain(cur ^ 1);
                     return;
                 }
                 // while the pairs are summed: the next move's increments, the
-                // move after it, and this move's acceptance draw
+                // move after it (drawn by the team's last warp, which waits at
+                // the barriers rather than leading the critical path), and this
+                // move's acceptance draw
                 if (pre) stage_increments(Isel((u + 1) & 1), m, u + 1, g0, g1, Dn.len, tt, T);
                 MoveDesc Dnn = Dn;
-                if (has_nn) Dnn = draw_move(u + 2, g0, g1, m, p_com, var_updates);
+                if (wi == nw - 1 && has_nn) {
+                    Dnn = draw_move(u + 2, g0, g1, m, p_com, var_updates);
+                    if (lane == 0) s_mv[slot][(u + 2) % 3] = Dnn;
+                }
                 MetroDraw md{0.0, 0.f};
                 if (tt == 0) {
                     const uint4 ra = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFFu);
@@ -1378,6 +1423,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 if (wi == 0) {
                     // the decision, the write-back and the patch belong to one warp;
                     // the others go on to the next move's barrier
+                    if (has_nn && nw > 1) Dnn = s_mv[slot][(u + 2) % 3];
                     const float2 v = ff_butterfly(lane < nw ? ffr[lane].x : 0.f, lane < nw ? ffr[lane].y : 0.f);
                     int ok = 0;
                     if (lane == 0) {
@@ -1421,9 +1467,11 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 const float sx = D.sx, sy = D.sy;
                 const uint4 r1 = wrand(m.key, (uint32_t)u, g0, g1, 0xFFFEu);
                 const float sz = m.com_delta * (u01f(r1.x) - 0.5f);
-                if (!last && !Dn.com) stage_increments(Isel((u + 1) & 1), m, u + 1, g0, g1, Dn.len, tt, T);
                 MoveDesc Dnn = Dn;
-                if (has_nn) Dnn = draw_move(u + 2, g0, g1, m, p_com, var_updates);
+                if (wi == nw - 1 && has_nn) {
+                    Dnn = draw_move(u + 2, g0, g1, m, p_com, var_updates);
+                    if (lane == 0) s_mv[slot][(u + 2) % 3] = Dnn;
+                }
                 KahanF acc;
                 int b = cur;
                 if (tt == 0) issue_rows(Bsel(b), P, N, M, 0, min(C, M), barsel(b));
@@ -1464,6 +1512,12 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                 }
                 team_sync(slot, T);
                 const int ok = s_acc[slot];
+                // move u + 1 (written during move u - 1 or at the sweep start)
+                // and its bridge increments, before this move's last barrier;
+                // warp 0 also takes move u + 2
+                if (wi != 0) Dn = s_mv[slot][(u + 1) % 3];
+                if (wi == 0 && has_nn && nw > 1) Dnn = s_mv[slot][(u + 2) % 3];
+                if (!last && !Dn.com) stage_increments(Isel((u + 1) & 1), m, u + 1, g0, g1, Dn.len, tt, T);
                 if (ok) {
                     for (int t2 = tt; t2 < M; t2 += T) {
                         float4 pi = P[(size_t)t2 * N + i];
@@ -1497,14 +1551,7 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
                     const int t = idx / N, ii = idx - t * N;
                     const float4 ri = buf[t * N + ii];
                     const int cnt = half + ((even && ii < N / 2) ? 1 : 0);
-                    for (int d = 1; d <= cnt; ++d) {
-                        int jj = ii + d; if (jj >= N) jj -= N;
-                        const float4 rj = buf[t * N + jj];
-                        const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
-                        const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
-                        const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
-                        pot.add(aziz_v32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
-                    }
+                    row_potential(buf + (size_t)t * N, ii, cnt, N, ri, m, az, pot);
                 }
                 team_sync(slot, T);
                 b ^= 1;
@@ -1546,16 +1593,17 @@ k_walkers_pipe(const WalkerMeta* __restrict__ meta, const int4* __restrict__ tea
 }
 
 // ---------------------------------------------------------------------------
-// Two-move schedule.  Consecutive staging moves whose closed imaginary-time
-// intervals [s0, s0 + len] (mod M) are disjoint read and write disjoint rows
-// of the slab, so they commute: running them at once gives the chain of
-// running them one after the other.  A team of nw >= 2 warps splits into two
-// halves; when moves u and u + 1 are such a pair, half 0 makes move u and
-// half 1 move u + 1, each with its own row buffer, bridge, pair sums and
-// decision; otherwise the whole team makes move u alone.  Centre-of-mass
-// moves and energy samples use the whole team as in the pipelined schedule.
-// One half's serial work (copy wait, bridge, decision, write-back) overlaps
-// the other half's pair sums.
+// Grouped schedule.  Consecutive staging moves whose closed imaginary-time
+// intervals [s0, s0 + len] (mod M) are pairwise disjoint read and write
+// disjoint rows of the slab, so they commute: making them at once gives the
+// chain of making them one after the other.  From move u on, a team takes the
+// longest run of up to GMAX such moves whose rows (len + 1 each) fit its
+// shared-memory row pool of 2 (Mbar + 1) rows, splits into 1, 2 or 4
+// sub-teams and gives each one move: its rows, bridge, pair sums and
+// decision.  A run of one is made by the whole team.  Centre-of-mass moves
+// and energy samples use the whole team as in the pipelined schedule.  One
+// sub-team's serial work (copy wait, bridge, decision, write-back) overlaps
+// the others' pair sums.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool stage_disjoint(const MoveDesc& a, const MoveDesc& b, int M) {
     int d1 = b.s0 - a.s0; if (d1 < 0) d1 += M;
@@ -1563,16 +1611,18 @@ __device__ __forceinline__ bool stage_disjoint(const MoveDesc& a, const MoveDesc
     return d1 > a.len && d2 > b.len;
 }
 
-// named barrier of half h of a team starting at warp `slot` (ids slot + 2,
-// slot + 3 lie inside the team's own range slot + 1 .. slot + nw)
-__device__ __forceinline__ void half_sync(int slot, int h, int HT) {
+// named barrier of sub-team g of a team starting at warp `slot`: ids
+// slot + 2 .. slot + 5 lie inside the team's own range slot + 1 .. slot + nw
+// whenever a sub-team has two or more warps (one-warp sub-teams use
+// __syncwarp)
+__device__ __forceinline__ void sub_sync(int slot, int g, int HT) {
     if (HT == 32) __syncwarp();
-    else asm volatile("bar.sync %0, %1;" :: "r"(slot + 2 + h), "r"(HT) : "memory");
+    else asm volatile("bar.sync %0, %1;" :: "r"(slot + 2 + g), "r"(HT) : "memory");
 }
 
-template <int CTA, int MINB>
+template <int CTA, int MINB, int GMAX>
 __global__ void __launch_bounds__(CTA, MINB)
-k_walkers_pair2(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
+k_walkers_group(const WalkerMeta* __restrict__ meta, const int4* __restrict__ teams,
                 float4* __restrict__ pos, WalkerAcc* __restrict__ accs,
                 unsigned long long* __restrict__ ctr, int* __restrict__ err, int sweeps, int measure,
                 AzizF az, double tau, double lambda, float p_com, int var_updates, uint64_t seed) {
@@ -1583,7 +1633,7 @@ k_walkers_pair2(const WalkerMeta* __restrict__ meta, const int4* __restrict__ te
     __shared__ double s_red[NW][NW];
     __shared__ int s_acc[NW];
     __shared__ int s_fail[NW];
-    __shared__ __align__(8) uint64_t s_bar[NW][2];
+    __shared__ __align__(8) uint64_t s_bar[NW][4];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int4 tm = make_int4(-1, 0, 0, 0);
     for (int k = 0; k < NW; ++k) {
@@ -1593,26 +1643,27 @@ k_walkers_pair2(const WalkerMeta* __restrict__ meta, const int4* __restrict__ te
     if (tm.x < 0) return;
     const int w = tm.x, slot = tm.y, nw = tm.z, T = nw * 32;
     const int tt = threadIdx.x - slot * 32, wi = warp - slot;
-    const int hw = nw / 2;                       // warps per half (0: no split)
     const WalkerMeta m = meta[w];
     float4* P = pos + m.off;
     const int N = m.N, M = m.M, C = m.mbar, R = C + 1;
+    // row pool of 2 (Mbar + 1) rows (the centre-of-mass and energy chunks use
+    // its halves B0, B1), then GMAX sets of bridge increments
     float4* const B0 = dyn + (tm.w - 1);
     float4* const B1 = B0 + (size_t)R * N;
-    float4* const I0 = B1 + (size_t)R * N;
-    float4* const I1 = I0 + kMaxStage;
-    uint64_t* const bar0 = &s_bar[slot][0];
-    uint64_t* const bar1 = &s_bar[slot][1];
+    float4* const Ibase = B1 + (size_t)R * N;
     auto Bsel = [&](int x) { return x ? B1 : B0; };
-    auto barsel = [&](int x) { return x ? bar1 : bar0; };
+    auto barsel = [&](int x) { return &s_bar[slot][x]; };
     double* red = s_red[slot];
     int* fail = &s_fail[slot];
-    if (tt == 0) { mbar_init(bar0, 1); mbar_init(bar1, 1); *fail = 0; }
+    if (tt == 0) {
+        for (int g = 0; g < 4; ++g) mbar_init(&s_bar[slot][g], 1);
+        *fail = 0;
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     team_sync(slot, T);
-    uint32_t ph0 = 0u, ph1 = 0u;
-    auto phsel = [&](int x) { return x ? ph1 : ph0; };
-    auto phflip = [&](int x) { if (x) ph1 ^= 1u; else ph0 ^= 1u; };
+    uint32_t phase = 0u;                          // bit g: parity of barrier g
+    auto phsel = [&](int x) { return (phase >> x) & 1u; };
+    auto phflip = [&](int x) { phase ^= 1u << x; };
     const unsigned long long sweep0 = ctr[w];
     double esum = 0.0, esumsq = 0.0;
     long long nsamp = 0, nbu = 0, att0 = 0, att1 = 0, acc0 = 0, acc1 = 0;
@@ -1633,126 +1684,147 @@ k_walkers_pair2(const WalkerMeta* __restrict__ meta, const int4* __restrict__ te
         while (u < m.num_updates) {
             const MoveDesc D0 = draw_move(u, g0, g1, m, p_com, var_updates);
             if (!D0.com) {
-                bool two = false;
-                MoveDesc D1 = D0;
-                if (hw > 0 && u + 1 < m.num_updates) {
-                    D1 = draw_move(u + 1, g0, g1, m, p_com, var_updates);
-                    two = !D1.com && stage_disjoint(D0, D1, M);
+                // the run of pairwise commuting staging moves that starts at u
+                int gs0[GMAX], glen[GMAX];
+                gs0[0] = D0.s0; glen[0] = D0.len;
+                int ng = 1, rows = D0.len + 1;
+                while (ng < GMAX && ng < nw && u + ng < m.num_updates) {
+                    const MoveDesc Dc = draw_move(u + ng, g0, g1, m, p_com, var_updates);
+                    if (Dc.com || rows + Dc.len + 1 > 2 * R) break;
+                    bool ok = true;
+                    for (int q = 0; q < ng; ++q) {
+                        MoveDesc Dq; Dq.s0 = gs0[q]; Dq.len = glen[q];
+                        ok = ok && stage_disjoint(Dq, Dc, M);
+                    }
+                    if (!ok) break;
+                    gs0[ng] = Dc.s0; glen[ng] = Dc.len;
+                    rows += Dc.len + 1;
+                    ++ng;
                 }
-                // this thread's group: the whole team, or its half
-                const int h = (two && wi >= hw) ? 1 : 0;
-                const int HT = two ? hw * 32 : T;
-                const int ht = tt - h * hw * 32, wih = wi - h * hw;
-                const int nwg = two ? hw : nw;
-                const MoveDesc D = h ? D1 : D0;
-                const int uh = u + h;
+                const int gsize = (ng == 1) ? 1 : (ng == 2) ? 2 : 4;
+                const int qw = nw / gsize;                 // warps per sub-team
+                const int sg = wi / qw;                    // this thread's sub-team
+                const bool active = sg < ng;
+                const int HT = qw * 32;
+                const int ht = tt - sg * HT, wih = wi - sg * qw;
+                int off = 0;
+                for (int q = 0; q < ng; ++q) if (q < sg) off += glen[q] + 1;
+                const int uh = u + sg;
+                const MoveDesc D = active ? draw_move(uh, g0, g1, m, p_com, var_updates) : D0;
                 const int i = D.i, s0 = D.s0, len = D.len, nmove = D.nmove;
-                float4* const buf = Bsel(h);
-                float4* const inc = h ? I1 : I0;
-                float4* const sn = s_new[slot + h * hw];
-                float2* const ffr = s_ff[slot + h * hw];
-                auto gsync = [&]() { if (two) half_sync(slot, h, HT); else team_sync(slot, T); };
-                // rows s0 .. s0 + len, increments and the acceptance draw
-                if (ht == 0) issue_rows(buf, P, N, M, s0, len + 1, barsel(h));
-                stage_increments(inc, m, uh, g0, g1, len, ht, HT);
+                float4* const buf = B0 + (size_t)off * N;
+                float4* const inc = Ibase + sg * kMaxStage;
+                float4* const sn = s_new[slot + sg * qw];
+                float2* const ffr = s_ff[slot + sg * qw];
+                uint64_t* const bar = &s_bar[slot][active ? sg : 0];
+                auto gsync = [&]() { if (gsize == 1) team_sync(slot, T); else sub_sync(slot, sg, HT); };
                 MetroDraw md{0.0, 0.f};
-                if (ht == 0) {
-                    const uint4 ra = wrand(m.key, (uint32_t)uh, g0, g1, 0xFFFFu);
-                    md = metropolis_draw(ra.x, ra.y);
-                }
-                gsync();
-                if (wih == 0) {
-                    long long nwait = 0;
-                    bool landed = true;
-                    while (!mbar_try_wait(barsel(h), phsel(h)))
-                        if (++nwait > kWaitLimit) { landed = false; break; }
-                    landed = __all_sync(0xffffffffu, landed);
-                    if (!landed) {
-                        // give the copy one more bounded wait before the team leaves
-                        if (lane == 0) { atomicExch(fail, 1); atomicExch(err + w, 1); drain(h); }
-                    } else {
-                        const float4 x0 = buf[i], xe = buf[(size_t)len * N + i];
-                        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-                        const float4 i1 = (lane < len) ? inc[lane] : zero;
-                        const float4 i2 = (lane + 32 < len) ? inc[lane + 32] : zero;
-                        const float W1x = warp_scan_incl(i1.x, lane), W1y = warp_scan_incl(i1.y, lane),
-                                    W1z = warp_scan_incl(i1.z, lane);
-                        const float W2x = warp_scan_incl(i2.x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
-                        const float W2y = warp_scan_incl(i2.y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
-                        const float W2z = warp_scan_incl(i2.z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
-                        const int src = (len <= 32) ? len - 1 : len - 33;
-                        const float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
-                        const float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
-                        const float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
-                        const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
-                        const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
-                        const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
-                        const float il = 1.0f / (float)len;
-                        #pragma unroll
-                        for (int hh = 0; hh < 2; ++hh) {
-                            const int k = lane + 32 * hh;
-                            if (k < nmove) {
-                                const float f = (float)(k + 1) * il;
-                                const float Wx = hh ? W2x : W1x, Wy = hh ? W2y : W1y, Wz = hh ? W2z : W1z;
-                                sn[k] = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
-                                                    put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
-                                                    put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
-                            }
-                        }
+                if (active) {
+                    // rows s0 .. s0 + len, increments and the acceptance draw
+                    if (ht == 0) issue_rows(buf, P, N, M, s0, len + 1, bar);
+                    stage_increments(inc, m, uh, g0, g1, len, ht, HT);
+                    if (ht == 0) {
+                        const uint4 ra = wrand(m.key, (uint32_t)uh, g0, g1, 0xFFFFu);
+                        md = metropolis_draw(ra.x, ra.y);
                     }
-                }
-                gsync();
-                if (!*(volatile int*)fail) {
-                    const int G = (HT >= N) ? HT / N : 1;
-                    const int j0 = (HT >= N) ? ((ht < G * N) ? ht % N : N) : ht;
-                    const int kb0 = (HT >= N) ? ht / N : 0;
-                    const int jstep = (HT >= N) ? N : HT;
-                    KahanF acc;
-                    for (int j = j0; j < N; j += jstep) {
-                        if (j == i) continue;
-                        #pragma unroll 4
-                        for (int k = kb0; k < nmove; k += G) {
-                            const float4 pj = buf[(size_t)(k + 1) * N + j];
-                            const float4 a = sn[k], b = buf[(size_t)(k + 1) * N + i];
-                            const float ax = min_image32(a.x - pj.x, m.L, m.Linv);
-                            const float ay = min_image32(a.y - pj.y, m.L, m.Linv);
-                            const float az_ = min_image32(a.z - pj.z, m.L, m.Linv);
-                            const float bx = min_image32(b.x - pj.x, m.L, m.Linv);
-                            const float by = min_image32(b.y - pj.y, m.L, m.Linv);
-                            const float bz = min_image32(b.z - pj.z, m.L, m.Linv);
-                            acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
-                                    aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
-                        }
-                    }
-                    const float2 part = warp_ff(acc);
-                    if (lane == 0) ffr[wih] = part;
                     gsync();
                     if (wih == 0) {
-                        const float2 v = ff_butterfly(lane < nwg ? ffr[lane].x : 0.f,
-                                                      lane < nwg ? ffr[lane].y : 0.f);
-                        int ok = 0;
-                        if (lane == 0) {
-                            ok = metropolis_ff(v.x, v.y, tau, (float)tau, md) ? 1 : 0;
-                            att1 += 1; acc1 += ok; nbu += nmove;
-                        }
-                        ok = __shfl_sync(0xffffffffu, ok, 0);
-                        if (ok) {
-                            for (int k = lane; k < nmove; k += 32) {
-                                int sl = s0 + 1 + k; if (sl >= M) sl -= M;
-                                P[(size_t)sl * N + i] = sn[k];
+                        long long nwait = 0;
+                        bool landed = true;
+                        while (!mbar_try_wait(bar, phsel(sg)))
+                            if (++nwait > kWaitLimit) { landed = false; break; }
+                        landed = __all_sync(0xffffffffu, landed);
+                        if (!landed) {
+                            // one more bounded wait for the copy before the team leaves
+                            if (lane == 0) {
+                                atomicExch(fail, 1); atomicExch(err + w, 1);
+                                long long n2 = 0;
+                                while (!mbar_try_wait(bar, phsel(sg)))
+                                    if (++n2 > kWaitLimit) break;
                             }
-                            fence_proxy_async_global();
+                        } else {
+                            const float4 x0 = buf[i], xe = buf[(size_t)len * N + i];
+                            const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+                            const float4 i1 = (lane < len) ? inc[lane] : zero;
+                            const float4 i2 = (lane + 32 < len) ? inc[lane + 32] : zero;
+                            const float W1x = warp_scan_incl(i1.x, lane), W1y = warp_scan_incl(i1.y, lane),
+                                        W1z = warp_scan_incl(i1.z, lane);
+                            const float W2x = warp_scan_incl(i2.x, lane) + __shfl_sync(0xffffffffu, W1x, 31);
+                            const float W2y = warp_scan_incl(i2.y, lane) + __shfl_sync(0xffffffffu, W1y, 31);
+                            const float W2z = warp_scan_incl(i2.z, lane) + __shfl_sync(0xffffffffu, W1z, 31);
+                            const int src = (len <= 32) ? len - 1 : len - 33;
+                            const float Lx = __shfl_sync(0xffffffffu, len <= 32 ? W1x : W2x, src);
+                            const float Ly = __shfl_sync(0xffffffffu, len <= 32 ? W1y : W2y, src);
+                            const float Lz = __shfl_sync(0xffffffffu, len <= 32 ? W1z : W2z, src);
+                            const float dx = min_image32(xe.x - x0.x, m.L, m.Linv);
+                            const float dy = min_image32(xe.y - x0.y, m.L, m.Linv);
+                            const float dz = min_image32(xe.z - x0.z, m.L, m.Linv);
+                            const float il = 1.0f / (float)len;
+                            #pragma unroll
+                            for (int hh = 0; hh < 2; ++hh) {
+                                const int k = lane + 32 * hh;
+                                if (k < nmove) {
+                                    const float f = (float)(k + 1) * il;
+                                    const float Wx = hh ? W2x : W1x, Wy = hh ? W2y : W1y, Wz = hh ? W2z : W1z;
+                                    sn[k] = make_float4(put_inside(x0.x + fmaf(f, dx - Lx, Wx), m.L, m.Linv),
+                                                        put_inside(x0.y + fmaf(f, dy - Ly, Wy), m.L, m.Linv),
+                                                        put_inside(x0.z + fmaf(f, dz - Lz, Wz), m.L, m.Linv), 0.f);
+                                }
+                            }
                         }
-                        __syncwarp();
+                    }
+                    gsync();
+                    if (!*(volatile int*)fail) {
+                        const int G = (HT >= N) ? HT / N : 1;
+                        const int j0 = (HT >= N) ? ((ht < G * N) ? ht % N : N) : ht;
+                        const int kb0 = (HT >= N) ? ht / N : 0;
+                        const int jstep = (HT >= N) ? N : HT;
+                        KahanF acc;
+                        for (int j = j0; j < N; j += jstep) {
+                            if (j == i) continue;
+                            #pragma unroll 4
+                            for (int k = kb0; k < nmove; k += G) {
+                                const float4 pj = buf[(size_t)(k + 1) * N + j];
+                                const float4 a = sn[k], b = buf[(size_t)(k + 1) * N + i];
+                                const float ax = min_image32(a.x - pj.x, m.L, m.Linv);
+                                const float ay = min_image32(a.y - pj.y, m.L, m.Linv);
+                                const float az_ = min_image32(a.z - pj.z, m.L, m.Linv);
+                                const float bx = min_image32(b.x - pj.x, m.L, m.Linv);
+                                const float by = min_image32(b.y - pj.y, m.L, m.Linv);
+                                const float bz = min_image32(b.z - pj.z, m.L, m.Linv);
+                                acc.add(aziz_v32(fmaf(ax, ax, fmaf(ay, ay, az_ * az_)), az) -
+                                        aziz_v32(fmaf(bx, bx, fmaf(by, by, bz * bz)), az));
+                            }
+                        }
+                        const float2 part = warp_ff(acc);
+                        if (lane == 0) ffr[wih] = part;
+                        gsync();
+                        if (wih == 0) {
+                            const float2 v = ff_butterfly(lane < qw ? ffr[lane].x : 0.f,
+                                                          lane < qw ? ffr[lane].y : 0.f);
+                            int ok = 0;
+                            if (lane == 0) {
+                                ok = metropolis_ff(v.x, v.y, tau, (float)tau, md) ? 1 : 0;
+                                att1 += 1; acc1 += ok; nbu += nmove;
+                            }
+                            ok = __shfl_sync(0xffffffffu, ok, 0);
+                            if (ok) {
+                                for (int k = lane; k < nmove; k += 32) {
+                                    int sl = s0 + 1 + k; if (sl >= M) sl -= M;
+                                    P[(size_t)sl * N + i] = sn[k];
+                                }
+                                fence_proxy_async_global();
+                            }
+                            __syncwarp();
+                        }
                     }
                 }
-                phflip(0);
-                if (two) phflip(1);
-                // both moves written back (and visible to later copies) before
-                // the buffers and the slab rows are reused
+                for (int q = 0; q < ng; ++q) phflip(q);
+                // every move written back (and visible to later copies) before
+                // the pool and the slab rows are reused
                 team_sync(slot, T);
                 if (*(volatile int*)fail) return;
-                u += two ? 2 : 1;
+                u += ng;
             } else {
                 const int i = D0.i;
                 const float sx = D0.sx, sy = D0.sy;
@@ -1832,14 +1904,7 @@ k_walkers_pair2(const WalkerMeta* __restrict__ meta, const int4* __restrict__ te
                     const int t = idx / N, ii = idx - t * N;
                     const float4 ri = buf[t * N + ii];
                     const int cnt = half + ((even && ii < N / 2) ? 1 : 0);
-                    for (int d = 1; d <= cnt; ++d) {
-                        int jj = ii + d; if (jj >= N) jj -= N;
-                        const float4 rj = buf[t * N + jj];
-                        const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
-                        const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
-                        const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
-                        pot.add(aziz_v32(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
-                    }
+                    row_potential(buf + (size_t)t * N, ii, cnt, N, ri, m, az, pot);
                 }
                 team_sync(slot, T);
                 b ^= 1;
@@ -1877,9 +1942,8 @@ k_walkers_pair2(const WalkerMeta* __restrict__ meta, const int4* __restrict__ te
         A.att[0] += att0; A.acc[0] += acc0;
         ctr[w] = sweep0 + min(sweeps, m.max_sweeps);
     }
-    // staging counters live with each group's deciding thread (team thread 0
-    // and the second half's thread 0)
-    if (tt == 0 || (hw > 0 && tt == hw * 32)) {
+    // staging counters live with the deciding thread of each sub-team
+    if (att1 || nbu) {
         atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].att[1]), (unsigned long long)att1);
         atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].acc[1]), (unsigned long long)acc1);
         atomicAdd(reinterpret_cast<unsigned long long*>(&accs[w].bead_updates), (unsigned long long)nbu);
@@ -1978,7 +2042,12 @@ struct pgb_walkers {
     WalkerAcc* d_acc = nullptr;
     unsigned long long* d_ctr = nullptr;
     double* d_en = nullptr;
-    double* d_stage = nullptr;
+    // host uploads: two FP64 staging buffers filled on their own stream, so
+    // the copy of the next state overlaps the sweep on the library stream
+    double* d_stage[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+    int stage_idx = 0;
     int* d_err = nullptr;                 // per-walker error word (bounded waits)
     // packed-team schedules, one per pairs-per-thread target
     // 0-2 team targets, 3 windows, 4-6 TMA targets, 7-10 pipelined (256/8, 256/16, 512/8, 512/16)
@@ -2101,7 +2170,7 @@ cudaError_t build_tma_teams(pgb_walkers* h, int ppt) {
 
 // Pipelined TMA teams: cta = 256 (teams of <= 8 warps, 2 CTAs per SM) or
 // 512 (<= 16 warps, 1 CTA per SM); two buffers of Mbar rows per walker.
-cudaError_t build_pipe_teams(pgb_walkers* h, int k, int cta, int ppt) {
+cudaError_t build_pipe_teams(pgb_walkers* h, int k, int cta, int ppt, int nsets = 2) {
     if (h->d_teams[k]) return cudaSuccess;
     const int cap = cta / 32;
     std::vector<int> tw(h->W);
@@ -2121,8 +2190,8 @@ cudaError_t build_pipe_teams(pgb_walkers* h, int k, int cta, int ppt) {
         while (t < need && t < cap) t <<= 1;
         tw[w] = t;
     }
-    // two buffers of Mbar + 1 rows and two sets of kMaxStage bridge increments
-    return pack_teams(h, k, tw, true, cap, 2, cta == 512 ? 200 * 1024 : 100 * 1024, 1, 2 * kMaxStage);
+    // two buffers of Mbar + 1 rows and nsets sets of kMaxStage bridge increments
+    return pack_teams(h, k, tw, true, cap, 2, cta == 512 ? 200 * 1024 : 100 * 1024, 1, nsets * kMaxStage);
 }
 
 // One warp per imaginary-time window: P = min(8, M / (Mbar + 1)) windows.
@@ -2136,18 +2205,25 @@ cudaError_t build_windows(pgb_walkers* h) {
 cudaError_t launch_run(pgb_walkers* h, int sched, int sweeps, int measure) {
     AzizF af = make_aziz_f(h->az);
     if (sched >= 7000) {
+        // 7xxx: runs of up to two commuting moves, 8xxx: up to four
         const int ppt = sched % 1000;
         const int k = 13 + (ppt == 0 ? 0 : ppt == 8 ? 1 : 2);
-        cudaError_t e = build_pipe_teams(h, k, 512, ppt);
+        cudaError_t e = build_pipe_teams(h, k, 512, ppt, 4);
         if (e != cudaSuccess) return e;
         static bool attr = false;
         if (!attr) {
-            cudaFuncSetAttribute(k_walkers_pair2<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_walkers_group<512, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_walkers_group<512, 1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             attr = true;
         }
-        k_walkers_pair2<512, 1><<<h->team_ctas[k], 512, h->team_smem[k], h->stream>>>(h->d_meta,
-            h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
-            h->lambda, (float)h->p_com, h->var_updates, h->seed);
+        if (sched >= 8000)
+            k_walkers_group<512, 1, 4><<<h->team_ctas[k], 512, h->team_smem[k], h->stream>>>(h->d_meta,
+                h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
+                h->lambda, (float)h->p_com, h->var_updates, h->seed);
+        else
+            k_walkers_group<512, 1, 2><<<h->team_ctas[k], 512, h->team_smem[k], h->stream>>>(h->d_meta,
+                h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
+                h->lambda, (float)h->p_com, h->var_updates, h->seed);
         h->launches += 1;
         return cudaGetLastError();
     }
@@ -2254,13 +2330,14 @@ int autotune(pgb_walkers* h) {
     cudaMemcpyAsync(save_ctr, h->d_ctr, h->W * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream);
     cudaEvent_t a, b;
     cudaEventCreate(&a); cudaEventCreate(&b);
-    const int cand[12] = {2008, 4008, 5000, 5008, 5016, 6000, 6008, 6016, 3002, 7000, 7008, 7016};
+    const int cand[15] = {2008, 4008, 5000, 5008, 5016, 6000, 6008, 6016, 3002, 7000, 7008, 7016,
+                          8000, 8008, 8016};
     float best = 1e30f; int best_t = 6000;
-    for (int c = 0; c < 12; ++c) {
+    for (int c = 0; c < 15; ++c) {
         cudaMemcpyAsync(h->d_pos, save, pb, cudaMemcpyDeviceToDevice, h->stream);
         cudaMemcpyAsync(h->d_ctr, save_ctr, h->W * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->stream);
         cudaEventRecord(a, h->stream);
-        e = launch_run(h, cand[c], 1, 0);
+        e = launch_run(h, cand[c], 1, 1);          // one sweep with its energy sample
         cudaEventRecord(b, h->stream);
         if (e != cudaSuccess) {
             // a schedule that does not fit this workload (e.g. shared memory) is skipped
@@ -2306,14 +2383,15 @@ int pgb_walkers_create(const pgb_walkers_params* p, pgb_walkers** out) {
         const bool team = (t / 1000 == 1 || t / 1000 == 2) && (t % 1000 == 4 || t % 1000 == 8 || t % 1000 == 16);
         const bool win = (t == 3002 || t == 3003 || t == 4004 || t == 4008 || t == 4016 ||
                           t == 5000 || t == 5008 || t == 5016 || t == 6000 || t == 6008 || t == 6016 ||
-                          t == 7000 || t == 7008 || t == 7016);
+                          t == 7000 || t == 7008 || t == 7016 || t == 8000 || t == 8008 || t == 8016);
         if (!(t == 0 || t == 64 || t == 128 || t == 256 || team || win)) {
             g_werr = "threads_per_walker must be 0 (autotune), 64/128/256 (one CTA per walker), "
                      "1004/1008/1016 / 2004/2008/2016 (packed teams, 4/8/16 pairs per thread, "
                      "3 or 2 CTAs per SM), 3002/3003 (time windows, 2 or 3 CTAs per SM) or "
                      "4004/4008/4016 (packed teams with TMA-staged rows) or 5000/5008/5016/6000/6008/"
                      "6016 (pipelined TMA teams in 256/512-thread CTAs; x000 = cost-balanced teams) "
-                     "or 7000/7008/7016 (two commuting moves at once in half-teams)";
+                     "or 7000/7008/7016 (up to two commuting moves at once in sub-teams) or "
+                     "8000/8008/8016 (up to four)";
             return PGB_EINVAL;
         }
     }
@@ -2388,9 +2466,15 @@ int pgb_walkers_destroy(pgb_walkers* h) {
     if (!h) return PGB_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->d_meta); cudaFree(h->d_order); cudaFree(h->d_pos); cudaFree(h->d_acc);
-    cudaFree(h->d_ctr); cudaFree(h->d_en); cudaFree(h->d_stage);
-    for (int k = 0; k < 13; ++k) cudaFree(h->d_teams[k]);
+    if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+    cudaFree(h->d_ctr); cudaFree(h->d_en); cudaFree(h->d_stage[0]); cudaFree(h->d_stage[1]);
+    for (int k = 0; k < 16; ++k) cudaFree(h->d_teams[k]);
     cudaFree(h->d_err);
+    for (int b = 0; b < 2; ++b) {
+        if (h->ev_copied[b]) cudaEventDestroy(h->ev_copied[b]);
+        if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
+    }
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return PGB_OK;
@@ -2459,16 +2543,34 @@ size_t pgb_walkers_state_bytes(pgb_walkers* h) { return h ? (size_t)h->total_bea
 int pgb_walkers_set_all_positions(pgb_walkers* h, const double* pos) {
     if (!h || !pos) return PGB_EINVAL;
     size_t bytes = (size_t)h->total_beads * 3 * sizeof(double);
-    if (!h->d_stage) {
-        cudaError_t e = cudaMalloc(&h->d_stage, bytes);
-        if (e != cudaSuccess) return h->cfail(e, "cudaMalloc(stage)");
+    cudaError_t e = cudaSuccess;
+    if (!h->copy_stream) {
+        if ((e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return h->cfail(e, "copy stream");
+        for (int b = 0; b < 2; ++b) {
+            if ((e = cudaEventCreateWithFlags(&h->ev_copied[b], cudaEventDisableTiming)) != cudaSuccess ||
+                (e = cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming)) != cudaSuccess)
+                return h->cfail(e, "upload events");
+        }
     }
-    cudaError_t e = cudaMemcpyAsync(h->d_stage, pos, bytes, cudaMemcpyHostToDevice, h->stream);
-    if (e != cudaSuccess) return h->cfail(e, "walkers upload");
+    const int b = h->stage_idx;
+    if (!h->d_stage[b]) {
+        if ((e = cudaMalloc(&h->d_stage[b], bytes)) != cudaSuccess) return h->cfail(e, "cudaMalloc(stage)");
+        // a fresh buffer has no reader yet
+        if ((e = cudaEventRecord(h->ev_free[b], h->stream)) != cudaSuccess) return h->cfail(e, "upload event");
+    }
+    // copy on the copy stream once the conversion that last read this buffer
+    // is done; convert on the library stream once the copy has landed
+    if ((e = cudaStreamWaitEvent(h->copy_stream, h->ev_free[b], 0)) != cudaSuccess) return h->cfail(e, "upload wait");
+    if ((e = cudaMemcpyAsync(h->d_stage[b], pos, bytes, cudaMemcpyHostToDevice, h->copy_stream)) != cudaSuccess)
+        return h->cfail(e, "walkers upload");
+    if ((e = cudaEventRecord(h->ev_copied[b], h->copy_stream)) != cudaSuccess) return h->cfail(e, "upload event");
+    if ((e = cudaStreamWaitEvent(h->stream, h->ev_copied[b], 0)) != cudaSuccess) return h->cfail(e, "upload wait");
     int blocks = 152 * 8;
-    k_walkers_from64<<<blocks, 256, 0, h->stream>>>(h->d_stage, h->d_pos, h->total_beads);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return h->cfail(e, "walkers upload convert");
+    k_walkers_from64<<<blocks, 256, 0, h->stream>>>(h->d_stage[b], h->d_pos, h->total_beads);
+    if ((e = cudaGetLastError()) != cudaSuccess) return h->cfail(e, "walkers upload convert");
+    if ((e = cudaEventRecord(h->ev_free[b], h->stream)) != cudaSuccess) return h->cfail(e, "upload event");
+    h->stage_idx ^= 1;
     h->launches += 1;
     return PGB_OK;
 }

@@ -26,7 +26,8 @@ def _walkers(pgb, num, seed, sched, n=8, t=4.0, tau=0.004):
 
 
 @pytest.mark.parametrize("sched", [128, 1004, 1008, 1016, 2008, 3002, 3003, 4004, 4008, 4016,
-                                   5000, 5008, 5016, 6000, 6008, 6016, 7000, 7008, 7016])
+                                   5000, 5008, 5016, 6000, 6008, 6016, 7000, 7008, 7016,
+                                   8000, 8008, 8016])
 def test_schedule_runs_and_is_deterministic(pgb, sched):
     # N <= 90 keeps two Mbar-row buffers of every walker within the 100 KB
     # budget of the 256-thread pipelined schedules (5008/5016)
@@ -47,7 +48,7 @@ def test_schedule_runs_and_is_deterministic(pgb, sched):
     assert np.all(np.abs(runs[0][1]) <= L / 2 + 1e-5)
 
 
-@pytest.mark.parametrize("sched", [128, 3002, 5008, 6000, 7016])
+@pytest.mark.parametrize("sched", [128, 3002, 5008, 6000, 7016, 8016])
 def test_matched_energy_vs_oracle_walkers(pgb, oracle_lib, sched):
     num, equil, prod = 256, 60, 200
     W, p = _walkers(pgb, num, 11, sched)
@@ -109,3 +110,27 @@ def test_stats_array_matches_stats(pgb):
     assert list(arr["bead_updates"]) == [s["bead_updates"] for s in st]
     assert list(arr["energy_sum"]) == [s["energy_sum"] for s in st]
     assert [list(a) for a in arr["accepted"]] == [s["accepted"] for s in st]
+
+
+def test_set_all_positions_double_buffered(pgb):
+    """Back-to-back uploads go through two staging buffers on a copy stream;
+    each one takes effect in stream order and the last one wins."""
+    import ctypes as C
+    w = pgb.worldlines.workload_walkers(num=6, seed=8, nmax=24)
+    W = pgb.Walkers(w["n"], w["m"], w["temperature"], w["side"], w["mbar"], w["tau"], w["lam"],
+                    seed=1, threads_per_walker=6016)
+    W.init()
+    nbytes = int(W.lib.pgb_walkers_state_bytes(W.h))
+    rng = np.random.default_rng(0)
+    states = [rng.uniform(-0.4, 0.4, nbytes // 8) for _ in range(3)]
+    for k in range(3):
+        sides = np.repeat(w["side"], w["n"] * w["m"] * 3)
+        states[k] *= sides
+        W._chk(W.lib.pgb_walkers_set_all_positions(W.h, states[k].ctypes.data_as(C.POINTER(C.c_double))))
+    W.sync()
+    off = 0
+    for i in range(6):
+        n = int(w["n"][i] * w["m"][i] * 3)
+        want = states[2][off:off + n].reshape(w["m"][i], w["n"][i], 3)
+        assert np.allclose(W.positions(i), want, rtol=0, atol=1e-5 * w["side"][i])
+        off += n
