@@ -48,7 +48,7 @@ PAIR_FLOP_VG = 52
 SFU_PER_SM_CLK = 16     # nominal special-function results per SM per clock
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on
 # the workload its bench leg runs (profiles/ holds the summaries)
-NCU_TRAFFIC = {"k_walkers_pipe": 160.0e6}
+NCU_TRAFFIC = {"k_walkers_pipe": 160.4e6, "k_walkers_group": 158.9e6}
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -153,6 +153,8 @@ class Clocks:
 
 def walker_kernel(sched):
     """Kernel that runs a walker schedule code."""
+    if sched >= 7000:
+        return "k_walkers_group"
     if sched >= 5000:
         return "k_walkers_pipe"
     if sched >= 4000:
@@ -385,7 +387,7 @@ def run_isf(args, pgb):
     # (the reference copies its bead array to the device every sample)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        a.load(cfg)
+        a.update_positions(cfg["pos"])      # the bead array, as the reference copies it per sample
         a.isf(q, mode=1)
     t_e2e = (time.perf_counter() - t0) / args.steps
     # rho_q (the dominant kernel): Q M N phase evaluations, 2 special-function
@@ -411,7 +413,7 @@ def run_isf(args, pgb):
                       "ms_ssf": res["ssf"],
                       "phase_evaluations_per_s": nq * m * n / t_rho},
            "e2e": {"value": 1.0 / t_e2e, "unit": "configurations/s",
-                   "h2d_bytes_per_step": int(cfg["pos"].nbytes + q.nbytes + cfg["next"].nbytes * 2),
+                   "h2d_bytes_per_step": int(cfg["pos"].nbytes + q.nbytes),
                    "d2h_bytes_per_step": int(nq * (m // 2 + 1) * 8)},
            "roofline": {"bound": "sfu", "kernel": "k_rhoq32", "achieved": sfu / 1e9,
                         "peak": sfu_pk / 1e9, "unit": "Gop/s", "frac": sfu / sfu_pk, "traffic": None,

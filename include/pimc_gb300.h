@@ -89,6 +89,12 @@ int pgb_grad2v_batch(pgb_ctx* ctx, const double* sep, double* out, int n);
 int pgb_load_path(pgb_ctx* ctx, const double* pos, const int32_t* next,
                   const int32_t* prev, const uint8_t* on, const int32_t* worm8);
 int pgb_update_beads(pgb_ctx* ctx, const int32_t* beads, const double* pos, int k);
+/* New positions for every bead (AoS FP64 [M][Ne][3]) with links, on flags and
+ * worm unchanged: one host-to-device copy and an on-device transpose, as the
+ * reference's GPU estimators copy Path::beads before each sample
+ * (estimator.cpp:3846).  Asynchronous on the context stream; pos must stay
+ * unchanged until the next synchronous call. */
+int pgb_update_positions(pgb_ctx* ctx, const double* pos);
 int pgb_get_positions(pgb_ctx* ctx, double* pos);
 
 /* ---- potential action: LocalAction (action.cpp:456-740) --------------

@@ -132,6 +132,12 @@ class Action:
         self._chk(self.lib.pgb_load_path(self.h, dptr(pos), iptr(nxt), iptr(prv), u8ptr(on),
                                          iptr(worm)))
 
+    def update_positions(self, pos):
+        """All bead positions (AoS [M][Ne][3]) with links and worm unchanged."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(self.M, self.Ne, 3)
+        self._keep = pos                    # the copy is asynchronous
+        self._chk(self.lib.pgb_update_positions(self.h, dptr(pos)))
+
     def update_beads(self, beads, pos):
         beads = np.ascontiguousarray(beads, dtype=np.int32).reshape(-1, 2)
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)

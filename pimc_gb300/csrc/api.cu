@@ -73,6 +73,21 @@ __global__ void k_update_beads(double* pos, float4* pos32, int Ne, const int2* b
     pos32[(size_t)b.x * Ne + b.y] = make_float4((float)p[3*i], (float)p[3*i+1], (float)p[3*i+2], 0.f);
 }
 
+// AoS [M][Ne][3] FP64 (the reference's bead array) -> SoA [M][3][Ne] and the
+// float4 mirror, one bead per thread
+__global__ void k_positions_from_aos(const double* __restrict__ aos, double* __restrict__ pos,
+                                     float4* __restrict__ pos32, int M, int Ne) {
+    const size_t n = (size_t)M * Ne;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = i / Ne, p = i - s * Ne;
+        const double x = aos[3 * i], y = aos[3 * i + 1], z = aos[3 * i + 2];
+        double* X = pos + s * 3 * Ne;
+        X[p] = x; X[Ne + p] = y; X[2 * Ne + p] = z;
+        pos32[i] = make_float4((float)x, (float)y, (float)z, 0.f);
+    }
+}
+
 }  // namespace pgb
 
 using namespace pgb;
@@ -334,6 +349,21 @@ int pgb_load_path(pgb_ctx* h, const double* pos, const int32_t* next, const int3
     PGB_CUDA(&c, launch_pos32_from64(c.view(), c.d_pos32, c.stream));
     PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
     c.loaded = true;
+    c.force_valid = false;
+    return PGB_OK;
+}
+
+int pgb_update_positions(pgb_ctx* h, const double* pos) {
+    if (check_ctx(h) || !pos) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    const size_t nb = (size_t)c.M * c.Ne, bytes = nb * 3 * sizeof(double);
+    rc = c.ensure_scratch(bytes); if (rc) return rc;
+    PGB_CUDA(&c, cudaMemcpyAsync(c.d_scratch, pos, bytes, cudaMemcpyHostToDevice, c.stream));
+    const int blocks = (int)std::min<size_t>((nb + 255) / 256, 152 * 16);
+    k_positions_from_aos<<<blocks, 256, 0, c.stream>>>(static_cast<const double*>(c.d_scratch), c.d_pos,
+                                                       c.d_pos32, c.M, c.Ne);
+    PGB_CUDA(&c, cudaGetLastError());
     c.force_valid = false;
     return PGB_OK;
 }
@@ -718,6 +748,14 @@ int pgb_qvectors(const char* type, const char* input, const double side[3], doub
 // ---------------------------------------------------------------------------
 namespace {
 
+// work layout: rho_q (room for FP64 values), then for the FP32 path the slices
+// as box fractions, then the tensor-core scratch
+size_t rho_region(const Ctx& c, int nq) {
+    return ((size_t)nq * c.M * 2 * sizeof(double) + 255) & ~(size_t)255;
+}
+size_t posbuf_region(const Ctx& c) {
+    return (c.p.precision == PGB_MIXED) ? ((rhoq32_work_bytes(c.view()) + 255) & ~(size_t)255) : 0;
+}
 int scatter_common(Ctx& c, const double* d_q, int nq, int what, int mode, double* d_out,
                    void* d_work) {
     // what: 0 ssf, 1 isf, 2 rho (FP64 values)
@@ -737,7 +775,8 @@ int scatter_common(Ctx& c, const double* d_q, int nq, int what, int mode, double
         }
     } else {
         float2* d_rho = static_cast<float2*>(d_work);
-        e = launch_rhoq32(v, d_q, nq, d_rho, c.stream);
+        void* posbuf = static_cast<char*>(d_work) + rho_region(c, nq);
+        e = launch_rhoq32(v, d_q, nq, d_rho, posbuf, c.stream);
         if (e == cudaSuccess) {
             if (what == 0) e = launch_ssf_from_rho32(d_rho, nq, c.M, norm, d_out, c.stream);
             else if (mode == 1) {
@@ -749,7 +788,7 @@ int scatter_common(Ctx& c, const double* d_q, int nq, int what, int mode, double
                     e = isf_tc_build_tables(c.M, c.d_tc_tables, c.stream);
                     if (e != cudaSuccess) return c.cuda_fail(e, "F(q,tau) tables");
                 }
-                void* tc = static_cast<char*>(d_work) + (((size_t)nq * c.M * sizeof(float2) + 255) & ~(size_t)255);
+                void* tc = static_cast<char*>(d_work) + rho_region(c, nq) + posbuf_region(c);
                 e = launch_isf_tc(d_rho, nq, c.M, norm, d_out, tc, c.d_tc_tables, c.stream);
             } else e = launch_isf_direct32(d_rho, nq, c.M, norm, d_out, c.stream);
         }
@@ -759,10 +798,9 @@ int scatter_common(Ctx& c, const double* d_q, int nq, int what, int mode, double
 }
 
 size_t scatter_work_bytes(const Ctx& c, int nq, int what, int mode) {
-    size_t rho = (size_t)nq * c.M * 2 * sizeof(double);
     size_t extra = (c.p.precision == PGB_MIXED && what == 1 && mode == 1)
                        ? isf_tc_scratch_bytes(nq, c.M) : 0;
-    return ((rho + 255) & ~(size_t)255) + extra;
+    return rho_region(c, nq) + posbuf_region(c) + extra;
 }
 
 int scatter_host(pgb_ctx* h, const double* q, int nq, int what, int mode, double* out) {

@@ -207,12 +207,17 @@ cudaError_t launch_bead_actions32(const PathView& v, AzizParams a, const int2* d
 }
 
 // One warp per bead when every active same-slice bead is in the list (the
-// cutoff covers the box): no list compaction, no block barriers, and the GSF
-// correction in O(n) from the cached slice forces `fall` (see
-// k_bead_actions32).  With `delta` set and trial positions given, the warp
-// evaluates the bead at its trial and at its current position and writes
-// U(trial) - U(current): one launch per batch of trial moves.
+// cutoff covers the box): no list compaction, and the GSF correction in O(n)
+// from the cached slice forces `fall` (see k_bead_actions32).  With `delta`
+// set and trial positions given, the warp evaluates the bead at its trial and
+// at its current position and writes U(trial) - U(current): one launch per
+// batch of trial moves.  Each warp takes kBeadsPerWarp beads in turn and
+// leaves its FP32 (hi, lo) sums in shared memory; the FP64 assembly of the
+// actions then runs one bead per lane, so the narrow FP64 pipe sees a full
+// warp per instruction instead of one lane.
 constexpr int kWarpBeadBlock = 256;
+constexpr int kBeadsPerWarp = 4;
+constexpr int kBeadsPerBlock = (kWarpBeadBlock / 32) * kBeadsPerWarp;   // 32
 
 __device__ __forceinline__ float pair_factor32(int st1, int st2) {
     if (st1 == 2 && st2 == 2) return 1.0f;
@@ -225,88 +230,111 @@ k_bead_actions32_full(PathView v, AzizF az, const int2* __restrict__ beads, int 
                       int mode, double tau, double lambda, double vf0, double vf1, double gf0,
                       double gf1, const double* __restrict__ over, const float4* __restrict__ fall,
                       int delta, double* __restrict__ out) {
-    const int lane = threadIdx.x & 31;
-    const int b = blockIdx.x * (kWarpBeadBlock / 32) + (threadIdx.x >> 5);
-    if (b >= k) return;
+    // per bead of the block: Vn Vo Tn To Fnx Fny Fnz Fox Foy Foz as (hi, lo)
+    __shared__ float2 s_part[kBeadsPerBlock][10];
+    __shared__ int s_state[kBeadsPerBlock];      // 0 inactive or out of range, 1 active
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Ne = v.Ne;
-    const int s = beads[b].x, p = beads[b].y;
-    if (s < 0 || s >= v.M || p < 0 || p >= Ne || !v.on[(size_t)s * Ne + p]) {
-        if (lane == 0) out[b] = 0.0;
-        return;
-    }
-    const int eo = s % 2;
-    const double vf = eo ? vf1 : vf0, gf = eo ? gf1 : gf0;
-    const double t = (double)shift * tau;
-    const bool need_v = (mode != PGB_ACTION_CORR);
-    const bool need_c = (mode == PGB_ACTION_CORR) ? (gf > kEPS)
-                      : (mode == PGB_ACTION_FULL) ? (shift == 1 && gf > kEPS) : false;
     const bool both = delta && over;             // also the current position
     const float L0 = (float)v.side[0], L1 = (float)v.side[1], L2 = (float)v.side[2];
     const float I0 = (float)v.sideInv[0], I1 = (float)v.sideInv[1], I2 = (float)v.sideInv[2];
-    const float4* P = v.pos32 + (size_t)s * Ne;
-    const float4* Fs = fall + (size_t)s * Ne;
-    const float4 rpo = P[p];
-    const float4 r1 = over ? make_float4((float)over[3 * b], (float)over[3 * b + 1],
-                                         (float)over[3 * b + 2], 0.f) : rpo;
-    const int st1 = bead_state(v, s, p);
-    KahanF vn, vo, tn, to;
-    float fnx = 0.f, fny = 0.f, fnz = 0.f, fox = 0.f, foy = 0.f, foz = 0.f;
-    for (int j = lane; j < Ne; j += 32) {
-        if (j == p || !v.on[(size_t)s * Ne + j]) continue;
-        const float4 rj = P[j];
-        const float dx = min_image32(rj.x - r1.x, L0, I0);
-        const float dy = min_image32(rj.y - r1.y, L1, I1);
-        const float dz = min_image32(rj.z - r1.z, L2, I2);
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float fac = pair_factor32(st1, bead_state(v, s, j));
-        float ox = dx, oy = dy, oz = dz, ro2 = r2;
-        if (over) {
-            ox = min_image32(rj.x - rpo.x, L0, I0);
-            oy = min_image32(rj.y - rpo.y, L1, I1);
-            oz = min_image32(rj.z - rpo.z, L2, I2);
-            ro2 = fmaf(ox, ox, fmaf(oy, oy, oz * oz));
+    for (int r = 0; r < kBeadsPerWarp; ++r) {
+        const int lb = warp * kBeadsPerWarp + r;           // bead within the block
+        const int b = blockIdx.x * kBeadsPerBlock + lb;
+        if (b >= k) { if (lane == 0) s_state[lb] = 0; continue; }
+        const int s = beads[b].x, p = beads[b].y;
+        if (s < 0 || s >= v.M || p < 0 || p >= Ne || !v.on[(size_t)s * Ne + p]) {
+            if (lane == 0) s_state[lb] = 0;
+            continue;
         }
-        if (need_v) {
-            vn.add(fac * aziz_v32(r2, az));
-            if (both) vo.add(fac * aziz_v32(ro2, az));
-        }
-        if (need_c) {
-            const float g = aziz_g32(r2, az);
-            const float F2x = g * dx, F2y = g * dy, F2z = g * dz;
-            float Fox = F2x, Foy = F2y, Foz = F2z;
+        const int eo = s % 2;
+        const double gf = eo ? gf1 : gf0;
+        const bool need_v = (mode != PGB_ACTION_CORR);
+        const bool need_c = (mode == PGB_ACTION_CORR) ? (gf > kEPS)
+                          : (mode == PGB_ACTION_FULL) ? (shift == 1 && gf > kEPS) : false;
+        const float4* P = v.pos32 + (size_t)s * Ne;
+        const float4* Fs = fall + (size_t)s * Ne;
+        const float4 rpo = P[p];
+        const float4 r1 = over ? make_float4((float)over[3 * b], (float)over[3 * b + 1],
+                                             (float)over[3 * b + 2], 0.f) : rpo;
+        const int st1 = bead_state(v, s, p);
+        KahanF vn, vo, tn, to;
+        float fnx = 0.f, fny = 0.f, fnz = 0.f, fox = 0.f, foy = 0.f, foz = 0.f;
+        for (int j = lane; j < Ne; j += 32) {
+            if (j == p || !v.on[(size_t)s * Ne + j]) continue;
+            const float4 rj = P[j];
+            const float dx = min_image32(rj.x - r1.x, L0, I0);
+            const float dy = min_image32(rj.y - r1.y, L1, I1);
+            const float dz = min_image32(rj.z - r1.z, L2, I2);
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float fac = pair_factor32(st1, bead_state(v, s, j));
+            float ox = dx, oy = dy, oz = dz, ro2 = r2;
             if (over) {
-                const float go = aziz_g32(ro2, az);
-                Fox = go * ox; Foy = go * oy; Foz = go * oz;
+                ox = min_image32(rj.x - rpo.x, L0, I0);
+                oy = min_image32(rj.y - rpo.y, L1, I1);
+                oz = min_image32(rj.z - rpo.z, L2, I2);
+                ro2 = fmaf(ox, ox, fmaf(oy, oy, oz * oz));
             }
-            const float4 fa = Fs[j];
-            // F3: the slice force on j less the term of p at its current position
-            const float F3x = fa.x - Fox, F3y = fa.y - Foy, F3z = fa.z - Foz;
-            fnx -= F2x; fny -= F2y; fnz -= F2z;
-            tn.add(fmaf(2.0f, fmaf(F2x, F3x, fmaf(F2y, F3y, F2z * F3z)),
-                        fmaf(F2x, F2x, fmaf(F2y, F2y, F2z * F2z))));
-            if (both) {
-                fox -= Fox; foy -= Foy; foz -= Foz;
-                to.add(fmaf(2.0f, fmaf(Fox, F3x, fmaf(Foy, F3y, Foz * F3z)),
-                            fmaf(Fox, Fox, fmaf(Foy, Foy, Foz * Foz))));
+            if (need_v) {
+                vn.add(fac * aziz_v32(r2, az));
+                if (both) vo.add(fac * aziz_v32(ro2, az));
             }
+            if (need_c) {
+                const float g = aziz_g32(r2, az);
+                const float F2x = g * dx, F2y = g * dy, F2z = g * dz;
+                float Fox = F2x, Foy = F2y, Foz = F2z;
+                if (over) {
+                    const float go = aziz_g32(ro2, az);
+                    Fox = go * ox; Foy = go * oy; Foz = go * oz;
+                }
+                const float4 fa = Fs[j];
+                // F3: the slice force on j less the term of p at its current position
+                const float F3x = fa.x - Fox, F3y = fa.y - Foy, F3z = fa.z - Foz;
+                fnx -= F2x; fny -= F2y; fnz -= F2z;
+                tn.add(fmaf(2.0f, fmaf(F2x, F3x, fmaf(F2y, F3y, F2z * F3z)),
+                            fmaf(F2x, F2x, fmaf(F2y, F2y, F2z * F2z))));
+                if (both) {
+                    fox -= Fox; foy -= Foy; foz -= Foz;
+                    to.add(fmaf(2.0f, fmaf(Fox, F3x, fmaf(Foy, F3y, Foz * F3z)),
+                                fmaf(Fox, Fox, fmaf(Foy, Foy, Foz * Foz))));
+                }
+            }
+        }
+        const float2 parts[10] = {warp_ff(vn), warp_ff(vo), warp_ff(tn), warp_ff(to),
+                                  ff_butterfly(fnx, 0.f), ff_butterfly(fny, 0.f), ff_butterfly(fnz, 0.f),
+                                  ff_butterfly(fox, 0.f), ff_butterfly(foy, 0.f), ff_butterfly(foz, 0.f)};
+        if (lane == 0) {
+            #pragma unroll
+            for (int q = 0; q < 10; ++q) s_part[lb][q] = parts[q];
+            s_state[lb] = 1;
         }
     }
-    const float2 Vn = warp_ff(vn), Vo = warp_ff(vo), Tn = warp_ff(tn), To = warp_ff(to);
-    const float2 Fnx = ff_butterfly(fnx, 0.f), Fny = ff_butterfly(fny, 0.f), Fnz = ff_butterfly(fnz, 0.f);
-    const float2 Fox2 = ff_butterfly(fox, 0.f), Foy2 = ff_butterfly(foy, 0.f), Foz2 = ff_butterfly(foz, 0.f);
-    if (lane == 0) {
-        auto dd = [](float2 x) { return (double)x.x + (double)x.y; };
-        auto action = [&](double V, double T, double fx, double fy, double fz) {
-            const double bareU = vf * t * V;
-            const double corU = need_c ? gf * t * t * t * lambda * (T + (fx * fx + fy * fy + fz * fz)) : 0.0;
-            return (mode == PGB_ACTION_BARE) ? bareU : (mode == PGB_ACTION_CORR) ? corU : bareU + corU;
-        };
-        const double un = action(need_v ? dd(Vn) : 0.0, dd(Tn), dd(Fnx), dd(Fny), dd(Fnz));
-        if (both) {
-            const double uo = action(need_v ? dd(Vo) : 0.0, dd(To), dd(Fox2), dd(Foy2), dd(Foz2));
-            out[b] = un - uo;
-        } else {
-            out[b] = un;
+    __syncthreads();
+    if (warp == 0) {
+        // one bead of the block per lane: the FP64 assembly of its action(s)
+        const int b = blockIdx.x * kBeadsPerBlock + lane;
+        if (b < k) {
+            double res = 0.0;
+            if (s_state[lane]) {
+                const int s = beads[b].x;
+                const int eo = s % 2;
+                const double vf = eo ? vf1 : vf0, gf = eo ? gf1 : gf0;
+                const double t = (double)shift * tau;
+                const bool need_v = (mode != PGB_ACTION_CORR);
+                const bool need_c = (mode == PGB_ACTION_CORR) ? (gf > kEPS)
+                                  : (mode == PGB_ACTION_FULL) ? (shift == 1 && gf > kEPS) : false;
+                const float2* q = s_part[lane];
+                auto dd = [](float2 x) { return (double)x.x + (double)x.y; };
+                auto action = [&](double V, double T, double fx, double fy, double fz) {
+                    const double bareU = vf * t * V;
+                    const double corU = need_c ? gf * t * t * t * lambda * (T + (fx * fx + fy * fy + fz * fz)) : 0.0;
+                    return (mode == PGB_ACTION_BARE) ? bareU : (mode == PGB_ACTION_CORR) ? corU : bareU + corU;
+                };
+                res = action(need_v ? dd(q[0]) : 0.0, dd(q[2]), dd(q[4]), dd(q[5]), dd(q[6]));
+                if (both)
+                    res -= action(need_v ? dd(q[1]) : 0.0, dd(q[3]), dd(q[7]), dd(q[8]), dd(q[9]));
+            }
+            out[b] = res;
         }
     }
 }
@@ -317,8 +345,7 @@ cudaError_t launch_bead_actions32_full(const PathView& v, AzizParams a, const in
                                        const float4* d_force, int delta, double* d_out,
                                        cudaStream_t s) {
     if (k <= 0) return cudaSuccess;
-    const int per = kWarpBeadBlock / 32;
-    k_bead_actions32_full<<<(k + per - 1) / per, kWarpBeadBlock, 0, s>>>(
+    k_bead_actions32_full<<<(k + kBeadsPerBlock - 1) / kBeadsPerBlock, kWarpBeadBlock, 0, s>>>(
         v, make_aziz_f(a), d_beads, k, shift, mode, tau, lambda, vf[0], vf[1], gf[0], gf[1],
         d_over, d_force, delta, d_out);
     return cudaGetLastError();

@@ -20,18 +20,32 @@ namespace pgb {
 // only the sine and cosine.
 constexpr int kRhoBlock = 256;
 
+// The beads of every slice as fractions of the box, once per call: FP32
+// turns for general q and 32-bit fixed-point turns for lattice q.  The FP64
+// conversion runs here once per bead instead of once per (bead, q block).
+__global__ void k_rho_positions(PathView v, float4* __restrict__ uf, int4* __restrict__ ui) {
+    const size_t n = (size_t)v.M * v.Ne;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t t = idx / v.Ne, j = idx - t * v.Ne;
+        const double* X = v.pos + t * 3 * v.Ne;
+        const double ux = X[j] * v.sideInv[0], uy = X[v.Ne + j] * v.sideInv[1],
+                     uz = X[2 * v.Ne + j] * v.sideInv[2];
+        uf[idx] = make_float4((float)ux, (float)uy, (float)uz, 0.f);
+        ui[idx] = make_int4(fixed_turns(ux), fixed_turns(uy), fixed_turns(uz), 0);
+    }
+}
+
 __global__ void __launch_bounds__(kRhoBlock)
-k_rhoq32(PathView v, const double* __restrict__ q, int nq, float2* __restrict__ rho) {
+k_rhoq32(PathView v, const float4* __restrict__ uf, const int4* __restrict__ ui,
+         const double* __restrict__ q, int nq, float2* __restrict__ rho) {
     extern __shared__ float4 su[];
     int4* si = reinterpret_cast<int4*>(su + v.Ne);
     const int t = blockIdx.y;
     const int n = v.nbs[t];
-    const double* X = v.pos + (size_t)t * 3 * v.Ne;
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double ux = X[j] * v.sideInv[0], uy = X[v.Ne + j] * v.sideInv[1],
-                     uz = X[2 * v.Ne + j] * v.sideInv[2];
-        su[j] = make_float4((float)ux, (float)uy, (float)uz, 0.f);
-        si[j] = make_int4(fixed_turns(ux), fixed_turns(uy), fixed_turns(uz), 0);
+        su[j] = uf[(size_t)t * v.Ne + j];
+        si[j] = ui[(size_t)t * v.Ne + j];
     }
     __syncthreads();
     const int iq = blockIdx.x * kRhoBlock + threadIdx.x;
@@ -49,9 +63,20 @@ k_rhoq32(PathView v, const double* __restrict__ q, int nq, float2* __restrict__ 
         : rho_partial(su, n, (float)dx, (float)dy, (float)dz);
 }
 
+size_t rhoq32_work_bytes(const PathView& v) {
+    return (size_t)v.M * v.Ne * (sizeof(float4) + sizeof(int4));
+}
+
 cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* d_rho,
-                          cudaStream_t s) {
+                          void* d_work, cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
+    float4* uf = static_cast<float4*>(d_work);
+    int4* ui = reinterpret_cast<int4*>(uf + (size_t)v.M * v.Ne);
+    {
+        const size_t nb = (size_t)v.M * v.Ne;
+        const int blocks = (int)std::min<size_t>((nb + 255) / 256, 152 * 16);
+        k_rho_positions<<<blocks, 256, 0, s>>>(v, uf, ui);
+    }
     dim3 grid((nq + kRhoBlock - 1) / kRhoBlock, v.M);
     size_t smem = (size_t)v.Ne * (sizeof(float4) + sizeof(int4));
     if (smem > 200 * 1024) return cudaErrorInvalidValue;   // one slice must fit in shared memory
@@ -60,7 +85,7 @@ cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* 
         cudaFuncSetAttribute(k_rhoq32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    k_rhoq32<<<grid, kRhoBlock, smem, s>>>(v, d_q, nq, d_rho);
+    k_rhoq32<<<grid, kRhoBlock, smem, s>>>(v, uf, ui, d_q, nq, d_rho);
     return cudaGetLastError();
 }
 

@@ -290,3 +290,23 @@ def test_mixed_correction_follows_updates(pgb, oracle_lib, small):
             r -= d["L"] * np.floor(r / d["L"] + 0.5)
             a.update_beads([[s, p]], [r])
             o.update_bead(s, p, r)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_update_positions(pgb, oracle_lib, small, precision):
+    """All positions replaced through the on-device transpose: positions,
+    actions and S(q) follow, with links and worm kept."""
+    d = small
+    a, o = make_pair(pgb, oracle_lib, d["cfg"], d["L"], d["m"], d["n"], d["tau"], d["lam"],
+                     action="gsf", precision=precision)
+    cfg2 = pgb.worldlines.seeded_worldlines(d["n"], d["m"], d["L"], d["lam"], d["tau"], 99)
+    a.bead_actions([[1, 1]])                 # builds any cached slice forces first
+    a.update_positions(cfg2["pos"])
+    o.load(dict(d["cfg"], pos=cfg2["pos"]))
+    assert np.array_equal(a.positions(), cfg2["pos"])
+    rng = np.random.default_rng(2)
+    beads = random_beads(rng, d["m"], d["n"], 20)
+    want = np.array([o.bead_action(int(s), int(p)) for s, p in beads])
+    got, _ = a.bead_actions(beads)
+    tol = TOL64 if precision == 0 else 2e-4
+    assert np.max(np.abs(got - want) / np.maximum(np.abs(want), 1.0)) <= tol
