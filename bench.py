@@ -390,6 +390,16 @@ def run_isf(args, pgb):
         a.update_positions(cfg["pos"])      # the bead array, as the reference copies it per sample
         a.isf(q, mode=1)
     t_e2e = (time.perf_counter() - t0) / args.steps
+    # the adjacent path-wide estimators on the same path (host calls,
+    # synchronous): g(r) over all slices, winding sums, permutation cycles
+    adj = {}
+    for name, fn in (("pair_correlation", lambda: a.pair_correlation(-1)),
+                     ("superfluid", a.superfluid), ("permutation_cycles", a.permutation_cycles)):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        adj[name + "_ms"] = 1e3 * (time.perf_counter() - t0) / args.steps
     # rho_q (the dominant kernel): Q M N phase evaluations, 2 special-function
     # ops (sin, cos) each; S(q) = rho_q plus an O(Q M) reduction, so its time
     # stands for the rho_q kernel.  Correlation (the GEMM part): the
@@ -410,7 +420,7 @@ def run_isf(args, pgb):
            "config": {"workload": "F(q,tau): N=512, M=512, 2048 lattice q |q|<=4/A, tau in [0,M/2]",
                       "l2": "flushed between timed steps",
                       "ms_cuda_core_correlation": res[0], "ms_tensor_core_correlation": res[1],
-                      "ms_ssf": res["ssf"],
+                      "ms_ssf": res["ssf"], "adjacent_estimators": adj,
                       "phase_evaluations_per_s": nq * m * n / t_rho},
            "e2e": {"value": 1.0 / t_e2e, "unit": "configurations/s",
                    "h2d_bytes_per_step": int(cfg["pos"].nbytes + q.nbytes),
@@ -442,6 +452,13 @@ def run_isf(args, pgb):
         out["cpu_baseline"] = {"value": 1.0 / per_cfg, "unit": "configurations/s", "cores": thr,
                                "kind": "port", "sample": "FP64 rho_q form for %d of the %d q-vectors, "
                                "scaled to all of them" % (len(sub), nq)}
+        cpu_adj = {}
+        for name, fn in (("pair_correlation", lambda: o.pair_correlation(-1)),
+                         ("superfluid", o.superfluid), ("permutation_cycles", o.permutation_cycles)):
+            t0 = time.perf_counter()
+            fn()
+            cpu_adj[name + "_ms"] = 1e3 * (time.perf_counter() - t0)
+        out["cpu_baseline"]["adjacent_estimators_1_thread"] = cpu_adj
     print(json.dumps(out))
 
 

@@ -161,6 +161,20 @@ int pgb_ssf(pgb_ctx* ctx, const double* q, int nq, double* out);
  * mode 0: CUDA-core correlation; mode 1: tensor-core (tcgen05, split-BF16)
  * DFT correlation.  PGB_FP64 contexts always use the FP64 direct form. */
 int pgb_isf(pgb_ctx* ctx, const double* q, int nq, int mode, double* out);
+/* The adjacent path-wide estimators, one accumulate() each (FP64):
+ * g(r): PairCorrelationEstimator (estimator.cpp:3181-3246), 50 bins of
+ *   0.5 sqrt(3) L_z / 50, the sample already times the estimator's norm;
+ *   slice >= 0 takes that slice's separation histogram, as the reference's
+ *   LocalAction::V(slice) leaves it (action.cpp:902-947), slice < 0 all of
+ *   them.
+ * superfluid: SuperfluidFractionEstimator (estimator.cpp:2000-2074), 26
+ *   columns W^2/N, W_x^2, W_y^2, W_z^2, P(-10..10), Az^2/I; the per-bin norms
+ *   T/(6 lambda) and T M/(2 lambda) are the caller's, as in the reference.
+ * permutation cycles: PermutationCycleEstimator (estimator.cpp:2735-2781), 40
+ *   columns; PGB_ESTATE if a worldline through slice 0 does not close. */
+int pgb_pair_correlation(pgb_ctx* ctx, int slice, double out50[50]);
+int pgb_superfluid(pgb_ctx* ctx, double out26[26]);
+int pgb_permutation_cycles(pgb_ctx* ctx, double out40[40]);
 /* rho_q(t) of the loaded path, layout [q][M][2] (FP64 values) */
 int pgb_rhoq(pgb_ctx* ctx, const double* q, int nq, double* out);
 

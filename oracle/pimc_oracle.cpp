@@ -1408,3 +1408,105 @@ double orc_walkers_cpu(int W, const int* N, const int* M, const double* T,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Adjacent path-wide estimators (the ranked-next rows of the hot-path table).
+// ---------------------------------------------------------------------------
+extern "C" {
+
+// PairCorrelationEstimator (estimator.cpp:3181-3246) over the separation
+// histogram that LocalAction::V(slice) fills (action.cpp:902-947 with
+// ActionBase::updateSepHist, action.cpp:216-224): bins of
+// dSep = 0.5 sqrt(3) L_z / NPCFSEP (action.cpp:192), pairs b1 < b2 of a
+// slice, |r_b2 - r_b1| (minimum image).  V(slice) clears the histogram, so
+// the reference's estimator sees the slice of the last V(slice) call;
+// slice >= 0 reproduces that, slice < 0 sums every slice.  Output: one
+// accumulate() increment already multiplied by the constructor's norm(n),
+// i.e. g(r_n) of this sample.
+void orc_pair_correlation(orc_sys* h, int slice, double* out50) {
+    Sys* s = h->s;
+    const int NPCF = 50;                       // NPCFSEP, include/common.h:85
+    const double dSep = 0.5 * std::sqrt(3.0) * s->side[2] / (1.0 * NPCF);
+    const double dR = 0.5 * std::sqrt(3.0) * s->side[2] / (1.0 * NPCF);   // periodic in all 3
+    std::vector<long long> hist(NPCF, 0);
+    const int t0 = slice >= 0 ? slice : 0, t1 = slice >= 0 ? slice + 1 : s->M;
+    for (int t = t0; t < t1; ++t)
+        for (int b1 = 0; b1 < s->nbs[t]; ++b1)
+            for (int b2 = b1 + 1; b2 < s->nbs[t]; ++b2) {
+                dVec d = s->sep(t, b2, t, b1);
+                int nR = int(std::sqrt(dot(d, d)) / dSep);
+                if (nR >= 0 && nR < NPCF) ++hist[nR];
+            }
+    const int N = s->trueNumParticles();
+    double tot = 0.0;
+    for (int n = 0; n < NPCF; ++n) tot += 1.0 * hist[n];
+    const double lnorm = 1.0 * (N - 1) / (1.0 * N);
+    const double volume = s->side[0] * s->side[1] * s->side[2];
+    const double gNorm = 3.0 / (2.0 * M_PI);
+    for (int n = 0; n < NPCF; ++n) {
+        const double dV = std::pow((n + 1) * dR, 3.0) - std::pow(n * dR, 3.0);
+        const double norm = 0.5 * (gNorm * volume) / dV;
+        out50[n] = ((N > 1) && (tot > 0.0)) ? lnorm * (1.0 * hist[n] / tot) * norm : 0.0;
+    }
+}
+
+// SuperfluidFractionEstimator::accumulate (estimator.cpp:2000-2074), one
+// increment of its 26 columns: W^2/N, W_x^2, W_y^2, W_z^2 (W in box units),
+// P(w) for w = -10..10 (|W_z/L - w| < 0.2), Az^2/I; the norms W2Norm =
+// T/(2 * 3 * lambda) and ANorm = T M/(2 lambda) are left to the caller
+// (estimator.cpp:1976-1980), as the reference applies them per bin.
+void orc_superfluid(orc_sys* h, double* out26) {
+    Sys* s = h->s;
+    dVec W{0, 0, 0};
+    double Az = 0.0, I = 0.0;
+    for (int t = 0; t < s->M; ++t)
+        for (int p = 0; p < s->nbs[t]; ++p) {
+            dVec v = s->velocity(t, p);
+            for (int d = 0; d < 3; ++d) W[d] += v[d];
+            auto nx = s->next(t, p);
+            if (nx[0] < 0) continue;                // no next bead: a worm end
+            dVec p1 = s->P(t, p);
+            dVec p2 = s->P(nx[0], nx[1]);
+            Az += p1[0] * p2[1] - p2[0] * p1[1];
+            I += p1[0] * p2[0] + p1[1] * p2[1];
+        }
+    for (int i = 0; i < 26; ++i) out26[i] = 0.0;
+    const int N = s->trueNumParticles();
+    if (N > 0) {
+        out26[0] = dot(W, W) / (1.0 * N);
+        out26[25] = Az * Az / I;
+    }
+    for (int d = 0; d < 3; ++d) W[d] *= s->sideInv[d];
+    for (int d = 0; d < 3; ++d) out26[1 + d] = W[d] * W[d];
+    int n = 0;
+    for (int p = -10; p <= 10; ++p) {
+        if (std::fabs(W[2] - 1.0 * p) < 0.2) out26[4 + n] = 1.0;
+        ++n;
+    }
+}
+
+// PermutationCycleEstimator::accumulate (estimator.cpp:2735-2781): every
+// worldline through slice 0, counted once, adds cycleNum/N to the entry of
+// its cycle length (up to 40).  Closed paths only.
+void orc_permutation_cycles(orc_sys* h, double* out40) {
+    Sys* s = h->s;
+    for (int i = 0; i < 40; ++i) out40[i] = 0.0;
+    const int N = s->trueNumParticles();
+    const double cycleNorm = N > 0 ? 1.0 / (1.0 * N) : 0.0;
+    const int nw = s->nbs[0];
+    std::vector<char> doBead(nw, 1);
+    for (int n = 0; n < nw; ++n) {
+        if (!doBead[n]) continue;
+        std::array<int,2> b{0, n};
+        int wl = 0;
+        do {
+            ++wl;
+            if (b[0] == 0 && b[1] < nw) doBead[b[1]] = 0;
+            b = s->next(b[0], b[1]);
+        } while (!(b[0] == 0 && b[1] == n) && wl <= s->M * s->Ne);
+        const int cycleNum = wl / s->M;
+        if (cycleNum > 0 && cycleNum <= 40) out40[cycleNum - 1] += 1.0 * cycleNum * cycleNorm;
+    }
+}
+
+}  // extern "C"

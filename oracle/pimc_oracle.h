@@ -96,6 +96,14 @@ void orc_virial(orc_sys* s, int cvcov2_quirk, double out19[19]);
 /* q-vector list (EstimatorBase::getQVectors); returns count, fills up to cap */
 int  orc_qvectors(const char* type, const char* input, const double side[3],
                   double* q, int cap);
+/* g(r): one PairCorrelationEstimator sample (50 bins) times its norm; slice
+ * >= 0 uses that slice's histogram (the reference's V(slice) side effect),
+ * slice < 0 every slice */
+void orc_pair_correlation(orc_sys* s, int slice, double* out50);
+/* one SuperfluidFractionEstimator increment (26 columns, norms not applied) */
+void orc_superfluid(orc_sys* s, double* out26);
+/* one PermutationCycleEstimator increment (40 columns) */
+void orc_permutation_cycles(orc_sys* s, double* out40);
 /* S(q) pairwise CPU form, per-sample value already normalised by 1/(N M) */
 void orc_ssf_pairwise(orc_sys* s, const double* q, int nq, double* out);
 /* S(q) by rho_q in FP64 */

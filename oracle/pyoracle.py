@@ -93,6 +93,9 @@ def load():
         "orc_isf_gpu_form": (None, [_VP, _DP, C.c_int, _DP]),
         "orc_isf_rhoq": (None, [_VP, _DP, C.c_int, C.c_int, _DP]),
         "orc_rhoq": (None, [_VP, _DP, C.c_int, _DP]),
+        "orc_pair_correlation": (None, [_VP, C.c_int, _DP]),
+        "orc_superfluid": (None, [_VP, _DP]),
+        "orc_permutation_cycles": (None, [_VP, _DP]),
         "orc_mt_create": (_VP, [C.c_uint32]),
         "orc_mt_destroy": (None, [_VP]),
         "orc_mt_randint": (C.c_uint32, [_VP]),
@@ -275,6 +278,21 @@ class Oracle:
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
         out = np.zeros((len(q), self.M // 2 + 1))
         self.lib.orc_isf_rhoq(self.h, _d(q), len(q), threads, _d(out))
+        return out
+
+    def pair_correlation(self, slice=-1):
+        out = np.zeros(50)
+        self.lib.orc_pair_correlation(self.h, slice, _d(out))
+        return out
+
+    def superfluid(self):
+        out = np.zeros(26)
+        self.lib.orc_superfluid(self.h, _d(out))
+        return out
+
+    def permutation_cycles(self):
+        out = np.zeros(40)
+        self.lib.orc_permutation_cycles(self.h, _d(out))
         return out
 
     def rhoq(self, q):

@@ -213,6 +213,21 @@ class Action:
         self._chk(self.lib.pgb_isf(self.h, dptr(q), len(q), mode, dptr(out)))
         return out
 
+    def pair_correlation(self, slice=-1):
+        out = np.zeros(50)
+        self._chk(self.lib.pgb_pair_correlation(self.h, slice, dptr(out)))
+        return out
+
+    def superfluid(self):
+        out = np.zeros(26)
+        self._chk(self.lib.pgb_superfluid(self.h, dptr(out)))
+        return out
+
+    def permutation_cycles(self):
+        out = np.zeros(40)
+        self._chk(self.lib.pgb_permutation_cycles(self.h, dptr(out)))
+        return out
+
     def rhoq(self, q):
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
         out = np.zeros((len(q), self.M, 2))

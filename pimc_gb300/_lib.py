@@ -112,6 +112,9 @@ _SIGS = {
     "pgb_rhoq": (C.c_int, [_VP, _DP, C.c_int, _DP]),
     "pgb_isf_device_async": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP]),
     "pgb_update_positions": (C.c_int, [_VP, _DP]),
+    "pgb_pair_correlation": (C.c_int, [_VP, C.c_int, _DP]),
+    "pgb_superfluid": (C.c_int, [_VP, _DP]),
+    "pgb_permutation_cycles": (C.c_int, [_VP, _DP]),
     "pgb_ssf_device_async": (C.c_int, [_VP, _VP, C.c_int, _VP]),
     "pgb_load_positions_device_async": (C.c_int, [_VP, _VP]),
     "pgb_stream": (_VP, [_VP]),

@@ -945,3 +945,92 @@ int pgb_trial_actions_device_async(pgb_ctx* h, const int32_t* d_beads, const dou
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Adjacent path-wide estimators: g(r), superfluid fraction, permutation cycles
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int pgb_pair_correlation(pgb_ctx* h, int slice, double* out50) {
+    if (check_ctx(h) || !out50) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    if (slice >= c.M) return c.fail(PGB_EINVAL, "pair_correlation: slice out of range");
+    rc = c.ensure_scratch(64 * sizeof(unsigned long long)); if (rc) return rc;
+    auto* d_hist = static_cast<unsigned long long*>(c.d_scratch);
+    PGB_CUDA(&c, launch_sep_hist(c.view(), slice, d_hist, c.stream));
+    unsigned long long hist[50];
+    PGB_CUDA(&c, cudaMemcpyAsync(hist, d_hist, sizeof(hist), cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    // PairCorrelationEstimator: constructor norm (estimator.cpp:3187-3223) and
+    // accumulate (estimator.cpp:3238-3246), 3D periodic box
+    const int N = c.numBeadsOn / c.M;
+    double tot = 0.0;
+    for (int n = 0; n < 50; ++n) tot += 1.0 * (double)hist[n];
+    const double lnorm = 1.0 * (N - 1) / (1.0 * N);
+    const double dR = 0.5 * std::sqrt(3.0) * c.p.side[2] / (1.0 * 50);
+    const double volume = c.p.side[0] * c.p.side[1] * c.p.side[2];
+    const double gNorm = 3.0 / (2.0 * M_PI);
+    for (int n = 0; n < 50; ++n) {
+        const double dV = std::pow((n + 1) * dR, 3.0) - std::pow(n * dR, 3.0);
+        const double norm = 0.5 * (gNorm * volume) / dV;
+        out50[n] = ((N > 1) && (tot > 0.0)) ? lnorm * (1.0 * (double)hist[n] / tot) * norm : 0.0;
+    }
+    return PGB_OK;
+}
+
+int pgb_superfluid(pgb_ctx* h, double* out26) {
+    if (check_ctx(h) || !out26) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    rc = c.ensure_scratch(winding_work_bytes()); if (rc) return rc;
+    double* d_work = static_cast<double*>(c.d_scratch);
+    double* d_out = d_work + (winding_work_bytes() / sizeof(double) - 5);
+    PGB_CUDA(&c, launch_winding(c.view(), d_work, d_out, c.stream));
+    double s5[5];
+    PGB_CUDA(&c, cudaMemcpyAsync(s5, d_out, sizeof(s5), cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    // SuperfluidFractionEstimator::accumulate, estimator.cpp:2000-2074
+    double W[3] = {s5[0], s5[1], s5[2]};
+    const double Az = s5[3], I = s5[4];
+    for (int i = 0; i < 26; ++i) out26[i] = 0.0;
+    const int N = c.numBeadsOn / c.M;
+    if (N > 0) {
+        out26[0] = (W[0] * W[0] + W[1] * W[1] + W[2] * W[2]) / (1.0 * N);
+        out26[25] = Az * Az / I;
+    }
+    for (int d = 0; d < 3; ++d) W[d] *= 1.0 / c.p.side[d];
+    for (int d = 0; d < 3; ++d) out26[1 + d] = W[d] * W[d];
+    int n = 0;
+    for (int p = -10; p <= 10; ++p) {
+        if (std::fabs(W[2] - 1.0 * p) < 0.2) out26[4 + n] = 1.0;
+        ++n;
+    }
+    return PGB_OK;
+}
+
+int pgb_permutation_cycles(pgb_ctx* h, double* out40) {
+    if (check_ctx(h) || !out40) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    const int nw = c.h_nbs.empty() ? 0 : c.h_nbs[0];
+    for (int i = 0; i < 40; ++i) out40[i] = 0.0;
+    if (nw == 0) return PGB_OK;
+    rc = c.ensure_scratch((size_t)nw * sizeof(int)); if (rc) return rc;
+    int* d_len = static_cast<int*>(c.d_scratch);
+    PGB_CUDA(&c, launch_cycles(c.view(), nw, d_len, c.stream));
+    std::vector<int> len(nw);
+    PGB_CUDA(&c, cudaMemcpyAsync(len.data(), d_len, nw * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    // PermutationCycleEstimator::accumulate, estimator.cpp:2735-2781
+    const int N = c.numBeadsOn / c.M;
+    const double cycleNorm = N > 0 ? 1.0 / (1.0 * N) : 0.0;
+    for (int i = 0; i < nw; ++i) {
+        if (len[i] < 0) return c.fail(PGB_ESTATE, "permutation_cycles: the path has an open worldline");
+        const int cycleNum = len[i] / c.M;
+        if (cycleNum > 0 && cycleNum <= 40) out40[cycleNum - 1] += 1.0 * cycleNum * cycleNorm;
+    }
+    return PGB_OK;
+}
+
+}  // extern "C"

@@ -138,6 +138,11 @@ cudaError_t launch_ssf_from_rho64(const double* d_rho, int nq, int M,
                                   double norm, double* d_out, cudaStream_t s);
 cudaError_t launch_isf_direct32(const float2* d_rho, int nq, int M, double norm,
                                 double* d_out, cudaStream_t s);
+// path_estimators.cu (g(r), winding, permutation cycles; FP64, -fmad=false)
+cudaError_t launch_sep_hist(const PathView& v, int slice, unsigned long long* d_hist, cudaStream_t s);
+size_t winding_work_bytes();
+cudaError_t launch_winding(const PathView& v, double* d_work, double* d_out5, cudaStream_t s);
+cudaError_t launch_cycles(const PathView& v, int nw, int* d_len, cudaStream_t s);
 // isf_tc.cu (tcgen05 split-BF16 DFT correlation)
 size_t isf_tc_scratch_bytes(int nq, int M);
 size_t isf_tc_table_bytes(int M);

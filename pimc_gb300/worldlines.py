@@ -152,3 +152,17 @@ def workload_walkers(num=1024, seed=0, tau=TAU, nmin=8, nmax=128, tmin=1.0, tmax
     mbar = np.array([default_mbar(int(k), s ** 3, LAMBDA_HE4, tau, int(mm))
                      for k, s, mm in zip(n, side, m)], dtype=np.int32)
     return dict(n=n, m=m, temperature=t, side=side, mbar=mbar, tau=tau, lam=LAMBDA_HE4)
+
+
+def permute(cfg, cycles):
+    """Close worldlines into exchange cycles: for each tuple (p0, p1, ...) of
+    particles, the bead of p_k on the last slice links to the bead of
+    p_{k+1} on slice 0 (cyclically), and the prev links follow."""
+    c = {k: v.copy() for k, v in cfg.items()}
+    m = c["pos"].shape[0]
+    for cyc in cycles:
+        for k, p in enumerate(cyc):
+            q = cyc[(k + 1) % len(cyc)]
+            c["next"][m - 1, p] = (0, q)
+            c["prev"][0, q] = (m - 1, p)
+    return c

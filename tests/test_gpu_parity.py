@@ -310,3 +310,31 @@ def test_update_positions(pgb, oracle_lib, small, precision):
     got, _ = a.bead_actions(beads)
     tol = TOL64 if precision == 0 else 2e-4
     assert np.max(np.abs(got - want) / np.maximum(np.abs(want), 1.0)) <= tol
+
+
+def test_path_estimators_match_oracle(pgb, oracle_lib, small):
+    """g(r) (exact histograms), winding sums and permutation cycles against the
+    oracle, on the identity permutation and on one with exchange cycles."""
+    d = small
+    for cycles in ([], [(0, 1), (2, 3, 4), (5, 6, 7, 8)]):
+        cfg = pgb.worldlines.permute(d["cfg"], cycles)
+        a, o = make_pair(pgb, oracle_lib, cfg, d["L"], d["m"], d["n"], d["tau"], d["lam"])
+        for s in (-1, 0, d["m"] - 1):
+            assert np.array_equal(a.pair_correlation(s), o.pair_correlation(s)), s
+        assert np.array_equal(a.permutation_cycles(), o.permutation_cycles())
+        got, want = a.superfluid(), o.superfluid()
+        # W^2 columns: sums of O(N M) minimum-image steps that cancel around
+        # closed worldlines, compared with an absolute tolerance on that scale
+        scale = d["n"] * d["m"] * d["L"]
+        assert np.all(np.abs(got[:4] - want[:4]) <= (1e-12 * scale) ** 2 + 1e-12 * np.abs(want[:4]))
+        assert np.array_equal(got[4:25], want[4:25])
+        assert abs(got[25] - want[25]) <= 1e-12 * max(1.0, abs(want[25]))
+
+
+def test_permutation_cycles_open_worm_is_an_error(pgb, small):
+    d = small
+    cfg = pgb.worldlines.open_worm(d["cfg"], head=(3, 2), tail=(9, 2))
+    a = pgb.Action(d["L"], d["m"], d["n"], d["tau"], d["lam"])
+    a.load(cfg)
+    with pytest.raises(pgb.PgbError):
+        a.permutation_cycles()

@@ -207,3 +207,33 @@ def test_golden_fixtures_reproduce(oracle_lib):
     for key, val in want.items():
         assert np.allclose(np.asarray(got[key], dtype=float), np.asarray(val, dtype=float),
                            rtol=1e-13, atol=1e-13), key
+
+
+def test_permutation_cycles_and_winding_of_constructed_paths(oracle_lib):
+    """PermutationCycleEstimator on paths with known exchange cycles, and the
+    winding sums of closed paths (zero for the identity permutation)."""
+    from pimc_gb300 import worldlines as wl
+    n, m, L, lam, tau = 10, 8, 7.5, 6.0596, 0.02
+    cfg = _cfg(n, m, L, lam, tau, 3)
+    o = oracle_lib.Oracle(L, m, n, tau, lam)
+    o.load(cfg)
+    pc = o.permutation_cycles()
+    assert pc[0] == pytest.approx(1.0) and not pc[1:].any()
+    sf = o.superfluid()
+    assert abs(sf[0]) < 1e-20 and sf[14] == 1.0 and sf.sum() == pytest.approx(1.0 + sf[25] + sf[0] + sf[1:4].sum())
+    o.load(wl.permute(cfg, [(0, 1), (2, 3, 4)]))
+    pc = o.permutation_cycles()
+    # five 1-cycles, one 2-cycle, one 3-cycle: weights cycleNum * count / N
+    assert pc[0] == pytest.approx(5 / n) and pc[1] == pytest.approx(2 / n) and pc[2] == pytest.approx(3 / n)
+    assert pc.sum() == pytest.approx(1.0)
+
+
+def test_pair_correlation_slice_sum(oracle_lib):
+    """g(r) from all slices is the count-weighted mean of the single-slice
+    histograms (same bins, same norm)."""
+    n, m, L, lam, tau = 12, 6, 8.0, 6.0596, 0.02
+    o = oracle_lib.Oracle(L, m, n, tau, lam)
+    o.load(_cfg(n, m, L, lam, tau, 5))
+    g_all = o.pair_correlation()
+    g_s = np.array([o.pair_correlation(s) for s in range(m)])
+    assert np.allclose(g_all, g_s.mean(axis=0), rtol=1e-12, atol=1e-12)
