@@ -248,6 +248,13 @@ int pgb_walkers_get_positions(pgb_walkers* w, int walker, double* pos);
  * stream order.  The host buffer must stay unchanged until the next
  * synchronizing call (pgb_walkers_sync, pgb_walkers_stats). */
 int pgb_walkers_set_all_positions(pgb_walkers* w, const double* pos);
+/* every walker's positions into one host buffer (the layout of
+ * pgb_walkers_set_all_positions; the device FP32 values, exact in FP64) */
+int pgb_walkers_get_all_positions(pgb_walkers* w, double* pos);
+/* sweeps made per walker: with the positions, all a walker's chain needs to
+ * resume exactly (its draws are indexed by walker, sweep and move) */
+int pgb_walkers_get_sweeps(pgb_walkers* w, unsigned long long* sweeps);
+int pgb_walkers_set_sweeps(pgb_walkers* w, const unsigned long long* sweeps);
 /* bytes of the host buffer pgb_walkers_set_all_positions reads */
 size_t pgb_walkers_state_bytes(pgb_walkers* w);
 /* Run `sweeps` MC steps for every walker (numUpdates moves per step,
@@ -362,6 +369,11 @@ typedef struct {
 
 /* Seed the context's MT19937 stream (MTRand(seed), MersenneTwister.h:170-206) */
 int pgb_plain_seed(pgb_ctx* ctx, uint32_t seed);
+/* The stream's state in MTRand::save layout (MersenneTwister.h:125-126): 624
+ * state words then `left`; the state file's generator line
+ * (pimc.cpp:966-971).  Setting it resumes the stream exactly. */
+int pgb_plain_get_rng(pgb_ctx* ctx, uint32_t out625[625]);
+int pgb_plain_set_rng(pgb_ctx* ctx, const uint32_t in625[625]);
 /* Run nsteps PathIntegralMonteCarlo::step() loops (pimc.cpp:724-741) of
  * centre-of-mass + diagonal moves on the loaded closed path, continuing the
  * context's MT19937 stream.  trace (optional) receives (move, accepted) int32

@@ -25,7 +25,10 @@
 #include "pimc_gb300.h"
 
 #include <array>
+#include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -109,6 +112,10 @@ class Context {
   uint64_t epoch() const { return epoch_; }
   void touch() { ++epoch_; }
   void check(int rc) const { pgb::check(rc, h_); }
+  /* MTRand::save / load (MersenneTwister.h) of the plain form's generator:
+   * 624 state words then `left`, the state file's last line */
+  void saveRandom(uint32_t out[625]) const { check(pgb_plain_get_rng(h_, out)); }
+  void loadRandom(const uint32_t in[625]) { check(pgb_plain_set_rng(h_, in)); }
 
  private:
   pgb_ctx* h_ = nullptr;
@@ -391,13 +398,14 @@ class LocalAction {
 class EstimatorBase {
  public:
   EstimatorBase(Context& ctx, int ncols, int frequency = 1)
-      : ctx_(&ctx), est_(ncols, 0.0), freq_(frequency < 1 ? 1 : frequency) {}
+      : ctx_(&ctx), est_(ncols, 0.0), norm_(ncols, 1.0), freq_(frequency < 1 ? 1 : frequency) {}
   virtual ~EstimatorBase() = default;
   virtual std::string getName() const { return "base"; }
   void sample() {
     if (numSampled_++ % freq_ == 0) {
       accumulate();
       ++numAccumulated_;
+      ++totNumAccumulated_;
     }
   }
   void reset() {
@@ -409,11 +417,34 @@ class EstimatorBase {
     return numAccumulated_ ? est_.at(i) / (double)numAccumulated_ : 0.0;
   }
   const std::vector<double>& sums() const { return est_; }
+  long long getNumSampled() const { return numSampled_; }
+  long long getTotNumAccumulated() const { return totNumAccumulated_; }
+  /* EstimatorBase::restart (estimator.cpp:333-337) */
+  void restart(long long numSampled, long long totNumAccumulated) {
+    numSampled_ = numSampled;
+    totNumAccumulated_ = totNumAccumulated;
+    reset();
+  }
+  /* EstimatorBase::output (estimator.cpp:348-363): the bin average
+   * estimator * norm / numAccumulated as "%16.8E" columns, then reset */
+  void output(std::ostream& os, bool endLine = true) {
+    char buf[32];
+    for (size_t n = 0; n < est_.size(); ++n) {
+      const double v = numAccumulated_ ? est_[n] * (norm_[n] / (1.0 * numAccumulated_)) : 0.0;
+      std::snprintf(buf, sizeof buf, "%16.8E", v);
+      os << buf;
+    }
+    if (endLine) os << "\n";
+    reset();
+  }
+  const std::vector<double>& norm() const { return norm_; }
 
  protected:
   virtual void accumulate() = 0;
   Context* ctx_;
   std::vector<double> est_;
+  std::vector<double> norm_;
+  long long totNumAccumulated_ = 0;
 
  private:
   int freq_;
@@ -452,6 +483,77 @@ class VirialEnergyEstimator : public EstimatorBase {
 
  private:
   bool quirk_;
+};
+
+/* PairCorrelationEstimator (estimator.cpp:3181-3246): the separation
+ * histogram of all slices, per sample lnorm * hist / sum(hist), lnorm =
+ * (N-1)/N; norm(n) = V (3 / 2 pi) / 2 / dV(n) for the periodic prism */
+class PairCorrelationEstimator : public EstimatorBase {
+ public:
+  /* numParticles: Path::getTrueNumParticles of the loaded path (active
+   * beads / M); by default every worldline of the array is active */
+  PairCorrelationEstimator(Context& ctx, int frequency = 1, int numParticles = -1)
+      : EstimatorBase(ctx, 50, frequency),
+        N_(numParticles < 0 ? ctx.params().num_ptcl_ext : numParticles) {
+    const pgb_params& p = ctx.params();
+    const double dR = 0.5 * std::sqrt(3.0) * p.side[2] / 50.0;
+    for (int n = 0; n < 50; ++n) {
+      const double dV = std::pow((n + 1) * dR, 3) - std::pow(n * dR, 3);
+      norm_[n] = 0.5 * (3.0 / (2.0 * 3.14159265358979323846)) * p.side[0] * p.side[1] * p.side[2] / dV;
+    }
+  }
+  std::string getName() const override { return "pair correlation function"; }
+  void setNumParticles(int n) { N_ = n; }
+
+ protected:
+  void accumulate() override {
+    double h[50], tot = 0.0;
+    ctx_->check(pgb_pair_correlation(ctx_->get(), -1, h));
+    for (double x : h) tot += x;
+    const int N = N_;
+    if (N > 1 && tot > 0.0) {
+      const double lnorm = 1.0 * (N - 1) / (1.0 * N);
+      for (int n = 0; n < 50; ++n) est_[n] += lnorm * (h[n] / tot);
+    }
+  }
+
+ private:
+  int N_;
+};
+
+/* SuperfluidFractionEstimator (estimator.cpp:1963-2074): W^2/N, W_x^2,
+ * W_y^2, W_z^2, P(-10..10), Az^2/I with norms T/(2*3*lambda) and
+ * T M/(2 lambda) on the first and last columns */
+class SuperfluidFractionEstimator : public EstimatorBase {
+ public:
+  SuperfluidFractionEstimator(Context& ctx, double temperature, int frequency = 1)
+      : EstimatorBase(ctx, 26, frequency) {
+    const pgb_params& p = ctx.params();
+    norm_[0] = temperature / (2.0 * 3.0 * p.lambda);
+    norm_[25] = 0.5 * temperature * p.num_slices / p.lambda;
+  }
+  std::string getName() const override { return "superfluid fraction"; }
+
+ protected:
+  void accumulate() override {
+    double v[26];
+    ctx_->check(pgb_superfluid(ctx_->get(), v));
+    for (int i = 0; i < 26; ++i) est_[i] += v[i];
+  }
+};
+
+/* PermutationCycleEstimator (estimator.cpp:2700-2781): 40 cycle lengths */
+class PermutationCycleEstimator : public EstimatorBase {
+ public:
+  explicit PermutationCycleEstimator(Context& ctx, int frequency = 1) : EstimatorBase(ctx, 40, frequency) {}
+  std::string getName() const override { return "permutation cycle"; }
+
+ protected:
+  void accumulate() override {
+    double v[40];
+    ctx_->check(pgb_permutation_cycles(ctx_->get(), v));
+    for (int i = 0; i < 40; ++i) est_[i] += v[i];
+  }
 };
 
 /* EstimatorBase::getQVectors (estimator.cpp:439-570) */

@@ -23,6 +23,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <chrono>
+#include <iomanip>
+#include <iostream>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -1338,6 +1340,17 @@ uint32_t orc_mt_randint_n(orc_mt* m, uint32_t n) { return m->m.randInt(n); }
 double orc_mt_rand(orc_mt* m) { return m->m.rand(); }
 double orc_mt_randexc(orc_mt* m) { return m->m.randExc(); }
 double orc_mt_randnorm(orc_mt* m, double mean, double sd) { return m->m.randNorm(mean, sd); }
+// MTRand::save / load (MersenneTwister.h): the 624 words, then `left`; the
+// next word read is state[N - left]
+void orc_mt_save(orc_mt* m, uint32_t* out625) {
+    for (int i = 0; i < MT::N; ++i) out625[i] = m->m.st[i];
+    out625[MT::N] = (uint32_t)m->m.left;
+}
+void orc_mt_load(orc_mt* m, const uint32_t* in625) {
+    for (int i = 0; i < MT::N; ++i) m->m.st[i] = in625[i];
+    m->m.left = (int)in625[MT::N];
+    m->m.pos = MT::N - m->m.left;
+}
 
 int orc_run_steps(orc_sys* h, orc_mt* mt, const orc_move_params* mp, int nsteps,
                   int32_t* trace, int trace_cap, double* energies, orc_move_stats* stats) {
@@ -1510,3 +1523,56 @@ void orc_permutation_cycles(orc_sys* h, double* out40) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// state-file text through std::ostream, the formatting the reference uses
+// ---------------------------------------------------------------------------
+namespace {
+template <class Cell>
+void stream_array2(std::ostream& os, int rows, int cols, Cell cell) {
+    os << "(" << 0 << "," << rows - 1 << ") x (" << 0 << "," << cols - 1 << ")\n";
+    os << "[ ";
+    for (int i = 0; i < rows; ++i) {
+        for (int j = 0; j < cols; ++j) { cell(os, i, j); os << " "; }
+        if (i < rows - 1) os << "\n  ";
+    }
+    os << "]" << std::endl;
+}
+}  // namespace
+
+extern "C" long orc_format_state(const double* pos, const int32_t* next, const int32_t* prev,
+                                 const uint8_t* on, int M, int Ne, const long long* counts,
+                                 int ncounts, const uint32_t* rng625, char* out, long cap) {
+    std::ostringstream os;
+    os << Ne << std::endl;
+    char line[64];
+    for (int k = 0; k < ncounts; ++k) {
+        std::snprintf(line, sizeof line, "%16lld\t%16lld\n", counts[2 * k], counts[2 * k + 1]);
+        os << line;
+    }
+    os << std::setprecision(16);
+    stream_array2(os, M, Ne, [&](std::ostream& o, int i, int j) {
+        const double* r = pos + ((size_t)i * Ne + j) * 3;
+        o << "(" << r[0] << "," << r[1] << "," << r[2] << ")";
+    });
+    os << std::endl;
+    stream_array2(os, M, Ne, [&](std::ostream& o, int i, int j) {
+        const int32_t* l = next + ((size_t)i * Ne + j) * 2;
+        o << "(" << l[0] << "," << l[1] << ")";
+    });
+    os << std::endl;
+    stream_array2(os, M, Ne, [&](std::ostream& o, int i, int j) {
+        const int32_t* l = prev + ((size_t)i * Ne + j) * 2;
+        o << "(" << l[0] << "," << l[1] << ")";
+    });
+    os << std::endl;
+    stream_array2(os, M, Ne, [&](std::ostream& o, int i, int j) {
+        o << (unsigned int)on[(size_t)i * Ne + j];
+    });
+    os << std::endl;
+    for (int i = 0; i < 625; ++i) os << rng625[i] << " ";
+    os << std::endl;
+    const std::string s = os.str();
+    if (out && cap > (long)s.size()) { std::memcpy(out, s.data(), s.size()); out[s.size()] = 0; }
+    return (long)s.size();
+}

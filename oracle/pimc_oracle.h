@@ -104,6 +104,15 @@ void orc_pair_correlation(orc_sys* s, int slice, double* out50);
 void orc_superfluid(orc_sys* s, double* out26);
 /* one PermutationCycleEstimator increment (40 columns) */
 void orc_permutation_cycles(orc_sys* s, double* out40);
+/* The state-file text of PathIntegralMonteCarlo::saveState's text branch
+ * (pimc.cpp:923-1000) written with C++ iostreams as the reference does:
+ * counts as "%16d\t%16d" lines (ncounts pairs, the first being the totals),
+ * then beads at setprecision(16), nextLink, prevLink, worm beads in the
+ * DynamicArray stream format (common.h:245-274) and 625 generator words.
+ * Returns the text length; the text is copied to out when cap allows. */
+long orc_format_state(const double* pos, const int32_t* next, const int32_t* prev,
+                      const uint8_t* on, int M, int Ne, const long long* counts, int ncounts,
+                      const uint32_t* rng625, char* out, long cap);
 /* S(q) pairwise CPU form, per-sample value already normalised by 1/(N M) */
 void orc_ssf_pairwise(orc_sys* s, const double* q, int nq, double* out);
 /* S(q) by rho_q in FP64 */
@@ -126,6 +135,8 @@ uint32_t orc_mt_randint_n(orc_mt* m, uint32_t n);
 double   orc_mt_rand(orc_mt* m);
 double   orc_mt_randexc(orc_mt* m);
 double   orc_mt_randnorm(orc_mt* m, double mean, double sd);
+void     orc_mt_save(orc_mt* m, uint32_t* out625);          /* MTRand::save layout */
+void     orc_mt_load(orc_mt* m, const uint32_t* in625);
 
 /* ---- diagonal moves + driver (src/move.cpp, src/pimc.cpp) ---- */
 typedef struct {

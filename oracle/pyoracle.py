@@ -96,6 +96,9 @@ def load():
         "orc_pair_correlation": (None, [_VP, C.c_int, _DP]),
         "orc_superfluid": (None, [_VP, _DP]),
         "orc_permutation_cycles": (None, [_VP, _DP]),
+        "orc_format_state": (C.c_long, [_DP, _IP, _IP, C.POINTER(C.c_uint8), C.c_int, C.c_int,
+                                        C.POINTER(C.c_longlong), C.c_int, C.POINTER(C.c_uint32),
+                                        C.c_char_p, C.c_long]),
         "orc_mt_create": (_VP, [C.c_uint32]),
         "orc_mt_destroy": (None, [_VP]),
         "orc_mt_randint": (C.c_uint32, [_VP]),
@@ -103,6 +106,8 @@ def load():
         "orc_mt_rand": (C.c_double, [_VP]),
         "orc_mt_randexc": (C.c_double, [_VP]),
         "orc_mt_randnorm": (C.c_double, [_VP, C.c_double, C.c_double]),
+        "orc_mt_save": (None, [_VP, C.POINTER(C.c_uint32)]),
+        "orc_mt_load": (None, [_VP, C.POINTER(C.c_uint32)]),
         "orc_run_steps": (C.c_int, [_VP, _VP, C.POINTER(OrcMoveParams), C.c_int, _IP, C.c_int,
                                     _DP, C.POINTER(OrcMoveStats)]),
         "orc_walkers_cpu": (C.c_double, [C.c_int, _IP, _IP, _DP, _DP, C.POINTER(C.c_uint32),
@@ -346,6 +351,34 @@ class MT:
 
     def randnorm(self, mean=0.0, sd=1.0):
         return self.lib.orc_mt_randnorm(self.h, mean, sd)
+
+    def save(self):
+        out = np.zeros(625, dtype=np.uint32)
+        self.lib.orc_mt_save(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32)))
+        return out
+
+    def load(self, words):
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        self.lib.orc_mt_load(self.h, w.ctypes.data_as(C.POINTER(C.c_uint32)))
+
+
+def format_state(cfg, rng_words, counts):
+    """The state text as the reference's C++ streams write it."""
+    lib = load()
+    pos = np.ascontiguousarray(cfg["pos"], dtype=np.float64)
+    nxt = np.ascontiguousarray(cfg["next"], dtype=np.int32)
+    prv = np.ascontiguousarray(cfg["prev"], dtype=np.int32)
+    on = np.ascontiguousarray(cfg["on"], dtype=np.uint8)
+    m, ne = on.shape
+    cnt = np.ascontiguousarray(counts, dtype=np.int64).reshape(-1, 2)
+    w = np.ascontiguousarray(rng_words, dtype=np.uint32)
+    args = (_d(pos), _i(nxt), _i(prv), on.ctypes.data_as(C.POINTER(C.c_uint8)), m, ne,
+            cnt.ctypes.data_as(C.POINTER(C.c_longlong)), len(cnt),
+            w.ctypes.data_as(C.POINTER(C.c_uint32)))
+    n = lib.orc_format_state(*args, None, 0)
+    buf = C.create_string_buffer(n + 1)
+    lib.orc_format_state(*args, buf, n + 1)
+    return buf.value.decode()
 
 
 def walkers_cpu(n, m, temperature, side, seeds, tau, lam, nsteps, threads, nequil=0):

@@ -238,6 +238,18 @@ class Action:
     def plain_seed(self, seed):
         self._chk(self.lib.pgb_plain_seed(self.h, seed))
 
+    def rng_state(self):
+        """The plain form's MT19937 state, MTRand::save layout (625 words)."""
+        out = np.zeros(625, dtype=np.uint32)
+        self._chk(self.lib.pgb_plain_get_rng(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return out
+
+    def set_rng_state(self, words):
+        words = np.ascontiguousarray(words, dtype=np.uint32)
+        if words.shape != (625,):
+            raise ValueError("an MT19937 state has 625 words")
+        self._chk(self.lib.pgb_plain_set_rng(self.h, words.ctypes.data_as(C.POINTER(C.c_uint32))))
+
     def plain_run(self, nsteps, mbar, temperature, diagonal_move=1, var_updates=1, max_wind=1,
                   p_com=0.05, num_updates=0, trace_cap=0):
         mp = _lib.PgbMoveParams(mbar, diagonal_move, var_updates, max_wind, temperature, p_com,
@@ -305,6 +317,26 @@ class Walkers:
         out = np.zeros((int(self.m[w]), int(self.n[w]), 3))
         self._chk(self.lib.pgb_walkers_get_positions(self.h, w, dptr(out)))
         return out
+
+    def all_positions(self):
+        """Every walker's positions, concatenated (walker w's [M_w][N_w][3])."""
+        out = np.zeros(int(self.lib.pgb_walkers_state_bytes(self.h)) // 8)
+        self._chk(self.lib.pgb_walkers_get_all_positions(self.h, dptr(out)))
+        return out
+
+    def set_all_positions(self, pos):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        self._keep = pos
+        self._chk(self.lib.pgb_walkers_set_all_positions(self.h, dptr(pos)))
+
+    def sweeps_done(self):
+        out = np.zeros(self.W, dtype=np.uint64)
+        self._chk(self.lib.pgb_walkers_get_sweeps(self.h, out.ctypes.data_as(C.POINTER(C.c_ulonglong))))
+        return out
+
+    def set_sweeps_done(self, sweeps):
+        s = np.ascontiguousarray(sweeps, dtype=np.uint64)
+        self._chk(self.lib.pgb_walkers_set_sweeps(self.h, s.ctypes.data_as(C.POINTER(C.c_ulonglong))))
 
     def run(self, sweeps, measure=1, sync=True):
         self._chk(self.lib.pgb_walkers_run_async(self.h, sweeps, measure))

@@ -113,6 +113,11 @@ _SIGS = {
     "pgb_isf_device_async": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP]),
     "pgb_update_positions": (C.c_int, [_VP, _DP]),
     "pgb_pair_correlation": (C.c_int, [_VP, C.c_int, _DP]),
+    "pgb_plain_get_rng": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
+    "pgb_plain_set_rng": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
+    "pgb_walkers_get_all_positions": (C.c_int, [_VP, _DP]),
+    "pgb_walkers_get_sweeps": (C.c_int, [_VP, C.POINTER(C.c_ulonglong)]),
+    "pgb_walkers_set_sweeps": (C.c_int, [_VP, C.POINTER(C.c_ulonglong)]),
     "pgb_superfluid": (C.c_int, [_VP, _DP]),
     "pgb_permutation_cycles": (C.c_int, [_VP, _DP]),
     "pgb_ssf_device_async": (C.c_int, [_VP, _VP, C.c_int, _VP]),

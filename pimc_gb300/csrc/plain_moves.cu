@@ -329,6 +329,28 @@ int pgb_plain_seed(pgb_ctx* h, uint32_t seed) {
     return PGB_OK;
 }
 
+int pgb_plain_get_rng(pgb_ctx* h, uint32_t* out625) {
+    if (!h || !out625) return PGB_EINVAL;
+    Ctx& c = h->c;
+    if (!c.mt_seeded) return c.fail(PGB_ESTATE, "plain_get_rng: the generator was never seeded");
+    // MTRand::save (MersenneTwister.h): the 624 state words, then `left`
+    for (int i = 0; i < 624; ++i) out625[i] = c.mt_state[i];
+    out625[624] = (uint32_t)c.mt_left;
+    return PGB_OK;
+}
+
+int pgb_plain_set_rng(pgb_ctx* h, const uint32_t* in625) {
+    if (!h || !in625) return PGB_EINVAL;
+    Ctx& c = h->c;
+    if (in625[624] > 624u) return c.fail(PGB_EINVAL, "plain_set_rng: `left` must be 0..624");
+    // MTRand::load: pNext = &state[N - left]
+    c.mt_state.assign(in625, in625 + 624);
+    c.mt_left = (int)in625[624];
+    c.mt_pos = 624 - c.mt_left;
+    c.mt_seeded = true;
+    return PGB_OK;
+}
+
 int pgb_plain_run(pgb_ctx* h, const pgb_move_params* mp, int nsteps, int32_t* trace, int trace_cap,
                   int* trace_len, double* energies, pgb_move_stats* stats) {
     if (!h || !mp || nsteps < 0) return PGB_EINVAL;

@@ -2540,6 +2540,35 @@ __global__ void k_walkers_from64(const double* __restrict__ src, float4* __restr
 
 size_t pgb_walkers_state_bytes(pgb_walkers* h) { return h ? (size_t)h->total_beads * 3 * sizeof(double) : 0; }
 
+int pgb_walkers_get_all_positions(pgb_walkers* h, double* pos) {
+    if (!h || !pos) return PGB_EINVAL;
+    std::vector<float4> tmp((size_t)h->total_beads);
+    cudaError_t e = cudaMemcpyAsync(tmp.data(), h->d_pos, tmp.size() * sizeof(float4),
+                                    cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "walkers get all positions");
+    for (size_t i = 0; i < tmp.size(); ++i) { pos[3*i] = tmp[i].x; pos[3*i+1] = tmp[i].y; pos[3*i+2] = tmp[i].z; }
+    return PGB_OK;
+}
+
+int pgb_walkers_get_sweeps(pgb_walkers* h, unsigned long long* sweeps) {
+    if (!h || !sweeps) return PGB_EINVAL;
+    cudaError_t e = cudaMemcpyAsync(sweeps, h->d_ctr, h->W * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "walkers get sweeps");
+    return PGB_OK;
+}
+
+int pgb_walkers_set_sweeps(pgb_walkers* h, const unsigned long long* sweeps) {
+    if (!h || !sweeps) return PGB_EINVAL;
+    cudaError_t e = cudaMemcpyAsync(h->d_ctr, sweeps, h->W * sizeof(unsigned long long),
+                                    cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "walkers set sweeps");
+    return PGB_OK;
+}
+
 int pgb_walkers_set_all_positions(pgb_walkers* h, const double* pos) {
     if (!h || !pos) return PGB_EINVAL;
     size_t bytes = (size_t)h->total_beads * 3 * sizeof(double);

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <random>
+#include <sstream>
 #include <vector>
 
 static int g_fail = 0;
@@ -26,6 +27,25 @@ static void cmp(const char* what, double got, double want, double tol = 1e-12) {
   if (err > g_worst) g_worst = err;
   if (!(err <= tol)) {
     std::printf("MISMATCH %s: got %.17g want %.17g (rel %.3g)\n", what, got, want, err);
+    ++g_fail;
+  }
+}
+
+static void check_rng(pgb::Context& ctx) {
+  ctx.check(pgb_plain_seed(ctx.get(), 4242u));
+  uint32_t got[625], want[625];
+  ctx.saveRandom(got);
+  orc_mt* mt = orc_mt_create(4242u);
+  for (int k = 0; k < 1000; ++k) orc_mt_randint(mt);
+  orc_mt_save(mt, want);
+  ctx.loadRandom(want);
+  uint32_t back[625];
+  ctx.saveRandom(back);
+  int bad = got[624] != 624u;
+  for (int i = 0; i < 625; ++i) bad += back[i] != want[i];
+  orc_mt_destroy(mt);
+  if (bad) {
+    std::printf("MISMATCH generator state save/load (%d words)\n", bad);
     ++g_fail;
   }
 }
@@ -171,6 +191,43 @@ int main(int argc, char** argv) {
   pgb::StaticStructureFactorEstimator ssf(ctx, q);
   ssf.sample();
   for (size_t k = 0; k < q.size(); ++k) cmp("S(q)", ssf.getEstimator((int)k), want[k], 1e-10);
+
+  // adjacent path-wide estimators, their norms and the bin row format
+  pgb::PairCorrelationEstimator pcf(ctx);
+  pgb::SuperfluidFractionEstimator sfe(ctx, 1.0 / (M * tau));
+  pgb::PermutationCycleEstimator pce(ctx);
+  pcf.sample();
+  sfe.sample();
+  pce.sample();
+  double h50[50], s26[26], c40[40], htot = 0.0;
+  orc_pair_correlation(o, -1, h50);
+  orc_superfluid(o, s26);
+  orc_permutation_cycles(o, c40);
+  for (double x : h50) htot += x;
+  for (int n = 0; n < 50; ++n)
+    cmp("g(r) bin", pcf.getEstimator(n), (N - 1.0) / N * h50[n] / htot, 1e-14);
+  for (int i = 0; i < 26; ++i) cmp("superfluid column", sfe.getEstimator(i), s26[i]);
+  for (int i = 0; i < 40; ++i) cmp("cycle column", pce.getEstimator(i), c40[i], 0.0);
+  {
+    // the first column is W^2/N times T/(6 lambda); W of closed paths is
+    // zero up to rounding, so take the library's own value for the format
+    const double w0 = sfe.getEstimator(0), a25 = sfe.getEstimator(25);
+    std::ostringstream row;
+    sfe.output(row);
+    char want0[40];
+    std::snprintf(want0, sizeof want0, "%16.8E", w0 * ((1.0 / (M * tau)) / (6.0 * lam)));
+    cmp("Area_rho_s column", sfe.norm()[25], 0.5 * (1.0 / (M * tau)) * M / lam, 1e-15);
+    (void)a25;
+    const std::string r = row.str();
+    if (r.size() != 26 * 16 + 1 || r.compare(0, 16, want0) != 0 || sfe.numAccumulated() != 0 ||
+        sfe.getTotNumAccumulated() != 1) {
+      std::printf("MISMATCH superfluid row '%s' (want first column '%s')\n", r.c_str(), want0);
+      ++g_fail;
+    }
+  }
+
+  // the plain form's generator state is MTRand::save's image
+  check_rng(ctx);
 
   // an out-of-range slice is an error, not a read past the arrays
   bool threw = false;
