@@ -63,7 +63,7 @@ def parse():
                     help="walker schedule code (0: autotune)")
     ap.add_argument("--no-baseline", action="store_true")
     ap.add_argument("--workload", default="walkers",
-                    choices=["walkers", "serving", "isf", "pair", "plain"])
+                    choices=["walkers", "serving", "isf", "pair", "plain", "gp"])
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     return ap.parse_args()
 
@@ -614,6 +614,104 @@ def run_plain(args, pgb):
     print(json.dumps(out))
 
 
+# ---------------------------------------------------------------------------
+# Gaussian-process external potential leg: one call evaluates the potential
+# at every bead of a path (64 particles x 64 slices) against 16384 training
+# points, the largest case of the reference's GP action sweep.
+# ---------------------------------------------------------------------------
+GP_FLOP = 38     # FP32 pipe instructions per kernel evaluation of k_gp32 (nu = 5/2)
+GP_SFU = 2       # exp2 and rsqrt per evaluation
+
+
+def run_gp(args, pgb):
+    import torch
+    from pimc_gb300 import worldlines as wl
+    from pimc_gb300.gp import GaussianProcess
+    npts, nptcl, nsl = 16384, 64, 64
+    w = wl.workload_gp(points=npts, num_ptcl=nptcl, num_slices=nsl, seed=0)
+    pos = np.ascontiguousarray(w["pos"])
+    count = len(pos)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    clk = Clocks()
+    res = {}
+    for prec, tag in ((pgb.PGB_FP64, "fp64"), (pgb.PGB_MIXED, "mixed")):
+        g = GaussianProcess(w["training"], precision=prec, **w["params"])
+        d_pos = torch.from_numpy(pos).cuda()
+        d_out = torch.empty(count, dtype=torch.float64, device="cuda")
+        stream = torch.cuda.ExternalStream(g.stream())
+        for _ in range(max(3, args.warmup)):
+            g._chk(g.lib.pgb_gp_eval_device_async(g.h, d_pos.data_ptr(), d_out.data_ptr(), count))
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                g._chk(g.lib.pgb_gp_eval_device_async(g.h, d_pos.data_ptr(), d_out.data_ptr(), count))
+                e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        t_dev = sum(ts) / len(ts)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            g(pos)
+        t_e2e = (time.perf_counter() - t0) / args.steps
+        res[tag] = {"call_ms": 1e3 * t_dev, "evaluations_per_s": count * npts / t_dev,
+                    "points_per_s": count / t_dev, "e2e_points_per_s": count / t_e2e,
+                    "e2e_call_ms": 1e3 * t_e2e, "_t": t_dev}
+        g.close()
+    clocks = clk.stop()
+    mx = res["mixed"]
+    t = mx.pop("_t")
+    res["fp64"].pop("_t")
+    peak = measured_fp32_peak()
+    ev = count * npts
+    flops = ev * GP_FLOP / t / 1e12
+    sfu = ev * GP_SFU / t
+    sfu_pk = sfu_peak(clocks.get("sm_mhz"))
+    f32, fs = flops / peak, sfu / sfu_pk
+    roof = {"bound": "fp32" if f32 >= fs else "sfu", "achieved": flops, "peak": peak,
+            "unit": "TFLOP/s", "frac": max(f32, fs), "fp32_frac": f32,
+            "sfu": {"achieved_gops": sfu / 1e9, "peak_gops": sfu_pk / 1e9, "frac": fs},
+            "traffic": None, "kernel": "k_gp32",
+            "note": "achieved = kernel evaluations x %d FP32 instructions / kernel time; FP32 peak "
+                    "= measured cuBLAS SGEMM (no TF32); SFU = %d ops per evaluation against "
+                    "nominal %d/clk/SM x SMs x median SM clock" % (GP_FLOP, GP_SFU, SFU_PER_SM_CLK)}
+    out = {"metric": "GP potential points/s (mixed, 16384 training points)",
+           "value": mx["points_per_s"], "unit": "points/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": max(3, args.warmup), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
+           "config": {"workload": "Gaussian-process external potential, Matern nu=5/2, 16384 "
+                                  "training points, %d positions per call (%d particles x %d "
+                                  "slices), periodic separations" % (count, nptcl, nsl),
+                      "l2": "flushed between timed calls", "results": res},
+           "e2e": {"value": mx["e2e_points_per_s"], "unit": "points/s",
+                   "h2d_bytes_per_step": count * 24, "d2h_bytes_per_step": count * 8},
+           "gpu_launches": args.steps, "roofline": roof, "clocks": clocks}
+    if not args.no_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        from concurrent.futures import ThreadPoolExecutor
+        threads = os.cpu_count() or 1
+        sample = pos
+        chunks = np.array_split(sample, threads)
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(threads) as ex:
+            want = np.concatenate(list(ex.map(
+                lambda c: pyoracle.gp_eval(w["training"], c, **w["params"]), chunks)))
+        dt = time.perf_counter() - t0
+        g = GaussianProcess(w["training"], precision=pgb.PGB_MIXED, **w["params"])
+        got = g(pos)
+        g.close()
+        out["config"]["mixed_max_abs_err_vs_fp64_oracle"] = float(np.max(np.abs(got - want)))
+        out["cpu_baseline"] = {"value": len(sample) / dt, "unit": "points/s", "cores": threads,
+                               "kind": "port", "sample": "%d positions against 16384 training "
+                               "points, FP64 oracle, %d threads, %.1f s" % (len(sample), threads, dt)}
+    print(json.dumps(out))
+
+
 def run_reference(args):
     rank, ws = dist_init()
     if rank != 0:
@@ -645,7 +743,7 @@ def main():
     if args.workload != "walkers":
         if rank == 0:
             {"serving": run_serving, "isf": run_isf, "pair": run_pair,
-             "plain": run_plain}[args.workload](args, pgb)
+             "plain": run_plain, "gp": run_gp}[args.workload](args, pgb)
         return
 
     w = workload(args.walkers, seed=rank)

@@ -155,6 +155,23 @@ int pgb_qvectors(const char* type, const char* input, const double side[3],
  * (estimator.cpp:3705-3737, 3824-3861), per-sample value already divided by
  * N M (the reference's norm 1/M applied), via rho_q. */
 int pgb_ssf(pgb_ctx* ctx, const double* q, int nq, double* out);
+/* Cylinder S(q): the beads inside x^2 + y^2 < maxR^2 only (include(),
+ * estimator.cpp:4309-4311).  out[k] = (1/M) sum_t sum_{i,j inside}
+ * cos(q_k . (r_j(t) - r_i(t))) -- what the cylinder GPU estimator's kernel
+ * (gpu_ssf_cyl, estimator_gpu.cu:169-285) is meant to sum, with its sum
+ * accumulated across the loop and its radius test the right way round -- and
+ * *num_inside0 = num1DParticles (estimator.cpp:4318-4327).  The CPU
+ * estimator's sample is out / num_inside0 per shell vector
+ * (estimator.cpp:5415-5458), the GPU estimator's out / N.  nq = 0 (q and
+ * out may be NULL) only counts. */
+int pgb_ssf_cylinder(pgb_ctx* ctx, const double* q, int nq, double maxR, double* out,
+                     int* num_inside0);
+/* EstimatorBase::getQVectors2 (estimator.cpp:762-824): the shell q-vectors
+ * of magnitudes 0, dq, 2dq, ... <= qmax; sphere = 0 is the "line" geometry
+ * (one vector along z per shell), 1 the octant grid.  shell[i] is the
+ * vector's shell index.  *count = total; at most cap are written. */
+int pgb_qvectors_shells(double dq, double qmax, int sphere, double* q, int* shell, int cap,
+                        int* count);
 /* F(q,tau): IntermediateScatteringFunctionEstimatorGpu::accumulate
  * (estimator.cpp:4063-4100, gpu_isf estimator_gpu.cu:67-165): layout
  * [q][M/2+1], value (1/(N M)) sum_{t,i,j} cos(q.(r_j(t+tau) - r_i(t))).
@@ -382,6 +399,41 @@ int pgb_plain_set_rng(pgb_ctx* ctx, const uint32_t in625[625]);
 int pgb_plain_run(pgb_ctx* ctx, const pgb_move_params* mp, int nsteps,
                   int32_t* trace, int trace_cap, int* trace_len,
                   double* energies, pgb_move_stats* stats);
+
+/* ---- Gaussian-process external potential ----------------------------------
+ * GaussianProcessPotential (include/potential.h:287-323, src/potential.cpp:
+ * 244-392) with the Matern kernel (include/gpkernel.h:48-72): the fields are
+ * the reference's gp parameter keys (kernel.maternNu, kernel.ell,
+ * data.normOffset, data.normScale, data.standardMean, data.standardStd,
+ * kernel.mean, kernel.sigma2) plus the container (sides, periodic flags),
+ * whose boundary conditions the CPU kernel applies to each separation.
+ * Training rows are x, y, z, (K^-1 Y): the first four doubles of each row of
+ * the reference's binary training file. */
+typedef struct pgb_gp pgb_gp;
+typedef struct {
+    double matern_nu;          /* 0.5, 1.5 or 2.5 */
+    double ell[3];
+    double norm_offset[3];
+    double norm_scale[3];
+    double standard_mean, standard_std;
+    double mean;               /* kernel.mean (mu) */
+    double sigma2;
+    double side[3];
+    int    periodic[3];
+    int    precision;          /* PGB_FP64: the CPU form bit for bit up to exp();
+                                  PGB_MIXED: FP32 kernel values, compensated sum */
+} pgb_gp_params;
+int pgb_gp_create(const pgb_gp_params* p, const double* training /* [n][4] */, int n,
+                  pgb_gp** out);
+int pgb_gp_destroy(pgb_gp* gp);
+const char* pgb_gp_last_error(const pgb_gp* gp);   /* gp may be NULL */
+void* pgb_gp_stream(pgb_gp* gp);
+/* GaussianProcessPotential::GP(const dVec*, double*, int), positions AoS */
+int pgb_gp_eval(pgb_gp* gp, const double* pos, double* values, int count);
+int pgb_gp_eval_device_async(pgb_gp* gp, const double* d_pos, double* d_values, int count);
+/* GPHeBenzenePotential::V(const dVec*, double*, int) (src/potential.cpp:
+ * 5610-5681): symmetry fold, hard core 10000 K, GP, long-range switch */
+int pgb_gp_benzene_v(pgb_gp* gp, const double* pos, double* values, int count);
 
 #ifdef __cplusplus
 }

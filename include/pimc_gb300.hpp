@@ -55,6 +55,12 @@ inline void check(int rc, const pgb_ctx* ctx) {
                         std::to_string(rc) + ")");
   }
 }
+/* the same with the message of another handle */
+inline void check(int rc, const pgb_ctx*, const char* msg) {
+  if (rc != PGB_OK)
+    throw Error(rc, std::string("pimc_gb300: ") + (msg ? msg : "error ") + " (code " +
+                        std::to_string(rc) + ")");
+}
 
 /* The LocalAction factors of Setup::action (src/setup.cpp:1216-1266):
  * primitive VFactor {1,1}, gradVFactor {0,0}, period 1;
@@ -392,6 +398,41 @@ class LocalAction {
   bool cached_ = false;
 };
 
+/* GaussianProcessPotential (include/potential.h:287-323) and the
+ * GPHeBenzenePotential external potential built on it
+ * (include/potential.h:2413-2450): GP(positions, values, count) and
+ * V(positions, values, count) over batches, on the device. */
+class GaussianProcessPotential {
+ public:
+  GaussianProcessPotential(const pgb_gp_params& p, const double* training, int n) {
+    const int rc = pgb_gp_create(&p, training, n, &h_);
+    pgb::check(rc, nullptr, pgb_gp_last_error(nullptr));
+  }
+  ~GaussianProcessPotential() {
+    if (h_) pgb_gp_destroy(h_);
+  }
+  GaussianProcessPotential(const GaussianProcessPotential&) = delete;
+  GaussianProcessPotential& operator=(const GaussianProcessPotential&) = delete;
+  double GP(const dVec& r) {
+    double v = 0.0;
+    GP(&r, &v, 1);
+    return v;
+  }
+  void GP(const dVec* positions, double* values, int count) {
+    const int rc = pgb_gp_eval(h_, count ? positions[0].data() : nullptr, values, count);
+    pgb::check(rc, nullptr, pgb_gp_last_error(h_));
+  }
+  /* GPHeBenzenePotential::V */
+  void benzeneV(const dVec* positions, double* values, int count) {
+    const int rc = pgb_gp_benzene_v(h_, count ? positions[0].data() : nullptr, values, count);
+    pgb::check(rc, nullptr, pgb_gp_last_error(h_));
+  }
+  pgb_gp* get() const { return h_; }
+
+ private:
+  pgb_gp* h_ = nullptr;
+};
+
 /* EstimatorBase (include/estimator.h:32-141): sample() accumulates every
  * `frequency` calls; getEstimator(i) is the running average
  * estimator(i) / numAccumulated that output() writes. */
@@ -402,7 +443,7 @@ class EstimatorBase {
   virtual ~EstimatorBase() = default;
   virtual std::string getName() const { return "base"; }
   void sample() {
-    if (numSampled_++ % freq_ == 0) {
+    if (numSampled_++ % freq_ == 0 && ready()) {
       accumulate();
       ++numAccumulated_;
       ++totNumAccumulated_;
@@ -441,6 +482,9 @@ class EstimatorBase {
 
  protected:
   virtual void accumulate() = 0;
+  /* whether this sample counts (the cylinder estimators skip samples with
+   * no particle inside their radius, estimator.cpp:5464-5471) */
+  virtual bool ready() { return true; }
   Context* ctx_;
   std::vector<double> est_;
   std::vector<double> norm_;
@@ -485,40 +529,20 @@ class VirialEnergyEstimator : public EstimatorBase {
   bool quirk_;
 };
 
-/* PairCorrelationEstimator (estimator.cpp:3181-3246): the separation
- * histogram of all slices, per sample lnorm * hist / sum(hist), lnorm =
- * (N-1)/N; norm(n) = V (3 / 2 pi) / 2 / dV(n) for the periodic prism */
+/* PairCorrelationEstimator (estimator.cpp:3181-3246): g(r) over 50 bins of
+ * 0.5 sqrt(3) L_z / 50 from the separation histogram of all slices; the
+ * library returns each sample with the estimator's norm applied */
 class PairCorrelationEstimator : public EstimatorBase {
  public:
-  /* numParticles: Path::getTrueNumParticles of the loaded path (active
-   * beads / M); by default every worldline of the array is active */
-  PairCorrelationEstimator(Context& ctx, int frequency = 1, int numParticles = -1)
-      : EstimatorBase(ctx, 50, frequency),
-        N_(numParticles < 0 ? ctx.params().num_ptcl_ext : numParticles) {
-    const pgb_params& p = ctx.params();
-    const double dR = 0.5 * std::sqrt(3.0) * p.side[2] / 50.0;
-    for (int n = 0; n < 50; ++n) {
-      const double dV = std::pow((n + 1) * dR, 3) - std::pow(n * dR, 3);
-      norm_[n] = 0.5 * (3.0 / (2.0 * 3.14159265358979323846)) * p.side[0] * p.side[1] * p.side[2] / dV;
-    }
-  }
+  explicit PairCorrelationEstimator(Context& ctx, int frequency = 1) : EstimatorBase(ctx, 50, frequency) {}
   std::string getName() const override { return "pair correlation function"; }
-  void setNumParticles(int n) { N_ = n; }
 
  protected:
   void accumulate() override {
-    double h[50], tot = 0.0;
-    ctx_->check(pgb_pair_correlation(ctx_->get(), -1, h));
-    for (double x : h) tot += x;
-    const int N = N_;
-    if (N > 1 && tot > 0.0) {
-      const double lnorm = 1.0 * (N - 1) / (1.0 * N);
-      for (int n = 0; n < 50; ++n) est_[n] += lnorm * (h[n] / tot);
-    }
+    double g[50];
+    ctx_->check(pgb_pair_correlation(ctx_->get(), -1, g));
+    for (int n = 0; n < 50; ++n) est_[n] += g[n];
   }
-
- private:
-  int N_;
 };
 
 /* SuperfluidFractionEstimator (estimator.cpp:1963-2074): W^2/N, W_x^2,
@@ -554,6 +578,91 @@ class PermutationCycleEstimator : public EstimatorBase {
     ctx_->check(pgb_permutation_cycles(ctx_->get(), v));
     for (int i = 0; i < 40; ++i) est_[i] += v[i];
   }
+};
+
+/* CylinderStaticStructureFactorEstimator (estimator.cpp:5363-5471): the
+ * "line" shells q = (0, 0, n 2 pi / L_z), |q| <= 4; per sample the included
+ * beads' sum / num1DParticles, norm 1/M per shell vector count; samples with
+ * no particle inside maxR are skipped */
+class CylinderStaticStructureFactorEstimator : public EstimatorBase {
+ public:
+  CylinderStaticStructureFactorEstimator(Context& ctx, double maxR, int frequency = 1)
+      : EstimatorBase(ctx, shellCount(ctx), frequency), maxR_(maxR) {
+    const double dq = 2.0 * 3.14159265358979323846 / ctx.params().side[2];
+    int n = 0;
+    check(pgb_qvectors_shells(dq, 4.0, 0, nullptr, nullptr, 0, &n), nullptr);
+    q_.resize((size_t)n);
+    shell_.resize((size_t)n);
+    if (n) check(pgb_qvectors_shells(dq, 4.0, 0, q_[0].data(), shell_.data(), n, &n), nullptr);
+    std::vector<int> per(est_.size(), 0);
+    for (int s : shell_) ++per[(size_t)s];
+    for (size_t k = 0; k < est_.size(); ++k)
+      norm_[k] = (1.0 / ctx.params().num_slices) / (per[k] > 0 ? per[k] : 1);
+    tmp_.resize(q_.size());
+  }
+  std::string getName() const override { return "cylinder static structure factor"; }
+
+ protected:
+  bool ready() override {
+    int n0 = 0;
+    ctx_->check(pgb_ssf_cylinder(ctx_->get(), nullptr, 0, maxR_, nullptr, &n0));
+    return n0 > 0;
+  }
+  void accumulate() override {
+    int n0 = 0;
+    ctx_->check(pgb_ssf_cylinder(ctx_->get(), q_[0].data(), (int)q_.size(), maxR_, tmp_.data(), &n0));
+    // the device value is already divided by M; the norm divides by M again
+    // in the reference's order, so undo it here
+    for (size_t i = 0; i < q_.size(); ++i)
+      est_[(size_t)shell_[i]] += tmp_[i] * ctx_->params().num_slices / n0;
+  }
+
+ private:
+  static int shellCount(const Context& ctx) {
+    const double dq = 2.0 * 3.14159265358979323846 / ctx.params().side[2];
+    int n = 0;
+    check(pgb_qvectors_shells(dq, 4.0, 0, nullptr, nullptr, 0, &n), nullptr);
+    std::vector<dVec> q((size_t)n);
+    std::vector<int> sh((size_t)n);
+    if (n) check(pgb_qvectors_shells(dq, 4.0, 0, q[0].data(), sh.data(), n, &n), nullptr);
+    return n ? sh.back() + 1 : 0;
+  }
+  double maxR_;
+  std::vector<dVec> q_;
+  std::vector<int> shell_;
+  std::vector<double> tmp_;
+};
+
+/* CylinderStaticStructureFactorGPUEstimator (estimator.cpp:5486-5613,
+ * gpu_ssf_cyl estimator_gpu.cu:169-285): user q-vectors, per sample the
+ * included beads' sum over ordered pairs / (N M); numParticles is
+ * Path::getTrueNumParticles (every worldline by default) */
+class CylinderStaticStructureFactorGPUEstimator : public EstimatorBase {
+ public:
+  CylinderStaticStructureFactorGPUEstimator(Context& ctx, std::vector<dVec> q, double maxR,
+                                            int frequency = 1, int numParticles = -1)
+      : EstimatorBase(ctx, (int)q.size(), frequency), q_(std::move(q)), maxR_(maxR),
+        N_(numParticles < 0 ? ctx.params().num_ptcl_ext : numParticles), tmp_(q_.size()) {}
+  std::string getName() const override { return "cylinder static structure factor gpu"; }
+
+ protected:
+  bool ready() override {
+    int n0 = 0;
+    ctx_->check(pgb_ssf_cylinder(ctx_->get(), nullptr, 0, maxR_, nullptr, &n0));
+    return n0 > 0;
+  }
+  void accumulate() override {
+    if (q_.empty()) return;
+    int n0 = 0;
+    ctx_->check(pgb_ssf_cylinder(ctx_->get(), q_[0].data(), (int)q_.size(), maxR_, tmp_.data(), &n0));
+    for (size_t i = 0; i < q_.size(); ++i) est_[i] += tmp_[i] / N_;
+  }
+
+ private:
+  std::vector<dVec> q_;
+  double maxR_;
+  int N_;
+  std::vector<double> tmp_;
 };
 
 /* EstimatorBase::getQVectors (estimator.cpp:439-570) */

@@ -1231,6 +1231,58 @@ void orc_ssf_pairwise(orc_sys* h, const double* q, int nq, double* out) {
     }
 }
 
+// CylinderStaticStructureFactorEstimator::accumulate (estimator.cpp:5415-5458)
+// with include() (4309-4311) and num1DParticles (4318-4327): per q the
+// sum over slices of 1 per included bead plus 2 cos(q . sep) per included
+// pair i < j, sep = Path::getSeparation.  Returned divided by M only (the
+// caller applies 1/num1D or 1/N); *n0 = num1DParticles.
+void orc_ssf_cylinder(orc_sys* h, const double* q, int nq, double maxR, double* out, int* n0) {
+    Sys* s = h->s;
+    auto include = [&](const dVec& r) { return r[0] * r[0] + r[1] * r[1] < maxR * maxR; };
+    int tot = 0;
+    for (int p = 0; p < s->nbs[0]; ++p)
+        if (include(s->P(0, p))) ++tot;
+    *n0 = tot;
+    for (int iq = 0; iq < nq; ++iq) {
+        dVec qv{q[3*iq], q[3*iq+1], q[3*iq+2]};
+        double sf = 0.0;
+        for (int t = 0; t < s->M; ++t)
+            for (int b1 = 0; b1 < s->nbs[t]; ++b1) {
+                if (!include(s->P(t, b1))) continue;
+                sf += 1.0;
+                for (int b2 = b1 + 1; b2 < s->nbs[t]; ++b2)
+                    if (include(s->P(t, b2))) sf += 2 * std::cos(dot(s->sep(t, b1, t, b2), qv));
+            }
+        out[iq] = sf * (1.0 / s->M);
+    }
+}
+
+// EstimatorBase::getQVectors2 (estimator.cpp:762-824)
+int orc_qvectors_shells(double dq, double qmax, int sphere, double* qv, int* shell, int cap) {
+    const double kEps = 1.0e-7;
+    int n = 0, ns = 0;
+    for (double cq = 0.0; cq <= qmax + kEps; cq += dq, ++ns) {
+        std::vector<dVec> v;
+        if (std::abs(cq) < kEps) v.push_back(dVec{0.0, 0.0, 0.0});
+        else {
+            v.push_back(dVec{0.0, 0.0, cq});
+            const int numTheta = 24;
+            const double dtheta = sphere ? 0.5 * M_PI / numTheta : M_PI;
+            for (double theta = dtheta; theta <= 0.5 * M_PI + kEps; theta += dtheta) {
+                const double dphi = dtheta / std::sin(theta);
+                for (double phi = 0.0; phi <= 0.5 * M_PI + kEps; phi += dphi)
+                    v.push_back(dVec{cq * std::sin(theta) * std::cos(phi),
+                                     cq * std::sin(theta) * std::sin(phi), cq * std::cos(theta)});
+            }
+        }
+        for (const dVec& x : v) {
+            if (n < cap) { qv[3*n] = x[0]; qv[3*n+1] = x[1]; qv[3*n+2] = x[2]; shell[n] = ns; }
+            ++n;
+        }
+    }
+    return n;
+}
+
 void orc_rhoq(orc_sys* h, const double* q, int nq, double* out) {
     Sys* s = h->s;
     for (int iq = 0; iq < nq; ++iq) {
@@ -1575,4 +1627,104 @@ extern "C" long orc_format_state(const double* pos, const int32_t* next, const i
     const std::string s = os.str();
     if (out && cap > (long)s.size()) { std::memcpy(out, s.data(), s.size()); out[s.size()] = 0; }
     return (long)s.size();
+}
+
+// ---------------------------------------------------------------------------
+// Gaussian-process potential (CPU form of the reference)
+// ---------------------------------------------------------------------------
+namespace {
+double orc_matern(double nu, double r) {
+    const double kSqrt3 = 1.7320508075688772935, kSqrt5 = 2.2360679774997896964;
+    if (std::abs(nu - 0.5) < 1.0e-12) return std::exp(-r);
+    if (std::abs(nu - 1.5) < 1.0e-12) { const double x = kSqrt3 * r; return (1.0 + x) * std::exp(-x); }
+    const double x = kSqrt5 * r;
+    return (1.0 + x + x * x / 3.0) * std::exp(-x);
+}
+
+// GaussianProcessPotential::GP(const dVec&) (potential.cpp:330-344)
+double orc_gp_one(const orc_gp_params* p, const double* tr, int n, const double* q) {
+    dVec r, invell, pside, sideInv;
+    for (int d = 0; d < 3; ++d) {
+        r[d] = (q[d] - p->norm_offset[d]) / p->norm_scale[d];
+        invell[d] = 1.0 / p->ell[d];
+        pside[d] = p->periodic[d] ? p->side[d] : 0.0;
+        sideInv[d] = 1.0 / p->side[d];
+    }
+    double kernelDot = 0.0;
+    for (int k = 0; k < n; ++k) {
+        // MaternKernel::K(r, trainX(k)): sep = trainX - r, putInBC, * 1/ell
+        dVec sep;
+        for (int d = 0; d < 3; ++d) sep[d] = tr[4 * (size_t)k + d] - r[d];
+        for (int d = 0; d < 3; ++d) sep[d] -= pside[d] * std::floor(sep[d] * sideInv[d] + 0.5);
+        for (int d = 0; d < 3; ++d) sep[d] = sep[d] * invell[d];
+        double d2 = 0.0;
+        for (int d = 0; d < 3; ++d) d2 += sep[d] * sep[d];
+        kernelDot += orc_matern(p->matern_nu, std::sqrt(d2)) * tr[4 * (size_t)k + 3];
+    }
+    return p->standard_mean + p->standard_std * (p->mean + p->sigma2 * kernelDot);
+}
+}  // namespace
+
+extern "C" void orc_gp_eval(const orc_gp_params* p, const double* training, int n,
+                            const double* pos, int count, double* out) {
+    for (int i = 0; i < count; ++i) out[i] = orc_gp_one(p, training, n, pos + 3 * (size_t)i);
+}
+
+// GPHeBenzenePotential::V(const dVec*, double*, int) and long_range
+// (potential.cpp:5610-5681, include/potential.h:2433-2480)
+extern "C" void orc_gp_benzene(const orc_gp_params* p, const double* training, int n,
+                               const double* pos, int count, double* out) {
+    const double r0 = 5.765366674e+00, gama = 1.671477473e+01;
+    const double x1 = 2.290626821e+05, x2 = 4.069217828e+06, x3 = 9.542607077e+07, x4 = 0.0;
+    const double x5 = -4.775615288e+04, x6 = -1.263899296e+07, x7 = -2.959330054e+08, x8 = 0.0;
+    const double x9 = 9.511488779e+05, x10 = 2.551023972e+08, x11 = 0.0, x12 = 1.883887454e+08;
+    auto rad2deg = [](double a) { return (a * 180.0) / M_PI; };
+    auto deg2rad = [](double a) { return (a * M_PI) / 180.0; };
+    for (int i = 0; i < count; ++i) {
+        const double x = pos[3 * (size_t)i], y = pos[3 * (size_t)i + 1];
+        double z = pos[3 * (size_t)i + 2];
+        double finx = 0.0, finy = 0.0;
+        if (z <= 0.0) z = -z;
+        const double pi = M_PI;
+        double angle = std::round(rad2deg(std::atan2(y, x)) * 10000.0) / 10000.0;
+        if (angle < 0.0) angle = 180.0 + (180.0 + angle);
+        if (angle <= 30.0) { finx = x; finy = y; }
+        else {
+            double rot = std::fmod(angle, 60.0) - angle;
+            if ((angle + rot) > 30.0) {
+                rot = deg2rad(rot);
+                const double rx = std::cos(rot) * x - std::sin(rot) * y;
+                const double ry = std::sin(rot) * x + std::cos(rot) * y;
+                finx = std::cos(pi / 3.0) * rx + std::sin(pi / 3.0) * ry;
+                finy = std::sin(pi / 3.0) * rx - std::cos(pi / 3.0) * ry;
+            } else {
+                rot = deg2rad(rot);
+                finx = std::cos(rot) * x - std::sin(rot) * y;
+                finy = std::sin(rot) * x + std::cos(rot) * y;
+            }
+        }
+        const double rho = std::sqrt(finx * finx + finy * finy);
+        if (rho < 3.0 && z < 2.0) { out[i] = 10000.0; continue; }
+        const double q[3] = {finx, finy, z};
+        const double gpv = orc_gp_one(p, training, n, q);
+        double d2 = 0.0;
+        d2 += finx * finx; d2 += finy * finy; d2 += z * z;
+        const double rnorm = std::sqrt(d2);
+        const double h_long = 1.0 / (1.0 + std::exp(-gama * (rnorm - r0)));
+        double value;
+        if (rho > 5.0 || z > 6.5) {
+            const double ph0 = std::atan2(finy, finx), th0 = std::acos(z / rnorm);
+            const double tt = std::cos(th0), fi = ph0;
+            const double normm1 = std::sqrt(5.0) / 5.0, normm2 = std::sqrt(13.0) / 13.0;
+            const double normm3 = 0.1792151994e-4;
+            const double p1 = -x1 / std::pow(rnorm, 6) - x2 / std::pow(rnorm, 8) - x3 / std::pow(rnorm, 10) - x4 / std::pow(rnorm, 12);
+            const double p2 = -normm1 * (1.5 * tt * tt - 0.5) *
+                              (x5 / std::pow(rnorm, 6) + x6 / std::pow(rnorm, 8) + x7 / std::pow(rnorm, 10) + x8 / std::pow(rnorm, 12));
+            const double p3 = -normm2 * (3.0 / 8.0 + 35.0 / 8.0 * std::pow(tt, 4) - 15.0 / 4.0 * tt * tt);
+            const double p4 = (x9 / std::pow(rnorm, 8) + x10 / std::pow(rnorm, 10) + x11 / std::pow(rnorm, 12));
+            const double p5 = -normm3 * 10395.0 * std::pow(1 - tt * tt, 3) * std::cos(6 * fi) * x12 / std::pow(rnorm, 10);
+            value = (1.0 - h_long) * gpv + h_long * (p1 + p2 + p3 * p4 + p5);
+        } else value = gpv;
+        out[i] = value / 0.695;
+    }
 }

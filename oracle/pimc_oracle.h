@@ -123,6 +123,23 @@ void orc_isf_cpu_form(orc_sys* s, const double* q, int nq, double* out);
 void orc_isf_gpu_form(orc_sys* s, const double* q, int nq, double* out);
 /* F(q,tau) by rho_q in FP64, tau in [0,M/2], layout [q][M/2+1]; nthreads>=1 */
 void orc_isf_rhoq(orc_sys* s, const double* q, int nq, int nthreads, double* out);
+/* cylinder S(q) (CylinderStaticStructureFactorEstimator), sum over slices / M
+ * of the included beads' pair cosines; *n0 = num1DParticles */
+void orc_ssf_cylinder(orc_sys* s, const double* q, int nq, double maxR, double* out, int* n0);
+/* getQVectors2 shells; returns the count, fills at most cap */
+int orc_qvectors_shells(double dq, double qmax, int sphere, double* q, int* shell, int cap);
+/* Gaussian-process potential: GaussianProcessPotential::GP with
+ * MaternKernel::K (potential.cpp:330-344, gpkernel.cpp:97-108), and
+ * GPHeBenzenePotential::V batch (potential.cpp:5610-5681) */
+typedef struct {
+    double matern_nu, ell[3], norm_offset[3], norm_scale[3];
+    double standard_mean, standard_std, mean, sigma2, side[3];
+    int periodic[3];
+} orc_gp_params;
+void orc_gp_eval(const orc_gp_params* p, const double* training, int n, const double* pos,
+                 int count, double* out);
+void orc_gp_benzene(const orc_gp_params* p, const double* training, int n, const double* pos,
+                    int count, double* out);
 /* rho_q(t) FP64, layout [q][M][2] */
 void orc_rhoq(orc_sys* s, const double* q, int nq, double* out);
 

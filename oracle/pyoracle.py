@@ -20,6 +20,13 @@ class OrcParams(C.Structure):
                 ("aziz_year", C.c_int), ("virial_window", C.c_int), ("mu", C.c_double)]
 
 
+class OrcGpParams(C.Structure):
+    _fields_ = [("matern_nu", C.c_double), ("ell", C.c_double * 3), ("norm_offset", C.c_double * 3),
+                ("norm_scale", C.c_double * 3), ("standard_mean", C.c_double),
+                ("standard_std", C.c_double), ("mean", C.c_double), ("sigma2", C.c_double),
+                ("side", C.c_double * 3), ("periodic", C.c_int * 3)]
+
+
 class OrcMoveParams(C.Structure):
     _fields_ = [("mbar", C.c_int), ("diagonal_move", C.c_int), ("var_updates", C.c_int),
                 ("max_wind", C.c_int), ("temperature", C.c_double), ("p_com", C.c_double),
@@ -96,6 +103,11 @@ def load():
         "orc_pair_correlation": (None, [_VP, C.c_int, _DP]),
         "orc_superfluid": (None, [_VP, _DP]),
         "orc_permutation_cycles": (None, [_VP, _DP]),
+        "orc_gp_eval": (None, [C.POINTER(OrcGpParams), _DP, C.c_int, _DP, C.c_int, _DP]),
+        "orc_gp_benzene": (None, [C.POINTER(OrcGpParams), _DP, C.c_int, _DP, C.c_int, _DP]),
+        "orc_ssf_cylinder": (None, [_VP, _DP, C.c_int, C.c_double, _DP, C.POINTER(C.c_int)]),
+        "orc_qvectors_shells": (C.c_int, [C.c_double, C.c_double, C.c_int, _DP,
+                                          C.POINTER(C.c_int), C.c_int]),
         "orc_format_state": (C.c_long, [_DP, _IP, _IP, C.POINTER(C.c_uint8), C.c_int, C.c_int,
                                         C.POINTER(C.c_longlong), C.c_int, C.POINTER(C.c_uint32),
                                         C.c_char_p, C.c_long]),
@@ -300,6 +312,13 @@ class Oracle:
         self.lib.orc_permutation_cycles(self.h, _d(out))
         return out
 
+    def ssf_cylinder(self, q, max_r):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(q))
+        n0 = C.c_int()
+        self.lib.orc_ssf_cylinder(self.h, _d(q), len(q), max_r, _d(out), C.byref(n0))
+        return out, n0.value
+
     def rhoq(self, q):
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
         out = np.zeros((len(q), self.M, 2))
@@ -317,6 +336,36 @@ class Oracle:
                                    _d(en), C.byref(st))
         return dict(trace=trace[:n], energies=en[:nsteps], attempted=list(st.attempted),
                     accepted=list(st.accepted), bead_updates=st.bead_updates)
+
+
+def gp_eval(training, pos, benzene=False, **kw):
+    """GaussianProcessPotential::GP (or GPHeBenzenePotential::V) on the CPU;
+    kw: matern_nu, ell, norm_offset, norm_scale, standard_mean, standard_std,
+    mean, sigma2, side, periodic."""
+    lib = load()
+    p = OrcGpParams()
+    p.matern_nu = kw["matern_nu"]
+    for d in range(3):
+        for k in ("ell", "norm_offset", "norm_scale", "side"):
+            getattr(p, k)[d] = np.broadcast_to(kw[k], 3)[d]
+        p.periodic[d] = int(np.broadcast_to(kw.get("periodic", 1), 3)[d])
+    p.standard_mean, p.standard_std = kw["standard_mean"], kw["standard_std"]
+    p.mean, p.sigma2 = kw["mean"], kw["sigma2"]
+    t = np.ascontiguousarray(training, dtype=np.float64).reshape(-1, 4)
+    x = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros(len(x))
+    fn = lib.orc_gp_benzene if benzene else lib.orc_gp_eval
+    fn(C.byref(p), _d(t), len(t), _d(x), len(x), _d(out))
+    return out
+
+
+def qvectors_shells(dq, qmax, sphere=False):
+    lib = load()
+    n = lib.orc_qvectors_shells(dq, qmax, 1 if sphere else 0, None, None, 0)
+    q = np.zeros((max(n, 1), 3))
+    sh = np.zeros(max(n, 1), dtype=np.int32)
+    lib.orc_qvectors_shells(dq, qmax, 1 if sphere else 0, _d(q), sh.ctypes.data_as(C.POINTER(C.c_int)), n)
+    return q[:n], sh[:n]
 
 
 def qvectors(kind, text, side):

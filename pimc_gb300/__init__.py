@@ -52,6 +52,19 @@ def qvectors(kind, text, side):
     return q[:n.value]
 
 
+def qvectors_shells(dq, qmax, sphere=False):
+    """EstimatorBase::getQVectors2: (q [n][3], shell index [n])."""
+    lib = _lib.load()
+    n = C.c_int()
+    _lib.check(lib.pgb_qvectors_shells(dq, qmax, 1 if sphere else 0, None, None, 0, C.byref(n)))
+    q = np.zeros((max(n.value, 1), 3))
+    sh = np.zeros(max(n.value, 1), dtype=np.int32)
+    _lib.check(lib.pgb_qvectors_shells(dq, qmax, 1 if sphere else 0, dptr(q),
+                                       sh.ctypes.data_as(C.POINTER(C.c_int)), n.value,
+                                       C.byref(n)))
+    return q[:n.value], sh[:n.value]
+
+
 class Action:
     """One path on the device with its Aziz tables and LocalAction factors."""
 
@@ -206,6 +219,16 @@ class Action:
         out = np.zeros(len(q))
         self._chk(self.lib.pgb_ssf(self.h, dptr(q), len(q), dptr(out)))
         return out
+
+    def ssf_cylinder(self, q, max_r):
+        """(1/M) sum_t |sum_{j inside} exp(i q.r_j)|^2 per q, and the number
+        of slice-0 beads inside x^2 + y^2 < max_r^2."""
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(q))
+        n0 = C.c_int()
+        self._chk(self.lib.pgb_ssf_cylinder(self.h, dptr(q), len(q), max_r, dptr(out),
+                                            C.byref(n0)))
+        return out, n0.value
 
     def isf(self, q, mode=0):
         q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)

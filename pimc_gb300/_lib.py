@@ -62,6 +62,13 @@ class PgbServerParams(C.Structure):
                 ("round_seconds", C.c_double)]
 
 
+class PgbGpParams(C.Structure):
+    _fields_ = [("matern_nu", C.c_double), ("ell", C.c_double * 3), ("norm_offset", C.c_double * 3),
+                ("norm_scale", C.c_double * 3), ("standard_mean", C.c_double),
+                ("standard_std", C.c_double), ("mean", C.c_double), ("sigma2", C.c_double),
+                ("side", C.c_double * 3), ("periodic", C.c_int * 3), ("precision", C.c_int)]
+
+
 class PgbJobSpec(C.Structure):
     _fields_ = [("n", C.c_int), ("temperature", C.c_double), ("mu", C.c_double),
                 ("density", C.c_double), ("sweeps", C.c_longlong), ("seed", C.c_uint64),
@@ -113,7 +120,17 @@ _SIGS = {
     "pgb_isf_device_async": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP]),
     "pgb_update_positions": (C.c_int, [_VP, _DP]),
     "pgb_pair_correlation": (C.c_int, [_VP, C.c_int, _DP]),
+    "pgb_ssf_cylinder": (C.c_int, [_VP, _DP, C.c_int, C.c_double, _DP, C.POINTER(C.c_int)]),
+    "pgb_qvectors_shells": (C.c_int, [C.c_double, C.c_double, C.c_int, _DP, C.POINTER(C.c_int),
+                                      C.c_int, C.POINTER(C.c_int)]),
     "pgb_plain_get_rng": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
+    "pgb_gp_create": (C.c_int, [C.POINTER(PgbGpParams), _DP, C.c_int, C.POINTER(C.c_void_p)]),
+    "pgb_gp_destroy": (C.c_int, [_VP]),
+    "pgb_gp_last_error": (C.c_char_p, [_VP]),
+    "pgb_gp_stream": (C.c_void_p, [_VP]),
+    "pgb_gp_eval": (C.c_int, [_VP, _DP, _DP, C.c_int]),
+    "pgb_gp_eval_device_async": (C.c_int, [_VP, _VP, _VP, C.c_int]),
+    "pgb_gp_benzene_v": (C.c_int, [_VP, _DP, _DP, C.c_int]),
     "pgb_plain_set_rng": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
     "pgb_walkers_get_all_positions": (C.c_int, [_VP, _DP]),
     "pgb_walkers_get_sweeps": (C.c_int, [_VP, C.POINTER(C.c_ulonglong)]),
@@ -199,10 +216,12 @@ def u8ptr(a):
     return a.ctypes.data_as(_U8)
 
 
-def check(rc, handle=None, walkers=False, server=False):
+def check(rc, handle=None, walkers=False, server=False, gp=False):
     if rc != PGB_OK:
         lib = load()
-        if server:
+        if gp:
+            msg = lib.pgb_gp_last_error(handle)
+        elif server:
             msg = lib.pgb_server_last_error(handle)
         elif walkers:
             msg = lib.pgb_walkers_last_error(handle)

@@ -29,9 +29,10 @@ PER_FILE = {
     "scatter.cu": ["-ftz=true"],
     "isf_static.cu": ["-ftz=true"],
     "path_estimators.cu": ["-fmad=false"],
+    "gp.cu": ["-fmad=false"],
 }
 SOURCES = ["api.cu", "fp64_kernels.cu", "mixed_kernels.cu", "scatter.cu",
-           "isf_tc.cu", "walkers.cu", "plain_moves.cu", "isf_static.cu", "path_estimators.cu"]
+           "isf_tc.cu", "walkers.cu", "plain_moves.cu", "isf_static.cu", "path_estimators.cu", "gp.cu"]
 
 
 def nvcc():

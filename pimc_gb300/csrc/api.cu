@@ -757,16 +757,18 @@ size_t posbuf_region(const Ctx& c) {
     return (c.p.precision == PGB_MIXED) ? ((rhoq32_work_bytes(c.view()) + 255) & ~(size_t)255) : 0;
 }
 int scatter_common(Ctx& c, const double* d_q, int nq, int what, int mode, double* d_out,
-                   void* d_work) {
-    // what: 0 ssf, 1 isf, 2 rho (FP64 values)
+                   void* d_work, double maxR2 = 0.0) {
+    // what: 0 ssf, 1 isf, 2 rho (FP64 values); maxR2 > 0 restricts the
+    // densities to the beads inside the cylinder x^2 + y^2 < maxR2 and leaves
+    // S(q) unnormalised by N (its per-sample sum over slices / M)
     PathView v = c.view();
     int N = c.numBeadsOn / c.M;
-    if (N <= 0) return c.fail(PGB_ESTATE, "structure factor needs at least one particle");
-    double norm = 1.0 / (1.0 * N * c.M);
+    if (N <= 0 && maxR2 <= 0.0) return c.fail(PGB_ESTATE, "structure factor needs at least one particle");
+    double norm = maxR2 > 0.0 ? 1.0 / (1.0 * c.M) : 1.0 / (1.0 * N * c.M);
     cudaError_t e;
     if (c.p.precision == PGB_FP64 || what == 2) {
         double* d_rho = static_cast<double*>(d_work);
-        e = launch_rhoq64(v, d_q, nq, d_rho, c.stream);
+        e = launch_rhoq64(v, d_q, nq, d_rho, c.stream, maxR2);
         if (e == cudaSuccess) {
             if (what == 0) e = launch_ssf_from_rho64(d_rho, nq, c.M, norm, d_out, c.stream);
             else if (what == 1) e = launch_isf_direct64(d_rho, nq, c.M, norm, d_out, c.stream);
@@ -776,7 +778,7 @@ int scatter_common(Ctx& c, const double* d_q, int nq, int what, int mode, double
     } else {
         float2* d_rho = static_cast<float2*>(d_work);
         void* posbuf = static_cast<char*>(d_work) + rho_region(c, nq);
-        e = launch_rhoq32(v, d_q, nq, d_rho, posbuf, c.stream);
+        e = launch_rhoq32(v, d_q, nq, d_rho, posbuf, c.stream, maxR2);
         if (e == cudaSuccess) {
             if (what == 0) e = launch_ssf_from_rho32(d_rho, nq, c.M, norm, d_out, c.stream);
             else if (mode == 1) {
@@ -832,6 +834,66 @@ int scatter_host(pgb_ctx* h, const double* q, int nq, int what, int mode, double
 extern "C" {
 
 int pgb_ssf(pgb_ctx* h, const double* q, int nq, double* out) { return scatter_host(h, q, nq, 0, 0, out); }
+
+int pgb_ssf_cylinder(pgb_ctx* h, const double* q, int nq, double maxR, double* out,
+                     int* num_inside0) {
+    if (!h || nq < 0 || !(maxR > 0.0) || (nq > 0 && (!q || !out))) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    const double maxR2 = maxR * maxR;
+    size_t qb = (size_t)nq * 3 * sizeof(double), ob = (size_t)nq * sizeof(double);
+    size_t off_o = (qb + 255) & ~(size_t)255;
+    size_t off_c = (off_o + ob + 255) & ~(size_t)255;
+    size_t off_w = off_c + 256;
+    rc = c.ensure_scratch(off_w + scatter_work_bytes(c, nq, 0, 0)); if (rc) return rc;
+    char* base = static_cast<char*>(c.d_scratch);
+    int* d_cnt = reinterpret_cast<int*>(base + off_c);
+    PGB_CUDA(&c, launch_count_inside(c.view(), maxR2, d_cnt, c.stream));
+    if (nq > 0) {
+        PGB_CUDA(&c, cudaMemcpyAsync(base, q, qb, cudaMemcpyHostToDevice, c.stream));
+        rc = scatter_common(c, reinterpret_cast<double*>(base), nq, 0, 0,
+                            reinterpret_cast<double*>(base + off_o), base + off_w, maxR2);
+        if (rc) return rc;
+        PGB_CUDA(&c, cudaMemcpyAsync(out, base + off_o, ob, cudaMemcpyDeviceToHost, c.stream));
+    }
+    int n0 = 0;
+    PGB_CUDA(&c, cudaMemcpyAsync(&n0, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    if (num_inside0) *num_inside0 = n0;
+    return PGB_OK;
+}
+
+int pgb_qvectors_shells(double dq, double qmax, int sphere, double* qvecs, int* shell, int cap,
+                        int* count) {
+    if (!count || !(dq > 0.0) || qmax < 0.0 || (cap > 0 && (!qvecs || !shell))) return PGB_EINVAL;
+    // EstimatorBase::getQVectors2 (estimator.cpp:762-824): magnitudes
+    // cq = 0, dq, 2 dq, ... (accumulated) up to qmax + EPS; q = 0 alone; then
+    // (0, 0, cq) and, for the sphere, the (theta, phi) grid of 24 steps over
+    // the first octant
+    const double kEps = 1.0e-7, kPi = 3.14159265358979323846;
+    int n = 0, nshell = 0;
+    auto put = [&](double x, double y, double z) {
+        if (n < cap) { qvecs[3*n] = x; qvecs[3*n+1] = y; qvecs[3*n+2] = z; shell[n] = nshell; }
+        ++n;
+    };
+    for (double cq = 0.0; cq <= qmax + kEps; cq += dq) {
+        if (std::fabs(cq) < kEps) put(0.0, 0.0, 0.0);
+        else {
+            put(0.0, 0.0, cq);
+            const int numTheta = 24;
+            const double dtheta = sphere ? 0.5 * kPi / numTheta : kPi;
+            for (double theta = dtheta; theta <= 0.5 * kPi + kEps; theta += dtheta) {
+                const double dphi = dtheta / std::sin(theta);
+                for (double phi = 0.0; phi <= 0.5 * kPi + kEps; phi += dphi)
+                    put(cq * std::sin(theta) * std::cos(phi), cq * std::sin(theta) * std::sin(phi),
+                        cq * std::cos(theta));
+            }
+        }
+        ++nshell;
+    }
+    *count = n;
+    return PGB_OK;
+}
 int pgb_isf(pgb_ctx* h, const double* q, int nq, int mode, double* out) { return scatter_host(h, q, nq, 1, mode, out); }
 int pgb_rhoq(pgb_ctx* h, const double* q, int nq, double* out) { return scatter_host(h, q, nq, 2, 0, out); }
 

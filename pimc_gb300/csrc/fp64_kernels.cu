@@ -411,7 +411,7 @@ cudaError_t launch_slice_terms64(const PathView& v, int window, int want_tmat,
 // rho_q(t) = sum_j exp(i q . r_j(t)) in FP64 (raw positions, as gpu_isf uses
 // raw bead coordinates).  One warp per (q, t).
 // ---------------------------------------------------------------------------
-__global__ void k_rhoq64(PathView v, const double* __restrict__ q, int nq,
+__global__ void k_rhoq64(PathView v, const double* __restrict__ q, int nq, double maxR2,
                          double* __restrict__ rho) {
     int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -423,6 +423,8 @@ __global__ void k_rhoq64(PathView v, const double* __restrict__ q, int nq,
     int n = v.nbs[t];
     double re = 0.0, im = 0.0;
     for (int j = lane; j < n; j += 32) {
+        // cylinder restriction: only beads with x^2 + y^2 < maxR^2
+        if (maxR2 > 0.0 && !(X[j] * X[j] + X[v.Ne + j] * X[v.Ne + j] < maxR2)) continue;
         double ph = 0.0;
         ph += qx * X[j]; ph += qy * X[v.Ne + j]; ph += qz * X[2 * v.Ne + j];
         double sn, cs;
@@ -434,11 +436,11 @@ __global__ void k_rhoq64(PathView v, const double* __restrict__ q, int nq,
 }
 
 cudaError_t launch_rhoq64(const PathView& v, const double* d_q, int nq, double* d_rho,
-                          cudaStream_t s) {
+                          cudaStream_t s, double maxR2) {
     long long warps = (long long)nq * v.M;
     int blocks = (int)((warps * 32 + 255) / 256);
     if (blocks < 1) return cudaSuccess;
-    k_rhoq64<<<blocks, 256, 0, s>>>(v, d_q, nq, d_rho);
+    k_rhoq64<<<blocks, 256, 0, s>>>(v, d_q, nq, maxR2, d_rho);
     return cudaGetLastError();
 }
 

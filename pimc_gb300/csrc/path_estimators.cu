@@ -12,24 +12,56 @@ constexpr int kEstBlock = 256;
 
 // Separation histogram of the pairs b1 < b2 of slices [t0, t1) with
 // ActionBase::updateSepHist's binning (action.cpp:216-224):
-// nR = int(|r_b2 - r_b1| / dSep).  One CTA per slice, integer counts.
+// nR = int(|r_b2 - r_b1| / dSep).  One CTA per slice.  The slice is staged
+// in shared memory as FP32; each pair's bin is first found in FP32 and, only
+// when the FP32 quotient lies within kEdge of a bin edge, recomputed from the
+// FP64 positions exactly as the reference does, so every count is the
+// reference's.  The FP32 quotient is within 1e-4 of the exact one for
+// |r| < 100 A (position rounding 2^-24 |r| per coordinate), far inside kEdge.
+// Counts go to per-warp shared histograms, so the result is order-free.
+constexpr int kEdgeMilli = 4;                 // kEdge = 4e-3 of a bin
+constexpr int kSepWarps = kEstBlock / 32;
+
 __global__ void __launch_bounds__(kEstBlock)
 k_sep_hist(PathView v, int t0, double dSep, unsigned long long* __restrict__ hist) {
-    __shared__ unsigned int sh[kPcfBins];
-    for (int b = threadIdx.x; b < kPcfBins; b += blockDim.x) sh[b] = 0u;
-    __syncthreads();
+    extern __shared__ float4 sp[];                       // [n] slice positions, FP32
+    __shared__ unsigned int sh[kSepWarps][kPcfBins];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int b = threadIdx.x; b < kSepWarps * kPcfBins; b += blockDim.x) (&sh[0][0])[b] = 0u;
     const int t = t0 + blockIdx.x;
     const int n = v.nbs[t];
-    for (long long q = threadIdx.x; q < (long long)n * n; q += blockDim.x) {
-        const int b1 = (int)(q / n), b2 = (int)(q - (long long)b1 * n);
-        if (b2 <= b1) continue;                              // each pair b1 < b2 once
-        const double3 d = sep64(v, t, b2, b1);
-        const int nR = (int)(sqrt(d.x * d.x + d.y * d.y + d.z * d.z) / dSep);
-        if (nR >= 0 && nR < kPcfBins) atomicAdd(&sh[nR], 1u);
+    const double* X = v.pos + (size_t)t * 3 * v.Ne;
+    for (int j = threadIdx.x; j < n; j += blockDim.x)
+        sp[j] = make_float4((float)X[j], (float)X[v.Ne + j], (float)X[2 * v.Ne + j], 0.f);
+    __syncthreads();
+    const float Lx = (float)v.side[0], Ly = (float)v.side[1], Lz = (float)v.side[2];
+    const float Lix = (float)v.sideInv[0], Liy = (float)v.sideInv[1], Liz = (float)v.sideInv[2];
+    const float invSep = (float)(1.0 / dSep);
+    const float edge = kEdgeMilli * 1.0e-3f;
+    for (int b1 = warp; b1 < n - 1; b1 += kSepWarps) {
+        const float4 r1 = sp[b1];
+        for (int b2 = b1 + 1 + lane; b2 < n; b2 += 32) {
+            const float4 r2 = sp[b2];
+            float dx = r2.x - r1.x, dy = r2.y - r1.y, dz = r2.z - r1.z;
+            dx -= Lx * rint_add(dx * Lix);
+            dy -= Ly * rint_add(dy * Liy);
+            dz -= Lz * rint_add(dz * Liz);
+            const float x = sqrtf(dx * dx + dy * dy + dz * dz) * invSep;
+            int nR = (int)x;
+            const float f = x - (float)nR;
+            if (f < edge || f > 1.0f - edge) {
+                const double3 d = sep64(v, t, b2, b1);
+                nR = (int)(sqrt(d.x * d.x + d.y * d.y + d.z * d.z) / dSep);
+            }
+            if (nR >= 0 && nR < kPcfBins) atomicAdd(&sh[warp][nR], 1u);
+        }
     }
     __syncthreads();
-    for (int b = threadIdx.x; b < kPcfBins; b += blockDim.x)
-        if (sh[b]) atomicAdd(&hist[b], (unsigned long long)sh[b]);
+    for (int b = threadIdx.x; b < kPcfBins; b += blockDim.x) {
+        unsigned long long c = 0;
+        for (int w = 0; w < kSepWarps; ++w) c += sh[w][b];
+        if (c) atomicAdd(&hist[b], c);
+    }
 }
 
 cudaError_t launch_sep_hist(const PathView& v, int slice, unsigned long long* d_hist, cudaStream_t s) {
@@ -37,7 +69,14 @@ cudaError_t launch_sep_hist(const PathView& v, int slice, unsigned long long* d_
     if (e != cudaSuccess) return e;
     const double dSep = 0.5 * sqrt(3.0) * v.side[2] / (1.0 * kPcfBins);   // action.cpp:192
     const int t0 = slice >= 0 ? slice : 0, nt = slice >= 0 ? 1 : v.M;
-    k_sep_hist<<<nt, kEstBlock, 0, s>>>(v, t0, dSep, d_hist);
+    const size_t smem = (size_t)v.Ne * sizeof(float4);
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;   // one slice in shared memory
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_sep_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    k_sep_hist<<<nt, kEstBlock, smem, s>>>(v, t0, dSep, d_hist);
     return cudaGetLastError();
 }
 
@@ -125,6 +164,30 @@ __global__ void k_cycles(PathView v, int* __restrict__ len_out) {
 cudaError_t launch_cycles(const PathView& v, int nw, int* d_len, cudaStream_t s) {
     if (nw <= 0) return cudaSuccess;
     k_cycles<<<(nw + 127) / 128, 128, 0, s>>>(v, d_len);
+    return cudaGetLastError();
+}
+
+// Beads of slice 0 inside the cylinder x^2 + y^2 < maxR2: num1DParticles
+// (estimator.cpp:4318-4327), one CTA, a fixed-order count.
+__global__ void k_count_inside(PathView v, double maxR2, int* __restrict__ out) {
+    __shared__ int red[kEstBlock];
+    int c = 0;
+    const int n = v.nbs[0];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double x = v.pos[j], y = v.pos[v.Ne + j];
+        c += (x * x + y * y < maxR2) ? 1 : 0;
+    }
+    red[threadIdx.x] = c;
+    __syncthreads();
+    for (int o = kEstBlock / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = red[0];
+}
+
+cudaError_t launch_count_inside(const PathView& v, double maxR2, int* d_out, cudaStream_t s) {
+    k_count_inside<<<1, kEstBlock, 0, s>>>(v, maxR2, d_out);
     return cudaGetLastError();
 }
 

@@ -104,8 +104,9 @@ cudaError_t launch_bead_actions64(const PathView& v, const int2* d_beads, int k,
                                   const double* d_over, double* d_out, cudaStream_t s);
 cudaError_t launch_slice_terms64(const PathView& v, int window, int want_tmat,
                                  double* d_terms /* [8][M] */, cudaStream_t s);
+// maxR2 > 0: only beads with x^2 + y^2 < maxR2 (cylinder estimators)
 cudaError_t launch_rhoq64(const PathView& v, const double* d_q, int nq,
-                          double* d_rho /* [q][M][2] */, cudaStream_t s);
+                          double* d_rho /* [q][M][2] */, cudaStream_t s, double maxR2 = 0.0);
 cudaError_t launch_isf_direct64(const double* d_rho, int nq, int M, double norm,
                                 double* d_out, cudaStream_t s);
 // mixed_kernels.cu (FP32 pairs, FP64 accumulation)
@@ -131,7 +132,8 @@ cudaError_t launch_pos32_from64(const PathView& v, float4* d_pos32,
 // d_work: rhoq32_work_bytes(v) of scratch for the slices as box fractions
 size_t rhoq32_work_bytes(const PathView& v);
 cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq,
-                          float2* d_rho /* [q][M] */, void* d_work, cudaStream_t s);
+                          float2* d_rho /* [q][M] */, void* d_work, cudaStream_t s,
+                          double maxR2 = 0.0);
 cudaError_t launch_ssf_from_rho32(const float2* d_rho, int nq, int M,
                                   double norm, double* d_out, cudaStream_t s);
 cudaError_t launch_ssf_from_rho64(const double* d_rho, int nq, int M,
@@ -143,6 +145,8 @@ cudaError_t launch_sep_hist(const PathView& v, int slice, unsigned long long* d_
 size_t winding_work_bytes();
 cudaError_t launch_winding(const PathView& v, double* d_work, double* d_out5, cudaStream_t s);
 cudaError_t launch_cycles(const PathView& v, int nw, int* d_len, cudaStream_t s);
+// slice-0 beads with x^2 + y^2 < maxR2 (one int)
+cudaError_t launch_count_inside(const PathView& v, double maxR2, int* d_out, cudaStream_t s);
 // isf_tc.cu (tcgen05 split-BF16 DFT correlation)
 size_t isf_tc_scratch_bytes(int nq, int M);
 size_t isf_tc_table_bytes(int M);

@@ -36,13 +36,58 @@ __global__ void k_rho_positions(PathView v, float4* __restrict__ uf, int4* __res
     }
 }
 
+// The same conversion restricted to the beads inside a cylinder about the z
+// axis, x^2 + y^2 < maxR^2 (include(), estimator.cpp:4309-4311), packed to
+// the front of each slice in bead order so that the sums keep one order.
+// One CTA per slice; cnt[t] receives the slice's count.
+constexpr int kMaskBlock = 256;
+
+__global__ void __launch_bounds__(kMaskBlock)
+k_rho_positions_masked(PathView v, double maxR2, float4* __restrict__ uf, int4* __restrict__ ui,
+                       int* __restrict__ cnt) {
+    __shared__ int warp_base[kMaskBlock / 32 + 1];
+    const int t = blockIdx.x;
+    const int n = v.nbs[t];
+    const double* X = v.pos + (size_t)t * 3 * v.Ne;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int base = 0;
+    for (int j0 = 0; j0 < n; j0 += kMaskBlock) {
+        const int j = j0 + threadIdx.x;
+        bool in = false;
+        double x = 0.0, y = 0.0, z = 0.0;
+        if (j < n) {
+            x = X[j]; y = X[v.Ne + j]; z = X[2 * v.Ne + j];
+            in = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)) < maxR2;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, in);
+        if (lane == 0) warp_base[warp] = __popc(bal);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int s = 0;
+            for (int w = 0; w < kMaskBlock / 32; ++w) { const int c = warp_base[w]; warp_base[w] = s; s += c; }
+            warp_base[kMaskBlock / 32] = s;
+        }
+        __syncthreads();
+        if (in) {
+            const size_t o = (size_t)t * v.Ne + base + warp_base[warp] + __popc(bal & ((1u << lane) - 1u));
+            const double ux = x * v.sideInv[0], uy = y * v.sideInv[1], uz = z * v.sideInv[2];
+            uf[o] = make_float4((float)ux, (float)uy, (float)uz, 0.f);
+            ui[o] = make_int4(fixed_turns(ux), fixed_turns(uy), fixed_turns(uz), 0);
+        }
+        base += warp_base[kMaskBlock / 32];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cnt[t] = base;
+}
+
 __global__ void __launch_bounds__(kRhoBlock)
 k_rhoq32(PathView v, const float4* __restrict__ uf, const int4* __restrict__ ui,
-         const double* __restrict__ q, int nq, float2* __restrict__ rho) {
+         const int* __restrict__ cnt, const double* __restrict__ q, int nq,
+         float2* __restrict__ rho) {
     extern __shared__ float4 su[];
     int4* si = reinterpret_cast<int4*>(su + v.Ne);
     const int t = blockIdx.y;
-    const int n = v.nbs[t];
+    const int n = cnt ? cnt[t] : v.nbs[t];
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
         su[j] = uf[(size_t)t * v.Ne + j];
         si[j] = ui[(size_t)t * v.Ne + j];
@@ -64,15 +109,19 @@ k_rhoq32(PathView v, const float4* __restrict__ uf, const int4* __restrict__ ui,
 }
 
 size_t rhoq32_work_bytes(const PathView& v) {
-    return (size_t)v.M * v.Ne * (sizeof(float4) + sizeof(int4));
+    return (size_t)v.M * v.Ne * (sizeof(float4) + sizeof(int4)) + (size_t)v.M * sizeof(int);
 }
 
 cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* d_rho,
-                          void* d_work, cudaStream_t s) {
+                          void* d_work, cudaStream_t s, double maxR2) {
     if (nq <= 0) return cudaSuccess;
     float4* uf = static_cast<float4*>(d_work);
     int4* ui = reinterpret_cast<int4*>(uf + (size_t)v.M * v.Ne);
-    {
+    int* cnt = nullptr;
+    if (maxR2 > 0.0) {
+        cnt = reinterpret_cast<int*>(ui + (size_t)v.M * v.Ne);
+        k_rho_positions_masked<<<v.M, kMaskBlock, 0, s>>>(v, maxR2, uf, ui, cnt);
+    } else {
         const size_t nb = (size_t)v.M * v.Ne;
         const int blocks = (int)std::min<size_t>((nb + 255) / 256, 152 * 16);
         k_rho_positions<<<blocks, 256, 0, s>>>(v, uf, ui);
@@ -85,7 +134,7 @@ cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* 
         cudaFuncSetAttribute(k_rhoq32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    k_rhoq32<<<grid, kRhoBlock, smem, s>>>(v, uf, ui, d_q, nq, d_rho);
+    k_rhoq32<<<grid, kRhoBlock, smem, s>>>(v, uf, ui, cnt, d_q, nq, d_rho);
     return cudaGetLastError();
 }
 

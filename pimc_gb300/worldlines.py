@@ -166,3 +166,22 @@ def permute(cfg, cycles):
             c["next"][m - 1, p] = (0, q)
             c["prev"][0, q] = (m - 1, p)
     return c
+
+
+def workload_gp(points=4096, num_ptcl=64, num_slices=64, seed=0, matern_nu=2.5):
+    """A seeded synthetic Gaussian-process potential and bead positions.
+
+    Training inputs uniform in the normalised cube [-1, 1]^3, coefficients
+    (K^-1 Y) normal with a small scale, hyperparameters of the magnitudes a
+    helium-surface fit has; positions uniform in a 14 A cell about the
+    origin.  The workload of one external-potential call is the beads of a
+    path, num_ptcl x num_slices points."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    train = np.empty((points, 4))
+    train[:, :3] = rng.uniform(-1.0, 1.0, size=(points, 3))
+    train[:, 3] = rng.normal(0.0, 2.0e-3, size=points)
+    params = dict(matern_nu=matern_nu, ell=[0.7, 1.9, 0.8], norm_offset=[0.0, 0.0, -0.1],
+                  norm_scale=[7.0, 3.5, 7.0], standard_mean=9.0, standard_std=95.0, mean=21.0,
+                  sigma2=750.0, side=[14.0, 14.0, 14.0], periodic=[1, 1, 1])
+    pos = rng.uniform(-7.0, 7.0, size=(num_ptcl * num_slices, 3))
+    return dict(training=train, params=params, pos=pos)

@@ -199,13 +199,11 @@ int main(int argc, char** argv) {
   pcf.sample();
   sfe.sample();
   pce.sample();
-  double h50[50], s26[26], c40[40], htot = 0.0;
-  orc_pair_correlation(o, -1, h50);
+  double g50[50], s26[26], c40[40];
+  orc_pair_correlation(o, -1, g50);
   orc_superfluid(o, s26);
   orc_permutation_cycles(o, c40);
-  for (double x : h50) htot += x;
-  for (int n = 0; n < 50; ++n)
-    cmp("g(r) bin", pcf.getEstimator(n), (N - 1.0) / N * h50[n] / htot, 1e-14);
+  for (int n = 0; n < 50; ++n) cmp("g(r) bin", pcf.getEstimator(n), g50[n], 1e-14);
   for (int i = 0; i < 26; ++i) cmp("superfluid column", sfe.getEstimator(i), s26[i]);
   for (int i = 0; i < 40; ++i) cmp("cycle column", pce.getEstimator(i), c40[i], 0.0);
   {
@@ -224,6 +222,31 @@ int main(int argc, char** argv) {
       std::printf("MISMATCH superfluid row '%s' (want first column '%s')\n", r.c_str(), want0);
       ++g_fail;
     }
+  }
+
+  // cylinder S(q): the CPU estimator's shells against the oracle's pair loop,
+  // the GPU estimator with every bead inside against the prism S(q)
+  {
+    const double R = 0.3 * L;
+    pgb::CylinderStaticStructureFactorEstimator cyl(ctx, R);
+    cyl.sample();
+    const int ns = (int)cyl.sums().size();
+    std::vector<double> qz((size_t)ns * 3, 0.0), want_c((size_t)ns);
+    int qn = 0;
+    std::vector<int> sh((size_t)ns);
+    pgb_qvectors_shells(2.0 * 3.14159265358979323846 / L, 4.0, 0, qz.data(), sh.data(), ns, &qn);
+    int n0 = 0;
+    orc_ssf_cylinder(o, qz.data(), ns, R, want_c.data(), &n0);
+    if (qn != ns || n0 <= 0 || cyl.numAccumulated() != 1) {
+      std::printf("MISMATCH cylinder shells %d/%d, inside %d\n", qn, ns, n0);
+      ++g_fail;
+    }
+    for (int k = 0; k < ns; ++k)
+      cmp("cylinder S(q) shell", cyl.getEstimator(k) * cyl.norm()[k], want_c[k] / n0, 1e-10);
+    pgb::CylinderStaticStructureFactorGPUEstimator cylg(ctx, q, 2.0 * L);
+    cylg.sample();
+    for (size_t k = 0; k < q.size(); ++k)
+      cmp("cylinder S(q), all inside", cylg.getEstimator((int)k), ssf.getEstimator((int)k), 1e-11);
   }
 
   // the plain form's generator state is MTRand::save's image

@@ -331,6 +331,20 @@ def test_path_estimators_match_oracle(pgb, oracle_lib, small):
         assert abs(got[25] - want[25]) <= 1e-12 * max(1.0, abs(want[25]))
 
 
+def test_pair_correlation_large_and_mixed(pgb, oracle_lib):
+    """The FP32-screened histogram at a size where many pairs sit near bin
+    edges (N = 256, M = 32), on FP64 and mixed contexts: every count exact."""
+    n, m, lam, tau = 256, 32, 6.0596, 0.004
+    L = pgb.worldlines.box_side(n)
+    cfg = pgb.worldlines.seeded_worldlines(n, m, L, lam, tau, 13)
+    for prec in (pgb.PGB_FP64, pgb.PGB_MIXED):
+        a, o = make_pair(pgb, oracle_lib, cfg, L, m, n, tau, lam, precision=prec)
+        want = o.pair_correlation(-1)
+        assert np.all(want[:40] > 0.0)
+        assert np.array_equal(a.pair_correlation(-1), want)
+        assert np.array_equal(a.pair_correlation(7), o.pair_correlation(7))
+
+
 def test_permutation_cycles_open_worm_is_an_error(pgb, small):
     d = small
     cfg = pgb.worldlines.open_worm(d["cfg"], head=(3, 2), tail=(9, 2))
