@@ -385,6 +385,8 @@ def run_isf(args, pgb):
     clocks = clk.stop()
     # e2e through the C ABI with host buffers: positions uploaded each step
     # (the reference copies its bead array to the device every sample)
+    a.update_positions(cfg["pos"])          # untimed: grows the pinned and scratch buffers
+    a.isf(q, mode=1)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         a.update_positions(cfg["pos"])      # the bead array, as the reference copies it per sample

@@ -10,10 +10,13 @@
 // out and divides by ell instead of multiplying by 1/ell.  This file follows
 // the CPU form, so both precisions agree with the reference's CPU path.
 //
-// FP64 kernel (compiled with -fmad=false): one thread per inference point,
-// training points streamed through shared memory in index order, so every
-// sum has the reference's order and rounding; only exp() may differ by an
-// ulp from the host's.
+// FP64 kernel (compiled with -fmad=false): one thread per inference point
+// and chunk of training points, streamed through shared memory in index
+// order; the chunk sums are added in chunk order.  Chunks exist only to fill
+// the GPU when a call has few points: from about 155 k points on there is one
+// chunk and every sum has the CPU form's order and rounding (up to exp(),
+// which may differ by an ulp from the host's); with several chunks the sum is
+// regrouped, a relative change of order 1e-16 of sum_k |K w_k|.
 // Mixed kernel: the separations and kernel values in FP32 and the sum in a
 // double-float pair (TwoSum), about 1e-7 of sum_k |K w_k| off the FP64 value.
 //
@@ -22,6 +25,7 @@
 // through the GP, then switched to the long-range form beyond the core.
 #include "pgb_device.cuh"
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -54,12 +58,16 @@ __device__ __forceinline__ float matern32(int nu2, float r) {
     return (1.0f + x + x * x * (1.0f / 3.0f)) * expf(-x);
 }
 
-// training data: SoA-packed double4 (x, y, z, w) rows
+// Grid: x over blocks of kGpBlock inference points, y over chunks of
+// `chunk` training points; each thread sums its chunk in index order and
+// writes the partial sum; k_gp*_combine adds the chunks in chunk order.  With
+// one chunk the FP64 sum is the CPU form's sequential sum.
 __global__ void __launch_bounds__(kGpBlock)
 k_gp64(GpDev g, const double4* __restrict__ train, const double* __restrict__ pos, int count,
-       double* __restrict__ out) {
+       int chunk, double* __restrict__ part) {
     __shared__ double4 tile[kGpTile];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int kb = blockIdx.y * chunk, ke = min(g.n, kb + chunk);
     double r0 = 0.0, r1 = 0.0, r2 = 0.0;
     if (i < count) {
         r0 = (pos[3 * (size_t)i] - g.off[0]) / g.scale[0];
@@ -67,8 +75,8 @@ k_gp64(GpDev g, const double4* __restrict__ train, const double* __restrict__ po
         r2 = (pos[3 * (size_t)i + 2] - g.off[2]) / g.scale[2];
     }
     double acc = 0.0;
-    for (int k0 = 0; k0 < g.n; k0 += kGpTile) {
-        const int nt = min(kGpTile, g.n - k0);
+    for (int k0 = kb; k0 < ke; k0 += kGpTile) {
+        const int nt = min(kGpTile, ke - k0);
         __syncthreads();
         for (int k = threadIdx.x; k < nt; k += blockDim.x) tile[k] = train[k0 + k];
         __syncthreads();
@@ -86,7 +94,16 @@ k_gp64(GpDev g, const double4* __restrict__ train, const double* __restrict__ po
             }
         }
     }
-    if (i < count) out[i] = g.standard_mean + g.standard_std * (g.mu + g.sigma2 * acc);
+    if (i < count) part[(size_t)blockIdx.y * count + i] = acc;
+}
+
+__global__ void k_gp64_combine(GpDev g, const double* __restrict__ part, int nsplit, int count,
+                               double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    double acc = part[i];
+    for (int s = 1; s < nsplit; ++s) acc += part[(size_t)s * count + i];
+    out[i] = g.standard_mean + g.standard_std * (g.mu + g.sigma2 * acc);
 }
 
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
@@ -99,9 +116,10 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 
 __global__ void __launch_bounds__(kGpBlock)
 k_gp32(GpDev g, const float4* __restrict__ train, const double* __restrict__ pos, int count,
-       double* __restrict__ out) {
+       int chunk, float2* __restrict__ part) {
     __shared__ float4 tile[kGpTile];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int kb = blockIdx.y * chunk, ke = min(g.n, kb + chunk);
     float r0 = 0.f, r1 = 0.f, r2 = 0.f;
     if (i < count) {
         r0 = (float)((pos[3 * (size_t)i] - g.off[0]) / g.scale[0]);
@@ -112,8 +130,8 @@ k_gp32(GpDev g, const float4* __restrict__ train, const double* __restrict__ pos
     const float si0 = (float)g.sideInv[0], si1 = (float)g.sideInv[1], si2 = (float)g.sideInv[2];
     const float il0 = (float)g.invell[0], il1 = (float)g.invell[1], il2 = (float)g.invell[2];
     float hi = 0.f, lo = 0.f;
-    for (int k0 = 0; k0 < g.n; k0 += kGpTile) {
-        const int nt = min(kGpTile, g.n - k0);
+    for (int k0 = kb; k0 < ke; k0 += kGpTile) {
+        const int nt = min(kGpTile, ke - k0);
         __syncthreads();
         for (int k = threadIdx.x; k < nt; k += blockDim.x) tile[k] = train[k0 + k];
         __syncthreads();
@@ -129,10 +147,19 @@ k_gp32(GpDev g, const float4* __restrict__ train, const double* __restrict__ pos
             }
         }
     }
-    if (i < count) {
-        const double acc = (double)hi + (double)lo;
-        out[i] = g.standard_mean + g.standard_std * (g.mu + g.sigma2 * acc);
+    if (i < count) part[(size_t)blockIdx.y * count + i] = make_float2(hi, lo);
+}
+
+__global__ void k_gp32_combine(GpDev g, const float2* __restrict__ part, int nsplit, int count,
+                               double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    double acc = 0.0;
+    for (int s = 0; s < nsplit; ++s) {
+        const float2 p = part[(size_t)s * count + i];
+        acc += (double)p.x + (double)p.y;
     }
+    out[i] = g.standard_mean + g.standard_std * (g.mu + g.sigma2 * acc);
 }
 
 // --------------------------------------------------------------------------
@@ -234,6 +261,8 @@ struct pgb_gp {
     // per-call scratch: positions, values, fold, cut flags (grown on demand)
     void* d_buf = nullptr;
     size_t buf_bytes = 0;
+    void* d_part = nullptr;              // per-chunk partial sums
+    size_t part_bytes = 0;
     std::string err;
     int fail(int code, const std::string& m) { err = m; return code; }
     int cfail(cudaError_t e, const char* where) {
@@ -254,13 +283,42 @@ int ensure_buf(pgb_gp* h, size_t bytes) {
     return PGB_OK;
 }
 
+// Chunks of training points so that the grid covers the GPU: about four
+// CTAs per SM, chunks no shorter than one shared-memory tile.
+int gp_splits(const pgb_gp* h, int count) {
+    const int bx = (count + kGpBlock - 1) / kGpBlock;
+    const int want = (4 * 152 + bx - 1) / bx;
+    const int maxs = (h->g.n + kGpTile - 1) / kGpTile;
+    return std::max(1, std::min(want, maxs));
+}
+
 cudaError_t launch_gp(pgb_gp* h, const double* d_pos, int count, double* d_out) {
     if (count <= 0) return cudaSuccess;
-    const int blocks = (count + kGpBlock - 1) / kGpBlock;
-    if (h->p.precision == PGB_MIXED)
-        k_gp32<<<blocks, kGpBlock, 0, h->stream>>>(h->g, h->d_train32, d_pos, count, d_out);
-    else
-        k_gp64<<<blocks, kGpBlock, 0, h->stream>>>(h->g, h->d_train64, d_pos, count, d_out);
+    const int bx = (count + kGpBlock - 1) / kGpBlock;
+    const int ns = gp_splits(h, count);
+    // chunk: a whole number of tiles, so only the last chunk is short
+    const int tiles = (h->g.n + kGpTile - 1) / kGpTile;
+    const int chunk = ((tiles + ns - 1) / ns) * kGpTile;
+    const int nsplit = (h->g.n + chunk - 1) / chunk;
+    const size_t need = (size_t)nsplit * count * sizeof(double2);
+    if (need > h->part_bytes) {
+        if (h->d_part) { cudaStreamSynchronize(h->stream); cudaFree(h->d_part); h->d_part = nullptr; h->part_bytes = 0; }
+        cudaError_t e = cudaMalloc(&h->d_part, need);
+        if (e != cudaSuccess) { h->d_part = nullptr; return e; }
+        h->part_bytes = need;
+    }
+    dim3 grid(bx, nsplit);
+    if (h->p.precision == PGB_MIXED) {
+        k_gp32<<<grid, kGpBlock, 0, h->stream>>>(h->g, h->d_train32, d_pos, count, chunk,
+                                                static_cast<float2*>(h->d_part));
+        k_gp32_combine<<<bx, kGpBlock, 0, h->stream>>>(h->g, static_cast<const float2*>(h->d_part),
+                                                      nsplit, count, d_out);
+    } else {
+        k_gp64<<<grid, kGpBlock, 0, h->stream>>>(h->g, h->d_train64, d_pos, count, chunk,
+                                                static_cast<double*>(h->d_part));
+        k_gp64_combine<<<bx, kGpBlock, 0, h->stream>>>(h->g, static_cast<const double*>(h->d_part),
+                                                      nsplit, count, d_out);
+    }
     return cudaGetLastError();
 }
 
@@ -327,7 +385,7 @@ int pgb_gp_create(const pgb_gp_params* p, const double* training, int n, pgb_gp*
 int pgb_gp_destroy(pgb_gp* h) {
     if (!h) return PGB_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
-    cudaFree(h->d_train64); cudaFree(h->d_train32); cudaFree(h->d_buf);
+    cudaFree(h->d_train64); cudaFree(h->d_train32); cudaFree(h->d_buf); cudaFree(h->d_part);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return PGB_OK;
