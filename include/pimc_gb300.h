@@ -96,6 +96,17 @@ int pgb_update_beads(pgb_ctx* ctx, const int32_t* beads, const double* pos, int 
  * unchanged until the next synchronous call. */
 int pgb_update_positions(pgb_ctx* ctx, const double* pos);
 int pgb_get_positions(pgb_ctx* ctx, double* pos);
+/* Mirror of Path::addBead / delBead / makeLink / breakLink / updateBead
+ * (path.cpp:197-420): k full bead records (slice, ptcl), position, next and
+ * prev links, active flag.  The active beads of every slice must stay packed
+ * at its front, as the reference's left-packed arrays keep them
+ * (PGB_ESTATE otherwise); numBeadsAtSlice follows. */
+int pgb_set_beads(pgb_ctx* ctx, const int32_t* beads, const double* pos, const int32_t* next,
+                  const int32_t* prev, const uint8_t* on, int k);
+/* The worm locators head, tail, special1, special2 (Worm::head ... special2) */
+int pgb_set_worm(pgb_ctx* ctx, const int32_t worm8[8]);
+/* The host mirror of the links, active flags and worm locators */
+int pgb_get_path(pgb_ctx* ctx, int32_t* next, int32_t* prev, uint8_t* on, int32_t worm8[8]);
 
 /* ---- potential action: LocalAction (action.cpp:456-740) --------------
  * Per-bead U_b for k beads at imaginary-time shift `shift` (bisection level
@@ -399,6 +410,41 @@ int pgb_plain_set_rng(pgb_ctx* ctx, const uint32_t in625[625]);
 int pgb_plain_run(pgb_ctx* ctx, const pgb_move_params* mp, int nsteps,
                   int32_t* trace, int trace_cap, int* trace_len,
                   double* energies, pgb_move_stats* stats);
+
+/* The worm algorithm in the plain form: PathIntegralMonteCarlo::step() over
+ * the reference's default PIMC move list (com, diagonal, open, close, insert,
+ * remove, advance head, recede head, advance tail, recede tail, swap head,
+ * swap tail; setup.cpp:466-470) with its attempt probabilities
+ * (constants.cpp:191-205) and diagonal/off-diagonal selection
+ * (pimc.cpp:120-208).  Moves run on the host in the reference's order of
+ * random numbers; every action is an FP64 device evaluation on the device
+ * mirror, which each path change updates (pgb_set_beads' path).  The worm
+ * state and the LookupTable order persist across calls until the next
+ * pgb_load_path.  Needs rc > L/2 (one LookupTable grid box, from which the
+ * swap moves draw their pivot) and a bead-array extent Ne with room for the
+ * particle-number fluctuations (PGB_ENOMEM when a slice outgrows it; the
+ * reference grows its arrays instead).
+ * trace: (move index in the list above, accepted) per attempted move;
+ * energies[step]: E/N, NaN when the step ends off-diagonal;
+ * nparticles[step]: active beads / M. */
+typedef struct {
+    int    mbar, diagonal_move, var_updates, max_wind;
+    double temperature, mu;
+    double worm_constant;          /* C0 (worm_constant, default 1) */
+    int    window;                 /* canonical particle window half-width, -1 none */
+    double gaussian_sd;            /* canonical Gaussian weight width, <= 0 none */
+    int    num_updates;            /* <= 0: ceil(max(N0,1) M / Mbar), at least 100 */
+    int    initial_num_particles;  /* N0 */
+} pgb_worm_params;
+typedef struct {
+    long long attempted[12];
+    long long accepted[12];
+    long long bead_updates;
+    int diagonal;                  /* 1 when the run ended on a closed configuration */
+} pgb_worm_stats;
+int pgb_plain_worm_run(pgb_ctx* ctx, const pgb_worm_params* wp, int nsteps, int32_t* trace,
+                       int trace_cap, int* trace_len, double* energies, int* nparticles,
+                       pgb_worm_stats* stats);
 
 /* ---- Gaussian-process external potential ----------------------------------
  * GaussianProcessPotential (include/potential.h:287-323, src/potential.cpp:

@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <chrono>
 #include <iomanip>
 #include <iostream>
@@ -257,6 +258,13 @@ struct Sys {
     int head[2], tail[2], sp1[2], sp2[2];
     int numBeadsOn = 0;
     std::vector<int> sepHist;         // action.h:109, 50 bins
+    // worm-move state: LookupTable slice lists (one grid box), Worm scalars
+    std::vector<std::vector<int>> hash;
+    std::vector<int> label;
+    bool diag = true;                 // Worm::isConfigDiagonal
+    int gap = XXX, length = 0;
+    dVec wsep{0.0, 0.0, 0.0};
+    bool full = false, broken = false;
     double dSep;
     // scratch interaction list (LookupTable::beadList/beadSep)
     std::vector<int> list; std::vector<dVec> lsep;
@@ -1054,6 +1062,28 @@ int run_steps(Sys* s, MT* mt, const orc_move_params* mp, int nsteps,
     return ntr;
 }
 
+#include "pimc_oracle_worm.inc"
+
+// Worm scalars of a loaded path (Worm::update without the unlinking)
+void worm_from_load(Sys& S) {
+    S.full = S.broken = false;
+    if (S.head[0] == XXX) { S.diag = true; S.gap = XXX; S.length = 0; S.wsep = {0.0, 0.0, 0.0}; return; }
+    S.diag = false;
+    S.gap = S.tail[0] - S.head[0];
+    if (S.gap < 0) S.gap += S.M;
+    Bead b{S.tail[0], S.tail[1]};
+    S.length = 0;
+    const long long limit = (long long)S.M * S.Ne + 1;
+    while (true) {
+        ++S.length;
+        if (b[0] == S.head[0] && b[1] == S.head[1]) break;
+        b = S.next(b[0], b[1]);
+        if (isXB(b) || S.length > limit) { S.broken = true; break; }
+    }
+    --S.length;   // the loop above counts the head once more than Worm::update
+    S.wsep = S.sep(S.tail[0], S.tail[1], S.head[0], S.head[1]);
+}
+
 }  // namespace
 
 struct orc_sys { Sys* s; };
@@ -1096,6 +1126,8 @@ void orc_load_path(orc_sys* h, const double* pos, const int32_t* next,
     s->sp1[0] = worm8[4]; s->sp1[1] = worm8[5];
     s->sp2[0] = worm8[6]; s->sp2[1] = worm8[7];
     recount(s);
+    reset_lookup(*s);
+    worm_from_load(*s);
 }
 void orc_get_positions(orc_sys* h, double* pos) {
     std::memcpy(pos, h->s->pos.data(), h->s->pos.size()*sizeof(double));
@@ -1727,4 +1759,22 @@ extern "C" void orc_gp_benzene(const orc_gp_params* p, const double* training, i
         } else value = gpv;
         out[i] = value / 0.695;
     }
+}
+
+extern "C" int orc_run_worm_steps(orc_sys* h, orc_mt* mt, const orc_worm_params* wp, int nsteps,
+                                  int32_t* trace, int trace_cap, double* energies,
+                                  int* nparticles, orc_worm_stats* stats) {
+    if (h->s->hash.size() != (size_t)h->s->M) reset_lookup(*h->s);
+    return run_worm_steps(h->s, &mt->m, wp, nsteps, trace, trace_cap, energies, nparticles, stats);
+}
+
+extern "C" void orc_get_path(orc_sys* h, int32_t* next, int32_t* prev, uint8_t* on, int32_t* worm8,
+                             int32_t* nbs) {
+    Sys* s = h->s;
+    size_t nb = (size_t)s->M * s->Ne;
+    for (size_t i = 0; i < nb * 2; ++i) { next[i] = s->nxt[i]; prev[i] = s->prv[i]; }
+    std::memcpy(on, s->on.data(), nb);
+    const int w[8] = {s->head[0], s->head[1], s->tail[0], s->tail[1], s->sp1[0], s->sp1[1], s->sp2[0], s->sp2[1]};
+    for (int i = 0; i < 8; ++i) worm8[i] = w[i];
+    for (int t = 0; t < s->M; ++t) nbs[t] = s->nbs[t];
 }

@@ -180,6 +180,34 @@ int orc_run_steps(orc_sys* s, orc_mt* mt, const orc_move_params* mp, int nsteps,
                   int32_t* trace, int trace_cap, double* energies,
                   orc_move_stats* stats);
 
+/* The worm-algorithm step driver over the reference's default PIMC move list
+ * (com, diagonal, open, close, insert, remove, advance head, recede head,
+ * advance tail, recede tail, swap head, swap tail; setup.cpp:466-470) with its
+ * attempt probabilities (constants.cpp:191-205).  Trace entries are (move
+ * index in that list, accepted) for every attempted move; energies[step] is
+ * E/N of the step's sample or NaN when the step ends off-diagonal;
+ * nparticles[step] = active beads / M.  Returns the trace length, -2 when a
+ * slice outgrows the bead-array extent Ne, -3 on a broken worm. */
+typedef struct {
+    int    mbar, diagonal_move, var_updates, max_wind;
+    double temperature, mu, worm_constant;   /* C0 */
+    int    window;                           /* canonical window half-width, -1 none */
+    double gaussian_sd;                      /* canonical Gaussian weight, <= 0 none */
+    int    num_updates;                      /* <= 0: the reference's default */
+    int    initial_num_particles;            /* N0 */
+} orc_worm_params;
+typedef struct {
+    long long attempted[12];
+    long long accepted[12];
+    long long bead_updates;
+    int diagonal;
+} orc_worm_stats;
+int orc_run_worm_steps(orc_sys* s, orc_mt* mt, const orc_worm_params* wp, int nsteps,
+                       int32_t* trace, int trace_cap, double* energies, int* nparticles,
+                       orc_worm_stats* stats);
+/* links [M][Ne][2], on [M][Ne], worm locators [8], numBeadsAtSlice [M] */
+void orc_get_path(orc_sys* s, int32_t* next, int32_t* prev, uint8_t* on, int32_t* worm8, int32_t* nbs);
+
 /* CPU baseline: run W independent canonical walkers (each its own system,
  * MT19937 seed seeds[w]) for nsteps each, on nthreads threads.  Each walker
  * w has N[w] particles, M[w] slices, temperature T[w], box side L[w];

@@ -27,6 +27,18 @@ class OrcGpParams(C.Structure):
                 ("side", C.c_double * 3), ("periodic", C.c_int * 3)]
 
 
+class OrcWormParams(C.Structure):
+    _fields_ = [("mbar", C.c_int), ("diagonal_move", C.c_int), ("var_updates", C.c_int),
+                ("max_wind", C.c_int), ("temperature", C.c_double), ("mu", C.c_double),
+                ("worm_constant", C.c_double), ("window", C.c_int), ("gaussian_sd", C.c_double),
+                ("num_updates", C.c_int), ("initial_num_particles", C.c_int)]
+
+
+class OrcWormStats(C.Structure):
+    _fields_ = [("attempted", C.c_longlong * 12), ("accepted", C.c_longlong * 12),
+                ("bead_updates", C.c_longlong), ("diagonal", C.c_int)]
+
+
 class OrcMoveParams(C.Structure):
     _fields_ = [("mbar", C.c_int), ("diagonal_move", C.c_int), ("var_updates", C.c_int),
                 ("max_wind", C.c_int), ("temperature", C.c_double), ("p_com", C.c_double),
@@ -103,6 +115,9 @@ def load():
         "orc_pair_correlation": (None, [_VP, C.c_int, _DP]),
         "orc_superfluid": (None, [_VP, _DP]),
         "orc_permutation_cycles": (None, [_VP, _DP]),
+        "orc_run_worm_steps": (C.c_int, [_VP, _VP, C.POINTER(OrcWormParams), C.c_int, _IP, C.c_int,
+                                         _DP, _IP, C.POINTER(OrcWormStats)]),
+        "orc_get_path": (None, [_VP, _IP, _IP, C.POINTER(C.c_uint8), _IP, _IP]),
         "orc_gp_eval": (None, [C.POINTER(OrcGpParams), _DP, C.c_int, _DP, C.c_int, _DP]),
         "orc_gp_benzene": (None, [C.POINTER(OrcGpParams), _DP, C.c_int, _DP, C.c_int, _DP]),
         "orc_ssf_cylinder": (None, [_VP, _DP, C.c_int, C.c_double, _DP, C.POINTER(C.c_int)]),
@@ -324,6 +339,35 @@ class Oracle:
         out = np.zeros((len(q), self.M, 2))
         self.lib.orc_rhoq(self.h, _d(q), len(q), _d(out))
         return out
+
+    def run_worm_steps(self, mt, nsteps, mbar, temperature, mu=0.0, worm_constant=1.0, window=-1,
+                       gaussian_sd=0.0, diagonal_move=1, var_updates=1, max_wind=1, num_updates=0,
+                       initial_num_particles=None, trace_cap=0):
+        wp = OrcWormParams(mbar, diagonal_move, var_updates, max_wind, temperature, mu,
+                           worm_constant, window, gaussian_sd, num_updates,
+                           self.Ne if initial_num_particles is None else initial_num_particles)
+        trace = np.zeros((max(trace_cap, 1), 2), dtype=np.int32)
+        en = np.zeros(max(nsteps, 1))
+        npart = np.zeros(max(nsteps, 1), dtype=np.int32)
+        st = OrcWormStats()
+        n = self.lib.orc_run_worm_steps(self.h, mt.h, C.byref(wp), nsteps, _i(trace), trace_cap,
+                                        _d(en), _i(npart), C.byref(st))
+        if n < 0:
+            raise RuntimeError("worm steps failed (%d)" % n)
+        return dict(trace=trace[:n], energies=en[:nsteps], num_particles=npart[:nsteps],
+                    attempted=list(st.attempted), accepted=list(st.accepted),
+                    bead_updates=st.bead_updates, diagonal=st.diagonal)
+
+    def path(self):
+        nb = self.M * self.Ne
+        nxt = np.zeros((self.M, self.Ne, 2), dtype=np.int32)
+        prv = np.zeros((self.M, self.Ne, 2), dtype=np.int32)
+        on = np.zeros((self.M, self.Ne), dtype=np.uint8)
+        worm = np.zeros(8, dtype=np.int32)
+        nbs = np.zeros(self.M, dtype=np.int32)
+        self.lib.orc_get_path(self.h, _i(nxt), _i(prv), on.ctypes.data_as(C.POINTER(C.c_uint8)),
+                              _i(worm), _i(nbs))
+        return dict(next=nxt, prev=prv, on=on, worm=worm, nbs=nbs, pos=self.positions())
 
     def run_steps(self, mt, nsteps, mbar, temperature, diagonal_move=1, var_updates=1,
                   max_wind=1, p_com=0.05, num_updates=0, trace_cap=0):

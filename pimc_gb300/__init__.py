@@ -273,6 +273,47 @@ class Action:
             raise ValueError("an MT19937 state has 625 words")
         self._chk(self.lib.pgb_plain_set_rng(self.h, words.ctypes.data_as(C.POINTER(C.c_uint32))))
 
+    def plain_worm_run(self, nsteps, mbar, temperature, initial_num_particles, mu=0.0,
+                       worm_constant=1.0, window=-1, gaussian_sd=0.0, diagonal_move=1,
+                       var_updates=1, max_wind=1, num_updates=0, trace_cap=0):
+        """The worm-algorithm step loop (default PIMC move list) in the plain form."""
+        wp = _lib.PgbWormParams(mbar, diagonal_move, var_updates, max_wind, temperature, mu,
+                                worm_constant, window, gaussian_sd, num_updates,
+                                initial_num_particles)
+        trace = np.zeros((max(trace_cap, 1), 2), dtype=np.int32)
+        ntr = C.c_int()
+        en = np.zeros(max(nsteps, 1))
+        npart = np.zeros(max(nsteps, 1), dtype=np.int32)
+        st = _lib.PgbWormStats()
+        self._chk(self.lib.pgb_plain_worm_run(self.h, C.byref(wp), nsteps, iptr(trace), trace_cap,
+                                              C.byref(ntr), dptr(en), iptr(npart), C.byref(st)))
+        return dict(trace=trace[:ntr.value], energies=en[:nsteps], num_particles=npart[:nsteps],
+                    attempted=list(st.attempted), accepted=list(st.accepted),
+                    bead_updates=st.bead_updates, diagonal=st.diagonal)
+
+    def path(self):
+        """Links, active flags and worm locators of the host mirror, with positions."""
+        nxt = np.zeros((self.M, self.Ne, 2), dtype=np.int32)
+        prv = np.zeros((self.M, self.Ne, 2), dtype=np.int32)
+        on = np.zeros((self.M, self.Ne), dtype=np.uint8)
+        worm = np.zeros(8, dtype=np.int32)
+        self._chk(self.lib.pgb_get_path(self.h, iptr(nxt), iptr(prv), u8ptr(on), iptr(worm)))
+        return dict(next=nxt, prev=prv, on=on, worm=worm, nbs=on.sum(axis=1).astype(np.int32),
+                    pos=self.positions())
+
+    def set_beads(self, beads, pos, nxt, prv, on):
+        beads = np.ascontiguousarray(beads, dtype=np.int32).reshape(-1, 2)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        nxt = np.ascontiguousarray(nxt, dtype=np.int32).reshape(-1, 2)
+        prv = np.ascontiguousarray(prv, dtype=np.int32).reshape(-1, 2)
+        on = np.ascontiguousarray(on, dtype=np.uint8).reshape(-1)
+        self._chk(self.lib.pgb_set_beads(self.h, iptr(beads), dptr(pos), iptr(nxt), iptr(prv),
+                                         u8ptr(on), len(beads)))
+
+    def set_worm(self, worm8):
+        w = np.ascontiguousarray(worm8, dtype=np.int32)
+        self._chk(self.lib.pgb_set_worm(self.h, iptr(w)))
+
     def plain_run(self, nsteps, mbar, temperature, diagonal_move=1, var_updates=1, max_wind=1,
                   p_com=0.05, num_updates=0, trace_cap=0):
         mp = _lib.PgbMoveParams(mbar, diagonal_move, var_updates, max_wind, temperature, p_com,

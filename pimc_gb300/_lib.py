@@ -69,6 +69,18 @@ class PgbGpParams(C.Structure):
                 ("side", C.c_double * 3), ("periodic", C.c_int * 3), ("precision", C.c_int)]
 
 
+class PgbWormParams(C.Structure):
+    _fields_ = [("mbar", C.c_int), ("diagonal_move", C.c_int), ("var_updates", C.c_int),
+                ("max_wind", C.c_int), ("temperature", C.c_double), ("mu", C.c_double),
+                ("worm_constant", C.c_double), ("window", C.c_int), ("gaussian_sd", C.c_double),
+                ("num_updates", C.c_int), ("initial_num_particles", C.c_int)]
+
+
+class PgbWormStats(C.Structure):
+    _fields_ = [("attempted", C.c_longlong * 12), ("accepted", C.c_longlong * 12),
+                ("bead_updates", C.c_longlong), ("diagonal", C.c_int)]
+
+
 class PgbJobSpec(C.Structure):
     _fields_ = [("n", C.c_int), ("temperature", C.c_double), ("mu", C.c_double),
                 ("density", C.c_double), ("sweeps", C.c_longlong), ("seed", C.c_uint64),
@@ -124,6 +136,11 @@ _SIGS = {
     "pgb_qvectors_shells": (C.c_int, [C.c_double, C.c_double, C.c_int, _DP, C.POINTER(C.c_int),
                                       C.c_int, C.POINTER(C.c_int)]),
     "pgb_plain_get_rng": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
+    "pgb_plain_worm_run": (C.c_int, [_VP, C.POINTER(PgbWormParams), C.c_int, _IP, C.c_int,
+                                     C.POINTER(C.c_int), _DP, _IP, C.POINTER(PgbWormStats)]),
+    "pgb_set_beads": (C.c_int, [_VP, _IP, _DP, _IP, _IP, C.POINTER(C.c_uint8), C.c_int]),
+    "pgb_set_worm": (C.c_int, [_VP, _IP]),
+    "pgb_get_path": (C.c_int, [_VP, _IP, _IP, C.POINTER(C.c_uint8), _IP]),
     "pgb_gp_create": (C.c_int, [C.POINTER(PgbGpParams), _DP, C.c_int, C.POINTER(C.c_void_p)]),
     "pgb_gp_destroy": (C.c_int, [_VP]),
     "pgb_gp_last_error": (C.c_char_p, [_VP]),

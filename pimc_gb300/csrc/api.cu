@@ -73,6 +73,22 @@ __global__ void k_update_beads(double* pos, float4* pos32, int Ne, const int2* b
     pos32[(size_t)b.x * Ne + b.y] = make_float4((float)p[3*i], (float)p[3*i+1], (float)p[3*i+2], 0.f);
 }
 
+// full bead records (position, links, active flag) into the device path
+struct BeadRec { int s, p, ns, np, ps, pp, on, pad; double x, y, z; };
+__global__ void k_set_beads(double* pos, float4* pos32, int2* nxt, int2* prv, uint8_t* on, int Ne,
+                            const BeadRec* r, int k) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    const BeadRec b = r[i];
+    double* X = pos + (size_t)b.s * 3 * Ne;
+    X[b.p] = b.x; X[Ne + b.p] = b.y; X[2 * Ne + b.p] = b.z;
+    const size_t j = (size_t)b.s * Ne + b.p;
+    pos32[j] = make_float4((float)b.x, (float)b.y, (float)b.z, 0.f);
+    nxt[j] = make_int2(b.ns, b.np);
+    prv[j] = make_int2(b.ps, b.pp);
+    on[j] = (uint8_t)b.on;
+}
+
 // AoS [M][Ne][3] FP64 (the reference's bead array) -> SoA [M][3][Ne] and the
 // float4 mirror, one bead per thread
 __global__ void k_positions_from_aos(const double* __restrict__ aos, double* __restrict__ pos,
@@ -350,6 +366,7 @@ int pgb_load_path(pgb_ctx* h, const double* pos, const int32_t* next, const int3
     PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
     c.loaded = true;
     c.force_valid = false;
+    c.lk_valid = false;
     return PGB_OK;
 }
 
@@ -399,6 +416,72 @@ int pgb_update_beads(pgb_ctx* h, const int32_t* beads, const double* pos, int k)
     PGB_CUDA(&c, cudaGetLastError());
     PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
     c.force_valid = false;
+    return PGB_OK;
+}
+
+int pgb_set_beads(pgb_ctx* h, const int32_t* beads, const double* pos, const int32_t* next,
+                  const int32_t* prev, const uint8_t* on, int k) {
+    if (check_ctx(h) || k < 0 || (k > 0 && (!beads || !pos || !next || !prev || !on))) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    auto okb = [&](int s, int p) { return (s == kXXX && p == kXXX) || (s >= 0 && s < c.M && p >= 0 && p < c.Ne); };
+    for (int i = 0; i < k; ++i)
+        if (beads[2*i] < 0 || beads[2*i] >= c.M || beads[2*i+1] < 0 || beads[2*i+1] >= c.Ne ||
+            !okb(next[2*i], next[2*i+1]) || !okb(prev[2*i], prev[2*i+1]))
+            return c.fail(PGB_EINVAL, "set_beads: bead or link out of range");
+    std::vector<int> lin((size_t)k);
+    std::vector<double> aos((size_t)c.M * c.Ne * 3, 0.0);
+    // numBeadsAtSlice: the active beads of a slice must stay packed at its
+    // front; checked on a copy so that a refused update changes nothing
+    std::vector<uint8_t> on2 = c.h_on;
+    for (int i = 0; i < k; ++i) on2[(size_t)beads[2*i] * c.Ne + beads[2*i+1]] = on[i] ? 1 : 0;
+    std::vector<int> nbs2(c.M);
+    int total = 0;
+    for (int s = 0; s < c.M; ++s) {
+        int cnt = 0;
+        for (int p = 0; p < c.Ne; ++p) cnt += on2[(size_t)s * c.Ne + p] ? 1 : 0;
+        for (int p = 0; p < c.Ne; ++p)
+            if ((p < cnt) != (on2[(size_t)s * c.Ne + p] != 0))
+                return c.fail(PGB_ESTATE, "set_beads: active beads of a slice must be packed at its front");
+        nbs2[s] = cnt;
+        total += cnt;
+    }
+    for (int i = 0; i < k; ++i) {
+        const size_t j = (size_t)beads[2*i] * c.Ne + beads[2*i+1];
+        lin[i] = (int)j;
+        c.h_next[2*j] = next[2*i]; c.h_next[2*j+1] = next[2*i+1];
+        c.h_prev[2*j] = prev[2*i]; c.h_prev[2*j+1] = prev[2*i+1];
+        for (int d = 0; d < 3; ++d) aos[3*j + d] = pos[3*i + d];
+    }
+    c.h_on.swap(on2);
+    c.h_nbs = nbs2;
+    c.numBeadsOn = total;
+    c.lk_valid = false;
+    return upload_beads(c, lin.data(), k, aos.data());
+}
+
+int pgb_set_worm(pgb_ctx* h, const int32_t* worm8) {
+    if (check_ctx(h) || !worm8) return PGB_EINVAL;
+    Ctx& c = h->c;
+    for (int i = 0; i < 8; i += 2)
+        if (!((worm8[i] == kXXX && worm8[i+1] == kXXX) ||
+              (worm8[i] >= 0 && worm8[i] < c.M && worm8[i+1] >= 0 && worm8[i+1] < c.Ne)))
+            return c.fail(PGB_EINVAL, "set_worm: locator out of range");
+    for (int i = 0; i < 8; ++i) c.worm[i] = worm8[i];
+    c.lk_valid = false;
+    c.force_valid = false;
+    return PGB_OK;
+}
+
+int pgb_get_path(pgb_ctx* h, int32_t* next, int32_t* prev, uint8_t* on, int32_t* worm8) {
+    if (check_ctx(h) || !next || !prev || !on || !worm8) return PGB_EINVAL;
+    Ctx& c = h->c;
+    int rc = need_path(c); if (rc) return rc;
+    const size_t nb = (size_t)c.M * c.Ne;
+    std::memcpy(next, c.h_next.data(), nb * 2 * sizeof(int32_t));
+    std::memcpy(prev, c.h_prev.data(), nb * 2 * sizeof(int32_t));
+    std::memcpy(on, c.h_on.data(), nb);
+    for (int i = 0; i < 8; ++i) worm8[i] = c.worm[i];
     return PGB_OK;
 }
 
@@ -1096,3 +1179,32 @@ int pgb_permutation_cycles(pgb_ctx* h, double* out40) {
 }
 
 }  // extern "C"
+
+namespace pgb {
+int upload_beads(Ctx& c, const int* lin, int k, const double* pos_aos) {
+    if (k > 0) {
+        const size_t rb = (size_t)k * sizeof(BeadRec);
+        int rc = c.ensure_scratch(rb + 64); if (rc) return rc;
+        rc = c.ensure_pinned(rb + 64); if (rc) return rc;
+        BeadRec* hr = static_cast<BeadRec*>(c.h_pinned);
+        for (int i = 0; i < k; ++i) {
+            const size_t j = (size_t)lin[i];
+            BeadRec r;
+            r.s = (int)(j / c.Ne); r.p = (int)(j % c.Ne);
+            r.ns = c.h_next[2*j]; r.np = c.h_next[2*j+1];
+            r.ps = c.h_prev[2*j]; r.pp = c.h_prev[2*j+1];
+            r.on = c.h_on[j]; r.pad = 0;
+            r.x = pos_aos[3*j]; r.y = pos_aos[3*j+1]; r.z = pos_aos[3*j+2];
+            hr[i] = r;
+        }
+        PGB_CUDA(&c, cudaMemcpyAsync(c.d_scratch, hr, rb, cudaMemcpyHostToDevice, c.stream));
+        k_set_beads<<<(k + 127) / 128, 128, 0, c.stream>>>(c.d_pos, c.d_pos32, c.d_next, c.d_prev, c.d_on,
+                                                           c.Ne, static_cast<const BeadRec*>(c.d_scratch), k);
+        PGB_CUDA(&c, cudaGetLastError());
+    }
+    PGB_CUDA(&c, cudaMemcpyAsync(c.d_nbs, c.h_nbs.data(), c.M * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    c.force_valid = false;
+    return PGB_OK;
+}
+}  // namespace pgb

@@ -72,6 +72,14 @@ struct Ctx {
     float4* d_force32 = nullptr;   // per-bead same-slice forces of the current configuration
     bool force_valid = false;      // cleared by every position change
     void* h_pinned = nullptr; size_t pinned_bytes = 0;
+    // plain-form worm state: the LookupTable's per-slice lists of a single
+    // grid box (their order decides swap pivots) and the Worm scalars
+    std::vector<std::vector<int>> lk_hash;
+    std::vector<int> lk_label;
+    bool lk_valid = false;
+    bool w_diag = true;
+    int w_gap = -1, w_length = 0;
+    double w_sep[3] = {0.0, 0.0, 0.0};
     // plain-form generator state (MT19937)
     std::vector<uint32_t> mt_state;
     int mt_left = 0, mt_pos = 0;
@@ -83,6 +91,11 @@ struct Ctx {
     int ensure_scratch(size_t bytes);
     int ensure_pinned(size_t bytes);
 };
+
+// Write the listed beads (linear index s*Ne + p) from the host mirrors
+// (h_next, h_prev, h_on; positions from pos_aos [M][Ne][3]) and numBeadsAtSlice
+// to the device; synchronous.
+int upload_beads(Ctx& c, const int* lin, int k, const double* pos_aos);
 
 #define PGB_CUDA(ctx, call)                                              \
     do {                                                                 \

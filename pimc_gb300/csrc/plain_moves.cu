@@ -10,6 +10,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #include "pgb_internal.h"
@@ -51,6 +52,7 @@ struct MT {
         return i;
     }
     double rand() { return double(randInt()) * (1.0 / 4294967295.0); }
+    double randExc() { return double(randInt()) * (1.0 / 4294967296.0); }
     double randNorm(double mean, double sd) {
         double x, y, r;
         do { x = 2.0 * rand() - 1.0; y = 2.0 * rand() - 1.0; r = x * x + y * y; }
@@ -118,6 +120,7 @@ struct Plain {
         err = pgb_update_beads(reinterpret_cast<pgb_ctx*>(&c), bl.data(), pl.data(), (int)beads.size());
     }
     double action_list(const std::vector<Bead>& beads) {
+        flush();
         if (err) return 0.0;
         std::vector<int32_t> bl;
         for (auto& bd : beads) if (on(bd)) { bl.push_back(bd[0]); bl.push_back(bd[1]); }
@@ -310,6 +313,727 @@ struct Plain {
         shift = 1;
         return moved;
     }
+
+    // ---------------------------------------------------------------------
+    // Worm-algorithm moves (src/move.cpp:1710-3826) on the host mirrors with
+    // FP64 device actions.  Path/LookupTable/Worm bookkeeping as in
+    // src/path.cpp:205-420, src/lookuptable.cpp:314-458, src/worm.cpp:52-118;
+    // every changed bead is written to the device before the next action.
+    // ---------------------------------------------------------------------
+    std::vector<int> dirty;
+    std::vector<char> isDirty;
+    bool full = false, broken = false;
+    pgb_worm_params wp{};
+    double Cw = 0.0;
+    int numBeads0 = 0;
+    double prob[12] = {0.01, 0.19, 0.4, 0.15, 0.4, 0.15, 0.075, 0.075, 0.075, 0.075, 0.1, 0.1};
+    pgb_worm_stats wst{};
+    std::vector<double> cumulant;
+    int sizeCDF = 0;
+    std::vector<Bead> fullList;
+    std::vector<dVec> originalPos;
+
+    size_t lin(Bead b) const { return (size_t)b[0] * c.Ne + b[1]; }
+    void touch(Bead b) {
+        if (isDirty.empty()) isDirty.assign((size_t)c.M * c.Ne, 0);
+        size_t j = lin(b);
+        if (!isDirty[j]) { isDirty[j] = 1; dirty.push_back((int)j); }
+    }
+    void flush() {
+        if (err) return;
+        if (dirty.empty()) return;
+        err = pgb::upload_beads(c, dirty.data(), (int)dirty.size(), pos.data());
+        for (int j : dirty) isDirty[j] = 0;
+        dirty.clear();
+    }
+    void setNextB(Bead b, Bead v) { size_t i = lin(b) * 2; c.h_next[i] = v[0]; c.h_next[i + 1] = v[1]; touch(b); }
+    void setPrevB(Bead b, Bead v) { size_t i = lin(b) * 2; c.h_prev[i] = v[0]; c.h_prev[i + 1] = v[1]; touch(b); }
+    void setPos(Bead b, const dVec& p) { for (int d = 0; d < 3; ++d) pos[lin(b) * 3 + d] = p[d]; touch(b); }
+    Bead W(int k) const { return {c.worm[2 * k], c.worm[2 * k + 1]}; }
+    void setW(int k, Bead b) { c.worm[2 * k] = b[0]; c.worm[2 * k + 1] = b[1]; }
+    Bead head() const { return W(0); }
+    Bead tail() const { return W(1); }
+    Bead sp1() const { return W(2); }
+
+    // LookupTable with one grid box: per-slice lists in the reference's order
+    void lookupInit() {
+        c.lk_hash.assign(c.M, std::vector<int>());
+        c.lk_label.assign((size_t)c.M * c.Ne, XXX);
+        for (int t = 0; t < c.M; ++t)
+            for (int p = 0; p < c.Ne; ++p)
+                if (c.h_on[(size_t)t * c.Ne + p]) {
+                    c.lk_label[(size_t)t * c.Ne + p] = (int)c.lk_hash[t].size();
+                    c.lk_hash[t].push_back(p);
+                }
+        // Worm scalars of the loaded path (Worm::update without unlinking)
+        if (c.worm[0] == XXX) { c.w_diag = true; c.w_gap = XXX; c.w_length = 0; c.w_sep[0] = c.w_sep[1] = c.w_sep[2] = 0.0; }
+        else {
+            c.w_diag = false;
+            c.w_gap = c.worm[2] - c.worm[0];
+            if (c.w_gap < 0) c.w_gap += c.M;
+            Bead b = tail();
+            int len = 0;
+            const long long limit = (long long)c.M * c.Ne + 1;
+            while (true) {
+                ++len;
+                if (b == head()) break;
+                b = next(b);
+                if (isX(b) || len > limit) { broken = true; break; }
+            }
+            c.w_length = len - 1;
+            dVec d = sep(tail(), head());
+            for (int i = 0; i < 3; ++i) c.w_sep[i] = d[i];
+        }
+        c.lk_valid = true;
+    }
+    void lookupAdd(Bead b) { c.lk_label[lin(b)] = (int)c.lk_hash[b[0]].size(); c.lk_hash[b[0]].push_back(b[1]); }
+    void lookupDel(Bead b) {
+        auto& h = c.lk_hash[b[0]];
+        const int l = c.lk_label[lin(b)], last = (int)h.size() - 1;
+        if (l < last) { const int moved = h[last]; h[l] = moved; c.lk_label[(size_t)b[0] * c.Ne + moved] = l; }
+        h.pop_back();
+        c.lk_label[lin(b)] = XXX;
+    }
+    // Path::addBead: a full slice is an error here (the reference grows Ne)
+    Bead addBead(int slice, const dVec& p) {
+        Bead last{slice, c.h_nbs[slice]};
+        if (last[1] >= c.Ne) { full = true; return {XXX, XXX}; }
+        c.h_on[lin(last)] = 1;
+        ++c.numBeadsOn;
+        ++c.h_nbs[slice];
+        setNextB(last, {XXX, XXX}); setPrevB(last, {XXX, XXX});
+        setPos(last, p);
+        lookupAdd(last);
+        return last;
+    }
+    Bead addNextBead(Bead pb, const dVec& p) {
+        int slice = pb[0] + 1;
+        if (slice >= c.M) slice -= c.M;
+        Bead b = addBead(slice, p);
+        if (full) return b;
+        setNextB(pb, b); setPrevB(b, pb);
+        return b;
+    }
+    Bead addPrevBead(Bead nb, const dVec& p) {
+        int slice = nb[0] - 1;
+        if (slice < 0) slice += c.M;
+        Bead b = addBead(slice, p);
+        if (full) return b;
+        setPrevB(nb, b); setNextB(b, nb);
+        return b;
+    }
+    void delBead(Bead b) {
+        lookupDel(b);
+        --c.h_nbs[b[0]];
+        Bead last{b[0], c.h_nbs[b[0]]};
+        if (!isX(next(b))) setPrevB(next(b), {XXX, XXX});
+        if (!isX(prev(b))) setNextB(prev(b), {XXX, XXX});
+        if (b[1] < c.h_nbs[b[0]]) {
+            lookupDel(last);
+            lookupAdd(b);
+            setPos(b, P(last));
+            setPrevB(b, prev(last));
+            setNextB(b, next(last));
+            if (!isX(next(last))) setPrevB(next(last), b);
+            if (!isX(prev(last))) setNextB(prev(last), b);
+            for (int k = 0; k < 4; ++k) if (W(k) == last) setW(k, b);
+        }
+        setNextB(last, {XXX, XXX}); setPrevB(last, {XXX, XXX});
+        c.h_on[lin(last)] = 0;
+        touch(last);
+        --c.numBeadsOn;
+    }
+    Bead delBeadGetNext(Bead b) { Bead n = next(b); delBead(b); return n; }
+    Bead delBeadGetPrev(Bead b) { Bead p = prev(b); delBead(b); return p; }
+    void wormReset() {
+        c.w_gap = XXX; c.w_length = 0; c.w_sep[0] = c.w_sep[1] = c.w_sep[2] = 0.0;
+        for (int k = 0; k < 4; ++k) setW(k, {XXX, XXX});
+    }
+    void wormUpdate(Bead nh, Bead nt) {
+        setW(0, nh); setW(1, nt);
+        c.w_gap = nt[0] - nh[0];
+        if (c.w_gap < 0) c.w_gap += c.M;
+        Bead b = nt;
+        c.w_length = 0;
+        const long long limit = (long long)c.M * c.Ne + 1;
+        do {
+            ++c.w_length;
+            b = next(b);
+            if (isX(b) || c.w_length > limit) { broken = true; break; }
+        } while (!(b == nh));
+        dVec d = sep(nt, nh);
+        for (int i = 0; i < 3; ++i) c.w_sep[i] = d[i];
+        setNextB(nh, {XXX, XXX}); setPrevB(nt, {XXX, XXX});
+        setW(2, {XXX, XXX}); setW(3, {XXX, XXX});
+    }
+    bool tooCostly(const dVec& s, int g) const {
+        if (g == 0) return true;
+        double d = 0.0; for (int i = 0; i < 3; ++i) d += s[i] * s[i];
+        return (d * (0.25 / (c.p.lambda * c.p.tau)) / (1.0 * g)) > 4.0;
+    }
+    double ensembleWeight(int dn) {
+        const bool window = wp.window >= 0, gauss = wp.gaussian_sd > 0.0;
+        if (window || gauss) {
+            int nb = c.numBeadsOn, nbp = nb + dn;
+            if (window) {
+                int w = c.M * wp.window;
+                if (nbp > numBeads0 + w || nbp < numBeads0 - w) return 0.0;
+            }
+            if (gauss) {
+                double sb = c.M * wp.gaussian_sd;
+                double xp = 1.0 * (nbp - numBeads0) * (nbp - numBeads0) / (2.0 * sb * sb);
+                double x = 1.0 * (nb - numBeads0) * (nb - numBeads0) / (2.0 * sb * sb);
+                return std::exp(-xp + x);
+            }
+            return 1.0;
+        }
+        return 1.0;
+    }
+    // one bead's action on the device (after the pending writes)
+    double beadAction(Bead b, int mode) {
+        flush();
+        if (err) return 0.0;
+        int32_t bl[2] = {b[0], b[1]};
+        double per = 0.0, tot = 0.0;
+        err = pgb_bead_actions(reinterpret_cast<pgb_ctx*>(&c), bl, 1, 1, mode, &per, &tot);
+        return per;
+    }
+    double bare(Bead b) { return beadAction(b, PGB_ACTION_BARE); }
+    double fullBead(Bead b) { return beadAction(b, PGB_ACTION_FULL); }
+    // potentialActionCorrection(start, end): per bead along next links, in order
+    double corrRange(Bead s, Bead e) {
+        flush();
+        if (err) return 0.0;
+        std::vector<int32_t> bl;
+        Bead b = s, stop = next(e);
+        do { if (on(b)) { bl.push_back(b[0]); bl.push_back(b[1]); } b = next(b); } while (!(b == stop));
+        std::vector<double> per(bl.size() / 2 + 1, 0.0);
+        double tot = 0.0;
+        err = pgb_bead_actions(reinterpret_cast<pgb_ctx*>(&c), bl.data(), (int)bl.size() / 2, 1,
+                               PGB_ACTION_CORR, per.data(), &tot);
+        double cr = 0.0;
+        for (size_t i = 0; i < bl.size() / 2; ++i) cr += per[i];
+        return cr;
+    }
+    double fullRange(Bead s, Bead e) {
+        flush();
+        if (err) return 0.0;
+        std::vector<int32_t> bl;
+        Bead b = s, stop = next(e);
+        do { if (on(b)) { bl.push_back(b[0]); bl.push_back(b[1]); } b = next(b); } while (!(b == stop));
+        std::vector<double> per(bl.size() / 2 + 1, 0.0);
+        double tot = 0.0;
+        err = pgb_bead_actions(reinterpret_cast<pgb_ctx*>(&c), bl.data(), (int)bl.size() / 2, 1,
+                               PGB_ACTION_FULL, per.data(), &tot);
+        double u = 0.0;
+        for (size_t i = 0; i < bl.size() / 2; ++i) u += per[i];
+        return u;
+    }
+    dVec freePos(Bead n) {
+        dVec r, p = P(n);
+        for (int i = 0; i < 3; ++i) r[i] = R.randNorm(p[i], sqrt2LambdaTau);
+        putInBC(r);
+        return r;
+    }
+    dVec randPosition() {
+        dVec r;
+        for (int i = 0; i < 3; ++i) r[i] = c.p.side[i] * (-0.5 + R.randExc());
+        return r;
+    }
+    std::array<int,3> sampleWindingT(Bead sb, Bead eb, int L, double& total) {
+        dVec pe = P(eb), ps = P(sb), vel;
+        for (int i = 0; i < 3; ++i) vel[i] = pe[i] - ps[i];
+        cumrho0[0] = rho0(vel, L);
+        total = cumrho0[0];
+        for (int n = 1; n < numWind; n++) {
+            dVec vw; for (int i = 0; i < 3; ++i) vw[i] = vel[i] + winding[n][i] * c.p.side[i];
+            double cr = rho0(vw, L);
+            total += cr;
+            cumrho0[n] = cumrho0[n - 1] + cr;
+        }
+        for (auto& x : cumrho0) x /= total;
+        int idx = int(std::lower_bound(cumrho0.begin(), cumrho0.end(), R.rand()) - cumrho0.begin());
+        if (idx >= numWind) idx = numWind - 1;
+        return winding[idx];
+    }
+    int Mbar() const { return wp.mbar; }
+    int randLen() { return 2 * (1 + (int)R.randInt((uint32_t)(Mbar() / 2 - 1))); }
+    bool metro(double dA) { return R.rand() < std::exp(-dA); }
+    int trueN() const { return c.numBeadsOn / c.M; }
+
+    int wOpen() {
+        if (c.numBeadsOn == 0 || trueN() == 0) return -1;
+        const int gapLength = randLen();
+        Bead hb, tb;
+        hb[0] = 2 * (int)R.randInt((uint32_t)(c.M / 2 - 1));
+        hb[1] = (int)R.randInt((uint32_t)(c.h_nbs[hb[0]] - 1));
+        tb = nextN(hb, gapLength);
+        double totalrho0;
+        auto wind = sampleWindingT(hb, tb, gapLength, totalrho0);
+        dVec pt = P(tb), ph = P(hb), sp;
+        for (int i = 0; i < 3; ++i) sp[i] = (pt[i] - ph[i]) + wind[i] * c.p.side[i];
+        if (tooCostly(sp, gapLength)) return -1;
+        double norm = (Cw * Mbar() * c.numBeadsOn) / totalrho0;
+        norm *= prob[3] / prob[2];
+        norm *= ensembleWeight(-gapLength + 1);
+        const double muShift = gapLength * wp.mu * c.p.tau;
+        wst.attempted[2]++;
+        setW(2, hb); setW(3, tb);
+        const double actionShift = (-std::log(norm) + muShift) / gapLength;
+        double factor = 0.5;
+        Bead b = hb;
+        do {
+            wst.bead_updates++;
+            double dA = -(bare(b) - factor * actionShift);
+            if (!metro(dA)) { wormReset(); c.w_diag = true; return 0; }
+            factor = 1.0;
+            b = next(b);
+        } while (!(b == tb));
+        wst.bead_updates++;
+        double dA = -(bare(tb) - 0.5 * actionShift);
+        dA -= corrRange(hb, tb);
+        if (metro(dA)) {
+            wst.accepted[2]++;
+            b = next(hb);
+            while (!(b == tb)) b = delBeadGetNext(b);
+            wormUpdate(hb, tb);
+            c.w_diag = false;
+            return 1;
+        }
+        wormReset(); c.w_diag = true;
+        return 0;
+    }
+    void closeUndo() {
+        Bead b = next(head());
+        while (!(b == tail()) && !isX(b)) b = delBeadGetNext(b);
+        setNextB(head(), {XXX, XXX}); setPrevB(tail(), {XXX, XXX});
+        c.w_diag = false;
+    }
+    int wClose() {
+        if (c.numBeadsOn == 0) return -1;
+        dVec ws{c.w_sep[0], c.w_sep[1], c.w_sep[2]};
+        if (c.w_gap > Mbar() || c.w_gap == 0 || tooCostly(ws, c.w_gap)) return -1;
+        wst.attempted[3]++;
+        const int gap = c.w_gap;
+        double totalrho0;
+        auto wind = sampleWindingT(head(), tail(), gap, totalrho0);
+        double norm = totalrho0 / (Cw * Mbar() * (c.numBeadsOn + gap - 1));
+        norm *= prob[2] / prob[3];
+        norm *= ensembleWeight(gap - 1);
+        const double muShift = gap * wp.mu * c.p.tau;
+        const double actionShift = (std::log(norm) + muShift) / gap;
+        Bead b = head();
+        wst.bead_updates++;
+        double dA = bare(b) - 0.5 * actionShift;
+        if (!metro(dA)) { closeUndo(); return 0; }
+        for (int k = 0; k < gap - 1; k++) {
+            dVec p = stagingPos(b, tail(), gap, k, wind);
+            b = addNextBead(b, p);
+            if (full) return -2;
+            wst.bead_updates++;
+            dA = bare(b) - actionShift;
+            if (!metro(dA)) { closeUndo(); return 0; }
+        }
+        setNextB(b, tail()); setPrevB(tail(), b);
+        wst.bead_updates++;
+        dA = bare(tail()) - 0.5 * actionShift;
+        dA += corrRange(head(), tail());
+        if (metro(dA)) { wst.accepted[3]++; wormReset(); c.w_diag = true; return 1; }
+        closeUndo();
+        return 0;
+    }
+    void insertUndo(Bead tb) {
+        Bead b = tb;
+        do { b = delBeadGetNext(b); } while (!isX(b));
+        wormReset(); c.w_diag = true;
+    }
+    int wInsert() {
+        const int wormLength = randLen();
+        wst.attempted[4]++;
+        double norm = Cw * Mbar() * c.M * (c.p.side[0] * c.p.side[1] * c.p.side[2]);
+        const double muShift = wormLength * c.p.tau * wp.mu;
+        norm *= prob[5] / prob[4];
+        norm *= ensembleWeight(wormLength);
+        if (norm < std::numeric_limits<double>::epsilon()) return 0;
+        const int slice = 2 * (int)R.randInt((uint32_t)(c.M / 2 - 1));
+        dVec rp = randPosition();
+        Bead tb = addBead(slice, rp);
+        if (full) return -2;
+        setW(3, tb);
+        const double actionShift = (std::log(norm) + muShift) / wormLength;
+        Bead b = tb;
+        wst.bead_updates++;
+        double dA = bare(b) - 0.5 * actionShift;
+        if (!metro(dA)) { insertUndo(tb); return 0; }
+        for (int k = 1; k < wormLength; k++) {
+            dVec p = freePos(b);
+            b = addNextBead(b, p);
+            if (full) return -2;
+            wst.bead_updates++;
+            dA = bare(b) - actionShift;
+            if (!metro(dA)) { insertUndo(tb); return 0; }
+        }
+        dVec p = freePos(b);
+        Bead hb = addNextBead(b, p);
+        if (full) return -2;
+        setW(2, hb);
+        wst.bead_updates++;
+        dA = bare(hb) - 0.5 * actionShift;
+        dA += corrRange(tb, hb);
+        if (metro(dA)) { wst.accepted[4]++; wormUpdate(hb, tb); c.w_diag = false; return 1; }
+        insertUndo(tb);
+        return 0;
+    }
+    int wRemove() {
+        if (c.w_length > Mbar() || c.w_length < 1) return -1;
+        wst.attempted[5]++;
+        double norm = 1.0 / (Cw * Mbar() * c.M * (c.p.side[0] * c.p.side[1] * c.p.side[2]));
+        const double muShift = c.w_length * wp.mu * c.p.tau;
+        norm *= prob[4] / prob[5];
+        norm *= ensembleWeight(-c.w_length);
+        if (norm < std::numeric_limits<double>::epsilon()) return 0;
+        const double actionShift = (-std::log(norm) + muShift) / c.w_length;
+        Bead b = head();
+        double factor = 0.5;
+        do {
+            wst.bead_updates++;
+            double dA = -(bare(b) - factor * actionShift);
+            if (!metro(dA)) { c.w_diag = false; return 0; }
+            factor = 1.0;
+            b = prev(b);
+        } while (!(b == tail()));
+        wst.bead_updates++;
+        double dA = -(bare(tail()) - 0.5 * actionShift);
+        dA -= corrRange(tail(), head());
+        if (metro(dA)) {
+            wst.accepted[5]++;
+            b = head();
+            do { b = delBeadGetPrev(b); } while (!isX(b));
+            wormReset(); c.w_diag = true;
+            return 1;
+        }
+        c.w_diag = false;
+        return 0;
+    }
+    void ahUndo() {
+        setW(0, sp1());
+        Bead b = next(head());
+        while (!isX(b)) b = delBeadGetNext(b);
+        setNextB(head(), {XXX, XXX});
+        c.w_diag = false;
+        setW(2, {XXX, XXX});
+    }
+    int wAdvanceHead() {
+        if (c.numBeadsOn == 0) return -1;
+        const int al = randLen();
+        wst.attempted[6]++;
+        const double muShift = al * c.p.tau * wp.mu;
+        double norm = prob[7] / prob[6];
+        norm *= ensembleWeight(al);
+        setW(2, head()); setW(0, {XXX, XXX});
+        const double actionShift = (std::log(norm) + muShift) / al;
+        Bead b = sp1();
+        wst.bead_updates++;
+        double dA = bare(b) - 0.5 * actionShift;
+        if (!metro(dA)) { ahUndo(); return 0; }
+        for (int k = 0; k < al - 1; k++) {
+            dVec p = freePos(b);
+            b = addNextBead(b, p);
+            if (full) return -2;
+            wst.bead_updates++;
+            dA = bare(b) - actionShift;
+            if (!metro(dA)) { ahUndo(); return 0; }
+        }
+        dVec p = freePos(b);
+        Bead hb = addNextBead(b, p);
+        if (full) return -2;
+        setW(0, hb);
+        wst.bead_updates++;
+        dA = fullBead(hb) - 0.5 * actionShift;
+        dA += corrRange(sp1(), head());
+        if (metro(dA)) { wst.accepted[6]++; wormUpdate(hb, tail()); c.w_diag = false; return 1; }
+        ahUndo();
+        return 0;
+    }
+    int wAdvanceTail() {
+        if (c.numBeadsOn == 0) return -1;
+        const int al = randLen();
+        if (!(al < c.w_length)) return -1;
+        Bead tb = nextN(tail(), al);
+        const double muShift = al * c.p.tau * wp.mu;
+        double norm = prob[9] / prob[8];
+        norm *= ensembleWeight(-al);
+        wst.attempted[8]++;
+        setW(2, tb);
+        const double actionShift = (-std::log(norm) + muShift) / al;
+        double factor = 0.5;
+        Bead b = tail();
+        do {
+            wst.bead_updates++;
+            double dA = -(bare(b) - factor * actionShift);
+            if (!metro(dA)) { c.w_diag = false; setW(2, {XXX, XXX}); return 0; }
+            factor = 1.0;
+            b = next(b);
+        } while (!(b == tb));
+        wst.bead_updates++;
+        double dA = -(bare(b) - 0.5 * actionShift);
+        dA -= corrRange(tail(), tb);
+        if (metro(dA)) {
+            wst.accepted[8]++;
+            b = prev(tb);
+            do { b = delBeadGetPrev(b); } while (!isX(b));
+            wormUpdate(head(), tb);
+            c.w_diag = false;
+            return 1;
+        }
+        c.w_diag = false; setW(2, {XXX, XXX});
+        return 0;
+    }
+    int wRecedeHead() {
+        if (c.numBeadsOn == 0) return -1;
+        const int rl = randLen();
+        if (!(rl < c.w_length)) return -1;
+        Bead hb = prevN(head(), rl);
+        const double muShift = rl * c.p.tau * wp.mu;
+        double norm = prob[6] / prob[7];
+        norm *= ensembleWeight(-rl);
+        wst.attempted[7]++;
+        setW(2, hb);
+        const double actionShift = (-std::log(norm) + muShift) / rl;
+        double factor = 0.5;
+        Bead b = head();
+        do {
+            wst.bead_updates++;
+            double dA = -(bare(b) - factor * actionShift);
+            if (!metro(dA)) { c.w_diag = false; setW(2, {XXX, XXX}); return 0; }
+            factor = 1.0;
+            b = prev(b);
+        } while (!(b == hb));
+        wst.bead_updates++;
+        double dA = -(bare(hb) - 0.5 * actionShift);
+        dA -= corrRange(sp1(), head());
+        if (metro(dA)) {
+            wst.accepted[7]++;
+            b = next(hb);
+            do { b = delBeadGetNext(b); } while (!isX(b));
+            wormUpdate(hb, tail());
+            c.w_diag = false;
+            return 1;
+        }
+        c.w_diag = false; setW(2, {XXX, XXX});
+        return 0;
+    }
+    void rtUndo() {
+        setW(1, sp1());
+        Bead b = prev(tail());
+        while (!isX(b)) b = delBeadGetPrev(b);
+        setPrevB(tail(), {XXX, XXX});
+        c.w_diag = false;
+        setW(2, {XXX, XXX});
+    }
+    int wRecedeTail() {
+        if (c.numBeadsOn == 0) return -1;
+        const int rl = randLen();
+        wst.attempted[9]++;
+        const double muShift = rl * c.p.tau * wp.mu;
+        double norm = prob[8] / prob[9];
+        norm *= ensembleWeight(rl);
+        setW(2, tail()); setW(1, {XXX, XXX});
+        const double actionShift = (std::log(norm) + muShift) / rl;
+        Bead b = sp1();
+        wst.bead_updates++;
+        double dA = bare(b) - 0.5 * actionShift;
+        if (!metro(dA)) { rtUndo(); return 0; }
+        for (int k = 0; k < rl - 1; k++) {
+            dVec p = freePos(b);
+            b = addPrevBead(b, p);
+            if (full) return -2;
+            wst.bead_updates++;
+            dA = bare(b) - actionShift;
+            if (!metro(dA)) { rtUndo(); return 0; }
+        }
+        dVec p = freePos(b);
+        Bead tb = addPrevBead(b, p);
+        if (full) return -2;
+        setW(1, tb);
+        wst.bead_updates++;
+        dA = bare(tb) - 0.5 * actionShift;
+        dA += corrRange(tb, sp1());
+        if (metro(dA)) { wst.accepted[9]++; wormUpdate(head(), tb); c.w_diag = false; return 1; }
+        rtUndo();
+        return 0;
+    }
+    // SwapMoveBase::getNorm / selectPivotBead (move.cpp:3223-3330)
+    double getNorm(Bead b, int sign) {
+        const int nL = (int)fullList.size();
+        sizeCDF = nL * numWind;
+        if ((int)cumulant.size() < sizeCDF) cumulant.assign(sizeCDF, 0.0);
+        const int L = Mbar();
+        int index = 0;
+        dVec pb = P(b);
+        auto sepTo = [&](Bead f) { dVec pf = P(f), d; for (int i = 0; i < 3; ++i) d[i] = pf[i] - pb[i]; return d; };
+        dVec sp = sepTo(fullList[0]);
+        double Sigma = rho0(sp, L);
+        cumulant[index++] = Sigma;
+        for (int n = 1; n < nL; n++) {
+            sp = sepTo(fullList[n]);
+            double cr = rho0(sp, L);
+            Sigma += cr;
+            cumulant[index] = cumulant[index - 1] + cr;
+            ++index;
+        }
+        for (int w = 1; w < numWind; w++) {
+            for (int n = 0; n < nL; n++) {
+                sp = sepTo(fullList[n]);
+                for (int i = 0; i < 3; ++i) sp[i] = sp[i] + (sign * winding[w][i]) * c.p.side[i];
+                double cr = rho0(sp, L);
+                Sigma += cr;
+                cumulant[index] = cumulant[index - 1] + cr;
+                ++index;
+            }
+        }
+        for (int n = 0; n < sizeCDF; n++) cumulant[n] /= Sigma;
+        return Sigma;
+    }
+    Bead selectPivot(std::array<int,3>& wind) {
+        const double x = R.rand();
+        const int index = int(std::lower_bound(cumulant.begin(), cumulant.begin() + sizeCDF, x) - cumulant.begin());
+        const int nL = (int)fullList.size();
+        const int w = (index / nL) % numWind;
+        const int p = index % nL;
+        wind = winding[w];
+        return fullList[p];
+    }
+    void fillList(int slice) {
+        fullList.clear();
+        for (int p : c.lk_hash[slice]) fullList.push_back({slice, p});
+    }
+    int wSwapHead() {
+        if (c.numBeadsOn == 0) return -1;
+        if (c.w_diag) return -1;
+        const int swapLength = Mbar();
+        int pivotSlice = c.worm[0] + swapLength;
+        if (pivotSlice >= c.M) pivotSlice -= c.M;
+        fillList(pivotSlice);
+        if (fullList.empty()) return -1;
+        const double SigmaHead = getNorm(head(), 1);
+        std::array<int,3> wind{0, 0, 0};
+        Bead pivot = selectPivot(wind);
+        Bead b = pivot;
+        for (int k = 0; k < swapLength; k++) {
+            if (b == tail()) return -1;
+            b = prev(b);
+        }
+        Bead swp = b;
+        if (tail() == swp) return -1;
+        wst.attempted[10]++;
+        const double SigmaSwap = getNorm(swp, 1);
+        const double PNorm = std::min(SigmaHead / SigmaSwap, 1.0);
+        if (R.rand() < PNorm) {
+            setW(2, swp); setW(3, pivot);
+            originalPos.clear();
+            b = swp;
+            do {
+                if (!(b == swp) && !(b == pivot)) originalPos.push_back(P(b));
+                b = next(b);
+            } while (!(b == next(pivot)));
+            const double oldAction = fullRange(swp, pivot);
+            Bead nextSwap = next(swp);
+            setNextB(head(), nextSwap);
+            setNextB(swp, {XXX, XXX});
+            setPrevB(nextSwap, head());
+            setW(2, head());
+            setW(0, swp);
+            const Bead s1 = sp1();
+            b = s1;
+            int k = 0;
+            do {
+                if (!(b == s1) && !(b == pivot)) {
+                    dVec p = stagingPos(prev(b), pivot, swapLength, k, wind);
+                    setPos(b, p);
+                    ++k;
+                    wst.bead_updates++;
+                }
+                b = next(b);
+            } while (!(b == next(pivot)));
+            const double newAction = fullRange(s1, pivot);
+            if (metro(newAction - oldAction)) { wst.accepted[10]++; wormUpdate(swp, tail()); return 1; }
+            setW(0, s1);
+            setNextB(head(), {XXX, XXX});
+            setNextB(swp, nextSwap);
+            setPrevB(nextSwap, swp);
+            b = next(swp);
+            k = 0;
+            do { setPos(b, originalPos[k]); ++k; b = next(b); } while (!(b == pivot));
+            c.w_diag = false;
+            setW(2, {XXX, XXX}); setW(3, {XXX, XXX});
+            return 0;
+        }
+        return 0;
+    }
+    int wSwapTail() {
+        if (c.numBeadsOn == 0) return -1;
+        if (c.w_diag) return -1;
+        const int swapLength = Mbar();
+        int pivotSlice = c.worm[2] - swapLength;
+        if (pivotSlice < 0) pivotSlice += c.M;
+        fillList(pivotSlice);
+        if (fullList.empty()) return -1;
+        const double SigmaTail = getNorm(tail(), -1);
+        std::array<int,3> wind{0, 0, 0};
+        Bead pivot = selectPivot(wind);
+        Bead b = pivot;
+        for (int k = 0; k < swapLength; k++) {
+            if (b == head()) return -1;
+            b = next(b);
+        }
+        Bead swp = b;
+        if (head() == swp) return -1;
+        wst.attempted[11]++;
+        const double SigmaSwap = getNorm(swp, 1);
+        const double PNorm = std::min(SigmaTail / SigmaSwap, 1.0);
+        if (R.rand() < PNorm) {
+            setW(2, swp); setW(3, pivot);
+            originalPos.clear();
+            b = pivot;
+            do {
+                if (!(b == swp) && !(b == pivot)) originalPos.push_back(P(b));
+                b = next(b);
+            } while (!(b == next(swp)));
+            const double oldAction = fullRange(pivot, swp);
+            Bead prevSwap = prev(swp);
+            setPrevB(tail(), prevSwap);
+            setPrevB(swp, {XXX, XXX});
+            setNextB(prevSwap, tail());
+            setW(2, tail());
+            setW(1, swp);
+            const Bead s1 = sp1();
+            int k = 0;
+            b = pivot;
+            do {
+                if (!(b == s1) && !(b == pivot)) {
+                    dVec p = stagingPos(prev(b), s1, swapLength, k, wind);
+                    setPos(b, p);
+                    ++k;
+                    wst.bead_updates++;
+                }
+                b = next(b);
+            } while (!(b == next(s1)));
+            const double newAction = fullRange(pivot, s1);
+            if (metro(newAction - oldAction)) { wst.accepted[11]++; wormUpdate(head(), swp); return 1; }
+            setW(1, s1);
+            setPrevB(tail(), {XXX, XXX});
+            setPrevB(swp, prevSwap);
+            setNextB(prevSwap, swp);
+            b = next(pivot);
+            k = 0;
+            do { setPos(b, originalPos[k]); ++k; b = next(b); } while (!(b == swp));
+            setW(2, {XXX, XXX}); setW(3, {XXX, XXX});
+            c.w_diag = false;
+            return 0;
+        }
+        return 0;
+    }
 };
 
 }  // namespace
@@ -394,3 +1118,99 @@ int pgb_plain_run(pgb_ctx* h, const pgb_move_params* mp, int nsteps, int32_t* tr
 }
 
 }  // extern "C"
+
+extern "C" int pgb_plain_worm_run(pgb_ctx* h, const pgb_worm_params* wp, int nsteps, int32_t* trace,
+                                  int trace_cap, int* trace_len, double* energies, int* nparticles,
+                                  pgb_worm_stats* stats) {
+    if (!h || !wp || nsteps < 0) return PGB_EINVAL;
+    Ctx& c = h->c;
+    if (!c.loaded) return c.fail(PGB_ESTATE, "plain_worm_run: no path loaded");
+    if (!c.mt_seeded) return c.fail(PGB_ESTATE, "plain_worm_run: call pgb_plain_seed first");
+    if (wp->mbar < 2 || wp->mbar >= c.M || (wp->mbar % 2) || wp->temperature <= 0 || c.M % 2 ||
+        wp->worm_constant <= 0 || wp->initial_num_particles < 0)
+        return c.fail(PGB_EINVAL, "plain_worm_run: need even 2 <= mbar < M, even M, T > 0, C0 > 0, N0 >= 0");
+    // the swap moves draw pivots from the LookupTable's single grid box,
+    // which the reference has when the cutoff exceeds half of every side
+    for (int d = 0; d < 3; ++d)
+        if (!(c.p.rc > 0.5 * c.p.side[d]))
+            return c.fail(PGB_EINVAL, "plain_worm_run: needs rc > L/2 (one LookupTable grid box)");
+    pgb_move_params mp{};
+    mp.mbar = wp->mbar; mp.diagonal_move = wp->diagonal_move; mp.var_updates = wp->var_updates;
+    mp.max_wind = wp->max_wind; mp.temperature = wp->temperature; mp.p_com = 0.0; mp.num_updates = 0;
+    Plain pl(c, mp);
+    pl.wp = *wp;
+    pl.Cw = wp->worm_constant / (1.0 * wp->mbar * c.M * (c.p.side[0] * c.p.side[1] * c.p.side[2]));
+    pl.numBeads0 = wp->initial_num_particles * c.M;
+    pl.pos.assign((size_t)c.M * c.Ne * 3, 0.0);
+    int rc = pgb_get_positions(h, pl.pos.data());
+    if (rc) return rc;
+    if (!c.lk_valid) pl.lookupInit();
+    if (pl.broken) return c.fail(PGB_ESTATE, "plain_worm_run: the loaded worm does not connect tail to head");
+    // pimc.cpp:120-152: cumulative probabilities over the default move list;
+    // com and the diagonal move act on any configuration, open and insert on
+    // diagonal ones, the rest on off-diagonal ones
+    const int onDiag[12] = {1, 1, 1, 0, 1, 0, 0, 0, 0, 0, 0, 0};
+    const int onOff[12] = {1, 1, 0, 1, 0, 1, 1, 1, 1, 1, 1, 1};
+    double cumDiag[12], cumOff[12], cd = 0.0, co = 0.0;
+    for (int i = 0; i < 12; ++i) {
+        if (onDiag[i]) cd += pl.prob[i];
+        cumDiag[i] = cd;
+        if (onOff[i]) co += pl.prob[i];
+        cumOff[i] = co;
+    }
+    cumDiag[11] = 1.0 + EPS;
+    cumOff[11] = 1.0 + EPS;
+    int nu = wp->num_updates;
+    if (nu <= 0) { nu = int(std::ceil(std::max(wp->initial_num_particles, 1) * c.M / (1.0 * wp->mbar))); if (nu < 100) nu = 100; }
+    int ntr = 0;
+    for (int step = 0; step < nsteps; ++step) {
+        for (int n = 0; n < nu; ++n) {
+            const double x = pl.R.rand();
+            const double* cum = c.w_diag ? cumDiag : cumOff;
+            const int index = int(std::lower_bound(cum, cum + 12, x) - cum);
+            int r = -1;
+            bool acc = false;
+            switch (index) {
+                case 0: { int m = pl.com(acc); r = m > 0 ? (acc ? 1 : 0) : -1; pl.wst.bead_updates += m;
+                          if (m > 0) { pl.wst.attempted[0]++; if (acc) pl.wst.accepted[0]++; } break; }
+                case 1: { int m = wp->diagonal_move == 1 ? pl.staging(acc) : pl.bisection(acc);
+                          r = m > 0 ? (acc ? 1 : 0) : -1; pl.wst.bead_updates += m;
+                          if (m > 0) { pl.wst.attempted[1]++; if (acc) pl.wst.accepted[1]++; } break; }
+                case 2: r = pl.wOpen(); break;
+                case 3: r = pl.wClose(); break;
+                case 4: r = pl.wInsert(); break;
+                case 5: r = pl.wRemove(); break;
+                case 6: r = pl.wAdvanceHead(); break;
+                case 7: r = pl.wRecedeHead(); break;
+                case 8: r = pl.wAdvanceTail(); break;
+                case 9: r = pl.wRecedeTail(); break;
+                case 10: r = pl.wSwapHead(); break;
+                case 11: r = pl.wSwapTail(); break;
+            }
+            if (pl.err) return pl.err;
+            if (r == -2 || pl.full) {
+                pl.flush();
+                return c.fail(PGB_ENOMEM, "plain_worm_run: a slice outgrew the bead-array extent Ne");
+            }
+            if (pl.broken) return c.fail(PGB_ESTATE, "plain_worm_run: worm length walk did not reach the head");
+            if (r >= 0 && trace && ntr < trace_cap) { trace[2 * ntr] = index; trace[2 * ntr + 1] = r; ++ntr; }
+        }
+        pl.flush();
+        if (pl.err) return pl.err;
+        if (energies) {
+            if (c.w_diag) {
+                double e[9];
+                rc = pgb_energy(h, e);
+                if (rc) return rc;
+                energies[step] = e[8];
+            } else energies[step] = std::nan("");
+        }
+        if (nparticles) nparticles[step] = c.numBeadsOn / c.M;
+    }
+    pl.flush();
+    if (pl.err) return pl.err;
+    pl.wst.diagonal = c.w_diag ? 1 : 0;
+    if (trace_len) *trace_len = ntr;
+    if (stats) *stats = pl.wst;
+    return PGB_OK;
+}
