@@ -573,46 +573,65 @@ def run_pair(args, pgb):
 
 # ---------------------------------------------------------------------------
 # Plain worm-PIMC leg (N=16, T=2 K -> M=124, tau=1/248): the plain FP64 GPU
-# form (host-driven moves, MT19937) against the oracle on one host thread,
-# with the energy and S(q) (|q| <= 4/A) estimators sampled every step.
+# form running the worm algorithm (the reference's default move list, host
+# moves, FP64 device actions, MT19937) against the oracle on one host thread,
+# with the energy and S(q) (|q| <= 4/A) estimators sampled every diagonal step.
 # ---------------------------------------------------------------------------
+WORM_MOVES = ["center of mass", "diagonal", "open", "close", "insert", "remove", "advance head",
+              "recede head", "advance tail", "recede tail", "swap head", "swap tail"]
+
+
 def run_plain(args, pgb):
     from pimc_gb300 import worldlines as wl
     w = wl.workload_plain_small()
     n, m, L = w["n"], w["m"], w["side"]
-    cfg = wl.seeded_worldlines(n, m, L, w["lam"], w["tau"], 0)
+    ne = 2 * n
+    cfg = wl.seeded_worldlines(n, m, L, w["lam"], w["tau"], 0, extent=ne)
     mbar = wl.default_mbar(n, L ** 3, w["lam"], 0.004, m)
     q = pgb.qvectors("max_float", "4 0 0", [L, L, L])
-    a = pgb.Action(L, m, n, w["tau"], w["lam"])
+    kw = dict(mbar=mbar, temperature=w["temperature"], initial_num_particles=n, window=1, mu=0.0)
+    a = pgb.Action(L, m, ne, w["tau"], w["lam"])
     a.load(cfg)
     a.plain_seed(139853)
-    a.plain_run(1, mbar=mbar, temperature=w["temperature"])
+    a.plain_worm_run(1, **kw)
     t0 = time.perf_counter()
-    bu = 0
+    bu, att, acc = 0, np.zeros(12, dtype=np.int64), np.zeros(12, dtype=np.int64)
+    nssf = 0
     for _ in range(args.steps):
-        r = a.plain_run(1, mbar=mbar, temperature=w["temperature"])
+        r = a.plain_worm_run(1, **kw)
         bu += r["bead_updates"]
-        a.ssf(q)
+        att += r["attempted"]; acc += r["accepted"]
+        if r["diagonal"]:
+            a.ssf(q)
+            nssf += 1
     dt = time.perf_counter() - t0
-    out = {"metric": "bead-updates/s (plain FP64 GPU form)", "value": bu / dt,
+    out = {"metric": "bead-updates/s (plain FP64 GPU form, worm algorithm)", "value": bu / dt,
            "unit": "bead-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": 1,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic",
-           "config": {"workload": "plain PIMC N=16, T=2 K, M=124 (tau=1/248), Mbar=%d, staging + COM, "
-                                  "energy + S(q) (%d q) every step" % (mbar, len(q))}}
+           "config": {"workload": "plain worm PIMC N=16, T=2 K, M=124 (tau=1/248), Mbar=%d, the "
+                                  "reference's default move list, canonical window 1, energy + "
+                                  "S(q) (%d q) every diagonal step" % (mbar, len(q)),
+                      "ssf_samples": nssf,
+                      "acceptance": {WORM_MOVES[i]: [int(acc[i]), int(att[i])] for i in range(12)}}}
     if not args.no_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
-        o = pyoracle.Oracle(L, m, n, w["tau"], w["lam"])
+        o = pyoracle.Oracle(L, m, ne, w["tau"], w["lam"])
         o.load(cfg)
         mt = pyoracle.MT(139853)
+        o.run_worm_steps(mt, 1, **kw)
         t0 = time.perf_counter()
-        r = o.run_steps(mt, args.steps, mbar=mbar, temperature=w["temperature"])
+        bu_o = 0
         for _ in range(args.steps):
-            o.ssf_pairwise(q)
+            r = o.run_worm_steps(mt, 1, **kw)
+            bu_o += r["bead_updates"]
+            if r["diagonal"]:
+                o.ssf_pairwise(q)
         dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": r["bead_updates"] / dt, "unit": "bead-updates/s", "cores": 1,
-                               "kind": "port", "sample": "%d steps of the oracle on one thread" % args.steps}
+        out["cpu_baseline"] = {"value": bu_o / dt, "unit": "bead-updates/s", "cores": 1,
+                               "kind": "port", "sample": "%d worm-algorithm steps of the oracle on "
+                               "one thread, same seed" % args.steps}
     print(json.dumps(out))
 
 

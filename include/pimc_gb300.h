@@ -446,6 +446,56 @@ int pgb_plain_worm_run(pgb_ctx* ctx, const pgb_worm_params* wp, int nsteps, int3
                        int trace_cap, int* trace_len, double* energies, int* nparticles,
                        pgb_worm_stats* stats);
 
+/* ---- Device-resident worm walkers -----------------------------------------
+ * Independent worm-algorithm paths (grand canonical, or canonical with a
+ * particle window), one warp each, advanced by whole PIMC steps on the
+ * device: the reference's default move list with its attempt probabilities
+ * (the same moves as pgb_plain_worm_run), primitive action, FP32 Aziz pairs
+ * reduced in double-float, a Philox stream per walker.  They agree with the
+ * plain form and the oracle statistically, not draw for draw.  Walker w has
+ * num_ptcl[w] initial particles, num_slices[w] (even) slices of width tau,
+ * box side side[w], chemical potential mu[w] (NULL: 0), update length
+ * mbar[w] (even, <= 64) and room for capacity[w] beads per slice.
+ * The swap moves draw their pivot from the pivot slice's beads in index
+ * order (the reference uses its LookupTable order: the same distribution). */
+typedef struct pgb_worm_walkers pgb_worm_walkers;
+typedef struct {
+    int           num_walkers;
+    const int*    num_ptcl;
+    const int*    num_slices;
+    const double* side;
+    const double* mu;
+    const int*    mbar;
+    const int*    capacity;
+    double        tau, lambda;
+    double        worm_constant;   /* C0 */
+    int           window;          /* canonical window half-width, -1 none */
+    uint64_t      seed;
+    int           aziz_year;       /* 1979 (default) */
+} pgb_worm_walkers_params;
+typedef struct {
+    double    energy_sum, energy_sumsq;   /* E/N of the closed configurations */
+    double    n_sum, n_sumsq;             /* particle number of the same samples */
+    long long samples;                    /* steps that ended closed */
+    long long attempted[12];              /* the move list of pgb_plain_worm_run */
+    long long accepted[12];
+    long long bead_updates;
+    int       error;                      /* 1 slice full, 2 bad link, 3 runaway walk */
+    int       pad;
+} pgb_worm_walker_stats;
+int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers** out);
+int pgb_worm_walkers_destroy(pgb_worm_walkers* w);
+const char* pgb_worm_walkers_last_error(const pgb_worm_walkers* w);
+/* closed worldlines on the identity permutation from positions [M][N][3] */
+int pgb_worm_walkers_load(pgb_worm_walkers* w, int walker, const double* pos);
+/* advance every walker by `sweeps` PIMC steps (synchronous) */
+int pgb_worm_walkers_run(pgb_worm_walkers* w, int sweeps);
+int pgb_worm_walkers_stats(pgb_worm_walkers* w, pgb_worm_walker_stats* per_walker);
+int pgb_worm_walkers_reset_stats(pgb_worm_walkers* w);
+/* one walker's arrays in the layouts of pgb_load_path ([M][capacity]) */
+int pgb_worm_walkers_get_path(pgb_worm_walkers* w, int walker, double* pos, int32_t* next,
+                              int32_t* prev, uint8_t* on, int32_t worm8[8]);
+
 /* ---- Gaussian-process external potential ----------------------------------
  * GaussianProcessPotential (include/potential.h:287-323, src/potential.cpp:
  * 244-392) with the Matern kernel (include/gpkernel.h:48-72): the fields are

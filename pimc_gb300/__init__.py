@@ -19,7 +19,7 @@ from ._lib import (PGB_FP64, PGB_MIXED, PGB_ACTION_FULL, PGB_ACTION_BARE, PGB_AC
                    PgbError, dptr, iptr, u8ptr)
 from . import worldlines
 
-__all__ = ["Action", "Walkers", "Server", "qvectors", "device_info", "PGB_FP64", "PGB_MIXED",
+__all__ = ["Action", "Walkers", "WormWalkers", "Server", "qvectors", "device_info", "PGB_FP64", "PGB_MIXED",
            "PGB_ACTION_FULL", "PGB_ACTION_BARE", "PGB_ACTION_CORR", "PgbError", "worldlines",
            "action_factors"]
 
@@ -456,6 +456,96 @@ class Walkers:
 
     def stream(self):
         return self.lib.pgb_walkers_stream(self.h)
+
+
+class WormWalkers:
+    """Device-resident worm-algorithm walkers, one warp each: the reference's
+    default PIMC move list on independent paths (grand canonical, or
+    canonical with a particle window)."""
+
+    STATS_DTYPE = np.dtype([("energy_sum", "<f8"), ("energy_sumsq", "<f8"), ("n_sum", "<f8"),
+                            ("n_sumsq", "<f8"), ("samples", "<i8"), ("attempted", "<i8", (12,)),
+                            ("accepted", "<i8", (12,)), ("bead_updates", "<i8"), ("error", "<i4"),
+                            ("pad", "<i4")])
+
+    def __init__(self, n, m, side, mbar, tau, lam, mu=None, capacity=None, worm_constant=1.0,
+                 window=-1, seed=0, aziz_year=1979):
+        self.lib = _lib.load()
+        self.n = np.ascontiguousarray(n, dtype=np.int32)
+        self.W = len(self.n)
+        self.m = np.ascontiguousarray(np.broadcast_to(m, self.W), dtype=np.int32)
+        self.side = np.ascontiguousarray(np.broadcast_to(side, self.W), dtype=np.float64)
+        self.mbar = np.ascontiguousarray(np.broadcast_to(mbar, self.W), dtype=np.int32)
+        self.mu = np.ascontiguousarray(np.broadcast_to(0.0 if mu is None else mu, self.W), dtype=np.float64)
+        cap = 2 * self.n + 8 if capacity is None else np.broadcast_to(capacity, self.W)
+        self.capacity = np.ascontiguousarray(cap, dtype=np.int32)
+        p = _lib.PgbWormWalkersParams()
+        p.num_walkers = self.W
+        p.num_ptcl = self.n.ctypes.data_as(C.POINTER(C.c_int))
+        p.num_slices = self.m.ctypes.data_as(C.POINTER(C.c_int))
+        p.side = dptr(self.side)
+        p.mu = dptr(self.mu)
+        p.mbar = self.mbar.ctypes.data_as(C.POINTER(C.c_int))
+        p.capacity = self.capacity.ctypes.data_as(C.POINTER(C.c_int))
+        p.tau, p.lambda_, p.worm_constant, p.window, p.seed, p.aziz_year = (
+            tau, lam, worm_constant, window, seed, aziz_year)
+        h = C.c_void_p()
+        rc = self.lib.pgb_worm_walkers_create(C.byref(p), C.byref(h))
+        if rc != 0:
+            raise PgbError(rc, (self.lib.pgb_worm_walkers_last_error(None) or b"").decode())
+        self.h = h
+        self.tau, self.lam = tau, lam
+
+    def _chk(self, rc):
+        return _lib.check(rc, self.h, worm=True)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pgb_worm_walkers_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, w, pos):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(int(self.m[w]), int(self.n[w]), 3)
+        self._chk(self.lib.pgb_worm_walkers_load(self.h, w, dptr(pos)))
+
+    def load_seeded(self, seed=0):
+        """Every walker from seeded closed worldlines (uniform centres, Gaussian jitter)."""
+        from . import worldlines as wl
+        for w in range(self.W):
+            cfg = wl.seeded_worldlines(int(self.n[w]), int(self.m[w]), float(self.side[w]), self.lam,
+                                       self.tau, seed * 100003 + w)
+            self.load(w, cfg["pos"])
+
+    def run(self, sweeps):
+        self._chk(self.lib.pgb_worm_walkers_run(self.h, sweeps))
+
+    def stats(self):
+        out = np.zeros(self.W, dtype=self.STATS_DTYPE)
+        assert out.itemsize == C.sizeof(_lib.PgbWormWalkerStats)
+        self._chk(self.lib.pgb_worm_walkers_stats(self.h, C.cast(out.ctypes.data,
+                                                                 C.POINTER(_lib.PgbWormWalkerStats))))
+        return out
+
+    def reset_stats(self):
+        self._chk(self.lib.pgb_worm_walkers_reset_stats(self.h))
+
+    def path(self, w):
+        M, ne = int(self.m[w]), int(self.capacity[w])
+        pos = np.zeros((M, ne, 3))
+        nxt = np.zeros((M, ne, 2), dtype=np.int32)
+        prv = np.zeros((M, ne, 2), dtype=np.int32)
+        on = np.zeros((M, ne), dtype=np.uint8)
+        worm = np.zeros(8, dtype=np.int32)
+        self._chk(self.lib.pgb_worm_walkers_get_path(self.h, w, dptr(pos), iptr(nxt), iptr(prv),
+                                                     u8ptr(on), iptr(worm)))
+        return dict(pos=pos, next=nxt, prev=prv, on=on, worm=worm,
+                    nbs=on.sum(axis=1).astype(np.int32))
 
 
 class Server:

@@ -81,6 +81,22 @@ class PgbWormStats(C.Structure):
                 ("bead_updates", C.c_longlong), ("diagonal", C.c_int)]
 
 
+class PgbWormWalkersParams(C.Structure):
+    _fields_ = [("num_walkers", C.c_int), ("num_ptcl", C.POINTER(C.c_int)),
+                ("num_slices", C.POINTER(C.c_int)), ("side", C.POINTER(C.c_double)),
+                ("mu", C.POINTER(C.c_double)), ("mbar", C.POINTER(C.c_int)),
+                ("capacity", C.POINTER(C.c_int)), ("tau", C.c_double), ("lambda_", C.c_double),
+                ("worm_constant", C.c_double), ("window", C.c_int), ("seed", C.c_uint64),
+                ("aziz_year", C.c_int)]
+
+
+class PgbWormWalkerStats(C.Structure):
+    _fields_ = [("energy_sum", C.c_double), ("energy_sumsq", C.c_double), ("n_sum", C.c_double),
+                ("n_sumsq", C.c_double), ("samples", C.c_longlong), ("attempted", C.c_longlong * 12),
+                ("accepted", C.c_longlong * 12), ("bead_updates", C.c_longlong), ("error", C.c_int),
+                ("pad", C.c_int)]
+
+
 class PgbJobSpec(C.Structure):
     _fields_ = [("n", C.c_int), ("temperature", C.c_double), ("mu", C.c_double),
                 ("density", C.c_double), ("sweeps", C.c_longlong), ("seed", C.c_uint64),
@@ -136,6 +152,14 @@ _SIGS = {
     "pgb_qvectors_shells": (C.c_int, [C.c_double, C.c_double, C.c_int, _DP, C.POINTER(C.c_int),
                                       C.c_int, C.POINTER(C.c_int)]),
     "pgb_plain_get_rng": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
+    "pgb_worm_walkers_create": (C.c_int, [C.POINTER(PgbWormWalkersParams), C.POINTER(C.c_void_p)]),
+    "pgb_worm_walkers_destroy": (C.c_int, [_VP]),
+    "pgb_worm_walkers_last_error": (C.c_char_p, [_VP]),
+    "pgb_worm_walkers_load": (C.c_int, [_VP, C.c_int, _DP]),
+    "pgb_worm_walkers_run": (C.c_int, [_VP, C.c_int]),
+    "pgb_worm_walkers_stats": (C.c_int, [_VP, C.POINTER(PgbWormWalkerStats)]),
+    "pgb_worm_walkers_reset_stats": (C.c_int, [_VP]),
+    "pgb_worm_walkers_get_path": (C.c_int, [_VP, C.c_int, _DP, _IP, _IP, C.POINTER(C.c_uint8), _IP]),
     "pgb_plain_worm_run": (C.c_int, [_VP, C.POINTER(PgbWormParams), C.c_int, _IP, C.c_int,
                                      C.POINTER(C.c_int), _DP, _IP, C.POINTER(PgbWormStats)]),
     "pgb_set_beads": (C.c_int, [_VP, _IP, _DP, _IP, _IP, C.POINTER(C.c_uint8), C.c_int]),
@@ -233,10 +257,12 @@ def u8ptr(a):
     return a.ctypes.data_as(_U8)
 
 
-def check(rc, handle=None, walkers=False, server=False, gp=False):
+def check(rc, handle=None, walkers=False, server=False, gp=False, worm=False):
     if rc != PGB_OK:
         lib = load()
-        if gp:
+        if worm:
+            msg = lib.pgb_worm_walkers_last_error(handle)
+        elif gp:
             msg = lib.pgb_gp_last_error(handle)
         elif server:
             msg = lib.pgb_server_last_error(handle)

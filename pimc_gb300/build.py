@@ -32,7 +32,7 @@ PER_FILE = {
     "gp.cu": ["-fmad=false"],
 }
 SOURCES = ["api.cu", "fp64_kernels.cu", "mixed_kernels.cu", "scatter.cu",
-           "isf_tc.cu", "walkers.cu", "plain_moves.cu", "isf_static.cu", "path_estimators.cu", "gp.cu"]
+           "isf_tc.cu", "walkers.cu", "plain_moves.cu", "isf_static.cu", "path_estimators.cu", "gp.cu", "worm_walkers.cu"]
 
 
 def nvcc():

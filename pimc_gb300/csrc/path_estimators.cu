@@ -16,10 +16,16 @@ constexpr int kEstBlock = 256;
 // in shared memory as FP32; each pair's bin is first found in FP32 and, only
 // when the FP32 quotient lies within kEdge of a bin edge, recomputed from the
 // FP64 positions exactly as the reference does, so every count is the
-// reference's.  The FP32 quotient is within 1e-4 of the exact one for
-// |r| < 100 A (position rounding 2^-24 |r| per coordinate), far inside kEdge.
-// Counts go to per-warp shared histograms, so the result is order-free.
-constexpr int kEdgeMilli = 4;                 // kEdge = 4e-3 of a bin
+// reference's.  Error of the FP32 quotient x = |r| / dSep: a position
+// (|r_d| <= L/2) rounds by at most 2^-24 L, the difference, the minimum image
+// and the sum of squares add a few such roundings, so |r| is off by at most
+// about 2^-20 L; with dSep = sqrt(3) L / 100 that is 100 / (sqrt(3) 2^20)
+// = 5.5e-5 of a bin for any box, plus 3e-6 from 1/dSep: below 6e-5, a third
+// of kEdge.  The FP64 recomputation then runs for about 4e-4 of the pairs:
+// one FP64 warp instruction costs the issue of sixteen FP32 ones on this
+// GPU, so the edge is kept narrow.  Counts go to per-warp shared
+// histograms, so the result is order-free.
+constexpr float kEdge = 2.0e-4f;
 constexpr int kSepWarps = kEstBlock / 32;
 
 __global__ void __launch_bounds__(kEstBlock)
@@ -37,7 +43,7 @@ k_sep_hist(PathView v, int t0, double dSep, unsigned long long* __restrict__ his
     const float Lx = (float)v.side[0], Ly = (float)v.side[1], Lz = (float)v.side[2];
     const float Lix = (float)v.sideInv[0], Liy = (float)v.sideInv[1], Liz = (float)v.sideInv[2];
     const float invSep = (float)(1.0 / dSep);
-    const float edge = kEdgeMilli * 1.0e-3f;
+    const float edge = kEdge;
     for (int b1 = warp; b1 < n - 1; b1 += kSepWarps) {
         const float4 r1 = sp[b1];
         for (int b2 = b1 + 1 + lane; b2 < n; b2 += 32) {
@@ -47,8 +53,11 @@ k_sep_hist(PathView v, int t0, double dSep, unsigned long long* __restrict__ his
             dy -= Ly * rint_add(dy * Liy);
             dz -= Lz * rint_add(dz * Liz);
             const float x = sqrtf(dx * dx + dy * dy + dz * dz) * invSep;
-            int nR = (int)x;
-            const float f = x - (float)nR;
+            // floor(x) without float/int conversions: adding 2^23 rounded
+            // down leaves floor(x) in the mantissa bits, for 0 <= x < 2^22
+            const float xf = __fadd_rd(x, 8388608.0f);
+            int nR = __float_as_int(xf) - 0x4B000000;
+            const float f = x - __fsub_rn(xf, 8388608.0f);
             if (f < edge || f > 1.0f - edge) {
                 const double3 d = sep64(v, t, b2, b1);
                 nR = (int)(sqrt(d.x * d.x + d.y * d.y + d.z * d.z) / dSep);

@@ -142,7 +142,8 @@ cudaError_t launch_slice_terms32(const PathView& v, AzizParams az, int window,
 cudaError_t launch_pos32_from64(const PathView& v, float4* d_pos32,
                                 cudaStream_t s);
 // scatter.cu
-// d_work: rhoq32_work_bytes(v) of scratch for the slices as box fractions
+// d_work: rhoq32_work_bytes(v) of scratch for the slices as box fractions;
+// d_rho must hold nq*M*16 bytes (the second half keeps the wave-vector table)
 size_t rhoq32_work_bytes(const PathView& v);
 cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq,
                           float2* d_rho /* [q][M] */, void* d_work, cudaStream_t s,

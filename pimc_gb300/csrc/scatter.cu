@@ -80,10 +80,28 @@ k_rho_positions_masked(PathView v, double maxR2, float4* __restrict__ uf, int4* 
     if (threadIdx.x == 0) cnt[t] = base;
 }
 
+// Each wave vector in turns per box side, n_d = q_d L_d / 2 pi, once per call
+// (not once per slice in every CTA): FP32 turns with a lattice flag in w, and
+// the integers of lattice vectors (the reference's q lists of lattice type)
+// for the exact fixed-point phase.
+__global__ void k_rho_qsetup(PathView v, const double* __restrict__ q, int nq,
+                             float4* __restrict__ qf, int4* __restrict__ qi) {
+    const int iq = blockIdx.x * blockDim.x + threadIdx.x;
+    if (iq >= nq) return;
+    const double inv2pi = 0.15915494309189533577;
+    const double dx = q[3*iq] * v.side[0] * inv2pi, dy = q[3*iq+1] * v.side[1] * inv2pi,
+                 dz = q[3*iq+2] * v.side[2] * inv2pi;
+    const double rx = rint(dx), ry = rint(dy), rz = rint(dz);
+    const bool lattice = fabs(dx - rx) < 1e-6 && fabs(dy - ry) < 1e-6 && fabs(dz - rz) < 1e-6 &&
+                         fabs(rx) < 1048576.0 && fabs(ry) < 1048576.0 && fabs(rz) < 1048576.0;
+    qf[iq] = make_float4((float)dx, (float)dy, (float)dz, lattice ? 1.f : 0.f);
+    qi[iq] = make_int4(lattice ? (int)rx : 0, lattice ? (int)ry : 0, lattice ? (int)rz : 0, 0);
+}
+
 __global__ void __launch_bounds__(kRhoBlock)
 k_rhoq32(PathView v, const float4* __restrict__ uf, const int4* __restrict__ ui,
-         const int* __restrict__ cnt, const double* __restrict__ q, int nq,
-         float2* __restrict__ rho) {
+         const int* __restrict__ cnt, const float4* __restrict__ qf, const int4* __restrict__ qi,
+         int nq, float2* __restrict__ rho) {
     extern __shared__ float4 su[];
     int4* si = reinterpret_cast<int4*>(su + v.Ne);
     const int t = blockIdx.y;
@@ -95,17 +113,15 @@ k_rhoq32(PathView v, const float4* __restrict__ uf, const int4* __restrict__ ui,
     __syncthreads();
     const int iq = blockIdx.x * kRhoBlock + threadIdx.x;
     if (iq >= nq) return;
-    const double inv2pi = 0.15915494309189533577;
-    const double dx = q[3*iq] * v.side[0] * inv2pi, dy = q[3*iq+1] * v.side[1] * inv2pi,
-                 dz = q[3*iq+2] * v.side[2] * inv2pi;
-    const double rx = rint(dx), ry = rint(dy), rz = rint(dz);
-    // lattice wave vectors (the reference's q lists of lattice type) take the
-    // exact fixed-point phase; any other q the FP32 turn reduction
-    const bool lattice = fabs(dx - rx) < 1e-6 && fabs(dy - ry) < 1e-6 && fabs(dz - rz) < 1e-6 &&
-                         fabs(rx) < 1048576.0 && fabs(ry) < 1048576.0 && fabs(rz) < 1048576.0;
-    rho[(size_t)iq * v.M + t] = lattice
-        ? rho_partial_lattice(si, n, (int)rx, (int)ry, (int)rz)
-        : rho_partial(su, n, (float)dx, (float)dy, (float)dz);
+    // lattice wave vectors take the exact fixed-point phase, any other q the
+    // FP32 turn reduction
+    const float4 f = qf[iq];
+    if (f.w != 0.f) {
+        const int4 k = qi[iq];
+        rho[(size_t)iq * v.M + t] = rho_partial_lattice(si, n, k.x, k.y, k.z);
+    } else {
+        rho[(size_t)iq * v.M + t] = rho_partial(su, n, f.x, f.y, f.z);
+    }
 }
 
 size_t rhoq32_work_bytes(const PathView& v) {
@@ -134,7 +150,13 @@ cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* 
         cudaFuncSetAttribute(k_rhoq32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    k_rhoq32<<<grid, kRhoBlock, smem, s>>>(v, uf, ui, cnt, d_q, nq, d_rho);
+    // the wave-vector table sits in the unused half of the rho region, which
+    // is sized for FP64 values (16 B per (q, slice)); M is even, so it starts
+    // 16-byte aligned
+    float4* qf = reinterpret_cast<float4*>(d_rho + (size_t)nq * v.M);
+    int4* qi = reinterpret_cast<int4*>(qf + nq);
+    k_rho_qsetup<<<(nq + 255) / 256, 256, 0, s>>>(v, d_q, nq, qf, qi);
+    k_rhoq32<<<grid, kRhoBlock, smem, s>>>(v, uf, ui, cnt, qf, qi, nq, d_rho);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,1311 @@
+// worm_walkers.cu -- device-resident worm-algorithm walkers.
+//
+// One warp owns one walker (an independent grand-canonical or windowed
+// canonical He-4 path) and runs the reference's PIMC step on it entirely on
+// the device: the default move list (centre of mass, staging, open, close,
+// insert, remove, advance/recede head and tail, swap head and tail) with the
+// reference's attempt probabilities and diagonal/off-diagonal selection
+// (src/pimc.cpp:120-208, src/constants.cpp:191-205), the move semantics of
+// src/move.cpp:1124-1412, 1710-3826, the Path bookkeeping of
+// src/path.cpp:205-420 and the Worm state of src/worm.cpp:52-118.  The
+// plain form (plain_moves.cu) runs the same moves from the host with FP64
+// device actions and matches the oracle bit for bit; these walkers draw from
+// a Philox stream per walker and evaluate the primitive action in FP32 pair
+// sums reduced in double-float, so they agree with it statistically.
+//
+// Execution model: the move logic runs redundantly and uniformly in all 32
+// lanes (every lane draws the same random numbers and makes the same
+// decisions); scalar state (worm locators, gap, length, counters) lives in
+// registers, identical in every lane; array writes (positions, links,
+// numBeadsAtSlice) are made by lane 0 and published with __syncwarp; pair
+// sums spread a bead's same-slice partners over the lanes.  Links store the
+// partner particle only: next(t, p) is on slice t + 1 and prev on t - 1.
+//
+// Differences from the reference, all documented where they occur:
+//  * the swap pivot is drawn from the pivot slice's beads in index order
+//    (the reference walks its LookupTable hash, whose order depends on the
+//    history of insertions and deletions): the same distribution;
+//  * the Aziz potential is the FP32 analytic form with the reference's
+//    hard-core branch (repulsive term only below x = r/rm = 0.01);
+//  * a slice that outgrows the bead-array capacity stops the walker with an
+//    error (the reference grows its arrays).
+#include "pgb_device.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+namespace pgb {
+
+struct WWMeta {
+    long long off;          // first bead of this walker in the bead arrays
+    int M, Ne, N0, mbar;
+    int num_updates;
+    int window;             // canonical window half-width, -1 none
+    float L, Linv;
+    double tau, lambda, mu, C, volume, tailV0, sqrt2LambdaTau, sqrtLambdaTau, comDelta;
+    uint2 key;
+};
+
+struct WWState {
+    int head[2], tail[2], sp1[2], sp2[2];
+    int gap, length, diag, numBeadsOn;
+    float sep[3];
+    int err;
+    unsigned long long ctr;
+};
+
+struct WB { int t, p; };
+__device__ __forceinline__ bool isXW(WB b) { return b.t < 0; }
+__device__ __forceinline__ bool eqW(WB a, WB b) { return a.t == b.t && a.p == b.p; }
+
+enum { WM_COM = 0, WM_DIAG, WM_OPEN, WM_CLOSE, WM_INSERT, WM_REMOVE, WM_AH, WM_RH, WM_AT, WM_RT,
+       WM_SH, WM_ST, WM_N };
+enum { WERR_FULL = 1, WERR_LINK = 2, WERR_LOOP = 3 };
+
+constexpr int kWWWarps = 4;          // walkers per CTA
+constexpr int kOrigCap = 72;         // saved positions per move (Mbar - 1 <= 63)
+constexpr int kMaxWind = 27;         // (2 maxWind + 1)^3 with maxWind = 1
+
+// Aziz V with the reference's hard-core branch (potential.cpp:1821-1843):
+// below x = 0.01 the attractive part is dropped
+__device__ __forceinline__ float aziz_v32_core(float r2, const AzizF& a) {
+    const float x = sqrtf(r2) * a.rminv;
+    if (x < 0.01f) return a.eps * a.A * __expf(x * fmaf(a.beta, x, -a.alpha));
+    return aziz_v32(r2, a);
+}
+
+struct WormWalker {
+    WWMeta m;
+    AzizF az;
+    float4* pos;
+    int* nxt;
+    int* prv;
+    int* nbs;
+    double* scratch;                 // per-walker tower-sampling scratch, kMaxWind * Ne
+    int lane;
+    // uniform scalar state
+    WB head, tail, sp1, sp2;
+    int gap, length, diag, numBeadsOn;
+    float sep[3];
+    int err;
+    // Philox stream: key per walker, one counter per draw block of four
+    unsigned long long ctr;
+    uint4 buf;
+    int bidx;
+    pgb_worm_walker_stats* acc;
+
+    // ---- random numbers (MTRand's conversions on Philox words) ----
+    __device__ uint32_t u32() {
+        if (bidx == 4) {
+            buf = philox4x32(make_uint4((uint32_t)ctr, (uint32_t)(ctr >> 32), 0x574F524Du, 0u), m.key);
+            ++ctr;
+            bidx = 0;
+        }
+        const int i = bidx++;
+        return i == 0 ? buf.x : i == 1 ? buf.y : i == 2 ? buf.z : buf.w;
+    }
+    __device__ uint32_t randInt(uint32_t n) {
+        uint32_t used = n;
+        used |= used >> 1; used |= used >> 2; used |= used >> 4; used |= used >> 8; used |= used >> 16;
+        uint32_t i;
+        int guard = 0;
+        do { i = u32() & used; } while (i > n && ++guard < 1000);
+        return i > n ? n : i;
+    }
+    __device__ double rand() { return double(u32()) * (1.0 / 4294967295.0); }
+    __device__ double randExc() { return double(u32()) * (1.0 / 4294967296.0); }
+    __device__ double randNorm(double mean, double sd) {
+        double x, y, r;
+        int guard = 0;
+        do { x = 2.0 * rand() - 1.0; y = 2.0 * rand() - 1.0; r = x * x + y * y; }
+        while ((r >= 1.0 || r == 0.0) && ++guard < 1000);
+        if (r >= 1.0 || r == 0.0) return mean;
+        return mean + x * sqrt(-2.0 * log(r) / r) * sd;
+    }
+
+    // ---- path access ----
+    __device__ size_t li(WB b) const { return (size_t)b.t * m.Ne + b.p; }
+    __device__ bool valid(WB b) const { return b.t >= 0 && b.t < m.M && b.p >= 0 && b.p < m.Ne; }
+    __device__ WB next(WB b) {
+        if (!valid(b)) { err = WERR_LINK; return {-1, -1}; }
+        const int p = nxt[li(b)];
+        if (p < 0) return {-1, -1};
+        if (p >= m.Ne) { err = WERR_LINK; return {-1, -1}; }
+        return {b.t + 1 == m.M ? 0 : b.t + 1, p};
+    }
+    __device__ WB prev(WB b) {
+        if (!valid(b)) { err = WERR_LINK; return {-1, -1}; }
+        const int p = prv[li(b)];
+        if (p < 0) return {-1, -1};
+        if (p >= m.Ne) { err = WERR_LINK; return {-1, -1}; }
+        return {b.t == 0 ? m.M - 1 : b.t - 1, p};
+    }
+    __device__ WB nextN(WB b, int n) { for (int i = 0; i < n && !isXW(b); ++i) b = next(b); return b; }
+    __device__ WB prevN(WB b, int n) { for (int i = 0; i < n && !isXW(b); ++i) b = prev(b); return b; }
+    // every access checks its bead: a bad locator sets the error word and
+    // touches no memory
+    __device__ float4 P(WB b) {
+        if (!valid(b)) { err = WERR_LINK; return make_float4(0.f, 0.f, 0.f, 0.f); }
+        return pos[li(b)];
+    }
+    __device__ void setP(WB b, float x, float y, float z) {
+        if (!valid(b)) { err = WERR_LINK; return; }
+        if (lane == 0) pos[li(b)] = make_float4(x, y, z, 0.f);
+        __syncwarp();
+    }
+    // links: the partner's particle index (slice implied)
+    __device__ void setNext(WB b, WB v) {
+        if (!valid(b)) { err = WERR_LINK; return; }
+        if (lane == 0) nxt[li(b)] = isXW(v) ? -1 : v.p;
+        __syncwarp();
+    }
+    __device__ void setPrev(WB b, WB v) {
+        if (!valid(b)) { err = WERR_LINK; return; }
+        if (lane == 0) prv[li(b)] = isXW(v) ? -1 : v.p;
+        __syncwarp();
+    }
+    __device__ int nb(int t) const { return nbs[t]; }
+    __device__ void setNb(int t, int v) { __syncwarp(); if (lane == 0) nbs[t] = v; __syncwarp(); }
+
+    // Worm::getState / factor (worm.h:110-118, worm.cpp:108-118)
+    __device__ int state(WB b) const {
+        if (eqW(b, head) || eqW(b, tail)) return 2;
+        if (eqW(b, sp1) || eqW(b, sp2)) return 1;
+        return 0;
+    }
+    __device__ static float factor(int s1, int s2) {
+        if (s1 == 0 && s2 == 0) return 1.f;
+        if (s1 == 2 && s2 == 2) return 0.f;
+        return 0.5f;
+    }
+    __device__ double putInBC(double x) const { return x - (double)m.L * floor(x * (double)m.Linv + 0.5); }
+
+    // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
+    // tau * sum over the other active beads of the slice of factor * V
+    __device__ double bare(WB b) {
+        if (!valid(b)) { err = WERR_LINK; return 0.0; }
+        const float4 rb = P(b);
+        const int s1 = state(b);
+        const int n = nb(b.t);
+        KahanF k;
+        for (int j = lane; j < n; j += 32) {
+            if (j == b.p) continue;
+            const WB o{b.t, j};
+            const float f = factor(s1, state(o));
+            if (f == 0.f) continue;
+            const float4 rj = pos[(size_t)b.t * m.Ne + j];
+            const float dx = min_image32(rj.x - rb.x, m.L, m.Linv);
+            const float dy = min_image32(rj.y - rb.y, m.L, m.Linv);
+            const float dz = min_image32(rj.z - rb.z, m.L, m.Linv);
+            k.add(f * aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+        }
+        return m.tau * warp_sum_ff(k);
+    }
+    // potentialAction over the active beads from s to e along next links
+    __device__ double rangeAction(WB s, WB e) {
+        double u = 0.0;
+        WB b = s;
+        const WB stop = next(e);
+        for (int g = 0; g <= m.M * m.Ne; ++g) {
+            if (isXW(b) || err) { err = err ? err : WERR_LINK; return u; }
+            if (b.p < nb(b.t)) u += bare(b);
+            b = next(b);
+            if (eqW(b, stop)) return u;
+        }
+        err = WERR_LOOP;
+        return u;
+    }
+    // the primitive action has no gradient correction (gradVFactor = 0)
+    __device__ double corrRange(WB, WB) { return 0.0; }
+
+    // ---- Path bookkeeping (path.cpp:205-420) ----
+    __device__ WB addBead(int slice, double x, double y, double z) {
+        const int k = nb(slice);
+        if (k >= m.Ne) { err = WERR_FULL; return {-1, -1}; }
+        WB last{slice, k};
+        setNb(slice, k + 1);
+        ++numBeadsOn;
+        setNext(last, {-1, -1}); setPrev(last, {-1, -1});
+        setP(last, (float)x, (float)y, (float)z);
+        return last;
+    }
+    __device__ WB addNextBead(WB pb, double x, double y, double z) {
+        const int slice = pb.t + 1 == m.M ? 0 : pb.t + 1;
+        WB b = addBead(slice, x, y, z);
+        if (err) return b;
+        setNext(pb, b); setPrev(b, pb);
+        return b;
+    }
+    __device__ WB addPrevBead(WB nb_, double x, double y, double z) {
+        const int slice = nb_.t == 0 ? m.M - 1 : nb_.t - 1;
+        WB b = addBead(slice, x, y, z);
+        if (err) return b;
+        setPrev(nb_, b); setNext(b, nb_);
+        return b;
+    }
+    __device__ void delBead(WB b) {
+        if (!valid(b)) { err = WERR_LINK; return; }
+        const int k = nb(b.t) - 1;
+        setNb(b.t, k);
+        const WB last{b.t, k};
+        const WB n = next(b), p = prev(b);
+        if (!isXW(n)) setPrev(n, {-1, -1});
+        if (!isXW(p)) setNext(p, {-1, -1});
+        if (b.p < k) {
+            const float4 r = P(last);
+            const WB ln = next(last), lp = prev(last);
+            setP(b, r.x, r.y, r.z);
+            setPrev(b, lp); setNext(b, ln);
+            if (!isXW(ln)) setPrev(ln, b);
+            if (!isXW(lp)) setNext(lp, b);
+            if (eqW(head, last)) head = b;
+            if (eqW(tail, last)) tail = b;
+            if (eqW(sp1, last)) sp1 = b;
+            if (eqW(sp2, last)) sp2 = b;
+        }
+        setNext(last, {-1, -1}); setPrev(last, {-1, -1});
+        --numBeadsOn;
+    }
+    __device__ WB delBeadGetNext(WB b) { WB n = next(b); delBead(b); return n; }
+    __device__ WB delBeadGetPrev(WB b) { WB p = prev(b); delBead(b); return p; }
+
+    // ---- Worm (worm.cpp:52-101, worm.h:68-81) ----
+    __device__ void wormReset() {
+        gap = -1; length = 0; sep[0] = sep[1] = sep[2] = 0.f;
+        head = tail = sp1 = sp2 = WB{-1, -1};
+    }
+    __device__ void wormUpdate(WB nh, WB nt) {
+        head = nh; tail = nt;
+        gap = nt.t - nh.t;
+        if (gap < 0) gap += m.M;
+        WB b = nt;
+        length = 0;
+        do {
+            ++length;
+            b = next(b);
+            if (isXW(b) || length > m.M * m.Ne) { err = WERR_LOOP; break; }
+        } while (!eqW(b, nh));
+        const float4 rt = P(nt), rh = P(nh);
+        sep[0] = (float)putInBC((double)rt.x - rh.x);
+        sep[1] = (float)putInBC((double)rt.y - rh.y);
+        sep[2] = (float)putInBC((double)rt.z - rh.z);
+        setNext(nh, {-1, -1}); setPrev(nt, {-1, -1});
+        sp1 = sp2 = WB{-1, -1};
+    }
+    __device__ bool tooCostly(double sx, double sy, double sz, int g) const {
+        if (g == 0) return true;
+        return ((sx * sx + sy * sy + sz * sz) * (0.25 / (m.lambda * m.tau)) / (1.0 * g)) > 4.0;
+    }
+    __device__ double ensembleWeight(int d) const {
+        if (m.window >= 0) {
+            const int nbp = numBeadsOn + d, nb0 = m.N0 * m.M, w = m.M * m.window;
+            if (nbp > nb0 + w || nbp < nb0 - w) return 0.0;
+        }
+        return 1.0;
+    }
+
+    // ---- sampling helpers (move.cpp:183-488) ----
+    __device__ double rho0(double d2, int L) const {
+        const double norm = pow(4.0 * 3.14159265358979323846 * m.lambda * L * m.tau, -1.5);
+        return norm * exp(-d2 / (4.0 * m.lambda * L * m.tau));
+    }
+    __device__ static int3 winding(int n) {
+        // MoveBase ctor (move.cpp:88-108) with maxWind = 1
+        int3 w;
+        w.x = (n / 9) % 3; w.x -= (w.x > 1) * 3;
+        w.y = (n / 3) % 3; w.y -= (w.y > 1) * 3;
+        w.z = n % 3; w.z -= (w.z > 1) * 3;
+        return w;
+    }
+    // sampleWindingSector (move.cpp:362-397)
+    __device__ int3 sampleWinding(WB sb, WB eb, int L, double& total) {
+        const float4 pe = P(eb), ps = P(sb);
+        const double vx = (double)pe.x - ps.x, vy = (double)pe.y - ps.y, vz = (double)pe.z - ps.z;
+        double cum[kMaxWind];
+        total = 0.0;
+        for (int n = 0; n < kMaxWind; ++n) {
+            const int3 w = winding(n);
+            const double ax = vx + w.x * (double)m.L, ay = vy + w.y * (double)m.L, az_ = vz + w.z * (double)m.L;
+            total += rho0(ax * ax + ay * ay + az_ * az_, L);
+            cum[n] = total;
+        }
+        const double x = rand();
+        int idx = kMaxWind - 1;
+        for (int n = 0; n < kMaxWind; ++n) if (cum[n] / total >= x) { idx = n; break; }
+        return winding(idx);
+    }
+    // newStagingPosition with winding (move.cpp:301-338)
+    __device__ void stagingPos(WB nbd, WB eb, int L, int k, int3& wind, double& x, double& y, double& z) {
+        const double f1 = 1.0 * (L - k - 1), f2 = 1.0 / (1.0 * (L - k));
+        const double sg = m.sqrt2LambdaTau * sqrt(f1 * f2);
+        const float4 np = P(nbd), e = P(eb);
+        double r[3] = {((double)e.x + (double)m.L * wind.x) - np.x, ((double)e.y + (double)m.L * wind.y) - np.y,
+                       ((double)e.z + (double)m.L * wind.z) - np.z};
+        const double n3[3] = {np.x, np.y, np.z};
+        int* wv[3] = {&wind.x, &wind.y, &wind.z};
+        for (int i = 0; i < 3; ++i) { r[i] *= f2; r[i] += n3[i]; }
+        for (int i = 0; i < 3; ++i) r[i] = randNorm(r[i], sg);
+        for (int i = 0; i < 3; ++i) {
+            for (int g = 0; g < 64 && r[i] < -0.5 * m.L; ++g) { ++*wv[i]; r[i] += m.L; }
+            for (int g = 0; g < 64 && r[i] >= 0.5 * m.L; ++g) { --*wv[i]; r[i] -= m.L; }
+        }
+        x = putInBC(r[0]); y = putInBC(r[1]); z = putInBC(r[2]);
+    }
+    __device__ void freePos(WB nbd, double& x, double& y, double& z) {
+        const float4 p = P(nbd);
+        x = putInBC(randNorm(p.x, m.sqrt2LambdaTau));
+        y = putInBC(randNorm(p.y, m.sqrt2LambdaTau));
+        z = putInBC(randNorm(p.z, m.sqrt2LambdaTau));
+    }
+    __device__ bool metro(double dA) { return rand() < exp(-dA); }
+    __device__ int randLen() { return 2 * (1 + (int)randInt((uint32_t)(m.mbar / 2 - 1))); }
+    __device__ int trueN() const { return numBeadsOn / m.M; }
+
+    // ---- diagonal moves ----
+    // CenterOfMassMove (move.cpp:1124-1262)
+    __device__ int com(bool& accepted) {
+        accepted = false;
+        if (numBeadsOn == 0 || nb(0) == 0) return 0;
+        const WB first{0, (int)randInt((uint32_t)(nb(0) - 1))};
+        WB sb = first, eb;
+        if (!isXW(prev(sb))) {
+            for (int g = 0; g <= m.M * m.Ne; ++g) {
+                sb = prev(sb);
+                if (eqW(prev(sb), first) || isXW(prev(sb))) break;
+            }
+        }
+        if (eqW(prev(sb), first)) { sb = first; eb = prev(sb); }
+        else {
+            eb = first;
+            for (int g = 0; g <= m.M * m.Ne && !isXW(next(eb)); ++g) eb = next(eb);
+        }
+        int wl = 0;
+        WB b = sb;
+        const WB stop = next(eb);
+        do { ++wl; b = next(b); } while (!eqW(b, stop) && !isXW(b) && wl <= m.M * m.Ne);
+        if (err || wl > m.M) return 0;
+        acc->attempted[WM_COM]++;
+        double sh[3];
+        for (int i = 0; i < 3; ++i) sh[i] = m.comDelta * (-0.5 + rand());
+        const double oldA = rangeAction(sb, eb);
+        b = sb;
+        for (int g = 0; g < wl; ++g) {
+            const float4 r = P(b);
+            setP(b, (float)putInBC(r.x + sh[0]), (float)putInBC(r.y + sh[1]), (float)putInBC(r.z + sh[2]));
+            b = next(b);
+        }
+        const double newA = rangeAction(sb, eb);
+        if (rand() < exp(-(newA - oldA))) { accepted = true; acc->accepted[WM_COM]++; }
+        else {
+            b = sb;
+            for (int g = 0; g < wl; ++g) {
+                const float4 r = P(b);
+                setP(b, (float)putInBC(r.x - sh[0]), (float)putInBC(r.y - sh[1]), (float)putInBC(r.z - sh[2]));
+                b = next(b);
+            }
+        }
+        return wl;
+    }
+    // StagingMove (move.cpp:1315-1412) with winding sectors
+    __device__ int staging(bool& accepted, float4* orig) {
+        accepted = false;
+        if (numBeadsOn == 0 || trueN() == 0) return 0;
+        WB sb;
+        sb.t = (int)randInt((uint32_t)(m.M - 1));
+        if (nb(sb.t) == 0) return 0;
+        sb.p = (int)randInt((uint32_t)(nb(sb.t) - 1));
+        const int L = 2 + (int)randInt((uint32_t)(m.mbar - 2));
+        WB b = sb;
+        for (int k = 0; k < L; ++k) {
+            if (b.p >= nb(b.t) || isXW(next(b))) return 0;
+            b = next(b);
+        }
+        const WB eb = b;
+        acc->attempted[WM_DIAG]++;
+        double tot;
+        int3 wind = sampleWinding(sb, eb, L, tot);
+        const WB pe = prev(eb);
+        const double oldA = rangeAction(sb, pe);
+        b = sb;
+        int k = 0;
+        do {
+            b = next(b);
+            if (k >= kOrigCap) { err = WERR_LOOP; return 0; }
+            orig[k] = P(b);
+            double x, y, z;
+            stagingPos(prev(b), eb, L, k, wind, x, y, z);
+            setP(b, (float)x, (float)y, (float)z);
+            ++k;
+        } while (!eqW(b, pe) && k < L);
+        const double newA = rangeAction(sb, pe);
+        if (rand() < exp(-(newA - oldA))) { accepted = true; acc->accepted[WM_DIAG]++; }
+        else {
+            b = sb;
+            for (int i = 0; i < k; ++i) { b = next(b); setP(b, orig[i].x, orig[i].y, orig[i].z); }
+        }
+        return L - 1;
+    }
+
+    // ---- worm moves (move.cpp:1736-3826), local-action branches ----
+    __device__ int open() {
+        if (numBeadsOn == 0 || trueN() == 0) return -1;
+        const int gapLength = randLen();
+        WB hb, tb;
+        hb.t = 2 * (int)randInt((uint32_t)(m.M / 2 - 1));
+        if (nb(hb.t) == 0) return -1;
+        hb.p = (int)randInt((uint32_t)(nb(hb.t) - 1));
+        tb = nextN(hb, gapLength);
+        if (isXW(tb)) return -1;
+        double totalrho0;
+        const int3 wind = sampleWinding(hb, tb, gapLength, totalrho0);
+        const float4 pt = P(tb), ph = P(hb);
+        const double sx = ((double)pt.x - ph.x) + wind.x * (double)m.L;
+        const double sy = ((double)pt.y - ph.y) + wind.y * (double)m.L;
+        const double sz = ((double)pt.z - ph.z) + wind.z * (double)m.L;
+        if (tooCostly(sx, sy, sz, gapLength)) return -1;
+        double norm = (m.C * m.mbar * numBeadsOn) / totalrho0;
+        norm *= 0.15 / 0.4;
+        norm *= ensembleWeight(-gapLength + 1);
+        const double muShift = gapLength * m.mu * m.tau;
+        acc->attempted[WM_OPEN]++;
+        sp1 = hb; sp2 = tb;
+        const double actionShift = (-log(norm) + muShift) / gapLength;
+        double factor = 0.5;
+        WB b = hb;
+        for (int g = 0; g <= m.M * m.Ne; ++g) {
+            acc->bead_updates++;
+            const double dA = -(bare(b) - factor * actionShift);
+            if (!metro(dA)) { wormReset(); diag = 1; return 0; }
+            factor = 1.0;
+            b = next(b);
+            if (eqW(b, tb) || isXW(b)) break;
+        }
+        acc->bead_updates++;
+        double dA = -(bare(tb) - 0.5 * actionShift);
+        dA -= corrRange(hb, tb);
+        if (metro(dA)) {
+            acc->accepted[WM_OPEN]++;
+            b = next(hb);
+            for (int g = 0; g <= m.M && !eqW(b, tb) && !isXW(b); ++g) b = delBeadGetNext(b);
+            wormUpdate(hb, tb);
+            diag = 0;
+            return 1;
+        }
+        wormReset(); diag = 1;
+        return 0;
+    }
+    __device__ void closeUndo() {
+        WB b = next(head);
+        for (int g = 0; g <= m.M && !eqW(b, tail) && !isXW(b); ++g) b = delBeadGetNext(b);
+        setNext(head, {-1, -1}); setPrev(tail, {-1, -1});
+        diag = 0;
+    }
+    __device__ int close() {
+        if (numBeadsOn == 0) return -1;
+        if (gap > m.mbar || gap == 0 || tooCostly(sep[0], sep[1], sep[2], gap)) return -1;
+        acc->attempted[WM_CLOSE]++;
+        const int g0 = gap;
+        double totalrho0;
+        int3 wind = sampleWinding(head, tail, g0, totalrho0);
+        double norm = totalrho0 / (m.C * m.mbar * (numBeadsOn + g0 - 1));
+        norm *= 0.4 / 0.15;
+        norm *= ensembleWeight(g0 - 1);
+        const double muShift = g0 * m.mu * m.tau;
+        const double actionShift = (log(norm) + muShift) / g0;
+        WB b = head;
+        acc->bead_updates++;
+        double dA = bare(b) - 0.5 * actionShift;
+        if (!metro(dA)) { closeUndo(); return 0; }
+        for (int k = 0; k < g0 - 1; k++) {
+            double x, y, z;
+            stagingPos(b, tail, g0, k, wind, x, y, z);
+            b = addNextBead(b, x, y, z);
+            if (err) return -2;
+            acc->bead_updates++;
+            dA = bare(b) - actionShift;
+            if (!metro(dA)) { closeUndo(); return 0; }
+        }
+        setNext(b, tail); setPrev(tail, b);
+        acc->bead_updates++;
+        dA = bare(tail) - 0.5 * actionShift;
+        dA += corrRange(head, tail);
+        if (metro(dA)) { acc->accepted[WM_CLOSE]++; wormReset(); diag = 1; return 1; }
+        closeUndo();
+        return 0;
+    }
+    __device__ void insertUndo(WB tb) {
+        WB b = tb;
+        for (int g = 0; g <= m.M + 1 && !isXW(b); ++g) b = delBeadGetNext(b);
+        wormReset(); diag = 1;
+    }
+    __device__ int insert() {
+        const int wl = randLen();
+        acc->attempted[WM_INSERT]++;
+        double norm = m.C * m.mbar * m.M * m.volume;
+        const double muShift = wl * m.tau * m.mu;
+        norm *= 0.15 / 0.4;
+        norm *= ensembleWeight(wl);
+        if (norm < 2.220446049250313e-16) return 0;
+        const int slice = 2 * (int)randInt((uint32_t)(m.M / 2 - 1));
+        const double x0 = m.L * (-0.5 + randExc()), y0 = m.L * (-0.5 + randExc()), z0 = m.L * (-0.5 + randExc());
+        const WB tb = addBead(slice, x0, y0, z0);
+        if (err) return -2;
+        sp2 = tb;
+        const double actionShift = (log(norm) + muShift) / wl;
+        WB b = tb;
+        acc->bead_updates++;
+        double dA = bare(b) - 0.5 * actionShift;
+        if (!metro(dA)) { insertUndo(tb); return 0; }
+        for (int k = 1; k < wl; k++) {
+            double x, y, z;
+            freePos(b, x, y, z);
+            b = addNextBead(b, x, y, z);
+            if (err) return -2;
+            acc->bead_updates++;
+            dA = bare(b) - actionShift;
+            if (!metro(dA)) { insertUndo(tb); return 0; }
+        }
+        double x, y, z;
+        freePos(b, x, y, z);
+        const WB hb = addNextBead(b, x, y, z);
+        if (err) return -2;
+        sp1 = hb;
+        acc->bead_updates++;
+        dA = bare(hb) - 0.5 * actionShift;
+        dA += corrRange(tb, hb);
+        if (metro(dA)) { acc->accepted[WM_INSERT]++; wormUpdate(hb, tb); diag = 0; return 1; }
+        insertUndo(tb);
+        return 0;
+    }
+    __device__ int remove() {
+        if (length > m.mbar || length < 1) return -1;
+        acc->attempted[WM_REMOVE]++;
+        double norm = 1.0 / (m.C * m.mbar * m.M * m.volume);
+        const double muShift = length * m.mu * m.tau;
+        norm *= 0.4 / 0.15;
+        norm *= ensembleWeight(-length);
+        if (norm < 2.220446049250313e-16) return 0;
+        const double actionShift = (-log(norm) + muShift) / length;
+        WB b = head;
+        double factor = 0.5;
+        for (int g = 0; g <= m.M * m.Ne; ++g) {
+            acc->bead_updates++;
+            const double dA = -(bare(b) - factor * actionShift);
+            if (!metro(dA)) { diag = 0; return 0; }
+            factor = 1.0;
+            b = prev(b);
+            if (eqW(b, tail) || isXW(b)) break;
+        }
+        acc->bead_updates++;
+        double dA = -(bare(tail) - 0.5 * actionShift);
+        dA -= corrRange(tail, head);
+        if (metro(dA)) {
+            acc->accepted[WM_REMOVE]++;
+            b = head;
+            for (int g = 0; g <= m.M * m.Ne && !isXW(b); ++g) b = delBeadGetPrev(b);
+            wormReset(); diag = 1;
+            return 1;
+        }
+        diag = 0;
+        return 0;
+    }
+    __device__ void ahUndo() {
+        head = sp1;
+        WB b = next(head);
+        for (int g = 0; g <= m.M && !isXW(b); ++g) b = delBeadGetNext(b);
+        setNext(head, {-1, -1});
+        diag = 0;
+        sp1 = WB{-1, -1};
+    }
+    __device__ int advanceHead() {
+        if (numBeadsOn == 0) return -1;
+        const int al = randLen();
+        acc->attempted[WM_AH]++;
+        const double muShift = al * m.tau * m.mu;
+        double norm = 1.0;
+        norm *= ensembleWeight(al);
+        sp1 = head; head = WB{-1, -1};
+        const double actionShift = (log(norm) + muShift) / al;
+        WB b = sp1;
+        acc->bead_updates++;
+        double dA = bare(b) - 0.5 * actionShift;
+        if (!metro(dA)) { ahUndo(); return 0; }
+        for (int k = 0; k < al - 1; k++) {
+            double x, y, z;
+            freePos(b, x, y, z);
+            b = addNextBead(b, x, y, z);
+            if (err) return -2;
+            acc->bead_updates++;
+            dA = bare(b) - actionShift;
+            if (!metro(dA)) { ahUndo(); return 0; }
+        }
+        double x, y, z;
+        freePos(b, x, y, z);
+        const WB hb = addNextBead(b, x, y, z);
+        if (err) return -2;
+        head = hb;
+        acc->bead_updates++;
+        dA = bare(hb) - 0.5 * actionShift;          // potentialAction(head): primitive
+        dA += corrRange(sp1, head);
+        if (metro(dA)) { acc->accepted[WM_AH]++; wormUpdate(hb, tail); diag = 0; return 1; }
+        ahUndo();
+        return 0;
+    }
+    __device__ int advanceTail() {
+        if (numBeadsOn == 0) return -1;
+        const int al = randLen();
+        if (!(al < length)) return -1;
+        const WB tb = nextN(tail, al);
+        if (isXW(tb)) return -1;
+        const double muShift = al * m.tau * m.mu;
+        double norm = 1.0;
+        norm *= ensembleWeight(-al);
+        acc->attempted[WM_AT]++;
+        sp1 = tb;
+        const double actionShift = (-log(norm) + muShift) / al;
+        double factor = 0.5;
+        WB b = tail;
+        for (int g = 0; g <= m.M * m.Ne; ++g) {
+            acc->bead_updates++;
+            const double dA = -(bare(b) - factor * actionShift);
+            if (!metro(dA)) { diag = 0; sp1 = WB{-1, -1}; return 0; }
+            factor = 1.0;
+            b = next(b);
+            if (eqW(b, tb) || isXW(b)) break;
+        }
+        acc->bead_updates++;
+        double dA = -(bare(b) - 0.5 * actionShift);
+        dA -= corrRange(tail, tb);
+        if (metro(dA)) {
+            acc->accepted[WM_AT]++;
+            b = prev(tb);
+            for (int g = 0; g <= m.M * m.Ne && !isXW(b); ++g) b = delBeadGetPrev(b);
+            wormUpdate(head, tb);
+            diag = 0;
+            return 1;
+        }
+        diag = 0; sp1 = WB{-1, -1};
+        return 0;
+    }
+    __device__ int recedeHead() {
+        if (numBeadsOn == 0) return -1;
+        const int rl = randLen();
+        if (!(rl < length)) return -1;
+        const WB hb = prevN(head, rl);
+        if (isXW(hb)) return -1;
+        const double muShift = rl * m.tau * m.mu;
+        double norm = 1.0;
+        norm *= ensembleWeight(-rl);
+        acc->attempted[WM_RH]++;
+        sp1 = hb;
+        const double actionShift = (-log(norm) + muShift) / rl;
+        double factor = 0.5;
+        WB b = head;
+        for (int g = 0; g <= m.M * m.Ne; ++g) {
+            acc->bead_updates++;
+            const double dA = -(bare(b) - factor * actionShift);
+            if (!metro(dA)) { diag = 0; sp1 = WB{-1, -1}; return 0; }
+            factor = 1.0;
+            b = prev(b);
+            if (eqW(b, hb) || isXW(b)) break;
+        }
+        acc->bead_updates++;
+        double dA = -(bare(hb) - 0.5 * actionShift);
+        dA -= corrRange(sp1, head);
+        if (metro(dA)) {
+            acc->accepted[WM_RH]++;
+            b = next(hb);
+            for (int g = 0; g <= m.M * m.Ne && !isXW(b); ++g) b = delBeadGetNext(b);
+            wormUpdate(hb, tail);
+            diag = 0;
+            return 1;
+        }
+        diag = 0; sp1 = WB{-1, -1};
+        return 0;
+    }
+    __device__ void rtUndo() {
+        tail = sp1;
+        WB b = prev(tail);
+        for (int g = 0; g <= m.M && !isXW(b); ++g) b = delBeadGetPrev(b);
+        setPrev(tail, {-1, -1});
+        diag = 0;
+        sp1 = WB{-1, -1};
+    }
+    __device__ int recedeTail() {
+        if (numBeadsOn == 0) return -1;
+        const int rl = randLen();
+        acc->attempted[WM_RT]++;
+        const double muShift = rl * m.tau * m.mu;
+        double norm = 1.0;
+        norm *= ensembleWeight(rl);
+        sp1 = tail; tail = WB{-1, -1};
+        const double actionShift = (log(norm) + muShift) / rl;
+        WB b = sp1;
+        acc->bead_updates++;
+        double dA = bare(b) - 0.5 * actionShift;
+        if (!metro(dA)) { rtUndo(); return 0; }
+        for (int k = 0; k < rl - 1; k++) {
+            double x, y, z;
+            freePos(b, x, y, z);
+            b = addPrevBead(b, x, y, z);
+            if (err) return -2;
+            acc->bead_updates++;
+            dA = bare(b) - actionShift;
+            if (!metro(dA)) { rtUndo(); return 0; }
+        }
+        double x, y, z;
+        freePos(b, x, y, z);
+        const WB tb = addPrevBead(b, x, y, z);
+        if (err) return -2;
+        tail = tb;
+        acc->bead_updates++;
+        dA = bare(tb) - 0.5 * actionShift;
+        dA += corrRange(tb, sp1);
+        if (metro(dA)) { acc->accepted[WM_RT]++; wormUpdate(head, tb); diag = 0; return 1; }
+        rtUndo();
+        return 0;
+    }
+    // SwapMoveBase::getNorm + selectPivotBead (move.cpp:3223-3330) over the
+    // pivot slice's beads in index order: weights rho0 for every bead and
+    // winding sector, a warp-parallel tower.  Returns Sigma; with x >= 0 the
+    // pivot and its winding sector are selected for the uniform deviate x.
+    __device__ double towerNorm(WB b, int pivotSlice, int sign, double x, WB& pivot, int3& wind) {
+        const int nL = nb(pivotSlice);
+        const int total = nL * kMaxWind;
+        const float4 pb = P(b);
+        // weights in the reference's order: n fastest, winding sector slowest
+        double sum = 0.0;
+        for (int i = lane; i < total; i += 32) {
+            const int w = i / nL, n = i - w * nL;
+            const int3 wv = winding(w);
+            const float4 pf = pos[(size_t)pivotSlice * m.Ne + n];
+            double sx = (double)pf.x - pb.x, sy = (double)pf.y - pb.y, sz = (double)pf.z - pb.z;
+            if (w > 0) { sx += (sign * wv.x) * (double)m.L; sy += (sign * wv.y) * (double)m.L; sz += (sign * wv.z) * (double)m.L; }
+            const double r = rho0(sx * sx + sy * sy + sz * sz, m.mbar);
+            scratch[i] = r;
+            sum += r;
+        }
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        __syncwarp();
+        if (x >= 0.0) {
+            // first index whose cumulative weight reaches x * Sigma
+            const double target = x * sum;
+            double carry = 0.0;
+            int found = total - 1;
+            for (int base = 0; base < total; base += 32) {
+                const int i = base + lane;
+                double v = i < total ? scratch[i] : 0.0;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const double u = __shfl_up_sync(0xffffffffu, v, o);
+                    if (lane >= o) v += u;
+                }
+                const double cum = carry + v;
+                const unsigned hit = __ballot_sync(0xffffffffu, i < total && cum >= target);
+                if (hit) { found = base + __ffs(hit) - 1; break; }
+                carry += __shfl_sync(0xffffffffu, v, 31);
+            }
+            const int w = found / nL, n = found - w * nL;
+            pivot = WB{pivotSlice, n};
+            wind = winding(w);
+        }
+        return sum;
+    }
+    __device__ int swapHead(float4* orig) {
+        if (numBeadsOn == 0 || diag) return -1;
+        const int swapLength = m.mbar;
+        int pivotSlice = head.t + swapLength;
+        if (pivotSlice >= m.M) pivotSlice -= m.M;
+        if (nb(pivotSlice) == 0) return -1;
+        WB pivot; int3 wind;
+        const double SigmaHead = towerNorm(head, pivotSlice, 1, rand(), pivot, wind);
+        WB b = pivot;
+        for (int k = 0; k < swapLength; k++) {
+            if (eqW(b, tail) || isXW(b)) return -1;
+            b = prev(b);
+        }
+        const WB swp = b;
+        if (isXW(swp) || eqW(tail, swp)) return -1;
+        acc->attempted[WM_SH]++;
+        WB dummy; int3 dw;
+        const double SigmaSwap = towerNorm(swp, pivotSlice, 1, -1.0, dummy, dw);
+        const double PNorm = fmin(SigmaHead / SigmaSwap, 1.0);
+        if (rand() < PNorm) {
+            sp1 = swp; sp2 = pivot;
+            int k = 0;
+            b = swp;
+            const WB stopB = next(pivot);
+            for (int g = 0; g <= m.M; ++g) {
+                if (!eqW(b, swp) && !eqW(b, pivot) && k < kOrigCap) orig[k++] = P(b);
+                b = next(b);
+                if (eqW(b, stopB) || isXW(b)) break;
+            }
+            const double oldA = rangeAction(swp, pivot);
+            const WB nextSwap = next(swp);
+            setNext(head, nextSwap);
+            setNext(swp, {-1, -1});
+            setPrev(nextSwap, head);
+            sp1 = head;
+            head = swp;
+            b = sp1;
+            k = 0;
+            for (int g = 0; g <= m.M; ++g) {
+                if (!eqW(b, sp1) && !eqW(b, pivot)) {
+                    double x, y, z;
+                    stagingPos(prev(b), pivot, swapLength, k, wind, x, y, z);
+                    setP(b, (float)x, (float)y, (float)z);
+                    ++k;
+                    acc->bead_updates++;
+                }
+                b = next(b);
+                if (eqW(b, stopB) || isXW(b)) break;
+            }
+            const double newA = rangeAction(sp1, pivot);
+            if (metro(newA - oldA)) { acc->accepted[WM_SH]++; wormUpdate(swp, tail); return 1; }
+            head = sp1;
+            setNext(head, {-1, -1});
+            setNext(swp, nextSwap);
+            setPrev(nextSwap, swp);
+            b = next(swp);
+            k = 0;
+            for (int g = 0; g <= m.M && !eqW(b, pivot) && !isXW(b) && k < kOrigCap; ++g) {
+                setP(b, orig[k].x, orig[k].y, orig[k].z);
+                ++k;
+                b = next(b);
+            }
+            diag = 0;
+            sp1 = sp2 = WB{-1, -1};
+            return 0;
+        }
+        return 0;
+    }
+    __device__ int swapTail(float4* orig) {
+        if (numBeadsOn == 0 || diag) return -1;
+        const int swapLength = m.mbar;
+        int pivotSlice = tail.t - swapLength;
+        if (pivotSlice < 0) pivotSlice += m.M;
+        if (nb(pivotSlice) == 0) return -1;
+        WB pivot; int3 wind;
+        const double SigmaTail = towerNorm(tail, pivotSlice, -1, rand(), pivot, wind);
+        WB b = pivot;
+        for (int k = 0; k < swapLength; k++) {
+            if (eqW(b, head) || isXW(b)) return -1;
+            b = next(b);
+        }
+        const WB swp = b;
+        if (isXW(swp) || eqW(head, swp)) return -1;
+        acc->attempted[WM_ST]++;
+        WB dummy; int3 dw;
+        const double SigmaSwap = towerNorm(swp, pivotSlice, 1, -1.0, dummy, dw);
+        const double PNorm = fmin(SigmaTail / SigmaSwap, 1.0);
+        if (rand() < PNorm) {
+            sp1 = swp; sp2 = pivot;
+            int k = 0;
+            b = pivot;
+            const WB stopB = next(swp);
+            for (int g = 0; g <= m.M; ++g) {
+                if (!eqW(b, swp) && !eqW(b, pivot) && k < kOrigCap) orig[k++] = P(b);
+                b = next(b);
+                if (eqW(b, stopB) || isXW(b)) break;
+            }
+            const double oldA = rangeAction(pivot, swp);
+            const WB prevSwap = prev(swp);
+            setPrev(tail, prevSwap);
+            setPrev(swp, {-1, -1});
+            setNext(prevSwap, tail);
+            sp1 = tail;
+            tail = swp;
+            const WB s1 = sp1;
+            const WB stop2 = next(s1);
+            k = 0;
+            b = pivot;
+            for (int g = 0; g <= m.M; ++g) {
+                if (!eqW(b, s1) && !eqW(b, pivot)) {
+                    double x, y, z;
+                    stagingPos(prev(b), s1, swapLength, k, wind, x, y, z);
+                    setP(b, (float)x, (float)y, (float)z);
+                    ++k;
+                    acc->bead_updates++;
+                }
+                b = next(b);
+                if (eqW(b, stop2) || isXW(b)) break;
+            }
+            const double newA = rangeAction(pivot, s1);
+            if (metro(newA - oldA)) { acc->accepted[WM_ST]++; wormUpdate(head, swp); return 1; }
+            tail = s1;
+            setPrev(tail, {-1, -1});
+            setPrev(swp, prevSwap);
+            setNext(prevSwap, swp);
+            b = next(pivot);
+            k = 0;
+            for (int g = 0; g <= m.M && !eqW(b, swp) && !isXW(b) && k < kOrigCap; ++g) {
+                setP(b, orig[k].x, orig[k].y, orig[k].z);
+                ++k;
+                b = next(b);
+            }
+            sp1 = sp2 = WB{-1, -1};
+            diag = 0;
+            return 0;
+        }
+        return 0;
+    }
+
+    // EnergyEstimator (estimator.cpp:940-1029), primitive action, E/N of a
+    // closed configuration: kinetic term over every bead's next link,
+    // potential over the pairs of every slice, the rc = L tail
+    __device__ double energy(int& N) {
+        N = numBeadsOn / m.M;
+        KahanF pot, kin;
+        for (int t = 0; t < m.M; ++t) {
+            const int n = nb(t);
+            const int tn = t + 1 == m.M ? 0 : t + 1;
+            for (int q = lane; q < n * n; q += 32) {
+                const int i = q / n, j = q - i * n;
+                const float4 ri = pos[(size_t)t * m.Ne + i];
+                if (j == 0) {
+                    const int pn = nxt[(size_t)t * m.Ne + i];
+                    if (pn >= 0 && pn < m.Ne) {
+                        const float4 rn = pos[(size_t)tn * m.Ne + pn];
+                        const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
+                        const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
+                        const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
+                        kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+                    }
+                }
+                if (j <= i) continue;
+                const float4 rj = pos[(size_t)t * m.Ne + j];
+                const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
+                const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
+                const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
+                pot.add(aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+            }
+        }
+        const double V = warp_sum_ff(pot), K2 = warp_sum_ff(kin);
+        if (N <= 0) return 0.0;
+        const double totK = 1.5 * N / m.tau - K2 * ((0.25 / (m.lambda * m.tau)) / (m.tau * m.M));
+        const double totV = V / m.M + (1.0 * N * N / m.volume) * m.tailV0;
+        return (totK + totV) / N;
+    }
+};
+
+
+__global__ void __launch_bounds__(kWWWarps * 32)
+k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* __restrict__ nxt,
+               int* __restrict__ prv, int* __restrict__ nbs, const long long* __restrict__ nbs_off,
+               WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
+               double* __restrict__ scratch, const long long* __restrict__ scratch_off,
+               AzizF az, int W, int sweeps) {
+    __shared__ float4 s_orig[kWWWarps][kOrigCap];
+    const int warp = threadIdx.x >> 5;
+    const int w = blockIdx.x * kWWWarps + warp;
+    if (w >= W) return;
+    WormWalker ww;
+    ww.m = meta[w];
+    ww.az = az;
+    ww.lane = threadIdx.x & 31;
+    ww.pos = pos + ww.m.off;
+    ww.nxt = nxt + ww.m.off;
+    ww.prv = prv + ww.m.off;
+    ww.nbs = nbs + nbs_off[w];
+    ww.scratch = scratch + scratch_off[w];
+    ww.acc = &stats[w];
+    const WWState st = states[w];
+    if (st.err) return;
+    ww.head = WB{st.head[0], st.head[1]}; ww.tail = WB{st.tail[0], st.tail[1]};
+    ww.sp1 = WB{st.sp1[0], st.sp1[1]}; ww.sp2 = WB{st.sp2[0], st.sp2[1]};
+    ww.gap = st.gap; ww.length = st.length; ww.diag = st.diag; ww.numBeadsOn = st.numBeadsOn;
+    ww.sep[0] = st.sep[0]; ww.sep[1] = st.sep[1]; ww.sep[2] = st.sep[2];
+    ww.err = 0;
+    ww.ctr = st.ctr; ww.bidx = 4;
+    // per-walker counters accumulate in a register copy, lane 0 writes back
+    pgb_worm_walker_stats local = stats[w];
+    ww.acc = &local;
+    // cumulative probabilities over the default move list (pimc.cpp:120-152)
+    const double prob[WM_N] = {0.01, 0.19, 0.4, 0.15, 0.4, 0.15, 0.075, 0.075, 0.075, 0.075, 0.1, 0.1};
+    const int onDiag[WM_N] = {1, 1, 1, 0, 1, 0, 0, 0, 0, 0, 0, 0};
+    double cumD[WM_N], cumO[WM_N], cd = 0.0, co = 0.0;
+    for (int i = 0; i < WM_N; ++i) {
+        if (onDiag[i]) cd += prob[i];
+        cumD[i] = cd;
+        if (!onDiag[i] || i < 2) co += prob[i];
+        cumO[i] = co;
+    }
+    cumD[WM_N - 1] = 1.0 + 1e-7;
+    cumO[WM_N - 1] = 1.0 + 1e-7;
+    float4* orig = s_orig[warp];
+    for (int sw = 0; sw < sweeps && !ww.err; ++sw) {
+        for (int u = 0; u < ww.m.num_updates && !ww.err; ++u) {
+            const double x = ww.rand();
+            const double* cum = ww.diag ? cumD : cumO;
+            int index = WM_N - 1;
+            for (int i = 0; i < WM_N; ++i) if (cum[i] >= x) { index = i; break; }
+            bool acc = false;
+            int moved = 0;
+            switch (index) {
+                case WM_COM: moved = ww.com(acc); local.bead_updates += moved; break;
+                case WM_DIAG: moved = ww.staging(acc, orig); local.bead_updates += moved; break;
+                case WM_OPEN: ww.open(); break;
+                case WM_CLOSE: ww.close(); break;
+                case WM_INSERT: ww.insert(); break;
+                case WM_REMOVE: ww.remove(); break;
+                case WM_AH: ww.advanceHead(); break;
+                case WM_RH: ww.recedeHead(); break;
+                case WM_AT: ww.advanceTail(); break;
+                case WM_RT: ww.recedeTail(); break;
+                case WM_SH: ww.swapHead(orig); break;
+                case WM_ST: ww.swapTail(orig); break;
+            }
+        }
+        if (!ww.err && ww.diag) {
+            int N;
+            const double e = ww.energy(N);
+            local.samples += 1;
+            local.energy_sum += e;
+            local.energy_sumsq += e * e;
+            local.n_sum += N;
+            local.n_sumsq += 1.0 * N * N;
+        }
+    }
+    __syncwarp();
+    if (ww.lane == 0) {
+        WWState o;
+        o.head[0] = ww.head.t; o.head[1] = ww.head.p; o.tail[0] = ww.tail.t; o.tail[1] = ww.tail.p;
+        o.sp1[0] = ww.sp1.t; o.sp1[1] = ww.sp1.p; o.sp2[0] = ww.sp2.t; o.sp2[1] = ww.sp2.p;
+        o.gap = ww.gap; o.length = ww.length; o.diag = ww.diag; o.numBeadsOn = ww.numBeadsOn;
+        o.sep[0] = ww.sep[0]; o.sep[1] = ww.sep[1]; o.sep[2] = ww.sep[2];
+        o.err = ww.err; o.ctr = ww.ctr;
+        states[w] = o;
+        local.error = ww.err;
+        stats[w] = local;
+    }
+}
+
+}  // namespace pgb
+
+// --------------------------------------------------------------------------
+// host side
+// --------------------------------------------------------------------------
+using namespace pgb;
+
+struct pgb_worm_walkers {
+    int W = 0;
+    std::vector<WWMeta> meta;
+    std::vector<long long> nbs_off, scratch_off;
+    long long total_beads = 0, total_slices = 0, total_scratch = 0;
+    WWMeta* d_meta = nullptr;
+    float4* d_pos = nullptr;
+    int *d_nxt = nullptr, *d_prv = nullptr, *d_nbs = nullptr;
+    long long *d_nbs_off = nullptr, *d_scratch_off = nullptr;
+    WWState* d_state = nullptr;
+    pgb_worm_walker_stats* d_stats = nullptr;
+    double* d_scratch = nullptr;
+    AzizF az{};
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int cfail(cudaError_t e, const char* where) {
+        err = std::string("CUDA error ") + cudaGetErrorString(e) + " at " + where;
+        return e == cudaErrorMemoryAllocation ? PGB_ENOMEM : PGB_ECUDA;
+    }
+};
+
+namespace {
+thread_local std::string g_wwerr;
+}
+
+extern "C" {
+
+const char* pgb_worm_walkers_last_error(const pgb_worm_walkers* h) { return h ? h->err.c_str() : g_wwerr.c_str(); }
+
+int pgb_worm_walkers_destroy(pgb_worm_walkers* h) {
+    if (!h) return PGB_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->d_meta); cudaFree(h->d_pos); cudaFree(h->d_nxt); cudaFree(h->d_prv); cudaFree(h->d_nbs);
+    cudaFree(h->d_nbs_off); cudaFree(h->d_scratch_off); cudaFree(h->d_state); cudaFree(h->d_stats);
+    cudaFree(h->d_scratch);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers** out) {
+    if (!out) return PGB_EINVAL;
+    *out = nullptr;
+    if (!p || p->num_walkers <= 0 || !p->num_ptcl || !p->num_slices || !p->side || !p->mbar ||
+        !p->capacity || !(p->tau > 0) || !(p->lambda > 0) || !(p->worm_constant > 0)) {
+        g_wwerr = "worm_walkers_create: walker arrays, tau, lambda and C0 are required";
+        return PGB_EINVAL;
+    }
+    int dev = 0;
+    if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) {
+        cudaGetLastError();
+        g_wwerr = "worm_walkers_create: no CUDA device";
+        return PGB_ECUDA;
+    }
+    pgb_worm_walkers* h = new pgb_worm_walkers();
+    h->W = p->num_walkers;
+    const AzizParams ap = aziz_params(p->aziz_year ? p->aziz_year : 1979);
+    h->az = make_aziz_f(ap);
+    long long off = 0, soff = 0, scoff = 0;
+    for (int w = 0; w < h->W; ++w) {
+        const int N = p->num_ptcl[w], M = p->num_slices[w], mb = p->mbar[w], ne = p->capacity[w];
+        const double L = p->side[w];
+        if (N < 1 || M < 4 || M % 2 || mb < 2 || mb % 2 || mb >= M || mb > 64 || ne < N || ne > 4096 || !(L > 0)) {
+            g_wwerr = "worm walker " + std::to_string(w) + ": need N >= 1, even M >= 4, even 2 <= Mbar < M, "
+                      "Mbar <= 64, N <= capacity <= 4096, L > 0";
+            pgb_worm_walkers_destroy(h);
+            return PGB_EINVAL;
+        }
+        WWMeta m{};
+        m.off = off; m.M = M; m.Ne = ne; m.N0 = N; m.mbar = mb;
+        int nu = (int)std::ceil(std::max(N, 1) * M / (1.0 * mb));
+        m.num_updates = nu < 100 ? 100 : nu;
+        m.window = p->window;
+        m.L = (float)L; m.Linv = (float)(1.0 / L);
+        m.tau = p->tau; m.lambda = p->lambda; m.mu = p->mu ? p->mu[w] : 0.0;
+        m.volume = L * L * L;
+        m.C = p->worm_constant / (1.0 * mb * M * m.volume);
+        const double rmorc = ap.rm / L;
+        const double t2 = ap.C6 * std::pow(rmorc, 3.0) / 3.0, t3 = ap.C8 * std::pow(rmorc, 5.0) / 5.0,
+                     t4 = ap.C10 * std::pow(rmorc, 7.0) / 7.0;
+        m.tailV0 = 2.0 * M_PI * ap.epsilon * (-ap.rm * ap.rm * ap.rm * (t2 + t3 + t4));
+        m.sqrtLambdaTau = std::sqrt(p->lambda * p->tau);
+        m.sqrt2LambdaTau = std::sqrt(2.0) * m.sqrtLambdaTau;
+        const double T = 1.0 / (M * p->tau);
+        m.comDelta = 0.04 * 2.0 * std::sqrt(M_PI * p->lambda / T);
+        const uint64_t s = p->seed * 0x9E3779B97F4A7C15ull + (uint64_t)w * 0xBF58476D1CE4E5B9ull + 0x94D049BB133111EBull;
+        m.key = make_uint2((uint32_t)s, (uint32_t)(s >> 32));
+        h->meta.push_back(m);
+        h->nbs_off.push_back(soff);
+        h->scratch_off.push_back(scoff);
+        off += (long long)M * ne;
+        soff += M;
+        scoff += (long long)kMaxWind * ne;
+    }
+    h->total_beads = off; h->total_slices = soff; h->total_scratch = scoff;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_meta, h->W * sizeof(WWMeta));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_pos, off * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_nxt, off * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_prv, off * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_nbs, soff * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_nbs_off, h->W * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_scratch_off, h->W * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_state, h->W * sizeof(WWState));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_stats, h->W * sizeof(pgb_worm_walker_stats));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_scratch, scoff * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_meta, h->meta.data(), h->W * sizeof(WWMeta), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_nbs_off, h->nbs_off.data(), h->W * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_scratch_off, h->scratch_off.data(), h->W * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(h->d_stats, 0, h->W * sizeof(pgb_worm_walker_stats));
+    if (e == cudaSuccess) e = cudaMemset(h->d_nbs, 0, soff * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->d_nxt, 0xff, off * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->d_prv, 0xff, off * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->d_pos, 0, off * sizeof(float4));
+    if (e != cudaSuccess) {
+        g_wwerr = std::string("worm_walkers_create: ") + cudaGetErrorString(e);
+        pgb_worm_walkers_destroy(h);
+        return e == cudaErrorMemoryAllocation ? PGB_ENOMEM : PGB_ECUDA;
+    }
+    // every walker starts empty and diagonal until a configuration is loaded
+    std::vector<WWState> st((size_t)h->W);
+    for (auto& s : st) {
+        s = WWState{};
+        for (int i = 0; i < 2; ++i) s.head[i] = s.tail[i] = s.sp1[i] = s.sp2[i] = -1;
+        s.gap = -1; s.diag = 1;
+    }
+    e = cudaMemcpy(h->d_state, st.data(), st.size() * sizeof(WWState), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { int rc = h->cfail(e, "worm walker state"); g_wwerr = h->err; pgb_worm_walkers_destroy(h); return rc; }
+    *out = h;
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_load(pgb_worm_walkers* h, int w, const double* pos) {
+    if (!h || !pos || w < 0 || w >= h->W) return PGB_EINVAL;
+    const WWMeta& m = h->meta[w];
+    const int N = m.N0, M = m.M, ne = m.Ne;
+    // closed worldlines on the identity permutation, beads 0..N-1 of every slice
+    std::vector<float4> p((size_t)M * ne, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<int> nx((size_t)M * ne, -1), pv((size_t)M * ne, -1), nb(M, N);
+    for (int t = 0; t < M; ++t)
+        for (int i = 0; i < N; ++i) {
+            const double* r = pos + ((size_t)t * N + i) * 3;
+            p[(size_t)t * ne + i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
+            nx[(size_t)t * ne + i] = i;
+            pv[(size_t)t * ne + i] = i;
+        }
+    WWState s{};
+    for (int i = 0; i < 2; ++i) s.head[i] = s.tail[i] = s.sp1[i] = s.sp2[i] = -1;
+    s.gap = -1; s.length = 0; s.diag = 1; s.numBeadsOn = N * M; s.err = 0; s.ctr = 0;
+    cudaError_t e = cudaMemcpy(h->d_pos + m.off, p.data(), p.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_nxt + m.off, nx.data(), nx.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_prv + m.off, pv.data(), pv.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_nbs + h->nbs_off[w], nb.data(), nb.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_state + w, &s, sizeof(WWState), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(h->d_stats + w, 0, sizeof(pgb_worm_walker_stats));
+    if (e != cudaSuccess) return h->cfail(e, "worm walker load");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_run(pgb_worm_walkers* h, int sweeps) {
+    if (!h || sweeps < 0) return PGB_EINVAL;
+    if (sweeps == 0) return PGB_OK;
+    const int blocks = (h->W + kWWWarps - 1) / kWWWarps;
+    k_worm_walkers<<<blocks, kWWWarps * 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
+                                                           h->d_nbs_off, h->d_state, h->d_stats, h->d_scratch,
+                                                           h->d_scratch_off, h->az, h->W, sweeps);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "worm walkers run");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_reset_stats(pgb_worm_walkers* h) {
+    if (!h) return PGB_EINVAL;
+    // keep the error words: a stopped walker stays stopped
+    std::vector<pgb_worm_walker_stats> st((size_t)h->W);
+    cudaError_t e = cudaMemcpy(st.data(), h->d_stats, st.size() * sizeof(pgb_worm_walker_stats), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cfail(e, "worm walker stats");
+    for (auto& x : st) { const int er = x.error; x = pgb_worm_walker_stats{}; x.error = er; }
+    e = cudaMemcpy(h->d_stats, st.data(), st.size() * sizeof(pgb_worm_walker_stats), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return h->cfail(e, "worm walker stats");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_stats(pgb_worm_walkers* h, pgb_worm_walker_stats* out) {
+    if (!h || !out) return PGB_EINVAL;
+    cudaError_t e = cudaMemcpy(out, h->d_stats, h->W * sizeof(pgb_worm_walker_stats), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cfail(e, "worm walker stats");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_get_path(pgb_worm_walkers* h, int w, double* pos, int32_t* next, int32_t* prev,
+                              uint8_t* on, int32_t* worm8) {
+    if (!h || w < 0 || w >= h->W || !pos || !next || !prev || !on || !worm8) return PGB_EINVAL;
+    const WWMeta& m = h->meta[w];
+    const int M = m.M, ne = m.Ne;
+    std::vector<float4> p((size_t)M * ne);
+    std::vector<int> nx((size_t)M * ne), pv((size_t)M * ne), nb(M);
+    WWState s;
+    cudaError_t e = cudaMemcpy(p.data(), h->d_pos + m.off, p.size() * sizeof(float4), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(nx.data(), h->d_nxt + m.off, nx.size() * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(pv.data(), h->d_prv + m.off, pv.size() * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(nb.data(), h->d_nbs + h->nbs_off[w], nb.size() * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&s, h->d_state + w, sizeof(WWState), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cfail(e, "worm walker path");
+    for (int t = 0; t < M; ++t)
+        for (int q = 0; q < ne; ++q) {
+            const size_t j = (size_t)t * ne + q;
+            pos[3 * j] = p[j].x; pos[3 * j + 1] = p[j].y; pos[3 * j + 2] = p[j].z;
+            const bool act = q < nb[t];
+            on[j] = act ? 1 : 0;
+            const int tn = t + 1 == M ? 0 : t + 1, tp = t == 0 ? M - 1 : t - 1;
+            next[2 * j] = (act && nx[j] >= 0) ? tn : -1; next[2 * j + 1] = (act && nx[j] >= 0) ? nx[j] : -1;
+            prev[2 * j] = (act && pv[j] >= 0) ? tp : -1; prev[2 * j + 1] = (act && pv[j] >= 0) ? pv[j] : -1;
+        }
+    const int wv[8] = {s.head[0], s.head[1], s.tail[0], s.tail[1], s.sp1[0], s.sp1[1], s.sp2[0], s.sp2[1]};
+    for (int i = 0; i < 8; ++i) worm8[i] = wv[i];
+    return PGB_OK;
+}
+
+}  // extern "C"

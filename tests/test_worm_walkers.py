@@ -1,0 +1,88 @@
+"""Device-resident worm walkers (one warp per walker): path invariants after
+many steps, determinism, and statistical agreement with the oracle's worm
+engine, which the plain GPU form matches bit for bit.
+
+The walkers draw from Philox streams and evaluate FP32 pair sums, so the
+comparison is of ensemble averages: the energy per particle and the particle
+number over closed configurations, within four combined standard errors.
+"""
+import numpy as np
+import pytest
+
+from pimc_gb300 import worldlines as wl
+from test_worm import check_path
+
+pytestmark = pytest.mark.gpu
+
+N, M, TAU, LAM = 8, 32, 0.01, 6.0596
+
+
+def _walkers(pgb, num, seed, window=1, mu=0.0):
+    L = wl.box_side(N)
+    W = pgb.WormWalkers(np.full(num, N), M, L, 8, TAU, LAM, mu=mu, window=window, seed=seed)
+    W.load_seeded(seed)
+    return W, L
+
+
+def test_worm_walkers_invariants_and_moves(pgb):
+    W, L = _walkers(pgb, 16, seed=3, window=-1)
+    for _ in range(4):
+        W.run(25)
+        st = W.stats()
+        assert np.all(st["error"] == 0), st["error"]
+        for w in (0, 5, 15):
+            check_path(W.path(w), M)
+    st = W.stats()
+    att, acc = st["attempted"].sum(axis=0), st["accepted"].sum(axis=0)
+    # every move of the list was attempted and accepted somewhere
+    assert np.all(att > 0) and np.all(acc > 0), (att, acc)
+    assert np.all(st["samples"] > 0)
+    # positions stay in the box
+    p = W.path(0)
+    assert np.all(np.abs(p["pos"][p["on"].astype(bool)]) <= L / 2 + 1e-5)
+
+
+def test_worm_walkers_deterministic(pgb):
+    runs = []
+    for _ in range(2):
+        W, _ = _walkers(pgb, 8, seed=9)
+        W.run(30)
+        runs.append((W.stats(), W.path(3)))
+    (s0, p0), (s1, p1) = runs
+    assert np.array_equal(s0["attempted"], s1["attempted"])
+    assert np.array_equal(s0["energy_sum"], s1["energy_sum"])
+    assert np.array_equal(p0["next"], p1["next"]) and np.array_equal(p0["pos"], p1["pos"])
+
+
+def test_worm_walkers_match_oracle_statistically(pgb, oracle_lib):
+    # oracle: one long chain, binned
+    L = wl.box_side(N)
+    cfg = wl.seeded_worldlines(N, M, L, LAM, TAU, 1, extent=3 * N)
+    o = oracle_lib.Oracle(L, M, 3 * N, TAU, LAM)
+    o.load(cfg)
+    mt = oracle_lib.MT(5)
+    kw = dict(mbar=8, temperature=1.0 / (M * TAU), initial_num_particles=N, window=1, mu=0.0)
+    o.run_worm_steps(mt, 200, **kw)
+    r = o.run_worm_steps(mt, 2400, **kw)
+    e = r["energies"]
+    n = r["num_particles"].astype(float)
+    ok = ~np.isnan(e)
+    assert ok.sum() > 500
+    eb = [e[i:i + 200][ok[i:i + 200]].mean() for i in range(0, 2400, 200)]
+    nb = [n[i:i + 200][ok[i:i + 200]].mean() for i in range(0, 2400, 200)]
+    eo, se_o = np.mean(eb), np.std(eb, ddof=1) / np.sqrt(len(eb))
+    no, sn_o = np.mean(nb), np.std(nb, ddof=1) / np.sqrt(len(nb))
+
+    W, _ = _walkers(pgb, 256, seed=11)
+    W.run(150)
+    W.reset_stats()
+    W.run(250)
+    st = W.stats()
+    assert np.all(st["error"] == 0)
+    has = st["samples"] > 0
+    ew = st["energy_sum"][has] / st["samples"][has]
+    nw = st["n_sum"][has] / st["samples"][has]
+    e_w, se_w = ew.mean(), ew.std(ddof=1) / np.sqrt(len(ew))
+    n_w, sn_w = nw.mean(), nw.std(ddof=1) / np.sqrt(len(nw))
+    assert abs(e_w - eo) <= 4.0 * np.hypot(se_w, se_o), (e_w, se_w, eo, se_o)
+    assert abs(n_w - no) <= 4.0 * np.hypot(sn_w, sn_o) + 1e-9, (n_w, sn_w, no, sn_o)
