@@ -63,7 +63,7 @@ def parse():
                     help="walker schedule code (0: autotune)")
     ap.add_argument("--no-baseline", action="store_true")
     ap.add_argument("--workload", default="walkers",
-                    choices=["walkers", "serving", "isf", "pair", "plain", "gp"])
+                    choices=["walkers", "serving", "isf", "pair", "plain", "gp", "worm"])
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     return ap.parse_args()
 
@@ -733,6 +733,71 @@ def run_gp(args, pgb):
     print(json.dumps(out))
 
 
+# ---------------------------------------------------------------------------
+# Device-resident worm walkers: the batched-walker workload (1024 He-4 paths,
+# N ~ U{8..128}, T ~ U[1,4] K, tau = 0.004, M even) run with the worm
+# algorithm's full move list, canonical window 1, one warp per walker.
+# ---------------------------------------------------------------------------
+def run_worm(args, pgb):
+    import torch
+    from pimc_gb300 import worldlines as wl
+    w = wl.workload_walkers(num=args.walkers, seed=0)
+    n, m = w["n"], w["m"]
+    L = w["side"]
+    W = pgb.WormWalkers(n, m, L, w["mbar"], w["tau"], w["lam"], window=1, seed=1)
+    W.load_seeded(1)
+    W.run(max(3, args.warmup))
+    W.reset_stats()
+    clk = Clocks()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    W.run(args.steps)
+    dt = time.perf_counter() - t0
+    clocks = clk.stop()
+    st = W.stats()
+    bu = float(st["bead_updates"].sum())
+    att, acc = st["attempted"].sum(axis=0), st["accepted"].sum(axis=0)
+    out = {"metric": "bead-updates/s (device worm walkers)", "value": bu / dt, "unit": "bead-updates/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": 1e3 * dt / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+f64",
+           "data": "synthetic",
+           "config": {"workload": "%d worm walkers (one warp each): N~U{8..128}, T~U[1,4] K, tau=0.004, "
+                                  "M even, Aziz, rho=0.02186, primitive action, the reference's full "
+                                  "move list, canonical window 1" % W.W,
+                      "errors": int((st["error"] != 0).sum()),
+                      "closed_samples": int(st["samples"].sum()),
+                      "acceptance": {WORM_MOVES[i]: [int(acc[i]), int(att[i])] for i in range(12)}},
+           "gpu_launches": args.steps, "clocks": clocks}
+    if not args.no_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        from concurrent.futures import ThreadPoolExecutor
+        threads = os.cpu_count() or 1
+        idx = list(np.argsort(n)[:: max(1, len(n) // 32)])[:32]
+
+        def one(i):
+            cfg = wl.seeded_worldlines(int(n[i]), int(m[i]), float(L[i]), w["lam"], w["tau"], 100003 + i,
+                                       extent=2 * int(n[i]) + 8)
+            o = pyoracle.Oracle(float(L[i]), int(m[i]), 2 * int(n[i]) + 8, w["tau"], w["lam"])
+            o.load(cfg)
+            mt = pyoracle.MT(7 + i)
+            kw = dict(mbar=int(w["mbar"][i]), temperature=1.0 / (int(m[i]) * w["tau"]),
+                      initial_num_particles=int(n[i]), window=1)
+            t0 = time.perf_counter()
+            r = o.run_worm_steps(mt, 1, **kw)
+            return r["bead_updates"], time.perf_counter() - t0
+
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(threads) as ex:
+            res = list(ex.map(one, idx))
+        wall = time.perf_counter() - t0
+        bu_c = sum(r[0] for r in res)
+        out["cpu_baseline"] = {"value": bu_c / wall, "unit": "bead-updates/s", "cores": threads,
+                               "kind": "port", "sample": "one worm-algorithm step of %d walkers spread over "
+                               "N, FP64 oracle with MT19937, %d threads, %.1f s" % (len(idx), threads, wall)}
+    print(json.dumps(out))
+
+
 def run_reference(args):
     rank, ws = dist_init()
     if rank != 0:
@@ -764,7 +829,7 @@ def main():
     if args.workload != "walkers":
         if rank == 0:
             {"serving": run_serving, "isf": run_isf, "pair": run_pair,
-             "plain": run_plain, "gp": run_gp}[args.workload](args, pgb)
+             "plain": run_plain, "gp": run_gp, "worm": run_worm}[args.workload](args, pgb)
         return
 
     w = workload(args.walkers, seed=rank)

@@ -114,15 +114,17 @@ struct WormWalker {
         do { i = u32() & used; } while (i > n && ++guard < 1000);
         return i > n ? n : i;
     }
-    __device__ double rand() { return double(u32()) * (1.0 / 4294967295.0); }
-    __device__ double randExc() { return double(u32()) * (1.0 / 4294967296.0); }
-    __device__ double randNorm(double mean, double sd) {
-        double x, y, r;
+    // FP32 deviates: the walkers agree with the reference statistically, and
+    // FP64 transcendentals are slow on this GPU
+    __device__ float rand() { return (float)u32() * 2.3283064365386963e-10f; }
+    __device__ float randExc() { return (float)(u32() >> 8) * 5.9604644775390625e-08f; }
+    __device__ float randNorm(float mean, float sd) {
+        float x, y, r;
         int guard = 0;
-        do { x = 2.0 * rand() - 1.0; y = 2.0 * rand() - 1.0; r = x * x + y * y; }
-        while ((r >= 1.0 || r == 0.0) && ++guard < 1000);
-        if (r >= 1.0 || r == 0.0) return mean;
-        return mean + x * sqrt(-2.0 * log(r) / r) * sd;
+        do { x = 2.0f * rand() - 1.0f; y = 2.0f * rand() - 1.0f; r = x * x + y * y; }
+        while ((r >= 1.0f || r == 0.0f) && ++guard < 1000);
+        if (r >= 1.0f || r == 0.0f) return mean;
+        return mean + x * sqrtf(-2.0f * logf(r) / r) * sd;
     }
 
     // ---- path access ----
@@ -180,7 +182,7 @@ struct WormWalker {
         if (s1 == 2 && s2 == 2) return 0.f;
         return 0.5f;
     }
-    __device__ double putInBC(double x) const { return x - (double)m.L * floor(x * (double)m.Linv + 0.5); }
+    __device__ float putInBC(float x) const { return x - m.L * floorf(x * m.Linv + 0.5f); }
 
     // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
     // tau * sum over the other active beads of the slice of factor * V
@@ -221,24 +223,24 @@ struct WormWalker {
     __device__ double corrRange(WB, WB) { return 0.0; }
 
     // ---- Path bookkeeping (path.cpp:205-420) ----
-    __device__ WB addBead(int slice, double x, double y, double z) {
+    __device__ WB addBead(int slice, float x, float y, float z) {
         const int k = nb(slice);
         if (k >= m.Ne) { err = WERR_FULL; return {-1, -1}; }
         WB last{slice, k};
         setNb(slice, k + 1);
         ++numBeadsOn;
         setNext(last, {-1, -1}); setPrev(last, {-1, -1});
-        setP(last, (float)x, (float)y, (float)z);
+        setP(last, x, y, z);
         return last;
     }
-    __device__ WB addNextBead(WB pb, double x, double y, double z) {
+    __device__ WB addNextBead(WB pb, float x, float y, float z) {
         const int slice = pb.t + 1 == m.M ? 0 : pb.t + 1;
         WB b = addBead(slice, x, y, z);
         if (err) return b;
         setNext(pb, b); setPrev(b, pb);
         return b;
     }
-    __device__ WB addPrevBead(WB nb_, double x, double y, double z) {
+    __device__ WB addPrevBead(WB nb_, float x, float y, float z) {
         const int slice = nb_.t == 0 ? m.M - 1 : nb_.t - 1;
         WB b = addBead(slice, x, y, z);
         if (err) return b;
@@ -288,9 +290,9 @@ struct WormWalker {
             if (isXW(b) || length > m.M * m.Ne) { err = WERR_LOOP; break; }
         } while (!eqW(b, nh));
         const float4 rt = P(nt), rh = P(nh);
-        sep[0] = (float)putInBC((double)rt.x - rh.x);
-        sep[1] = (float)putInBC((double)rt.y - rh.y);
-        sep[2] = (float)putInBC((double)rt.z - rh.z);
+        sep[0] = putInBC(rt.x - rh.x);
+        sep[1] = putInBC(rt.y - rh.y);
+        sep[2] = putInBC(rt.z - rh.z);
         setNext(nh, {-1, -1}); setPrev(nt, {-1, -1});
         sp1 = sp2 = WB{-1, -1};
     }
@@ -307,9 +309,11 @@ struct WormWalker {
     }
 
     // ---- sampling helpers (move.cpp:183-488) ----
-    __device__ double rho0(double d2, int L) const {
-        const double norm = pow(4.0 * 3.14159265358979323846 * m.lambda * L * m.tau, -1.5);
-        return norm * exp(-d2 / (4.0 * m.lambda * L * m.tau));
+    // ActionBase::rho0 (action.cpp:254-260) in FP32
+    __device__ float rho0(float d2, int L) const {
+        const float den = (float)(4.0 * m.lambda * L * m.tau);
+        const float g = rsqrtf(3.14159265358979f * den);
+        return g * g * g * expf(-d2 / den);
     }
     __device__ static int3 winding(int n) {
         // MoveBase ctor (move.cpp:88-108) with maxWind = 1
@@ -320,46 +324,51 @@ struct WormWalker {
         return w;
     }
     // sampleWindingSector (move.cpp:362-397)
-    __device__ int3 sampleWinding(WB sb, WB eb, int L, double& total) {
+    __device__ int3 sampleWinding(WB sb, WB eb, int L, double& totald) {
         const float4 pe = P(eb), ps = P(sb);
-        const double vx = (double)pe.x - ps.x, vy = (double)pe.y - ps.y, vz = (double)pe.z - ps.z;
-        double cum[kMaxWind];
-        total = 0.0;
+        const float vx = pe.x - ps.x, vy = pe.y - ps.y, vz = pe.z - ps.z;
+        float cum[kMaxWind];
+        float total = 0.0f;
         for (int n = 0; n < kMaxWind; ++n) {
             const int3 w = winding(n);
-            const double ax = vx + w.x * (double)m.L, ay = vy + w.y * (double)m.L, az_ = vz + w.z * (double)m.L;
+            const float ax = vx + w.x * m.L, ay = vy + w.y * m.L, az_ = vz + w.z * m.L;
             total += rho0(ax * ax + ay * ay + az_ * az_, L);
             cum[n] = total;
         }
-        const double x = rand();
+        totald = total;
+        const float x = rand();
         int idx = kMaxWind - 1;
         for (int n = 0; n < kMaxWind; ++n) if (cum[n] / total >= x) { idx = n; break; }
         return winding(idx);
     }
     // newStagingPosition with winding (move.cpp:301-338)
-    __device__ void stagingPos(WB nbd, WB eb, int L, int k, int3& wind, double& x, double& y, double& z) {
-        const double f1 = 1.0 * (L - k - 1), f2 = 1.0 / (1.0 * (L - k));
-        const double sg = m.sqrt2LambdaTau * sqrt(f1 * f2);
+    __device__ void stagingPos(WB nbd, WB eb, int L, int k, int3& wind, float& x, float& y, float& z) {
+        const float f1 = 1.0f * (L - k - 1), f2 = 1.0f / (1.0f * (L - k));
+        const float sg = (float)m.sqrt2LambdaTau * sqrtf(f1 * f2);
         const float4 np = P(nbd), e = P(eb);
-        double r[3] = {((double)e.x + (double)m.L * wind.x) - np.x, ((double)e.y + (double)m.L * wind.y) - np.y,
-                       ((double)e.z + (double)m.L * wind.z) - np.z};
-        const double n3[3] = {np.x, np.y, np.z};
-        int* wv[3] = {&wind.x, &wind.y, &wind.z};
-        for (int i = 0; i < 3; ++i) { r[i] *= f2; r[i] += n3[i]; }
-        for (int i = 0; i < 3; ++i) r[i] = randNorm(r[i], sg);
-        for (int i = 0; i < 3; ++i) {
-            for (int g = 0; g < 64 && r[i] < -0.5 * m.L; ++g) { ++*wv[i]; r[i] += m.L; }
-            for (int g = 0; g < 64 && r[i] >= 0.5 * m.L; ++g) { --*wv[i]; r[i] -= m.L; }
-        }
-        x = putInBC(r[0]); y = putInBC(r[1]); z = putInBC(r[2]);
+        float rx = ((e.x + m.L * wind.x) - np.x) * f2 + np.x;
+        float ry = ((e.y + m.L * wind.y) - np.y) * f2 + np.y;
+        float rz = ((e.z + m.L * wind.z) - np.z) * f2 + np.z;
+        rx = randNorm(rx, sg); ry = randNorm(ry, sg); rz = randNorm(rz, sg);
+        // the winding sector follows the sampled point (move.cpp:327-336)
+        const float h = 0.5f * m.L;
+        for (int g = 0; g < 64 && rx < -h; ++g) { ++wind.x; rx += m.L; }
+        for (int g = 0; g < 64 && rx >= h; ++g) { --wind.x; rx -= m.L; }
+        for (int g = 0; g < 64 && ry < -h; ++g) { ++wind.y; ry += m.L; }
+        for (int g = 0; g < 64 && ry >= h; ++g) { --wind.y; ry -= m.L; }
+        for (int g = 0; g < 64 && rz < -h; ++g) { ++wind.z; rz += m.L; }
+        for (int g = 0; g < 64 && rz >= h; ++g) { --wind.z; rz -= m.L; }
+        x = putInBC(rx); y = putInBC(ry); z = putInBC(rz);
     }
-    __device__ void freePos(WB nbd, double& x, double& y, double& z) {
+    __device__ void freePos(WB nbd, float& x, float& y, float& z) {
         const float4 p = P(nbd);
-        x = putInBC(randNorm(p.x, m.sqrt2LambdaTau));
-        y = putInBC(randNorm(p.y, m.sqrt2LambdaTau));
-        z = putInBC(randNorm(p.z, m.sqrt2LambdaTau));
+        const float sg = (float)m.sqrt2LambdaTau;
+        x = putInBC(randNorm(p.x, sg));
+        y = putInBC(randNorm(p.y, sg));
+        z = putInBC(randNorm(p.z, sg));
     }
-    __device__ bool metro(double dA) { return rand() < exp(-dA); }
+    // a NaN difference rejects
+    __device__ bool metro(double dA) { return rand() < expf(-(float)dA); }
     __device__ int randLen() { return 2 * (1 + (int)randInt((uint32_t)(m.mbar / 2 - 1))); }
     __device__ int trueN() const { return numBeadsOn / m.M; }
 
@@ -387,8 +396,8 @@ struct WormWalker {
         do { ++wl; b = next(b); } while (!eqW(b, stop) && !isXW(b) && wl <= m.M * m.Ne);
         if (err || wl > m.M) return 0;
         acc->attempted[WM_COM]++;
-        double sh[3];
-        for (int i = 0; i < 3; ++i) sh[i] = m.comDelta * (-0.5 + rand());
+        float sh[3];
+        for (int i = 0; i < 3; ++i) sh[i] = (float)m.comDelta * (-0.5f + rand());
         const double oldA = rangeAction(sb, eb);
         b = sb;
         for (int g = 0; g < wl; ++g) {
@@ -397,7 +406,7 @@ struct WormWalker {
             b = next(b);
         }
         const double newA = rangeAction(sb, eb);
-        if (rand() < exp(-(newA - oldA))) { accepted = true; acc->accepted[WM_COM]++; }
+        if (metro(newA - oldA)) { accepted = true; acc->accepted[WM_COM]++; }
         else {
             b = sb;
             for (int g = 0; g < wl; ++g) {
@@ -434,13 +443,13 @@ struct WormWalker {
             b = next(b);
             if (k >= kOrigCap) { err = WERR_LOOP; return 0; }
             orig[k] = P(b);
-            double x, y, z;
+            float x, y, z;
             stagingPos(prev(b), eb, L, k, wind, x, y, z);
             setP(b, (float)x, (float)y, (float)z);
             ++k;
         } while (!eqW(b, pe) && k < L);
         const double newA = rangeAction(sb, pe);
-        if (rand() < exp(-(newA - oldA))) { accepted = true; acc->accepted[WM_DIAG]++; }
+        if (metro(newA - oldA)) { accepted = true; acc->accepted[WM_DIAG]++; }
         else {
             b = sb;
             for (int i = 0; i < k; ++i) { b = next(b); setP(b, orig[i].x, orig[i].y, orig[i].z); }
@@ -461,9 +470,9 @@ struct WormWalker {
         double totalrho0;
         const int3 wind = sampleWinding(hb, tb, gapLength, totalrho0);
         const float4 pt = P(tb), ph = P(hb);
-        const double sx = ((double)pt.x - ph.x) + wind.x * (double)m.L;
-        const double sy = ((double)pt.y - ph.y) + wind.y * (double)m.L;
-        const double sz = ((double)pt.z - ph.z) + wind.z * (double)m.L;
+        const double sx = (double)((pt.x - ph.x) + wind.x * m.L);
+        const double sy = (double)((pt.y - ph.y) + wind.y * m.L);
+        const double sz = (double)((pt.z - ph.z) + wind.z * m.L);
         if (tooCostly(sx, sy, sz, gapLength)) return -1;
         double norm = (m.C * m.mbar * numBeadsOn) / totalrho0;
         norm *= 0.15 / 0.4;
@@ -519,7 +528,7 @@ struct WormWalker {
         double dA = bare(b) - 0.5 * actionShift;
         if (!metro(dA)) { closeUndo(); return 0; }
         for (int k = 0; k < g0 - 1; k++) {
-            double x, y, z;
+            float x, y, z;
             stagingPos(b, tail, g0, k, wind, x, y, z);
             b = addNextBead(b, x, y, z);
             if (err) return -2;
@@ -549,7 +558,7 @@ struct WormWalker {
         norm *= ensembleWeight(wl);
         if (norm < 2.220446049250313e-16) return 0;
         const int slice = 2 * (int)randInt((uint32_t)(m.M / 2 - 1));
-        const double x0 = m.L * (-0.5 + randExc()), y0 = m.L * (-0.5 + randExc()), z0 = m.L * (-0.5 + randExc());
+        const float x0 = m.L * (-0.5f + randExc()), y0 = m.L * (-0.5f + randExc()), z0 = m.L * (-0.5f + randExc());
         const WB tb = addBead(slice, x0, y0, z0);
         if (err) return -2;
         sp2 = tb;
@@ -559,7 +568,7 @@ struct WormWalker {
         double dA = bare(b) - 0.5 * actionShift;
         if (!metro(dA)) { insertUndo(tb); return 0; }
         for (int k = 1; k < wl; k++) {
-            double x, y, z;
+            float x, y, z;
             freePos(b, x, y, z);
             b = addNextBead(b, x, y, z);
             if (err) return -2;
@@ -567,7 +576,7 @@ struct WormWalker {
             dA = bare(b) - actionShift;
             if (!metro(dA)) { insertUndo(tb); return 0; }
         }
-        double x, y, z;
+        float x, y, z;
         freePos(b, x, y, z);
         const WB hb = addNextBead(b, x, y, z);
         if (err) return -2;
@@ -633,7 +642,7 @@ struct WormWalker {
         double dA = bare(b) - 0.5 * actionShift;
         if (!metro(dA)) { ahUndo(); return 0; }
         for (int k = 0; k < al - 1; k++) {
-            double x, y, z;
+            float x, y, z;
             freePos(b, x, y, z);
             b = addNextBead(b, x, y, z);
             if (err) return -2;
@@ -641,7 +650,7 @@ struct WormWalker {
             dA = bare(b) - actionShift;
             if (!metro(dA)) { ahUndo(); return 0; }
         }
-        double x, y, z;
+        float x, y, z;
         freePos(b, x, y, z);
         const WB hb = addNextBead(b, x, y, z);
         if (err) return -2;
@@ -747,7 +756,7 @@ struct WormWalker {
         double dA = bare(b) - 0.5 * actionShift;
         if (!metro(dA)) { rtUndo(); return 0; }
         for (int k = 0; k < rl - 1; k++) {
-            double x, y, z;
+            float x, y, z;
             freePos(b, x, y, z);
             b = addPrevBead(b, x, y, z);
             if (err) return -2;
@@ -755,7 +764,7 @@ struct WormWalker {
             dA = bare(b) - actionShift;
             if (!metro(dA)) { rtUndo(); return 0; }
         }
-        double x, y, z;
+        float x, y, z;
         freePos(b, x, y, z);
         const WB tb = addPrevBead(b, x, y, z);
         if (err) return -2;
@@ -771,37 +780,38 @@ struct WormWalker {
     // pivot slice's beads in index order: weights rho0 for every bead and
     // winding sector, a warp-parallel tower.  Returns Sigma; with x >= 0 the
     // pivot and its winding sector are selected for the uniform deviate x.
-    __device__ double towerNorm(WB b, int pivotSlice, int sign, double x, WB& pivot, int3& wind) {
+    __device__ double towerNorm(WB b, int pivotSlice, int sign, float x, WB& pivot, int3& wind) {
         const int nL = nb(pivotSlice);
         const int total = nL * kMaxWind;
         const float4 pb = P(b);
+        float* sc = reinterpret_cast<float*>(scratch);
         // weights in the reference's order: n fastest, winding sector slowest
-        double sum = 0.0;
+        float sum = 0.0f;
         for (int i = lane; i < total; i += 32) {
             const int w = i / nL, n = i - w * nL;
             const int3 wv = winding(w);
             const float4 pf = pos[(size_t)pivotSlice * m.Ne + n];
-            double sx = (double)pf.x - pb.x, sy = (double)pf.y - pb.y, sz = (double)pf.z - pb.z;
-            if (w > 0) { sx += (sign * wv.x) * (double)m.L; sy += (sign * wv.y) * (double)m.L; sz += (sign * wv.z) * (double)m.L; }
-            const double r = rho0(sx * sx + sy * sy + sz * sz, m.mbar);
-            scratch[i] = r;
+            float sx = pf.x - pb.x, sy = pf.y - pb.y, sz = pf.z - pb.z;
+            if (w > 0) { sx += (sign * wv.x) * m.L; sy += (sign * wv.y) * m.L; sz += (sign * wv.z) * m.L; }
+            const float r = rho0(sx * sx + sy * sy + sz * sz, m.mbar);
+            sc[i] = r;
             sum += r;
         }
         for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
         __syncwarp();
-        if (x >= 0.0) {
+        if (x >= 0.0f) {
             // first index whose cumulative weight reaches x * Sigma
-            const double target = x * sum;
-            double carry = 0.0;
+            const float target = x * sum;
+            float carry = 0.0f;
             int found = total - 1;
             for (int base = 0; base < total; base += 32) {
                 const int i = base + lane;
-                double v = i < total ? scratch[i] : 0.0;
+                float v = i < total ? sc[i] : 0.0f;
                 for (int o = 1; o < 32; o <<= 1) {
-                    const double u = __shfl_up_sync(0xffffffffu, v, o);
+                    const float u = __shfl_up_sync(0xffffffffu, v, o);
                     if (lane >= o) v += u;
                 }
-                const double cum = carry + v;
+                const float cum = carry + v;
                 const unsigned hit = __ballot_sync(0xffffffffu, i < total && cum >= target);
                 if (hit) { found = base + __ffs(hit) - 1; break; }
                 carry += __shfl_sync(0xffffffffu, v, 31);
@@ -810,7 +820,7 @@ struct WormWalker {
             pivot = WB{pivotSlice, n};
             wind = winding(w);
         }
-        return sum;
+        return (double)sum;
     }
     __device__ int swapHead(float4* orig) {
         if (numBeadsOn == 0 || diag) return -1;
@@ -829,8 +839,8 @@ struct WormWalker {
         if (isXW(swp) || eqW(tail, swp)) return -1;
         acc->attempted[WM_SH]++;
         WB dummy; int3 dw;
-        const double SigmaSwap = towerNorm(swp, pivotSlice, 1, -1.0, dummy, dw);
-        const double PNorm = fmin(SigmaHead / SigmaSwap, 1.0);
+        const double SigmaSwap = towerNorm(swp, pivotSlice, 1, -1.0f, dummy, dw);
+        const float PNorm = (float)fmin(SigmaHead / SigmaSwap, 1.0);
         if (rand() < PNorm) {
             sp1 = swp; sp2 = pivot;
             int k = 0;
@@ -852,7 +862,7 @@ struct WormWalker {
             k = 0;
             for (int g = 0; g <= m.M; ++g) {
                 if (!eqW(b, sp1) && !eqW(b, pivot)) {
-                    double x, y, z;
+                    float x, y, z;
                     stagingPos(prev(b), pivot, swapLength, k, wind, x, y, z);
                     setP(b, (float)x, (float)y, (float)z);
                     ++k;
@@ -897,8 +907,8 @@ struct WormWalker {
         if (isXW(swp) || eqW(head, swp)) return -1;
         acc->attempted[WM_ST]++;
         WB dummy; int3 dw;
-        const double SigmaSwap = towerNorm(swp, pivotSlice, 1, -1.0, dummy, dw);
-        const double PNorm = fmin(SigmaTail / SigmaSwap, 1.0);
+        const double SigmaSwap = towerNorm(swp, pivotSlice, 1, -1.0f, dummy, dw);
+        const float PNorm = (float)fmin(SigmaTail / SigmaSwap, 1.0);
         if (rand() < PNorm) {
             sp1 = swp; sp2 = pivot;
             int k = 0;
@@ -922,7 +932,7 @@ struct WormWalker {
             b = pivot;
             for (int g = 0; g <= m.M; ++g) {
                 if (!eqW(b, s1) && !eqW(b, pivot)) {
-                    double x, y, z;
+                    float x, y, z;
                     stagingPos(prev(b), s1, swapLength, k, wind, x, y, z);
                     setP(b, (float)x, (float)y, (float)z);
                     ++k;
