@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--walkers", type=int, default=1024)
+    ap.add_argument("--serve-canonical", action="store_true",
+                    help="serve canonical staging + COM chains instead of grand-canonical worm jobs")
     ap.add_argument("--schedule", type=int, default=0,
                     help="walker schedule code (0: autotune)")
     ap.add_argument("--no-baseline", action="store_true")
@@ -285,7 +287,7 @@ def plain_form_rate(pgb, n=64, t=2.0, tau=0.004, steps=1):
 # load far exceeds capacity, so the window is bounded and the report states
 # how many jobs reached a first bin / completed (the rest are censored).
 # ---------------------------------------------------------------------------
-def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02):
+def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02, grand_canonical=True):
     rng = np.random.Generator(np.random.Philox(seed))
     arrivals = []
     t = 0.0
@@ -294,7 +296,8 @@ def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02):
         if t > 0.6 * seconds:
             break
         arrivals.append(t)
-    srv = pgb.Server(150e9, max_active=1024, bin_sweeps=100, round_seconds=round_seconds)
+    srv = pgb.Server(150e9, max_active=1024, bin_sweeps=100, round_seconds=round_seconds,
+                     grand_canonical=grand_canonical)
     ids = []
     for k, ta in enumerate(arrivals):
         n = int(round(math.exp(rng.uniform(math.log(8), math.log(512)))))
@@ -327,13 +330,15 @@ def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02):
             "ttfb_p50_s": pct(ttfb, 50), "ttfb_p99_s": pct(ttfb, 99),
             "completion_p50_s": pct(done, 50), "completion_p99_s": pct(done, 99),
             "note": "Poisson 50 jobs/s for %.1f s of a %.1f s window; percentiles over jobs that "
-                    "reached the event inside the window (the others are censored); canonical "
-                    "chains (staging + COM), bins of 100 sweeps, rounds of %g s of device time"
-                    % (0.6 * seconds, seconds, round_seconds)}
+                    "reached the event inside the window (the others are censored); %s, bins of "
+                    "100 sweeps, rounds of %g s of device time"
+                    % (0.6 * seconds, seconds,
+                       "grand-canonical worm walkers at each job's mu (the full move list)"
+                       if grand_canonical else "canonical chains (staging + COM)", round_seconds)}
 
 
 def run_serving(args, pgb):
-    r = serving_run(pgb, seconds=args.serve_seconds)
+    r = serving_run(pgb, seconds=args.serve_seconds, grand_canonical=not args.serve_canonical)
     out = {"metric": "serving p99 time-to-first-bin", "value": r["ttfb_p99_s"], "unit": "s",
            "n_gpus": 1, "steps": r["rounds"], "warmup": 0, "higher_is_better": False,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
@@ -924,7 +929,7 @@ def main():
         out["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
         out["plain_fp64"] = plain_form_rate(pgb)
         out["plain_fp64"]["batched_over_plain"] = value / out["plain_fp64"]["value"]
-        out["serving"] = serving_run(pgb, seconds=args.serve_seconds)
+        out["serving"] = serving_run(pgb, seconds=args.serve_seconds, grand_canonical=not args.serve_canonical)
     if rank == 0:
         print(json.dumps(out))
 

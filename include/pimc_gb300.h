@@ -480,6 +480,7 @@ typedef struct {
     long long attempted[12];              /* the move list of pgb_plain_worm_run */
     long long accepted[12];
     long long bead_updates;
+    long long sweeps;                     /* PIMC steps made */
     int       error;                      /* 1 slice full, 2 bad link, 3 runaway walk */
     int       pad;
 } pgb_worm_walker_stats;
@@ -495,6 +496,21 @@ int pgb_worm_walkers_reset_stats(pgb_worm_walkers* w);
 /* one walker's arrays in the layouts of pgb_load_path ([M][capacity]) */
 int pgb_worm_walkers_get_path(pgb_worm_walkers* w, int walker, double* pos, int32_t* next,
                               int32_t* prev, uint8_t* on, int32_t worm8[8]);
+
+/* Grand-canonical job server: pgb_server_*'s interface and semantics (the
+ * same parameter, job, bin and job-info records) with every job a device worm
+ * walker at its own chemical potential mu (worm constant C0 = 1, no window).
+ * A job's bins depend only on its spec: the same alone and in any mix. */
+typedef struct pgb_worm_server pgb_worm_server;
+int         pgb_worm_server_create(const pgb_server_params* p, pgb_worm_server** out);
+int         pgb_worm_server_destroy(pgb_worm_server* s);
+int         pgb_worm_server_submit(pgb_worm_server* s, const pgb_job_spec* job, int* job_id);
+int         pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued);
+int         pgb_worm_server_poll_bins(pgb_worm_server* s, pgb_bin* out, int cap, int* n);
+int         pgb_worm_server_job_info(pgb_worm_server* s, int job, pgb_job_info* out);
+double      pgb_worm_server_clock(pgb_worm_server* s);
+int         pgb_worm_server_active_bead_updates(pgb_worm_server* s, long long* total);
+const char* pgb_worm_server_last_error(const pgb_worm_server* s);
 
 /* ---- Gaussian-process external potential ----------------------------------
  * GaussianProcessPotential (include/potential.h:287-323, src/potential.cpp:

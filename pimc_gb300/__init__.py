@@ -465,8 +465,8 @@ class WormWalkers:
 
     STATS_DTYPE = np.dtype([("energy_sum", "<f8"), ("energy_sumsq", "<f8"), ("n_sum", "<f8"),
                             ("n_sumsq", "<f8"), ("samples", "<i8"), ("attempted", "<i8", (12,)),
-                            ("accepted", "<i8", (12,)), ("bead_updates", "<i8"), ("error", "<i4"),
-                            ("pad", "<i4")])
+                            ("accepted", "<i8", (12,)), ("bead_updates", "<i8"), ("sweeps", "<i8"),
+                            ("error", "<i4"), ("pad", "<i4")])
 
     def __init__(self, n, m, side, mbar, tau, lam, mu=None, capacity=None, worm_constant=1.0,
                  window=-1, seed=0, aziz_year=1979):
@@ -554,23 +554,31 @@ class Server:
     estimator bins back."""
 
     def __init__(self, hbm_budget_bytes, max_active=1024, sweeps_per_round=10, bin_sweeps=100,
-                 tau=0.004, lam=None, p_com=0.05, aziz_year=1979, round_seconds=0.0):
+                 tau=0.004, lam=None, p_com=0.05, aziz_year=1979, round_seconds=0.0,
+                 grand_canonical=False):
+        """grand_canonical: every job a device worm walker at its mu
+        (pgb_worm_server_*); otherwise canonical staging + COM chains."""
         self.lib = _lib.load()
         lam = worldlines.LAMBDA_HE4 if lam is None else lam
         p = _lib.PgbServerParams(float(hbm_budget_bytes), max_active, sweeps_per_round, bin_sweeps,
                                  tau, lam, p_com, aziz_year, float(round_seconds))
+        self.gc = bool(grand_canonical)
+        self.pre = "pgb_worm_server_" if self.gc else "pgb_server_"
         h = C.c_void_p()
-        rc = self.lib.pgb_server_create(C.byref(p), C.byref(h))
+        rc = getattr(self.lib, self.pre + "create")(C.byref(p), C.byref(h))
         if rc != 0:
-            raise PgbError(rc, (self.lib.pgb_server_last_error(None) or b"").decode())
+            raise PgbError(rc, (getattr(self.lib, self.pre + "last_error")(None) or b"").decode())
         self.h = h
 
+    def _f(self, name):
+        return getattr(self.lib, self.pre + name)
+
     def _chk(self, rc):
-        return _lib.check(rc, self.h, server=True)
+        return _lib.check(rc, self.h, server=not self.gc, worm_server=self.gc)
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.pgb_server_destroy(self.h)
+            self._f("destroy")(self.h)
             self.h = None
 
     def __del__(self):
@@ -584,12 +592,12 @@ class Server:
         spec = _lib.PgbJobSpec(int(n), float(temperature), float(mu), float(density), int(sweeps),
                                int(seed), float(arrival))
         jid = C.c_int()
-        self._chk(self.lib.pgb_server_submit(self.h, C.byref(spec), C.byref(jid)))
+        self._chk(self._f("submit")(self.h, C.byref(spec), C.byref(jid)))
         return jid.value
 
     def step(self):
         a, q = C.c_int(), C.c_int()
-        self._chk(self.lib.pgb_server_step(self.h, C.byref(a), C.byref(q)))
+        self._chk(self._f("step")(self.h, C.byref(a), C.byref(q)))
         return a.value, q.value
 
     def bins(self):
@@ -597,7 +605,7 @@ class Server:
         buf = (_lib.PgbBin * 1024)()
         while True:
             n = C.c_int()
-            self._chk(self.lib.pgb_server_poll_bins(self.h, buf, 1024, C.byref(n)))
+            self._chk(self._f("poll_bins")(self.h, buf, 1024, C.byref(n)))
             out += [dict(job=b.job, bin=b.bin, energy=b.energy_per_particle, samples=b.samples,
                          time=b.time) for b in buf[:n.value]]
             if n.value < 1024:
@@ -605,14 +613,14 @@ class Server:
 
     def job(self, jid):
         i = _lib.PgbJobInfo()
-        self._chk(self.lib.pgb_server_job_info(self.h, jid, C.byref(i)))
+        self._chk(self._f("job_info")(self.h, jid, C.byref(i)))
         return dict(state=i.state, arrival=i.arrival, admitted=i.admitted, first_bin=i.first_bin,
                     completed=i.completed, sweeps_done=i.sweeps_done, n=i.n, m=i.m, bytes=i.bytes)
 
     def clock(self):
-        return self.lib.pgb_server_clock(self.h)
+        return self._f("clock")(self.h)
 
     def bead_updates(self):
         t = C.c_longlong()
-        self._chk(self.lib.pgb_server_active_bead_updates(self.h, C.byref(t)))
+        self._chk(self._f("active_bead_updates")(self.h, C.byref(t)))
         return t.value

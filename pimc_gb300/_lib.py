@@ -93,8 +93,8 @@ class PgbWormWalkersParams(C.Structure):
 class PgbWormWalkerStats(C.Structure):
     _fields_ = [("energy_sum", C.c_double), ("energy_sumsq", C.c_double), ("n_sum", C.c_double),
                 ("n_sumsq", C.c_double), ("samples", C.c_longlong), ("attempted", C.c_longlong * 12),
-                ("accepted", C.c_longlong * 12), ("bead_updates", C.c_longlong), ("error", C.c_int),
-                ("pad", C.c_int)]
+                ("accepted", C.c_longlong * 12), ("bead_updates", C.c_longlong),
+                ("sweeps", C.c_longlong), ("error", C.c_int), ("pad", C.c_int)]
 
 
 class PgbJobSpec(C.Structure):
@@ -152,6 +152,15 @@ _SIGS = {
     "pgb_qvectors_shells": (C.c_int, [C.c_double, C.c_double, C.c_int, _DP, C.POINTER(C.c_int),
                                       C.c_int, C.POINTER(C.c_int)]),
     "pgb_plain_get_rng": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
+    "pgb_worm_server_create": (C.c_int, [C.POINTER(PgbServerParams), C.POINTER(C.c_void_p)]),
+    "pgb_worm_server_destroy": (C.c_int, [_VP]),
+    "pgb_worm_server_submit": (C.c_int, [_VP, C.POINTER(PgbJobSpec), C.POINTER(C.c_int)]),
+    "pgb_worm_server_step": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "pgb_worm_server_poll_bins": (C.c_int, [_VP, C.POINTER(PgbBin), C.c_int, C.POINTER(C.c_int)]),
+    "pgb_worm_server_job_info": (C.c_int, [_VP, C.c_int, C.POINTER(PgbJobInfo)]),
+    "pgb_worm_server_clock": (C.c_double, [_VP]),
+    "pgb_worm_server_active_bead_updates": (C.c_int, [_VP, C.POINTER(C.c_longlong)]),
+    "pgb_worm_server_last_error": (C.c_char_p, [_VP]),
     "pgb_worm_walkers_create": (C.c_int, [C.POINTER(PgbWormWalkersParams), C.POINTER(C.c_void_p)]),
     "pgb_worm_walkers_destroy": (C.c_int, [_VP]),
     "pgb_worm_walkers_last_error": (C.c_char_p, [_VP]),
@@ -257,10 +266,12 @@ def u8ptr(a):
     return a.ctypes.data_as(_U8)
 
 
-def check(rc, handle=None, walkers=False, server=False, gp=False, worm=False):
+def check(rc, handle=None, walkers=False, server=False, gp=False, worm=False, worm_server=False):
     if rc != PGB_OK:
         lib = load()
-        if worm:
+        if worm_server:
+            msg = lib.pgb_worm_server_last_error(handle)
+        elif worm:
             msg = lib.pgb_worm_walkers_last_error(handle)
         elif gp:
             msg = lib.pgb_gp_last_error(handle)

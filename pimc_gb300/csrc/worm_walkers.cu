@@ -32,7 +32,12 @@
 #include "pgb_device.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <deque>
+#include <limits>
+#include <map>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -53,7 +58,7 @@ struct WWState {
     int gap, length, diag, numBeadsOn;
     float sep[3];
     int err;
-    unsigned long long ctr;
+    unsigned long long ctr;          // sweeps made: the random stream's sweep index
 };
 
 struct WB { int t, p; };
@@ -205,19 +210,37 @@ struct WormWalker {
         }
         return m.tau * warp_sum_ff(k);
     }
-    // potentialAction over the active beads from s to e along next links
+    // one bead's pair terms, accumulated into a lane's running sum
+    __device__ void bareTerms(WB b, KahanF& k) {
+        const float4 rb = P(b);
+        const int s1 = state(b);
+        const int n = nb(b.t);
+        for (int j = lane; j < n; j += 32) {
+            if (j == b.p) continue;
+            const WB o{b.t, j};
+            const float f = factor(s1, state(o));
+            if (f == 0.f) continue;
+            const float4 rj = pos[(size_t)b.t * m.Ne + j];
+            const float dx = min_image32(rj.x - rb.x, m.L, m.Linv);
+            const float dy = min_image32(rj.y - rb.y, m.L, m.Linv);
+            const float dz = min_image32(rj.z - rb.z, m.L, m.Linv);
+            k.add(f * aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+        }
+    }
+    // potentialAction over the active beads from s to e along next links:
+    // the lanes keep one running sum over the whole range and reduce once
     __device__ double rangeAction(WB s, WB e) {
-        double u = 0.0;
+        KahanF k;
         WB b = s;
         const WB stop = next(e);
         for (int g = 0; g <= m.M * m.Ne; ++g) {
-            if (isXW(b) || err) { err = err ? err : WERR_LINK; return u; }
-            if (b.p < nb(b.t)) u += bare(b);
+            if (isXW(b) || err) { err = err ? err : WERR_LINK; break; }
+            if (b.p < nb(b.t)) bareTerms(b, k);
             b = next(b);
-            if (eqW(b, stop)) return u;
+            if (eqW(b, stop)) return m.tau * warp_sum_ff(k);
         }
-        err = WERR_LOOP;
-        return u;
+        if (!err) err = WERR_LOOP;
+        return m.tau * warp_sum_ff(k);
     }
     // the primitive action has no gradient correction (gradVFactor = 0)
     __device__ double corrRange(WB, WB) { return 0.0; }
@@ -1005,11 +1028,16 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
                int* __restrict__ prv, int* __restrict__ nbs, const long long* __restrict__ nbs_off,
                WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
                double* __restrict__ scratch, const long long* __restrict__ scratch_off,
-               AzizF az, int W, int sweeps) {
+               AzizF az, int W, int sweeps, const int* __restrict__ order,
+               const int* __restrict__ limit, unsigned long long budget_ns) {
+    // walker i of this launch is order[i] (all walkers in index order when
+    // order is null); limit[w] caps its sweeps; with budget_ns > 0 a walker
+    // stops between sweeps once that much device time has passed
     __shared__ float4 s_orig[kWWWarps][kOrigCap];
     const int warp = threadIdx.x >> 5;
-    const int w = blockIdx.x * kWWWarps + warp;
-    if (w >= W) return;
+    const int wi = blockIdx.x * kWWWarps + warp;
+    if (wi >= W) return;
+    const int w = order ? order[wi] : wi;
     WormWalker ww;
     ww.m = meta[w];
     ww.az = az;
@@ -1027,7 +1055,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     ww.gap = st.gap; ww.length = st.length; ww.diag = st.diag; ww.numBeadsOn = st.numBeadsOn;
     ww.sep[0] = st.sep[0]; ww.sep[1] = st.sep[1]; ww.sep[2] = st.sep[2];
     ww.err = 0;
-    ww.ctr = st.ctr; ww.bidx = 4;
+    ww.ctr = 0; ww.bidx = 4;
     // per-walker counters accumulate in a register copy, lane 0 writes back
     pgb_worm_walker_stats local = stats[w];
     ww.acc = &local;
@@ -1044,7 +1072,22 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     cumD[WM_N - 1] = 1.0 + 1e-7;
     cumO[WM_N - 1] = 1.0 + 1e-7;
     float4* orig = s_orig[warp];
-    for (int sw = 0; sw < sweeps && !ww.err; ++sw) {
+    const int lim = limit ? min(sweeps, limit[w]) : sweeps;
+    const unsigned long long t0 = __shfl_sync(0xffffffffu, gtimer_ns(), 0);
+    // the walker's random stream is indexed by (sweep, draw): each sweep
+    // starts at counter sweep << 32, so where launches split a run does not
+    // change the draws
+    unsigned long long sweep_no = st.ctr;
+    for (int sw = 0; sw < lim && !ww.err; ++sw) {
+        if (budget_ns) {
+            // lane 0's clock for every lane: the decision must be uniform
+            const unsigned long long now = __shfl_sync(0xffffffffu, gtimer_ns(), 0);
+            if (now - t0 > budget_ns) break;
+        }
+        ww.ctr = sweep_no << 32;
+        ww.bidx = 4;
+        ++sweep_no;
+        local.sweeps += 1;
         for (int u = 0; u < ww.m.num_updates && !ww.err; ++u) {
             const double x = ww.rand();
             const double* cum = ww.diag ? cumD : cumO;
@@ -1084,7 +1127,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
         o.sp1[0] = ww.sp1.t; o.sp1[1] = ww.sp1.p; o.sp2[0] = ww.sp2.t; o.sp2[1] = ww.sp2.p;
         o.gap = ww.gap; o.length = ww.length; o.diag = ww.diag; o.numBeadsOn = ww.numBeadsOn;
         o.sep[0] = ww.sep[0]; o.sep[1] = ww.sep[1]; o.sep[2] = ww.sep[2];
-        o.err = ww.err; o.ctr = ww.ctr;
+        o.err = ww.err; o.ctr = sweep_no;
         states[w] = o;
         local.error = ww.err;
         stats[w] = local;
@@ -1263,7 +1306,8 @@ int pgb_worm_walkers_run(pgb_worm_walkers* h, int sweeps) {
     const int blocks = (h->W + kWWWarps - 1) / kWWWarps;
     k_worm_walkers<<<blocks, kWWWarps * 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
                                                            h->d_nbs_off, h->d_state, h->d_stats, h->d_scratch,
-                                                           h->d_scratch_off, h->az, h->W, sweeps);
+                                                           h->d_scratch_off, h->az, h->W, sweeps, nullptr,
+                                                           nullptr, 0ull);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return h->cfail(e, "worm walkers run");
@@ -1315,6 +1359,376 @@ int pgb_worm_walkers_get_path(pgb_worm_walkers* h, int w, double* pos, int32_t* 
         }
     const int wv[8] = {s.head[0], s.head[1], s.tail[0], s.tail[1], s.sp1[0], s.sp1[1], s.sp2[0], s.sp2[1]};
     for (int i = 0; i < 8; ++i) worm8[i] = wv[i];
+    return PGB_OK;
+}
+
+}  // extern "C"
+
+// --------------------------------------------------------------------------
+// Grand-canonical job server over the worm walkers: the canonical server's
+// interface (jobs arrive, are admitted when their arrays fit the HBM budget,
+// run together in shared launches, stream estimator bins back), with every
+// job a device worm walker at its own chemical potential.
+// --------------------------------------------------------------------------
+namespace {
+
+struct WPool {
+    std::map<long long, long long> free_blocks;      // offset -> length
+    void init(long long n) { free_blocks.clear(); if (n > 0) free_blocks[0] = n; }
+    long long alloc(long long n) {
+        for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it)
+            if (it->second >= n) {
+                const long long off = it->first, len = it->second;
+                free_blocks.erase(it);
+                if (len > n) free_blocks[off + n] = len - n;
+                return off;
+            }
+        return -1;
+    }
+    void release(long long off, long long n) {
+        auto it = free_blocks.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_blocks.end() && it->first + it->second == nx->first) { it->second += nx->second; free_blocks.erase(nx); }
+        if (it != free_blocks.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) { pv->second += it->second; free_blocks.erase(it); }
+        }
+    }
+};
+
+struct WServerJob {
+    pgb_job_spec spec{};
+    int state = 0;
+    double t_admit = -1, t_first = -1, t_done = -1;
+    long long sweeps_done = 0, bin_start = 0, samples0 = 0;
+    double esum0 = 0.0;
+    int bins = 0;
+    int M = 0, N0 = 0, Ne = 0, mbar = 0;
+    double L = 0;
+    int slot = -1;
+    long long bead_off = -1, slice_off = -1, scratch_off = -1;
+    size_t bytes = 0;
+};
+
+thread_local std::string g_wserr;
+
+}  // namespace
+
+struct pgb_worm_server {
+    pgb_server_params p{};
+    AzizParams ap{};
+    AzizF az{};
+    int max_slots = 0;
+    std::vector<int> slot_job, free_slots;
+    std::vector<WServerJob> jobs;
+    std::deque<int> queue;
+    std::vector<pgb_bin> bins;
+    WPool beads, slices, scratch;
+    long long n_beads = 0, n_slices = 0, n_scratch = 0;
+    float4* d_pos = nullptr;
+    int *d_nxt = nullptr, *d_prv = nullptr, *d_nbs = nullptr;
+    double* d_scratch = nullptr;
+    WWMeta* d_meta = nullptr;
+    WWState* d_state = nullptr;
+    pgb_worm_walker_stats* d_stats = nullptr;
+    long long *d_nbs_off = nullptr, *d_scratch_off = nullptr;
+    int *d_order = nullptr, *d_limit = nullptr;
+    std::vector<WWMeta> h_meta;
+    std::vector<long long> h_nbs_off, h_scratch_off;
+    std::vector<int> h_limit;
+    cudaStream_t stream = nullptr;
+    std::chrono::steady_clock::time_point t0;
+    long long bead_updates = 0;
+    std::string err;
+    int fail(int code, const std::string& m) { err = m; return code; }
+    int cfail(cudaError_t e, const char* where) {
+        err = std::string("CUDA error ") + cudaGetErrorString(e) + " at " + where;
+        return e == cudaErrorMemoryAllocation ? PGB_ENOMEM : PGB_ECUDA;
+    }
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+extern "C" {
+
+const char* pgb_worm_server_last_error(const pgb_worm_server* s) { return s ? s->err.c_str() : g_wserr.c_str(); }
+
+int pgb_worm_server_destroy(pgb_worm_server* s) {
+    if (!s) return PGB_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    cudaFree(s->d_pos); cudaFree(s->d_nxt); cudaFree(s->d_prv); cudaFree(s->d_nbs); cudaFree(s->d_scratch);
+    cudaFree(s->d_meta); cudaFree(s->d_state); cudaFree(s->d_stats); cudaFree(s->d_nbs_off);
+    cudaFree(s->d_scratch_off); cudaFree(s->d_order); cudaFree(s->d_limit);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return PGB_OK;
+}
+
+int pgb_worm_server_create(const pgb_server_params* p, pgb_worm_server** out) {
+    if (!out) return PGB_EINVAL;
+    *out = nullptr;
+    if (!p || p->hbm_budget_bytes < 1e6 || p->max_active <= 0 || p->sweeps_per_round <= 0 ||
+        p->bin_sweeps <= 0 || p->tau <= 0 || p->lambda <= 0 || !(p->round_seconds >= 0.0) ||
+        p->round_seconds > 10.0) {
+        g_wserr = "worm_server_create: need budget >= 1 MB, max_active > 0, sweeps_per_round > 0, "
+                  "bin_sweeps > 0, 0 <= round_seconds <= 10";
+        return PGB_EINVAL;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); g_wserr = "no CUDA device available"; return PGB_ECUDA; }
+    pgb_worm_server* s = new pgb_worm_server();
+    s->p = *p;
+    s->ap = aziz_params(p->aziz_year ? p->aziz_year : 1979);
+    s->az = make_aziz_f(s->ap);
+    s->max_slots = p->max_active;
+    // the budget: 85 % for bead arrays (24 B a bead), 15 % for the swap-move
+    // tower scratch, slice counters sized from the bead pool
+    s->n_beads = (long long)(0.85 * p->hbm_budget_bytes / 24.0);
+    s->n_scratch = (long long)(0.15 * p->hbm_budget_bytes / 8.0);
+    s->n_slices = s->n_beads / 8 + 1;
+    s->beads.init(s->n_beads); s->slices.init(s->n_slices); s->scratch.init(s->n_scratch);
+    s->slot_job.assign(s->max_slots, -1);
+    for (int k = s->max_slots - 1; k >= 0; --k) s->free_slots.push_back(k);
+    s->h_meta.assign(s->max_slots, WWMeta{});
+    s->h_nbs_off.assign(s->max_slots, 0);
+    s->h_scratch_off.assign(s->max_slots, 0);
+    s->h_limit.assign(s->max_slots, 0);
+    s->t0 = std::chrono::steady_clock::now();
+    cudaError_t e;
+    do {
+        if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_pos, s->n_beads * sizeof(float4))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_nxt, s->n_beads * sizeof(int))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_prv, s->n_beads * sizeof(int))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_nbs, s->n_slices * sizeof(int))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_scratch, s->n_scratch * sizeof(double))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_meta, s->max_slots * sizeof(WWMeta))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_state, s->max_slots * sizeof(WWState))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_stats, s->max_slots * sizeof(pgb_worm_walker_stats))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_nbs_off, s->max_slots * sizeof(long long))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_scratch_off, s->max_slots * sizeof(long long))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_order, s->max_slots * sizeof(int))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_limit, s->max_slots * sizeof(int))) != cudaSuccess) break;
+    } while (0);
+    if (e != cudaSuccess) {
+        g_wserr = std::string("worm_server_create: ") + cudaGetErrorString(e);
+        pgb_worm_server_destroy(s);
+        return e == cudaErrorMemoryAllocation ? PGB_ENOMEM : PGB_ECUDA;
+    }
+    *out = s;
+    return PGB_OK;
+}
+
+int pgb_worm_server_submit(pgb_worm_server* s, const pgb_job_spec* j, int* job_id) {
+    if (!s || !j) return PGB_EINVAL;
+    if (j->n < 1 || j->n > 2000 || j->temperature <= 0 || j->density <= 0 || j->sweeps <= 0)
+        return s->fail(PGB_EINVAL, "job: need 1 <= n <= 2000, temperature > 0, density > 0, sweeps > 0");
+    WServerJob job;
+    job.spec = *j;
+    job.N0 = j->n;
+    int M = (int)std::lround(1.0 / (j->temperature * s->p.tau));
+    if (M % 2) M += 1;
+    if (M < 4) M = 4;
+    job.M = M;
+    job.L = std::cbrt(j->n / j->density);
+    // Mbar (setup.cpp:1079-1104), even, at most 64 and below M
+    const double ell = std::pow(1.0 * j->n / (job.L * job.L * job.L), -1.0 / 3.0);
+    int mb = (int)(ell * ell / (16.0 * s->p.lambda * s->p.tau));
+    if (mb < 2) mb = 2; else if (mb > M) mb = M / 2;
+    if (mb % 2) mb += 1;
+    mb = std::min(mb, 64);
+    if (mb >= M) mb = (M / 2) % 2 ? M / 2 - 1 : M / 2;
+    if (mb < 2) mb = 2;
+    job.mbar = mb;
+    job.Ne = 2 * j->n + 8;
+    job.bytes = (size_t)M * job.Ne * 24 + (size_t)M * 4 + (size_t)kMaxWind * job.Ne * 8;
+    if (job.Ne > 4096) return s->fail(PGB_EINVAL, "job: n too large for one walker");
+    s->jobs.push_back(job);
+    if (job_id) *job_id = (int)s->jobs.size() - 1;
+    return PGB_OK;
+}
+
+int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
+    if (!s) return PGB_EINVAL;
+    const double now = s->now();
+    for (size_t k = 0; k < s->jobs.size(); ++k)
+        if (s->jobs[k].state == 0 && s->jobs[k].spec.arrival <= now) { s->jobs[k].state = 1; s->queue.push_back((int)k); }
+    cudaError_t e = cudaSuccess;
+    // admission: FIFO while a slot and all three pools have room
+    while (!s->queue.empty() && !s->free_slots.empty()) {
+        WServerJob& job = s->jobs[s->queue.front()];
+        const long long nb = (long long)job.M * job.Ne, ns = job.M, nsc = (long long)kMaxWind * job.Ne;
+        const long long bo = s->beads.alloc(nb);
+        if (bo < 0) break;
+        const long long so = s->slices.alloc(ns);
+        if (so < 0) { s->beads.release(bo, nb); break; }
+        const long long co = s->scratch.alloc(nsc);
+        if (co < 0) { s->beads.release(bo, nb); s->slices.release(so, ns); break; }
+        job.bead_off = bo; job.slice_off = so; job.scratch_off = co;
+        job.slot = s->free_slots.back();
+        s->free_slots.pop_back();
+        job.state = 2;
+        job.t_admit = now;
+        const int k = job.slot;
+        s->slot_job[k] = s->queue.front();
+        s->queue.pop_front();
+        WWMeta m{};
+        m.off = bo; m.M = job.M; m.Ne = job.Ne; m.N0 = job.N0; m.mbar = job.mbar;
+        int nu = (int)std::ceil(std::max(job.N0, 1) * job.M / (1.0 * job.mbar));
+        m.num_updates = nu < 100 ? 100 : nu;
+        m.window = -1;                        // grand canonical
+        m.L = (float)job.L; m.Linv = (float)(1.0 / job.L);
+        m.tau = s->p.tau; m.lambda = s->p.lambda; m.mu = job.spec.mu;
+        m.volume = job.L * job.L * job.L;
+        m.C = 1.0 / (1.0 * job.mbar * job.M * m.volume);      // worm constant C0 = 1
+        const double rmorc = s->ap.rm / job.L;
+        const double t2 = s->ap.C6 * std::pow(rmorc, 3.0) / 3.0, t3 = s->ap.C8 * std::pow(rmorc, 5.0) / 5.0,
+                     t4 = s->ap.C10 * std::pow(rmorc, 7.0) / 7.0;
+        m.tailV0 = 2.0 * M_PI * s->ap.epsilon * (-s->ap.rm * s->ap.rm * s->ap.rm * (t2 + t3 + t4));
+        m.sqrtLambdaTau = std::sqrt(s->p.lambda * s->p.tau);
+        m.sqrt2LambdaTau = std::sqrt(2.0) * m.sqrtLambdaTau;
+        const double T = 1.0 / (job.M * s->p.tau);
+        m.comDelta = 0.04 * 2.0 * std::sqrt(M_PI * s->p.lambda / T);
+        const uint64_t sd = job.spec.seed * 0x9E3779B97F4A7C15ull + 0x94D049BB133111EBull;
+        m.key = make_uint2((uint32_t)sd, (uint32_t)(sd >> 32));
+        s->h_meta[k] = m;
+        s->h_nbs_off[k] = so;
+        s->h_scratch_off[k] = co;
+        // seeded closed worldlines: uniform centres, Gaussian jitter per bead
+        std::mt19937_64 rng(job.spec.seed);
+        std::uniform_real_distribution<double> u(-0.5, 0.5);
+        std::normal_distribution<double> g(0.0, std::sqrt(2.0 * s->p.lambda * s->p.tau));
+        std::vector<float4> pp((size_t)job.M * job.Ne, make_float4(0.f, 0.f, 0.f, 0.f));
+        std::vector<int> nx((size_t)job.M * job.Ne, -1);
+        std::vector<int> nbv(job.M, job.N0);
+        for (int i = 0; i < job.N0; ++i) {
+            const double c[3] = {u(rng) * job.L, u(rng) * job.L, u(rng) * job.L};
+            for (int t = 0; t < job.M; ++t) {
+                double r[3];
+                for (int d = 0; d < 3; ++d) { r[d] = c[d] + g(rng); r[d] -= job.L * std::floor(r[d] / job.L + 0.5); }
+                pp[(size_t)t * job.Ne + i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
+                nx[(size_t)t * job.Ne + i] = i;
+            }
+        }
+        WWState st{};
+        for (int i = 0; i < 2; ++i) st.head[i] = st.tail[i] = st.sp1[i] = st.sp2[i] = -1;
+        st.gap = -1; st.diag = 1; st.numBeadsOn = job.N0 * job.M;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_pos + bo, pp.data(), pp.size() * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nxt + bo, nx.data(), nx.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_prv + bo, nx.data(), nx.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nbs + so, nbv.data(), nbv.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_state + k, &st, sizeof(WWState), cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->d_stats + k, 0, sizeof(pgb_worm_walker_stats), s->stream);
+        // the host vectors must live until the copies finish
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return s->cfail(e, "worm server admit");
+    }
+    std::vector<int> active;
+    for (int k = 0; k < s->max_slots; ++k) {
+        if (s->slot_job[k] < 0) { s->h_limit[k] = 0; continue; }
+        WServerJob& job = s->jobs[s->slot_job[k]];
+        // never past the job's end or its current bin
+        const long long left = job.spec.sweeps - job.sweeps_done;
+        const long long bin_left = s->p.bin_sweeps - (job.sweeps_done - job.bin_start);
+        long long cap = std::min(left, bin_left);
+        if (s->p.round_seconds <= 0.0) cap = std::min<long long>(cap, s->p.sweeps_per_round);
+        s->h_limit[k] = (int)std::max<long long>(cap, 1);
+        active.push_back(k);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_meta, s->h_meta.data(), s->max_slots * sizeof(WWMeta), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nbs_off, s->h_nbs_off.data(), s->max_slots * sizeof(long long), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_scratch_off, s->h_scratch_off.data(), s->max_slots * sizeof(long long), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_limit, s->h_limit.data(), s->max_slots * sizeof(int), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess && !active.empty()) e = cudaMemcpyAsync(s->d_order, active.data(), active.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
+    if (e != cudaSuccess) return s->cfail(e, "worm server upload");
+    if (!active.empty()) {
+        const int W = (int)active.size();
+        const bool timed = s->p.round_seconds > 0.0;
+        k_worm_walkers<<<(W + kWWWarps - 1) / kWWWarps, kWWWarps * 32, 0, s->stream>>>(
+            s->d_meta, s->d_pos, s->d_nxt, s->d_prv, s->d_nbs, s->d_nbs_off, s->d_state, s->d_stats,
+            s->d_scratch, s->d_scratch_off, s->az, W, timed ? (1 << 30) : s->p.sweeps_per_round,
+            s->d_order, s->d_limit, timed ? (unsigned long long)(s->p.round_seconds * 1e9) : 0ull);
+        if ((e = cudaGetLastError()) != cudaSuccess) return s->cfail(e, "worm server launch");
+    }
+    std::vector<pgb_worm_walker_stats> st(s->max_slots);
+    e = cudaMemcpyAsync(st.data(), s->d_stats, s->max_slots * sizeof(pgb_worm_walker_stats), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return s->cfail(e, "worm server round");
+    const double t_end = s->now();
+    for (int k : active) {
+        const int jid = s->slot_job[k];
+        WServerJob& job = s->jobs[jid];
+        const pgb_worm_walker_stats& a = st[k];
+        job.sweeps_done = a.sweeps;
+        const bool failed = a.error != 0;
+        const bool finished = failed || job.sweeps_done >= job.spec.sweeps;
+        if (job.sweeps_done - job.bin_start >= s->p.bin_sweeps || (finished && job.sweeps_done > job.bin_start)) {
+            pgb_bin b;
+            b.job = jid;
+            b.bin = job.bins++;
+            b.samples = a.samples - job.samples0;
+            b.energy_per_particle = b.samples > 0 ? (a.energy_sum - job.esum0) / (double)b.samples
+                                                  : std::numeric_limits<double>::quiet_NaN();
+            b.time = t_end;
+            s->bins.push_back(b);
+            if (job.t_first < 0) job.t_first = t_end;
+            job.bin_start = job.sweeps_done;
+            job.samples0 = a.samples;
+            job.esum0 = a.energy_sum;
+        }
+        if (finished) {
+            job.state = 3;
+            job.t_done = t_end;
+            s->bead_updates += a.bead_updates;
+            s->beads.release(job.bead_off, (long long)job.M * job.Ne);
+            s->slices.release(job.slice_off, job.M);
+            s->scratch.release(job.scratch_off, (long long)kMaxWind * job.Ne);
+            s->slot_job[k] = -1;
+            s->free_slots.push_back(k);
+            job.slot = -1;
+        }
+    }
+    int na = 0;
+    for (int k = 0; k < s->max_slots; ++k) na += s->slot_job[k] >= 0;
+    if (n_active) *n_active = na;
+    if (n_queued) *n_queued = (int)s->queue.size();
+    return PGB_OK;
+}
+
+int pgb_worm_server_poll_bins(pgb_worm_server* s, pgb_bin* out, int cap, int* n) {
+    if (!s || !n || cap < 0 || (cap > 0 && !out)) return PGB_EINVAL;
+    const int k = std::min<int>(cap, (int)s->bins.size());
+    for (int i = 0; i < k; ++i) out[i] = s->bins[i];
+    s->bins.erase(s->bins.begin(), s->bins.begin() + k);
+    *n = k;
+    return PGB_OK;
+}
+
+int pgb_worm_server_job_info(pgb_worm_server* s, int jid, pgb_job_info* out) {
+    if (!s || !out || jid < 0 || jid >= (int)s->jobs.size()) return PGB_EINVAL;
+    const WServerJob& j = s->jobs[jid];
+    out->state = j.state;
+    out->arrival = j.spec.arrival;
+    out->admitted = j.t_admit;
+    out->first_bin = j.t_first;
+    out->completed = j.t_done;
+    out->sweeps_done = j.sweeps_done;
+    out->n = j.N0;
+    out->m = j.M;
+    out->bytes = j.bytes;
+    return PGB_OK;
+}
+
+double pgb_worm_server_clock(pgb_worm_server* s) { return s ? s->now() : 0.0; }
+
+int pgb_worm_server_active_bead_updates(pgb_worm_server* s, long long* total) {
+    if (!s || !total) return PGB_EINVAL;
+    std::vector<pgb_worm_walker_stats> st(s->max_slots);
+    cudaError_t e = cudaMemcpyAsync(st.data(), s->d_stats, s->max_slots * sizeof(pgb_worm_walker_stats), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return s->cfail(e, "worm server stats");
+    long long t = s->bead_updates;
+    for (int k = 0; k < s->max_slots; ++k) if (s->slot_job[k] >= 0) t += st[k].bead_updates;
+    *total = t;
     return PGB_OK;
 }
 

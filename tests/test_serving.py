@@ -85,3 +85,34 @@ def test_oversized_job_rejected(pgb):
     s = pgb.Server(1e6, sweeps_per_round=5, bin_sweeps=10)
     with pytest.raises(pgb.PgbError):
         s.submit(n=512, temperature=0.5, sweeps=10, seed=1)
+
+
+# ---------------------------------------------------------------------------
+# grand-canonical jobs: every job a device worm walker at its own mu
+# ---------------------------------------------------------------------------
+def test_grand_canonical_job_same_alone_and_in_mix(pgb):
+    X = dict(n=12, temperature=2.5, sweeps=30, seed=7, mu=-4.0)
+    alone = pgb.Server(2e9, sweeps_per_round=4, bin_sweeps=10, grand_canonical=True)
+    jx = alone.submit(**X)
+    b_alone = [b for b in _run(alone, [jx]) if b["job"] == jx]
+    assert [b["bin"] for b in b_alone] == [0, 1, 2]
+
+    mix = pgb.Server(2e9, sweeps_per_round=4, bin_sweeps=10, grand_canonical=True, round_seconds=0.005)
+    rng = np.random.default_rng(1)
+    others = [mix.submit(n=int(rng.integers(6, 24)), temperature=float(rng.uniform(1.5, 4)),
+                         mu=float(rng.uniform(-10, 0)), sweeps=int(rng.integers(10, 40)), seed=300 + k,
+                         arrival=0.01 * k) for k in range(6)]
+    jm = mix.submit(**X)
+    bins = _run(mix, others + [jm])
+    b_mix = [b for b in bins if b["job"] == jm]
+    # the same sweeps in every bin, whatever the rounds: identical bins
+    assert [(b["bin"], b["samples"]) for b in b_mix] == [(b["bin"], b["samples"]) for b in b_alone]
+    ea = np.array([b["energy"] for b in b_alone])
+    em = np.array([b["energy"] for b in b_mix])
+    assert np.array_equal(np.isnan(ea), np.isnan(em))
+    ok = ~np.isnan(ea)
+    assert np.array_equal(ea[ok], em[ok])
+    for j in others + [jm]:
+        info = mix.job(j)
+        assert info["state"] == 3 and info["sweeps_done"] > 0 and info["first_bin"] >= info["admitted"]
+    assert mix.bead_updates() > 0
