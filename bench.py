@@ -325,7 +325,8 @@ def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02, grand_
     srv.close()
     return {"bead_updates_per_s": bu / elapsed, "window_s": round(elapsed, 2), "rounds": rounds,
             "jobs_arrived": len(arrived), "jobs_admitted": sum(1 for i in arrived if i["admitted"] >= 0),
-            "jobs_with_first_bin": len(ttfb), "jobs_completed": len(done), "bins": nbins,
+            "jobs_with_first_bin": len(ttfb), "jobs_completed": len(done),
+            "jobs_failed": sum(1 for i in arrived if i["state"] == 4), "bins": nbins,
             "peak_active": peak_active,
             "ttfb_p50_s": pct(ttfb, 50), "ttfb_p99_s": pct(ttfb, 99),
             "completion_p50_s": pct(done, 50), "completion_p99_s": pct(done, 99),

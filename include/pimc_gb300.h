@@ -356,7 +356,9 @@ typedef struct {
     double    time;            /* server clock when the bin became available */
 } pgb_bin;
 typedef struct {
-    int       state;           /* 0 submitted, 1 queued, 2 on the device, 3 done */
+    int       state;           /* 0 submitted, 1 queued, 2 on the device, 3 done,
+                                  4 stopped by a walker error (worm server: the job's
+                                  bead capacity 2 n + 8 per slice ran out) */
     double    arrival, admitted, first_bin, completed;  /* -1 when not yet */
     long long sweeps_done;
     int       n, m;

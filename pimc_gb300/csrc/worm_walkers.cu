@@ -21,6 +21,20 @@
 // sums spread a bead's same-slice partners over the lanes.  Links store the
 // partner particle only: next(t, p) is on slice t + 1 and prev on t - 1.
 //
+// Latency, not throughput, bounds a walker: a move is a chain of dependent
+// link loads and warp reductions.  So (1) a move walks its range once and
+// caches the beads in shared memory (chain[]), and the actions, saves,
+// restores and centre-of-mass shifts index that cache, lane-parallel where
+// the beads are independent; (2) the pair terms of a lane have no branches
+// (absent partners add zero), so its four partner terms schedule together;
+// (3) the heavy helpers (pair sums, tower sampling, staging positions, bead
+// insertion and deletion, the energy) are not inlined: one copy of each
+// serves all twelve moves, which keeps the kernel's hot code within the
+// instruction cache when the warps of one SM run different moves; (4) one
+// walker per CTA, launched largest first, spreads the largest walkers over
+// the SMs; (5) a staging move's normal deviates come from the lanes together
+// (normals()), in the same order and from the same words as serial draws.
+//
 // Differences from the reference, all documented where they occur:
 //  * the swap pivot is drawn from the pivot slice's beads in index order
 //    (the reference walks its LookupTable hash, whose order depends on the
@@ -58,7 +72,11 @@ struct WWState {
     int gap, length, diag, numBeadsOn;
     float sep[3];
     int err;
-    unsigned long long ctr;          // sweeps made: the random stream's sweep index
+    unsigned long long ctr;          // sweeps completed: the random stream's sweep index
+    // a sweep stopped part-way by the time budget: moves made in it and the
+    // random stream's position (draw-block counter and word index)
+    int upd, rbidx;
+    unsigned long long rctr;
 };
 
 struct WB { int t, p; };
@@ -69,9 +87,10 @@ enum { WM_COM = 0, WM_DIAG, WM_OPEN, WM_CLOSE, WM_INSERT, WM_REMOVE, WM_AH, WM_R
        WM_SH, WM_ST, WM_N };
 enum { WERR_FULL = 1, WERR_LINK = 2, WERR_LOOP = 3 };
 
-constexpr int kWWWarps = 4;          // walkers per CTA
+constexpr int kWWWarps = 1;          // walkers per CTA: one, so the largest walkers spread over the SMs
 constexpr int kOrigCap = 72;         // saved positions per move (Mbar - 1 <= 63)
 constexpr int kMaxWind = 27;         // (2 maxWind + 1)^3 with maxWind = 1
+constexpr int kChainCap = 1024;      // beads of one move's range cached per walker (M < 1024)
 
 // Aziz V with the reference's hard-core branch (potential.cpp:1821-1843):
 // below x = 0.01 the attractive part is dropped
@@ -79,6 +98,21 @@ __device__ __forceinline__ float aziz_v32_core(float r2, const AzizF& a) {
     const float x = sqrtf(r2) * a.rminv;
     if (x < 0.01f) return a.eps * a.A * __expf(x * fmaf(a.beta, x, -a.alpha));
     return aziz_v32(r2, a);
+}
+// the same without branches, so that the pair terms of a lane schedule
+// together: below x = 0.01 the attractive terms are selected away
+__device__ __forceinline__ float aziz_v32_sel(float r2, const AzizF& a) {
+    const float rinv = rsqrtf(r2);
+    const float x = r2 * rinv * a.rminv;
+    const float ix = rinv * a.rm;
+    const float ix2 = ix * ix;
+    const float ix6 = ix2 * ix2 * ix2;
+    const bool core = x < 0.01f;
+    const float poly = core ? 0.0f : ix6 * fmaf(ix2, fmaf(ix2, a.C10, a.C8), a.C6);
+    const float urep = a.A * __expf(x * fmaf(a.beta, x, -a.alpha));
+    const float t = fmaxf(fmaf(a.D, ix, -1.0f), 0.0f);
+    const float F = core ? 0.0f : __expf(-t * t);
+    return a.eps * fmaf(-poly, F, urep);
 }
 
 struct WormWalker {
@@ -88,7 +122,9 @@ struct WormWalker {
     int* nxt;
     int* prv;
     int* nbs;
-    double* scratch;                 // per-walker tower-sampling scratch, kMaxWind * Ne
+    double* scratch;                 // per-walker scratch, kMaxWind * Ne
+    int* chain;                      // shared: the beads of the current move's range, packed
+    float* znorm;                    // shared: a move's normal deviates, 3 (Mbar - 1) at most
     int lane;
     // uniform scalar state
     WB head, tail, sp1, sp2;
@@ -123,13 +159,68 @@ struct WormWalker {
     // FP64 transcendentals are slow on this GPU
     __device__ float rand() { return (float)u32() * 2.3283064365386963e-10f; }
     __device__ float randExc() { return (float)(u32() >> 8) * 5.9604644775390625e-08f; }
-    __device__ float randNorm(float mean, float sd) {
+    // polar-method deviate z; randNorm(mean, sd) is mean + z * sd
+    __device__ __noinline__ float randNormZ() {
         float x, y, r;
         int guard = 0;
-        do { x = 2.0f * rand() - 1.0f; y = 2.0f * rand() - 1.0f; r = x * x + y * y; }
+        do {
+            x = 2.0f * rand() - 1.0f;
+            y = 2.0f * rand() - 1.0f;
+            r = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));    // no contraction: normals() rounds alike
+        }
         while ((r >= 1.0f || r == 0.0f) && ++guard < 1000);
-        if (r >= 1.0f || r == 0.0f) return mean;
-        return mean + x * sqrtf(-2.0f * logf(r) / r) * sd;
+        if (r >= 1.0f || r == 0.0f) return 0.0f;
+        return x * sqrtf(-2.0f * logf(r) / r);
+    }
+    __device__ float randNorm(float mean, float sd) { return mean + randNormZ() * sd; }
+    // word i ahead in the stream (rem = words left in buf)
+    __device__ uint32_t wordAhead(long long i, int rem) const {
+        if (i < rem) {
+            const int q = bidx + (int)i;
+            return q == 0 ? buf.x : q == 1 ? buf.y : q == 2 ? buf.z : buf.w;
+        }
+        const long long j = i - rem;
+        const unsigned long long c = ctr + (unsigned long long)(j >> 2);
+        const uint4 w = philox4x32(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0x574F524Du, 0u), m.key);
+        const int q = (int)(j & 3);
+        return q == 0 ? w.x : q == 1 ? w.y : q == 2 ? w.z : w.w;
+    }
+    // the next cnt deviates that cnt calls of randNormZ() would return, made
+    // by the lanes together from the same words: lane l tests attempt
+    // a = base + l on words 2a and 2a + 1, the accepted attempts in order
+    // give the deviates, and the stream then moves past the last attempt
+    // used, exactly where the serial draws would leave it
+    __device__ __noinline__ void normals(int cnt, float* out) {
+        const int rem = 4 - bidx;
+        int have = 0;
+        long long base = 0, used = 0;
+        for (int round = 0; have < cnt && round < 64; ++round, base += 32) {
+            const long long a = base + lane;
+            const float x = 2.0f * ((float)wordAhead(2 * a, rem) * 2.3283064365386963e-10f) - 1.0f;
+            const float y = 2.0f * ((float)wordAhead(2 * a + 1, rem) * 2.3283064365386963e-10f) - 1.0f;
+            const float r = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));
+            const bool ok = !(r >= 1.0f || r == 0.0f);
+            const unsigned mask = __ballot_sync(0xffffffffu, ok);
+            const int rank = __popc(mask & ((1u << lane) - 1u));
+            if (ok && have + rank < cnt) out[have + rank] = x * sqrtf(-2.0f * logf(r) / r);
+            const unsigned last = __ballot_sync(0xffffffffu, ok && rank == cnt - have - 1);
+            if (last) used = 2 * (base + __ffs(last));
+            have += __popc(mask);
+        }
+        if (have < cnt) {                           // never in practice: 2048 attempts
+            for (int i = have + lane; i < cnt; i += 32) out[i] = 0.0f;
+            used = 2 * base;
+        }
+        if (used <= rem) {
+            bidx += (int)used;
+        } else {
+            const long long wb = used - rem, nb = (wb + 3) >> 2;
+            const unsigned long long c = ctr + (unsigned long long)(nb - 1);
+            buf = philox4x32(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0x574F524Du, 0u), m.key);
+            ctr = c + 1;
+            bidx = (int)(wb - 4 * (nb - 1));
+        }
+        __syncwarp();
     }
 
     // ---- path access ----
@@ -189,64 +280,102 @@ struct WormWalker {
     }
     __device__ float putInBC(float x) const { return x - m.L * floorf(x * m.Linv + 0.5f); }
 
+    // ---- pair sums ----
+    // A bead is packed as slice << 12 | particle (Ne <= 4096, M < kChainCap).
+    __device__ static int pack(WB b) { return (b.t << 12) | b.p; }
+    __device__ static WB unpack(int c) { return {c >> 12, c & 4095}; }
+    __device__ size_t at(int c) const { return (size_t)(c >> 12) * m.Ne + (c & 4095); }
+
+    // one bead's loads, all independent of one another: its slice's bead
+    // count, its own position and the first 128 same-slice positions
+    // (issued for every index below Ne, used below the count)
+    struct BeadLoad { WB b; int n; float4 rb; float4 r[4]; };
+    __device__ void loadBead(int c, BeadLoad& L) {
+        L.b = unpack(c);
+        const bool ok = valid(L.b);
+        if (!ok) { err = WERR_LINK; L.b = WB{0, 0}; }
+        const float4* row = pos + (size_t)L.b.t * m.Ne;
+        L.n = ok ? nbs[L.b.t] : 0;
+        L.rb = row[L.b.p];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = 32 * u + lane;
+            L.r[u] = j < m.Ne ? row[j] : L.rb;
+        }
+    }
+    // one pair term, without branches: a partner that is absent (j at or
+    // beyond the count, or the bead itself) adds zero
+    __device__ void pairTerm(WB b, int s1, int j, int n, float4 rb, float4 rj, KahanF& k) {
+        const bool ok = j < n && j != b.p;
+        const float f = ok ? factor(s1, state(WB{b.t, j})) : 0.0f;
+        const float dx = min_image32(rj.x - rb.x, m.L, m.Linv);
+        const float dy = min_image32(rj.y - rb.y, m.L, m.Linv);
+        const float dz = min_image32(rj.z - rb.z, m.L, m.Linv);
+        const float r2 = ok ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : 1.0f;
+        k.add(f * aziz_v32_sel(r2, az));
+    }
+    // tau-less pair terms of a loaded bead with its active same-slice
+    // partners, added to the lane's running sum in ascending partner order
+    __device__ void pairsLoaded(const BeadLoad& L, KahanF& k) {
+        const int s1 = state(L.b);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) pairTerm(L.b, s1, 32 * u + lane, L.n, L.rb, L.r[u], k);
+        const float4* row = pos + (size_t)L.b.t * m.Ne;
+        for (int j0 = 128; j0 < L.n; j0 += 128) {
+            float4 r[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int j = j0 + 32 * u + lane;
+                r[u] = j < L.n ? row[j] : L.rb;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) pairTerm(L.b, s1, j0 + 32 * u + lane, L.n, L.rb, r[u], k);
+        }
+    }
     // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
     // tau * sum over the other active beads of the slice of factor * V
-    __device__ double bare(WB b) {
+    __device__ __noinline__ double bare(WB b) {
         if (!valid(b)) { err = WERR_LINK; return 0.0; }
-        const float4 rb = P(b);
-        const int s1 = state(b);
-        const int n = nb(b.t);
+        BeadLoad L;
+        loadBead(pack(b), L);
         KahanF k;
-        for (int j = lane; j < n; j += 32) {
-            if (j == b.p) continue;
-            const WB o{b.t, j};
-            const float f = factor(s1, state(o));
-            if (f == 0.f) continue;
-            const float4 rj = pos[(size_t)b.t * m.Ne + j];
-            const float dx = min_image32(rj.x - rb.x, m.L, m.Linv);
-            const float dy = min_image32(rj.y - rb.y, m.L, m.Linv);
-            const float dz = min_image32(rj.z - rb.z, m.L, m.Linv);
-            k.add(f * aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+        pairsLoaded(L, k);
+        return m.tau * warp_sum_ff(k);
+    }
+    // potentialAction over chain[c0 .. c0 + cnt - 1]: the lanes keep one
+    // running sum over the whole range and reduce once
+    __device__ __noinline__ double chainAction(int c0, int cnt) {
+        KahanF k;
+        for (int c = 0; c < cnt; ++c) {
+            BeadLoad cur;
+            loadBead(chain[c0 + c], cur);
+            if (cur.b.p < cur.n) pairsLoaded(cur, k);
         }
         return m.tau * warp_sum_ff(k);
     }
-    // one bead's pair terms, accumulated into a lane's running sum
-    __device__ void bareTerms(WB b, KahanF& k) {
-        const float4 rb = P(b);
-        const int s1 = state(b);
-        const int n = nb(b.t);
-        for (int j = lane; j < n; j += 32) {
-            if (j == b.p) continue;
-            const WB o{b.t, j};
-            const float f = factor(s1, state(o));
-            if (f == 0.f) continue;
-            const float4 rj = pos[(size_t)b.t * m.Ne + j];
-            const float dx = min_image32(rj.x - rb.x, m.L, m.Linv);
-            const float dy = min_image32(rj.y - rb.y, m.L, m.Linv);
-            const float dz = min_image32(rj.z - rb.z, m.L, m.Linv);
-            k.add(f * aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
-        }
-    }
-    // potentialAction over the active beads from s to e along next links:
-    // the lanes keep one running sum over the whole range and reduce once
-    __device__ double rangeAction(WB s, WB e) {
-        KahanF k;
+    // the beads from s to e along next links into chain[0 ..]: returns their
+    // count, 0 with the error word set when the range breaks or is longer
+    // than the cache
+    __device__ int walk(WB s, WB e) {
         WB b = s;
-        const WB stop = next(e);
-        for (int g = 0; g <= m.M * m.Ne; ++g) {
-            if (isXW(b) || err) { err = err ? err : WERR_LINK; break; }
-            if (b.p < nb(b.t)) bareTerms(b, k);
+        for (int k = 0; k < kChainCap; ++k) {
+            if (isXW(b) || err) { err = err ? err : WERR_LINK; return 0; }
+            if (lane == 0) chain[k] = pack(b);
+            if (eqW(b, e)) { __syncwarp(); return k + 1; }
             b = next(b);
-            if (eqW(b, stop)) return m.tau * warp_sum_ff(k);
         }
-        if (!err) err = WERR_LOOP;
-        return m.tau * warp_sum_ff(k);
+        err = WERR_LOOP;
+        return 0;
+    }
+    __device__ double rangeAction(WB s, WB e) {
+        const int cnt = walk(s, e);
+        return chainAction(0, cnt);
     }
     // the primitive action has no gradient correction (gradVFactor = 0)
     __device__ double corrRange(WB, WB) { return 0.0; }
 
     // ---- Path bookkeeping (path.cpp:205-420) ----
-    __device__ WB addBead(int slice, float x, float y, float z) {
+    __device__ __noinline__ WB addBead(int slice, float x, float y, float z) {
         const int k = nb(slice);
         if (k >= m.Ne) { err = WERR_FULL; return {-1, -1}; }
         WB last{slice, k};
@@ -270,7 +399,7 @@ struct WormWalker {
         setPrev(nb_, b); setNext(b, nb_);
         return b;
     }
-    __device__ void delBead(WB b) {
+    __device__ __noinline__ void delBead(WB b) {
         if (!valid(b)) { err = WERR_LINK; return; }
         const int k = nb(b.t) - 1;
         setNb(b.t, k);
@@ -301,7 +430,7 @@ struct WormWalker {
         gap = -1; length = 0; sep[0] = sep[1] = sep[2] = 0.f;
         head = tail = sp1 = sp2 = WB{-1, -1};
     }
-    __device__ void wormUpdate(WB nh, WB nt) {
+    __device__ __noinline__ void wormUpdate(WB nh, WB nt) {
         head = nh; tail = nt;
         gap = nt.t - nh.t;
         if (gap < 0) gap += m.M;
@@ -347,7 +476,7 @@ struct WormWalker {
         return w;
     }
     // sampleWindingSector (move.cpp:362-397)
-    __device__ int3 sampleWinding(WB sb, WB eb, int L, double& totald) {
+    __device__ __noinline__ int3 sampleWinding(WB sb, WB eb, int L, double& totald) {
         const float4 pe = P(eb), ps = P(sb);
         const float vx = pe.x - ps.x, vy = pe.y - ps.y, vz = pe.z - ps.z;
         float cum[kMaxWind];
@@ -364,15 +493,16 @@ struct WormWalker {
         for (int n = 0; n < kMaxWind; ++n) if (cum[n] / total >= x) { idx = n; break; }
         return winding(idx);
     }
-    // newStagingPosition with winding (move.cpp:301-338)
-    __device__ void stagingPos(WB nbd, WB eb, int L, int k, int3& wind, float& x, float& y, float& z) {
+    // newStagingPosition with winding (move.cpp:301-338): np is the previous
+    // bead's (new) position, e the range's end bead, z the three deviates
+    __device__ void stagingPosZ(float4 np, float4 e, int L, int k, int3& wind, float zx, float zy, float zz,
+                                float& x, float& y, float& z) {
         const float f1 = 1.0f * (L - k - 1), f2 = 1.0f / (1.0f * (L - k));
         const float sg = (float)m.sqrt2LambdaTau * sqrtf(f1 * f2);
-        const float4 np = P(nbd), e = P(eb);
         float rx = ((e.x + m.L * wind.x) - np.x) * f2 + np.x;
         float ry = ((e.y + m.L * wind.y) - np.y) * f2 + np.y;
         float rz = ((e.z + m.L * wind.z) - np.z) * f2 + np.z;
-        rx = randNorm(rx, sg); ry = randNorm(ry, sg); rz = randNorm(rz, sg);
+        rx = rx + zx * sg; ry = ry + zy * sg; rz = rz + zz * sg;
         // the winding sector follows the sampled point (move.cpp:327-336)
         const float h = 0.5f * m.L;
         for (int g = 0; g < 64 && rx < -h; ++g) { ++wind.x; rx += m.L; }
@@ -383,7 +513,38 @@ struct WormWalker {
         for (int g = 0; g < 64 && rz >= h; ++g) { --wind.z; rz -= m.L; }
         x = putInBC(rx); y = putInBC(ry); z = putInBC(rz);
     }
-    __device__ void freePos(WB nbd, float& x, float& y, float& z) {
+    __device__ __noinline__ void stagingPosR(float4 np, float4 e, int L, int k, int3& wind, float& x, float& y,
+                                             float& z) {
+        const float zx = randNormZ(), zy = randNormZ(), zz = randNormZ();
+        stagingPosZ(np, e, L, k, wind, zx, zy, zz, x, y, z);
+    }
+    __device__ void stagingPos(WB nbd, WB eb, int L, int k, int3& wind, float& x, float& y, float& z) {
+        stagingPosR(P(nbd), P(eb), L, k, wind, x, y, z);
+    }
+    // new staging positions for chain[1 .. cnt] from chain[0]'s position
+    // towards e, written by lane 0 and published once
+    __device__ void stageChain(int cnt, float4 start, float4 e, int L, int3& wind) {
+        normals(3 * cnt, znorm);
+        float4 pp = start;
+        for (int k = 0; k < cnt; ++k) {
+            float x, y, z;
+            stagingPosZ(pp, e, L, k, wind, znorm[3 * k], znorm[3 * k + 1], znorm[3 * k + 2], x, y, z);
+            pp = make_float4(x, y, z, 0.f);
+            if (lane == 0) pos[at(chain[k + 1])] = pp;
+        }
+        __syncwarp();
+    }
+    // save / restore chain[1 .. cnt] positions, lane-parallel
+    __device__ void saveChain(int cnt, float4* orig) {
+        for (int i = lane; i < cnt; i += 32) orig[i] = pos[at(chain[i + 1])];
+        __syncwarp();
+    }
+    __device__ void restoreChain(int cnt, const float4* orig) {
+        __syncwarp();
+        for (int i = lane; i < cnt; i += 32) pos[at(chain[i + 1])] = orig[i];
+        __syncwarp();
+    }
+    __device__ __noinline__ void freePos(WB nbd, float& x, float& y, float& z) {
         const float4 p = P(nbd);
         const float sg = (float)m.sqrt2LambdaTau;
         x = putInBC(randNorm(p.x, sg));
@@ -396,51 +557,66 @@ struct WormWalker {
     __device__ int trueN() const { return numBeadsOn / m.M; }
 
     // ---- diagonal moves ----
-    // CenterOfMassMove (move.cpp:1124-1262)
+    // CenterOfMassMove (move.cpp:1124-1262).  The worldline through a
+    // random bead of slice 0 is cached in chain[c0 .. c0 + wl - 1]: for a
+    // closed single-particle loop by one walk back from that bead (its
+    // k-th predecessor lands at M - k), for the worm's segment by a walk
+    // back to its start and one forward; ranges longer than M beads are not
+    // moved, as in the reference.
     __device__ int com(bool& accepted) {
         accepted = false;
         if (numBeadsOn == 0 || nb(0) == 0) return 0;
         const WB first{0, (int)randInt((uint32_t)(nb(0) - 1))};
-        WB sb = first, eb;
-        if (!isXW(prev(sb))) {
-            for (int g = 0; g <= m.M * m.Ne; ++g) {
-                sb = prev(sb);
-                if (eqW(prev(sb), first) || isXW(prev(sb))) break;
+        WB b = first;
+        int back = 0;
+        bool closed = false;
+        for (;;) {
+            const WB pb = prev(b);
+            if (err) return 0;
+            if (isXW(pb)) break;
+            if (eqW(pb, first)) { closed = true; break; }
+            if (back + 1 >= m.M) return 0;
+            ++back;
+            b = pb;
+            if (lane == 0) chain[m.M - back] = pack(b);
+        }
+        int c0 = 0, wl = 0;
+        if (closed) {
+            c0 = m.M - back - 1;
+            wl = back + 1;
+            if (lane == 0) chain[c0] = pack(first);
+        } else {
+            for (WB s = b;;) {
+                if (wl >= m.M) return 0;
+                if (lane == 0) chain[wl] = pack(s);
+                ++wl;
+                const WB ns = next(s);
+                if (err) return 0;
+                if (isXW(ns)) break;
+                s = ns;
             }
         }
-        if (eqW(prev(sb), first)) { sb = first; eb = prev(sb); }
-        else {
-            eb = first;
-            for (int g = 0; g <= m.M * m.Ne && !isXW(next(eb)); ++g) eb = next(eb);
-        }
-        int wl = 0;
-        WB b = sb;
-        const WB stop = next(eb);
-        do { ++wl; b = next(b); } while (!eqW(b, stop) && !isXW(b) && wl <= m.M * m.Ne);
-        if (err || wl > m.M) return 0;
+        __syncwarp();
         acc->attempted[WM_COM]++;
         float sh[3];
         for (int i = 0; i < 3; ++i) sh[i] = (float)m.comDelta * (-0.5f + rand());
-        const double oldA = rangeAction(sb, eb);
-        b = sb;
-        for (int g = 0; g < wl; ++g) {
-            const float4 r = P(b);
-            setP(b, (float)putInBC(r.x + sh[0]), (float)putInBC(r.y + sh[1]), (float)putInBC(r.z + sh[2]));
-            b = next(b);
-        }
-        const double newA = rangeAction(sb, eb);
+        const double oldA = chainAction(c0, wl);
+        shiftChain(c0, wl, sh[0], sh[1], sh[2]);
+        const double newA = chainAction(c0, wl);
         if (metro(newA - oldA)) { accepted = true; acc->accepted[WM_COM]++; }
-        else {
-            b = sb;
-            for (int g = 0; g < wl; ++g) {
-                const float4 r = P(b);
-                setP(b, (float)putInBC(r.x - sh[0]), (float)putInBC(r.y - sh[1]), (float)putInBC(r.z - sh[2]));
-                b = next(b);
-            }
-        }
+        else shiftChain(c0, wl, -sh[0], -sh[1], -sh[2]);
         return wl;
     }
-    // StagingMove (move.cpp:1315-1412) with winding sectors
+    __device__ void shiftChain(int c0, int cnt, float sx, float sy, float sz) {
+        for (int i = lane; i < cnt; i += 32) {
+            const size_t q = at(chain[c0 + i]);
+            const float4 r = pos[q];
+            pos[q] = make_float4(putInBC(r.x + sx), putInBC(r.y + sy), putInBC(r.z + sz), 0.f);
+        }
+        __syncwarp();
+    }
+    // StagingMove (move.cpp:1315-1412) with winding sectors: chain[0] is the
+    // start bead, chain[L] the end bead, chain[1 .. L-1] are restaged
     __device__ int staging(bool& accepted, float4* orig) {
         accepted = false;
         if (numBeadsOn == 0 || trueN() == 0) return 0;
@@ -451,32 +627,25 @@ struct WormWalker {
         const int L = 2 + (int)randInt((uint32_t)(m.mbar - 2));
         WB b = sb;
         for (int k = 0; k < L; ++k) {
-            if (b.p >= nb(b.t) || isXW(next(b))) return 0;
-            b = next(b);
+            if (b.p >= nb(b.t)) return 0;
+            const WB nb_ = next(b);
+            if (isXW(nb_)) return 0;
+            if (lane == 0) chain[k] = pack(b);
+            b = nb_;
         }
+        if (lane == 0) chain[L] = pack(b);
+        __syncwarp();
         const WB eb = b;
         acc->attempted[WM_DIAG]++;
         double tot;
         int3 wind = sampleWinding(sb, eb, L, tot);
-        const WB pe = prev(eb);
-        const double oldA = rangeAction(sb, pe);
-        b = sb;
-        int k = 0;
-        do {
-            b = next(b);
-            if (k >= kOrigCap) { err = WERR_LOOP; return 0; }
-            orig[k] = P(b);
-            float x, y, z;
-            stagingPos(prev(b), eb, L, k, wind, x, y, z);
-            setP(b, (float)x, (float)y, (float)z);
-            ++k;
-        } while (!eqW(b, pe) && k < L);
-        const double newA = rangeAction(sb, pe);
+        if (L - 1 > kOrigCap) { err = WERR_LOOP; return 0; }
+        const double oldA = chainAction(0, L);
+        saveChain(L - 1, orig);
+        stageChain(L - 1, P(sb), P(eb), L, wind);
+        const double newA = chainAction(0, L);
         if (metro(newA - oldA)) { accepted = true; acc->accepted[WM_DIAG]++; }
-        else {
-            b = sb;
-            for (int i = 0; i < k; ++i) { b = next(b); setP(b, orig[i].x, orig[i].y, orig[i].z); }
-        }
+        else restoreChain(L - 1, orig);
         return L - 1;
     }
 
@@ -799,52 +968,78 @@ struct WormWalker {
         rtUndo();
         return 0;
     }
-    // SwapMoveBase::getNorm + selectPivotBead (move.cpp:3223-3330) over the
-    // pivot slice's beads in index order: weights rho0 for every bead and
-    // winding sector, a warp-parallel tower.  Returns Sigma; with x >= 0 the
-    // pivot and its winding sector are selected for the uniform deviate x.
-    __device__ double towerNorm(WB b, int pivotSlice, int sign, float x, WB& pivot, int3& wind) {
+    // SwapMoveBase::getNorm + selectPivotBead (move.cpp:3212-3338) over the
+    // pivot slice's beads in index order.  Lane w (< 27) accumulates the
+    // weight of winding sector w summed over the slice; Sigma is the total.
+    // With x >= 0 the pivot is the first (sector, bead) in the reference's
+    // order (bead fastest, sector slowest) whose cumulative weight reaches
+    // x * Sigma: the sector by a scan over the lanes' sector sums, the bead
+    // by a scan inside that sector.
+    __device__ float rho0Shifted(float4 pf, float4 pb, int3 wv, int sign, float g3, float den) const {
+        const float ax = (pf.x - pb.x) + (sign * wv.x) * m.L, ay = (pf.y - pb.y) + (sign * wv.y) * m.L,
+                    az_ = (pf.z - pb.z) + (sign * wv.z) * m.L;
+        return g3 * expf(-(ax * ax + ay * ay + az_ * az_) / den);
+    }
+    __device__ __noinline__ double towerNorm(WB b, int pivotSlice, int sign, float x, WB& pivot, int3& wind) {
         const int nL = nb(pivotSlice);
-        const int total = nL * kMaxWind;
         const float4 pb = P(b);
-        float* sc = reinterpret_cast<float*>(scratch);
-        // weights in the reference's order: n fastest, winding sector slowest
-        float sum = 0.0f;
-        for (int i = lane; i < total; i += 32) {
-            const int w = i / nL, n = i - w * nL;
-            const int3 wv = winding(w);
-            const float4 pf = pos[(size_t)pivotSlice * m.Ne + n];
-            float sx = pf.x - pb.x, sy = pf.y - pb.y, sz = pf.z - pb.z;
-            if (w > 0) { sx += (sign * wv.x) * m.L; sy += (sign * wv.y) * m.L; sz += (sign * wv.z) * m.L; }
-            const float r = rho0(sx * sx + sy * sy + sz * sz, m.mbar);
-            sc[i] = r;
-            sum += r;
+        const float4* row = pos + (size_t)pivotSlice * m.Ne;
+        const float den = (float)(4.0 * m.lambda * m.mbar * m.tau);
+        const float g = rsqrtf(3.14159265358979f * den);
+        const float g3 = g * g * g;
+        float mine = 0.0f;                       // lane w: sector w's weight
+        for (int n0 = 0; n0 < nL; n0 += 128) {
+            float4 pf[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int n = n0 + 32 * u + lane;
+                pf[u] = n < nL ? row[n] : pb;
+            }
+            for (int w = 0; w < kMaxWind; ++w) {
+                const int3 wv = winding(w);
+                float v = 0.0f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float r = rho0Shifted(pf[u], pb, wv, sign, g3, den);
+                    v += n0 + 32 * u + lane < nL ? r : 0.0f;
+                }
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == w) mine += v;
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        __syncwarp();
+        // inclusive scan of the sector sums over lanes 0..26
+        float cum = lane < kMaxWind ? mine : 0.0f;
+        for (int o = 1; o < 32; o <<= 1) {
+            const float u = __shfl_up_sync(0xffffffffu, cum, o);
+            if (lane >= o) cum += u;
+        }
+        const float sum = __shfl_sync(0xffffffffu, cum, kMaxWind - 1);
         if (x >= 0.0f) {
-            // first index whose cumulative weight reaches x * Sigma
             const float target = x * sum;
-            float carry = 0.0f;
-            int found = total - 1;
-            for (int base = 0; base < total; base += 32) {
-                const int i = base + lane;
-                float v = i < total ? sc[i] : 0.0f;
+            const unsigned hs = __ballot_sync(0xffffffffu, lane < kMaxWind && cum >= target);
+            const int ws = hs ? __ffs(hs) - 1 : kMaxWind - 1;
+            const float before = __shfl_sync(0xffffffffu, cum - mine, ws);
+            const int3 wv = winding(ws);
+            float carry = before;
+            int found = nL - 1;
+            for (int base = 0; base < nL; base += 32) {
+                const int n = base + lane;
+                float v = n < nL ? rho0Shifted(row[n], pb, wv, sign, g3, den) : 0.0f;
                 for (int o = 1; o < 32; o <<= 1) {
                     const float u = __shfl_up_sync(0xffffffffu, v, o);
                     if (lane >= o) v += u;
                 }
-                const float cum = carry + v;
-                const unsigned hit = __ballot_sync(0xffffffffu, i < total && cum >= target);
-                if (hit) { found = base + __ffs(hit) - 1; break; }
+                const unsigned h = __ballot_sync(0xffffffffu, n < nL && carry + v >= target);
+                if (h) { found = base + __ffs(h) - 1; break; }
                 carry += __shfl_sync(0xffffffffu, v, 31);
             }
-            const int w = found / nL, n = found - w * nL;
-            pivot = WB{pivotSlice, n};
-            wind = winding(w);
+            pivot = WB{pivotSlice, found};
+            wind = wv;
         }
         return (double)sum;
     }
+    // SwapHeadMove (move.cpp:3388-3622): chain[0 .. Mbar] runs from the swap
+    // bead to the pivot; after relinking chain[0] is the old head
     __device__ int swapHead(float4* orig) {
         if (numBeadsOn == 0 || diag) return -1;
         const int swapLength = m.mbar;
@@ -856,63 +1051,46 @@ struct WormWalker {
         WB b = pivot;
         for (int k = 0; k < swapLength; k++) {
             if (eqW(b, tail) || isXW(b)) return -1;
+            if (lane == 0) chain[swapLength - k] = pack(b);
             b = prev(b);
         }
         const WB swp = b;
         if (isXW(swp) || eqW(tail, swp)) return -1;
+        if (lane == 0) chain[0] = pack(swp);
+        __syncwarp();
         acc->attempted[WM_SH]++;
         WB dummy; int3 dw;
         const double SigmaSwap = towerNorm(swp, pivotSlice, 1, -1.0f, dummy, dw);
         const float PNorm = (float)fmin(SigmaHead / SigmaSwap, 1.0);
         if (rand() < PNorm) {
+            const int nm = swapLength - 1;
             sp1 = swp; sp2 = pivot;
-            int k = 0;
-            b = swp;
-            const WB stopB = next(pivot);
-            for (int g = 0; g <= m.M; ++g) {
-                if (!eqW(b, swp) && !eqW(b, pivot) && k < kOrigCap) orig[k++] = P(b);
-                b = next(b);
-                if (eqW(b, stopB) || isXW(b)) break;
-            }
-            const double oldA = rangeAction(swp, pivot);
+            saveChain(nm, orig);
+            const double oldA = chainAction(0, swapLength + 1);
             const WB nextSwap = next(swp);
             setNext(head, nextSwap);
             setNext(swp, {-1, -1});
             setPrev(nextSwap, head);
             sp1 = head;
             head = swp;
-            b = sp1;
-            k = 0;
-            for (int g = 0; g <= m.M; ++g) {
-                if (!eqW(b, sp1) && !eqW(b, pivot)) {
-                    float x, y, z;
-                    stagingPos(prev(b), pivot, swapLength, k, wind, x, y, z);
-                    setP(b, (float)x, (float)y, (float)z);
-                    ++k;
-                    acc->bead_updates++;
-                }
-                b = next(b);
-                if (eqW(b, stopB) || isXW(b)) break;
-            }
-            const double newA = rangeAction(sp1, pivot);
+            if (lane == 0) chain[0] = pack(sp1);
+            stageChain(nm, P(sp1), P(pivot), swapLength, wind);
+            acc->bead_updates += nm;
+            const double newA = chainAction(0, swapLength + 1);
             if (metro(newA - oldA)) { acc->accepted[WM_SH]++; wormUpdate(swp, tail); return 1; }
             head = sp1;
             setNext(head, {-1, -1});
             setNext(swp, nextSwap);
             setPrev(nextSwap, swp);
-            b = next(swp);
-            k = 0;
-            for (int g = 0; g <= m.M && !eqW(b, pivot) && !isXW(b) && k < kOrigCap; ++g) {
-                setP(b, orig[k].x, orig[k].y, orig[k].z);
-                ++k;
-                b = next(b);
-            }
+            restoreChain(nm, orig);
             diag = 0;
             sp1 = sp2 = WB{-1, -1};
             return 0;
         }
         return 0;
     }
+    // SwapTailMove (move.cpp:3624-3826): chain[0 .. Mbar] runs from the
+    // pivot to the swap bead; after relinking chain[Mbar] is the old tail
     __device__ int swapTail(float4* orig) {
         if (numBeadsOn == 0 || diag) return -1;
         const int swapLength = m.mbar;
@@ -924,25 +1102,22 @@ struct WormWalker {
         WB b = pivot;
         for (int k = 0; k < swapLength; k++) {
             if (eqW(b, head) || isXW(b)) return -1;
+            if (lane == 0) chain[k] = pack(b);
             b = next(b);
         }
         const WB swp = b;
         if (isXW(swp) || eqW(head, swp)) return -1;
+        if (lane == 0) chain[swapLength] = pack(swp);
+        __syncwarp();
         acc->attempted[WM_ST]++;
         WB dummy; int3 dw;
         const double SigmaSwap = towerNorm(swp, pivotSlice, 1, -1.0f, dummy, dw);
         const float PNorm = (float)fmin(SigmaTail / SigmaSwap, 1.0);
         if (rand() < PNorm) {
+            const int nm = swapLength - 1;
             sp1 = swp; sp2 = pivot;
-            int k = 0;
-            b = pivot;
-            const WB stopB = next(swp);
-            for (int g = 0; g <= m.M; ++g) {
-                if (!eqW(b, swp) && !eqW(b, pivot) && k < kOrigCap) orig[k++] = P(b);
-                b = next(b);
-                if (eqW(b, stopB) || isXW(b)) break;
-            }
-            const double oldA = rangeAction(pivot, swp);
+            saveChain(nm, orig);
+            const double oldA = chainAction(0, swapLength + 1);
             const WB prevSwap = prev(swp);
             setPrev(tail, prevSwap);
             setPrev(swp, {-1, -1});
@@ -950,33 +1125,16 @@ struct WormWalker {
             sp1 = tail;
             tail = swp;
             const WB s1 = sp1;
-            const WB stop2 = next(s1);
-            k = 0;
-            b = pivot;
-            for (int g = 0; g <= m.M; ++g) {
-                if (!eqW(b, s1) && !eqW(b, pivot)) {
-                    float x, y, z;
-                    stagingPos(prev(b), s1, swapLength, k, wind, x, y, z);
-                    setP(b, (float)x, (float)y, (float)z);
-                    ++k;
-                    acc->bead_updates++;
-                }
-                b = next(b);
-                if (eqW(b, stop2) || isXW(b)) break;
-            }
-            const double newA = rangeAction(pivot, s1);
+            if (lane == 0) chain[swapLength] = pack(s1);
+            stageChain(nm, P(pivot), P(s1), swapLength, wind);
+            acc->bead_updates += nm;
+            const double newA = chainAction(0, swapLength + 1);
             if (metro(newA - oldA)) { acc->accepted[WM_ST]++; wormUpdate(head, swp); return 1; }
             tail = s1;
             setPrev(tail, {-1, -1});
             setPrev(swp, prevSwap);
             setNext(prevSwap, swp);
-            b = next(pivot);
-            k = 0;
-            for (int g = 0; g <= m.M && !eqW(b, swp) && !isXW(b) && k < kOrigCap; ++g) {
-                setP(b, orig[k].x, orig[k].y, orig[k].z);
-                ++k;
-                b = next(b);
-            }
+            restoreChain(nm, orig);
             sp1 = sp2 = WB{-1, -1};
             diag = 0;
             return 0;
@@ -987,31 +1145,34 @@ struct WormWalker {
     // EnergyEstimator (estimator.cpp:940-1029), primitive action, E/N of a
     // closed configuration: kinetic term over every bead's next link,
     // potential over the pairs of every slice, the rc = L tail
-    __device__ double energy(int& N) {
+    __device__ __noinline__ double energy(int& N) {
         N = numBeadsOn / m.M;
         KahanF pot, kin;
         for (int t = 0; t < m.M; ++t) {
             const int n = nb(t);
             const int tn = t + 1 == m.M ? 0 : t + 1;
-            for (int q = lane; q < n * n; q += 32) {
-                const int i = q / n, j = q - i * n;
-                const float4 ri = pos[(size_t)t * m.Ne + i];
-                if (j == 0) {
-                    const int pn = nxt[(size_t)t * m.Ne + i];
-                    if (pn >= 0 && pn < m.Ne) {
-                        const float4 rn = pos[(size_t)tn * m.Ne + pn];
-                        const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
-                        const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
-                        const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
-                        kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
-                    }
+            const float4* row = pos + (size_t)t * m.Ne;
+            // kinetic: every bead's link to the next slice, lane-parallel
+            for (int i = lane; i < n; i += 32) {
+                const int pn = nxt[(size_t)t * m.Ne + i];
+                if (pn >= 0 && pn < m.Ne) {
+                    const float4 ri = row[i], rn = pos[(size_t)tn * m.Ne + pn];
+                    const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
+                    const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
+                    const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
+                    kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
                 }
-                if (j <= i) continue;
-                const float4 rj = pos[(size_t)t * m.Ne + j];
-                const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
-                const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
-                const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
-                pot.add(aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+            }
+            // potential: row i against partners j > i spread over the lanes
+            for (int i = 0; i + 1 < n; ++i) {
+                const float4 ri = row[i];
+                for (int j = i + 1 + lane; j < n; j += 32) {
+                    const float4 rj = row[j];
+                    const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
+                    const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
+                    const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
+                    pot.add(aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+                }
             }
         }
         const double V = warp_sum_ff(pot), K2 = warp_sum_ff(kin);
@@ -1031,9 +1192,14 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
                AzizF az, int W, int sweeps, const int* __restrict__ order,
                const int* __restrict__ limit, unsigned long long budget_ns) {
     // walker i of this launch is order[i] (all walkers in index order when
-    // order is null); limit[w] caps its sweeps; with budget_ns > 0 a walker
-    // stops between sweeps once that much device time has passed
+    // order is null); limit[w] caps its completed sweeps; with budget_ns > 0
+    // a walker stops between two moves (checked every 8 moves) once that much
+    // device time has passed, and the next launch resumes the sweep there
     __shared__ float4 s_orig[kWWWarps][kOrigCap];
+    __shared__ int s_chain[kWWWarps][kChainCap];
+    __shared__ float s_norm[kWWWarps][3 * kOrigCap];
+    __shared__ double s_cum[kWWWarps][2][WM_N];
+
     const int warp = threadIdx.x >> 5;
     const int wi = blockIdx.x * kWWWarps + warp;
     if (wi >= W) return;
@@ -1048,6 +1214,8 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     ww.nbs = nbs + nbs_off[w];
     ww.scratch = scratch + scratch_off[w];
     ww.acc = &stats[w];
+    ww.chain = s_chain[warp];
+    ww.znorm = s_norm[warp];
     const WWState st = states[w];
     if (st.err) return;
     ww.head = WB{st.head[0], st.head[1]}; ww.tail = WB{st.tail[0], st.tail[1]};
@@ -1059,36 +1227,54 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     // per-walker counters accumulate in a register copy, lane 0 writes back
     pgb_worm_walker_stats local = stats[w];
     ww.acc = &local;
-    // cumulative probabilities over the default move list (pimc.cpp:120-152)
-    const double prob[WM_N] = {0.01, 0.19, 0.4, 0.15, 0.4, 0.15, 0.075, 0.075, 0.075, 0.075, 0.1, 0.1};
-    const int onDiag[WM_N] = {1, 1, 1, 0, 1, 0, 0, 0, 0, 0, 0, 0};
-    double cumD[WM_N], cumO[WM_N], cd = 0.0, co = 0.0;
-    for (int i = 0; i < WM_N; ++i) {
-        if (onDiag[i]) cd += prob[i];
-        cumD[i] = cd;
-        if (!onDiag[i] || i < 2) co += prob[i];
-        cumO[i] = co;
+    // cumulative probabilities over the default move list (pimc.cpp:120-152),
+    // one copy per warp in shared memory
+    double* cumD = s_cum[warp][0];
+    double* cumO = s_cum[warp][1];
+    if (ww.lane == 0) {
+        const double prob[WM_N] = {0.01, 0.19, 0.4, 0.15, 0.4, 0.15, 0.075, 0.075, 0.075, 0.075, 0.1, 0.1};
+        const int onDiag[WM_N] = {1, 1, 1, 0, 1, 0, 0, 0, 0, 0, 0, 0};
+        double cd = 0.0, co = 0.0;
+        for (int i = 0; i < WM_N; ++i) {
+            if (onDiag[i]) cd += prob[i];
+            cumD[i] = cd;
+            if (!onDiag[i] || i < 2) co += prob[i];
+            cumO[i] = co;
+        }
+        cumD[WM_N - 1] = 1.0 + 1e-7;
+        cumO[WM_N - 1] = 1.0 + 1e-7;
     }
-    cumD[WM_N - 1] = 1.0 + 1e-7;
-    cumO[WM_N - 1] = 1.0 + 1e-7;
+    __syncwarp();
     float4* orig = s_orig[warp];
     const int lim = limit ? min(sweeps, limit[w]) : sweeps;
     const unsigned long long t0 = __shfl_sync(0xffffffffu, gtimer_ns(), 0);
     // the walker's random stream is indexed by (sweep, draw): each sweep
-    // starts at counter sweep << 32, so where launches split a run does not
-    // change the draws
+    // starts at counter sweep << 32, and a sweep stopped part-way resumes at
+    // the saved move and draw, so where launches split a run does not change
+    // the draws
     unsigned long long sweep_no = st.ctr;
-    for (int sw = 0; sw < lim && !ww.err; ++sw) {
-        if (budget_ns) {
-            // lane 0's clock for every lane: the decision must be uniform
-            const unsigned long long now = __shfl_sync(0xffffffffu, gtimer_ns(), 0);
-            if (now - t0 > budget_ns) break;
+    int u0 = st.upd;
+    if (u0 > 0) {
+        ww.ctr = st.rctr;
+        ww.bidx = st.rbidx;
+        if (ww.bidx < 4) {
+            const unsigned long long c = ww.ctr - 1;
+            ww.buf = philox4x32(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0x574F524Du, 0u), ww.m.key);
         }
-        ww.ctr = sweep_no << 32;
-        ww.bidx = 4;
-        ++sweep_no;
-        local.sweeps += 1;
-        for (int u = 0; u < ww.m.num_updates && !ww.err; ++u) {
+    }
+    for (int sw = 0; sw < lim && !ww.err; ++sw) {
+        if (u0 == 0) {
+            ww.ctr = sweep_no << 32;
+            ww.bidx = 4;
+        }
+        int u = u0;
+        bool out_of_time = false;
+        for (; u < ww.m.num_updates && !ww.err; ++u) {
+            if (budget_ns && (u & 7) == 0) {
+                // lane 0's clock for every lane: the decision must be uniform
+                const unsigned long long now = __shfl_sync(0xffffffffu, gtimer_ns(), 0);
+                if (now - t0 > budget_ns) { out_of_time = true; break; }
+            }
             const double x = ww.rand();
             const double* cum = ww.diag ? cumD : cumO;
             int index = WM_N - 1;
@@ -1110,7 +1296,11 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
                 case WM_ST: ww.swapTail(orig); break;
             }
         }
-        if (!ww.err && ww.diag) {
+        if (out_of_time || ww.err) { u0 = u; break; }
+        u0 = 0;
+        ++sweep_no;
+        local.sweeps += 1;
+        if (ww.diag) {
             int N;
             const double e = ww.energy(N);
             local.samples += 1;
@@ -1128,6 +1318,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
         o.gap = ww.gap; o.length = ww.length; o.diag = ww.diag; o.numBeadsOn = ww.numBeadsOn;
         o.sep[0] = ww.sep[0]; o.sep[1] = ww.sep[1]; o.sep[2] = ww.sep[2];
         o.err = ww.err; o.ctr = sweep_no;
+        o.upd = u0; o.rctr = ww.ctr; o.rbidx = ww.bidx;
         states[w] = o;
         local.error = ww.err;
         stats[w] = local;
@@ -1153,6 +1344,7 @@ struct pgb_worm_walkers {
     WWState* d_state = nullptr;
     pgb_worm_walker_stats* d_stats = nullptr;
     double* d_scratch = nullptr;
+    int* d_order = nullptr;          // walkers by decreasing cost N^2 M: the largest start first
     AzizF az{};
     cudaStream_t stream = nullptr;
     std::string err;
@@ -1175,7 +1367,7 @@ int pgb_worm_walkers_destroy(pgb_worm_walkers* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->d_meta); cudaFree(h->d_pos); cudaFree(h->d_nxt); cudaFree(h->d_prv); cudaFree(h->d_nbs);
     cudaFree(h->d_nbs_off); cudaFree(h->d_scratch_off); cudaFree(h->d_state); cudaFree(h->d_stats);
-    cudaFree(h->d_scratch);
+    cudaFree(h->d_scratch); cudaFree(h->d_order);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return PGB_OK;
@@ -1203,9 +1395,10 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
     for (int w = 0; w < h->W; ++w) {
         const int N = p->num_ptcl[w], M = p->num_slices[w], mb = p->mbar[w], ne = p->capacity[w];
         const double L = p->side[w];
-        if (N < 1 || M < 4 || M % 2 || mb < 2 || mb % 2 || mb >= M || mb > 64 || ne < N || ne > 4096 || !(L > 0)) {
-            g_wwerr = "worm walker " + std::to_string(w) + ": need N >= 1, even M >= 4, even 2 <= Mbar < M, "
-                      "Mbar <= 64, N <= capacity <= 4096, L > 0";
+        if (N < 1 || M < 4 || M % 2 || M >= kChainCap || mb < 2 || mb % 2 || mb >= M || mb > 64 || ne < N ||
+            ne > 4096 || !(L > 0)) {
+            g_wwerr = "worm walker " + std::to_string(w) + ": need N >= 1, even 4 <= M < 1024, "
+                      "even 2 <= Mbar < M, Mbar <= 64, N <= capacity <= 4096, L > 0";
             pgb_worm_walkers_destroy(h);
             return PGB_EINVAL;
         }
@@ -1247,6 +1440,19 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
     if (e == cudaSuccess) e = cudaMalloc(&h->d_state, h->W * sizeof(WWState));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_stats, h->W * sizeof(pgb_worm_walker_stats));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_scratch, scoff * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_order, h->W * sizeof(int));
+    if (e == cudaSuccess) {
+        // the sweep lasts as long as the largest walker needs: start the
+        // largest first so that they spread over the SMs
+        std::vector<int> order(h->W);
+        for (int w = 0; w < h->W; ++w) order[w] = w;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            const double ca = 1.0 * h->meta[a].N0 * h->meta[a].N0 * h->meta[a].M;
+            const double cb = 1.0 * h->meta[b].N0 * h->meta[b].N0 * h->meta[b].M;
+            return ca > cb;
+        });
+        e = cudaMemcpy(h->d_order, order.data(), h->W * sizeof(int), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemcpy(h->d_meta, h->meta.data(), h->W * sizeof(WWMeta), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_nbs_off, h->nbs_off.data(), h->W * sizeof(long long), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_scratch_off, h->scratch_off.data(), h->W * sizeof(long long), cudaMemcpyHostToDevice);
@@ -1306,7 +1512,7 @@ int pgb_worm_walkers_run(pgb_worm_walkers* h, int sweeps) {
     const int blocks = (h->W + kWWWarps - 1) / kWWWarps;
     k_worm_walkers<<<blocks, kWWWarps * 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
                                                            h->d_nbs_off, h->d_state, h->d_stats, h->d_scratch,
-                                                           h->d_scratch_off, h->az, h->W, sweeps, nullptr,
+                                                           h->d_scratch_off, h->az, h->W, sweeps, h->d_order,
                                                            nullptr, 0ull);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -1542,6 +1748,7 @@ int pgb_worm_server_submit(pgb_worm_server* s, const pgb_job_spec* j, int* job_i
     job.Ne = 2 * j->n + 8;
     job.bytes = (size_t)M * job.Ne * 24 + (size_t)M * 4 + (size_t)kMaxWind * job.Ne * 8;
     if (job.Ne > 4096) return s->fail(PGB_EINVAL, "job: n too large for one walker");
+    if (job.M >= kChainCap) return s->fail(PGB_EINVAL, "job: temperature too low for one walker (M < 1024)");
     s->jobs.push_back(job);
     if (job_id) *job_id = (int)s->jobs.size() - 1;
     return PGB_OK;
@@ -1634,6 +1841,11 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
         s->h_limit[k] = (int)std::max<long long>(cap, 1);
         active.push_back(k);
     }
+    std::stable_sort(active.begin(), active.end(), [&](int a, int b) {
+        const WWMeta& ma = s->h_meta[a];
+        const WWMeta& mb = s->h_meta[b];
+        return 1.0 * ma.N0 * ma.N0 * ma.M > 1.0 * mb.N0 * mb.N0 * mb.M;
+    });
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_meta, s->h_meta.data(), s->max_slots * sizeof(WWMeta), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nbs_off, s->h_nbs_off.data(), s->max_slots * sizeof(long long), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_scratch_off, s->h_scratch_off.data(), s->max_slots * sizeof(long long), cudaMemcpyHostToDevice, s->stream);
@@ -1676,7 +1888,7 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
             job.esum0 = a.energy_sum;
         }
         if (finished) {
-            job.state = 3;
+            job.state = failed ? 4 : 3;
             job.t_done = t_end;
             s->bead_updates += a.bead_updates;
             s->beads.release(job.bead_off, (long long)job.M * job.Ne);
