@@ -773,7 +773,7 @@ def run_worm(args, pgb):
                       "errors": int((st["error"] != 0).sum()),
                       "closed_samples": int(st["samples"].sum()),
                       "acceptance": {WORM_MOVES[i]: [int(acc[i]), int(att[i])] for i in range(12)}},
-           "gpu_launches": args.steps, "clocks": clocks}
+           "gpu_launches": 1, "clocks": clocks}
     if not args.no_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle

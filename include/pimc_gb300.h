@@ -498,6 +498,14 @@ int pgb_worm_walkers_reset_stats(pgb_worm_walkers* w);
 /* one walker's arrays in the layouts of pgb_load_path ([M][capacity]) */
 int pgb_worm_walkers_get_path(pgb_worm_walkers* w, int walker, double* pos, int32_t* next,
                               int32_t* prev, uint8_t* on, int32_t worm8[8]);
+/* Self-check of the walkers' random streams: from the stream of `seed`
+ * advanced by `skip` words, `count` (<= 192) normal deviates drawn one at a
+ * time (serial[]) and made by the 32 lanes together (parallel[]), and the
+ * stream position after each (state[0..2] serial counter low, high, word
+ * index; state[3..5] the same after the parallel form).  The two agree bit
+ * for bit. */
+int pgb_worm_normals_check(uint64_t seed, int skip, int count, float* serial, float* parallel,
+                           int32_t state[6]);
 
 /* Grand-canonical job server: pgb_server_*'s interface and semantics (the
  * same parameter, job, bin and job-info records) with every job a device worm

@@ -116,6 +116,7 @@ class PgbJobInfo(C.Structure):
 
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int32)
+_FP = C.POINTER(C.c_float)
 _U8 = C.POINTER(C.c_uint8)
 _VP = C.c_void_p
 
@@ -169,6 +170,7 @@ _SIGS = {
     "pgb_worm_walkers_stats": (C.c_int, [_VP, C.POINTER(PgbWormWalkerStats)]),
     "pgb_worm_walkers_reset_stats": (C.c_int, [_VP]),
     "pgb_worm_walkers_get_path": (C.c_int, [_VP, C.c_int, _DP, _IP, _IP, C.POINTER(C.c_uint8), _IP]),
+    "pgb_worm_normals_check": (C.c_int, [C.c_uint64, C.c_int, C.c_int, _FP, _FP, _IP]),
     "pgb_plain_worm_run": (C.c_int, [_VP, C.POINTER(PgbWormParams), C.c_int, _IP, C.c_int,
                                      C.POINTER(C.c_int), _DP, _IP, C.POINTER(PgbWormStats)]),
     "pgb_set_beads": (C.c_int, [_VP, _IP, _DP, _IP, _IP, C.POINTER(C.c_uint8), C.c_int]),

@@ -122,7 +122,6 @@ struct WormWalker {
     int* nxt;
     int* prv;
     int* nbs;
-    double* scratch;                 // per-walker scratch, kMaxWind * Ne
     int* chain;                      // shared: the beads of the current move's range, packed
     float* znorm;                    // shared: a move's normal deviates, 3 (Mbar - 1) at most
     int lane;
@@ -1188,7 +1187,6 @@ __global__ void __launch_bounds__(kWWWarps * 32)
 k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* __restrict__ nxt,
                int* __restrict__ prv, int* __restrict__ nbs, const long long* __restrict__ nbs_off,
                WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
-               double* __restrict__ scratch, const long long* __restrict__ scratch_off,
                AzizF az, int W, int sweeps, const int* __restrict__ order,
                const int* __restrict__ limit, unsigned long long budget_ns) {
     // walker i of this launch is order[i] (all walkers in index order when
@@ -1212,7 +1210,6 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     ww.nxt = nxt + ww.m.off;
     ww.prv = prv + ww.m.off;
     ww.nbs = nbs + nbs_off[w];
-    ww.scratch = scratch + scratch_off[w];
     ww.acc = &stats[w];
     ww.chain = s_chain[warp];
     ww.znorm = s_norm[warp];
@@ -1325,6 +1322,29 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     }
 }
 
+// one warp: the serial and the lane-parallel normal deviates from the same
+// stream position
+__global__ void k_normals_check(uint2 key, int skip, int count, float* serial, float* parallel, int* state) {
+    __shared__ float s_out[3 * kOrigCap];
+    WormWalker a;
+    a.m = WWMeta{};
+    a.m.key = key;
+    a.lane = threadIdx.x & 31;
+    a.ctr = 0; a.bidx = 4;
+    for (int i = 0; i < skip; ++i) a.u32();
+    WormWalker b = a;
+    for (int i = 0; i < count; ++i) {
+        const float z = a.randNormZ();
+        if (a.lane == 0) serial[i] = z;
+    }
+    b.normals(count, s_out);
+    for (int i = a.lane; i < count; i += 32) parallel[i] = s_out[i];
+    if (a.lane == 0) {
+        state[0] = (int)(uint32_t)a.ctr; state[1] = (int)(uint32_t)(a.ctr >> 32); state[2] = a.bidx;
+        state[3] = (int)(uint32_t)b.ctr; state[4] = (int)(uint32_t)(b.ctr >> 32); state[5] = b.bidx;
+    }
+}
+
 }  // namespace pgb
 
 // --------------------------------------------------------------------------
@@ -1335,15 +1355,14 @@ using namespace pgb;
 struct pgb_worm_walkers {
     int W = 0;
     std::vector<WWMeta> meta;
-    std::vector<long long> nbs_off, scratch_off;
-    long long total_beads = 0, total_slices = 0, total_scratch = 0;
+    std::vector<long long> nbs_off;
+    long long total_beads = 0, total_slices = 0;
     WWMeta* d_meta = nullptr;
     float4* d_pos = nullptr;
     int *d_nxt = nullptr, *d_prv = nullptr, *d_nbs = nullptr;
-    long long *d_nbs_off = nullptr, *d_scratch_off = nullptr;
+    long long* d_nbs_off = nullptr;
     WWState* d_state = nullptr;
     pgb_worm_walker_stats* d_stats = nullptr;
-    double* d_scratch = nullptr;
     int* d_order = nullptr;          // walkers by decreasing cost N^2 M: the largest start first
     AzizF az{};
     cudaStream_t stream = nullptr;
@@ -1366,8 +1385,7 @@ int pgb_worm_walkers_destroy(pgb_worm_walkers* h) {
     if (!h) return PGB_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->d_meta); cudaFree(h->d_pos); cudaFree(h->d_nxt); cudaFree(h->d_prv); cudaFree(h->d_nbs);
-    cudaFree(h->d_nbs_off); cudaFree(h->d_scratch_off); cudaFree(h->d_state); cudaFree(h->d_stats);
-    cudaFree(h->d_scratch); cudaFree(h->d_order);
+    cudaFree(h->d_nbs_off); cudaFree(h->d_state); cudaFree(h->d_stats); cudaFree(h->d_order);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return PGB_OK;
@@ -1391,7 +1409,7 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
     h->W = p->num_walkers;
     const AzizParams ap = aziz_params(p->aziz_year ? p->aziz_year : 1979);
     h->az = make_aziz_f(ap);
-    long long off = 0, soff = 0, scoff = 0;
+    long long off = 0, soff = 0;
     for (int w = 0; w < h->W; ++w) {
         const int N = p->num_ptcl[w], M = p->num_slices[w], mb = p->mbar[w], ne = p->capacity[w];
         const double L = p->side[w];
@@ -1423,12 +1441,10 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
         m.key = make_uint2((uint32_t)s, (uint32_t)(s >> 32));
         h->meta.push_back(m);
         h->nbs_off.push_back(soff);
-        h->scratch_off.push_back(scoff);
         off += (long long)M * ne;
         soff += M;
-        scoff += (long long)kMaxWind * ne;
     }
-    h->total_beads = off; h->total_slices = soff; h->total_scratch = scoff;
+    h->total_beads = off; h->total_slices = soff;
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_meta, h->W * sizeof(WWMeta));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_pos, off * sizeof(float4));
@@ -1436,10 +1452,8 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
     if (e == cudaSuccess) e = cudaMalloc(&h->d_prv, off * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_nbs, soff * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_nbs_off, h->W * sizeof(long long));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_scratch_off, h->W * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_state, h->W * sizeof(WWState));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_stats, h->W * sizeof(pgb_worm_walker_stats));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_scratch, scoff * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_order, h->W * sizeof(int));
     if (e == cudaSuccess) {
         // the sweep lasts as long as the largest walker needs: start the
@@ -1455,7 +1469,6 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
     }
     if (e == cudaSuccess) e = cudaMemcpy(h->d_meta, h->meta.data(), h->W * sizeof(WWMeta), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_nbs_off, h->nbs_off.data(), h->W * sizeof(long long), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(h->d_scratch_off, h->scratch_off.data(), h->W * sizeof(long long), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(h->d_stats, 0, h->W * sizeof(pgb_worm_walker_stats));
     if (e == cudaSuccess) e = cudaMemset(h->d_nbs, 0, soff * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(h->d_nxt, 0xff, off * sizeof(int));
@@ -1511,8 +1524,8 @@ int pgb_worm_walkers_run(pgb_worm_walkers* h, int sweeps) {
     if (sweeps == 0) return PGB_OK;
     const int blocks = (h->W + kWWWarps - 1) / kWWWarps;
     k_worm_walkers<<<blocks, kWWWarps * 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
-                                                           h->d_nbs_off, h->d_state, h->d_stats, h->d_scratch,
-                                                           h->d_scratch_off, h->az, h->W, sweeps, h->d_order,
+                                                           h->d_nbs_off, h->d_state, h->d_stats,
+                                                           h->az, h->W, sweeps, h->d_order,
                                                            nullptr, 0ull);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -1612,7 +1625,7 @@ struct WServerJob {
     int M = 0, N0 = 0, Ne = 0, mbar = 0;
     double L = 0;
     int slot = -1;
-    long long bead_off = -1, slice_off = -1, scratch_off = -1;
+    long long bead_off = -1, slice_off = -1;
     size_t bytes = 0;
 };
 
@@ -1629,18 +1642,17 @@ struct pgb_worm_server {
     std::vector<WServerJob> jobs;
     std::deque<int> queue;
     std::vector<pgb_bin> bins;
-    WPool beads, slices, scratch;
-    long long n_beads = 0, n_slices = 0, n_scratch = 0;
+    WPool beads, slices;
+    long long n_beads = 0, n_slices = 0;
     float4* d_pos = nullptr;
     int *d_nxt = nullptr, *d_prv = nullptr, *d_nbs = nullptr;
-    double* d_scratch = nullptr;
     WWMeta* d_meta = nullptr;
     WWState* d_state = nullptr;
     pgb_worm_walker_stats* d_stats = nullptr;
-    long long *d_nbs_off = nullptr, *d_scratch_off = nullptr;
+    long long* d_nbs_off = nullptr;
     int *d_order = nullptr, *d_limit = nullptr;
     std::vector<WWMeta> h_meta;
-    std::vector<long long> h_nbs_off, h_scratch_off;
+    std::vector<long long> h_nbs_off;
     std::vector<int> h_limit;
     cudaStream_t stream = nullptr;
     std::chrono::steady_clock::time_point t0;
@@ -1661,9 +1673,9 @@ const char* pgb_worm_server_last_error(const pgb_worm_server* s) { return s ? s-
 int pgb_worm_server_destroy(pgb_worm_server* s) {
     if (!s) return PGB_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    cudaFree(s->d_pos); cudaFree(s->d_nxt); cudaFree(s->d_prv); cudaFree(s->d_nbs); cudaFree(s->d_scratch);
+    cudaFree(s->d_pos); cudaFree(s->d_nxt); cudaFree(s->d_prv); cudaFree(s->d_nbs);
     cudaFree(s->d_meta); cudaFree(s->d_state); cudaFree(s->d_stats); cudaFree(s->d_nbs_off);
-    cudaFree(s->d_scratch_off); cudaFree(s->d_order); cudaFree(s->d_limit);
+    cudaFree(s->d_order); cudaFree(s->d_limit);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PGB_OK;
@@ -1686,17 +1698,14 @@ int pgb_worm_server_create(const pgb_server_params* p, pgb_worm_server** out) {
     s->ap = aziz_params(p->aziz_year ? p->aziz_year : 1979);
     s->az = make_aziz_f(s->ap);
     s->max_slots = p->max_active;
-    // the budget: 85 % for bead arrays (24 B a bead), 15 % for the swap-move
-    // tower scratch, slice counters sized from the bead pool
-    s->n_beads = (long long)(0.85 * p->hbm_budget_bytes / 24.0);
-    s->n_scratch = (long long)(0.15 * p->hbm_budget_bytes / 8.0);
+    // the budget: bead arrays (24 B a bead), slice counters sized from them
+    s->n_beads = (long long)(p->hbm_budget_bytes / 24.0);
     s->n_slices = s->n_beads / 8 + 1;
-    s->beads.init(s->n_beads); s->slices.init(s->n_slices); s->scratch.init(s->n_scratch);
+    s->beads.init(s->n_beads); s->slices.init(s->n_slices);
     s->slot_job.assign(s->max_slots, -1);
     for (int k = s->max_slots - 1; k >= 0; --k) s->free_slots.push_back(k);
     s->h_meta.assign(s->max_slots, WWMeta{});
     s->h_nbs_off.assign(s->max_slots, 0);
-    s->h_scratch_off.assign(s->max_slots, 0);
     s->h_limit.assign(s->max_slots, 0);
     s->t0 = std::chrono::steady_clock::now();
     cudaError_t e;
@@ -1706,12 +1715,10 @@ int pgb_worm_server_create(const pgb_server_params* p, pgb_worm_server** out) {
         if ((e = cudaMalloc(&s->d_nxt, s->n_beads * sizeof(int))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_prv, s->n_beads * sizeof(int))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_nbs, s->n_slices * sizeof(int))) != cudaSuccess) break;
-        if ((e = cudaMalloc(&s->d_scratch, s->n_scratch * sizeof(double))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_meta, s->max_slots * sizeof(WWMeta))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_state, s->max_slots * sizeof(WWState))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_stats, s->max_slots * sizeof(pgb_worm_walker_stats))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_nbs_off, s->max_slots * sizeof(long long))) != cudaSuccess) break;
-        if ((e = cudaMalloc(&s->d_scratch_off, s->max_slots * sizeof(long long))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_order, s->max_slots * sizeof(int))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_limit, s->max_slots * sizeof(int))) != cudaSuccess) break;
     } while (0);
@@ -1746,7 +1753,7 @@ int pgb_worm_server_submit(pgb_worm_server* s, const pgb_job_spec* j, int* job_i
     if (mb < 2) mb = 2;
     job.mbar = mb;
     job.Ne = 2 * j->n + 8;
-    job.bytes = (size_t)M * job.Ne * 24 + (size_t)M * 4 + (size_t)kMaxWind * job.Ne * 8;
+    job.bytes = (size_t)M * job.Ne * 24 + (size_t)M * 4;
     if (job.Ne > 4096) return s->fail(PGB_EINVAL, "job: n too large for one walker");
     if (job.M >= kChainCap) return s->fail(PGB_EINVAL, "job: temperature too low for one walker (M < 1024)");
     s->jobs.push_back(job);
@@ -1760,17 +1767,15 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
     for (size_t k = 0; k < s->jobs.size(); ++k)
         if (s->jobs[k].state == 0 && s->jobs[k].spec.arrival <= now) { s->jobs[k].state = 1; s->queue.push_back((int)k); }
     cudaError_t e = cudaSuccess;
-    // admission: FIFO while a slot and all three pools have room
+    // admission: FIFO while a slot and both pools have room
     while (!s->queue.empty() && !s->free_slots.empty()) {
         WServerJob& job = s->jobs[s->queue.front()];
-        const long long nb = (long long)job.M * job.Ne, ns = job.M, nsc = (long long)kMaxWind * job.Ne;
+        const long long nb = (long long)job.M * job.Ne, ns = job.M;
         const long long bo = s->beads.alloc(nb);
         if (bo < 0) break;
         const long long so = s->slices.alloc(ns);
         if (so < 0) { s->beads.release(bo, nb); break; }
-        const long long co = s->scratch.alloc(nsc);
-        if (co < 0) { s->beads.release(bo, nb); s->slices.release(so, ns); break; }
-        job.bead_off = bo; job.slice_off = so; job.scratch_off = co;
+        job.bead_off = bo; job.slice_off = so;
         job.slot = s->free_slots.back();
         s->free_slots.pop_back();
         job.state = 2;
@@ -1799,7 +1804,6 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
         m.key = make_uint2((uint32_t)sd, (uint32_t)(sd >> 32));
         s->h_meta[k] = m;
         s->h_nbs_off[k] = so;
-        s->h_scratch_off[k] = co;
         // seeded closed worldlines: uniform centres, Gaussian jitter per bead
         std::mt19937_64 rng(job.spec.seed);
         std::uniform_real_distribution<double> u(-0.5, 0.5);
@@ -1848,7 +1852,6 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
     });
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_meta, s->h_meta.data(), s->max_slots * sizeof(WWMeta), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nbs_off, s->h_nbs_off.data(), s->max_slots * sizeof(long long), cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_scratch_off, s->h_scratch_off.data(), s->max_slots * sizeof(long long), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_limit, s->h_limit.data(), s->max_slots * sizeof(int), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess && !active.empty()) e = cudaMemcpyAsync(s->d_order, active.data(), active.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
     if (e != cudaSuccess) return s->cfail(e, "worm server upload");
@@ -1857,7 +1860,7 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
         const bool timed = s->p.round_seconds > 0.0;
         k_worm_walkers<<<(W + kWWWarps - 1) / kWWWarps, kWWWarps * 32, 0, s->stream>>>(
             s->d_meta, s->d_pos, s->d_nxt, s->d_prv, s->d_nbs, s->d_nbs_off, s->d_state, s->d_stats,
-            s->d_scratch, s->d_scratch_off, s->az, W, timed ? (1 << 30) : s->p.sweeps_per_round,
+            s->az, W, timed ? (1 << 30) : s->p.sweeps_per_round,
             s->d_order, s->d_limit, timed ? (unsigned long long)(s->p.round_seconds * 1e9) : 0ull);
         if ((e = cudaGetLastError()) != cudaSuccess) return s->cfail(e, "worm server launch");
     }
@@ -1893,7 +1896,6 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
             s->bead_updates += a.bead_updates;
             s->beads.release(job.bead_off, (long long)job.M * job.Ne);
             s->slices.release(job.slice_off, job.M);
-            s->scratch.release(job.scratch_off, (long long)kMaxWind * job.Ne);
             s->slot_job[k] = -1;
             s->free_slots.push_back(k);
             job.slot = -1;
@@ -1945,3 +1947,25 @@ int pgb_worm_server_active_bead_updates(pgb_worm_server* s, long long* total) {
 }
 
 }  // extern "C"
+
+extern "C" int pgb_worm_normals_check(uint64_t seed, int skip, int count, float* serial, float* parallel,
+                                      int32_t state[6]) {
+    using namespace pgb;
+    if (!serial || !parallel || !state || count < 1 || count > 3 * kOrigCap || skip < 0 || skip > 1000000)
+        return PGB_EINVAL;
+    const uint64_t sd = seed * 0x9E3779B97F4A7C15ull + 0x94D049BB133111EBull;
+    float *d_s = nullptr, *d_p = nullptr;
+    int* d_st = nullptr;
+    cudaError_t e = cudaMalloc(&d_s, count * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_p, count * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_st, 6 * sizeof(int));
+    if (e == cudaSuccess) {
+        k_normals_check<<<1, 32>>>(make_uint2((uint32_t)sd, (uint32_t)(sd >> 32)), skip, count, d_s, d_p, d_st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(serial, d_s, count * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(parallel, d_p, count * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(state, d_st, 6 * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_s); cudaFree(d_p); cudaFree(d_st);
+    return e == cudaSuccess ? PGB_OK : PGB_ECUDA;
+}

@@ -86,3 +86,23 @@ def test_worm_walkers_match_oracle_statistically(pgb, oracle_lib):
     n_w, sn_w = nw.mean(), nw.std(ddof=1) / np.sqrt(len(nw))
     assert abs(e_w - eo) <= 4.0 * np.hypot(se_w, se_o), (e_w, se_w, eo, se_o)
     assert abs(n_w - no) <= 4.0 * np.hypot(sn_w, sn_o) + 1e-9, (n_w, sn_w, no, sn_o)
+
+
+@pytest.mark.parametrize("skip", [0, 1, 3, 6])
+def test_parallel_normals_equal_serial_draws(pgb, skip):
+    """A staging move's deviates made by the lanes together are the serial
+    draws bit for bit, and leave the stream at the same position."""
+    import ctypes as C
+    from pimc_gb300 import _lib
+    lib = _lib.load()
+    for count in (1, 7, 45, 189):
+        a = np.zeros(count, dtype=np.float32)
+        b = np.zeros(count, dtype=np.float32)
+        st = np.zeros(6, dtype=np.int32)
+        rc = lib.pgb_worm_normals_check(12345 + skip, skip, count,
+                                        a.ctypes.data_as(_lib._FP), b.ctypes.data_as(_lib._FP),
+                                        st.ctypes.data_as(_lib._IP))
+        assert rc == 0
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (count, a[:4], b[:4])
+        assert np.array_equal(st[:3], st[3:]), st
+        assert np.all(np.isfinite(a)) and abs(a.std() - 1.0) < 0.6 if count > 40 else True
