@@ -285,71 +285,103 @@ struct WormWalker {
     __device__ static WB unpack(int c) { return {c >> 12, c & 4095}; }
     __device__ size_t at(int c) const { return (size_t)(c >> 12) * m.Ne + (c & 4095); }
 
+    // The fields a pair sum reads, copied once per call into registers: the
+    // walker itself lives in local memory around the helpers that are not
+    // inlined, and reading it there per pair would cost a load each time.
+    struct PairCtx {
+        const float4* pos;
+        const int* nbs;
+        int Ne, M;
+        float L, Linv;
+        AzizF az;
+        WB head, tail, sp1, sp2;
+        int lane;
+        __device__ int state(WB b) const {
+            if (eqW(b, head) || eqW(b, tail)) return 2;
+            if (eqW(b, sp1) || eqW(b, sp2)) return 1;
+            return 0;
+        }
+    };
+    __device__ PairCtx pairCtx() const {
+        PairCtx c;
+        c.pos = pos; c.nbs = nbs; c.Ne = m.Ne; c.M = m.M; c.L = m.L; c.Linv = m.Linv; c.az = az;
+        c.head = head; c.tail = tail; c.sp1 = sp1; c.sp2 = sp2; c.lane = lane;
+        return c;
+    }
     // one bead's loads, all independent of one another: its slice's bead
     // count, its own position and the first 128 same-slice positions
-    // (issued for every index below Ne, used below the count)
+    // (issued for every index below Ne, used below the count); false for a
+    // locator outside the walker's arrays, which then loads bead (0, 0)
+    // with no partners
     struct BeadLoad { WB b; int n; float4 rb; float4 r[4]; };
-    __device__ void loadBead(int c, BeadLoad& L) {
-        L.b = unpack(c);
-        const bool ok = valid(L.b);
-        if (!ok) { err = WERR_LINK; L.b = WB{0, 0}; }
-        const float4* row = pos + (size_t)L.b.t * m.Ne;
-        L.n = ok ? nbs[L.b.t] : 0;
+    __device__ static bool loadBead(const PairCtx& c, int code, BeadLoad& L) {
+        L.b = unpack(code);
+        const bool ok = L.b.t < c.M && L.b.p < c.Ne;
+        if (!ok) L.b = WB{0, 0};
+        const float4* row = c.pos + (size_t)L.b.t * c.Ne;
+        L.n = ok ? c.nbs[L.b.t] : 0;
         L.rb = row[L.b.p];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int j = 32 * u + lane;
-            L.r[u] = j < m.Ne ? row[j] : L.rb;
+            const int j = 32 * u + c.lane;
+            L.r[u] = j < c.Ne ? row[j] : L.rb;
         }
+        return ok;
     }
     // one pair term, without branches: a partner that is absent (j at or
     // beyond the count, or the bead itself) adds zero
-    __device__ void pairTerm(WB b, int s1, int j, int n, float4 rb, float4 rj, KahanF& k) {
+    __device__ static void pairTerm(const PairCtx& c, WB b, int s1, int j, int n, float4 rb, float4 rj,
+                                    KahanF& k) {
         const bool ok = j < n && j != b.p;
-        const float f = ok ? factor(s1, state(WB{b.t, j})) : 0.0f;
-        const float dx = min_image32(rj.x - rb.x, m.L, m.Linv);
-        const float dy = min_image32(rj.y - rb.y, m.L, m.Linv);
-        const float dz = min_image32(rj.z - rb.z, m.L, m.Linv);
+        const float f = ok ? factor(s1, c.state(WB{b.t, j})) : 0.0f;
+        const float dx = min_image32(rj.x - rb.x, c.L, c.Linv);
+        const float dy = min_image32(rj.y - rb.y, c.L, c.Linv);
+        const float dz = min_image32(rj.z - rb.z, c.L, c.Linv);
         const float r2 = ok ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : 1.0f;
-        k.add(f * aziz_v32_sel(r2, az));
+        k.add(f * aziz_v32_sel(r2, c.az));
     }
     // tau-less pair terms of a loaded bead with its active same-slice
     // partners, added to the lane's running sum in ascending partner order
-    __device__ void pairsLoaded(const BeadLoad& L, KahanF& k) {
-        const int s1 = state(L.b);
+    __device__ static void pairsLoaded(const PairCtx& c, const BeadLoad& L, KahanF& k) {
+        const int s1 = c.state(L.b);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) pairTerm(L.b, s1, 32 * u + lane, L.n, L.rb, L.r[u], k);
-        const float4* row = pos + (size_t)L.b.t * m.Ne;
+        for (int u = 0; u < 4; ++u) pairTerm(c, L.b, s1, 32 * u + c.lane, L.n, L.rb, L.r[u], k);
+        const float4* row = c.pos + (size_t)L.b.t * c.Ne;
         for (int j0 = 128; j0 < L.n; j0 += 128) {
             float4 r[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const int j = j0 + 32 * u + lane;
+                const int j = j0 + 32 * u + c.lane;
                 r[u] = j < L.n ? row[j] : L.rb;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) pairTerm(L.b, s1, j0 + 32 * u + lane, L.n, L.rb, r[u], k);
+            for (int u = 0; u < 4; ++u) pairTerm(c, L.b, s1, j0 + 32 * u + c.lane, L.n, L.rb, r[u], k);
         }
     }
     // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
     // tau * sum over the other active beads of the slice of factor * V
     __device__ __noinline__ double bare(WB b) {
         if (!valid(b)) { err = WERR_LINK; return 0.0; }
+        const PairCtx c = pairCtx();
         BeadLoad L;
-        loadBead(pack(b), L);
+        loadBead(c, pack(b), L);
         KahanF k;
-        pairsLoaded(L, k);
+        pairsLoaded(c, L, k);
         return m.tau * warp_sum_ff(k);
     }
     // potentialAction over chain[c0 .. c0 + cnt - 1]: the lanes keep one
     // running sum over the whole range and reduce once
     __device__ __noinline__ double chainAction(int c0, int cnt) {
+        const PairCtx c = pairCtx();
+        const int* ch = chain;
         KahanF k;
-        for (int c = 0; c < cnt; ++c) {
-            BeadLoad cur;
-            loadBead(chain[c0 + c], cur);
-            if (cur.b.p < cur.n) pairsLoaded(cur, k);
+        bool ok = true;
+        for (int i = 0; i < cnt; ++i) {
+            BeadLoad L;
+            ok &= loadBead(c, ch[c0 + i], L);
+            if (L.b.p < L.n) pairsLoaded(c, L, k);
         }
+        if (!ok) err = WERR_LINK;
         return m.tau * warp_sum_ff(k);
     }
     // the beads from s to e along next links into chain[0 ..]: returns their
@@ -974,9 +1006,9 @@ struct WormWalker {
     // order (bead fastest, sector slowest) whose cumulative weight reaches
     // x * Sigma: the sector by a scan over the lanes' sector sums, the bead
     // by a scan inside that sector.
-    __device__ float rho0Shifted(float4 pf, float4 pb, int3 wv, int sign, float g3, float den) const {
-        const float ax = (pf.x - pb.x) + (sign * wv.x) * m.L, ay = (pf.y - pb.y) + (sign * wv.y) * m.L,
-                    az_ = (pf.z - pb.z) + (sign * wv.z) * m.L;
+    __device__ static float rho0Shifted(float4 pf, float4 pb, int3 wv, int sign, float g3, float den, float L) {
+        const float ax = (pf.x - pb.x) + (sign * wv.x) * L, ay = (pf.y - pb.y) + (sign * wv.y) * L,
+                    az_ = (pf.z - pb.z) + (sign * wv.z) * L;
         return g3 * expf(-(ax * ax + ay * ay + az_ * az_) / den);
     }
     __device__ __noinline__ double towerNorm(WB b, int pivotSlice, int sign, float x, WB& pivot, int3& wind) {
@@ -986,12 +1018,14 @@ struct WormWalker {
         const float den = (float)(4.0 * m.lambda * m.mbar * m.tau);
         const float g = rsqrtf(3.14159265358979f * den);
         const float g3 = g * g * g;
-        float mine = 0.0f;                       // lane w: sector w's weight
+        const float L = m.L;
+        const int ln = lane;
+        float mine = 0.0f;                       // ln w: sector w's weight
         for (int n0 = 0; n0 < nL; n0 += 128) {
             float4 pf[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const int n = n0 + 32 * u + lane;
+                const int n = n0 + 32 * u + ln;
                 pf[u] = n < nL ? row[n] : pb;
             }
             for (int w = 0; w < kMaxWind; ++w) {
@@ -999,34 +1033,34 @@ struct WormWalker {
                 float v = 0.0f;
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const float r = rho0Shifted(pf[u], pb, wv, sign, g3, den);
-                    v += n0 + 32 * u + lane < nL ? r : 0.0f;
+                    const float r = rho0Shifted(pf[u], pb, wv, sign, g3, den, L);
+                    v += n0 + 32 * u + ln < nL ? r : 0.0f;
                 }
                 for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                if (lane == w) mine += v;
+                if (ln == w) mine += v;
             }
         }
         // inclusive scan of the sector sums over lanes 0..26
-        float cum = lane < kMaxWind ? mine : 0.0f;
+        float cum = ln < kMaxWind ? mine : 0.0f;
         for (int o = 1; o < 32; o <<= 1) {
             const float u = __shfl_up_sync(0xffffffffu, cum, o);
-            if (lane >= o) cum += u;
+            if (ln >= o) cum += u;
         }
         const float sum = __shfl_sync(0xffffffffu, cum, kMaxWind - 1);
         if (x >= 0.0f) {
             const float target = x * sum;
-            const unsigned hs = __ballot_sync(0xffffffffu, lane < kMaxWind && cum >= target);
+            const unsigned hs = __ballot_sync(0xffffffffu, ln < kMaxWind && cum >= target);
             const int ws = hs ? __ffs(hs) - 1 : kMaxWind - 1;
             const float before = __shfl_sync(0xffffffffu, cum - mine, ws);
             const int3 wv = winding(ws);
             float carry = before;
             int found = nL - 1;
             for (int base = 0; base < nL; base += 32) {
-                const int n = base + lane;
-                float v = n < nL ? rho0Shifted(row[n], pb, wv, sign, g3, den) : 0.0f;
+                const int n = base + ln;
+                float v = n < nL ? rho0Shifted(row[n], pb, wv, sign, g3, den, L) : 0.0f;
                 for (int o = 1; o < 32; o <<= 1) {
                     const float u = __shfl_up_sync(0xffffffffu, v, o);
-                    if (lane >= o) v += u;
+                    if (ln >= o) v += u;
                 }
                 const unsigned h = __ballot_sync(0xffffffffu, n < nL && carry + v >= target);
                 if (h) { found = base + __ffs(h) - 1; break; }
