@@ -492,12 +492,8 @@ struct WormWalker {
     }
 
     // ---- sampling helpers (move.cpp:183-488) ----
-    // ActionBase::rho0 (action.cpp:254-260) in FP32
-    __device__ float rho0(float d2, int L) const {
-        const float den = (float)(4.0 * m.lambda * L * m.tau);
-        const float g = rsqrtf(3.14159265358979f * den);
-        return g * g * g * expf(-d2 / den);
-    }
+    // ActionBase::rho0 (action.cpp:254-260) is evaluated in FP32 inline where
+    // used: (4 pi lambda L tau)^(-3/2) exp(-d^2 / (4 lambda L tau))
     __device__ static int3 winding(int n) {
         // MoveBase ctor (move.cpp:88-108) with maxWind = 1
         int3 w;
@@ -508,20 +504,30 @@ struct WormWalker {
     }
     // sampleWindingSector (move.cpp:362-397)
     __device__ __noinline__ int3 sampleWinding(WB sb, WB eb, int L, double& totald) {
+        // lane n < 27 weighs winding sector n; a scan over the lanes gives the
+        // cumulative weights in sector order
         const float4 pe = P(eb), ps = P(sb);
+        const float Lb = m.L;
+        const float den = (float)(4.0 * m.lambda * L * m.tau);
+        const float g = rsqrtf(3.14159265358979f * den);
+        const float g3 = g * g * g;
+        const int ln = lane;
         const float vx = pe.x - ps.x, vy = pe.y - ps.y, vz = pe.z - ps.z;
-        float cum[kMaxWind];
-        float total = 0.0f;
-        for (int n = 0; n < kMaxWind; ++n) {
-            const int3 w = winding(n);
-            const float ax = vx + w.x * m.L, ay = vy + w.y * m.L, az_ = vz + w.z * m.L;
-            total += rho0(ax * ax + ay * ay + az_ * az_, L);
-            cum[n] = total;
+        float v = 0.0f;
+        if (ln < kMaxWind) {
+            const int3 w = winding(ln);
+            const float ax = vx + w.x * Lb, ay = vy + w.y * Lb, az_ = vz + w.z * Lb;
+            v = g3 * expf(-(ax * ax + ay * ay + az_ * az_) / den);
         }
+        for (int o = 1; o < 32; o <<= 1) {
+            const float u = __shfl_up_sync(0xffffffffu, v, o);
+            if (ln >= o) v += u;
+        }
+        const float total = __shfl_sync(0xffffffffu, v, kMaxWind - 1);
         totald = total;
         const float x = rand();
-        int idx = kMaxWind - 1;
-        for (int n = 0; n < kMaxWind; ++n) if (cum[n] / total >= x) { idx = n; break; }
+        const unsigned h = __ballot_sync(0xffffffffu, ln < kMaxWind && v / total >= x);
+        const int idx = h ? __ffs(h) - 1 : kMaxWind - 1;
         return winding(idx);
     }
     // newStagingPosition with winding (move.cpp:301-338): np is the previous
@@ -1180,31 +1186,38 @@ struct WormWalker {
     // potential over the pairs of every slice, the rc = L tail
     __device__ __noinline__ double energy(int& N) {
         N = numBeadsOn / m.M;
+        // register copies of the walker's fields (see PairCtx)
+        const float4* P_ = pos;
+        const int* nx_ = nxt;
+        const int* nb_ = nbs;
+        const int M = m.M, Ne = m.Ne, ln = lane;
+        const float L = m.L, Linv = m.Linv;
+        const AzizF a = az;
         KahanF pot, kin;
-        for (int t = 0; t < m.M; ++t) {
-            const int n = nb(t);
-            const int tn = t + 1 == m.M ? 0 : t + 1;
-            const float4* row = pos + (size_t)t * m.Ne;
+        for (int t = 0; t < M; ++t) {
+            const int n = nb_[t];
+            const int tn = t + 1 == M ? 0 : t + 1;
+            const float4* row = P_ + (size_t)t * Ne;
             // kinetic: every bead's link to the next slice, lane-parallel
-            for (int i = lane; i < n; i += 32) {
-                const int pn = nxt[(size_t)t * m.Ne + i];
-                if (pn >= 0 && pn < m.Ne) {
-                    const float4 ri = row[i], rn = pos[(size_t)tn * m.Ne + pn];
-                    const float vx = min_image32(rn.x - ri.x, m.L, m.Linv);
-                    const float vy = min_image32(rn.y - ri.y, m.L, m.Linv);
-                    const float vz = min_image32(rn.z - ri.z, m.L, m.Linv);
+            for (int i = ln; i < n; i += 32) {
+                const int pn = nx_[(size_t)t * Ne + i];
+                if (pn >= 0 && pn < Ne) {
+                    const float4 ri = row[i], rn = P_[(size_t)tn * Ne + pn];
+                    const float vx = min_image32(rn.x - ri.x, L, Linv);
+                    const float vy = min_image32(rn.y - ri.y, L, Linv);
+                    const float vz = min_image32(rn.z - ri.z, L, Linv);
                     kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
                 }
             }
             // potential: row i against partners j > i spread over the lanes
             for (int i = 0; i + 1 < n; ++i) {
                 const float4 ri = row[i];
-                for (int j = i + 1 + lane; j < n; j += 32) {
+                for (int j = i + 1 + ln; j < n; j += 32) {
                     const float4 rj = row[j];
-                    const float dx = min_image32(ri.x - rj.x, m.L, m.Linv);
-                    const float dy = min_image32(ri.y - rj.y, m.L, m.Linv);
-                    const float dz = min_image32(ri.z - rj.z, m.L, m.Linv);
-                    pot.add(aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), az));
+                    const float dx = min_image32(ri.x - rj.x, L, Linv);
+                    const float dy = min_image32(ri.y - rj.y, L, Linv);
+                    const float dz = min_image32(ri.z - rj.z, L, Linv);
+                    pot.add(aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), a));
                 }
             }
         }

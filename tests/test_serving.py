@@ -116,3 +116,11 @@ def test_grand_canonical_job_same_alone_and_in_mix(pgb):
         info = mix.job(j)
         assert info["state"] == 3 and info["sweeps_done"] > 0 and info["first_bin"] >= info["admitted"]
     assert mix.bead_updates() > 0
+    # rounds of 0.2 ms stop most sweeps part-way: the resumed sweeps draw the
+    # same numbers
+    tiny = pgb.Server(2e9, sweeps_per_round=4, bin_sweeps=10, grand_canonical=True, round_seconds=0.0002)
+    jt = tiny.submit(**X)
+    b_tiny = [b for b in _run(tiny, [jt]) if b["job"] == jt]
+    assert [(b["bin"], b["samples"]) for b in b_tiny] == [(b["bin"], b["samples"]) for b in b_alone]
+    et = np.array([b["energy"] for b in b_tiny])
+    assert np.array_equal(np.isnan(ea), np.isnan(et)) and np.array_equal(ea[ok], et[ok])
