@@ -20,7 +20,7 @@ Reported on one JSON line:
   cpu_baseline / plain_fp64  the FP64 CPU oracle walkers on the host cores and
             the plain FP64 GPU form (host-driven moves) on a sample walker
   matched_energy  E/N of the batched walkers (replicas of the plain leg's
-            walker) beside the plain FP64 form's, with error bars
+            walker) beside the FP64 oracle's walkers, with error bars
 
 `--impl reference` times the reference's CPU path for the same workload (the
 oracle restatement: the reference itself cannot be built here).
@@ -282,15 +282,19 @@ def plain_form_rate(pgb, n=64, t=2.0, tau=0.004, steps=1):
                 accepted=r["accepted"], attempted=r["attempted"])
 
 
-def matched_energy(pgb, n=64, t=2.0, tau=0.004, replicas=256, equil=100, sweeps=200,
-                   plain_equil=100, plain_steps=100):
-    """Energy per particle of the batched mixed-precision walkers and of the
-    plain FP64 GPU form on the same configuration (the plain leg's walker):
-    the batched mean over independent replicas with its standard error, the
-    plain chain's mean with a binned error (10 bins), and their difference in
-    combined standard deviations.  A statistical check, bounded to a few
-    seconds: the test suite compares against the oracle at tighter error."""
+def matched_energy(pgb, threads, n=64, t=2.0, tau=0.004, replicas=256, equil=100, sweeps=200,
+                   oracle_replicas=16, oracle_equil=100, oracle_sweeps=100):
+    """Energy per particle of the batched mixed-precision walkers beside the
+    FP64 oracle's walkers on the same configuration (the plain leg's walker):
+    each the mean over independent replicas with its standard error, and
+    their difference in combined standard errors.  One long chain of the
+    plain FP64 form would need thousands of steps for an honest error bar
+    (its 50-step block means scatter by about 1.7 K here), so the FP64 side is
+    the oracle's replicas on the host cores, which the plain form matches
+    draw for draw."""
     from pimc_gb300 import worldlines as wl
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
     m = wl.even_slices(t, tau)
     L = wl.box_side(n)
     mbar = wl.default_mbar(n, L ** 3, wl.LAMBDA_HE4, tau, m)
@@ -305,18 +309,17 @@ def matched_energy(pgb, n=64, t=2.0, tau=0.004, replicas=256, equil=100, sweeps=
     e_rep = st["energy_sum"] / np.maximum(st["samples"], 1)
     eb, sb = float(e_rep.mean()), float(e_rep.std(ddof=1) / np.sqrt(replicas))
     W.close()
-    a = pgb.Action(L, m, n, tau, wl.LAMBDA_HE4, precision=pgb.PGB_FP64)
-    a.load(wl.seeded_worldlines(n, m, L, wl.LAMBDA_HE4, tau, 5))
-    a.plain_seed(2718)
-    a.plain_run(plain_equil, mbar=mbar, temperature=T)
-    en = a.plain_run(plain_steps, mbar=mbar, temperature=T)["energies"]
-    bins = en[: (len(en) // 10) * 10].reshape(10, -1).mean(axis=1)
-    ep, sp = float(en.mean()), float(bins.std(ddof=1) / np.sqrt(10))
+    sec, en, _ = pyoracle.walkers_cpu(np.full(oracle_replicas, n), np.full(oracle_replicas, m),
+                                      np.full(oracle_replicas, T), np.full(oracle_replicas, L),
+                                      np.arange(oracle_replicas, dtype=np.uint32) + 99, tau, wl.LAMBDA_HE4,
+                                      oracle_sweeps, threads, nequil=oracle_equil)
+    eo, so = float(en.mean()), float(en.std(ddof=1) / np.sqrt(oracle_replicas))
     return dict(config="N=%d M=%d T=%.3f Mbar=%d" % (n, m, T, mbar),
-                batched=[eb, sb], plain_fp64=[ep, sp],
-                diff_sigma=abs(eb - ep) / math.hypot(sb, sp),
-                sample="batched: %d replicas, %d + %d sweeps; plain FP64: one chain, %d + %d steps"
-                       % (replicas, equil, sweeps, plain_equil, plain_steps))
+                batched=[eb, sb], oracle_fp64=[eo, so],
+                diff_sigma=abs(eb - eo) / math.hypot(sb, so),
+                sample="batched: %d replicas, %d + %d sweeps; FP64 oracle walkers: %d replicas, %d + %d "
+                       "sweeps on %d host threads (%.0f s)"
+                       % (replicas, equil, sweeps, oracle_replicas, oracle_equil, oracle_sweeps, threads, sec))
 
 
 # ---------------------------------------------------------------------------
@@ -969,7 +972,7 @@ def main():
         out["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
         out["plain_fp64"] = plain_form_rate(pgb)
         out["plain_fp64"]["batched_over_plain"] = value / out["plain_fp64"]["value"]
-        out["matched_energy"] = matched_energy(pgb)
+        out["matched_energy"] = matched_energy(pgb, os.cpu_count() or 1)
         out["serving"] = serving_run(pgb, seconds=args.serve_seconds, grand_canonical=not args.serve_canonical)
     if rank == 0:
         print(json.dumps(out))
