@@ -376,10 +376,15 @@ struct WormWalker {
         const int* ch = chain;
         KahanF k;
         bool ok = true;
-        for (int i = 0; i < cnt; ++i) {
-            BeadLoad L;
-            ok &= loadBead(c, ch[c0 + i], L);
-            if (L.b.p < L.n) pairsLoaded(c, L, k);
+        if (cnt > 0) {
+            // the next bead's loads are in flight while this bead's pairs are summed
+            BeadLoad cur, nx;
+            ok &= loadBead(c, ch[c0], cur);
+            for (int i = 0; i < cnt; ++i) {
+                if (i + 1 < cnt) ok &= loadBead(c, ch[c0 + i + 1], nx);
+                if (cur.b.p < cur.n) pairsLoaded(c, cur, k);
+                cur = nx;
+            }
         }
         if (!ok) err = WERR_LINK;
         return m.tau * warp_sum_ff(k);
