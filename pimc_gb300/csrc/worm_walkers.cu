@@ -329,23 +329,23 @@ struct WormWalker {
         return ok;
     }
     // one pair term, without branches: a partner that is absent (j at or
-    // beyond the count, or the bead itself) adds zero
+    // beyond the count, or the bead itself) adds zero.  With Plain set the
+    // slice holds no worm or special bead and every factor is one.
+    template <bool Plain>
     __device__ static void pairTerm(const PairCtx& c, WB b, int s1, int j, int n, float4 rb, float4 rj,
                                     KahanF& k) {
         const bool ok = j < n && j != b.p;
-        const float f = ok ? factor(s1, c.state(WB{b.t, j})) : 0.0f;
+        const float f = ok ? (Plain ? 1.0f : factor(s1, c.state(WB{b.t, j}))) : 0.0f;
         const float dx = min_image32(rj.x - rb.x, c.L, c.Linv);
         const float dy = min_image32(rj.y - rb.y, c.L, c.Linv);
         const float dz = min_image32(rj.z - rb.z, c.L, c.Linv);
         const float r2 = ok ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : 1.0f;
         k.add(f * aziz_v32_sel(r2, c.az));
     }
-    // tau-less pair terms of a loaded bead with its active same-slice
-    // partners, added to the lane's running sum in ascending partner order
-    __device__ static void pairsLoaded(const PairCtx& c, const BeadLoad& L, KahanF& k) {
-        const int s1 = c.state(L.b);
+    template <bool Plain>
+    __device__ static void pairsOf(const PairCtx& c, const BeadLoad& L, int s1, KahanF& k) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) pairTerm(c, L.b, s1, 32 * u + c.lane, L.n, L.rb, L.r[u], k);
+        for (int u = 0; u < 4; ++u) pairTerm<Plain>(c, L.b, s1, 32 * u + c.lane, L.n, L.rb, L.r[u], k);
         const float4* row = c.pos + (size_t)L.b.t * c.Ne;
         for (int j0 = 128; j0 < L.n; j0 += 128) {
             float4 r[4];
@@ -355,8 +355,16 @@ struct WormWalker {
                 r[u] = j < L.n ? row[j] : L.rb;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) pairTerm(c, L.b, s1, j0 + 32 * u + c.lane, L.n, L.rb, r[u], k);
+            for (int u = 0; u < 4; ++u) pairTerm<Plain>(c, L.b, s1, j0 + 32 * u + c.lane, L.n, L.rb, r[u], k);
         }
+    }
+    // tau-less pair terms of a loaded bead with its active same-slice
+    // partners, added to the lane's running sum in ascending partner order
+    __device__ static void pairsLoaded(const PairCtx& c, const BeadLoad& L, KahanF& k) {
+        const int s1 = c.state(L.b);
+        const int t = L.b.t;
+        if (s1 == 0 && c.head.t != t && c.tail.t != t && c.sp1.t != t && c.sp2.t != t) pairsOf<true>(c, L, s1, k);
+        else pairsOf<false>(c, L, s1, k);
     }
     // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
     // tau * sum over the other active beads of the slice of factor * V
@@ -1374,6 +1382,33 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     }
 }
 
+// an admitted job's seeded closed worldlines: particle i's centre uniform in
+// the box (Philox block (i, 0)), each of its beads jittered by sigma per
+// coordinate (Box-Muller on block (i, t + 1)) and put back in the box,
+// identity links, N0 beads on every slice; the unused capacity cleared
+__global__ void k_seed_worldlines(float4* __restrict__ pos, int* __restrict__ nxt, int* __restrict__ prv,
+                                  int* __restrict__ nbs, int M, int Ne, int N0, float L, float sigma, uint2 key) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (long long)M * Ne) return;
+    const int t = (int)(k / Ne), i = (int)(k - (long long)t * Ne);
+    if (i < N0) {
+        const uint4 c = philox4x32(make_uint4((uint32_t)i, 0u, 0x43454E54u, 0u), key);
+        const uint4 g = philox4x32(make_uint4((uint32_t)i, (uint32_t)(t + 1), 0x4A495454u, 0u), key);
+        const float2 n01 = box_muller(g.x, g.y), n23 = box_muller(g.z, g.w);
+        float r[3] = {L * (u01f(c.x) - 0.5f) + sigma * n01.x, L * (u01f(c.y) - 0.5f) + sigma * n01.y,
+                      L * (u01f(c.z) - 0.5f) + sigma * n23.x};
+        for (int d = 0; d < 3; ++d) r[d] -= L * floorf(r[d] / L + 0.5f);
+        pos[k] = make_float4(r[0], r[1], r[2], 0.f);
+        nxt[k] = i;
+        prv[k] = i;
+    } else {
+        pos[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        nxt[k] = -1;
+        prv[k] = -1;
+    }
+    if (i == 0) nbs[t] = N0;
+}
+
 // one warp: the serial and the lane-parallel normal deviates from the same
 // stream position
 __global__ void k_normals_check(uint2 key, int skip, int count, float* serial, float* parallel, int* state) {
@@ -1856,33 +1891,22 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
         m.key = make_uint2((uint32_t)sd, (uint32_t)(sd >> 32));
         s->h_meta[k] = m;
         s->h_nbs_off[k] = so;
-        // seeded closed worldlines: uniform centres, Gaussian jitter per bead
-        std::mt19937_64 rng(job.spec.seed);
-        std::uniform_real_distribution<double> u(-0.5, 0.5);
-        std::normal_distribution<double> g(0.0, std::sqrt(2.0 * s->p.lambda * s->p.tau));
-        std::vector<float4> pp((size_t)job.M * job.Ne, make_float4(0.f, 0.f, 0.f, 0.f));
-        std::vector<int> nx((size_t)job.M * job.Ne, -1);
-        std::vector<int> nbv(job.M, job.N0);
-        for (int i = 0; i < job.N0; ++i) {
-            const double c[3] = {u(rng) * job.L, u(rng) * job.L, u(rng) * job.L};
-            for (int t = 0; t < job.M; ++t) {
-                double r[3];
-                for (int d = 0; d < 3; ++d) { r[d] = c[d] + g(rng); r[d] -= job.L * std::floor(r[d] / job.L + 0.5); }
-                pp[(size_t)t * job.Ne + i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
-                nx[(size_t)t * job.Ne + i] = i;
-            }
-        }
+        // the job's seeded worldlines are made on the device; its constants,
+        // slice offset and initial state are uploaded once (pageable copies
+        // return once the source is staged)
+        const long long nbe = (long long)job.M * job.Ne;
+        const uint64_t ws = job.spec.seed * 0xD1B54A32D192ED03ull + 0x8CB92BA72F3D8DD7ull;
+        k_seed_worldlines<<<(unsigned)((nbe + 255) / 256), 256, 0, s->stream>>>(
+            s->d_pos + bo, s->d_nxt + bo, s->d_prv + bo, s->d_nbs + so, job.M, job.Ne, job.N0, (float)job.L,
+            (float)std::sqrt(2.0 * s->p.lambda * s->p.tau), make_uint2((uint32_t)ws, (uint32_t)(ws >> 32)));
+        if (e == cudaSuccess) e = cudaGetLastError();
         WWState st{};
         for (int i = 0; i < 2; ++i) st.head[i] = st.tail[i] = st.sp1[i] = st.sp2[i] = -1;
         st.gap = -1; st.diag = 1; st.numBeadsOn = job.N0 * job.M;
-        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_pos + bo, pp.data(), pp.size() * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nxt + bo, nx.data(), nx.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_prv + bo, nx.data(), nx.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nbs + so, nbv.data(), nbv.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_state + k, &st, sizeof(WWState), cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_meta + k, &s->h_meta[k], sizeof(WWMeta), cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nbs_off + k, &s->h_nbs_off[k], sizeof(long long), cudaMemcpyHostToDevice, s->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(s->d_stats + k, 0, sizeof(pgb_worm_walker_stats), s->stream);
-        // the host vectors must live until the copies finish
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) return s->cfail(e, "worm server admit");
     }
     std::vector<int> active;
@@ -1902,8 +1926,6 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
         const WWMeta& mb = s->h_meta[b];
         return 1.0 * ma.N0 * ma.N0 * ma.M > 1.0 * mb.N0 * mb.N0 * mb.M;
     });
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_meta, s->h_meta.data(), s->max_slots * sizeof(WWMeta), cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_nbs_off, s->h_nbs_off.data(), s->max_slots * sizeof(long long), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_limit, s->h_limit.data(), s->max_slots * sizeof(int), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess && !active.empty()) e = cudaMemcpyAsync(s->d_order, active.data(), active.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
     if (e != cudaSuccess) return s->cfail(e, "worm server upload");
