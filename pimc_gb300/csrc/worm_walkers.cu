@@ -77,6 +77,9 @@ struct WWState {
     // random stream's position (draw-block counter and word index)
     int upd, rbidx;
     unsigned long long rctr;
+    // an energy sample stopped part-way: the next slice and the sums so far
+    int epending, eslice;
+    double epot, ekin;
 };
 
 struct WB { int t, p; };
@@ -1197,44 +1200,54 @@ struct WormWalker {
     // EnergyEstimator (estimator.cpp:940-1029), primitive action, E/N of a
     // closed configuration: kinetic term over every bead's next link,
     // potential over the pairs of every slice, the rc = L tail
-    __device__ __noinline__ double energy(int& N) {
-        N = numBeadsOn / m.M;
-        // register copies of the walker's fields (see PairCtx)
-        const float4* P_ = pos;
+    // the sums of the primitive energy over slices [t0, t1): the pair
+    // potential of every slice (row i against the partners j > i, four
+    // partners a lane at a time without branches) and every bead's squared
+    // link to the next slice
+    __device__ __noinline__ double2 energySums(int t0, int t1) {
+        const PairCtx c = pairCtx();
         const int* nx_ = nxt;
-        const int* nb_ = nbs;
-        const int M = m.M, Ne = m.Ne, ln = lane;
-        const float L = m.L, Linv = m.Linv;
-        const AzizF a = az;
         KahanF pot, kin;
-        for (int t = 0; t < M; ++t) {
-            const int n = nb_[t];
-            const int tn = t + 1 == M ? 0 : t + 1;
-            const float4* row = P_ + (size_t)t * Ne;
-            // kinetic: every bead's link to the next slice, lane-parallel
-            for (int i = ln; i < n; i += 32) {
-                const int pn = nx_[(size_t)t * Ne + i];
-                if (pn >= 0 && pn < Ne) {
-                    const float4 ri = row[i], rn = P_[(size_t)tn * Ne + pn];
-                    const float vx = min_image32(rn.x - ri.x, L, Linv);
-                    const float vy = min_image32(rn.y - ri.y, L, Linv);
-                    const float vz = min_image32(rn.z - ri.z, L, Linv);
+        for (int t = t0; t < t1; ++t) {
+            const int n = c.nbs[t];
+            const int tn = t + 1 == c.M ? 0 : t + 1;
+            const float4* row = c.pos + (size_t)t * c.Ne;
+            for (int i = c.lane; i < n; i += 32) {
+                const int pn = nx_[(size_t)t * c.Ne + i];
+                if (pn >= 0 && pn < c.Ne) {
+                    const float4 ri = row[i], rn = c.pos[(size_t)tn * c.Ne + pn];
+                    const float vx = min_image32(rn.x - ri.x, c.L, c.Linv);
+                    const float vy = min_image32(rn.y - ri.y, c.L, c.Linv);
+                    const float vz = min_image32(rn.z - ri.z, c.L, c.Linv);
                     kin.add(fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
                 }
             }
-            // potential: row i against partners j > i spread over the lanes
             for (int i = 0; i + 1 < n; ++i) {
                 const float4 ri = row[i];
-                for (int j = i + 1 + ln; j < n; j += 32) {
-                    const float4 rj = row[j];
-                    const float dx = min_image32(ri.x - rj.x, L, Linv);
-                    const float dy = min_image32(ri.y - rj.y, L, Linv);
-                    const float dz = min_image32(ri.z - rj.z, L, Linv);
-                    pot.add(aziz_v32_core(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), a));
+                for (int j0 = i + 1; j0 < n; j0 += 128) {
+                    float4 r[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int j = j0 + 32 * u + c.lane;
+                        r[u] = j < n ? row[j] : ri;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const bool ok = j0 + 32 * u + c.lane < n;
+                        const float dx = min_image32(ri.x - r[u].x, c.L, c.Linv);
+                        const float dy = min_image32(ri.y - r[u].y, c.L, c.Linv);
+                        const float dz = min_image32(ri.z - r[u].z, c.L, c.Linv);
+                        const float r2 = ok ? fmaf(dx, dx, fmaf(dy, dy, dz * dz)) : 1.0f;
+                        pot.add(ok ? aziz_v32_sel(r2, c.az) : 0.0f);
+                    }
                 }
             }
         }
-        const double V = warp_sum_ff(pot), K2 = warp_sum_ff(kin);
+        return make_double2(warp_sum_ff(pot), warp_sum_ff(kin));
+    }
+    // EnergyEstimator's E/N from the sums over all slices
+    __device__ double energyFrom(double V, double K2, int& N) const {
+        N = numBeadsOn / m.M;
         if (N <= 0) return 0.0;
         const double totK = 1.5 * N / m.tau - K2 * ((0.25 / (m.lambda * m.tau)) / (m.tau * m.M));
         const double totV = V / m.M + (1.0 * N * N / m.volume) * m.tailV0;
@@ -1251,7 +1264,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
                const int* __restrict__ limit, unsigned long long budget_ns) {
     // walker i of this launch is order[i] (all walkers in index order when
     // order is null); limit[w] caps its completed sweeps; with budget_ns > 0
-    // a walker stops between two moves (checked every 8 moves) once that much
+    // a walker stops between two moves (the clock read before each) once that much
     // device time has passed, and the next launch resumes the sweep there
     __shared__ float4 s_orig[kWWWarps][kOrigCap];
     __shared__ int s_chain[kWWWarps][kChainCap];
@@ -1319,53 +1332,75 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
             ww.buf = philox4x32(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0x574F524Du, 0u), ww.m.key);
         }
     }
+    // an energy sample in progress resumes at its next slice (its sweep's
+    // moves are done)
+    int eslice = st.epending ? st.eslice : -1;
+    double epot = st.epending ? st.epot : 0.0, ekin = st.epending ? st.ekin : 0.0;
+    auto out_of_time = [&]() {
+        // lane 0's clock for every lane: the decision must be uniform
+        if (!budget_ns) return false;
+        const unsigned long long now = __shfl_sync(0xffffffffu, gtimer_ns(), 0);
+        return now - t0 > budget_ns;
+    };
+    bool stopped = false;
     for (int sw = 0; sw < lim && !ww.err; ++sw) {
-        if (u0 == 0) {
-            ww.ctr = sweep_no << 32;
-            ww.bidx = 4;
-        }
-        int u = u0;
-        bool out_of_time = false;
-        for (; u < ww.m.num_updates && !ww.err; ++u) {
-            if (budget_ns && (u & 7) == 0) {
-                // lane 0's clock for every lane: the decision must be uniform
-                const unsigned long long now = __shfl_sync(0xffffffffu, gtimer_ns(), 0);
-                if (now - t0 > budget_ns) { out_of_time = true; break; }
+        if (eslice < 0) {
+            if (u0 == 0) {
+                ww.ctr = sweep_no << 32;
+                ww.bidx = 4;
             }
-            const double x = ww.rand();
-            const double* cum = ww.diag ? cumD : cumO;
-            int index = WM_N - 1;
-            for (int i = 0; i < WM_N; ++i) if (cum[i] >= x) { index = i; break; }
-            bool acc = false;
-            int moved = 0;
-            switch (index) {
-                case WM_COM: moved = ww.com(acc); local.bead_updates += moved; break;
-                case WM_DIAG: moved = ww.staging(acc, orig); local.bead_updates += moved; break;
-                case WM_OPEN: ww.open(); break;
-                case WM_CLOSE: ww.close(); break;
-                case WM_INSERT: ww.insert(); break;
-                case WM_REMOVE: ww.remove(); break;
-                case WM_AH: ww.advanceHead(); break;
-                case WM_RH: ww.recedeHead(); break;
-                case WM_AT: ww.advanceTail(); break;
-                case WM_RT: ww.recedeTail(); break;
-                case WM_SH: ww.swapHead(orig); break;
-                case WM_ST: ww.swapTail(orig); break;
+            int u = u0;
+            for (; u < ww.m.num_updates && !ww.err; ++u) {
+                if (out_of_time()) { stopped = true; break; }
+                const double x = ww.rand();
+                const double* cum = ww.diag ? cumD : cumO;
+                int index = WM_N - 1;
+                for (int i = 0; i < WM_N; ++i) if (cum[i] >= x) { index = i; break; }
+                bool acc = false;
+                int moved = 0;
+                switch (index) {
+                    case WM_COM: moved = ww.com(acc); local.bead_updates += moved; break;
+                    case WM_DIAG: moved = ww.staging(acc, orig); local.bead_updates += moved; break;
+                    case WM_OPEN: ww.open(); break;
+                    case WM_CLOSE: ww.close(); break;
+                    case WM_INSERT: ww.insert(); break;
+                    case WM_REMOVE: ww.remove(); break;
+                    case WM_AH: ww.advanceHead(); break;
+                    case WM_RH: ww.recedeHead(); break;
+                    case WM_AT: ww.advanceTail(); break;
+                    case WM_RT: ww.recedeTail(); break;
+                    case WM_SH: ww.swapHead(orig); break;
+                    case WM_ST: ww.swapTail(orig); break;
+                }
             }
+            if (stopped || ww.err) { u0 = u; break; }
+            u0 = 0;
+            if (ww.diag) { eslice = 0; epot = 0.0; ekin = 0.0; }
         }
-        if (out_of_time || ww.err) { u0 = u; break; }
-        u0 = 0;
-        ++sweep_no;
-        local.sweeps += 1;
-        if (ww.diag) {
+        if (eslice >= 0) {
+            // the energy sample in chunks of 8 slices, the budget checked
+            // between chunks; the chunk sums add in slice order, so where a
+            // launch stops does not change the sample
+            while (eslice < ww.m.M && !ww.err) {
+                if (out_of_time()) { stopped = true; break; }
+                const int t1 = min(eslice + 8, ww.m.M);
+                const double2 r = ww.energySums(eslice, t1);
+                epot += r.x;
+                ekin += r.y;
+                eslice = t1;
+            }
+            if (stopped || ww.err) break;
             int N;
-            const double e = ww.energy(N);
+            const double e = ww.energyFrom(epot, ekin, N);
             local.samples += 1;
             local.energy_sum += e;
             local.energy_sumsq += e * e;
             local.n_sum += N;
             local.n_sumsq += 1.0 * N * N;
+            eslice = -1;
         }
+        ++sweep_no;
+        local.sweeps += 1;
     }
     __syncwarp();
     if (ww.lane == 0) {
@@ -1376,6 +1411,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
         o.sep[0] = ww.sep[0]; o.sep[1] = ww.sep[1]; o.sep[2] = ww.sep[2];
         o.err = ww.err; o.ctr = sweep_no;
         o.upd = u0; o.rctr = ww.ctr; o.rbidx = ww.bidx;
+        o.epending = eslice >= 0; o.eslice = eslice < 0 ? 0 : eslice; o.epot = epot; o.ekin = ekin;
         states[w] = o;
         local.error = ww.err;
         stats[w] = local;
