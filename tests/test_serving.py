@@ -124,3 +124,4 @@ def test_grand_canonical_job_same_alone_and_in_mix(pgb):
     assert [(b["bin"], b["samples"]) for b in b_tiny] == [(b["bin"], b["samples"]) for b in b_alone]
     et = np.array([b["energy"] for b in b_tiny])
     assert np.array_equal(np.isnan(ea), np.isnan(et)) and np.array_equal(ea[ok], et[ok])
+

@@ -106,3 +106,21 @@ def test_parallel_normals_equal_serial_draws(pgb, skip):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (count, a[:4], b[:4])
         assert np.array_equal(st[:3], st[3:]), st
         assert np.all(np.isfinite(a)) and abs(a.std() - 1.0) < 0.6 if count > 40 else True
+
+
+def test_worm_walker_with_full_slices_stops_alone(pgb):
+    """A walker whose slices are full (capacity = N) stops with error 1 on its
+    first bead insertion, its arrays untouched beyond their capacity; the
+    other walkers run on."""
+    L = wl.box_side(N)
+    W = pgb.WormWalkers(np.full(4, N), M, L, 8, TAU, LAM, mu=0.0, window=-1, seed=5,
+                        capacity=np.array([N, 2 * N + 8, 2 * N + 8, 2 * N + 8]))
+    W.load_seeded(5)
+    W.run(40)
+    st = W.stats()
+    assert st["error"][0] == 1, st["error"]
+    assert np.all(st["error"][1:] == 0), st["error"]
+    assert np.all(st["sweeps"][1:] == 40) and st["sweeps"][0] < 40
+    p = W.path(0)
+    assert np.all(p["nbs"] <= N)
+    check_path(W.path(1), M)
