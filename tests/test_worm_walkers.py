@@ -124,3 +124,40 @@ def test_worm_walker_with_full_slices_stops_alone(pgb):
     p = W.path(0)
     assert np.all(p["nbs"] <= N)
     check_path(W.path(1), M)
+
+
+def test_worm_walkers_grand_canonical_match_oracle_statistically(pgb, oracle_lib):
+    """Grand canonical (no window) at mu = -2 K, as the serving jobs run:
+    <N> and <E/N> over closed configurations agree with the oracle's worm
+    engine within four combined standard errors."""
+    mu = -2.0
+    L = wl.box_side(N)
+    cfg = wl.seeded_worldlines(N, M, L, LAM, TAU, 1, extent=3 * N)
+    o = oracle_lib.Oracle(L, M, 3 * N, TAU, LAM, mu=mu)
+    o.load(cfg)
+    mt = oracle_lib.MT(17)
+    kw = dict(mbar=8, temperature=1.0 / (M * TAU), initial_num_particles=N, window=-1, mu=mu)
+    o.run_worm_steps(mt, 500, **kw)
+    r = o.run_worm_steps(mt, 8000, **kw)
+    e = r["energies"]
+    n = r["num_particles"].astype(float)
+    ok = ~np.isnan(e)
+    assert ok.sum() > 1000
+    eb = [e[i:i + 500][ok[i:i + 500]].mean() for i in range(0, 8000, 500)]
+    nb = [n[i:i + 500][ok[i:i + 500]].mean() for i in range(0, 8000, 500)]
+    eo, se_o = np.mean(eb), np.std(eb, ddof=1) / np.sqrt(len(eb))
+    no, sn_o = np.mean(nb), np.std(nb, ddof=1) / np.sqrt(len(nb))
+
+    W, _ = _walkers(pgb, 256, seed=21, window=-1, mu=mu)
+    W.run(200)
+    W.reset_stats()
+    W.run(300)
+    st = W.stats()
+    assert np.all(st["error"] == 0)
+    has = st["samples"] > 0
+    ew = st["energy_sum"][has] / st["samples"][has]
+    nw = st["n_sum"][has] / st["samples"][has]
+    e_w, se_w = ew.mean(), ew.std(ddof=1) / np.sqrt(len(ew))
+    n_w, sn_w = nw.mean(), nw.std(ddof=1) / np.sqrt(len(nw))
+    assert abs(n_w - no) <= 4.0 * np.hypot(sn_w, sn_o), (n_w, sn_w, no, sn_o)
+    assert abs(e_w - eo) <= 4.0 * np.hypot(se_w, se_o), (e_w, se_w, eo, se_o)
