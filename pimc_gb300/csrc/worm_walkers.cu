@@ -369,17 +369,6 @@ struct WormWalker {
         if (s1 == 0 && c.head.t != t && c.tail.t != t && c.sp1.t != t && c.sp2.t != t) pairsOf<true>(c, L, s1, k);
         else pairsOf<false>(c, L, s1, k);
     }
-    // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
-    // tau * sum over the other active beads of the slice of factor * V
-    __device__ __noinline__ double bare(WB b) {
-        if (!valid(b)) { err = WERR_LINK; return 0.0; }
-        const PairCtx c = pairCtx();
-        BeadLoad L;
-        loadBead(c, pack(b), L);
-        KahanF k;
-        pairsLoaded(c, L, k);
-        return m.tau * warp_sum_ff(k);
-    }
     // potentialAction over chain[c0 .. c0 + cnt - 1]: the lanes keep one
     // running sum over the whole range and reduce once
     __device__ __noinline__ double chainAction(int c0, int cnt) {
@@ -400,23 +389,15 @@ struct WormWalker {
         if (!ok) err = WERR_LINK;
         return m.tau * warp_sum_ff(k);
     }
-    // the beads from s to e along next links into chain[0 ..]: returns their
-    // count, 0 with the error word set when the range breaks or is longer
-    // than the cache
-    __device__ int walk(WB s, WB e) {
-        WB b = s;
-        for (int k = 0; k < kChainCap; ++k) {
-            if (isXW(b) || err) { err = err ? err : WERR_LINK; return 0; }
-            if (lane == 0) chain[k] = pack(b);
-            if (eqW(b, e)) { __syncwarp(); return k + 1; }
-            b = next(b);
-        }
-        err = WERR_LOOP;
-        return 0;
-    }
-    __device__ double rangeAction(WB s, WB e) {
-        const int cnt = walk(s, e);
-        return chainAction(0, cnt);
+    // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
+    // tau * sum over the other active beads of the slice of factor * V, as
+    // a one-bead range in the cache's last slot (no move's range reaches it:
+    // a range holds at most M < kChainCap beads)
+    __device__ double bare(WB b) {
+        if (!valid(b)) { err = WERR_LINK; return 0.0; }
+        if (lane == 0) chain[kChainCap - 1] = pack(b);
+        __syncwarp();
+        return chainAction(kChainCap - 1, 1);
     }
     // the primitive action has no gradient correction (gradVFactor = 0)
     __device__ double corrRange(WB, WB) { return 0.0; }
