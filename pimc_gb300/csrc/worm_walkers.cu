@@ -1009,10 +1009,12 @@ struct WormWalker {
     // order (bead fastest, sector slowest) whose cumulative weight reaches
     // x * Sigma: the sector by a scan over the lanes' sector sums, the bead
     // by a scan inside that sector.
+    // rho0 of one sector as the product of its three axis factors, the form
+    // the sector sums use
     __device__ static float rho0Shifted(float4 pf, float4 pb, int3 wv, int sign, float g3, float den, float L) {
-        const float ax = (pf.x - pb.x) + (sign * wv.x) * L, ay = (pf.y - pb.y) + (sign * wv.y) * L,
-                    az_ = (pf.z - pb.z) + (sign * wv.z) * L;
-        return g3 * expf(-(ax * ax + ay * ay + az_ * az_) / den);
+        const float ax = (pf.x - pb.x) + (float)(sign * wv.x) * L, ay = (pf.y - pb.y) + (float)(sign * wv.y) * L,
+                    az_ = (pf.z - pb.z) + (float)(sign * wv.z) * L;
+        return g3 * expf(-(ax * ax) / den) * expf(-(ay * ay) / den) * expf(-(az_ * az_) / den);
     }
     __device__ __noinline__ double towerNorm(WB b, int pivotSlice, int sign, float x, WB& pivot, int3& wind) {
         const int nL = nb(pivotSlice);
@@ -1031,14 +1033,29 @@ struct WormWalker {
                 const int n = n0 + 32 * u + ln;
                 pf[u] = n < nL ? row[n] : pb;
             }
+            // rho0 factorises over the axes: three shifts per axis (component
+            // 0, +1, -1 of the winding vector) give the 27 sector weights as
+            // products, 9 exponentials a bead instead of 27
+            float ex[4][3], ey[4][3], ez[4][3];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const bool ok = n0 + 32 * u + ln < nL;
+                const float dx = pf[u].x - pb.x, dy = pf[u].y - pb.y, dz = pf[u].z - pb.z;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float sh = (float)(sign * (k == 2 ? -1 : k)) * L;
+                    const float ax = dx + sh, ay = dy + sh, az_ = dz + sh;
+                    ex[u][k] = ok ? g3 * expf(-(ax * ax) / den) : 0.0f;
+                    ey[u][k] = expf(-(ay * ay) / den);
+                    ez[u][k] = expf(-(az_ * az_) / den);
+                }
+            }
+#pragma unroll
             for (int w = 0; w < kMaxWind; ++w) {
-                const int3 wv = winding(w);
+                const int kx = (w / 9) % 3, ky = (w / 3) % 3, kz = w % 3;
                 float v = 0.0f;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const float r = rho0Shifted(pf[u], pb, wv, sign, g3, den, L);
-                    v += n0 + 32 * u + ln < nL ? r : 0.0f;
-                }
+                for (int u = 0; u < 4; ++u) v += ex[u][kx] * ey[u][ky] * ez[u][kz];
                 for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
                 if (ln == w) mine += v;
             }
