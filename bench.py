@@ -1,29 +1,35 @@
-"""Benchmark: batched-walker bead updates per second on one GB300.
+"""Benchmark: batched bosonic walkers, bead updates per second on one GB300.
 
 Workload (the batched-walker configuration of the reference benchmark):
-1024 independent canonical He-4 chains, Aziz HFD-HE2, density 0.02186 A^-3,
+1024 independent He-4 paths, Aziz HFD-HE2, density 0.02186 A^-3,
 N ~ U{8..128}, T ~ U[1, 4] K, tau = 0.004 1/K, M = even round(1/(T tau)) (the
-reference forces M even), Philox streams per walker.  One *step* is one
-Monte Carlo sweep of every walker: numUpdates = max(100, ceil(N M / Mbar))
-staging / centre-of-mass moves per walker followed by one thermodynamic
-energy sample (the reference's PathIntegralMonteCarlo::step with the energy
-estimator).  A bead update is one bead proposed and Metropolis-tested.
+reference forces M even), Philox streams per walker, each run by the worm
+algorithm with the reference's default PIMC move list (centre of mass,
+bisection, open, close, insert, remove, advance/recede head and tail, swap
+head and tail; setup.cpp:467-471) and a canonical window of one particle, so
+exchange cycles are sampled.  One *step* is one PathIntegralMonteCarlo::step
+of every walker: numUpdates = max(100, ceil(N M / Mbar)) moves followed by the
+energy sample when the configuration is closed.  A bead update is one bead
+proposed and Metropolis-tested.
 
 Reported on one JSON line:
   value     bead-updates/s with the worldlines resident in HBM (CUDA events on
-            the library's stream, L2 flushed between timed steps)
+            the walkers' stream, L2 flushed between timed steps)
   e2e       the same through the C ABI with host buffers: every step uploads the
-            whole worldline state from pinned host memory, runs the sweep and
+            whole device state image from pinned host memory, runs the step and
             reads the per-walker estimator accumulators back
-  roofline  the walker kernel against the FP32 pipe (pair sums are FP32 FMA +
-            SFU work; HBM and tensor cores do not bind)
-  cpu_baseline / plain_fp64  the FP64 CPU oracle walkers on the host cores and
-            the plain FP64 GPU form (host-driven moves) on a sample walker
-  matched_energy  E/N of the batched walkers (replicas of the plain leg's
-            walker) beside the FP64 oracle's walkers, with error bars
+  roofline  the walker kernel against the FP32 and special-function pipes (pair
+            sums are FP32 FMA + SFU work; HBM and tensor cores do not bind)
+  cpu_baseline / plain_fp64  the FP64 oracle's worm engine on the same 1024
+            walkers on the host cores (set-up untimed), and the plain FP64 GPU
+            form (host-driven moves) on one walker
+  matched_energy  E/N of the batched walkers beside the FP64 oracle's, with
+            error bars
 
-`--impl reference` times the reference's CPU path for the same workload (the
-oracle restatement: the reference itself cannot be built here).
+`--workload canonical` runs the canonical staging + centre-of-mass walkers
+(no exchange moves) on the same 1024 paths.  `--impl reference` times the
+reference's CPU path for the default workload (the oracle restatement: the
+reference itself cannot be built on the benchmark host).
 """
 import argparse
 import json
@@ -51,6 +57,8 @@ SFU_PER_SM_CLK = 16     # nominal special-function results per SM per clock
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel on
 # the workload its bench leg runs (profiles/ holds the summaries)
 NCU_TRAFFIC = {"k_walkers_pipe": 160.4e6, "k_walkers_group": 158.9e6}
+# per-sweep DRAM bytes of k_worm_walkers on the 1024-walker workload (profiles/)
+NCU_TRAFFIC_WORM = None
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -67,7 +75,9 @@ def parse():
                     help="walker schedule code (0: autotune)")
     ap.add_argument("--no-baseline", action="store_true")
     ap.add_argument("--workload", default="walkers",
-                    choices=["walkers", "serving", "isf", "pair", "plain", "gp", "worm"])
+                    choices=["walkers", "canonical", "serving", "isf", "pair", "plain", "gp"])
+    ap.add_argument("--diagonal", default="bisection", choices=["bisection", "staging"],
+                    help="diagonal move of the worm walkers (the reference's default is bisection)")
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     return ap.parse_args()
 
@@ -339,13 +349,44 @@ def matched_energy(pgb, threads, n=64, t=2.0, tau=0.004, replicas=256, equil=100
 # load far exceeds capacity, so the window is bounded and the report states
 # how many jobs reached a first bin / completed (the rest are censored).
 # ---------------------------------------------------------------------------
-def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02, grand_canonical=True):
+def km_quantiles(durations, observed, qs=(50, 99)):
+    """Kaplan-Meier estimate of the event-time distribution from right-censored
+    durations (observed False: the event had not happened when the window
+    closed, the duration is the time the job was watched).  Returns, per
+    quantile, the smallest duration t with 1 - S(t) >= q/100, or None when
+    the estimate never reaches q (the quantile lies beyond the window)."""
+    d = np.asarray(durations, dtype=float)
+    o = np.asarray(observed, dtype=bool)
+    order = np.lexsort((~o, d))                 # events before censorings at equal times
+    d, o = d[order], o[order]
+    at_risk = len(d)
+    surv = 1.0
+    out = {q: None for q in qs}
+    for t, ev in zip(d, o):
+        if ev:
+            surv *= 1.0 - 1.0 / at_risk
+            for q in qs:
+                if out[q] is None and 1.0 - surv >= q / 100.0 - 1e-12:
+                    out[q] = float(t)
+        at_risk -= 1
+    return out
+
+
+def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02, grand_canonical=True,
+                arrival_seconds=None):
+    """Poisson arrivals at `rate` for arrival_seconds (0.6 of the window by
+    default), the server stepped until `seconds` have passed.  Time to first
+    bin and to completion are reported over every arrived job with the jobs
+    still waiting at the window's end treated as right-censored
+    (Kaplan-Meier), beside the plain percentiles over the jobs that reached
+    the event."""
     rng = np.random.Generator(np.random.Philox(seed))
+    arrive_for = 0.6 * seconds if arrival_seconds is None else arrival_seconds
     arrivals = []
     t = 0.0
     while True:
         t += rng.exponential(1.0 / rate)
-        if t > 0.6 * seconds:
+        if t > arrive_for:
             break
         arrivals.append(t)
     srv = pgb.Server(150e9, max_active=1024, bin_sweeps=100, round_seconds=round_seconds,
@@ -368,35 +409,51 @@ def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02, grand_
         peak_active = max(peak_active, a)
         nbins += len(srv.bins())
     elapsed = time.perf_counter() - t0
+    t_end = srv.clock()
     bu = srv.bead_updates()
     infos = [srv.job(j) for j in ids]
     arrived = [i for i in infos if i["state"] >= 1]
     ttfb = [i["first_bin"] - i["arrival"] for i in arrived if i["first_bin"] >= 0]
     done = [i["completed"] - i["arrival"] for i in arrived if i["completed"] >= 0]
     pct = lambda v, p: float(np.percentile(v, p)) if v else None
+    km_first = km_quantiles([(i["first_bin"] if i["first_bin"] >= 0 else t_end) - i["arrival"] for i in arrived],
+                            [i["first_bin"] >= 0 for i in arrived])
+    km_done = km_quantiles([(i["completed"] if i["completed"] >= 0 else t_end) - i["arrival"] for i in arrived],
+                           [i["completed"] >= 0 for i in arrived])
     srv.close()
-    return {"bead_updates_per_s": bu / elapsed, "window_s": round(elapsed, 2), "rounds": rounds,
+    n_arr = max(len(arrived), 1)
+    return {"bead_updates_per_s": bu / elapsed, "window_s": round(elapsed, 2),
+            "arrival_window_s": round(arrive_for, 2), "rounds": rounds,
             "jobs_arrived": len(arrived), "jobs_admitted": sum(1 for i in arrived if i["admitted"] >= 0),
             "jobs_with_first_bin": len(ttfb), "jobs_completed": len(done),
+            "censored_first_bin_frac": 1.0 - len(ttfb) / n_arr,
+            "censored_completion_frac": 1.0 - len(done) / n_arr,
             "jobs_failed": sum(1 for i in arrived if i["state"] == 4), "bins": nbins,
             "peak_active": peak_active,
-            "ttfb_p50_s": pct(ttfb, 50), "ttfb_p99_s": pct(ttfb, 99),
-            "completion_p50_s": pct(done, 50), "completion_p99_s": pct(done, 99),
-            "note": "Poisson 50 jobs/s for %.1f s of a %.1f s window; percentiles over jobs that "
-                    "reached the event inside the window (the others are censored); %s, bins of "
-                    "100 sweeps, rounds of %g s of device time"
-                    % (0.6 * seconds, seconds,
-                       "grand-canonical worm walkers at each job's mu (the full move list)"
+            "ttfb_p50_s": km_first[50], "ttfb_p99_s": km_first[99],
+            "completion_p50_s": km_done[50], "completion_p99_s": km_done[99],
+            "uncensored": {"ttfb_p50_s": pct(ttfb, 50), "ttfb_p99_s": pct(ttfb, 99),
+                           "completion_p50_s": pct(done, 50), "completion_p99_s": pct(done, 99)},
+            "note": "Poisson %g jobs/s for %.1f s of a %.1f s window; p50/p99 are Kaplan-Meier "
+                    "estimates over every arrived job, a job still waiting when the window closed "
+                    "counted as right-censored at its time in the system (null: the quantile lies "
+                    "beyond the window); 'uncensored' gives the percentiles over the jobs that "
+                    "reached the event; %s, bins of 100 sweeps, rounds of %g s of device time"
+                    % (rate, arrive_for, seconds,
+                       "grand-canonical worm walkers at each job's mu (the full move list, bisection)"
                        if grand_canonical else "canonical chains (staging + COM)", round_seconds)}
 
 
 def run_serving(args, pgb):
-    r = serving_run(pgb, seconds=args.serve_seconds, grand_canonical=not args.serve_canonical)
+    arrive = args.serve_seconds if args.serve_seconds >= 120 else None
+    r = serving_run(pgb, seconds=args.serve_seconds, grand_canonical=not args.serve_canonical,
+                    arrival_seconds=arrive)
     out = {"metric": "serving p99 time-to-first-bin", "value": r["ttfb_p99_s"], "unit": "s",
            "n_gpus": 1, "steps": r["rounds"], "warmup": 0, "higher_is_better": False,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
            "config": {"workload": "serving: Poisson 50 jobs/s, N0 log-U[8,512], T U[0.5,4], "
-                                  "mu U[-10,0], sweeps log-U[1e3,1e5], 150 GB HBM budget"},
+                                  "mu U[-10,0], sweeps log-U[1e3,1e5], 150 GB HBM budget",
+                      "censoring": "Kaplan-Meier over all arrived jobs"},
            "serving": r}
     print(json.dumps(out))
 
@@ -792,68 +849,229 @@ def run_gp(args, pgb):
 
 
 # ---------------------------------------------------------------------------
-# Device-resident worm walkers: the batched-walker workload (1024 He-4 paths,
-# N ~ U{8..128}, T ~ U[1,4] K, tau = 0.004, M even) run with the worm
-# algorithm's full move list, canonical window 1, one warp per walker.
+# The default line: the batched-walker workload (1024 He-4 paths,
+# N ~ U{8..128}, T ~ U[1,4] K, tau = 0.004, M even) run by the device worm
+# walkers with the reference's default move list and a canonical window of
+# one particle.
 # ---------------------------------------------------------------------------
-def run_worm(args, pgb):
-    import torch
+DIAGONAL = {"bisection": 0, "staging": 1}
+
+
+def worm_pair_evals(w, st):
+    """Algorithmic pair evaluations of the walkers' steps: every bead update
+    compares the bead's action before and after the proposal against its N-1
+    partners (2 (N-1) pairs; the single-bead worm moves evaluate one action per
+    bead and are counted the same way), and each energy sample sums
+    M N (N-1)/2 pairs.  N is the walker's target particle number."""
+    n, m = w["n"].astype(float), w["m"].astype(float)
+    return float((2.0 * (n - 1) * st["bead_updates"] + st["samples"] * m * n * (n - 1) / 2.0).sum())
+
+
+PRE_SWEEPS = 20       # diagonal pre-equilibration steps before the warm-up (both arms)
+
+
+def worm_sample(w, every=4):
+    """Every `every`-th walker of the workload in order of cost N^2 M: a
+    stratified sample with the workload's mix of sizes."""
+    order = np.argsort(w["n"].astype(float) ** 2 * w["m"], kind="stable")
+    idx = np.sort(order[::every])
+    return {k: (v[idx] if isinstance(v, np.ndarray) else v) for k, v in w.items()}
+
+
+def cpu_baseline_worm(w, threads, nequil=3, nsteps=5, diagonal_move=0, seed=7, every=4):
+    """The oracle's FP64 worm engine (MT19937, the same move list, window and
+    worm constant) on a stratified quarter of the workload's walkers, all host
+    threads: set-up, PRE_SWEEPS diagonal pre-equilibration steps and nequil
+    steps untimed, nsteps steps of every sampled walker timed (the walkers
+    outnumber the threads 16 to 1, taken largest first, so none idles)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    s = worm_sample(w, every)
+    r = pyoracle.worm_walkers_cpu(s["n"], s["m"], s["side"], s["mbar"],
+                                  np.arange(len(s["n"]), dtype=np.uint32) + seed, w["tau"], w["lam"],
+                                  nsteps, threads, nequil=nequil, window=1, diagonal_move=diagonal_move,
+                                  npre=PRE_SWEEPS)
+    bu = int(r["bead_updates"].sum())
+    return dict(value=bu / r["seconds"], unit="bead-updates/s", cores=threads, kind="port",
+                timed="sweeps only",
+                sample="%d of the %d walkers (every %d-th by N^2 M), %d timed step(s) each after %d "
+                       "pre-equilibration and %d untimed steps (set-up %.1f s untimed), FP64 oracle "
+                       "worm engine with MT19937, %s, window 1, C0 1, %d threads, %.1f s timed"
+                       % (len(s["n"]), len(w["n"]), every, nsteps, PRE_SWEEPS, nequil,
+                          r["setup_seconds"], ["bisection", "staging"][diagonal_move], threads,
+                          r["seconds"]),
+                failed_walkers=r["failed"])
+
+
+def plain_worm_rate(pgb, n=64, t=2.0, tau=0.004, steps=2, diagonal_move=0):
+    """The plain FP64 GPU form of the same algorithm: the reference's move
+    loop on the host (MT19937, worm moves, window 1) with one FP64 device
+    action call per Metropolis decision, on one walker of the workload's mean
+    size."""
     from pimc_gb300 import worldlines as wl
-    w = wl.workload_walkers(num=args.walkers, seed=0)
-    n, m = w["n"], w["m"]
-    L = w["side"]
-    W = pgb.WormWalkers(n, m, L, w["mbar"], w["tau"], w["lam"], window=1, seed=1)
-    W.load_seeded(1)
-    W.run(max(3, args.warmup))
-    W.reset_stats()
-    clk = Clocks()
-    torch.cuda.synchronize()
+    m = wl.even_slices(t, tau)
+    L = wl.box_side(n)
+    mbar = wl.default_mbar(n, L ** 3, wl.LAMBDA_HE4, tau, m)
+    ne = 2 * n + 8
+    a = pgb.Action(L, m, ne, tau, wl.LAMBDA_HE4, precision=pgb.PGB_FP64)
+    a.load(wl.seeded_worldlines(n, m, L, wl.LAMBDA_HE4, tau, 5, extent=ne))
+    a.plain_seed(139853)
+    kw = dict(mbar=mbar, temperature=1.0 / (m * tau), initial_num_particles=n, window=1,
+              diagonal_move=diagonal_move)
+    a.plain_worm_run(1, **kw)                                  # warm-up
     t0 = time.perf_counter()
-    W.run(args.steps)
+    r = a.plain_worm_run(steps, **kw)
     dt = time.perf_counter() - t0
+    a.close()
+    return dict(value=r["bead_updates"] / dt, unit="bead-updates/s",
+                walker="N=%d M=%d T=%.3f Mbar=%d, %d step(s) of the worm algorithm, window 1"
+                       % (n, m, 1.0 / (m * tau), mbar, steps))
+
+
+def matched_energy_worm(pgb, diagonal_move=0, path=None):
+    """Energy per particle of the batched walkers (FP32 pair sums, Philox)
+    beside the FP64 oracle's worm engine (MT19937) at the points of
+    tests/golden/matched_energy.json, which holds the oracle side (hours of
+    host time, made once by tests/golden/make_matched_energy.py).  The GPU
+    side runs the same replicas, pre-equilibration, equilibration and
+    sampled steps; each side's value is the mean over replicas of the
+    replica's mean E/N over its closed steps, with the standard error over
+    replicas, and diff_sigma the difference in combined standard errors."""
+    path = path or os.path.join(ROOT, "tests", "golden", "matched_energy.json")
+    if not os.path.exists(path):
+        return {"note": "no oracle fixture (tests/golden/matched_energy.json)"}
+    fx = json.load(open(path))
+    out = []
+    for pt in fx["points"]:
+        if pt.get("diagonal_move", 0) != diagonal_move:
+            continue
+        R = pt["replicas"]
+        n, m, L, mbar = pt["n"], pt["m"], pt["side"], pt["mbar"]
+        W = pgb.WormWalkers(np.full(R, n), m, L, mbar, fx["tau"], fx["lambda"], window=fx["window"],
+                            seed=777 + n, diagonal_move=diagonal_move, worm_constant=pt["worm_constant"])
+        W.seed_device(777 + n)
+        t0 = time.perf_counter()
+        W.equilibrate(pt["pre"])
+        W.run(pt["equil"])
+        W.reset_stats()
+        W.run(pt["sweeps"])
+        dt = time.perf_counter() - t0
+        st = W.stats()
+        W.close()
+        has = st["samples"] > 0
+        e = st["energy_sum"][has] / st["samples"][has]
+        eb, sb = float(e.mean()), float(e.std(ddof=1) / math.sqrt(max(len(e), 1)))
+        eo, so = pt["mean"], pt["stderr"]
+        out.append({"config": "N=%d M=%d T=%.3f Mbar=%d C0=%.4g" % (n, m, pt["temperature"], mbar,
+                                                                     pt["worm_constant"]),
+                    "batched": [eb, sb], "oracle_fp64": [eo, so],
+                    "diff_sigma": abs(eb - eo) / math.hypot(sb, so),
+                    "closed_replicas": [int(has.sum()), pt["closed_replicas"]],
+                    "sample": "%d replicas each side, %d pre-equilibration + %d + %d sampled steps; "
+                              "GPU side %.1f s" % (R, pt["pre"], pt["equil"], pt["sweeps"], dt)})
+    return out
+
+
+def run_walkers(args, pgb, rank, ws):
+    import torch
+    dm = DIAGONAL[args.diagonal]
+    w = workload(args.walkers, seed=rank)
+    W = pgb.WormWalkers(w["n"], w["m"], w["side"], w["mbar"], w["tau"], w["lam"], window=1,
+                        seed=1000 + rank, diagonal_move=dm)
+    W.seed_device(1000 + rank)
+    stream = torch.cuda.ExternalStream(W.stream())
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    warm = max(3, args.warmup)
+    W.equilibrate(PRE_SWEEPS)
+    W.run(warm)
+    W.reset_stats()
+    # device-resident timed steps
+    barrier(ws)
+    torch.cuda.synchronize()
+    clk = Clocks()
+    evs = []
+    l0 = W.launch_count()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            W.run(1, sync=False)
+            e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    barrier(ws)
     clocks = clk.stop()
+    launches = W.launch_count() - l0
+    t_dev = sum(a.elapsed_time(b) for a, b in evs) / 1e3
     st = W.stats()
     bu = float(st["bead_updates"].sum())
+    pairs = worm_pair_evals(w, st)
+    errors = int((st["error"] != 0).sum())
     att, acc = st["attempted"].sum(axis=0), st["accepted"].sum(axis=0)
-    out = {"metric": "bead-updates/s (device worm walkers)", "value": bu / dt, "unit": "bead-updates/s",
-           "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": 1e3 * dt / args.steps,
+    closed = int(st["samples"].sum())
+    t_max = max_over_ranks(t_dev, ws)
+    value = sum_over_ranks(bu, ws) / t_max
+
+    # e2e through the C ABI with host buffers: every step uploads the whole
+    # device state image from pinned memory, runs one step and reads the
+    # per-walker accumulators back
+    nbytes = W.state_bytes()
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    image = host.numpy()
+    W.get_state(image)
+    stats_host = torch.empty(W.W * W.STATS_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+    st_view = stats_host.numpy().view(W.STATS_DTYPE)
+    W.reset_stats()
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        W.set_state_async(image)
+        W.run(1, sync=False)
+        W.stats_async(st_view)
+        W.synchronize()
+    t_e2e = time.perf_counter() - t0
+    bu_e2e = float(st_view["bead_updates"].sum())
+    t_e2e = max_over_ranks(t_e2e, ws)
+    e2e_val = sum_over_ranks(bu_e2e, ws) / t_e2e
+
+    roof = pair_roofline(pairs, 0.0, t_dev, "k_worm_walkers", measured_fp32_peak(),
+                         clocks.get("sm_mhz"), NCU_TRAFFIC_WORM)
+    roof["note"] += ("; pair evaluations = 2 (N-1) per bead update + M N (N-1)/2 per energy "
+                     "sample, N the walker's target particle number")
+    out = {"metric": "bead-updates/s", "value": value, "unit": "bead-updates/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": warm, "ms_per_step": 1e3 * t_max / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+f64",
            "data": "synthetic",
-           "config": {"workload": "%d worm walkers (one warp each): N~U{8..128}, T~U[1,4] K, tau=0.004, "
-                                  "M even, Aziz, rho=0.02186, primitive action, the reference's full "
-                                  "move list, canonical window 1" % W.W,
-                      "errors": int((st["error"] != 0).sum()),
-                      "closed_samples": int(st["samples"].sum()),
+           "config": {"workload": "batched bosonic walkers: %d He-4 paths, N~U{8..128}, T~U[1,4] K, "
+                                  "tau=0.004, M even, Aziz HFDHE2, rho=0.02186, primitive action, "
+                                  "the reference's default PIMC move list (centre of mass, %s, open, "
+                                  "close, insert, remove, advance/recede head and tail, swap head and "
+                                  "tail), canonical window 1, C0 1, energy sampled at every closed "
+                                  "step; %d staging + COM pre-equilibration steps from the seeded "
+                                  "worldlines, then the warm-up" % (W.W, args.diagonal, PRE_SWEEPS),
+                      "l2": "flushed between timed steps",
+                      "parallelism": "replicas" if ws > 1 else "single",
+                      "walker_errors": errors, "closed_samples": closed,
+                      "pair_evaluations_per_step": pairs / args.steps,
                       "acceptance": {WORM_MOVES[i]: [int(acc[i]), int(att[i])] for i in range(12)}},
-           "gpu_launches": 1, "clocks": clocks}
-    if not args.no_baseline:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import pyoracle
-        from concurrent.futures import ThreadPoolExecutor
+           "e2e": {"value": e2e_val, "unit": "bead-updates/s", "h2d_bytes_per_step": nbytes,
+                   "d2h_bytes_per_step": W.W * W.STATS_DTYPE.itemsize},
+           "gpu_launches": int(launches),
+           "roofline": roof,
+           "clocks": clocks}
+    W.close()
+    if rank == 0 and not args.no_baseline:
         threads = os.cpu_count() or 1
-        idx = list(np.argsort(n)[:: max(1, len(n) // 32)])[:32]
-
-        def one(i):
-            cfg = wl.seeded_worldlines(int(n[i]), int(m[i]), float(L[i]), w["lam"], w["tau"], 100003 + i,
-                                       extent=2 * int(n[i]) + 8)
-            o = pyoracle.Oracle(float(L[i]), int(m[i]), 2 * int(n[i]) + 8, w["tau"], w["lam"])
-            o.load(cfg)
-            mt = pyoracle.MT(7 + i)
-            kw = dict(mbar=int(w["mbar"][i]), temperature=1.0 / (int(m[i]) * w["tau"]),
-                      initial_num_particles=int(n[i]), window=1)
-            t0 = time.perf_counter()
-            r = o.run_worm_steps(mt, 1, **kw)
-            return r["bead_updates"], time.perf_counter() - t0
-
-        t0 = time.perf_counter()
-        with ThreadPoolExecutor(threads) as ex:
-            res = list(ex.map(one, idx))
-        wall = time.perf_counter() - t0
-        bu_c = sum(r[0] for r in res)
-        out["cpu_baseline"] = {"value": bu_c / wall, "unit": "bead-updates/s", "cores": threads,
-                               "kind": "port", "sample": "one worm-algorithm step of %d walkers spread over "
-                               "N, FP64 oracle with MT19937, %d threads, %.1f s" % (len(idx), threads, wall)}
-    print(json.dumps(out))
+        out["cpu_baseline"] = cpu_baseline_worm(w, threads, diagonal_move=dm)
+        out["plain_fp64"] = plain_worm_rate(pgb, diagonal_move=dm)
+        out["plain_fp64"]["batched_over_plain"] = value / out["plain_fp64"]["value"]
+        out["matched_energy"] = matched_energy_worm(pgb, diagonal_move=dm)
+        out["serving"] = serving_run(pgb, seconds=args.serve_seconds, grand_canonical=not args.serve_canonical)
+    if rank == 0:
+        print(json.dumps(out))
 
 
 def run_reference(args):
@@ -862,34 +1080,27 @@ def run_reference(args):
         return
     w = workload(args.walkers)
     threads = os.cpu_count() or 1
-    base = cpu_baseline(w, threads, budget_s=max(5.0, 2.0 * args.steps))
+    dm = DIAGONAL[args.diagonal]
+    base = cpu_baseline_worm(w, threads, nequil=max(3, args.warmup), nsteps=args.steps, diagonal_move=dm)
     line = {"metric": "bead-updates/s", "value": base["value"], "unit": "bead-updates/s",
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "batched walkers: 1024 canonical He-4 chains, "
-                                             "N~U{8..128}, T~U[1,4] K, tau=0.004, Aziz, rho=0.02186",
-                                             "sample": base["sample"]},
+            "data": "synthetic",
+            "config": {"workload": "batched bosonic walkers: %d He-4 paths, N~U{8..128}, T~U[1,4] K, "
+                                   "tau=0.004, Aziz, rho=0.02186, the reference's default PIMC move "
+                                   "list (%s), canonical window 1, C0 1" % (len(w["n"]), args.diagonal),
+                       "sample": base["sample"], "timed": "sweeps only"},
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": "bead-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def main():
-    args = parse()
-    if args.impl == "reference":
-        run_reference(args)
-        return
+def run_canonical(args, pgb, rank, ws):
+    """The canonical staging + centre-of-mass walkers (no exchange moves) on
+    the same 1024 paths: the persistent packed-team kernel with its
+    autotuned schedule."""
     import torch
-    rank, ws = dist_init()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    import pimc_gb300 as pgb
-    if args.workload != "walkers":
-        if rank == 0:
-            {"serving": run_serving, "isf": run_isf, "pair": run_pair,
-             "plain": run_plain, "gp": run_gp, "worm": run_worm}[args.workload](args, pgb)
-        return
-
     w = workload(args.walkers, seed=rank)
     W = pgb.Walkers(w["n"], w["m"], w["temperature"], w["side"], w["mbar"], w["tau"], w["lam"],
                     seed=1000 + rank, threads_per_walker=args.schedule)
@@ -983,9 +1194,26 @@ def main():
         out["plain_fp64"] = plain_form_rate(pgb)
         out["plain_fp64"]["batched_over_plain"] = value / out["plain_fp64"]["value"]
         out["matched_energy"] = matched_energy(pgb, os.cpu_count() or 1)
-        out["serving"] = serving_run(pgb, seconds=args.serve_seconds, grand_canonical=not args.serve_canonical)
     if rank == 0:
         print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    rank, ws = dist_init()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    import pimc_gb300 as pgb
+    if args.workload == "walkers":
+        run_walkers(args, pgb, rank, ws)
+    elif args.workload == "canonical":
+        run_canonical(args, pgb, rank, ws)
+    elif rank == 0:
+        {"serving": run_serving, "isf": run_isf, "pair": run_pair,
+         "plain": run_plain, "gp": run_gp}[args.workload](args, pgb)
 
 
 if __name__ == "__main__":

@@ -222,12 +222,15 @@ void* pgb_stream(pgb_ctx* ctx);   /* the context's cudaStream_t */
  * slice are used; d_qvecs [nq][3]; d_isf [nq][num_slices/2+1], the same values
  * as pgb_isf mode 0 on a PGB_MIXED context.  The densities rho_q(t) go to a
  * static 16 MiB device array held by every GPU that loads the library, so
- * nq * num_slices must not exceed 2^21 (PGB_EINVAL otherwise).  Work is
- * queued on `stream` (a cudaStream_t, NULL for the default stream) and the
- * call returns without waiting.  The first call on a device looks up the
- * array's device address with that device current; make that first call
- * before any stream capture.  Calls share the array: calls that overlap on
- * the GPU race, so order them.  Errors are reported by pgb_last_error(NULL). */
+ * nq * num_slices must not exceed 2^21, num_slices 25600 and num_ptcl 6400
+ * (PGB_EINVAL otherwise, with the limit in the message).  Work is queued on
+ * `stream` (a cudaStream_t, NULL for the default stream) and the call returns
+ * without waiting.  The first call on a device looks up the array's device
+ * address with that device current and caches it; make that first call
+ * before any stream capture, and do not call the entry point on a device
+ * after cudaDeviceReset (the cached address is then stale).  Calls share the
+ * array: calls that overlap on the GPU race, so order them.  Errors are
+ * reported by pgb_last_error(NULL). */
 int pgb_isf_static(const double* d_beads, int num_slices, int num_ptcl,
                    int ptcl_extent, const double side[3], const double* d_qvecs,
                    int nq, double* d_isf, void* stream);
@@ -339,6 +342,8 @@ typedef struct {
     double round_seconds;      /* > 0: every job runs for this much device time per round,
                                   stopping and resuming between moves (sweeps_per_round
                                   then unused); 0: sweeps_per_round as above */
+    int    diagonal_move;      /* worm server: 0 bisection (the reference's default),
+                                  1 staging; unused by the canonical server */
 } pgb_server_params;
 typedef struct {
     int       n;               /* particles N0 */
@@ -474,6 +479,8 @@ typedef struct {
     int           window;          /* canonical window half-width, -1 none */
     uint64_t      seed;
     int           aziz_year;       /* 1979 (default) */
+    int           diagonal_move;   /* 0 bisection (the reference's default), 1 staging */
+    const double* worm_constants;  /* per-walker C0; NULL: worm_constant for every walker */
 } pgb_worm_walkers_params;
 typedef struct {
     double    energy_sum, energy_sumsq;   /* E/N of the closed configurations */
@@ -493,6 +500,29 @@ const char* pgb_worm_walkers_last_error(const pgb_worm_walkers* w);
 int pgb_worm_walkers_load(pgb_worm_walkers* w, int walker, const double* pos);
 /* advance every walker by `sweeps` PIMC steps (synchronous) */
 int pgb_worm_walkers_run(pgb_worm_walkers* w, int sweeps);
+/* the same queued on the walkers' stream, returning without waiting */
+int pgb_worm_walkers_run_async(pgb_worm_walkers* w, int sweeps);
+/* diagonal pre-equilibration (after PathIntegralMonteCarlo::equilStepDiagonal,
+ * pimc.cpp:216-300): `sweeps` steps of centre-of-mass (probability 0.05) and
+ * staging moves only, no worm moves, no energy samples; synchronous */
+int pgb_worm_walkers_equilibrate(pgb_worm_walkers* w, int sweeps);
+int pgb_worm_walkers_synchronize(pgb_worm_walkers* w);
+void* pgb_worm_walkers_stream(pgb_worm_walkers* w);   /* the cudaStream_t */
+long long pgb_worm_walkers_launch_count(pgb_worm_walkers* w);
+/* every walker from seeded closed worldlines made on the device: particle
+ * i's centre uniform in the box, each bead jittered by N(0, 2 lambda tau) per
+ * coordinate, identity links, N beads per slice; the statistics cleared */
+int pgb_worm_walkers_seed(pgb_worm_walkers* w, uint64_t seed);
+/* The whole device state as one host image of pgb_worm_walkers_state_bytes
+ * bytes (positions, links, bead counts, worm records), for checkpoints and
+ * for callers that keep the worldlines on the host between steps.  get waits
+ * for the copy; set_async queues it on the walkers' stream (the image must
+ * stay valid until the stream reaches it; pinned memory for full speed). */
+long long pgb_worm_walkers_state_bytes(pgb_worm_walkers* w);
+int pgb_worm_walkers_get_state(pgb_worm_walkers* w, void* image);
+int pgb_worm_walkers_set_state_async(pgb_worm_walkers* w, const void* image);
+/* statistics copy queued on the walkers' stream (synchronize before reading) */
+int pgb_worm_walkers_stats_async(pgb_worm_walkers* w, pgb_worm_walker_stats* per_walker);
 int pgb_worm_walkers_stats(pgb_worm_walkers* w, pgb_worm_walker_stats* per_walker);
 int pgb_worm_walkers_reset_stats(pgb_worm_walkers* w);
 /* one walker's arrays in the layouts of pgb_load_path ([M][capacity]) */

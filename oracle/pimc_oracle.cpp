@@ -23,6 +23,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <chrono>
 #include <iomanip>
 #include <iostream>
@@ -116,10 +119,16 @@ struct MT {
 // and include/potential.h:963-983 (F, dF, d2F).  Table: potential.h:163-183
 // (r accumulated by r += dr, not k*dr), lookup potential.h:249-260.
 // ---------------------------------------------------------------------------
+struct AzizTables { std::vector<double> V, dV, d2V; };
+
 struct Aziz {
     double rm, A, epsilon, alpha, beta, D, C6, C8, C10;
     double dr = 0; int tableLength = 0;
-    std::vector<double> tV, tdV, td2V;
+    // The tables of one parameter year: entry n is the value at the n-th
+    // point of the r += dr grid, which does not depend on the table's length,
+    // so every system of that year shares the longest table built so far and
+    // reads only its own first tableLength entries.
+    std::shared_ptr<const AzizTables> tab;
     double tailV = 0;
 
     void set_year(int year) {
@@ -204,14 +213,23 @@ struct Aziz {
         dr = (1.0E-6)*rm;
         tableLength = int(maxSep/dr);
         if (build_tables) {
-            tV.assign(tableLength, 0.0); tdV.assign(tableLength, 0.0); td2V.assign(tableLength, 0.0);
-            double r = 0;
-            for (int n = 0; n < tableLength; n++) {
-                tV[n] = valueV(r);
-                tdV[n] = valuedVdr(r);
-                td2V[n] = valued2Vdr2(r);
-                r += dr;
+            static std::mutex mu;
+            static std::map<int, std::shared_ptr<const AzizTables>> cache;
+            std::lock_guard<std::mutex> lk(mu);
+            auto& c = cache[year];
+            if (!c || (int)c->V.size() < tableLength) {
+                auto t = std::make_shared<AzizTables>();
+                t->V.assign(tableLength, 0.0); t->dV.assign(tableLength, 0.0); t->d2V.assign(tableLength, 0.0);
+                double r = 0;
+                for (int n = 0; n < tableLength; n++) {
+                    t->V[n] = valueV(r);
+                    t->dV[n] = valuedVdr(r);
+                    t->d2V[n] = valued2Vdr2(r);
+                    r += dr;
+                }
+                c = t;
             }
+            tab = c;
         }
         // tail correction, potential.cpp:1801-1806
         double rmorc = rm / rc;
@@ -228,13 +246,13 @@ struct Aziz {
         return T[k];
     }
     // AzizPotential::V/gradV/grad2V, potential.h:985-1017
-    double V(const dVec& r) const { return direct(tV, std::sqrt(dot(r, r))); }
+    double V(const dVec& r) const { return direct(tab->V, std::sqrt(dot(r, r))); }
     dVec gradV(const dVec& r) const {
         double rnorm = std::sqrt(dot(r, r));
-        double g = direct(tdV, rnorm) / rnorm;
+        double g = direct(tab->dV, rnorm) / rnorm;
         return {g*r[0], g*r[1], g*r[2]};
     }
-    double grad2V(const dVec& r) const { return direct(td2V, std::sqrt(dot(r, r))); }
+    double grad2V(const dVec& r) const { return direct(tab->d2V, std::sqrt(dot(r, r))); }
 };
 
 enum BeadState { HEADTAIL = 0, SPECIAL = 1, NONE = 2 };
@@ -1103,9 +1121,9 @@ double orc_table_dr(orc_sys* s) { return s->s->pot.dr; }
 double orc_tailV(orc_sys* s) { return s->s->pot.tailV; }
 void orc_copy_tables(orc_sys* s, double* V, double* dV, double* d2V) {
     auto& p = s->s->pot;
-    if (V) std::memcpy(V, p.tV.data(), sizeof(double)*p.tableLength);
-    if (dV) std::memcpy(dV, p.tdV.data(), sizeof(double)*p.tableLength);
-    if (d2V) std::memcpy(d2V, p.td2V.data(), sizeof(double)*p.tableLength);
+    if (V) std::memcpy(V, p.tab->V.data(), sizeof(double)*p.tableLength);
+    if (dV) std::memcpy(dV, p.tab->dV.data(), sizeof(double)*p.tableLength);
+    if (d2V) std::memcpy(d2V, p.tab->d2V.data(), sizeof(double)*p.tableLength);
 }
 double orc_V(orc_sys* s, const double sep[3]) { return s->s->pot.V({sep[0], sep[1], sep[2]}); }
 void orc_gradV(orc_sys* s, const double sep[3], double out[3]) {
@@ -1441,67 +1459,116 @@ int orc_run_steps(orc_sys* h, orc_mt* mt, const orc_move_params* mp, int nsteps,
     return run_steps(h->s, &mt->m, mp, nsteps, trace, trace_cap, energies, stats);
 }
 
+}  // extern "C"
+
+// Seeded closed worldlines (the benchmark inputs): particle i's centre
+// uniform in the box, each bead jittered by N(0, 2 lambda tau) per coordinate
+// and put back in the box, identity permutation, N beads on every slice.
+static void seed_worldlines(Sys* s, MT& mt, int N) {
+    const double sig = std::sqrt(2.0*s->lambda*s->tau);
+    for (int i = 0; i < N; ++i) {
+        dVec c;
+        for (int d = 0; d < 3; ++d) c[d] = s->side[d]*(-0.5 + mt.randExc());
+        for (int t = 0; t < s->M; ++t) {
+            dVec r;
+            for (int d = 0; d < 3; ++d) r[d] = mt.randNorm(c[d], sig);
+            s->putInBC(r);
+            s->setP(t, i, r);
+            size_t k = ((size_t)t*s->Ne + i);
+            s->on[k] = 1;
+            s->nxt[2*k] = (t + 1) % s->M; s->nxt[2*k+1] = i;
+            s->prv[2*k] = (t - 1 + s->M) % s->M; s->prv[2*k+1] = i;
+        }
+    }
+    recount(s);
+}
+
+// setup.cpp:1079-1104 with the free-particle density estimate: Mbar from the
+// interparticle spacing, even, at least 2, at most M/2 when it exceeds M
+static int default_mbar(int N, double L, double lambda, double tau, int M) {
+    double ell = std::pow(1.0*N/(L*L*L), -1.0/3.0);
+    int mbar = int(ell*ell/(16*lambda*tau));
+    if (mbar < 2) mbar = 2; else if (mbar > M) mbar = M/2;
+    if (mbar % 2) mbar++;
+    return mbar;
+}
+
+// Runs `work(w)` for w in order[0 .. W) on nthreads threads, each thread
+// taking the next walker when it finishes one.  Returns wall seconds.
+template <class F>
+static double run_pool(const std::vector<int>& order, int nthreads, F&& work) {
+    std::atomic<int> next(0);
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> th;
+    for (int k = 0; k < nthreads; ++k)
+        th.emplace_back([&]() {
+            for (;;) {
+                int i = next.fetch_add(1);
+                if (i >= (int)order.size()) break;
+                work(order[i]);
+            }
+        });
+    for (auto& x : th) x.join();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Walkers in decreasing N^2 M (largest first keeps the pool's tail short).
+static std::vector<int> largest_first(int W, const int* N, const int* M) {
+    std::vector<int> order(W);
+    for (int w = 0; w < W; ++w) order[w] = w;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return 1.0*N[a]*N[a]*M[a] > 1.0*N[b]*N[b]*M[b];
+    });
+    return order;
+}
+
+extern "C" {
+
 double orc_walkers_cpu(int W, const int* N, const int* M, const double* T,
                        const double* L, const uint32_t* seeds, double tau,
                        double lambda, int nequil, int nsteps, int nthreads,
-                       double* mean_en, long long* bead_updates) {
+                       double* mean_en, long long* bead_updates, double* setup_seconds) {
     if (nthreads < 1) nthreads = 1;
-    std::atomic<int> nextw(0);
-    auto t0 = std::chrono::steady_clock::now();
-    auto work = [&]() {
-        for (;;) {
-            int w = nextw.fetch_add(1);
-            if (w >= W) break;
-            orc_params p{};
-            p.side[0] = p.side[1] = p.side[2] = L[w];
-            p.num_slices = M[w]; p.num_ptcl_ext = N[w];
-            p.tau = tau; p.lambda = lambda; p.rc = L[w];
-            p.vfactor[0] = p.vfactor[1] = 1.0;
-            p.gradvfactor[0] = p.gradvfactor[1] = 0.0;
-            p.aziz_year = 1979; p.virial_window = 5; p.mu = 0.0;
-            Sys* s = make_sys(&p);
-            MT mt(seeds[w]);
-            // seeded worldlines: uniform positions + N(0, 2 lambda tau) jitter,
-            // identity permutation
-            double sig = std::sqrt(2.0*lambda*tau);
-            for (int i = 0; i < N[w]; ++i) {
-                dVec c;
-                for (int d = 0; d < 3; ++d) c[d] = L[w]*(-0.5 + mt.randExc());
-                for (int t = 0; t < M[w]; ++t) {
-                    dVec r;
-                    for (int d = 0; d < 3; ++d) r[d] = mt.randNorm(c[d], sig);
-                    s->putInBC(r);
-                    s->setP(t, i, r);
-                    size_t k = ((size_t)t*s->Ne + i);
-                    s->on[k] = 1;
-                    s->nxt[2*k] = (t + 1) % M[w]; s->nxt[2*k+1] = i;
-                    s->prv[2*k] = (t - 1 + M[w]) % M[w]; s->prv[2*k+1] = i;
-                }
-            }
-            recount(s);
-            orc_move_params mp{};
-            double ell = std::pow(1.0*N[w]/(L[w]*L[w]*L[w]), -1.0/3.0);
-            int mbar = int(ell*ell/(16*lambda*tau));
-            if (mbar < 2) mbar = 2; else if (mbar > M[w]) mbar = M[w]/2;
-            if (mbar % 2) mbar++;
-            mp.mbar = mbar; mp.diagonal_move = 1; mp.var_updates = 1; mp.max_wind = 1;
-            mp.temperature = T[w]; mp.p_com = 0.05; mp.num_updates = 0;
-            std::vector<double> en(nsteps);
-            orc_move_stats st{};
-            if (nequil > 0) run_steps(s, &mt, &mp, nequil, nullptr, 0, nullptr, &st);
-            st = orc_move_stats{};
-            run_steps(s, &mt, &mp, nsteps, nullptr, 0, en.data(), &st);
-            double acc = 0.0;
-            for (double e : en) acc += e;
-            if (mean_en) mean_en[w] = nsteps ? acc / nsteps : 0.0;
-            if (bead_updates) bead_updates[w] = st.bead_updates;
-            delete s;
-        }
-    };
-    std::vector<std::thread> th;
-    for (int k = 0; k < nthreads; ++k) th.emplace_back(work);
-    for (auto& x : th) x.join();
-    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::vector<Sys*> sys(W, nullptr);
+    std::vector<MT> mts;
+    mts.reserve(W);
+    for (int w = 0; w < W; ++w) mts.emplace_back(seeds[w]);
+    std::vector<orc_move_params> mps(W);
+    const std::vector<int> order = largest_first(W, N, M);
+    // set-up, untimed: the system (tables shared), seeded worldlines and the
+    // unsampled steps; PathIntegralMonteCarlo::step (pimc.cpp:724) is the
+    // timed unit, as in the reference's own timing of a run
+    const double t_setup = run_pool(order, nthreads, [&](int w) {
+        orc_params p{};
+        p.side[0] = p.side[1] = p.side[2] = L[w];
+        p.num_slices = M[w]; p.num_ptcl_ext = N[w];
+        p.tau = tau; p.lambda = lambda; p.rc = L[w];
+        p.vfactor[0] = p.vfactor[1] = 1.0;
+        p.gradvfactor[0] = p.gradvfactor[1] = 0.0;
+        p.aziz_year = 1979; p.virial_window = 5; p.mu = 0.0;
+        Sys* s = make_sys(&p);
+        seed_worldlines(s, mts[w], N[w]);
+        orc_move_params& mp = mps[w];
+        mp = orc_move_params{};
+        mp.mbar = default_mbar(N[w], L[w], lambda, tau, M[w]);
+        mp.diagonal_move = 1; mp.var_updates = 1; mp.max_wind = 1;
+        mp.temperature = T[w]; mp.p_com = 0.05; mp.num_updates = 0;
+        orc_move_stats st{};
+        if (nequil > 0) run_steps(s, &mts[w], &mp, nequil, nullptr, 0, nullptr, &st);
+        sys[w] = s;
+    });
+    if (setup_seconds) *setup_seconds = t_setup;
+    const double t_run = run_pool(order, nthreads, [&](int w) {
+        std::vector<double> en(nsteps);
+        orc_move_stats st{};
+        run_steps(sys[w], &mts[w], &mps[w], nsteps, nullptr, 0, en.data(), &st);
+        double acc = 0.0;
+        for (double e : en) acc += e;
+        if (mean_en) mean_en[w] = nsteps ? acc / nsteps : 0.0;
+        if (bead_updates) bead_updates[w] = st.bead_updates;
+    });
+    for (Sys* s : sys) delete s;
+    return t_run;
 }
 
 }  // extern "C"
@@ -1766,6 +1833,75 @@ extern "C" int orc_run_worm_steps(orc_sys* h, orc_mt* mt, const orc_worm_params*
                                   int* nparticles, orc_worm_stats* stats) {
     if (h->s->hash.size() != (size_t)h->s->M) reset_lookup(*h->s);
     return run_worm_steps(h->s, &mt->m, wp, nsteps, trace, trace_cap, energies, nparticles, stats);
+}
+
+// CPU baseline of the device worm walkers: W independent paths run by the
+// worm engine above with the reference's default move list, each its own
+// system (bead extent 2 N + 8 per slice, the walkers' capacity) and
+// MT19937(seeds[w]).  Set-up (system, shared tables, seeded worldlines) and
+// npre diagonal pre-equilibration steps and the first nequil steps are
+// untimed; nsteps steps of every walker are timed (C0[w] the walker's worm
+// constant, NULL for 1)
+// on nthreads threads, walkers taken largest first.  Returns the timed wall
+// seconds; fills per-walker bead updates of the timed steps, the mean E/N
+// over the timed steps that ended diagonal (NaN if none) and the set-up
+// seconds.  A walker whose slice outgrows its extent stops (bead_updates of
+// the steps it made are kept) and is counted in *failed.
+extern "C" double orc_worm_walkers_cpu(int W, const int* N, const int* M, const double* L,
+                                       const int* mbar, const double* C0, const uint32_t* seeds,
+                                       double tau, double lambda, int window, int diagonal_move, int npre, int nequil,
+                                       int nsteps, int nthreads, double* mean_en,
+                                       long long* bead_updates, double* setup_seconds, int* failed) {
+    if (nthreads < 1) nthreads = 1;
+    std::vector<Sys*> sys(W, nullptr);
+    std::vector<MT> mts;
+    mts.reserve(W);
+    for (int w = 0; w < W; ++w) mts.emplace_back(seeds[w]);
+    std::vector<orc_worm_params> wps(W);
+    std::atomic<int> nfail(0);
+    const std::vector<int> order = largest_first(W, N, M);
+    const double t_setup = run_pool(order, nthreads, [&](int w) {
+        orc_params p{};
+        p.side[0] = p.side[1] = p.side[2] = L[w];
+        p.num_slices = M[w]; p.num_ptcl_ext = 2 * N[w] + 8;
+        p.tau = tau; p.lambda = lambda; p.rc = L[w];
+        p.vfactor[0] = p.vfactor[1] = 1.0;
+        p.gradvfactor[0] = p.gradvfactor[1] = 0.0;
+        p.aziz_year = 1979; p.virial_window = 5; p.mu = 0.0;
+        Sys* s = make_sys(&p);
+        seed_worldlines(s, mts[w], N[w]);
+        reset_lookup(*s);
+        orc_worm_params& wp = wps[w];
+        wp = orc_worm_params{};
+        wp.mbar = mbar[w]; wp.diagonal_move = diagonal_move; wp.var_updates = 1; wp.max_wind = 1;
+        wp.temperature = 1.0 / (M[w] * tau); wp.mu = 0.0; wp.worm_constant = C0 ? C0[w] : 1.0;
+        wp.window = window; wp.gaussian_sd = 0.0; wp.num_updates = 0;
+        wp.initial_num_particles = N[w];
+        if (npre > 0) run_diag_steps(s, &mts[w], &wp, npre);
+        if (nequil > 0 && run_worm_steps(s, &mts[w], &wp, nequil, nullptr, 0, nullptr, nullptr, nullptr) < 0) {
+            ++nfail;
+            delete s;
+            s = nullptr;
+        }
+        sys[w] = s;
+    });
+    if (setup_seconds) *setup_seconds = t_setup;
+    const double t_run = run_pool(order, nthreads, [&](int w) {
+        if (bead_updates) bead_updates[w] = 0;
+        if (mean_en) mean_en[w] = std::nan("");
+        if (!sys[w]) return;
+        std::vector<double> en(nsteps);
+        orc_worm_stats st{};
+        if (run_worm_steps(sys[w], &mts[w], &wps[w], nsteps, nullptr, 0, en.data(), nullptr, &st) < 0) ++nfail;
+        double acc = 0.0;
+        int cnt = 0;
+        for (double e : en) if (e == e) { acc += e; ++cnt; }
+        if (mean_en && cnt) mean_en[w] = acc / cnt;
+        if (bead_updates) bead_updates[w] = st.bead_updates;
+    });
+    for (Sys* s : sys) delete s;
+    if (failed) *failed = nfail.load();
+    return t_run;
 }
 
 extern "C" void orc_get_path(orc_sys* h, int32_t* next, int32_t* prev, uint8_t* on, int32_t* worm8,

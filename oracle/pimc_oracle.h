@@ -212,13 +212,27 @@ void orc_get_path(orc_sys* s, int32_t* next, int32_t* prev, uint8_t* on, int32_t
  * MT19937 seed seeds[w]) for nsteps each, on nthreads threads.  Each walker
  * w has N[w] particles, M[w] slices, temperature T[w], box side L[w];
  * initial worldlines are generated by the oracle's lattice-free generator
- * from the same seed.  The first nequil steps are not sampled.  Returns wall
- * seconds; fills per-walker mean E/N over the nsteps sampled steps and the
- * bead-update counts of the sampled steps. */
+ * from the same seed.  Set-up and the first nequil steps are untimed
+ * (*setup_seconds receives their wall time); the nsteps sampled steps of
+ * every walker are timed, walkers taken largest first by the threads.
+ * Returns the timed wall seconds; fills per-walker mean E/N over the nsteps
+ * sampled steps and the bead-update counts of the sampled steps. */
 double orc_walkers_cpu(int W, const int* N, const int* M, const double* T,
                        const double* L, const uint32_t* seeds, double tau,
                        double lambda, int nequil, int nsteps, int nthreads,
-                       double* mean_en, long long* bead_updates);
+                       double* mean_en, long long* bead_updates, double* setup_seconds);
+/* The same for the worm engine (orc_run_worm_steps' move list), bead extent
+ * 2 N + 8 per slice, canonical window `window` (-1: grand canonical at
+ * mu = 0), diagonal_move 1 staging / 0 bisection.  mean_en[w] averages the
+ * timed steps that end diagonal (NaN if none); *failed counts walkers that
+ * outgrew their extent.  C0[w] is walker w's worm constant (NULL: 1).  npre
+ * diagonal pre-equilibration steps (centre of mass with probability 0.05,
+ * else staging) come first, untimed. */
+double orc_worm_walkers_cpu(int W, const int* N, const int* M, const double* L,
+                            const int* mbar, const double* C0, const uint32_t* seeds, double tau,
+                            double lambda, int window, int diagonal_move, int npre, int nequil,
+                            int nsteps, int nthreads, double* mean_en,
+                            long long* bead_updates, double* setup_seconds, int* failed);
 
 #ifdef __cplusplus
 }

@@ -139,7 +139,11 @@ def load():
                                     _DP, C.POINTER(OrcMoveStats)]),
         "orc_walkers_cpu": (C.c_double, [C.c_int, _IP, _IP, _DP, _DP, C.POINTER(C.c_uint32),
                                          C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _DP,
-                                         C.POINTER(C.c_longlong)]),
+                                         C.POINTER(C.c_longlong), _DP]),
+        "orc_worm_walkers_cpu": (C.c_double, [C.c_int, _IP, _IP, _DP, _IP, _DP, C.POINTER(C.c_uint32),
+                                              C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                              C.c_int, C.c_int, C.c_int, _DP, C.POINTER(C.c_longlong),
+                                              _DP, _IP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -474,7 +478,12 @@ def format_state(cfg, rng_words, counts):
     return buf.value.decode()
 
 
-def walkers_cpu(n, m, temperature, side, seeds, tau, lam, nsteps, threads, nequil=0):
+def walkers_cpu(n, m, temperature, side, seeds, tau, lam, nsteps, threads, nequil=0,
+                with_setup=False):
+    """Canonical staging + COM walkers on `threads` host threads.  Returns the
+    wall seconds of the nsteps timed steps (set-up and the nequil unsampled
+    steps excluded), per-walker mean E/N and bead updates of the timed steps,
+    and with with_setup the set-up seconds as a fourth value."""
     lib = load()
     n = np.ascontiguousarray(n, dtype=np.int32)
     m = np.ascontiguousarray(m, dtype=np.int32)
@@ -483,8 +492,39 @@ def walkers_cpu(n, m, temperature, side, seeds, tau, lam, nsteps, threads, nequi
     s = np.ascontiguousarray(seeds, dtype=np.uint32)
     en = np.zeros(len(n))
     bu = np.zeros(len(n), dtype=np.int64)
+    setup = C.c_double()
     sec = lib.orc_walkers_cpu(len(n), _i(n), _i(m), _d(t), _d(L),
                               s.ctypes.data_as(C.POINTER(C.c_uint32)), tau, lam, nequil, nsteps,
                               threads,
-                              _d(en), bu.ctypes.data_as(C.POINTER(C.c_longlong)))
-    return sec, en, bu
+                              _d(en), bu.ctypes.data_as(C.POINTER(C.c_longlong)), C.byref(setup))
+    return (sec, en, bu, setup.value) if with_setup else (sec, en, bu)
+
+
+def worm_walkers_cpu(n, m, side, mbar, seeds, tau, lam, nsteps, threads, nequil=0, window=1,
+                     diagonal_move=0, worm_constant=1.0, npre=0):
+    """Worm-engine walkers (the reference's default move list; diagonal_move 0
+    bisection, 1 staging) on `threads` host threads.  Returns a dict with the
+    timed wall seconds of nsteps steps of every walker, the set-up seconds
+    (system, tables, seeded worldlines and nequil untimed steps), per-walker
+    bead updates and mean E/N over the timed steps that ended diagonal, and
+    the number of walkers that outgrew their bead extent.  npre diagonal
+    pre-equilibration steps (centre of mass and diagonal moves only) come
+    before the nequil steps, untimed."""
+    lib = load()
+    n = np.ascontiguousarray(n, dtype=np.int32)
+    m = np.ascontiguousarray(m, dtype=np.int32)
+    L = np.ascontiguousarray(side, dtype=np.float64)
+    mb = np.ascontiguousarray(mbar, dtype=np.int32)
+    c0 = np.ascontiguousarray(np.broadcast_to(worm_constant, len(n)), dtype=np.float64)
+    s = np.ascontiguousarray(seeds, dtype=np.uint32)
+    en = np.zeros(len(n))
+    bu = np.zeros(len(n), dtype=np.int64)
+    setup = C.c_double()
+    failed = C.c_int()
+    sec = lib.orc_worm_walkers_cpu(len(n), _i(n), _i(m), _d(L), _i(mb), _d(c0),
+                                   s.ctypes.data_as(C.POINTER(C.c_uint32)), tau, lam, window,
+                                   diagonal_move, npre, nequil, nsteps, threads, _d(en),
+                                   bu.ctypes.data_as(C.POINTER(C.c_longlong)), C.byref(setup),
+                                   C.byref(failed))
+    return dict(seconds=sec, setup_seconds=setup.value, bead_updates=bu, energy=en,
+                failed=failed.value)

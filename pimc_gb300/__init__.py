@@ -469,7 +469,9 @@ class WormWalkers:
                             ("error", "<i4"), ("pad", "<i4")])
 
     def __init__(self, n, m, side, mbar, tau, lam, mu=None, capacity=None, worm_constant=1.0,
-                 window=-1, seed=0, aziz_year=1979):
+                 window=-1, seed=0, aziz_year=1979, diagonal_move=0):
+        """diagonal_move: 0 bisection (the reference's default), 1 staging;
+        worm_constant: C0 for every walker, or one per walker."""
         self.lib = _lib.load()
         self.n = np.ascontiguousarray(n, dtype=np.int32)
         self.W = len(self.n)
@@ -488,7 +490,13 @@ class WormWalkers:
         p.mbar = self.mbar.ctypes.data_as(C.POINTER(C.c_int))
         p.capacity = self.capacity.ctypes.data_as(C.POINTER(C.c_int))
         p.tau, p.lambda_, p.worm_constant, p.window, p.seed, p.aziz_year = (
-            tau, lam, worm_constant, window, seed, aziz_year)
+            tau, lam, float(np.ravel(worm_constant)[0]), window, seed, aziz_year)
+        p.diagonal_move = int(diagonal_move)
+        self.diagonal_move = int(diagonal_move)
+        if np.ndim(worm_constant) > 0:
+            self.c0 = np.ascontiguousarray(np.broadcast_to(worm_constant, self.W), dtype=np.float64)
+            p.worm_constants = dptr(self.c0)
+            p.worm_constant = float(self.c0[0])
         h = C.c_void_p()
         rc = self.lib.pgb_worm_walkers_create(C.byref(p), C.byref(h))
         if rc != 0:
@@ -522,8 +530,43 @@ class WormWalkers:
                                        self.tau, seed * 100003 + w)
             self.load(w, cfg["pos"])
 
-    def run(self, sweeps):
-        self._chk(self.lib.pgb_worm_walkers_run(self.h, sweeps))
+    def run(self, sweeps, sync=True):
+        if sync:
+            self._chk(self.lib.pgb_worm_walkers_run(self.h, sweeps))
+        else:
+            self._chk(self.lib.pgb_worm_walkers_run_async(self.h, sweeps))
+
+    def synchronize(self):
+        self._chk(self.lib.pgb_worm_walkers_synchronize(self.h))
+
+    def equilibrate(self, sweeps):
+        """Diagonal pre-equilibration: centre-of-mass and diagonal moves only."""
+        self._chk(self.lib.pgb_worm_walkers_equilibrate(self.h, sweeps))
+
+    def stream(self):
+        return self.lib.pgb_worm_walkers_stream(self.h)
+
+    def launch_count(self):
+        return int(self.lib.pgb_worm_walkers_launch_count(self.h))
+
+    def seed_device(self, seed=0):
+        """Every walker from seeded closed worldlines made on the device."""
+        self._chk(self.lib.pgb_worm_walkers_seed(self.h, seed))
+
+    def state_bytes(self):
+        return int(self.lib.pgb_worm_walkers_state_bytes(self.h))
+
+    def get_state(self, image):
+        """Copy the whole device state into `image` (a writable buffer of
+        state_bytes() bytes, e.g. a pinned tensor's numpy view)."""
+        self._chk(self.lib.pgb_worm_walkers_get_state(self.h, C.c_void_p(image.ctypes.data)))
+
+    def set_state_async(self, image):
+        self._chk(self.lib.pgb_worm_walkers_set_state_async(self.h, C.c_void_p(image.ctypes.data)))
+
+    def stats_async(self, out):
+        self._chk(self.lib.pgb_worm_walkers_stats_async(self.h, C.cast(out.ctypes.data,
+                                                                       C.POINTER(_lib.PgbWormWalkerStats))))
 
     def stats(self):
         out = np.zeros(self.W, dtype=self.STATS_DTYPE)
@@ -555,13 +598,14 @@ class Server:
 
     def __init__(self, hbm_budget_bytes, max_active=1024, sweeps_per_round=10, bin_sweeps=100,
                  tau=0.004, lam=None, p_com=0.05, aziz_year=1979, round_seconds=0.0,
-                 grand_canonical=False):
+                 grand_canonical=False, diagonal_move=0):
         """grand_canonical: every job a device worm walker at its mu
-        (pgb_worm_server_*); otherwise canonical staging + COM chains."""
+        (pgb_worm_server_*), diagonal_move 0 bisection (the reference's
+        default) or 1 staging; otherwise canonical staging + COM chains."""
         self.lib = _lib.load()
         lam = worldlines.LAMBDA_HE4 if lam is None else lam
         p = _lib.PgbServerParams(float(hbm_budget_bytes), max_active, sweeps_per_round, bin_sweeps,
-                                 tau, lam, p_com, aziz_year, float(round_seconds))
+                                 tau, lam, p_com, aziz_year, float(round_seconds), int(diagonal_move))
         self.gc = bool(grand_canonical)
         self.pre = "pgb_worm_server_" if self.gc else "pgb_server_"
         h = C.c_void_p()

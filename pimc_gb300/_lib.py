@@ -59,7 +59,7 @@ class PgbServerParams(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int),
                 ("sweeps_per_round", C.c_int), ("bin_sweeps", C.c_int), ("tau", C.c_double),
                 ("lambda_", C.c_double), ("p_com", C.c_double), ("aziz_year", C.c_int),
-                ("round_seconds", C.c_double)]
+                ("round_seconds", C.c_double), ("diagonal_move", C.c_int)]
 
 
 class PgbGpParams(C.Structure):
@@ -87,7 +87,8 @@ class PgbWormWalkersParams(C.Structure):
                 ("mu", C.POINTER(C.c_double)), ("mbar", C.POINTER(C.c_int)),
                 ("capacity", C.POINTER(C.c_int)), ("tau", C.c_double), ("lambda_", C.c_double),
                 ("worm_constant", C.c_double), ("window", C.c_int), ("seed", C.c_uint64),
-                ("aziz_year", C.c_int)]
+                ("aziz_year", C.c_int), ("diagonal_move", C.c_int),
+                ("worm_constants", C.POINTER(C.c_double))]
 
 
 class PgbWormWalkerStats(C.Structure):
@@ -167,6 +168,16 @@ _SIGS = {
     "pgb_worm_walkers_last_error": (C.c_char_p, [_VP]),
     "pgb_worm_walkers_load": (C.c_int, [_VP, C.c_int, _DP]),
     "pgb_worm_walkers_run": (C.c_int, [_VP, C.c_int]),
+    "pgb_worm_walkers_run_async": (C.c_int, [_VP, C.c_int]),
+    "pgb_worm_walkers_equilibrate": (C.c_int, [_VP, C.c_int]),
+    "pgb_worm_walkers_synchronize": (C.c_int, [_VP]),
+    "pgb_worm_walkers_stream": (_VP, [_VP]),
+    "pgb_worm_walkers_launch_count": (C.c_longlong, [_VP]),
+    "pgb_worm_walkers_seed": (C.c_int, [_VP, C.c_uint64]),
+    "pgb_worm_walkers_state_bytes": (C.c_longlong, [_VP]),
+    "pgb_worm_walkers_get_state": (C.c_int, [_VP, _VP]),
+    "pgb_worm_walkers_set_state_async": (C.c_int, [_VP, _VP]),
+    "pgb_worm_walkers_stats_async": (C.c_int, [_VP, C.POINTER(PgbWormWalkerStats)]),
     "pgb_worm_walkers_stats": (C.c_int, [_VP, C.POINTER(PgbWormWalkerStats)]),
     "pgb_worm_walkers_reset_stats": (C.c_int, [_VP]),
     "pgb_worm_walkers_get_path": (C.c_int, [_VP, C.c_int, _DP, _IP, _IP, C.POINTER(C.c_uint8), _IP]),

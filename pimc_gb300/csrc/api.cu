@@ -4,6 +4,8 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -168,6 +170,21 @@ int compute_terms(Ctx& c, std::vector<double>& h, bool want_tmat) {
 }  // namespace
 
 void pgb::set_global_error(const std::string& msg) { g_last_error = msg; }
+
+cudaError_t pgb::set_smem_limit(const void* func, int bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> done;   // (kernel, device) -> bytes set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = done.find({func, dev});
+    if (it != done.end() && it->second >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    done[{func, dev}] = bytes;
+    return cudaSuccess;
+}
 
 extern "C" {
 

@@ -245,10 +245,9 @@ cudaError_t launch_bead_actions64(const PathView& v, const int2* d_beads, int k,
                                   cudaStream_t s) {
     if (k <= 0) return cudaSuccess;
     size_t smem = (size_t)v.Ne * (3 * sizeof(double) + sizeof(int));
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_bead_actions64, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    {
+        const cudaError_t ae = set_smem_limit(k_bead_actions64, 200 * 1024);
+        if (ae != cudaSuccess) return ae;
     }
     k_bead_actions64<<<k, kBeadBlock, smem, s>>>(v, d_beads, k, shift, mode, tau, lambda,
                                                  vf[0], vf[1], gf[0], gf[1], d_over, d_out);
@@ -398,10 +397,9 @@ k_slice_terms64(PathView v, int window, int want_tmat, double* __restrict__ term
 cudaError_t launch_slice_terms64(const PathView& v, int window, int want_tmat,
                                  double* d_terms, cudaStream_t s) {
     size_t smem = (size_t)v.Ne * 3 * sizeof(double);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_slice_terms64, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    {
+        const cudaError_t ae = set_smem_limit(k_slice_terms64, 200 * 1024);
+        if (ae != cudaSuccess) return ae;
     }
     k_slice_terms64<<<v.M, kSliceBlock, smem, s>>>(v, window, want_tmat, d_terms);
     return cudaGetLastError();

@@ -14,6 +14,12 @@
 // every rho_q(t) entry the correlation later reads.  Calls whose work
 // overlaps on the GPU (two streams, two host threads) race on it, so callers
 // must order their calls.
+//
+// The array's device address is looked up once per device (on the first
+// call made with that device current) and cached for the life of the
+// process.  A cudaDeviceReset, or any other teardown of the device's primary
+// context, invalidates the cached address, so the entry point must not be
+// called on a device after it has been reset.
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -24,6 +30,9 @@ namespace pgb {
 
 // At most nq * M = 2^21 densities per call: 16 MiB per device.
 constexpr long long kStaticRhoMax = 1LL << 21;
+// The correlation keeps one q's M densities in shared memory (8 B each, at
+// most 200 KB), and the density grid has one row of blocks per slice.
+constexpr int kStaticMaxSlices = 25600;
 static __device__ __align__(256) float2 g_static_rho[kStaticRhoMax];
 
 namespace {
@@ -98,8 +107,15 @@ extern "C" int pgb_isf_static(const double* d_beads, int num_slices, int num_ptc
                          " densities (16 MiB); split the q-vectors over several calls");
         return PGB_EINVAL;
     }
+    if (num_slices > kStaticMaxSlices) {
+        set_global_error("isf_static: num_slices = " + std::to_string(num_slices) + " exceeds " +
+                         std::to_string(kStaticMaxSlices) +
+                         " (one q's densities must fit in 200 KB of shared memory)");
+        return PGB_EINVAL;
+    }
     if ((size_t)num_ptcl * (sizeof(float4) + sizeof(int4)) > 200 * 1024) {
-        set_global_error("isf_static: num_ptcl too large for one slice in shared memory");
+        set_global_error("isf_static: num_ptcl = " + std::to_string(num_ptcl) +
+                         " exceeds 6400 (one slice's beads must fit in 200 KB of shared memory)");
         return PGB_EINVAL;
     }
     float2* rho = nullptr;
@@ -109,10 +125,10 @@ extern "C" int pgb_isf_static(const double* d_beads, int num_slices, int num_ptc
         return PGB_ECUDA;
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_rhoq32_aos, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    e = set_smem_limit(k_rhoq32_aos, 200 * 1024);
+    if (e != cudaSuccess) {
+        set_global_error(std::string("isf_static: cudaFuncSetAttribute failed: ") + cudaGetErrorString(e));
+        return PGB_ECUDA;
     }
     dim3 grid((nq + kBlock - 1) / kBlock, num_slices);
     double3 sd = make_double3(side[0], side[1], side[2]);

@@ -404,11 +404,9 @@ cudaError_t launch_isf_tc(const float2* d_rho, int nq, int M, double norm, doubl
     auto* b2h = reinterpret_cast<const __nv_bfloat16*>(tb + T.b2);
     auto* b2l = b2h + (size_t)T.colpad2 * M;
     int* err = reinterpret_cast<int*>(base + L.err);
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_split_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
+    {
+        const cudaError_t ae = set_smem_limit(k_gemm_split_bf16, (int)kSmem);
+        if (ae != cudaSuccess) return ae;
     }
     cudaMemsetAsync(err, 0, sizeof(int), s);
     k_prep_rho<<<152 * 4, 256, 0, s>>>(d_rho, nq, M, L.qpad, a1h, a1l);

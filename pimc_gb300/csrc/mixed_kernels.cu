@@ -195,10 +195,9 @@ cudaError_t launch_bead_actions32(const PathView& v, AzizParams a, const int2* d
     if (k <= 0) return cudaSuccess;
     size_t smem = (size_t)v.Ne * (sizeof(float4) + sizeof(int));
     if (smem > 200 * 1024) return cudaErrorInvalidValue;     // one slice's list in shared memory
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_bead_actions32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    {
+        const cudaError_t ae = set_smem_limit(k_bead_actions32, 200 * 1024);
+        if (ae != cudaSuccess) return ae;
     }
     k_bead_actions32<<<k, kBeadBlock32, smem, s>>>(v, make_aziz_f(a), d_beads, k, shift, mode,
                                                    tau, lambda, vf[0], vf[1], gf[0], gf[1], d_over,
@@ -389,10 +388,9 @@ k_slice_forces32(PathView v, AzizF az, float4* __restrict__ force) {
 cudaError_t launch_slice_forces32(const PathView& v, AzizParams a, float4* d_force, cudaStream_t s) {
     size_t smem = (size_t)v.Ne * sizeof(float4);
     if (smem > 200 * 1024) return cudaErrorInvalidValue;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_slice_forces32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    {
+        const cudaError_t ae = set_smem_limit(k_slice_forces32, 200 * 1024);
+        if (ae != cudaSuccess) return ae;
     }
     k_slice_forces32<<<v.M, kForceBlock, smem, s>>>(v, make_aziz_f(a), d_force);
     return cudaGetLastError();
@@ -507,10 +505,9 @@ k_slice_terms32(PathView v, AzizF az, int window, double* __restrict__ terms) {
 cudaError_t launch_slice_terms32(const PathView& v, AzizParams a, int window, double* d_terms,
                                  cudaStream_t s) {
     size_t smem = (size_t)v.Ne * sizeof(float4);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_slice_terms32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    {
+        const cudaError_t ae = set_smem_limit(k_slice_terms32, 200 * 1024);
+        if (ae != cudaSuccess) return ae;
     }
     k_slice_terms32<<<v.M, kSliceBlock32, smem, s>>>(v, make_aziz_f(a), window, d_terms);
     return cudaGetLastError();

@@ -80,10 +80,9 @@ cudaError_t launch_sep_hist(const PathView& v, int slice, unsigned long long* d_
     const int t0 = slice >= 0 ? slice : 0, nt = slice >= 0 ? 1 : v.M;
     const size_t smem = (size_t)v.Ne * sizeof(float4);
     if (smem > 200 * 1024) return cudaErrorInvalidValue;   // one slice in shared memory
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_sep_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    {
+        const cudaError_t ae = set_smem_limit(k_sep_hist, 200 * 1024);
+        if (ae != cudaSuccess) return ae;
     }
     k_sep_hist<<<nt, kEstBlock, smem, s>>>(v, t0, dSep, d_hist);
     return cudaGetLastError();

@@ -22,6 +22,13 @@ struct AzizParams {
 AzizParams aziz_params(int year);
 // message returned by pgb_last_error(NULL) on this host thread
 void set_global_error(const std::string& msg);
+// Raise func's dynamic shared-memory limit to bytes on the current device.
+// The attribute belongs to the device's context, so it is set once per
+// (kernel, device) pair, under a process-wide lock, and its return code is
+// passed back; a failure is not recorded, so the next call tries again.
+cudaError_t set_smem_limit(const void* func, int bytes);
+template <class F>
+cudaError_t set_smem_limit(F* func, int bytes) { return set_smem_limit(reinterpret_cast<const void*>(func), bytes); }
 
 // Read-only view of one path handed to kernels by value.
 struct PathView {

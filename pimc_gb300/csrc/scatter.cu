@@ -145,10 +145,9 @@ cudaError_t launch_rhoq32(const PathView& v, const double* d_q, int nq, float2* 
     dim3 grid((nq + kRhoBlock - 1) / kRhoBlock, v.M);
     size_t smem = (size_t)v.Ne * (sizeof(float4) + sizeof(int4));
     if (smem > 200 * 1024) return cudaErrorInvalidValue;   // one slice must fit in shared memory
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_rhoq32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    {
+        const cudaError_t ae = set_smem_limit(k_rhoq32, 200 * 1024);
+        if (ae != cudaSuccess) return ae;
     }
     // the wave-vector table sits in the unused half of the rho region, which
     // is sized for FP64 values (16 B per (q, slice)); M is even, so it starts
@@ -232,7 +231,13 @@ cudaError_t launch_isf_direct32(const float2* d_rho, int nq, int M, double norm,
     int threads = (nt + kTauPerThread - 1) / kTauPerThread;
     threads = ((threads + 31) / 32) * 32;
     if (threads > 256) threads = 256;
-    k_isf_direct32<<<nq, threads, (size_t)M * sizeof(float2), s>>>(d_rho, nq, M, norm, d_out);
+    const size_t smem = (size_t)M * sizeof(float2);
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;    // one q's densities in shared memory
+    if (smem > 48 * 1024) {
+        const cudaError_t ae = set_smem_limit(k_isf_direct32, 200 * 1024);
+        if (ae != cudaSuccess) return ae;
+    }
+    k_isf_direct32<<<nq, threads, smem, s>>>(d_rho, nq, M, norm, d_out);
     return cudaGetLastError();
 }
 

@@ -2210,12 +2210,9 @@ cudaError_t launch_run(pgb_walkers* h, int sched, int sweeps, int measure) {
         const int k = 13 + (ppt == 0 ? 0 : ppt == 8 ? 1 : 2);
         cudaError_t e = build_pipe_teams(h, k, 512, ppt, 4);
         if (e != cudaSuccess) return e;
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_walkers_group<512, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            cudaFuncSetAttribute(k_walkers_group<512, 1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            attr = true;
-        }
+        e = set_smem_limit(k_walkers_group<512, 1, 2>, 200 * 1024);
+        if (e == cudaSuccess) e = set_smem_limit(k_walkers_group<512, 1, 4>, 200 * 1024);
+        if (e != cudaSuccess) return e;
         if (sched >= 8000)
             k_walkers_group<512, 1, 4><<<h->team_ctas[k], 512, h->team_smem[k], h->stream>>>(h->d_meta,
                 h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
@@ -2233,12 +2230,9 @@ cudaError_t launch_run(pgb_walkers* h, int sched, int sweeps, int measure) {
         const int k = (ppt == 0) ? (cta == 512 ? 12 : 11) : 7 + (cta == 512 ? 2 : 0) + (ppt == 16 ? 1 : 0);
         cudaError_t e = build_pipe_teams(h, k, cta, ppt);
         if (e != cudaSuccess) return e;
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_walkers_pipe<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-            cudaFuncSetAttribute(k_walkers_pipe<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            attr = true;
-        }
+        e = set_smem_limit(k_walkers_pipe<256, 2>, 100 * 1024);
+        if (e == cudaSuccess) e = set_smem_limit(k_walkers_pipe<512, 1>, 200 * 1024);
+        if (e != cudaSuccess) return e;
         if (cta == 512)
             k_walkers_pipe<512, 1><<<h->team_ctas[k], 512, h->team_smem[k], h->stream>>>(h->d_meta,
                 h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,
@@ -2255,11 +2249,8 @@ cudaError_t launch_run(pgb_walkers* h, int sched, int sweeps, int measure) {
         const int k = 4 + ((ppt == 4) ? 0 : (ppt == 16) ? 2 : 1);
         cudaError_t e = build_tma_teams(h, ppt);
         if (e != cudaSuccess) return e;
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_walkers_tma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-            attr = true;
-        }
+        e = set_smem_limit(k_walkers_tma<2>, 160 * 1024);
+        if (e != cudaSuccess) return e;
         if (h->team_smem[k] > 160 * 1024) return cudaErrorInvalidValue;
         k_walkers_tma<2><<<h->team_ctas[k], kTeamCta, h->team_smem[k], h->stream>>>(h->d_meta,
             h->d_teams[k], h->d_pos, h->d_acc, h->d_ctr, h->d_err, sweeps, measure, af, h->tau,

@@ -60,6 +60,8 @@ namespace pgb {
 struct WWMeta {
     long long off;          // first bead of this walker in the bead arrays
     int M, Ne, N0, mbar;
+    int blev;               // bisection levels b (constants.cpp:116-120)
+    int diag_move;          // diagonal move: 0 bisection (the reference's default), 1 staging
     int num_updates;
     int window;             // canonical window half-width, -1 none
     float L, Linv;
@@ -94,6 +96,9 @@ constexpr int kWWWarps = 1;          // walkers per CTA: one, so the largest wal
 constexpr int kOrigCap = 72;         // saved positions per move (Mbar - 1 <= 63)
 constexpr int kMaxWind = 27;         // (2 maxWind + 1)^3 with maxWind = 1
 constexpr int kChainCap = 1024;      // beads of one move's range cached per walker (M < 1024)
+// A bisection's per-level bead lists are gathered into chain[kListOff ..]: the
+// move's own range holds at most 2^b + 1 <= 65 beads (Mbar <= 64), below it.
+constexpr int kListOff = 512;
 
 // Aziz V with the reference's hard-core branch (potential.cpp:1821-1843):
 // below x = 0.01 the attractive part is dropped
@@ -683,6 +688,98 @@ struct WormWalker {
         return L - 1;
     }
 
+    // BisectionMove (move.cpp:1484-1666), local-action branch: chain[0] is
+    // the start bead, chain[2^l] the end bead, chain[1 .. 2^l - 1] are moved.
+    // Level l (shift s = 2^(l-1)) places the beads at offsets s, 3s, 5s, ...
+    // about the midpoint of their neighbours at -s and +s, which are fixed
+    // ends or beads placed at earlier levels, so the lanes place them
+    // together (deviates in the reference's bead order from normals()).  The
+    // level's action is the list action of those beads at tau() = s tau
+    // (primitive: no correction); level 1 adds the beads of the earlier
+    // levels in their new and old positions; each level is tested against
+    // exp(-dA + dA_previous level) and a rejection restores every bead moved
+    // so far.  Returns the beads proposed, as the oracle counts them.
+    __device__ void gatherStride(int first, int stride, int cnt) {
+        for (int i = lane; i < cnt; i += 32) chain[kListOff + i] = chain[first + stride * i];
+        __syncwarp();
+    }
+    __device__ int bisection(bool& accepted, float4* orig, float4* newp) {
+        accepted = false;
+        if (numBeadsOn == 0) return 0;
+        const int numLevels = 1 + (int)randInt((uint32_t)(m.blev - 1));   // variable length (varUpdates)
+        const int numActive = (1 << numLevels) - 1;
+        if (trueN() == 0) return 0;
+        WB sb;
+        sb.t = (int)randInt((uint32_t)(m.M - 1));
+        if (nb(sb.t) == 0) return 0;
+        sb.p = (int)randInt((uint32_t)(nb(sb.t) - 1));
+        if (numActive > kOrigCap) { err = WERR_LOOP; return 0; }
+        WB b = sb;
+        for (int k = 0; k <= numActive; ++k) {
+            if (b.p >= nb(b.t)) return 0;
+            const WB nx = next(b);
+            if (isXW(nx)) return 0;
+            if (lane == 0) chain[k] = pack(b);
+            b = nx;
+        }
+        if (lane == 0) chain[numActive + 1] = pack(b);
+        __syncwarp();
+        acc->attempted[WM_DIAG]++;
+        saveChain(numActive, orig);                     // orig[j - 1]: bead at offset j
+        const float sgBase = (float)m.sqrtLambdaTau;
+        double oldDelta = 0.0;
+        int moved = 0;
+        for (int level = numLevels; level > 0; --level) {
+            const int s = 1 << (level - 1);
+            const int cnt = 1 << (numLevels - level);  // offsets s (2i + 1), i < cnt
+            gatherStride(s, 2 * s, cnt);
+            double oldA = s * chainAction(kListOff, cnt);
+            normals(3 * cnt, znorm);
+            const float sg = sgBase * sqrtf((float)s);
+            for (int i = lane; i < cnt; i += 32) {
+                const int j = s * (2 * i + 1);
+                const float4 pp = pos[at(chain[j - s])], pn = pos[at(chain[j + s])];
+                // newBisectionPosition (move.cpp:467-488): midpoint of the
+                // neighbours at -s and +s, then a Gaussian kick, then inside
+                const float mx = fmaf(0.5f, min_image32(pn.x - pp.x, m.L, m.Linv), pp.x);
+                const float my = fmaf(0.5f, min_image32(pn.y - pp.y, m.L, m.Linv), pp.y);
+                const float mz = fmaf(0.5f, min_image32(pn.z - pp.z, m.L, m.Linv), pp.z);
+                const float4 q = make_float4(putInBC(fmaf(znorm[3 * i], sg, mx)),
+                                             putInBC(fmaf(znorm[3 * i + 1], sg, my)),
+                                             putInBC(fmaf(znorm[3 * i + 2], sg, mz)), 0.f);
+                newp[j - 1] = q;
+                pos[at(chain[j])] = q;
+            }
+            __syncwarp();
+            moved += cnt;
+            double newA = s * chainAction(kListOff, cnt);
+            if (level == 1 && numActive > 1) {
+                // the beads of the earlier levels: offsets 2, 4, .., numActive - 1
+                const int pc = (numActive - 1) / 2;
+                gatherStride(2, 2, pc);
+                newA += chainAction(kListOff, pc);
+                for (int i = lane; i < pc; i += 32) pos[at(chain[2 * (i + 1)])] = orig[2 * i + 1];
+                __syncwarp();
+                oldA += chainAction(kListOff, pc);
+                for (int i = lane; i < pc; i += 32) pos[at(chain[2 * (i + 1)])] = newp[2 * i + 1];
+                __syncwarp();
+            }
+            const double dA = newA - oldA;
+            if (metro(dA - oldDelta)) {
+                if (level == 1) { accepted = true; acc->accepted[WM_DIAG]++; }
+            } else {
+                // undoMove (move.cpp:1694-1707): every bead moved so far, the
+                // offsets that are multiples of s
+                for (int j = lane + 1; j <= numActive; j += 32)
+                    if (j % s == 0) pos[at(chain[j])] = orig[j - 1];
+                __syncwarp();
+                break;
+            }
+            oldDelta = dA;
+        }
+        return moved;
+    }
+
     // ---- worm moves (move.cpp:1736-3826), local-action branches ----
     __device__ int open() {
         if (numBeadsOn == 0 || trueN() == 0) return -1;
@@ -1259,12 +1356,20 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
                int* __restrict__ prv, int* __restrict__ nbs, const long long* __restrict__ nbs_off,
                WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
                AzizF az, int W, int sweeps, const int* __restrict__ order,
-               const int* __restrict__ limit, unsigned long long budget_ns) {
+               const int* __restrict__ limit, unsigned long long budget_ns, int diag_only) {
     // walker i of this launch is order[i] (all walkers in index order when
     // order is null); limit[w] caps its completed sweeps; with budget_ns > 0
     // a walker stops between two moves (the clock read before each) once that much
-    // device time has passed, and the next launch resumes the sweep there
+    // device time has passed, and the next launch resumes the sweep there.
+    // diag_only: diagonal pre-equilibration in the manner of
+    // PathIntegralMonteCarlo::equilStepDiagonal (pimc.cpp:216-300): only
+    // centre-of-mass and diagonal moves, no worm moves and no energy sample.
+    // Unlike the reference (centre of mass 1 %, the configured diagonal move,
+    // an adaptive centre-of-mass step) it makes 5 % centre-of-mass moves and
+    // staging moves: from seeded worldlines with overlapping particles these
+    // relax in tens of steps where bisection needs hundreds
     __shared__ float4 s_orig[kWWWarps][kOrigCap];
+    __shared__ float4 s_newp[kWWWarps][kOrigCap];
     __shared__ int s_chain[kWWWarps][kChainCap];
     __shared__ float s_norm[kWWWarps][3 * kOrigCap];
     __shared__ double s_cum[kWWWarps][2][WM_N];
@@ -1299,7 +1404,10 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     // one copy per warp in shared memory
     double* cumD = s_cum[warp][0];
     double* cumO = s_cum[warp][1];
-    if (ww.lane == 0) {
+    if (ww.lane == 0 && diag_only) {
+        for (int i = 0; i < WM_N; ++i) cumD[i] = cumO[i] = 1.0 + 1e-7;
+        cumD[WM_COM] = cumO[WM_COM] = 0.05;
+    } else if (ww.lane == 0) {
         const double prob[WM_N] = {0.01, 0.19, 0.4, 0.15, 0.4, 0.15, 0.075, 0.075, 0.075, 0.075, 0.1, 0.1};
         const int onDiag[WM_N] = {1, 1, 1, 0, 1, 0, 0, 0, 0, 0, 0, 0};
         double cd = 0.0, co = 0.0;
@@ -1358,7 +1466,11 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
                 int moved = 0;
                 switch (index) {
                     case WM_COM: moved = ww.com(acc); local.bead_updates += moved; break;
-                    case WM_DIAG: moved = ww.staging(acc, orig); local.bead_updates += moved; break;
+                    case WM_DIAG:
+                        moved = (ww.m.diag_move == 1 || diag_only) ? ww.staging(acc, orig)
+                                                                   : ww.bisection(acc, orig, s_newp[warp]);
+                        local.bead_updates += moved;
+                        break;
                     case WM_OPEN: ww.open(); break;
                     case WM_CLOSE: ww.close(); break;
                     case WM_INSERT: ww.insert(); break;
@@ -1373,7 +1485,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
             }
             if (stopped || ww.err) { u0 = u; break; }
             u0 = 0;
-            if (ww.diag) { eslice = 0; epot = 0.0; ekin = 0.0; }
+            if (ww.diag && !diag_only) { eslice = 0; epot = 0.0; ekin = 0.0; }
         }
         if (eslice >= 0) {
             // the energy sample in chunks of 8 slices, the budget checked
@@ -1473,6 +1585,14 @@ __global__ void k_normals_check(uint2 key, int skip, int count, float* serial, f
 // --------------------------------------------------------------------------
 using namespace pgb;
 
+// bisection levels b of ConstantParameters::initConstants
+// (constants.cpp:116-120): ceil(log2 Mbar), lowered while 2^b >= M
+static int bisection_levels(int mbar, int M) {
+    int b = (int)std::ceil(std::log(1.0 * mbar) / std::log(2.0) - 1.0e-7);
+    while (b > 1 && (1 << b) >= M) --b;
+    return b < 1 ? 1 : b;
+}
+
 struct pgb_worm_walkers {
     int W = 0;
     std::vector<WWMeta> meta;
@@ -1487,6 +1607,7 @@ struct pgb_worm_walkers {
     int* d_order = nullptr;          // walkers by decreasing cost N^2 M: the largest start first
     AzizF az{};
     cudaStream_t stream = nullptr;
+    long long launches = 0;          // kernels this handle has launched
     std::string err;
     int cfail(cudaError_t e, const char* where) {
         err = std::string("CUDA error ") + cudaGetErrorString(e) + " at " + where;
@@ -1543,13 +1664,21 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
         }
         WWMeta m{};
         m.off = off; m.M = M; m.Ne = ne; m.N0 = N; m.mbar = mb;
+        m.blev = bisection_levels(mb, M);
+        m.diag_move = p->diagonal_move == 1 ? 1 : 0;
         int nu = (int)std::ceil(std::max(N, 1) * M / (1.0 * mb));
         m.num_updates = nu < 100 ? 100 : nu;
         m.window = p->window;
         m.L = (float)L; m.Linv = (float)(1.0 / L);
         m.tau = p->tau; m.lambda = p->lambda; m.mu = p->mu ? p->mu[w] : 0.0;
         m.volume = L * L * L;
-        m.C = p->worm_constant / (1.0 * mb * M * m.volume);
+        const double c0 = p->worm_constants ? p->worm_constants[w] : p->worm_constant;
+        if (!(c0 > 0)) {
+            g_wwerr = "worm walker " + std::to_string(w) + ": the worm constant must be positive";
+            pgb_worm_walkers_destroy(h);
+            return PGB_EINVAL;
+        }
+        m.C = c0 / (1.0 * mb * M * m.volume);
         const double rmorc = ap.rm / L;
         const double t2 = ap.C6 * std::pow(rmorc, 3.0) / 3.0, t3 = ap.C8 * std::pow(rmorc, 5.0) / 5.0,
                      t4 = ap.C10 * std::pow(rmorc, 7.0) / 7.0;
@@ -1640,17 +1769,125 @@ int pgb_worm_walkers_load(pgb_worm_walkers* h, int w, const double* pos) {
     return PGB_OK;
 }
 
-int pgb_worm_walkers_run(pgb_worm_walkers* h, int sweeps) {
+static int ww_launch(pgb_worm_walkers* h, int sweeps, int diag_only) {
     if (!h || sweeps < 0) return PGB_EINVAL;
     if (sweeps == 0) return PGB_OK;
     const int blocks = (h->W + kWWWarps - 1) / kWWWarps;
     k_worm_walkers<<<blocks, kWWWarps * 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
                                                            h->d_nbs_off, h->d_state, h->d_stats,
                                                            h->az, h->W, sweeps, h->d_order,
-                                                           nullptr, 0ull);
+                                                           nullptr, 0ull, diag_only);
+    ++h->launches;
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return h->cfail(e, "worm walkers run");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_run_async(pgb_worm_walkers* h, int sweeps) { return ww_launch(h, sweeps, 0); }
+
+int pgb_worm_walkers_equilibrate(pgb_worm_walkers* h, int sweeps) {
+    const int rc = ww_launch(h, sweeps, 1);
+    if (rc != PGB_OK || sweeps == 0) return rc;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "worm walkers equilibrate");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_run(pgb_worm_walkers* h, int sweeps) {
+    const int rc = pgb_worm_walkers_run_async(h, sweeps);
+    if (rc != PGB_OK || sweeps == 0) return rc;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "worm walkers run");
+    return PGB_OK;
+}
+
+void* pgb_worm_walkers_stream(pgb_worm_walkers* h) { return h ? (void*)h->stream : nullptr; }
+
+long long pgb_worm_walkers_launch_count(pgb_worm_walkers* h) { return h ? h->launches : 0; }
+
+int pgb_worm_walkers_seed(pgb_worm_walkers* h, uint64_t seed) {
+    if (!h) return PGB_EINVAL;
+    cudaError_t e = cudaSuccess;
+    std::vector<WWState> st((size_t)h->W);
+    for (int w = 0; w < h->W && e == cudaSuccess; ++w) {
+        const WWMeta& m = h->meta[w];
+        const long long nbe = (long long)m.M * m.Ne;
+        const uint64_t ws = seed * 0x9E3779B97F4A7C15ull + (uint64_t)w * 0xD1B54A32D192ED03ull + 0x8CB92BA72F3D8DD7ull;
+        k_seed_worldlines<<<(unsigned)((nbe + 255) / 256), 256, 0, h->stream>>>(
+            h->d_pos + m.off, h->d_nxt + m.off, h->d_prv + m.off, h->d_nbs + h->nbs_off[w], m.M, m.Ne, m.N0,
+            m.L, (float)m.sqrt2LambdaTau, make_uint2((uint32_t)ws, (uint32_t)(ws >> 32)));
+        ++h->launches;
+        e = cudaGetLastError();
+        WWState& s = st[w];
+        s = WWState{};
+        for (int i = 0; i < 2; ++i) s.head[i] = s.tail[i] = s.sp1[i] = s.sp2[i] = -1;
+        s.gap = -1; s.diag = 1; s.numBeadsOn = m.N0 * m.M;
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_state, st.data(), st.size() * sizeof(WWState), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_stats, 0, h->W * sizeof(pgb_worm_walker_stats), h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "worm walkers seed");
+    return PGB_OK;
+}
+
+// The whole device state as one image: positions (float4 per bead), next and
+// prev links, bead counts per slice, and the per-walker worm records.
+static size_t ww_image_parts(const pgb_worm_walkers* h, size_t part[5]) {
+    part[0] = (size_t)h->total_beads * sizeof(float4);
+    part[1] = part[2] = (size_t)h->total_beads * sizeof(int);
+    part[3] = (size_t)h->total_slices * sizeof(int);
+    part[4] = (size_t)h->W * sizeof(WWState);
+    return part[0] + part[1] + part[2] + part[3] + part[4];
+}
+
+long long pgb_worm_walkers_state_bytes(pgb_worm_walkers* h) {
+    if (!h) return 0;
+    size_t part[5];
+    return (long long)ww_image_parts(h, part);
+}
+
+int pgb_worm_walkers_get_state(pgb_worm_walkers* h, void* image) {
+    if (!h || !image) return PGB_EINVAL;
+    size_t part[5];
+    ww_image_parts(h, part);
+    char* q = static_cast<char*>(image);
+    void* src[5] = {h->d_pos, h->d_nxt, h->d_prv, h->d_nbs, h->d_state};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) {
+        e = cudaMemcpyAsync(q, src[i], part[i], cudaMemcpyDeviceToHost, h->stream);
+        q += part[i];
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "worm walkers get state");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_set_state_async(pgb_worm_walkers* h, const void* image) {
+    if (!h || !image) return PGB_EINVAL;
+    size_t part[5];
+    ww_image_parts(h, part);
+    const char* q = static_cast<const char*>(image);
+    void* dst[5] = {h->d_pos, h->d_nxt, h->d_prv, h->d_nbs, h->d_state};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) {
+        e = cudaMemcpyAsync(dst[i], q, part[i], cudaMemcpyHostToDevice, h->stream);
+        q += part[i];
+    }
+    if (e != cudaSuccess) return h->cfail(e, "worm walkers set state");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_stats_async(pgb_worm_walkers* h, pgb_worm_walker_stats* out) {
+    if (!h || !out) return PGB_EINVAL;
+    cudaError_t e = cudaMemcpyAsync(out, h->d_stats, h->W * sizeof(pgb_worm_walker_stats), cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "worm walker stats");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_synchronize(pgb_worm_walkers* h) {
+    if (!h) return PGB_EINVAL;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cfail(e, "worm walkers synchronize");
     return PGB_OK;
 }
 
@@ -1758,6 +1995,7 @@ struct pgb_worm_server {
     pgb_server_params p{};
     AzizParams ap{};
     AzizF az{};
+    int diag_move = 0;               // 0 bisection, 1 staging
     int max_slots = 0;
     std::vector<int> slot_job, free_slots;
     std::vector<WServerJob> jobs;
@@ -1818,6 +2056,7 @@ int pgb_worm_server_create(const pgb_server_params* p, pgb_worm_server** out) {
     s->p = *p;
     s->ap = aziz_params(p->aziz_year ? p->aziz_year : 1979);
     s->az = make_aziz_f(s->ap);
+    s->diag_move = p->diagonal_move == 1 ? 1 : 0;
     s->max_slots = p->max_active;
     // the budget: bead arrays (24 B a bead), slice counters sized from them
     s->n_beads = (long long)(p->hbm_budget_bytes / 24.0);
@@ -1906,6 +2145,8 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
         s->queue.pop_front();
         WWMeta m{};
         m.off = bo; m.M = job.M; m.Ne = job.Ne; m.N0 = job.N0; m.mbar = job.mbar;
+        m.blev = bisection_levels(job.mbar, job.M);
+        m.diag_move = s->diag_move;
         int nu = (int)std::ceil(std::max(job.N0, 1) * job.M / (1.0 * job.mbar));
         m.num_updates = nu < 100 ? 100 : nu;
         m.window = -1;                        // grand canonical
@@ -1969,7 +2210,7 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
         k_worm_walkers<<<(W + kWWWarps - 1) / kWWWarps, kWWWarps * 32, 0, s->stream>>>(
             s->d_meta, s->d_pos, s->d_nxt, s->d_prv, s->d_nbs, s->d_nbs_off, s->d_state, s->d_stats,
             s->az, W, timed ? (1 << 30) : s->p.sweeps_per_round,
-            s->d_order, s->d_limit, timed ? (unsigned long long)(s->p.round_seconds * 1e9) : 0ull);
+            s->d_order, s->d_limit, timed ? (unsigned long long)(s->p.round_seconds * 1e9) : 0ull, 0);
         if ((e = cudaGetLastError()) != cudaSuccess) return s->cfail(e, "worm server launch");
     }
     std::vector<pgb_worm_walker_stats> st(s->max_slots);

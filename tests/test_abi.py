@@ -78,3 +78,21 @@ def test_qvectors_host_logic_matches_oracle(pgb, oracle_lib):
         a = pgb.qvectors(kind, text, [L, L, L])
         b = oracle_lib.qvectors(kind, text, [L, L, L])
         assert a.shape == b.shape and np.array_equal(a, b), kind
+
+
+def test_isf_static_rejects_sizes_on_the_host(pgb):
+    """The allocation-free F(q,tau) checks its sizes before any CUDA call:
+    too many slices for one q's densities in shared memory, too many
+    particles for one slice, too many densities for the static array.  The
+    pointers are placeholders that the host never dereferences."""
+    lib = pgb._lib.load()
+    side = np.array([9.0, 9.0, 9.0])
+    sp = side.ctypes.data_as(C.POINTER(C.c_double))
+    fake = C.c_void_p(0x1000)
+    assert lib.pgb_isf_static(fake, 25602, 16, 16, sp, fake, 1, fake, None) == -1
+    assert b"num_slices" in lib.pgb_last_error(None)
+    assert lib.pgb_isf_static(fake, 64, 7000, 7000, sp, fake, 1, fake, None) == -1
+    assert b"num_ptcl" in lib.pgb_last_error(None)
+    assert lib.pgb_isf_static(fake, 64, 16, 16, sp, fake, 1 << 16, fake, None) == -1
+    assert b"static scratch limit" in lib.pgb_last_error(None)
+    assert lib.pgb_isf_static(fake, 64, 16, 8, sp, fake, 4, fake, None) == -1   # extent < N

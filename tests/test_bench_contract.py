@@ -29,7 +29,8 @@ def _cpu_env():
 
 
 def test_reference_arm_line():
-    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "1"],
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "1",
+                        "--walkers", "64"],
                        cwd=ROOT, capture_output=True, text=True, timeout=600, env=_cpu_env())
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)
@@ -48,7 +49,8 @@ def test_reference_arm_under_torchrun_prints_once():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port),
-           "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1"]
+           "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1",
+           "--walkers", "64"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=_cpu_env())
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)

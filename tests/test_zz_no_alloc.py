@@ -3,11 +3,13 @@
 It serves callers that may not call cudaMalloc when they measure (device
 memory reserved up front by a pool they do not own, or work allowed only
 after set-up).  The test drives it through the C ABI with device buffers it
-owns and checks two calls in a row against pgb_isf (mode 0, mixed precision)
-on the same worldlines, within the mixed-path tolerance of the other tests
-(2e-4 absolute on F(q,tau) values of order one).  The second call uses fewer
-q-vectors, so a stale density left in the shared static array by the first
-call would show up as a mismatch.
+owns and checks two calls in a row against the oracle's FP64 rho_q form of
+F(q,tau) on the same worldlines, within the mixed-path tolerance of the other
+tests (2e-4 absolute on F(q,tau) values of order one).  The second call uses
+other worldlines and other q-vectors than the first, and more of them, so a
+density left in the shared static array by the first call and read again by
+the second would show up as a mismatch.  The pgb_isf mode 0 value, which the
+entry point is documented to equal, is checked beside the oracle.
 """
 import ctypes as C
 
@@ -21,22 +23,23 @@ pytestmark = pytest.mark.gpu
 TOL = 2e-4
 
 
-def test_isf_static_matches_isf(pgb, oracle_lib):
+def test_isf_static_matches_oracle(pgb, oracle_lib):
     torch = pytest.importorskip("torch")
     lib = pgb._lib.load()
     n, m = 96, 64
     L = pgb.worldlines.box_side(n)
     lam, tau = pgb.worldlines.LAMBDA_HE4, 0.004
-    cfg = pgb.worldlines.seeded_worldlines(n, m, L, lam, tau, 8)
-    a, _ = make_pair(pgb, oracle_lib, cfg, L, m, n, tau, lam, precision=pgb.PGB_MIXED)
-    q, _ = pgb.worldlines.isf_qvectors(L, count=200, seed=3)
-
     dev = torch.device("cuda", 0)
-    d_beads = torch.from_numpy(np.ascontiguousarray(cfg["pos"])).to(dev)
     side = np.array([L, L, L])
-    for nq in (200, 57):                      # two calls in a row on the shared array
-        want = a.isf(q[:nq], mode=0)
-        d_q = torch.from_numpy(np.ascontiguousarray(q[:nq])).to(dev)
+    # two calls in a row on the shared array: different worldlines (seeds 8
+    # and 9), different q-vectors (seeds 3 and 5), the second call larger
+    for cfg_seed, q_seed, nq in ((8, 3, 120), (9, 5, 200)):
+        cfg = pgb.worldlines.seeded_worldlines(n, m, L, lam, tau, cfg_seed)
+        a, o = make_pair(pgb, oracle_lib, cfg, L, m, n, tau, lam, precision=pgb.PGB_MIXED)
+        q, _ = pgb.worldlines.isf_qvectors(L, count=nq, seed=q_seed)
+        want = o.isf_rhoq(q, threads=4)
+        d_beads = torch.from_numpy(np.ascontiguousarray(cfg["pos"])).to(dev)
+        d_q = torch.from_numpy(np.ascontiguousarray(q)).to(dev)
         d_out = torch.full((nq, m // 2 + 1), float("nan"), dtype=torch.float64, device=dev)
         stream = torch.cuda.current_stream(dev).cuda_stream
         rc = lib.pgb_isf_static(C.c_void_p(d_beads.data_ptr()), m, n, n,
@@ -48,6 +51,8 @@ def test_isf_static_matches_isf(pgb, oracle_lib):
         got = d_out.cpu().numpy()
         assert np.all(np.isfinite(got))
         assert np.max(np.abs(got - want)) <= TOL
+        assert np.max(np.abs(got - a.isf(q, mode=0))) <= TOL
+        a.close()
 
     # sizes beyond the static limit are rejected with a message, nothing launched
     big = 1 << 16
