@@ -175,6 +175,16 @@ class Clocks:
                 "samples": len(rows)}
 
 
+def err_stats(got, want, floor=1.0):
+    """Error of a result against the FP64 oracle: max and median of the
+    absolute error and of the relative error |got - want| / max(|want|, floor)."""
+    got, want = np.asarray(got, dtype=float).ravel(), np.asarray(want, dtype=float).ravel()
+    a = np.abs(got - want)
+    r = a / np.maximum(np.abs(want), floor)
+    return {"max_abs": float(a.max()), "median_abs": float(np.median(a)), "max_rel": float(r.max()),
+            "median_rel": float(np.median(r)), "count": int(a.size), "rel_floor": floor}
+
+
 def walker_kernel(sched):
     """Kernel that runs a walker schedule code."""
     if sched >= 7000:
@@ -555,11 +565,18 @@ def run_isf(args, pgb):
                                             "executes more (3 products, DFT then cosine GEMM); peak "
                                             "= MEASURED_PEAKS bf16 burst"},
            "clocks": clocks}
+    # error against the FP64 oracle's rho_q form on 64 of the q-vectors
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    o = pyoracle.Oracle(L, m, n, w["tau"], w["lam"])
+    o.load(cfg)
+    sub_q = np.arange(0, nq, max(1, nq // 64))
+    want = o.isf_rhoq(q[sub_q], threads=os.cpu_count() or 1)
+    out["err_vs_oracle"] = {"tensor_core": err_stats(a.isf(q[sub_q], mode=1), want),
+                            "cuda_core": err_stats(a.isf(q[sub_q], mode=0), want),
+                            "note": "F(q,tau) for %d of the %d q-vectors against the FP64 oracle's "
+                                    "rho_q form; values of order one" % (len(sub_q), nq)}
     if not args.no_baseline:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import pyoracle
-        o = pyoracle.Oracle(L, m, n, w["tau"], w["lam"])
-        o.load(cfg)
         thr = os.cpu_count() or 1
         sub = q[:max(thr * 4, 32)]
         t0 = time.perf_counter()
@@ -651,6 +668,32 @@ def run_pair(args, pgb):
             "reference_equivalent_pairs_per_s": trial_pairs / t_trial,
             "trial_moves_per_s": k / t_trial, "_pv": tp_v, "_pvg": tp_vg, "_t": t_trial}
     clocks = clk.stop()
+    # error of the trial-move action differences against the FP64 oracle on
+    # 256 of the trials (FP64 and mixed device forms, through the C ABI)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    o = pyoracle.Oracle(L, m, n, w["tau"], w["lam"], action="gsf")
+    o.load(cfg)
+    ks = np.arange(0, ntrial, ntrial // 256)[:256]
+    tb = beads[ks]
+    tp = cfg["pos"][tb[:, 0], tb[:, 1]] + disp[ks]
+    tp -= L * np.floor(tp / L + 0.5)
+    want = np.empty(len(ks))
+    for i, (s_, p_) in enumerate(tb):
+        u0 = o.bead_action(int(s_), int(p_))
+        old = cfg["pos"][s_, p_].copy()
+        o.update_bead(int(s_), int(p_), tp[i])
+        want[i] = o.bead_action(int(s_), int(p_)) - u0
+        o.update_bead(int(s_), int(p_), old)
+    err = {}
+    for prec, tag in ((pgb.PGB_FP64, "fp64"), (pgb.PGB_MIXED, "mixed")):
+        a = pgb.Action(L, m, n, w["tau"], w["lam"], action="gsf", precision=prec)
+        a.load(cfg)
+        err[tag] = err_stats(a.trial_actions(tb, tp), want)
+        err[tag + "_full_action"] = err_stats([a.full_action()], [o.full_action()])
+        a.close()
+    err["note"] = ("trial-move action differences dU of 256 of the trials and the full-path action "
+                   "against the FP64 oracle")
     mx = res["mixed"]
     roof = pair_roofline(mx.pop("_pv"), mx.pop("_pvg"), mx.pop("_t"), "k_bead_actions32_full",
                          measured_fp32_peak(), clocks.get("sm_mhz"))
@@ -663,12 +706,8 @@ def run_pair(args, pgb):
            "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
            "config": {"workload": "pair action: N=256, M=250, GSF, rc=L, 10^6 trial displacements "
                                   "uniform in [-0.04 lambda_dB, 0.04 lambda_dB]^3", "results": res},
-           "roofline": roof, "clocks": clocks}
+           "roofline": roof, "clocks": clocks, "err_vs_oracle": err}
     if not args.no_baseline:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import pyoracle
-        o = pyoracle.Oracle(L, m, n, w["tau"], w["lam"], action="gsf")
-        o.load(cfg)
         t0 = time.perf_counter()
         cnt = 0
         while time.perf_counter() - t0 < 5.0:
@@ -842,6 +881,8 @@ def run_gp(args, pgb):
         got = g(pos)
         g.close()
         out["config"]["mixed_max_abs_err_vs_fp64_oracle"] = float(np.max(np.abs(got - want)))
+        out["err_vs_oracle"] = {"mixed": err_stats(got, want), "note": "GP potential at every position "
+                                "of the call against the FP64 oracle"}
         out["cpu_baseline"] = {"value": len(sample) / dt, "unit": "points/s", "cores": threads,
                                "kind": "port", "sample": "%d positions against 16384 training "
                                "points, FP64 oracle, %d threads, %.1f s" % (len(sample), threads, dt)}
@@ -973,6 +1014,31 @@ def matched_energy_worm(pgb, diagonal_move=0, path=None):
     return out
 
 
+def walker_pair_sum_errors(W, w, walkers=8, beads=48, seed=3):
+    """The walkers' FP32 pair sums against the FP64 oracle on the walkers'
+    own current paths: the bare potential action of `beads` active beads of
+    `walkers` walkers spread over N (worm open or closed as the steps left
+    them), through pgb_worm_walkers_bead_actions."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    rng = np.random.default_rng(seed)
+    order = np.argsort(w["n"], kind="stable")
+    picks = order[np.linspace(0, len(order) - 1, walkers).astype(int)]
+    got, want = [], []
+    for i in picks:
+        p = W.path(int(i))
+        o = pyoracle.Oracle(float(w["side"][i]), int(w["m"][i]), int(W.capacity[i]), w["tau"], w["lam"])
+        o.load(p)
+        act = np.argwhere(p["on"])
+        b = act[rng.choice(len(act), size=min(beads, len(act)), replace=False)].astype(np.int32)
+        got.append(W.bead_actions(int(i), b))
+        want.append([o.bead_action(int(t), int(q), mode=1) for t, q in b])
+    return dict(err_stats(np.concatenate(got), np.concatenate(want)),
+                note="bare potential action of %d active beads in each of %d walkers (N %d..%d) by "
+                     "the walkers' FP32 pair sums against the FP64 oracle on the same paths"
+                     % (beads, walkers, int(w["n"][picks].min()), int(w["n"][picks].max())))
+
+
 def run_walkers(args, pgb, rank, ws):
     import torch
     dm = DIAGONAL[args.diagonal]
@@ -1062,6 +1128,8 @@ def run_walkers(args, pgb, rank, ws):
            "gpu_launches": int(launches),
            "roofline": roof,
            "clocks": clocks}
+    if rank == 0:
+        out["err_vs_oracle"] = {"pair_sums": walker_pair_sum_errors(W, w)}
     W.close()
     if rank == 0 and not args.no_baseline:
         threads = os.cpu_count() or 1

@@ -523,6 +523,11 @@ int pgb_worm_walkers_get_state(pgb_worm_walkers* w, void* image);
 int pgb_worm_walkers_set_state_async(pgb_worm_walkers* w, const void* image);
 /* statistics copy queued on the walkers' stream (synchronize before reading) */
 int pgb_worm_walkers_stats_async(pgb_worm_walkers* w, pgb_worm_walker_stats* per_walker);
+/* LocalAction::barePotentialAction (action.cpp:628-645, primitive action) of
+ * beads [k][2] (slice, particle) of walker `walker`'s current path, computed
+ * by the walkers' own FP32 pair sums, for checking them against FP64 */
+int pgb_worm_walkers_bead_actions(pgb_worm_walkers* w, int walker, const int32_t* beads, int k,
+                                  double* out);
 int pgb_worm_walkers_stats(pgb_worm_walkers* w, pgb_worm_walker_stats* per_walker);
 int pgb_worm_walkers_reset_stats(pgb_worm_walkers* w);
 /* one walker's arrays in the layouts of pgb_load_path ([M][capacity]) */

@@ -568,6 +568,14 @@ class WormWalkers:
         self._chk(self.lib.pgb_worm_walkers_stats_async(self.h, C.cast(out.ctypes.data,
                                                                        C.POINTER(_lib.PgbWormWalkerStats))))
 
+    def bead_actions(self, w, beads):
+        """Bare potential action of beads [k][2] of walker w by the walkers'
+        own FP32 pair sums."""
+        beads = np.ascontiguousarray(beads, dtype=np.int32).reshape(-1, 2)
+        out = np.zeros(len(beads))
+        self._chk(self.lib.pgb_worm_walkers_bead_actions(self.h, w, iptr(beads), len(beads), dptr(out)))
+        return out
+
     def stats(self):
         out = np.zeros(self.W, dtype=self.STATS_DTYPE)
         assert out.itemsize == C.sizeof(_lib.PgbWormWalkerStats)

@@ -178,6 +178,7 @@ _SIGS = {
     "pgb_worm_walkers_get_state": (C.c_int, [_VP, _VP]),
     "pgb_worm_walkers_set_state_async": (C.c_int, [_VP, _VP]),
     "pgb_worm_walkers_stats_async": (C.c_int, [_VP, C.POINTER(PgbWormWalkerStats)]),
+    "pgb_worm_walkers_bead_actions": (C.c_int, [_VP, C.c_int, _IP, C.c_int, _DP]),
     "pgb_worm_walkers_stats": (C.c_int, [_VP, C.POINTER(PgbWormWalkerStats)]),
     "pgb_worm_walkers_reset_stats": (C.c_int, [_VP]),
     "pgb_worm_walkers_get_path": (C.c_int, [_VP, C.c_int, _DP, _IP, _IP, C.POINTER(C.c_uint8), _IP]),

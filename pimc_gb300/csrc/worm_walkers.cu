@@ -85,6 +85,7 @@ struct WWState {
 };
 
 struct WB { int t, p; };
+
 __device__ __forceinline__ bool isXW(WB b) { return b.t < 0; }
 __device__ __forceinline__ bool eqW(WB a, WB b) { return a.t == b.t && a.p == b.p; }
 
@@ -92,13 +93,36 @@ enum { WM_COM = 0, WM_DIAG, WM_OPEN, WM_CLOSE, WM_INSERT, WM_REMOVE, WM_AH, WM_R
        WM_SH, WM_ST, WM_N };
 enum { WERR_FULL = 1, WERR_LINK = 2, WERR_LOOP = 3 };
 
-constexpr int kWWWarps = 1;          // walkers per CTA: one, so the largest walkers spread over the SMs
+// A CTA holds kCtaWarps warps: either kCtaWarps small walkers of one warp
+// each, or one large walker (N0 >= kTeamMinN) served by a team of all of them.
+// In a team, warp 0 runs the move logic as a single-warp walker does, and
+// every pair sum (a move's range or bead action) and every energy sample is
+// split over the team's warps: warp 0 posts the job in shared memory, the
+// team meets at a named barrier, each warp sums its share of the partners
+// (or slices), and after a second barrier warp 0 adds the shares in warp
+// order.  A large walker's chain of dependent moves stays on one warp; its
+// pair work, most of its instructions, runs on four.
+constexpr int kCtaWarps = 4;
+constexpr int kTeamMinN = 64;
 constexpr int kOrigCap = 72;         // saved positions per move (Mbar - 1 <= 63)
 constexpr int kMaxWind = 27;         // (2 maxWind + 1)^3 with maxWind = 1
 constexpr int kChainCap = 1024;      // beads of one move's range cached per walker (M < 1024)
 // A bisection's per-level bead lists are gathered into chain[kListOff ..]: the
 // move's own range holds at most 2^b + 1 <= 65 beads (Mbar <= 64), below it.
 constexpr int kListOff = 512;
+
+// the shared-memory mailbox of a team: the posted job and each warp's share
+struct TeamJob {
+    int op;                          // 0 stop, 1 range action, 2 energy sums
+    int a, b;                        // chain offset and count, or slices [a, b)
+    WB head, tail, sp1, sp2;         // the worm state that sets the pair factors
+    float hi[kCtaWarps], lo[kCtaWarps];      // each warp's (double-float) share
+    float khi[kCtaWarps], klo[kCtaWarps];    // each warp's kinetic share (energy)
+    int bad[kCtaWarps];                      // a warp met a locator outside the arrays
+};
+__device__ __forceinline__ void team_sync(int nthreads) {
+    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
 
 // Aziz V with the reference's hard-core branch (potential.cpp:1821-1843):
 // below x = 0.01 the attractive part is dropped
@@ -133,6 +157,9 @@ struct WormWalker {
     int* chain;                      // shared: the beads of the current move's range, packed
     float* znorm;                    // shared: a move's normal deviates, 3 (Mbar - 1) at most
     int lane;
+    int team = 1;                    // warps serving this walker (1, or kCtaWarps for a team)
+    int wk = 0;                      // this warp's place in the team
+    TeamJob* job = nullptr;          // the team's mailbox
     // uniform scalar state
     WB head, tail, sp1, sp2;
     int gap, length, diag, numBeadsOn;
@@ -374,9 +401,77 @@ struct WormWalker {
         if (s1 == 0 && c.head.t != t && c.tail.t != t && c.sp1.t != t && c.sp2.t != t) pairsOf<true>(c, L, s1, k);
         else pairsOf<false>(c, L, s1, k);
     }
+    // One warp's share of a team's range action: beads chain[c0 ..], the
+    // partners j = 32 wk + lane, stepping 32 T.  The next bead's slice
+    // count, position and first partner load while this bead's terms are
+    // summed.  Returns the warp's (double-float) sum; ok false for a locator
+    // outside the walker's arrays.
+    struct TeamLoad { WB b; int n; float4 rb, r0; };
+    __device__ static bool teamLoad(const PairCtx& c, int code, int j0, TeamLoad& L) {
+        L.b = unpack(code);
+        const bool ok = L.b.t < c.M && L.b.p < c.Ne;
+        if (!ok) L.b = WB{0, 0};
+        const float4* row = c.pos + (size_t)L.b.t * c.Ne;
+        L.n = ok ? c.nbs[L.b.t] : 0;
+        L.rb = row[L.b.p];
+        L.r0 = j0 < c.Ne ? row[j0] : L.rb;
+        return ok;
+    }
+    template <bool Plain>
+    __device__ static void teamPairs(const PairCtx& c, const TeamLoad& L, int s1, int j0, int stride, KahanF& k) {
+        pairTerm<Plain>(c, L.b, s1, j0, L.n, L.rb, L.r0, k);
+        const float4* row = c.pos + (size_t)L.b.t * c.Ne;
+        for (int j = j0 + stride; j < L.n; j += stride) pairTerm<Plain>(c, L.b, s1, j, L.n, L.rb, row[j], k);
+    }
+    __device__ __noinline__ static float2 teamShare(const PairCtx& c, const int* ch, int c0, int cnt, int wk, int T,
+                                                    bool& ok) {
+        KahanF k;
+        const int j0 = 32 * wk + c.lane, stride = 32 * T;
+        if (cnt > 0) {
+            TeamLoad cur, nx;
+            ok &= teamLoad(c, ch[c0], j0, cur);
+            for (int i = 0; i < cnt; ++i) {
+                if (i + 1 < cnt) ok &= teamLoad(c, ch[c0 + i + 1], j0, nx);
+                if (cur.b.p < cur.n) {
+                    const int s1 = c.state(cur.b);
+                    const int t = cur.b.t;
+                    if (s1 == 0 && c.head.t != t && c.tail.t != t && c.sp1.t != t && c.sp2.t != t)
+                        teamPairs<true>(c, cur, s1, j0, stride, k);
+                    else
+                        teamPairs<false>(c, cur, s1, j0, stride, k);
+                }
+                cur = nx;
+            }
+        }
+        return warp_ff(k);
+    }
+    // warp 0 of a team: post a job, take its own share, collect the others'
+    __device__ void teamPost(int op, int a, int b) {
+        if (lane == 0) {
+            job->op = op; job->a = a; job->b = b;
+            job->head = head; job->tail = tail; job->sp1 = sp1; job->sp2 = sp2;
+        }
+        team_sync(32 * team);
+    }
+    __device__ double teamCollect(float2 mine, bool ok) {
+        if (lane == 0) { job->hi[0] = mine.x; job->lo[0] = mine.y; job->bad[0] = ok ? 0 : 1; }
+        team_sync(32 * team);
+        double s = 0.0;
+        int bad = 0;
+        for (int q = 0; q < team; ++q) { s += (double)job->hi[q] + (double)job->lo[q]; bad |= job->bad[q]; }
+        if (bad) err = WERR_LINK;
+        return s;
+    }
     // potentialAction over chain[c0 .. c0 + cnt - 1]: the lanes keep one
-    // running sum over the whole range and reduce once
+    // running sum over the whole range and reduce once (a team: each warp
+    // over its share of the partners)
     __device__ __noinline__ double chainAction(int c0, int cnt) {
+        if (team > 1) {
+            teamPost(1, c0, cnt);
+            bool ok = true;
+            const float2 mine = teamShare(pairCtx(), chain, c0, cnt, 0, team, ok);
+            return m.tau * teamCollect(mine, ok);
+        }
         const PairCtx c = pairCtx();
         const int* ch = chain;
         KahanF k;
@@ -467,13 +562,20 @@ struct WormWalker {
         head = nh; tail = nt;
         gap = nt.t - nh.t;
         if (gap < 0) gap += m.M;
+        // Worm::update (worm.cpp:52-101) counts the worm's beads by walking it
+        // from tail to head.  The moves only compare that length with Mbar
+        // (remove needs length <= Mbar; advance tail and recede head need it
+        // above their step, which is at most Mbar), so the walk stops after
+        // Mbar + 1 links and a longer worm counts as Mbar + 1: the same
+        // decisions without chasing up to N M dependent links.
         WB b = nt;
         length = 0;
+        const int cap = m.mbar + 1;
         do {
             ++length;
             b = next(b);
-            if (isXW(b) || length > m.M * m.Ne) { err = WERR_LOOP; break; }
-        } while (!eqW(b, nh));
+            if (isXW(b)) { err = WERR_LOOP; break; }
+        } while (!eqW(b, nh) && length < cap);
         const float4 rt = P(nt), rh = P(nh);
         sep[0] = putInBC(rt.x - rh.x);
         sep[1] = putInBC(rt.y - rh.y);
@@ -1299,11 +1401,32 @@ struct WormWalker {
     // potential of every slice (row i against the partners j > i, four
     // partners a lane at a time without branches) and every bead's squared
     // link to the next slice
+    // (a team: warp wk sums the slices t0 + wk, t0 + wk + T, ..., and warp 0
+    // adds the warps' sums in warp order)
     __device__ __noinline__ double2 energySums(int t0, int t1) {
-        const PairCtx c = pairCtx();
-        const int* nx_ = nxt;
+        if (team > 1) {
+            teamPost(2, t0, t1);
+            float2 p, k;
+            energyShare(pairCtx(), nxt, t0, t1, team, p, k);
+            if (lane == 0) { job->hi[0] = p.x; job->lo[0] = p.y; job->khi[0] = k.x; job->klo[0] = k.y; }
+            team_sync(32 * team);
+            double pot = 0.0, kin = 0.0;
+            for (int q = 0; q < team; ++q) {
+                pot += (double)job->hi[q] + (double)job->lo[q];
+                kin += (double)job->khi[q] + (double)job->klo[q];
+            }
+            return make_double2(pot, kin);
+        }
+        float2 p, k;
+        energyShare(pairCtx(), nxt, t0, t1, 1, p, k);
+        return make_double2((double)p.x + (double)p.y, (double)k.x + (double)k.y);
+    }
+    // the energy sums of slices t0, t0 + step, ... below t1 by one warp:
+    // (pot, kin) as double-float pairs
+    __device__ __noinline__ static void energyShare(const PairCtx& c, const int* nx_, int t0, int t1, int step,
+                                                    float2& pot_out, float2& kin_out) {
         KahanF pot, kin;
-        for (int t = t0; t < t1; ++t) {
+        for (int t = t0; t < t1; t += step) {
             const int n = c.nbs[t];
             const int tn = t + 1 == c.M ? 0 : t + 1;
             const float4* row = c.pos + (size_t)t * c.Ne;
@@ -1338,7 +1461,8 @@ struct WormWalker {
                 }
             }
         }
-        return make_double2(warp_sum_ff(pot), warp_sum_ff(kin));
+        pot_out = warp_ff(pot);
+        kin_out = warp_ff(kin);
     }
     // EnergyEstimator's E/N from the sums over all slices
     __device__ double energyFrom(double V, double K2, int& N) const {
@@ -1351,33 +1475,26 @@ struct WormWalker {
 };
 
 
-__global__ void __launch_bounds__(kWWWarps * 32)
-k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* __restrict__ nxt,
-               int* __restrict__ prv, int* __restrict__ nbs, const long long* __restrict__ nbs_off,
-               WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
-               AzizF az, int W, int sweeps, const int* __restrict__ order,
-               const int* __restrict__ limit, unsigned long long budget_ns, int diag_only) {
-    // walker i of this launch is order[i] (all walkers in index order when
-    // order is null); limit[w] caps its completed sweeps; with budget_ns > 0
-    // a walker stops between two moves (the clock read before each) once that much
-    // device time has passed, and the next launch resumes the sweep there.
-    // diag_only: diagonal pre-equilibration in the manner of
-    // PathIntegralMonteCarlo::equilStepDiagonal (pimc.cpp:216-300): only
-    // centre-of-mass and diagonal moves, no worm moves and no energy sample.
-    // Unlike the reference (centre of mass 1 %, the configured diagonal move,
-    // an adaptive centre-of-mass step) it makes 5 % centre-of-mass moves and
-    // staging moves: from seeded worldlines with overlapping particles these
-    // relax in tens of steps where bisection needs hundreds
-    __shared__ float4 s_orig[kWWWarps][kOrigCap];
-    __shared__ float4 s_newp[kWWWarps][kOrigCap];
-    __shared__ int s_chain[kWWWarps][kChainCap];
-    __shared__ float s_norm[kWWWarps][3 * kOrigCap];
-    __shared__ double s_cum[kWWWarps][2][WM_N];
-
-    const int warp = threadIdx.x >> 5;
-    const int wi = blockIdx.x * kWWWarps + warp;
-    if (wi >= W) return;
-    const int w = order ? order[wi] : wi;
+// One walker's launch: run by the single warp of a small walker, or by warp 0
+// of a team (team > 1, job the team's mailbox).  limit[w] caps the walker's
+// completed sweeps; with budget_ns > 0 a walker stops between two moves (the
+// clock read before each) once that much device time has passed, and the
+// next launch resumes the sweep there.
+//
+// diag_only: diagonal pre-equilibration in the manner of
+// PathIntegralMonteCarlo::equilStepDiagonal (pimc.cpp:216-300): only
+// centre-of-mass and diagonal moves, no worm moves and no energy sample.
+// Unlike the reference (centre of mass 1 %, the configured diagonal move, an
+// adaptive centre-of-mass step) it makes 5 % centre-of-mass moves and
+// staging moves: from seeded worldlines with overlapping particles these
+// relax in tens of steps where bisection needs hundreds.
+__device__ __noinline__ void run_walker(int w, int team, TeamJob* job, const WWMeta* __restrict__ meta,
+                                        float4* __restrict__ pos, int* __restrict__ nxt, int* __restrict__ prv,
+                                        int* __restrict__ nbs, const long long* __restrict__ nbs_off,
+                                        WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
+                                        const AzizF& az, int sweeps, const int* __restrict__ limit,
+                                        unsigned long long budget_ns, int diag_only, float4* s_orig,
+                                        float4* s_newp, int* s_chain, float* s_norm, double* s_cum) {
     WormWalker ww;
     ww.m = meta[w];
     ww.az = az;
@@ -1387,8 +1504,11 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     ww.prv = prv + ww.m.off;
     ww.nbs = nbs + nbs_off[w];
     ww.acc = &stats[w];
-    ww.chain = s_chain[warp];
-    ww.znorm = s_norm[warp];
+    ww.chain = s_chain;
+    ww.znorm = s_norm;
+    ww.team = team;
+    ww.wk = 0;
+    ww.job = job;
     const WWState st = states[w];
     if (st.err) return;
     ww.head = WB{st.head[0], st.head[1]}; ww.tail = WB{st.tail[0], st.tail[1]};
@@ -1402,8 +1522,8 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     ww.acc = &local;
     // cumulative probabilities over the default move list (pimc.cpp:120-152),
     // one copy per warp in shared memory
-    double* cumD = s_cum[warp][0];
-    double* cumO = s_cum[warp][1];
+    double* cumD = s_cum;
+    double* cumO = s_cum + WM_N;
     if (ww.lane == 0 && diag_only) {
         for (int i = 0; i < WM_N; ++i) cumD[i] = cumO[i] = 1.0 + 1e-7;
         cumD[WM_COM] = cumO[WM_COM] = 0.05;
@@ -1421,7 +1541,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
         cumO[WM_N - 1] = 1.0 + 1e-7;
     }
     __syncwarp();
-    float4* orig = s_orig[warp];
+    float4* orig = s_orig;
     const int lim = limit ? min(sweeps, limit[w]) : sweeps;
     const unsigned long long t0 = __shfl_sync(0xffffffffu, gtimer_ns(), 0);
     // the walker's random stream is indexed by (sweep, draw): each sweep
@@ -1468,7 +1588,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
                     case WM_COM: moved = ww.com(acc); local.bead_updates += moved; break;
                     case WM_DIAG:
                         moved = (ww.m.diag_move == 1 || diag_only) ? ww.staging(acc, orig)
-                                                                   : ww.bisection(acc, orig, s_newp[warp]);
+                                                                   : ww.bisection(acc, orig, s_newp);
                         local.bead_updates += moved;
                         break;
                     case WM_OPEN: ww.open(); break;
@@ -1528,6 +1648,78 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     }
 }
 
+
+// the helper warps of a team: take the share that warp 0 posts until it
+// posts the stop
+__device__ __noinline__ void team_helper(int w, int wk, const WWMeta* __restrict__ meta, float4* __restrict__ pos,
+                                         int* __restrict__ nxt, int* __restrict__ nbs,
+                                         const long long* __restrict__ nbs_off, const AzizF& az, int* chain,
+                                         TeamJob* job) {
+    WormWalker ww;
+    ww.m = meta[w];
+    ww.az = az;
+    ww.lane = threadIdx.x & 31;
+    ww.pos = pos + ww.m.off;
+    ww.nxt = nxt + ww.m.off;
+    ww.nbs = nbs + nbs_off[w];
+    ww.chain = chain;
+    for (;;) {
+        team_sync(32 * kCtaWarps);
+        const int op = job->op;
+        if (op == 0) break;
+        ww.head = job->head; ww.tail = job->tail; ww.sp1 = job->sp1; ww.sp2 = job->sp2;
+        const WormWalker::PairCtx c = ww.pairCtx();
+        if (op == 1) {
+            bool ok = true;
+            const float2 r = WormWalker::teamShare(c, chain, job->a, job->b, wk, kCtaWarps, ok);
+            if (ww.lane == 0) { job->hi[wk] = r.x; job->lo[wk] = r.y; job->bad[wk] = ok ? 0 : 1; }
+        } else {
+            float2 p, k;
+            WormWalker::energyShare(c, ww.nxt, job->a + wk, job->b, kCtaWarps, p, k);
+            if (ww.lane == 0) { job->hi[wk] = p.x; job->lo[wk] = p.y; job->khi[wk] = k.x; job->klo[wk] = k.y; }
+        }
+        team_sync(32 * kCtaWarps);
+    }
+}
+
+// plan[4 b .. 4 b + 3] lists the walkers of CTA b: up to four small walkers
+// (-1 for an empty place), or one large walker and kPlanTeam in the second
+// place, served by the CTA's warps as a team
+constexpr int kPlanTeam = -2;
+
+__global__ void __launch_bounds__(kCtaWarps * 32)
+k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* __restrict__ nxt,
+               int* __restrict__ prv, int* __restrict__ nbs, const long long* __restrict__ nbs_off,
+               WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
+               AzizF az, int sweeps, const int* __restrict__ plan, const int* __restrict__ limit,
+               unsigned long long budget_ns, int diag_only) {
+    __shared__ float4 s_orig[kCtaWarps][kOrigCap];
+    __shared__ float4 s_newp[kCtaWarps][kOrigCap];
+    __shared__ int s_chain[kCtaWarps][kChainCap];
+    __shared__ float s_norm[kCtaWarps][3 * kOrigCap];
+    __shared__ double s_cum[kCtaWarps][2 * WM_N];
+    __shared__ TeamJob s_job;
+    const int warp = threadIdx.x >> 5;
+    const int* pl = plan + kCtaWarps * blockIdx.x;
+    if (pl[1] == kPlanTeam) {
+        const int w = pl[0];
+        if (warp == 0) {
+            run_walker(w, kCtaWarps, &s_job, meta, pos, nxt, prv, nbs, nbs_off, states, stats, az, sweeps, limit,
+                       budget_ns, diag_only, s_orig[0], s_newp[0], s_chain[0], s_norm[0], s_cum[0]);
+            // every path out of run_walker ends here: release the helpers
+            if ((threadIdx.x & 31) == 0) s_job.op = 0;
+            team_sync(32 * kCtaWarps);
+        } else {
+            team_helper(w, warp, meta, pos, nxt, nbs, nbs_off, az, s_chain[0], &s_job);
+        }
+        return;
+    }
+    const int w = pl[warp];
+    if (w < 0) return;
+    run_walker(w, 1, nullptr, meta, pos, nxt, prv, nbs, nbs_off, states, stats, az, sweeps, limit, budget_ns,
+               diag_only, s_orig[warp], s_newp[warp], s_chain[warp], s_norm[warp], s_cum[warp]);
+}
+
 // an admitted job's seeded closed worldlines: particle i's centre uniform in
 // the box (Philox block (i, 0)), each of its beads jittered by sigma per
 // coordinate (Box-Muller on block (i, t + 1)) and put back in the box,
@@ -1553,6 +1745,36 @@ __global__ void k_seed_worldlines(float4* __restrict__ pos, int* __restrict__ nx
         prv[k] = -1;
     }
     if (i == 0) nbs[t] = N0;
+}
+
+// one warp: walker w's bare potential action of each listed bead, by the
+// walkers' own pair sums (FP32 terms, Kahan lanes, double-float warp
+// reduction), for checking them against the FP64 oracle on the walker's
+// current path.  A bead that is not active on its slice gives 0 with the
+// worm factors of the walker's worm state, as the moves evaluate it.
+__global__ void k_worm_bead_actions(const WWMeta* __restrict__ meta, float4* pos, int* nxt, int* prv, int* nbs,
+                                    const long long* __restrict__ nbs_off, const WWState* __restrict__ states,
+                                    AzizF az, int w, const int2* __restrict__ beads, int k, double* out) {
+    __shared__ int s_chain[kChainCap];
+    WormWalker ww;
+    ww.m = meta[w];
+    ww.az = az;
+    ww.lane = threadIdx.x & 31;
+    ww.pos = pos + ww.m.off;
+    ww.nxt = nxt + ww.m.off;
+    ww.prv = prv + ww.m.off;
+    ww.nbs = nbs + nbs_off[w];
+    ww.chain = s_chain;
+    const WWState st = states[w];
+    ww.head = WB{st.head[0], st.head[1]}; ww.tail = WB{st.tail[0], st.tail[1]};
+    ww.sp1 = WB{st.sp1[0], st.sp1[1]}; ww.sp2 = WB{st.sp2[0], st.sp2[1]};
+    ww.err = 0;
+    for (int i = 0; i < k; ++i) {
+        const WB b{beads[i].x, beads[i].y};
+        const bool on = ww.valid(b) && b.p < ww.nbs[b.t];
+        const double v = on ? ww.bare(b) : 0.0;
+        if (ww.lane == 0) out[i] = v;
+    }
 }
 
 // one warp: the serial and the lane-parallel normal deviates from the same
@@ -1585,6 +1807,22 @@ __global__ void k_normals_check(uint2 key, int skip, int count, float* serial, f
 // --------------------------------------------------------------------------
 using namespace pgb;
 
+// The CTAs of a launch over walkers listed largest first: a walker of
+// N0 >= kTeamMinN gets a CTA of its own, served as a team; the others share
+// CTAs four to one, in the same order.  A walker's schedule depends only on
+// its own N0, so its chain does not depend on which walkers run beside it.
+static int build_plan(const std::vector<int>& order, const std::vector<WWMeta>& meta, std::vector<int>& plan) {
+    plan.clear();
+    std::vector<int> small;
+    for (int w : order) {
+        if (meta[w].N0 >= kTeamMinN) plan.insert(plan.end(), {w, kPlanTeam, -1, -1});
+        else small.push_back(w);
+    }
+    for (size_t i = 0; i < small.size(); i += kCtaWarps)
+        for (int k = 0; k < kCtaWarps; ++k) plan.push_back(i + k < small.size() ? small[i + k] : -1);
+    return (int)(plan.size() / kCtaWarps);
+}
+
 // bisection levels b of ConstantParameters::initConstants
 // (constants.cpp:116-120): ceil(log2 Mbar), lowered while 2^b >= M
 static int bisection_levels(int mbar, int M) {
@@ -1604,7 +1842,8 @@ struct pgb_worm_walkers {
     long long* d_nbs_off = nullptr;
     WWState* d_state = nullptr;
     pgb_worm_walker_stats* d_stats = nullptr;
-    int* d_order = nullptr;          // walkers by decreasing cost N^2 M: the largest start first
+    int* d_plan = nullptr;           // the launch's CTAs (build_plan), the largest walkers first
+    int n_cta = 0;
     AzizF az{};
     cudaStream_t stream = nullptr;
     long long launches = 0;          // kernels this handle has launched
@@ -1627,7 +1866,7 @@ int pgb_worm_walkers_destroy(pgb_worm_walkers* h) {
     if (!h) return PGB_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->d_meta); cudaFree(h->d_pos); cudaFree(h->d_nxt); cudaFree(h->d_prv); cudaFree(h->d_nbs);
-    cudaFree(h->d_nbs_off); cudaFree(h->d_state); cudaFree(h->d_stats); cudaFree(h->d_order);
+    cudaFree(h->d_nbs_off); cudaFree(h->d_state); cudaFree(h->d_stats); cudaFree(h->d_plan);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return PGB_OK;
@@ -1704,7 +1943,7 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
     if (e == cudaSuccess) e = cudaMalloc(&h->d_nbs_off, h->W * sizeof(long long));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_state, h->W * sizeof(WWState));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_stats, h->W * sizeof(pgb_worm_walker_stats));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_order, h->W * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_plan, (size_t)kCtaWarps * h->W * sizeof(int));
     if (e == cudaSuccess) {
         // the sweep lasts as long as the largest walker needs: start the
         // largest first so that they spread over the SMs
@@ -1715,7 +1954,9 @@ int pgb_worm_walkers_create(const pgb_worm_walkers_params* p, pgb_worm_walkers**
             const double cb = 1.0 * h->meta[b].N0 * h->meta[b].N0 * h->meta[b].M;
             return ca > cb;
         });
-        e = cudaMemcpy(h->d_order, order.data(), h->W * sizeof(int), cudaMemcpyHostToDevice);
+        std::vector<int> plan;
+        h->n_cta = build_plan(order, h->meta, plan);
+        e = cudaMemcpy(h->d_plan, plan.data(), plan.size() * sizeof(int), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMemcpy(h->d_meta, h->meta.data(), h->W * sizeof(WWMeta), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_nbs_off, h->nbs_off.data(), h->W * sizeof(long long), cudaMemcpyHostToDevice);
@@ -1772,11 +2013,9 @@ int pgb_worm_walkers_load(pgb_worm_walkers* h, int w, const double* pos) {
 static int ww_launch(pgb_worm_walkers* h, int sweeps, int diag_only) {
     if (!h || sweeps < 0) return PGB_EINVAL;
     if (sweeps == 0) return PGB_OK;
-    const int blocks = (h->W + kWWWarps - 1) / kWWWarps;
-    k_worm_walkers<<<blocks, kWWWarps * 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
-                                                           h->d_nbs_off, h->d_state, h->d_stats,
-                                                           h->az, h->W, sweeps, h->d_order,
-                                                           nullptr, 0ull, diag_only);
+    k_worm_walkers<<<h->n_cta, kCtaWarps * 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
+                                                               h->d_nbs_off, h->d_state, h->d_stats, h->az,
+                                                               sweeps, h->d_plan, nullptr, 0ull, diag_only);
     ++h->launches;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return h->cfail(e, "worm walkers run");
@@ -1881,6 +2120,34 @@ int pgb_worm_walkers_stats_async(pgb_worm_walkers* h, pgb_worm_walker_stats* out
     if (!h || !out) return PGB_EINVAL;
     cudaError_t e = cudaMemcpyAsync(out, h->d_stats, h->W * sizeof(pgb_worm_walker_stats), cudaMemcpyDeviceToHost, h->stream);
     if (e != cudaSuccess) return h->cfail(e, "worm walker stats");
+    return PGB_OK;
+}
+
+int pgb_worm_walkers_bead_actions(pgb_worm_walkers* h, int w, const int32_t* beads, int k, double* out) {
+    if (!h || w < 0 || w >= h->W || !beads || !out || k < 0) return PGB_EINVAL;
+    if (k == 0) return PGB_OK;
+    const WWMeta& m = h->meta[w];
+    for (int i = 0; i < k; ++i)
+        if (beads[2 * i] < 0 || beads[2 * i] >= m.M || beads[2 * i + 1] < 0 || beads[2 * i + 1] >= m.Ne) {
+            h->err = "worm_walkers_bead_actions: bead outside the walker's arrays";
+            return PGB_EINVAL;
+        }
+    int2* d_b = nullptr;
+    double* d_o = nullptr;
+    cudaError_t e = cudaMalloc(&d_b, k * sizeof(int2));
+    if (e == cudaSuccess) e = cudaMalloc(&d_o, k * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_b, beads, k * sizeof(int2), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        k_worm_bead_actions<<<1, 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
+                                                     h->d_nbs_off, h->d_state, h->az, w, d_b, k, d_o);
+        ++h->launches;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_o, k * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d_b);
+    cudaFree(d_o);
+    if (e != cudaSuccess) return h->cfail(e, "worm walker bead actions");
     return PGB_OK;
 }
 
@@ -2009,10 +2276,11 @@ struct pgb_worm_server {
     WWState* d_state = nullptr;
     pgb_worm_walker_stats* d_stats = nullptr;
     long long* d_nbs_off = nullptr;
-    int *d_order = nullptr, *d_limit = nullptr;
+    int *d_plan = nullptr, *d_limit = nullptr;
     std::vector<WWMeta> h_meta;
     std::vector<long long> h_nbs_off;
     std::vector<int> h_limit;
+    std::vector<int> h_plan;         // the round's CTAs (build_plan)
     cudaStream_t stream = nullptr;
     std::chrono::steady_clock::time_point t0;
     long long bead_updates = 0;
@@ -2034,7 +2302,7 @@ int pgb_worm_server_destroy(pgb_worm_server* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     cudaFree(s->d_pos); cudaFree(s->d_nxt); cudaFree(s->d_prv); cudaFree(s->d_nbs);
     cudaFree(s->d_meta); cudaFree(s->d_state); cudaFree(s->d_stats); cudaFree(s->d_nbs_off);
-    cudaFree(s->d_order); cudaFree(s->d_limit);
+    cudaFree(s->d_plan); cudaFree(s->d_limit);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return PGB_OK;
@@ -2079,7 +2347,7 @@ int pgb_worm_server_create(const pgb_server_params* p, pgb_worm_server** out) {
         if ((e = cudaMalloc(&s->d_state, s->max_slots * sizeof(WWState))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_stats, s->max_slots * sizeof(pgb_worm_walker_stats))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_nbs_off, s->max_slots * sizeof(long long))) != cudaSuccess) break;
-        if ((e = cudaMalloc(&s->d_order, s->max_slots * sizeof(int))) != cudaSuccess) break;
+        if ((e = cudaMalloc(&s->d_plan, (size_t)kCtaWarps * s->max_slots * sizeof(int))) != cudaSuccess) break;
         if ((e = cudaMalloc(&s->d_limit, s->max_slots * sizeof(int))) != cudaSuccess) break;
     } while (0);
     if (e != cudaSuccess) {
@@ -2202,15 +2470,17 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
         return 1.0 * ma.N0 * ma.N0 * ma.M > 1.0 * mb.N0 * mb.N0 * mb.M;
     });
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_limit, s->h_limit.data(), s->max_slots * sizeof(int), cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess && !active.empty()) e = cudaMemcpyAsync(s->d_order, active.data(), active.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream);
+    const int n_cta = active.empty() ? 0 : build_plan(active, s->h_meta, s->h_plan);
+    if (e == cudaSuccess && n_cta > 0)
+        e = cudaMemcpyAsync(s->d_plan, s->h_plan.data(), s->h_plan.size() * sizeof(int), cudaMemcpyHostToDevice,
+                            s->stream);
     if (e != cudaSuccess) return s->cfail(e, "worm server upload");
-    if (!active.empty()) {
-        const int W = (int)active.size();
+    if (n_cta > 0) {
         const bool timed = s->p.round_seconds > 0.0;
-        k_worm_walkers<<<(W + kWWWarps - 1) / kWWWarps, kWWWarps * 32, 0, s->stream>>>(
+        k_worm_walkers<<<n_cta, kCtaWarps * 32, 0, s->stream>>>(
             s->d_meta, s->d_pos, s->d_nxt, s->d_prv, s->d_nbs, s->d_nbs_off, s->d_state, s->d_stats,
-            s->az, W, timed ? (1 << 30) : s->p.sweeps_per_round,
-            s->d_order, s->d_limit, timed ? (unsigned long long)(s->p.round_seconds * 1e9) : 0ull, 0);
+            s->az, timed ? (1 << 30) : s->p.sweeps_per_round,
+            s->d_plan, s->d_limit, timed ? (unsigned long long)(s->p.round_seconds * 1e9) : 0ull, 0);
         if ((e = cudaGetLastError()) != cudaSuccess) return s->cfail(e, "worm server launch");
     }
     std::vector<pgb_worm_walker_stats> st(s->max_slots);

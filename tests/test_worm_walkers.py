@@ -171,3 +171,79 @@ def test_worm_walkers_grand_canonical_match_oracle_statistically(pgb, oracle_lib
     n_w, sn_w = nw.mean(), nw.std(ddof=1) / np.sqrt(len(nw))
     assert abs(n_w - no) <= 4.0 * np.hypot(sn_w, sn_o), (n_w, sn_w, no, sn_o)
     assert abs(e_w - eo) <= 4.0 * np.hypot(se_w, se_o), (e_w, se_w, eo, se_o)
+
+
+@pytest.mark.parametrize("n", [8, 80], ids=["one_warp", "team"])
+def test_walker_pair_sums_match_fp64_oracle(pgb, oracle_lib, n):
+    """The walkers' FP32 pair sums (Kahan lanes, double-float warp reduction)
+    against the FP64 oracle's barePotentialAction on the walkers' own paths
+    after some steps (worm open or closed, special beads set): within 2e-4
+    relative, most of it the oracle's piecewise-constant table (|V'| dr).
+    N = 80 walkers run as four-warp teams."""
+    L = wl.box_side(n)
+    W = pgb.WormWalkers(np.full(8, n), M, L, 8, TAU, LAM, mu=-1.0, window=-1, seed=13)
+    W.seed_device(13)
+    W.equilibrate(10)
+    W.run(30)
+    assert np.all(W.stats()["error"] == 0)
+    rng = np.random.default_rng(2)
+    for w in range(8):
+        p = W.path(w)
+        check_path(p, M)
+        o = oracle_lib.Oracle(L, M, int(W.capacity[w]), TAU, LAM, mu=-1.0)
+        o.load(p)
+        act = np.argwhere(p["on"])
+        beads = act[rng.choice(len(act), size=min(40, len(act)), replace=False)].astype(np.int32)
+        got = W.bead_actions(w, beads)
+        want = np.array([o.bead_action(int(t), int(q), mode=1) for t, q in beads])
+        assert np.max(np.abs(got - want) / np.maximum(np.abs(want), 1.0)) <= 2e-4, w
+
+
+def test_team_walkers_match_oracle_statistically(pgb, oracle_lib):
+    """Walkers of N >= 64 run as four-warp teams (pair sums and energy samples
+    split over the warps): grand canonical at mu = -1 K, N0 = 64, M = 16,
+    <E/N> and <N> over closed configurations within four combined standard
+    errors of the oracle's worm engine; a team walker and the same walker run
+    twice give the same chain."""
+    n, m, tau, mu = 64, 16, 0.01, -1.0
+    L = wl.box_side(n)
+    cfg = wl.seeded_worldlines(n, m, L, LAM, tau, 1, extent=3 * n)
+    kw = dict(mbar=8, temperature=1.0 / (m * tau), initial_num_particles=n, window=-1, mu=mu,
+              diagonal_move=0)
+    es, ns = [], []
+    for seed in range(6):
+        o = oracle_lib.Oracle(L, m, 3 * n, tau, LAM, mu=mu)
+        o.load(cfg)
+        mt = oracle_lib.MT(31 + seed)
+        o.run_steps(mt, 60, mbar=8, temperature=kw["temperature"], diagonal_move=1, p_com=0.05)
+        o.run_worm_steps(mt, 100, **kw)
+        r = o.run_worm_steps(mt, 500, **kw)
+        ok = ~np.isnan(r["energies"])
+        if ok.sum() > 20:
+            es.append(r["energies"][ok].mean())
+            ns.append(r["num_particles"][ok].mean())
+    assert len(es) >= 4
+    eo, se_o = np.mean(es), np.std(es, ddof=1) / np.sqrt(len(es))
+    no, sn_o = np.mean(ns), np.std(ns, ddof=1) / np.sqrt(len(ns))
+
+    runs = []
+    for _ in range(2):
+        W = pgb.WormWalkers(np.full(64, n), m, L, 8, tau, LAM, mu=mu, window=-1, seed=7)
+        W.seed_device(7)
+        W.equilibrate(60)
+        W.run(100)
+        W.reset_stats()
+        W.run(300)
+        runs.append((W.stats(), W.path(5)))
+    (st, p0), (st1, p1) = runs
+    assert np.array_equal(st["energy_sum"], st1["energy_sum"])
+    assert np.array_equal(p0["pos"], p1["pos"]) and np.array_equal(p0["next"], p1["next"])
+    assert np.all(st["error"] == 0)
+    check_path(p0, m)
+    has = st["samples"] > 20
+    ew = st["energy_sum"][has] / st["samples"][has]
+    nw = st["n_sum"][has] / st["samples"][has]
+    e_w, se_w = ew.mean(), ew.std(ddof=1) / np.sqrt(len(ew))
+    n_w, sn_w = nw.mean(), nw.std(ddof=1) / np.sqrt(len(nw))
+    assert abs(e_w - eo) <= 4.0 * np.hypot(se_w, se_o), (e_w, se_w, eo, se_o)
+    assert abs(n_w - no) <= 4.0 * np.hypot(sn_w, sn_o), (n_w, sn_w, no, sn_o)
