@@ -266,30 +266,26 @@ def measured_fp32_peak():
     return 2.0 * n ** 3 / best / 1e12
 
 
-def cpu_baseline(w, threads, budget_s=15.0):
-    """Oracle walkers (FP64, MT19937, reference staging with winding sampling)
-    on a stratified sample of the workload's walkers, all host threads."""
+def cpu_baseline(w, threads, nequil=1, nsteps=5, every=4):
+    """Oracle walkers (FP64, MT19937, the reference's staging with winding
+    sampling and centre-of-mass moves) on a stratified quarter of the
+    workload's walkers (every 4th by N^2 M), all host threads: set-up and
+    nequil steps untimed, nsteps steps of every sampled walker timed."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
-    order = np.argsort(w["n"].astype(float) ** 2 * w["m"])
-    idx = order[np.linspace(0, len(order) - 1, num=min(len(order), max(threads, 16))).astype(int)]
+    order = np.argsort(w["n"].astype(float) ** 2 * w["m"], kind="stable")
+    idx = np.sort(order[::every])
     sel = {k: (v[idx] if isinstance(v, np.ndarray) else v) for k, v in w.items()}
     seeds = np.arange(len(idx), dtype=np.uint32) + 139853
-    # one sweep per walker; repeat while within the budget
-    total_bu, total_s, reps = 0, 0.0, 0
-    while total_s < budget_s and reps < 4:
-        sec, en, bu = pyoracle.walkers_cpu(sel["n"], sel["m"], sel["temperature"], sel["side"], seeds,
-                                           w["tau"], w["lam"], 1, threads)
-        total_bu += int(bu.sum())
-        total_s += sec
-        reps += 1
-    # per-bead-update cost of the sample scaled to the whole workload's mix
-    rate = total_bu / total_s
-    return dict(value=rate, unit="bead-updates/s", cores=threads, kind="port",
-                sample="%d walkers stratified by N^2 M (N %d..%d), %d sweep(s) each from fresh "
-                       "seeded worldlines, FP64 oracle with MT19937, %d threads"
-                       % (len(idx), int(sel["n"].min()), int(sel["n"].max()), reps, threads))
+    sec, en, bu, setup = pyoracle.walkers_cpu(sel["n"], sel["m"], sel["temperature"], sel["side"], seeds,
+                                              w["tau"], w["lam"], nsteps, threads, nequil=nequil,
+                                              with_setup=True)
+    return dict(value=float(bu.sum()) / sec, unit="bead-updates/s", cores=threads, kind="port",
+                timed="sweeps only",
+                sample="%d of the %d walkers (every %d-th by N^2 M), %d timed sweep(s) each after %d "
+                       "untimed (set-up %.1f s untimed), FP64 oracle with MT19937, %d threads, %.1f s timed"
+                       % (len(idx), len(w["n"]), every, nsteps, nequil, setup, threads, sec))
 
 
 def plain_form_rate(pgb, n=64, t=2.0, tau=0.004, steps=1):

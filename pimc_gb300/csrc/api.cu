@@ -171,6 +171,21 @@ int compute_terms(Ctx& c, std::vector<double>& h, bool want_tmat) {
 
 void pgb::set_global_error(const std::string& msg) { g_last_error = msg; }
 
+cudaError_t pgb::set_carveout(const void* func, int percent) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> done;   // (kernel, device) -> percent set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = done.find({func, dev});
+    if (it != done.end() && it->second == percent) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout, percent);
+    if (e != cudaSuccess) return e;
+    done[{func, dev}] = percent;
+    return cudaSuccess;
+}
+
 cudaError_t pgb::set_smem_limit(const void* func, int bytes) {
     static std::mutex mu;
     static std::map<std::pair<const void*, int>, int> done;   // (kernel, device) -> bytes set

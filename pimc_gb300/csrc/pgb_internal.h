@@ -29,6 +29,11 @@ void set_global_error(const std::string& msg);
 cudaError_t set_smem_limit(const void* func, int bytes);
 template <class F>
 cudaError_t set_smem_limit(F* func, int bytes) { return set_smem_limit(reinterpret_cast<const void*>(func), bytes); }
+// Prefer a shared-memory carveout of `percent` (0..100) of the SM's unified
+// L1/shared storage for func on the current device, once per (kernel, device)
+cudaError_t set_carveout(const void* func, int percent);
+template <class F>
+cudaError_t set_carveout(F* func, int percent) { return set_carveout(reinterpret_cast<const void*>(func), percent); }
 
 // Read-only view of one path handed to kernels by value.
 struct PathView {

@@ -258,18 +258,24 @@ struct WormWalker {
     }
 
     // ---- path access ----
+    // Positions are slice-major ([M][Ne]: a slice's beads contiguous, for the
+    // pair sums); links are particle-major ([Ne][M]: one particle index's
+    // beads contiguous), so that a walk along a worldline, which mostly keeps
+    // its particle index from slice to slice, reads one cache line every 32
+    // links instead of one line every link.
     __device__ size_t li(WB b) const { return (size_t)b.t * m.Ne + b.p; }
+    __device__ size_t lk(WB b) const { return (size_t)b.p * m.M + b.t; }
     __device__ bool valid(WB b) const { return b.t >= 0 && b.t < m.M && b.p >= 0 && b.p < m.Ne; }
     __device__ WB next(WB b) {
         if (!valid(b)) { err = WERR_LINK; return {-1, -1}; }
-        const int p = nxt[li(b)];
+        const int p = nxt[lk(b)];
         if (p < 0) return {-1, -1};
         if (p >= m.Ne) { err = WERR_LINK; return {-1, -1}; }
         return {b.t + 1 == m.M ? 0 : b.t + 1, p};
     }
     __device__ WB prev(WB b) {
         if (!valid(b)) { err = WERR_LINK; return {-1, -1}; }
-        const int p = prv[li(b)];
+        const int p = prv[lk(b)];
         if (p < 0) return {-1, -1};
         if (p >= m.Ne) { err = WERR_LINK; return {-1, -1}; }
         return {b.t == 0 ? m.M - 1 : b.t - 1, p};
@@ -290,12 +296,12 @@ struct WormWalker {
     // links: the partner's particle index (slice implied)
     __device__ void setNext(WB b, WB v) {
         if (!valid(b)) { err = WERR_LINK; return; }
-        if (lane == 0) nxt[li(b)] = isXW(v) ? -1 : v.p;
+        if (lane == 0) nxt[lk(b)] = isXW(v) ? -1 : v.p;
         __syncwarp();
     }
     __device__ void setPrev(WB b, WB v) {
         if (!valid(b)) { err = WERR_LINK; return; }
-        if (lane == 0) prv[li(b)] = isXW(v) ? -1 : v.p;
+        if (lane == 0) prv[lk(b)] = isXW(v) ? -1 : v.p;
         __syncwarp();
     }
     __device__ int nb(int t) const { return nbs[t]; }
@@ -1431,7 +1437,7 @@ struct WormWalker {
             const int tn = t + 1 == c.M ? 0 : t + 1;
             const float4* row = c.pos + (size_t)t * c.Ne;
             for (int i = c.lane; i < n; i += 32) {
-                const int pn = nx_[(size_t)t * c.Ne + i];
+                const int pn = nx_[(size_t)i * c.M + t];
                 if (pn >= 0 && pn < c.Ne) {
                     const float4 ri = row[i], rn = c.pos[(size_t)tn * c.Ne + pn];
                     const float vx = min_image32(rn.x - ri.x, c.L, c.Linv);
@@ -1737,12 +1743,12 @@ __global__ void k_seed_worldlines(float4* __restrict__ pos, int* __restrict__ nx
                       L * (u01f(c.z) - 0.5f) + sigma * n23.x};
         for (int d = 0; d < 3; ++d) r[d] -= L * floorf(r[d] / L + 0.5f);
         pos[k] = make_float4(r[0], r[1], r[2], 0.f);
-        nxt[k] = i;
-        prv[k] = i;
+        nxt[(size_t)i * M + t] = i;          // links particle-major
+        prv[(size_t)i * M + t] = i;
     } else {
         pos[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        nxt[k] = -1;
-        prv[k] = -1;
+        nxt[(size_t)i * M + t] = -1;
+        prv[(size_t)i * M + t] = -1;
     }
     if (i == 0) nbs[t] = N0;
 }
@@ -1994,8 +2000,8 @@ int pgb_worm_walkers_load(pgb_worm_walkers* h, int w, const double* pos) {
         for (int i = 0; i < N; ++i) {
             const double* r = pos + ((size_t)t * N + i) * 3;
             p[(size_t)t * ne + i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
-            nx[(size_t)t * ne + i] = i;
-            pv[(size_t)t * ne + i] = i;
+            nx[(size_t)i * M + t] = i;                 // links particle-major
+            pv[(size_t)i * M + t] = i;
         }
     WWState s{};
     for (int i = 0; i < 2; ++i) s.head[i] = s.tail[i] = s.sp1[i] = s.sp2[i] = -1;
@@ -2010,9 +2016,22 @@ int pgb_worm_walkers_load(pgb_worm_walkers* h, int w, const double* pos) {
     return PGB_OK;
 }
 
+// The walkers' state lives in local memory around the helpers that are not
+// inlined, and a large walker's positions (up to a megabyte) and links stream
+// through L1, so the kernel trades shared memory for L1: a carveout of 25 %
+// (two 30 KB CTAs an SM) measured fastest on the 1024-walker workload (27 ms
+// a step against 31 ms at 50 %, 35 ms at the smallest that fits one CTA,
+// 45 ms at 100 %).
+constexpr int kWWCarveoutPercent = 25;
+static cudaError_t ww_prefer_l1() { return set_carveout(k_worm_walkers, kWWCarveoutPercent); }
+
 static int ww_launch(pgb_worm_walkers* h, int sweeps, int diag_only) {
     if (!h || sweeps < 0) return PGB_EINVAL;
     if (sweeps == 0) return PGB_OK;
+    {
+        const cudaError_t ce = ww_prefer_l1();
+        if (ce != cudaSuccess) return h->cfail(ce, "worm walkers carveout");
+    }
     k_worm_walkers<<<h->n_cta, kCtaWarps * 32, 0, h->stream>>>(h->d_meta, h->d_pos, h->d_nxt, h->d_prv, h->d_nbs,
                                                                h->d_nbs_off, h->d_state, h->d_stats, h->az,
                                                                sweeps, h->d_plan, nullptr, 0ull, diag_only);
@@ -2198,8 +2217,9 @@ int pgb_worm_walkers_get_path(pgb_worm_walkers* h, int w, double* pos, int32_t* 
             const bool act = q < nb[t];
             on[j] = act ? 1 : 0;
             const int tn = t + 1 == M ? 0 : t + 1, tp = t == 0 ? M - 1 : t - 1;
-            next[2 * j] = (act && nx[j] >= 0) ? tn : -1; next[2 * j + 1] = (act && nx[j] >= 0) ? nx[j] : -1;
-            prev[2 * j] = (act && pv[j] >= 0) ? tp : -1; prev[2 * j + 1] = (act && pv[j] >= 0) ? pv[j] : -1;
+            const size_t k = (size_t)q * M + t;        // links particle-major
+            next[2 * j] = (act && nx[k] >= 0) ? tn : -1; next[2 * j + 1] = (act && nx[k] >= 0) ? nx[k] : -1;
+            prev[2 * j] = (act && pv[k] >= 0) ? tp : -1; prev[2 * j + 1] = (act && pv[k] >= 0) ? pv[k] : -1;
         }
     const int wv[8] = {s.head[0], s.head[1], s.tail[0], s.tail[1], s.sp1[0], s.sp1[1], s.sp2[0], s.sp2[1]};
     for (int i = 0; i < 8; ++i) worm8[i] = wv[i];
@@ -2477,6 +2497,7 @@ int pgb_worm_server_step(pgb_worm_server* s, int* n_active, int* n_queued) {
     if (e != cudaSuccess) return s->cfail(e, "worm server upload");
     if (n_cta > 0) {
         const bool timed = s->p.round_seconds > 0.0;
+        if ((e = ww_prefer_l1()) != cudaSuccess) return s->cfail(e, "worm server carveout");
         k_worm_walkers<<<n_cta, kCtaWarps * 32, 0, s->stream>>>(
             s->d_meta, s->d_pos, s->d_nxt, s->d_prv, s->d_nbs, s->d_nbs_off, s->d_state, s->d_stats,
             s->az, timed ? (1 << 30) : s->p.sweeps_per_round,
