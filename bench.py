@@ -355,12 +355,14 @@ def matched_energy(pgb, threads, n=64, t=2.0, tau=0.004, replicas=256, equil=100
 # load far exceeds capacity, so the window is bounded and the report states
 # how many jobs reached a first bin / completed (the rest are censored).
 # ---------------------------------------------------------------------------
-def km_quantiles(durations, observed, qs=(50, 99)):
+def km_quantiles(durations, observed, qs=(50, 99), with_risk=False):
     """Kaplan-Meier estimate of the event-time distribution from right-censored
     durations (observed False: the event had not happened when the window
     closed, the duration is the time the job was watched).  Returns, per
     quantile, the smallest duration t with 1 - S(t) >= q/100, or None when
-    the estimate never reaches q (the quantile lies beyond the window)."""
+    the estimate never reaches q (the quantile lies beyond the window).
+    With with_risk, also the number of jobs at risk where each quantile was
+    reached: a quantile reached with few jobs at risk rests on few jobs."""
     d = np.asarray(durations, dtype=float)
     o = np.asarray(observed, dtype=bool)
     order = np.lexsort((~o, d))                 # events before censorings at equal times
@@ -368,13 +370,17 @@ def km_quantiles(durations, observed, qs=(50, 99)):
     at_risk = len(d)
     surv = 1.0
     out = {q: None for q in qs}
+    risk = {q: None for q in qs}
     for t, ev in zip(d, o):
         if ev:
             surv *= 1.0 - 1.0 / at_risk
             for q in qs:
                 if out[q] is None and 1.0 - surv >= q / 100.0 - 1e-12:
                     out[q] = float(t)
+                    risk[q] = at_risk
         at_risk -= 1
+    if with_risk:
+        return out, risk
     return out
 
 
@@ -422,10 +428,12 @@ def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02, grand_
     ttfb = [i["first_bin"] - i["arrival"] for i in arrived if i["first_bin"] >= 0]
     done = [i["completed"] - i["arrival"] for i in arrived if i["completed"] >= 0]
     pct = lambda v, p: float(np.percentile(v, p)) if v else None
-    km_first = km_quantiles([(i["first_bin"] if i["first_bin"] >= 0 else t_end) - i["arrival"] for i in arrived],
-                            [i["first_bin"] >= 0 for i in arrived])
-    km_done = km_quantiles([(i["completed"] if i["completed"] >= 0 else t_end) - i["arrival"] for i in arrived],
-                           [i["completed"] >= 0 for i in arrived])
+    km_first, risk_first = km_quantiles(
+        [(i["first_bin"] if i["first_bin"] >= 0 else t_end) - i["arrival"] for i in arrived],
+        [i["first_bin"] >= 0 for i in arrived], with_risk=True)
+    km_done, risk_done = km_quantiles(
+        [(i["completed"] if i["completed"] >= 0 else t_end) - i["arrival"] for i in arrived],
+        [i["completed"] >= 0 for i in arrived], with_risk=True)
     srv.close()
     n_arr = max(len(arrived), 1)
     return {"bead_updates_per_s": bu / elapsed, "window_s": round(elapsed, 2),
@@ -438,6 +446,8 @@ def serving_run(pgb, seconds=12.0, rate=50.0, seed=0, round_seconds=0.02, grand_
             "peak_active": peak_active,
             "ttfb_p50_s": km_first[50], "ttfb_p99_s": km_first[99],
             "completion_p50_s": km_done[50], "completion_p99_s": km_done[99],
+            "at_risk": {"ttfb_p50": risk_first[50], "ttfb_p99": risk_first[99],
+                        "completion_p50": risk_done[50], "completion_p99": risk_done[99]},
             "uncensored": {"ttfb_p50_s": pct(ttfb, 50), "ttfb_p99_s": pct(ttfb, 99),
                            "completion_p50_s": pct(done, 50), "completion_p99_s": pct(done, 99)},
             "note": "Poisson %g jobs/s for %.1f s of a %.1f s window; p50/p99 are Kaplan-Meier "
@@ -1066,7 +1076,8 @@ def run_walkers(args, pgb, rank, ws):
     barrier(ws)
     clocks = clk.stop()
     launches = W.launch_count() - l0
-    t_dev = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    t_dev = sum(step_ms) / 1e3
     st = W.stats()
     bu = float(st["bead_updates"].sum())
     pairs = worm_pair_evals(w, st)
@@ -1117,6 +1128,7 @@ def run_walkers(args, pgb, rank, ws):
                       "l2": "flushed between timed steps",
                       "parallelism": "replicas" if ws > 1 else "single",
                       "walker_errors": errors, "closed_samples": closed,
+                      "step_ms": [round(x, 3) for x in step_ms],
                       "pair_evaluations_per_step": pairs / args.steps,
                       "acceptance": {WORM_MOVES[i]: [int(acc[i]), int(att[i])] for i in range(12)}},
            "e2e": {"value": e2e_val, "unit": "bead-updates/s", "h2d_bytes_per_step": nbytes,

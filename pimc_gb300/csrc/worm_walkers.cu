@@ -104,6 +104,7 @@ enum { WERR_FULL = 1, WERR_LINK = 2, WERR_LOOP = 3 };
 // pair work, most of its instructions, runs on four.
 constexpr int kCtaWarps = 4;
 constexpr int kTeamMinN = 64;
+constexpr int kTeamMinBeads = 4;     // shorter range actions of a team walker stay on its warp 0
 constexpr int kOrigCap = 72;         // saved positions per move (Mbar - 1 <= 63)
 constexpr int kMaxWind = 27;         // (2 maxWind + 1)^3 with maxWind = 1
 constexpr int kChainCap = 1024;      // beads of one move's range cached per walker (M < 1024)
@@ -472,7 +473,10 @@ struct WormWalker {
     // running sum over the whole range and reduce once (a team: each warp
     // over its share of the partners)
     __device__ __noinline__ double chainAction(int c0, int cnt) {
-        if (team > 1) {
+        // short ranges (a single bead's action in the worm moves) stay on
+        // warp 0: the team's two barriers and mailbox cost more than the
+        // few pair terms a lane would give away
+        if (team > 1 && cnt >= kTeamMinBeads) {
             teamPost(1, c0, cnt);
             bool ok = true;
             const float2 mine = teamShare(pairCtx(), chain, c0, cnt, 0, team, ok);
