@@ -103,7 +103,7 @@ enum { WERR_FULL = 1, WERR_LINK = 2, WERR_LOOP = 3 };
 // order.  A large walker's chain of dependent moves stays on one warp; its
 // pair work, most of its instructions, runs on four.
 constexpr int kCtaWarps = 4;
-constexpr int kTeamMinN = 64;
+constexpr int kTeamMinN = 32;
 constexpr int kTeamMinBeads = 4;     // shorter range actions of a team walker stay on its warp 0
 constexpr int kOrigCap = 72;         // saved positions per move (Mbar - 1 <= 63)
 constexpr int kMaxWind = 27;         // (2 maxWind + 1)^3 with maxWind = 1

@@ -200,7 +200,7 @@ def test_walker_pair_sums_match_fp64_oracle(pgb, oracle_lib, n):
 
 
 def test_team_walkers_match_oracle_statistically(pgb, oracle_lib):
-    """Walkers of N >= 64 run as four-warp teams (pair sums and energy samples
+    """Walkers of N >= 32 run as four-warp teams (pair sums and energy samples
     split over the warps): grand canonical at mu = -1 K, N0 = 64, M = 16,
     <E/N> and <N> over closed configurations within four combined standard
     errors of the oracle's worm engine; a team walker and the same walker run
