@@ -105,6 +105,7 @@ enum { WERR_FULL = 1, WERR_LINK = 2, WERR_LOOP = 3 };
 constexpr int kCtaWarps = 4;
 constexpr int kTeamMinN = 32;
 constexpr int kTeamMinBeads = 4;     // shorter range actions of a team walker stay on its warp 0
+constexpr int kRunCap = 128;         // per-bead shares a team warp keeps (a worm move's run <= Mbar + 1)
 constexpr int kOrigCap = 72;         // saved positions per move (Mbar - 1 <= 63)
 constexpr int kMaxWind = 27;         // (2 maxWind + 1)^3 with maxWind = 1
 constexpr int kChainCap = 1024;      // beads of one move's range cached per walker (M < 1024)
@@ -114,7 +115,7 @@ constexpr int kListOff = 512;
 
 // the shared-memory mailbox of a team: the posted job and each warp's share
 struct TeamJob {
-    int op;                          // 0 stop, 1 range action, 2 energy sums
+    int op;                          // 0 stop, 1 range action, 2 energy sums, 3 per-bead actions
     int a, b;                        // chain offset and count, or slices [a, b)
     WB head, tail, sp1, sp2;         // the worm state that sets the pair factors
     float hi[kCtaWarps], lo[kCtaWarps];      // each warp's (double-float) share
@@ -161,6 +162,9 @@ struct WormWalker {
     int team = 1;                    // warps serving this walker (1, or kCtaWarps for a team)
     int wk = 0;                      // this warp's place in the team
     TeamJob* job = nullptr;          // the team's mailbox
+    float2* tpart = nullptr;         // shared: a team's per-bead shares, kCtaWarps x kRunCap
+    float4* qbuf = nullptr;          // shared: a move's new bead positions, kOrigCap at most
+    double* acts = nullptr;          // shared: a move's per-bead actions (aliases znorm)
     // uniform scalar state
     WB head, tail, sp1, sp2;
     int gap, length, diag, numBeadsOn;
@@ -499,6 +503,70 @@ struct WormWalker {
         if (!ok) err = WERR_LINK;
         return m.tau * warp_sum_ff(k);
     }
+    // One warp's share of a team's per-bead actions: like teamShare, but each
+    // bead's terms reduced on their own, written to part[i] by lane 0
+    __device__ __noinline__ static void teamBeadShares(const PairCtx& c, const int* ch, int c0, int cnt, int wk,
+                                                       int T, bool& ok, float2* part) {
+        const int j0 = 32 * wk + c.lane, stride = 32 * T;
+        if (cnt <= 0) return;
+        TeamLoad cur, nx;
+        ok &= teamLoad(c, ch[c0], j0, cur);
+        for (int i = 0; i < cnt; ++i) {
+            if (i + 1 < cnt) ok &= teamLoad(c, ch[c0 + i + 1], j0, nx);
+            KahanF k;
+            if (cur.b.p < cur.n) {
+                const int s1 = c.state(cur.b);
+                const int t = cur.b.t;
+                if (s1 == 0 && c.head.t != t && c.tail.t != t && c.sp1.t != t && c.sp2.t != t)
+                    teamPairs<true>(c, cur, s1, j0, stride, k);
+                else
+                    teamPairs<false>(c, cur, s1, j0, stride, k);
+            }
+            const float2 r = warp_ff(k);
+            if (c.lane == 0) part[i] = r;
+            cur = nx;
+        }
+    }
+    // The bare potential action of each bead chain[c0 .. c0 + cnt - 1]
+    // (barePotentialAction, action.cpp:628-645, primitive) with the walker's
+    // current worm state, into out[0 .. cnt - 1] (shared): the worm moves'
+    // beads evaluated together, their Metropolis tests made afterwards in
+    // the reference's order.  A bead's value equals bare() of that bead; the
+    // next bead's loads are in flight while a bead's terms are summed.
+    __device__ __noinline__ void beadActions(int c0, int cnt, double* out) {
+        if (team > 1 && cnt >= kTeamMinBeads && cnt <= kRunCap) {
+            teamPost(3, c0, cnt);
+            bool ok = true;
+            teamBeadShares(pairCtx(), chain, c0, cnt, 0, team, ok, tpart);
+            if (lane == 0) job->bad[0] = ok ? 0 : 1;
+            team_sync(32 * team);
+            int bad = 0;
+            for (int q = 0; q < team; ++q) bad |= job->bad[q];
+            if (bad) err = WERR_LINK;
+            for (int i = lane; i < cnt; i += 32) {
+                double v = 0.0;
+                for (int q = 0; q < team; ++q)
+                    v += (double)tpart[q * kRunCap + i].x + (double)tpart[q * kRunCap + i].y;
+                out[i] = m.tau * v;
+            }
+            __syncwarp();
+            return;
+        }
+        const PairCtx c = pairCtx();
+        bool ok = true;
+        BeadLoad cur, nx;
+        if (cnt > 0) ok &= loadBead(c, chain[c0], cur);
+        for (int i = 0; i < cnt; ++i) {
+            if (i + 1 < cnt) ok &= loadBead(c, chain[c0 + i + 1], nx);
+            KahanF k;
+            if (cur.b.p < cur.n) pairsLoaded(c, cur, k);
+            const double v = warp_sum_ff(k);
+            if (lane == 0) out[i] = m.tau * v;
+            cur = nx;
+        }
+        if (!ok) err = WERR_LINK;
+        __syncwarp();
+    }
     // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
     // tau * sum over the other active beads of the slice of factor * V, as
     // a one-bead range in the cache's last slot (no move's range reaches it:
@@ -559,6 +627,78 @@ struct WormWalker {
         }
         setNext(last, {-1, -1}); setPrev(last, {-1, -1});
         --numBeadsOn;
+    }
+    // A run of cnt new beads on the slices after (dir = +1) or before
+    // (dir = -1) bead `from`, linked in a chain from it, at positions q[0 ..
+    // cnt - 1]: what cnt calls of addNextBead / addPrevBead (path.cpp:266-300)
+    // leave, made one lane a bead (the slices are distinct, cnt < M).  Bead k
+    // goes to the end of its slice; the run's locators land in chain[c0 + 1 ..
+    // c0 + cnt] and chain[c0] = from.  A slice without room stops the walker
+    // (WERR_FULL) with nothing added.
+    __device__ __noinline__ bool appendRun(WB from, int cnt, int dir, const float4* q, int c0) {
+        if (!valid(from) || cnt < 1 || cnt >= m.M) { err = WERR_LINK; return false; }
+        bool full = false;
+        for (int k = lane; k < cnt; k += 32) {
+            int t = from.t + dir * (k + 1);
+            t = ((t % m.M) + m.M) % m.M;
+            const int slot = nbs[t];
+            full |= slot >= m.Ne;
+            chain[c0 + 1 + k] = pack(WB{t, slot < m.Ne ? slot : 0});
+        }
+        if (lane == 0) chain[c0] = pack(from);
+        if (__any_sync(0xffffffffu, full)) { err = WERR_FULL; return false; }
+        __syncwarp();
+        for (int k = lane; k < cnt; k += 32) {
+            const WB b = unpack(chain[c0 + 1 + k]);
+            const WB before = unpack(chain[c0 + k]);
+            const int after = k + 1 < cnt ? unpack(chain[c0 + 2 + k]).p : -1;
+            nbs[b.t] = b.p + 1;
+            pos[li(b)] = q[k];
+            if (dir > 0) { prv[lk(b)] = before.p; nxt[lk(b)] = after; }
+            else { nxt[lk(b)] = before.p; prv[lk(b)] = after; }
+        }
+        if (lane == 0) {
+            const int first = unpack(chain[c0 + 1]).p;
+            if (dir > 0) nxt[lk(from)] = first;
+            else prv[lk(from)] = first;
+        }
+        numBeadsOn += cnt;
+        __syncwarp();
+        return true;
+    }
+    // the undo of appendRun(from, cnt, dir, ., c0) with the run's locators
+    // still in chain[c0 .. c0 + cnt]: each bead of the run is the last of its
+    // slice, so the cnt delBead calls (path.cpp:318-368) that remove it move
+    // no other bead; they drop the slice counts and the run's links, and
+    // unlink `from`
+    __device__ void dropRun(int cnt, int dir, int c0) {
+        for (int k = lane; k < cnt; k += 32) {
+            const WB b = unpack(chain[c0 + 1 + k]);
+            nbs[b.t] = b.p;
+            nxt[lk(b)] = -1; prv[lk(b)] = -1;
+        }
+        if (lane == 0) {
+            const WB from = unpack(chain[c0]);
+            if (dir > 0) nxt[lk(from)] = -1;
+            else prv[lk(from)] = -1;
+        }
+        numBeadsOn -= cnt;
+        __syncwarp();
+    }
+    // positions of a free-particle walk of cnt beads from r0 (newFreeParticle
+    // position, move.cpp:183-203: each bead a Gaussian step of sqrt(2 lambda
+    // tau) from the previous), into qbuf; the 3 cnt deviates come from the
+    // lanes together, the same words serial draws would use
+    __device__ void freeWalk(float4 r0, int cnt) {
+        normals(3 * cnt, znorm);
+        const float sg = (float)m.sqrt2LambdaTau;
+        float4 r = r0;
+        for (int k = 0; k < cnt; ++k) {
+            r = make_float4(putInBC(fmaf(znorm[3 * k], sg, r.x)), putInBC(fmaf(znorm[3 * k + 1], sg, r.y)),
+                            putInBC(fmaf(znorm[3 * k + 2], sg, r.z)), 0.f);
+            if (lane == 0) qbuf[k] = r;
+        }
+        __syncwarp();
     }
     __device__ WB delBeadGetNext(WB b) { WB n = next(b); delBead(b); return n; }
     __device__ WB delBeadGetPrev(WB b) { WB p = prev(b); delBead(b); return p; }
@@ -893,6 +1033,86 @@ struct WormWalker {
     }
 
     // ---- worm moves (move.cpp:1736-3826), local-action branches ----
+    // The worm moves below propose or remove a run of beads and test them one
+    // at a time in the reference's order, rejecting at the first failure
+    // (move.cpp:1736-3185).  Here the run's beads are placed first (new beads
+    // one lane a bead, appendRun), their bare actions evaluated together
+    // (beadActions), and then the same sequence of Metropolis tests reads the
+    // stored values.  The beads of a run sit on distinct slices and the pair
+    // action couples only beads of one slice, so a bead's action is the one
+    // the sequential form would find; the worm state is set as the reference
+    // sets it while the beads are evaluated.  A new run's normal deviates are
+    // all drawn before its uniform ones: a different order of independent
+    // draws, the same distribution.
+
+    // the beads from `a` along next (dir > 0) or prev links to `b` inclusive,
+    // into chain[0 ..]; returns their number (b not reached: the walk's end,
+    // with err set for a broken link)
+    __device__ int collectRun(WB a, WB b, int dir) {
+        int cnt = 0;
+        WB x = a;
+        for (int g = 0; g <= m.mbar + 1; ++g) {
+            if (isXW(x)) { err = WERR_LINK; break; }
+            if (lane == 0) chain[cnt] = pack(x);
+            ++cnt;
+            if (eqW(x, b)) break;
+            x = dir > 0 ? next(x) : prev(x);
+        }
+        __syncwarp();
+        return cnt;
+    }
+    // acts[k] for chain[k], evaluated a chunk at a time once the tests reach
+    // it: the first chunk one bead (kTeamMinBeads for a team), each next one
+    // twice as long, so that a run rejected at its first beads costs about
+    // what the sequential form costs and a long accepted run is evaluated in
+    // a few batches
+    __device__ void actsUpTo(int k, int total, int& ev, int& chunk) {
+        if (k < ev) return;
+        const int n = min(chunk, total - ev);
+        beadActions(ev, n, acts + ev);
+        ev += n;
+        chunk = min(2 * chunk, kRunCap);
+    }
+    __device__ int firstChunk() const { return team > 1 ? kTeamMinBeads : 1; }
+    // removal-type test over the beads chain[0 .. cnt - 1]: -(U_k - f_k
+    // shift), f = 1/2 at both ends and 1 between; true when every bead is
+    // accepted
+    __device__ bool removalTests(int cnt, double actionShift, double corr) {
+        int ev = 0, chunk = firstChunk();
+        for (int k = 0; k < cnt; ++k) {
+            actsUpTo(k, cnt, ev, chunk);
+            acc->bead_updates++;
+            double dA = -(acts[k] - ((k == 0 || k == cnt - 1) ? 0.5 : 1.0) * actionShift);
+            if (k == cnt - 1) dA -= corr;
+            if (!metro(dA)) return false;
+        }
+        return true;
+    }
+    // insertion-type test over the beads chain[0 .. cnt]: U_k - f_k shift,
+    // f = 1/2 at both ends and 1 between.  With `endRef` set, the last bead
+    // `end` becomes that worm end (*endRef = end) before its action is taken,
+    // as the reference sets the new head or tail before its test; chain[cnt]
+    // is then not read.
+    __device__ bool insertionTests(int cnt, double actionShift, double corr, WB* endRef, WB end) {
+        int ev = 0, chunk = firstChunk();
+        const int total = endRef ? cnt : cnt + 1;
+        for (int k = 0; k <= cnt; ++k) {
+            double u;
+            if (k == cnt && endRef) {
+                *endRef = end;
+                u = bare(end);
+            } else {
+                actsUpTo(k, total, ev, chunk);
+                u = acts[k];
+            }
+            acc->bead_updates++;
+            double dA = u - ((k == 0 || k == cnt) ? 0.5 : 1.0) * actionShift;
+            if (k == cnt) dA += corr;
+            if (!metro(dA)) return false;
+        }
+        return true;
+    }
+
     __device__ int open() {
         if (numBeadsOn == 0 || trueN() == 0) return -1;
         const int gapLength = randLen();
@@ -916,22 +1136,12 @@ struct WormWalker {
         acc->attempted[WM_OPEN]++;
         sp1 = hb; sp2 = tb;
         const double actionShift = (-log(norm) + muShift) / gapLength;
-        double factor = 0.5;
-        WB b = hb;
-        for (int g = 0; g <= m.M * m.Ne; ++g) {
-            acc->bead_updates++;
-            const double dA = -(bare(b) - factor * actionShift);
-            if (!metro(dA)) { wormReset(); diag = 1; return 0; }
-            factor = 1.0;
-            b = next(b);
-            if (eqW(b, tb) || isXW(b)) break;
-        }
-        acc->bead_updates++;
-        double dA = -(bare(tb) - 0.5 * actionShift);
-        dA -= corrRange(hb, tb);
-        if (metro(dA)) {
+        // hb, the gap's beads and tb: removed but the ends
+        const int cnt = collectRun(hb, tb, +1);
+        if (err) return -2;
+        if (removalTests(cnt, actionShift, corrRange(hb, tb))) {
             acc->accepted[WM_OPEN]++;
-            b = next(hb);
+            WB b = next(hb);
             for (int g = 0; g <= m.M && !eqW(b, tb) && !isXW(b); ++g) b = delBeadGetNext(b);
             wormUpdate(hb, tb);
             diag = 0;
@@ -940,9 +1150,9 @@ struct WormWalker {
         wormReset(); diag = 1;
         return 0;
     }
-    __device__ void closeUndo() {
-        WB b = next(head);
-        for (int g = 0; g <= m.M && !eqW(b, tail) && !isXW(b); ++g) b = delBeadGetNext(b);
+    // the undo of a close whose nnew staging beads are chain[1 .. nnew]
+    __device__ void closeUndo(int nnew) {
+        if (nnew > 0) dropRun(nnew, +1, 0);
         setNext(head, {-1, -1}); setPrev(tail, {-1, -1});
         diag = 0;
     }
@@ -958,30 +1168,40 @@ struct WormWalker {
         norm *= ensembleWeight(g0 - 1);
         const double muShift = g0 * m.mu * m.tau;
         const double actionShift = (log(norm) + muShift) / g0;
-        WB b = head;
-        acc->bead_updates++;
-        double dA = bare(b) - 0.5 * actionShift;
-        if (!metro(dA)) { closeUndo(); return 0; }
-        for (int k = 0; k < g0 - 1; k++) {
-            float x, y, z;
-            stagingPos(b, tail, g0, k, wind, x, y, z);
-            b = addNextBead(b, x, y, z);
-            if (err) return -2;
-            acc->bead_updates++;
-            dA = bare(b) - actionShift;
-            if (!metro(dA)) { closeUndo(); return 0; }
+        // the g0 - 1 staging positions from the head towards the tail
+        // (newStagingPosition with the winding sector, move.cpp:301-338)
+        const int nnew = g0 - 1;
+        if (nnew > 0) {
+            normals(3 * nnew, znorm);
+            float4 pp = P(head);
+            const float4 e = P(tail);
+            for (int k = 0; k < nnew; ++k) {
+                float x, y, z;
+                stagingPosZ(pp, e, g0, k, wind, znorm[3 * k], znorm[3 * k + 1], znorm[3 * k + 2], x, y, z);
+                pp = make_float4(x, y, z, 0.f);
+                if (lane == 0) qbuf[k] = pp;
+            }
+            __syncwarp();
+            if (!appendRun(head, nnew, +1, qbuf, 0)) return -2;
+        } else {
+            if (lane == 0) chain[0] = pack(head);
+            __syncwarp();
         }
-        setNext(b, tail); setPrev(tail, b);
-        acc->bead_updates++;
-        dA = bare(tail) - 0.5 * actionShift;
-        dA += corrRange(head, tail);
-        if (metro(dA)) { acc->accepted[WM_CLOSE]++; wormReset(); diag = 1; return 1; }
-        closeUndo();
+        const WB last = unpack(chain[nnew]);
+        setNext(last, tail); setPrev(tail, last);
+        if (lane == 0) chain[g0] = pack(tail);
+        __syncwarp();
+        // head, the new beads and the tail
+        if (insertionTests(g0, actionShift, corrRange(head, tail), nullptr, tail)) {
+            acc->accepted[WM_CLOSE]++; wormReset(); diag = 1; return 1;
+        }
+        closeUndo(nnew);
         return 0;
     }
-    __device__ void insertUndo(WB tb) {
-        WB b = tb;
-        for (int g = 0; g <= m.M + 1 && !isXW(b); ++g) b = delBeadGetNext(b);
+    // the undo of an insert: the run of wl beads after tb, then tb
+    __device__ void insertUndo(WB tb, int wl) {
+        dropRun(wl, +1, 0);
+        delBead(tb);
         wormReset(); diag = 1;
     }
     __device__ int insert() {
@@ -998,29 +1218,15 @@ struct WormWalker {
         if (err) return -2;
         sp2 = tb;
         const double actionShift = (log(norm) + muShift) / wl;
-        WB b = tb;
-        acc->bead_updates++;
-        double dA = bare(b) - 0.5 * actionShift;
-        if (!metro(dA)) { insertUndo(tb); return 0; }
-        for (int k = 1; k < wl; k++) {
-            float x, y, z;
-            freePos(b, x, y, z);
-            b = addNextBead(b, x, y, z);
-            if (err) return -2;
-            acc->bead_updates++;
-            dA = bare(b) - actionShift;
-            if (!metro(dA)) { insertUndo(tb); return 0; }
+        // the new worldline: tb, wl - 1 beads, the head
+        freeWalk(make_float4(x0, y0, z0, 0.f), wl);
+        if (!appendRun(tb, wl, +1, qbuf, 0)) return -2;
+        const WB hb = unpack(chain[wl]);
+        // tb, the intermediate beads and the head (sp1 = hb before its test)
+        if (insertionTests(wl, actionShift, corrRange(tb, hb), &sp1, hb)) {
+            acc->accepted[WM_INSERT]++; wormUpdate(hb, tb); diag = 0; return 1;
         }
-        float x, y, z;
-        freePos(b, x, y, z);
-        const WB hb = addNextBead(b, x, y, z);
-        if (err) return -2;
-        sp1 = hb;
-        acc->bead_updates++;
-        dA = bare(hb) - 0.5 * actionShift;
-        dA += corrRange(tb, hb);
-        if (metro(dA)) { acc->accepted[WM_INSERT]++; wormUpdate(hb, tb); diag = 0; return 1; }
-        insertUndo(tb);
+        insertUndo(tb, wl);
         return 0;
     }
     __device__ int remove() {
@@ -1032,22 +1238,12 @@ struct WormWalker {
         norm *= ensembleWeight(-length);
         if (norm < 2.220446049250313e-16) return 0;
         const double actionShift = (-log(norm) + muShift) / length;
-        WB b = head;
-        double factor = 0.5;
-        for (int g = 0; g <= m.M * m.Ne; ++g) {
-            acc->bead_updates++;
-            const double dA = -(bare(b) - factor * actionShift);
-            if (!metro(dA)) { diag = 0; return 0; }
-            factor = 1.0;
-            b = prev(b);
-            if (eqW(b, tail) || isXW(b)) break;
-        }
-        acc->bead_updates++;
-        double dA = -(bare(tail) - 0.5 * actionShift);
-        dA -= corrRange(tail, head);
-        if (metro(dA)) {
+        // the worm from the head back to the tail
+        const int cnt = collectRun(head, tail, -1);
+        if (err) return -2;
+        if (removalTests(cnt, actionShift, corrRange(tail, head))) {
             acc->accepted[WM_REMOVE]++;
-            b = head;
+            WB b = head;
             for (int g = 0; g <= m.M * m.Ne && !isXW(b); ++g) b = delBeadGetPrev(b);
             wormReset(); diag = 1;
             return 1;
@@ -1055,11 +1251,9 @@ struct WormWalker {
         diag = 0;
         return 0;
     }
-    __device__ void ahUndo() {
+    __device__ void ahUndo(int al) {
         head = sp1;
-        WB b = next(head);
-        for (int g = 0; g <= m.M && !isXW(b); ++g) b = delBeadGetNext(b);
-        setNext(head, {-1, -1});
+        dropRun(al, +1, 0);
         diag = 0;
         sp1 = WB{-1, -1};
     }
@@ -1072,29 +1266,16 @@ struct WormWalker {
         norm *= ensembleWeight(al);
         sp1 = head; head = WB{-1, -1};
         const double actionShift = (log(norm) + muShift) / al;
-        WB b = sp1;
-        acc->bead_updates++;
-        double dA = bare(b) - 0.5 * actionShift;
-        if (!metro(dA)) { ahUndo(); return 0; }
-        for (int k = 0; k < al - 1; k++) {
-            float x, y, z;
-            freePos(b, x, y, z);
-            b = addNextBead(b, x, y, z);
-            if (err) return -2;
-            acc->bead_updates++;
-            dA = bare(b) - actionShift;
-            if (!metro(dA)) { ahUndo(); return 0; }
+        // the old head and al new beads, the last the new head
+        freeWalk(P(sp1), al);
+        if (!appendRun(sp1, al, +1, qbuf, 0)) return -2;
+        const WB hb = unpack(chain[al]);
+        // the old head, the intermediate beads and the new head, set before
+        // its test (potentialAction(head): primitive)
+        if (insertionTests(al, actionShift, corrRange(sp1, hb), &head, hb)) {
+            acc->accepted[WM_AH]++; wormUpdate(hb, tail); diag = 0; return 1;
         }
-        float x, y, z;
-        freePos(b, x, y, z);
-        const WB hb = addNextBead(b, x, y, z);
-        if (err) return -2;
-        head = hb;
-        acc->bead_updates++;
-        dA = bare(hb) - 0.5 * actionShift;          // potentialAction(head): primitive
-        dA += corrRange(sp1, head);
-        if (metro(dA)) { acc->accepted[WM_AH]++; wormUpdate(hb, tail); diag = 0; return 1; }
-        ahUndo();
+        ahUndo(al);
         return 0;
     }
     __device__ int advanceTail() {
@@ -1109,22 +1290,12 @@ struct WormWalker {
         acc->attempted[WM_AT]++;
         sp1 = tb;
         const double actionShift = (-log(norm) + muShift) / al;
-        double factor = 0.5;
-        WB b = tail;
-        for (int g = 0; g <= m.M * m.Ne; ++g) {
-            acc->bead_updates++;
-            const double dA = -(bare(b) - factor * actionShift);
-            if (!metro(dA)) { diag = 0; sp1 = WB{-1, -1}; return 0; }
-            factor = 1.0;
-            b = next(b);
-            if (eqW(b, tb) || isXW(b)) break;
-        }
-        acc->bead_updates++;
-        double dA = -(bare(b) - 0.5 * actionShift);
-        dA -= corrRange(tail, tb);
-        if (metro(dA)) {
+        // the tail and the beads up to tb: removed but tb
+        const int cnt = collectRun(tail, tb, +1);
+        if (err) return -2;
+        if (removalTests(cnt, actionShift, corrRange(tail, tb))) {
             acc->accepted[WM_AT]++;
-            b = prev(tb);
+            WB b = prev(tb);
             for (int g = 0; g <= m.M * m.Ne && !isXW(b); ++g) b = delBeadGetPrev(b);
             wormUpdate(head, tb);
             diag = 0;
@@ -1145,22 +1316,12 @@ struct WormWalker {
         acc->attempted[WM_RH]++;
         sp1 = hb;
         const double actionShift = (-log(norm) + muShift) / rl;
-        double factor = 0.5;
-        WB b = head;
-        for (int g = 0; g <= m.M * m.Ne; ++g) {
-            acc->bead_updates++;
-            const double dA = -(bare(b) - factor * actionShift);
-            if (!metro(dA)) { diag = 0; sp1 = WB{-1, -1}; return 0; }
-            factor = 1.0;
-            b = prev(b);
-            if (eqW(b, hb) || isXW(b)) break;
-        }
-        acc->bead_updates++;
-        double dA = -(bare(hb) - 0.5 * actionShift);
-        dA -= corrRange(sp1, head);
-        if (metro(dA)) {
+        // the head and the beads back to hb: removed but hb
+        const int cnt = collectRun(head, hb, -1);
+        if (err) return -2;
+        if (removalTests(cnt, actionShift, corrRange(sp1, head))) {
             acc->accepted[WM_RH]++;
-            b = next(hb);
+            WB b = next(hb);
             for (int g = 0; g <= m.M * m.Ne && !isXW(b); ++g) b = delBeadGetNext(b);
             wormUpdate(hb, tail);
             diag = 0;
@@ -1169,11 +1330,9 @@ struct WormWalker {
         diag = 0; sp1 = WB{-1, -1};
         return 0;
     }
-    __device__ void rtUndo() {
+    __device__ void rtUndo(int rl) {
         tail = sp1;
-        WB b = prev(tail);
-        for (int g = 0; g <= m.M && !isXW(b); ++g) b = delBeadGetPrev(b);
-        setPrev(tail, {-1, -1});
+        dropRun(rl, -1, 0);
         diag = 0;
         sp1 = WB{-1, -1};
     }
@@ -1186,29 +1345,16 @@ struct WormWalker {
         norm *= ensembleWeight(rl);
         sp1 = tail; tail = WB{-1, -1};
         const double actionShift = (log(norm) + muShift) / rl;
-        WB b = sp1;
-        acc->bead_updates++;
-        double dA = bare(b) - 0.5 * actionShift;
-        if (!metro(dA)) { rtUndo(); return 0; }
-        for (int k = 0; k < rl - 1; k++) {
-            float x, y, z;
-            freePos(b, x, y, z);
-            b = addPrevBead(b, x, y, z);
-            if (err) return -2;
-            acc->bead_updates++;
-            dA = bare(b) - actionShift;
-            if (!metro(dA)) { rtUndo(); return 0; }
+        // the old tail and rl new beads before it, the last the new tail
+        freeWalk(P(sp1), rl);
+        if (!appendRun(sp1, rl, -1, qbuf, 0)) return -2;
+        const WB tb = unpack(chain[rl]);
+        // the old tail, the intermediate beads and the new tail, set before
+        // its test
+        if (insertionTests(rl, actionShift, corrRange(tb, sp1), &tail, tb)) {
+            acc->accepted[WM_RT]++; wormUpdate(head, tb); diag = 0; return 1;
         }
-        float x, y, z;
-        freePos(b, x, y, z);
-        const WB tb = addPrevBead(b, x, y, z);
-        if (err) return -2;
-        tail = tb;
-        acc->bead_updates++;
-        dA = bare(tb) - 0.5 * actionShift;
-        dA += corrRange(tb, sp1);
-        if (metro(dA)) { acc->accepted[WM_RT]++; wormUpdate(head, tb); diag = 0; return 1; }
-        rtUndo();
+        rtUndo(rl);
         return 0;
     }
     // SwapMoveBase::getNorm + selectPivotBead (move.cpp:3212-3338) over the
@@ -1504,7 +1650,8 @@ __device__ __noinline__ void run_walker(int w, int team, TeamJob* job, const WWM
                                         WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
                                         const AzizF& az, int sweeps, const int* __restrict__ limit,
                                         unsigned long long budget_ns, int diag_only, float4* s_orig,
-                                        float4* s_newp, int* s_chain, float* s_norm, double* s_cum) {
+                                        float4* s_newp, int* s_chain, double* s_scr, double* s_cum,
+                                        float2* tpart) {
     WormWalker ww;
     ww.m = meta[w];
     ww.az = az;
@@ -1515,10 +1662,13 @@ __device__ __noinline__ void run_walker(int w, int team, TeamJob* job, const WWM
     ww.nbs = nbs + nbs_off[w];
     ww.acc = &stats[w];
     ww.chain = s_chain;
-    ww.znorm = s_norm;
+    ww.znorm = reinterpret_cast<float*>(s_scr);  // a move's deviates, then its per-bead actions
+    ww.acts = s_scr;
+    ww.qbuf = s_newp;
     ww.team = team;
     ww.wk = 0;
     ww.job = job;
+    ww.tpart = tpart;
     const WWState st = states[w];
     if (st.err) return;
     ww.head = WB{st.head[0], st.head[1]}; ww.tail = WB{st.tail[0], st.tail[1]};
@@ -1664,7 +1814,7 @@ __device__ __noinline__ void run_walker(int w, int team, TeamJob* job, const WWM
 __device__ __noinline__ void team_helper(int w, int wk, const WWMeta* __restrict__ meta, float4* __restrict__ pos,
                                          int* __restrict__ nxt, int* __restrict__ nbs,
                                          const long long* __restrict__ nbs_off, const AzizF& az, int* chain,
-                                         TeamJob* job) {
+                                         TeamJob* job, float2* tpart) {
     WormWalker ww;
     ww.m = meta[w];
     ww.az = az;
@@ -1683,6 +1833,10 @@ __device__ __noinline__ void team_helper(int w, int wk, const WWMeta* __restrict
             bool ok = true;
             const float2 r = WormWalker::teamShare(c, chain, job->a, job->b, wk, kCtaWarps, ok);
             if (ww.lane == 0) { job->hi[wk] = r.x; job->lo[wk] = r.y; job->bad[wk] = ok ? 0 : 1; }
+        } else if (op == 3) {
+            bool ok = true;
+            WormWalker::teamBeadShares(c, chain, job->a, job->b, wk, kCtaWarps, ok, tpart + wk * kRunCap);
+            if (ww.lane == 0) job->bad[wk] = ok ? 0 : 1;
         } else {
             float2 p, k;
             WormWalker::energyShare(c, ww.nxt, job->a + wk, job->b, kCtaWarps, p, k);
@@ -1706,7 +1860,7 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     __shared__ float4 s_orig[kCtaWarps][kOrigCap];
     __shared__ float4 s_newp[kCtaWarps][kOrigCap];
     __shared__ int s_chain[kCtaWarps][kChainCap];
-    __shared__ float s_norm[kCtaWarps][3 * kOrigCap];
+    __shared__ double s_scr[kCtaWarps][3 * kOrigCap / 2];
     __shared__ double s_cum[kCtaWarps][2 * WM_N];
     __shared__ TeamJob s_job;
     const int warp = threadIdx.x >> 5;
@@ -1714,20 +1868,24 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     if (pl[1] == kPlanTeam) {
         const int w = pl[0];
         if (warp == 0) {
+            // a team uses only the first warp's buffers; the second warp's chain
+            // cache holds the team's per-bead shares
+            float2* tpart = reinterpret_cast<float2*>(s_chain[1]);
             run_walker(w, kCtaWarps, &s_job, meta, pos, nxt, prv, nbs, nbs_off, states, stats, az, sweeps, limit,
-                       budget_ns, diag_only, s_orig[0], s_newp[0], s_chain[0], s_norm[0], s_cum[0]);
+                       budget_ns, diag_only, s_orig[0], s_newp[0], s_chain[0], s_scr[0], s_cum[0], tpart);
             // every path out of run_walker ends here: release the helpers
             if ((threadIdx.x & 31) == 0) s_job.op = 0;
             team_sync(32 * kCtaWarps);
         } else {
-            team_helper(w, warp, meta, pos, nxt, nbs, nbs_off, az, s_chain[0], &s_job);
+            team_helper(w, warp, meta, pos, nxt, nbs, nbs_off, az, s_chain[0], &s_job,
+                        reinterpret_cast<float2*>(s_chain[1]));
         }
         return;
     }
     const int w = pl[warp];
     if (w < 0) return;
     run_walker(w, 1, nullptr, meta, pos, nxt, prv, nbs, nbs_off, states, stats, az, sweeps, limit, budget_ns,
-               diag_only, s_orig[warp], s_newp[warp], s_chain[warp], s_norm[warp], s_cum[warp]);
+               diag_only, s_orig[warp], s_newp[warp], s_chain[warp], s_scr[warp], s_cum[warp], nullptr);
 }
 
 // an admitted job's seeded closed worldlines: particle i's centre uniform in
