@@ -162,7 +162,7 @@ struct WormWalker {
     int team = 1;                    // warps serving this walker (1, or kCtaWarps for a team)
     int wk = 0;                      // this warp's place in the team
     TeamJob* job = nullptr;          // the team's mailbox
-    float2* tpart = nullptr;         // shared: a team's per-bead shares, kCtaWarps x kRunCap
+    float2* tpart = nullptr;         // shared: a team's per-bead sums, kRunCap at most
     float4* qbuf = nullptr;          // shared: a move's new bead positions, kOrigCap at most
     double* acts = nullptr;          // shared: a move's per-bead actions (aliases znorm)
     // uniform scalar state
@@ -412,45 +412,22 @@ struct WormWalker {
         if (s1 == 0 && c.head.t != t && c.tail.t != t && c.sp1.t != t && c.sp2.t != t) pairsOf<true>(c, L, s1, k);
         else pairsOf<false>(c, L, s1, k);
     }
-    // One warp's share of a team's range action: beads chain[c0 ..], the
-    // partners j = 32 wk + lane, stepping 32 T.  The next bead's slice
-    // count, position and first partner load while this bead's terms are
-    // summed.  Returns the warp's (double-float) sum; ok false for a locator
-    // outside the walker's arrays.
-    struct TeamLoad { WB b; int n; float4 rb, r0; };
-    __device__ static bool teamLoad(const PairCtx& c, int code, int j0, TeamLoad& L) {
-        L.b = unpack(code);
-        const bool ok = L.b.t < c.M && L.b.p < c.Ne;
-        if (!ok) L.b = WB{0, 0};
-        const float4* row = c.pos + (size_t)L.b.t * c.Ne;
-        L.n = ok ? c.nbs[L.b.t] : 0;
-        L.rb = row[L.b.p];
-        L.r0 = j0 < c.Ne ? row[j0] : L.rb;
-        return ok;
-    }
-    template <bool Plain>
-    __device__ static void teamPairs(const PairCtx& c, const TeamLoad& L, int s1, int j0, int stride, KahanF& k) {
-        pairTerm<Plain>(c, L.b, s1, j0, L.n, L.rb, L.r0, k);
-        const float4* row = c.pos + (size_t)L.b.t * c.Ne;
-        for (int j = j0 + stride; j < L.n; j += stride) pairTerm<Plain>(c, L.b, s1, j, L.n, L.rb, row[j], k);
-    }
+    // One warp's share of a team's range action: the beads chain[c0 + wk],
+    // chain[c0 + wk + T], ..., each with all its partners as the single-warp
+    // form sums them (the next bead of the share loading meanwhile).  The
+    // four warps walk four beads at a time, so a range costs about a quarter
+    // of the dependent load chain of one warp walking it.  Returns the
+    // warp's (double-float) sum; ok false for a locator outside the walker's
+    // arrays.
     __device__ __noinline__ static float2 teamShare(const PairCtx& c, const int* ch, int c0, int cnt, int wk, int T,
                                                     bool& ok) {
         KahanF k;
-        const int j0 = 32 * wk + c.lane, stride = 32 * T;
-        if (cnt > 0) {
-            TeamLoad cur, nx;
-            ok &= teamLoad(c, ch[c0], j0, cur);
-            for (int i = 0; i < cnt; ++i) {
-                if (i + 1 < cnt) ok &= teamLoad(c, ch[c0 + i + 1], j0, nx);
-                if (cur.b.p < cur.n) {
-                    const int s1 = c.state(cur.b);
-                    const int t = cur.b.t;
-                    if (s1 == 0 && c.head.t != t && c.tail.t != t && c.sp1.t != t && c.sp2.t != t)
-                        teamPairs<true>(c, cur, s1, j0, stride, k);
-                    else
-                        teamPairs<false>(c, cur, s1, j0, stride, k);
-                }
+        if (wk < cnt) {
+            BeadLoad cur, nx;
+            ok &= loadBead(c, ch[c0 + wk], cur);
+            for (int i = wk; i < cnt; i += T) {
+                if (i + T < cnt) ok &= loadBead(c, ch[c0 + i + T], nx);
+                if (cur.b.p < cur.n) pairsLoaded(c, cur, k);
                 cur = nx;
             }
         }
@@ -503,25 +480,18 @@ struct WormWalker {
         if (!ok) err = WERR_LINK;
         return m.tau * warp_sum_ff(k);
     }
-    // One warp's share of a team's per-bead actions: like teamShare, but each
-    // bead's terms reduced on their own, written to part[i] by lane 0
+    // One warp's share of a team's per-bead actions: the beads of its
+    // teamShare share, each reduced on its own and written to part[i] by
+    // lane 0
     __device__ __noinline__ static void teamBeadShares(const PairCtx& c, const int* ch, int c0, int cnt, int wk,
                                                        int T, bool& ok, float2* part) {
-        const int j0 = 32 * wk + c.lane, stride = 32 * T;
-        if (cnt <= 0) return;
-        TeamLoad cur, nx;
-        ok &= teamLoad(c, ch[c0], j0, cur);
-        for (int i = 0; i < cnt; ++i) {
-            if (i + 1 < cnt) ok &= teamLoad(c, ch[c0 + i + 1], j0, nx);
+        if (wk >= cnt) return;
+        BeadLoad cur, nx;
+        ok &= loadBead(c, ch[c0 + wk], cur);
+        for (int i = wk; i < cnt; i += T) {
+            if (i + T < cnt) ok &= loadBead(c, ch[c0 + i + T], nx);
             KahanF k;
-            if (cur.b.p < cur.n) {
-                const int s1 = c.state(cur.b);
-                const int t = cur.b.t;
-                if (s1 == 0 && c.head.t != t && c.tail.t != t && c.sp1.t != t && c.sp2.t != t)
-                    teamPairs<true>(c, cur, s1, j0, stride, k);
-                else
-                    teamPairs<false>(c, cur, s1, j0, stride, k);
-            }
+            if (cur.b.p < cur.n) pairsLoaded(c, cur, k);
             const float2 r = warp_ff(k);
             if (c.lane == 0) part[i] = r;
             cur = nx;
@@ -543,12 +513,7 @@ struct WormWalker {
             int bad = 0;
             for (int q = 0; q < team; ++q) bad |= job->bad[q];
             if (bad) err = WERR_LINK;
-            for (int i = lane; i < cnt; i += 32) {
-                double v = 0.0;
-                for (int q = 0; q < team; ++q)
-                    v += (double)tpart[q * kRunCap + i].x + (double)tpart[q * kRunCap + i].y;
-                out[i] = m.tau * v;
-            }
+            for (int i = lane; i < cnt; i += 32) out[i] = m.tau * ((double)tpart[i].x + (double)tpart[i].y);
             __syncwarp();
             return;
         }
@@ -1835,7 +1800,7 @@ __device__ __noinline__ void team_helper(int w, int wk, const WWMeta* __restrict
             if (ww.lane == 0) { job->hi[wk] = r.x; job->lo[wk] = r.y; job->bad[wk] = ok ? 0 : 1; }
         } else if (op == 3) {
             bool ok = true;
-            WormWalker::teamBeadShares(c, chain, job->a, job->b, wk, kCtaWarps, ok, tpart + wk * kRunCap);
+            WormWalker::teamBeadShares(c, chain, job->a, job->b, wk, kCtaWarps, ok, tpart);
             if (ww.lane == 0) job->bad[wk] = ok ? 0 : 1;
         } else {
             float2 p, k;
