@@ -177,12 +177,14 @@ struct WormWalker {
     pgb_worm_walker_stats* acc;
 
     // ---- random numbers (MTRand's conversions on Philox words) ----
+    // the next draw block (one copy of the Philox rounds for every call site)
+    __device__ __noinline__ void refill() {
+        buf = philox4x32(make_uint4((uint32_t)ctr, (uint32_t)(ctr >> 32), 0x574F524Du, 0u), m.key);
+        ++ctr;
+        bidx = 0;
+    }
     __device__ uint32_t u32() {
-        if (bidx == 4) {
-            buf = philox4x32(make_uint4((uint32_t)ctr, (uint32_t)(ctr >> 32), 0x574F524Du, 0u), m.key);
-            ++ctr;
-            bidx = 0;
-        }
+        if (bidx == 4) refill();
         const int i = bidx++;
         return i == 0 ? buf.x : i == 1 ? buf.y : i == 2 ? buf.z : buf.w;
     }
@@ -463,22 +465,12 @@ struct WormWalker {
             const float2 mine = teamShare(pairCtx(), chain, c0, cnt, 0, team, ok);
             return m.tau * teamCollect(mine, ok);
         }
-        const PairCtx c = pairCtx();
-        const int* ch = chain;
-        KahanF k;
+        // one warp: the team form with a team of one (one copy of the pair
+        // loop in the kernel's code)
         bool ok = true;
-        if (cnt > 0) {
-            // the next bead's loads are in flight while this bead's pairs are summed
-            BeadLoad cur, nx;
-            ok &= loadBead(c, ch[c0], cur);
-            for (int i = 0; i < cnt; ++i) {
-                if (i + 1 < cnt) ok &= loadBead(c, ch[c0 + i + 1], nx);
-                if (cur.b.p < cur.n) pairsLoaded(c, cur, k);
-                cur = nx;
-            }
-        }
+        const float2 r = teamShare(pairCtx(), chain, c0, cnt, 0, 1, ok);
         if (!ok) err = WERR_LINK;
-        return m.tau * warp_sum_ff(k);
+        return m.tau * ((double)r.x + (double)r.y);
     }
     // One warp's share of a team's per-bead actions: the beads of its
     // teamShare share, each reduced on its own and written to part[i] by
@@ -517,19 +509,17 @@ struct WormWalker {
             __syncwarp();
             return;
         }
-        const PairCtx c = pairCtx();
+        // one warp: the team form with a team of one, each bead's (double-
+        // float) sum written over its own output slot and widened there
         bool ok = true;
-        BeadLoad cur, nx;
-        if (cnt > 0) ok &= loadBead(c, chain[c0], cur);
-        for (int i = 0; i < cnt; ++i) {
-            if (i + 1 < cnt) ok &= loadBead(c, chain[c0 + i + 1], nx);
-            KahanF k;
-            if (cur.b.p < cur.n) pairsLoaded(c, cur, k);
-            const double v = warp_sum_ff(k);
-            if (lane == 0) out[i] = m.tau * v;
-            cur = nx;
-        }
+        float2* part = reinterpret_cast<float2*>(out);
+        teamBeadShares(pairCtx(), chain, c0, cnt, 0, 1, ok, part);
         if (!ok) err = WERR_LINK;
+        __syncwarp();
+        for (int i = lane; i < cnt; i += 32) {
+            const float2 r = part[i];
+            out[i] = m.tau * ((double)r.x + (double)r.y);
+        }
         __syncwarp();
     }
     // LocalAction::barePotentialAction(bead), primitive action (VF = 1):
