@@ -187,8 +187,15 @@ int pgb_qvectors_shells(double dq, double qmax, int sphere, double* q, int* shel
  * (estimator.cpp:4063-4100, gpu_isf estimator_gpu.cu:67-165): layout
  * [q][M/2+1], value (1/(N M)) sum_{t,i,j} cos(q.(r_j(t+tau) - r_i(t))).
  * mode 0: CUDA-core correlation; mode 1: tensor-core (tcgen05, split-BF16)
- * DFT correlation.  PGB_FP64 contexts always use the FP64 direct form. */
+ * DFT correlation.  PGB_FP64 contexts always use the FP64 direct form.
+ * Every wait of the tensor-core pipeline is bounded (about a second); one
+ * that runs out makes the call return PGB_ETIMEOUT, the context usable. */
 int pgb_isf(pgb_ctx* ctx, const double* q, int nq, int mode, double* out);
+/* Test of the bounded waits (no counterpart in the reference): with on != 0
+ * the first tensor-core GEMM of every later pgb_isf (mode 1, PGB_MIXED)
+ * stops issuing before its last K chunk, so a wait runs out and the call
+ * returns PGB_ETIMEOUT; on = 0 restores normal operation.  Process-wide. */
+void pgb_test_isf_tc_stall(int on);
 /* The adjacent path-wide estimators, one accumulate() each (FP64):
  * g(r): PairCorrelationEstimator (estimator.cpp:3181-3246), 50 bins of
  *   0.5 sqrt(3) L_z / 50, the sample already times the estimator's norm;
@@ -207,7 +214,8 @@ int pgb_permutation_cycles(pgb_ctx* ctx, double out40[40]);
 int pgb_rhoq(pgb_ctx* ctx, const double* q, int nq, double* out);
 
 /* ---- device-resident variants for timing: inputs already in device
- *      memory, results left on the device (no host copies, no syncs). ---- */
+ *      memory, results left on the device (no host copies, no syncs; the
+ *      tensor-core pipeline's timeout word is checked by pgb_isf only). ---- */
 int pgb_isf_device_async(pgb_ctx* ctx, const double* d_q, int nq, int mode,
                          double* d_out);
 int pgb_ssf_device_async(pgb_ctx* ctx, const double* d_q, int nq, double* d_out);

@@ -146,6 +146,7 @@ _SIGS = {
     "pgb_qvectors": (C.c_int, [C.c_char_p, C.c_char_p, _DP, _DP, C.c_int, C.POINTER(C.c_int)]),
     "pgb_ssf": (C.c_int, [_VP, _DP, C.c_int, _DP]),
     "pgb_isf": (C.c_int, [_VP, _DP, C.c_int, C.c_int, _DP]),
+    "pgb_test_isf_tc_stall": (None, [C.c_int]),
     "pgb_rhoq": (C.c_int, [_VP, _DP, C.c_int, _DP]),
     "pgb_isf_device_async": (C.c_int, [_VP, _VP, C.c_int, C.c_int, _VP]),
     "pgb_update_positions": (C.c_int, [_VP, _DP]),

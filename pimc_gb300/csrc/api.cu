@@ -940,7 +940,18 @@ int scatter_host(pgb_ctx* h, const double* q, int nq, int what, int mode, double
                         reinterpret_cast<double*>(base + off_o), base + off_w);
     if (rc) return rc;
     PGB_CUDA(&c, cudaMemcpyAsync(out, base + off_o, ob, cudaMemcpyDeviceToHost, c.stream));
+    const bool tc = c.p.precision == PGB_MIXED && what == 1 && mode == 1;
+    int tc_err = 0;
+    if (tc) {
+        // the tensor-core pipeline's error word: a bounded wait ran out
+        const char* w = base + off_w + rho_region(c, nq) + posbuf_region(c);
+        PGB_CUDA(&c, cudaMemcpyAsync(&tc_err, w + isf_tc_error_offset(nq, c.M), sizeof(int),
+                                     cudaMemcpyDeviceToHost, c.stream));
+    }
     PGB_CUDA(&c, cudaStreamSynchronize(c.stream));
+    if (tc_err)
+        return c.fail(PGB_ETIMEOUT, "F(q,tau): a tensor-core pipeline wait ran out (a staged copy or "
+                                    "the MMAs did not complete within the wait limit)");
     return PGB_OK;
 }
 
@@ -1011,6 +1022,8 @@ int pgb_qvectors_shells(double dq, double qmax, int sphere, double* qvecs, int* 
 }
 int pgb_isf(pgb_ctx* h, const double* q, int nq, int mode, double* out) { return scatter_host(h, q, nq, 1, mode, out); }
 int pgb_rhoq(pgb_ctx* h, const double* q, int nq, double* out) { return scatter_host(h, q, nq, 2, 0, out); }
+
+void pgb_test_isf_tc_stall(int on) { isf_tc_set_stall_test(on); }
 
 int pgb_isf_device_async(pgb_ctx* h, const double* d_q, int nq, int mode, double* d_out) {
     if (!h || !d_q || !d_out || nq <= 0) return PGB_EINVAL;

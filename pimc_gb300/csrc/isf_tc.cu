@@ -23,6 +23,7 @@
 // accumulator (128 lanes x 256 FP32 columns of TMEM) is read back with
 // tcgen05.ld by all four warps.
 #include <cuda_bf16.h>
+#include <atomic>
 #include <cstdint>
 
 #include "pgb_device.cuh"
@@ -41,6 +42,7 @@ constexpr int kStages = 2;
 constexpr uint32_t kStageBytes = 2 * kTileA + 2 * kTileB;     // Ah, Al, Bh, Bl of one chunk
 constexpr uint32_t kSmem = kStages * kStageBytes + 1024;
 constexpr long long kMmaWaitLimit = 1LL << 24;
+constexpr unsigned long long kWaitNs = 1000000000ull;   // one second of wall clock per wait
 
 // Element index of (r, k) in a tile-ordered [rows x K] bf16 operand whose
 // tiles are TR rows x 64 K: tile (r / TR, k / 64) is one contiguous block of
@@ -118,10 +120,22 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                  :: "r"(su32(dst)), "l"(src), "r"(bytes), "r"(su32(bar)) : "memory");
 }
 
+__device__ __forceinline__ unsigned long long wall_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// a wait on an mbarrier phase that gives up after kMmaWaitLimit polls or
+// kWaitNs of wall clock, whichever comes first (false: the phase did not
+// complete)
 __device__ __forceinline__ bool bar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    const unsigned long long t0 = wall_ns();
     long long n = 0;
-    while (!bar_try_wait(bar, parity))
+    while (!bar_try_wait(bar, parity)) {
         if (++n > kMmaWaitLimit) return false;
+        if ((n & 255) == 0 && wall_ns() - t0 > kWaitNs) return false;
+    }
     return true;
 }
 
@@ -129,11 +143,16 @@ __device__ __forceinline__ bool bar_wait_bounded(uint64_t* bar, uint32_t parity)
 // [cols x K] tile-ordered (tiled_index with TR = 128 and 256), hi/lo parts.
 // mode 0: interleaved (re, im) columns -> P[row][col/2] = re^2 + im^2
 // mode 1: out[row][col] = scale * C  (FP64), for row < rows_valid, col < cols_valid
+// stall_last: a test of the bounded waits.  The producer stops before the
+// last chunk (no arrival, no copy), so the MMA thread's wait for that chunk
+// runs out; every copy issued has been consumed, the CTA writes no output,
+// sets *err, frees its TMEM and returns.
 __global__ void __launch_bounds__(kThreads, 1)
 k_gemm_split_bf16(const __nv_bfloat16* __restrict__ Ah, const __nv_bfloat16* __restrict__ Al,
                   const __nv_bfloat16* __restrict__ Bh, const __nv_bfloat16* __restrict__ Bl,
                   int K, int mode, float* __restrict__ P, int ldp, double* __restrict__ out,
-                  int ldo, int rows_valid, int cols_valid, double scale, int* __restrict__ err) {
+                  int ldo, int rows_valid, int cols_valid, double scale, int* __restrict__ err,
+                  int stall_last) {
     extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
     uint64_t* empty = full + kStages;
@@ -173,6 +192,7 @@ k_gemm_split_bf16(const __nv_bfloat16* __restrict__ Ah, const __nv_bfloat16* __r
             int c = 0;
             for (; c < nk; ++c) {
                 const int st = c % kStages;
+                if (stall_last && c == nk - 1) break;
                 if (c >= kStages && !bar_wait_bounded(empty + st, (uint32_t)((c / kStages - 1) & 1))) {
                     atomicExch(s_fail, 1);
                     break;
@@ -215,7 +235,9 @@ k_gemm_split_bf16(const __nv_bfloat16* __restrict__ Ah, const __nv_bfloat16* __r
         }
         __syncwarp();
     }
-    // everyone: the accumulator is complete (or the pipeline gave up)
+    // everyone, once the producer and the MMA thread have stopped issuing:
+    // the accumulator is complete (or the pipeline gave up)
+    __syncthreads();
     const bool landed = bar_wait_bounded(done, 0u);
     if (!landed) atomicExch(s_fail, 1);
     __syncthreads();
@@ -366,6 +388,13 @@ Tables tables(int M) {
 
 }  // namespace
 
+// the bounded-wait test switch (pgb_test_isf_tc_stall)
+std::atomic<int> g_stall_test{0};
+
+void isf_tc_set_stall_test(int on) { g_stall_test.store(on ? 1 : 0); }
+
+size_t isf_tc_error_offset(int nq, int M) { return layout(nq, M).err; }
+
 bool isf_tc_supported(int M) { return M >= 128 && M <= 2048 && (M % 128) == 0; }
 
 size_t isf_tc_scratch_bytes(int nq, int M) { return layout(nq, M).total; }
@@ -390,6 +419,7 @@ cudaError_t isf_tc_build_tables(int M, void* d_tables, cudaStream_t s) {
 cudaError_t launch_isf_tc(const float2* d_rho, int nq, int M, double norm, double* d_out,
                           void* d_scratch, const void* d_tables, cudaStream_t s) {
     if (!isf_tc_supported(M) || nq <= 0 || !d_tables) return cudaErrorInvalidValue;
+    const int stall = g_stall_test.load();
     const Layout L = layout(nq, M);
     const Tables T = tables(M);
     char* base = static_cast<char*>(d_scratch);
@@ -413,12 +443,12 @@ cudaError_t launch_isf_tc(const float2* d_rho, int nq, int M, double norm, doubl
     // GEMM 1: [qpad x 2M] x [2M x 2M] -> P [qpad x M]
     dim3 g1(2 * M / kTN, L.qpad / kTM);
     k_gemm_split_bf16<<<g1, kThreads, kSmem, s>>>(a1h, a1l, b1h, b1l, 2 * M, 0, P, M, nullptr, 0,
-                                                  L.qpad, 2 * M, 0.0, err);
+                                                  L.qpad, 2 * M, 0.0, err, stall);
     k_prep_p<<<152 * 4, 256, 0, s>>>(P, L.qpad, M, a2h, a2l);
     // GEMM 2: [qpad x M] x [M x colpad2] -> F [nq x (M/2+1)]
     dim3 g2(L.colpad2 / kTN, L.qpad / kTM);
     k_gemm_split_bf16<<<g2, kThreads, kSmem, s>>>(a2h, a2l, b2h, b2l, M, 1, nullptr, 0, d_out,
-                                                  M / 2 + 1, nq, M / 2 + 1, norm / (double)M, err);
+                                                  M / 2 + 1, nq, M / 2 + 1, norm / (double)M, err, 0);
     return cudaGetLastError();
 }
 

@@ -180,6 +180,10 @@ cudaError_t isf_tc_build_tables(int M, void* d_tables, cudaStream_t s);
 cudaError_t launch_isf_tc(const float2* d_rho, int nq, int M, double norm,
                           double* d_out, void* d_scratch, const void* d_tables, cudaStream_t s);
 bool isf_tc_supported(int M);
+// the pipeline's error word (int, 0 or 1) at this offset of the scratch
+size_t isf_tc_error_offset(int nq, int M);
+// test switch: the first GEMM of later calls stalls before its last chunk
+void isf_tc_set_stall_test(int on);
 
 }  // namespace pgb
 
