@@ -93,17 +93,19 @@ enum { WM_COM = 0, WM_DIAG, WM_OPEN, WM_CLOSE, WM_INSERT, WM_REMOVE, WM_AH, WM_R
        WM_SH, WM_ST, WM_N };
 enum { WERR_FULL = 1, WERR_LINK = 2, WERR_LOOP = 3 };
 
-// A CTA holds kCtaWarps warps: either kCtaWarps small walkers of one warp
-// each, or one large walker (N0 >= kTeamMinN) served by a team of all of them.
-// In a team, warp 0 runs the move logic as a single-warp walker does, and
-// every pair sum (a move's range or bead action) and every energy sample is
-// split over the team's warps: warp 0 posts the job in shared memory, the
-// team meets at a named barrier, each warp sums its share of the partners
-// (or slices), and after a second barrier warp 0 adds the shares in warp
-// order.  A large walker's chain of dependent moves stays on one warp; its
-// pair work, most of its instructions, runs on four.
+// A CTA holds kCtaWarps warps: kCtaWarps small walkers of one warp each, two
+// walkers of kTeamMinN <= N0 < kTeam4MinN served by teams of two warps, or
+// one walker of N0 >= kTeam4MinN served by a team of all four.  In a team,
+// its first warp runs the move logic as a single-warp walker does, and every
+// pair sum (a move's range or bead action) and every energy sample is split
+// over the team's warps: the first warp posts the job in shared memory, the
+// team meets at its own named barrier, each warp sums its share of the beads
+// (or slices), and after a second barrier the first warp adds the shares in
+// warp order.  A large walker's chain of dependent moves stays on one warp;
+// its pair work, most of its instructions, runs on the team.
 constexpr int kCtaWarps = 4;
 constexpr int kTeamMinN = 32;
+constexpr int kTeam4MinN = 64;
 constexpr int kTeamMinBeads = 4;     // shorter range actions of a team walker stay on its warp 0
 constexpr int kRunCap = 128;         // per-bead shares a team warp keeps (a worm move's run <= Mbar + 1)
 constexpr int kOrigCap = 72;         // saved positions per move (Mbar - 1 <= 63)
@@ -122,8 +124,11 @@ struct TeamJob {
     float khi[kCtaWarps], klo[kCtaWarps];    // each warp's kinetic share (energy)
     int bad[kCtaWarps];                      // a warp met a locator outside the arrays
 };
-__device__ __forceinline__ void team_sync(int nthreads) {
-    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+// named barrier `id` (1 + the team's place in its CTA: 1 or 2) over the
+// team's threads; constant ids, so the kernel reserves three barriers
+__device__ __forceinline__ void team_sync(int id, int nthreads) {
+    if (id == 1) asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+    else asm volatile("bar.sync 2, %0;" ::"r"(nthreads) : "memory");
 }
 
 // Aziz V with the reference's hard-core branch (potential.cpp:1821-1843):
@@ -159,7 +164,8 @@ struct WormWalker {
     int* chain;                      // shared: the beads of the current move's range, packed
     float* znorm;                    // shared: a move's normal deviates, 3 (Mbar - 1) at most
     int lane;
-    int team = 1;                    // warps serving this walker (1, or kCtaWarps for a team)
+    int team = 1;                    // warps serving this walker (1, 2 or kCtaWarps)
+    int bar = 1;                     // the team's named barrier
     int wk = 0;                      // this warp's place in the team
     TeamJob* job = nullptr;          // the team's mailbox
     float2* tpart = nullptr;         // shared: a team's per-bead sums, kRunCap at most
@@ -441,11 +447,11 @@ struct WormWalker {
             job->op = op; job->a = a; job->b = b;
             job->head = head; job->tail = tail; job->sp1 = sp1; job->sp2 = sp2;
         }
-        team_sync(32 * team);
+        team_sync(bar, 32 * team);
     }
     __device__ double teamCollect(float2 mine, bool ok) {
         if (lane == 0) { job->hi[0] = mine.x; job->lo[0] = mine.y; job->bad[0] = ok ? 0 : 1; }
-        team_sync(32 * team);
+        team_sync(bar, 32 * team);
         double s = 0.0;
         int bad = 0;
         for (int q = 0; q < team; ++q) { s += (double)job->hi[q] + (double)job->lo[q]; bad |= job->bad[q]; }
@@ -501,7 +507,7 @@ struct WormWalker {
             bool ok = true;
             teamBeadShares(pairCtx(), chain, c0, cnt, 0, team, ok, tpart);
             if (lane == 0) job->bad[0] = ok ? 0 : 1;
-            team_sync(32 * team);
+            team_sync(bar, 32 * team);
             int bad = 0;
             for (int q = 0; q < team; ++q) bad |= job->bad[q];
             if (bad) err = WERR_LINK;
@@ -1520,7 +1526,7 @@ struct WormWalker {
             float2 p, k;
             energyShare(pairCtx(), nxt, t0, t1, team, p, k);
             if (lane == 0) { job->hi[0] = p.x; job->lo[0] = p.y; job->khi[0] = k.x; job->klo[0] = k.y; }
-            team_sync(32 * team);
+            team_sync(bar, 32 * team);
             double pot = 0.0, kin = 0.0;
             for (int q = 0; q < team; ++q) {
                 pot += (double)job->hi[q] + (double)job->lo[q];
@@ -1599,7 +1605,7 @@ struct WormWalker {
 // adaptive centre-of-mass step) it makes 5 % centre-of-mass moves and
 // staging moves: from seeded worldlines with overlapping particles these
 // relax in tens of steps where bisection needs hundreds.
-__device__ __noinline__ void run_walker(int w, int team, TeamJob* job, const WWMeta* __restrict__ meta,
+__device__ __noinline__ void run_walker(int w, int team, int bar, TeamJob* job, const WWMeta* __restrict__ meta,
                                         float4* __restrict__ pos, int* __restrict__ nxt, int* __restrict__ prv,
                                         int* __restrict__ nbs, const long long* __restrict__ nbs_off,
                                         WWState* __restrict__ states, pgb_worm_walker_stats* __restrict__ stats,
@@ -1621,6 +1627,7 @@ __device__ __noinline__ void run_walker(int w, int team, TeamJob* job, const WWM
     ww.acts = s_scr;
     ww.qbuf = s_newp;
     ww.team = team;
+    ww.bar = bar;
     ww.wk = 0;
     ww.job = job;
     ww.tpart = tpart;
@@ -1764,9 +1771,11 @@ __device__ __noinline__ void run_walker(int w, int team, TeamJob* job, const WWM
 }
 
 
-// the helper warps of a team: take the share that warp 0 posts until it
-// posts the stop
-__device__ __noinline__ void team_helper(int w, int wk, const WWMeta* __restrict__ meta, float4* __restrict__ pos,
+// the helper warps of a team of T warps (this one the wk-th) meeting at
+// named barrier `bar`: take the share that the team's first warp posts until
+// it posts the stop
+__device__ __noinline__ void team_helper(int w, int wk, int T, int bar, const WWMeta* __restrict__ meta,
+                                         float4* __restrict__ pos,
                                          int* __restrict__ nxt, int* __restrict__ nbs,
                                          const long long* __restrict__ nbs_off, const AzizF& az, int* chain,
                                          TeamJob* job, float2* tpart) {
@@ -1779,32 +1788,35 @@ __device__ __noinline__ void team_helper(int w, int wk, const WWMeta* __restrict
     ww.nbs = nbs + nbs_off[w];
     ww.chain = chain;
     for (;;) {
-        team_sync(32 * kCtaWarps);
+        team_sync(bar, 32 * T);
         const int op = job->op;
         if (op == 0) break;
         ww.head = job->head; ww.tail = job->tail; ww.sp1 = job->sp1; ww.sp2 = job->sp2;
         const WormWalker::PairCtx c = ww.pairCtx();
         if (op == 1) {
             bool ok = true;
-            const float2 r = WormWalker::teamShare(c, chain, job->a, job->b, wk, kCtaWarps, ok);
+            const float2 r = WormWalker::teamShare(c, chain, job->a, job->b, wk, T, ok);
             if (ww.lane == 0) { job->hi[wk] = r.x; job->lo[wk] = r.y; job->bad[wk] = ok ? 0 : 1; }
         } else if (op == 3) {
             bool ok = true;
-            WormWalker::teamBeadShares(c, chain, job->a, job->b, wk, kCtaWarps, ok, tpart);
+            WormWalker::teamBeadShares(c, chain, job->a, job->b, wk, T, ok, tpart);
             if (ww.lane == 0) job->bad[wk] = ok ? 0 : 1;
         } else {
             float2 p, k;
-            WormWalker::energyShare(c, ww.nxt, job->a + wk, job->b, kCtaWarps, p, k);
+            WormWalker::energyShare(c, ww.nxt, job->a + wk, job->b, T, p, k);
             if (ww.lane == 0) { job->hi[wk] = p.x; job->lo[wk] = p.y; job->khi[wk] = k.x; job->klo[wk] = k.y; }
         }
-        team_sync(32 * kCtaWarps);
+        team_sync(bar, 32 * T);
     }
 }
 
 // plan[4 b .. 4 b + 3] lists the walkers of CTA b: up to four small walkers
-// (-1 for an empty place), or one large walker and kPlanTeam in the second
-// place, served by the CTA's warps as a team
+// (-1 for an empty place); or one large walker and kPlanTeam in the second
+// place, served by the CTA's four warps as a team; or two walkers in the
+// first and third places (the third -1 when there is one) and kPlanPair in
+// the second, each served by a team of two warps
 constexpr int kPlanTeam = -2;
+constexpr int kPlanPair = -3;
 
 __global__ void __launch_bounds__(kCtaWarps * 32)
 k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* __restrict__ nxt,
@@ -1817,29 +1829,35 @@ k_worm_walkers(const WWMeta* __restrict__ meta, float4* __restrict__ pos, int* _
     __shared__ int s_chain[kCtaWarps][kChainCap];
     __shared__ double s_scr[kCtaWarps][3 * kOrigCap / 2];
     __shared__ double s_cum[kCtaWarps][2 * WM_N];
-    __shared__ TeamJob s_job;
+    __shared__ TeamJob s_job[2];
     const int warp = threadIdx.x >> 5;
     const int* pl = plan + kCtaWarps * blockIdx.x;
-    if (pl[1] == kPlanTeam) {
-        const int w = pl[0];
-        if (warp == 0) {
-            // a team uses only the first warp's buffers; the second warp's chain
-            // cache holds the team's per-bead shares
-            float2* tpart = reinterpret_cast<float2*>(s_chain[1]);
-            run_walker(w, kCtaWarps, &s_job, meta, pos, nxt, prv, nbs, nbs_off, states, stats, az, sweeps, limit,
-                       budget_ns, diag_only, s_orig[0], s_newp[0], s_chain[0], s_scr[0], s_cum[0], tpart);
+    if (pl[1] == kPlanTeam || pl[1] == kPlanPair) {
+        const int T = pl[1] == kPlanTeam ? kCtaWarps : 2;
+        const int g = warp / T;                 // the team's place in the CTA
+        const int first = g * T;                // its first warp
+        const int w = pl[2 * g];
+        if (w < 0) return;                      // an empty pair place: no barrier is used
+        const int bar = 1 + g;
+        // a team uses its first warp's buffers; its second warp's chain cache
+        // holds the team's per-bead shares
+        float2* tpart = reinterpret_cast<float2*>(s_chain[first + 1]);
+        if (warp == first) {
+            run_walker(w, T, bar, &s_job[g], meta, pos, nxt, prv, nbs, nbs_off, states, stats, az, sweeps, limit,
+                       budget_ns, diag_only, s_orig[first], s_newp[first], s_chain[first], s_scr[first],
+                       s_cum[first], tpart);
             // every path out of run_walker ends here: release the helpers
-            if ((threadIdx.x & 31) == 0) s_job.op = 0;
-            team_sync(32 * kCtaWarps);
+            if ((threadIdx.x & 31) == 0) s_job[g].op = 0;
+            team_sync(bar, 32 * T);
         } else {
-            team_helper(w, warp, meta, pos, nxt, nbs, nbs_off, az, s_chain[0], &s_job,
-                        reinterpret_cast<float2*>(s_chain[1]));
+            team_helper(w, warp - first, T, bar, meta, pos, nxt, nbs, nbs_off, az, s_chain[first], &s_job[g],
+                        tpart);
         }
         return;
     }
     const int w = pl[warp];
     if (w < 0) return;
-    run_walker(w, 1, nullptr, meta, pos, nxt, prv, nbs, nbs_off, states, stats, az, sweeps, limit, budget_ns,
+    run_walker(w, 1, 1, nullptr, meta, pos, nxt, prv, nbs, nbs_off, states, stats, az, sweeps, limit, budget_ns,
                diag_only, s_orig[warp], s_newp[warp], s_chain[warp], s_scr[warp], s_cum[warp], nullptr);
 }
 
@@ -1931,16 +1949,23 @@ __global__ void k_normals_check(uint2 key, int skip, int count, float* serial, f
 using namespace pgb;
 
 // The CTAs of a launch over walkers listed largest first: a walker of
-// N0 >= kTeamMinN gets a CTA of its own, served as a team; the others share
-// CTAs four to one, in the same order.  A walker's schedule depends only on
-// its own N0, so its chain does not depend on which walkers run beside it.
+// N0 >= kTeam4MinN gets a CTA of its own, served by a team of four warps;
+// walkers of kTeamMinN <= N0 < kTeam4MinN share CTAs two to one, each served
+// by a team of two; the others share CTAs four to one; each kind in the
+// same order.  A walker's schedule depends only on its own N0, so its chain
+// does not depend on which walkers run beside it.
 static int build_plan(const std::vector<int>& order, const std::vector<WWMeta>& meta, std::vector<int>& plan) {
     plan.clear();
     std::vector<int> small;
+    int pending = -1;                           // a pair walker waiting for its partner
     for (int w : order) {
-        if (meta[w].N0 >= kTeamMinN) plan.insert(plan.end(), {w, kPlanTeam, -1, -1});
-        else small.push_back(w);
+        if (meta[w].N0 >= kTeam4MinN) plan.insert(plan.end(), {w, kPlanTeam, -1, -1});
+        else if (meta[w].N0 >= kTeamMinN) {
+            if (pending < 0) pending = w;
+            else { plan.insert(plan.end(), {pending, kPlanPair, w, -1}); pending = -1; }
+        } else small.push_back(w);
     }
+    if (pending >= 0) plan.insert(plan.end(), {pending, kPlanPair, -1, -1});
     for (size_t i = 0; i < small.size(); i += kCtaWarps)
         for (int k = 0; k < kCtaWarps; ++k) plan.push_back(i + k < small.size() ? small[i + k] : -1);
     return (int)(plan.size() / kCtaWarps);

@@ -173,13 +173,13 @@ def test_worm_walkers_grand_canonical_match_oracle_statistically(pgb, oracle_lib
     assert abs(e_w - eo) <= 4.0 * np.hypot(se_w, se_o), (e_w, se_w, eo, se_o)
 
 
-@pytest.mark.parametrize("n", [8, 80], ids=["one_warp", "team"])
+@pytest.mark.parametrize("n", [8, 48, 112], ids=["one_warp", "pair_team", "quad_team"])
 def test_walker_pair_sums_match_fp64_oracle(pgb, oracle_lib, n):
     """The walkers' FP32 pair sums (Kahan lanes, double-float warp reduction)
     against the FP64 oracle's barePotentialAction on the walkers' own paths
     after some steps (worm open or closed, special beads set): within 2e-4
     relative, most of it the oracle's piecewise-constant table (|V'| dr).
-    N = 80 walkers run as four-warp teams."""
+    N = 48 walkers run as two-warp teams, N = 112 as four-warp teams."""
     L = wl.box_side(n)
     W = pgb.WormWalkers(np.full(8, n), M, L, 8, TAU, LAM, mu=-1.0, window=-1, seed=13)
     W.seed_device(13)
@@ -199,13 +199,14 @@ def test_walker_pair_sums_match_fp64_oracle(pgb, oracle_lib, n):
         assert np.max(np.abs(got - want) / np.maximum(np.abs(want), 1.0)) <= 2e-4, w
 
 
-def test_team_walkers_match_oracle_statistically(pgb, oracle_lib):
-    """Walkers of N >= 32 run as four-warp teams (pair sums and energy samples
-    split over the warps): grand canonical at mu = -1 K, N0 = 64, M = 16,
-    <E/N> and <N> over closed configurations within four combined standard
-    errors of the oracle's worm engine; a team walker and the same walker run
-    twice give the same chain."""
-    n, m, tau, mu = 64, 16, 0.01, -1.0
+@pytest.mark.parametrize("n", [48, 100], ids=["pair_team", "quad_team"])
+def test_team_walkers_match_oracle_statistically(pgb, oracle_lib, n):
+    """Walkers of 32 <= N0 < 64 run as two-warp teams, N0 >= 64 as four-warp
+    teams (pair sums and energy samples split over the warps): grand canonical
+    at mu = -1 K, M = 16, <E/N> and <N> over closed configurations within
+    four combined standard errors of the oracle's worm engine; a team walker
+    and the same walker run twice give the same chain."""
+    m, tau, mu = 16, 0.01, -1.0
     L = wl.box_side(n)
     cfg = wl.seeded_worldlines(n, m, L, LAM, tau, 1, extent=3 * n)
     kw = dict(mbar=8, temperature=1.0 / (m * tau), initial_num_particles=n, window=-1, mu=mu,
