@@ -649,15 +649,29 @@ struct WormWalker {
     // positions of a free-particle walk of cnt beads from r0 (newFreeParticle
     // position, move.cpp:183-203: each bead a Gaussian step of sqrt(2 lambda
     // tau) from the previous), into qbuf; the 3 cnt deviates come from the
-    // lanes together, the same words serial draws would use
-    __device__ void freeWalk(float4 r0, int cnt) {
+    // lanes together, the same words serial draws would use.  The walk is a
+    // prefix sum of the steps over the lanes in unwrapped coordinates, each
+    // bead put in the box afterwards: the positions the serial walk (which
+    // wraps every step) gives, up to rounding.
+    __device__ __noinline__ void freeWalk(float4 r0, int cnt) {
         normals(3 * cnt, znorm);
         const float sg = (float)m.sqrt2LambdaTau;
-        float4 r = r0;
-        for (int k = 0; k < cnt; ++k) {
-            r = make_float4(putInBC(fmaf(znorm[3 * k], sg, r.x)), putInBC(fmaf(znorm[3 * k + 1], sg, r.y)),
-                            putInBC(fmaf(znorm[3 * k + 2], sg, r.z)), 0.f);
-            if (lane == 0) qbuf[k] = r;
+        float ux = r0.x, uy = r0.y, uz = r0.z;
+        for (int base = 0; base < cnt; base += 32) {
+            const int k = base + lane;
+            float dx = 0.f, dy = 0.f, dz = 0.f;
+            if (k < cnt) { dx = znorm[3 * k] * sg; dy = znorm[3 * k + 1] * sg; dz = znorm[3 * k + 2] * sg; }
+            for (int o = 1; o < 32; o <<= 1) {
+                const float px = __shfl_up_sync(0xffffffffu, dx, o), py = __shfl_up_sync(0xffffffffu, dy, o),
+                            pz = __shfl_up_sync(0xffffffffu, dz, o);
+                if (lane >= o) { dx += px; dy += py; dz += pz; }
+            }
+            const float vx = ux + dx, vy = uy + dy, vz = uz + dz;
+            if (k < cnt) qbuf[k] = make_float4(putInBC(vx), putInBC(vy), putInBC(vz), 0.f);
+            const int last = min(cnt - base, 32) - 1;
+            ux = __shfl_sync(0xffffffffu, vx, last);
+            uy = __shfl_sync(0xffffffffu, vy, last);
+            uz = __shfl_sync(0xffffffffu, vz, last);
         }
         __syncwarp();
     }
@@ -745,45 +759,59 @@ struct WormWalker {
         const int idx = h ? __ffs(h) - 1 : kMaxWind - 1;
         return winding(idx);
     }
-    // newStagingPosition with winding (move.cpp:301-338): np is the previous
-    // bead's (new) position, e the range's end bead, z the three deviates
-    __device__ void stagingPosZ(float4 np, float4 e, int L, int k, int3& wind, float zx, float zy, float zz,
-                                float& x, float& y, float& z) {
-        const float f1 = 1.0f * (L - k - 1), f2 = 1.0f / (1.0f * (L - k));
-        const float sg = (float)m.sqrt2LambdaTau * sqrtf(f1 * f2);
-        float rx = ((e.x + m.L * wind.x) - np.x) * f2 + np.x;
-        float ry = ((e.y + m.L * wind.y) - np.y) * f2 + np.y;
-        float rz = ((e.z + m.L * wind.z) - np.z) * f2 + np.z;
-        rx = rx + zx * sg; ry = ry + zy * sg; rz = rz + zz * sg;
-        // the winding sector follows the sampled point (move.cpp:327-336)
-        const float h = 0.5f * m.L;
-        for (int g = 0; g < 64 && rx < -h; ++g) { ++wind.x; rx += m.L; }
-        for (int g = 0; g < 64 && rx >= h; ++g) { --wind.x; rx -= m.L; }
-        for (int g = 0; g < 64 && ry < -h; ++g) { ++wind.y; ry += m.L; }
-        for (int g = 0; g < 64 && ry >= h; ++g) { --wind.y; ry -= m.L; }
-        for (int g = 0; g < 64 && rz < -h; ++g) { ++wind.z; rz += m.L; }
-        for (int g = 0; g < 64 && rz >= h; ++g) { --wind.z; rz -= m.L; }
-        x = putInBC(rx); y = putInBC(ry); z = putInBC(rz);
-    }
-    __device__ __noinline__ void stagingPosR(float4 np, float4 e, int L, int k, int3& wind, float& x, float& y,
-                                             float& z) {
-        const float zx = randNormZ(), zy = randNormZ(), zz = randNormZ();
-        stagingPosZ(np, e, L, k, wind, zx, zy, zz, x, y, z);
-    }
-    __device__ void stagingPos(WB nbd, WB eb, int L, int k, int3& wind, float& x, float& y, float& z) {
-        stagingPosR(P(nbd), P(eb), L, k, wind, x, y, z);
+    // cnt <= 2 kOrigCap new staging positions (newStagingPosition with the
+    // winding sector, move.cpp:301-338) from `start` towards e over a range
+    // of L links, into out[0 .. cnt - 1] (shared), made by the lanes together.
+    // Bead k is r_k = (1 - f_k) r_{k-1} + f_k (e + L_box wind) + sigma_k z_k
+    // with f_k = 1 / (L - k); the sector's shifts, which the serial form
+    // applies whenever a bead leaves the box, move r_{k-1} and the target by
+    // the same amount and cancel, so the chain is an affine recurrence in
+    // unwrapped coordinates: a scan of the lanes' maps (A, B): u -> A u + B,
+    // each bead put in the box afterwards and the sector left where the
+    // serial wraps leave it.  The same positions up to rounding.
+    __device__ __noinline__ void stagePositions(int cnt, float4 start, float4 e, int L, int3& wind, float4* out) {
+        normals(3 * cnt, znorm);
+        const float Lb = m.L;
+        const float sg0 = (float)m.sqrt2LambdaTau;
+        const float Ex = e.x + Lb * wind.x, Ey = e.y + Lb * wind.y, Ez = e.z + Lb * wind.z;
+        float ux = start.x, uy = start.y, uz = start.z;
+        for (int base = 0; base < cnt; base += 32) {
+            const int k = base + lane;
+            float A = 1.0f, bx = 0.0f, by = 0.0f, bz = 0.0f;
+            if (k < cnt) {
+                const float f1 = 1.0f * (L - k - 1), f2 = 1.0f / (1.0f * (L - k));
+                const float sg = sg0 * sqrtf(f1 * f2);
+                A = 1.0f - f2;
+                bx = fmaf(znorm[3 * k], sg, Ex * f2);
+                by = fmaf(znorm[3 * k + 1], sg, Ey * f2);
+                bz = fmaf(znorm[3 * k + 2], sg, Ez * f2);
+            }
+            // inclusive scan: the earlier lanes' map applied first
+            for (int o = 1; o < 32; o <<= 1) {
+                const float pa = __shfl_up_sync(0xffffffffu, A, o);
+                const float px = __shfl_up_sync(0xffffffffu, bx, o), py = __shfl_up_sync(0xffffffffu, by, o),
+                            pz = __shfl_up_sync(0xffffffffu, bz, o);
+                if (lane >= o) { bx = fmaf(A, px, bx); by = fmaf(A, py, by); bz = fmaf(A, pz, bz); A *= pa; }
+            }
+            const float vx = fmaf(A, ux, bx), vy = fmaf(A, uy, by), vz = fmaf(A, uz, bz);
+            if (k < cnt) out[k] = make_float4(putInBC(vx), putInBC(vy), putInBC(vz), 0.f);
+            const int last = min(cnt - base, 32) - 1;
+            ux = __shfl_sync(0xffffffffu, vx, last);
+            uy = __shfl_sync(0xffffffffu, vy, last);
+            uz = __shfl_sync(0xffffffffu, vz, last);
+        }
+        if (cnt > 0) {
+            wind.x -= (int)rintf((ux - putInBC(ux)) * m.Linv);
+            wind.y -= (int)rintf((uy - putInBC(uy)) * m.Linv);
+            wind.z -= (int)rintf((uz - putInBC(uz)) * m.Linv);
+        }
+        __syncwarp();
     }
     // new staging positions for chain[1 .. cnt] from chain[0]'s position
-    // towards e, written by lane 0 and published once
+    // towards e (through qbuf), written lane-parallel
     __device__ void stageChain(int cnt, float4 start, float4 e, int L, int3& wind) {
-        normals(3 * cnt, znorm);
-        float4 pp = start;
-        for (int k = 0; k < cnt; ++k) {
-            float x, y, z;
-            stagingPosZ(pp, e, L, k, wind, znorm[3 * k], znorm[3 * k + 1], znorm[3 * k + 2], x, y, z);
-            pp = make_float4(x, y, z, 0.f);
-            if (lane == 0) pos[at(chain[k + 1])] = pp;
-        }
+        stagePositions(cnt, start, e, L, wind, qbuf);
+        for (int i = lane; i < cnt; i += 32) pos[at(chain[i + 1])] = qbuf[i];
         __syncwarp();
     }
     // save / restore chain[1 .. cnt] positions, lane-parallel
@@ -1133,16 +1161,7 @@ struct WormWalker {
         // (newStagingPosition with the winding sector, move.cpp:301-338)
         const int nnew = g0 - 1;
         if (nnew > 0) {
-            normals(3 * nnew, znorm);
-            float4 pp = P(head);
-            const float4 e = P(tail);
-            for (int k = 0; k < nnew; ++k) {
-                float x, y, z;
-                stagingPosZ(pp, e, g0, k, wind, znorm[3 * k], znorm[3 * k + 1], znorm[3 * k + 2], x, y, z);
-                pp = make_float4(x, y, z, 0.f);
-                if (lane == 0) qbuf[k] = pp;
-            }
-            __syncwarp();
+            stagePositions(nnew, P(head), P(tail), g0, wind, qbuf);
             if (!appendRun(head, nnew, +1, qbuf, 0)) return -2;
         } else {
             if (lane == 0) chain[0] = pack(head);
