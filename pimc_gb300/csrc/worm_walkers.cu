@@ -934,7 +934,8 @@ struct WormWalker {
     // Level l (shift s = 2^(l-1)) places the beads at offsets s, 3s, 5s, ...
     // about the midpoint of their neighbours at -s and +s, which are fixed
     // ends or beads placed at earlier levels, so the lanes place them
-    // together (deviates in the reference's bead order from normals()).  The
+    // together (the deviates of all levels made at the start by normals(),
+    // in the reference's level and bead order).  The
     // level's action is the list action of those beads at tau() = s tau
     // (primitive: no correction); level 1 adds the beads of the earlier
     // levels in their new and old positions; each level is tested against
@@ -968,6 +969,11 @@ struct WormWalker {
         acc->attempted[WM_DIAG]++;
         saveChain(numActive, orig);                     // orig[j - 1]: bead at offset j
         const float sgBase = (float)m.sqrtLambdaTau;
+        // the normal deviates of every level at once, level by level in the
+        // reference's order (a level rejected early leaves the later levels'
+        // deviates unused: independent draws, the same distribution)
+        normals(3 * numActive, znorm);
+        int zoff = 0;
         double oldDelta = 0.0;
         int moved = 0;
         for (int level = numLevels; level > 0; --level) {
@@ -975,8 +981,9 @@ struct WormWalker {
             const int cnt = 1 << (numLevels - level);  // offsets s (2i + 1), i < cnt
             gatherStride(s, 2 * s, cnt);
             double oldA = s * chainAction(kListOff, cnt);
-            normals(3 * cnt, znorm);
             const float sg = sgBase * sqrtf((float)s);
+            const float* z = znorm + 3 * zoff;
+            zoff += cnt;
             for (int i = lane; i < cnt; i += 32) {
                 const int j = s * (2 * i + 1);
                 const float4 pp = pos[at(chain[j - s])], pn = pos[at(chain[j + s])];
@@ -985,9 +992,8 @@ struct WormWalker {
                 const float mx = fmaf(0.5f, min_image32(pn.x - pp.x, m.L, m.Linv), pp.x);
                 const float my = fmaf(0.5f, min_image32(pn.y - pp.y, m.L, m.Linv), pp.y);
                 const float mz = fmaf(0.5f, min_image32(pn.z - pp.z, m.L, m.Linv), pp.z);
-                const float4 q = make_float4(putInBC(fmaf(znorm[3 * i], sg, mx)),
-                                             putInBC(fmaf(znorm[3 * i + 1], sg, my)),
-                                             putInBC(fmaf(znorm[3 * i + 2], sg, mz)), 0.f);
+                const float4 q = make_float4(putInBC(fmaf(z[3 * i], sg, mx)), putInBC(fmaf(z[3 * i + 1], sg, my)),
+                                             putInBC(fmaf(z[3 * i + 2], sg, mz)), 0.f);
                 newp[j - 1] = q;
                 pos[at(chain[j])] = q;
             }
@@ -1346,10 +1352,10 @@ struct WormWalker {
     // by a scan inside that sector.
     // rho0 of one sector as the product of its three axis factors, the form
     // the sector sums use
-    __device__ static float rho0Shifted(float4 pf, float4 pb, int3 wv, int sign, float g3, float den, float L) {
+    __device__ static float rho0Shifted(float4 pf, float4 pb, int3 wv, int sign, float g3, float nden, float L) {
         const float ax = (pf.x - pb.x) + (float)(sign * wv.x) * L, ay = (pf.y - pb.y) + (float)(sign * wv.y) * L,
                     az_ = (pf.z - pb.z) + (float)(sign * wv.z) * L;
-        return g3 * expf(-(ax * ax) / den) * expf(-(ay * ay) / den) * expf(-(az_ * az_) / den);
+        return g3 * expf(ax * ax * nden) * expf(ay * ay * nden) * expf(az_ * az_ * nden);
     }
     __device__ __noinline__ double towerNorm(WB b, int pivotSlice, int sign, float x, WB& pivot, int3& wind) {
         const int nL = nb(pivotSlice);
@@ -1360,7 +1366,12 @@ struct WormWalker {
         const float g3 = g * g * g;
         const float L = m.L;
         const int ln = lane;
-        float mine = 0.0f;                       // ln w: sector w's weight
+        const float nden = -1.0f / den;
+        // each lane's share of the 27 sector weights (32 slots, the last five
+        // zero), summed over its beads
+        float acc[32];
+#pragma unroll
+        for (int w = 0; w < 32; ++w) acc[w] = 0.0f;
         for (int n0 = 0; n0 < nL; n0 += 128) {
             float4 pf[4];
 #pragma unroll
@@ -1371,30 +1382,38 @@ struct WormWalker {
             // rho0 factorises over the axes: three shifts per axis (component
             // 0, +1, -1 of the winding vector) give the 27 sector weights as
             // products, 9 exponentials a bead instead of 27
-            float ex[4][3], ey[4][3], ez[4][3];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const bool ok = n0 + 32 * u + ln < nL;
                 const float dx = pf[u].x - pb.x, dy = pf[u].y - pb.y, dz = pf[u].z - pb.z;
+                float ex[3], ey[3], ez[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const float sh = (float)(sign * (k == 2 ? -1 : k)) * L;
                     const float ax = dx + sh, ay = dy + sh, az_ = dz + sh;
-                    ex[u][k] = ok ? g3 * expf(-(ax * ax) / den) : 0.0f;
-                    ey[u][k] = expf(-(ay * ay) / den);
-                    ez[u][k] = expf(-(az_ * az_) / den);
+                    ex[k] = ok ? g3 * expf(ax * ax * nden) : 0.0f;
+                    ey[k] = expf(ay * ay * nden);
+                    ez[k] = expf(az_ * az_ * nden);
                 }
-            }
 #pragma unroll
-            for (int w = 0; w < kMaxWind; ++w) {
-                const int kx = (w / 9) % 3, ky = (w / 3) % 3, kz = w % 3;
-                float v = 0.0f;
-#pragma unroll
-                for (int u = 0; u < 4; ++u) v += ex[u][kx] * ey[u][ky] * ez[u][kz];
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                if (ln == w) mine += v;
+                for (int w = 0; w < kMaxWind; ++w) acc[w] = fmaf(ex[(w / 9) % 3] * ey[(w / 3) % 3], ez[w % 3], acc[w]);
             }
         }
+        // sector totals over the lanes by recursive halving: at each step a
+        // lane keeps the half of its slots that its partner lane does not,
+        // adding the partner's copy of them; lane w ends with sector w's total
+        // (31 shuffles instead of 27 five-step reductions)
+#pragma unroll
+        for (int h = 16; h >= 1; h >>= 1) {
+            const bool upper = (ln & h) != 0;
+#pragma unroll
+            for (int i = 0; i < h; ++i) {
+                const float send = upper ? acc[i] : acc[i + h];
+                const float keep = upper ? acc[i + h] : acc[i];
+                acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+            }
+        }
+        const float mine = ln < kMaxWind ? acc[0] : 0.0f;   // ln w: sector w's weight
         // inclusive scan of the sector sums over lanes 0..26
         float cum = ln < kMaxWind ? mine : 0.0f;
         for (int o = 1; o < 32; o <<= 1) {
@@ -1412,7 +1431,7 @@ struct WormWalker {
             int found = nL - 1;
             for (int base = 0; base < nL; base += 32) {
                 const int n = base + ln;
-                float v = n < nL ? rho0Shifted(row[n], pb, wv, sign, g3, den, L) : 0.0f;
+                float v = n < nL ? rho0Shifted(row[n], pb, wv, sign, g3, nden, L) : 0.0f;
                 for (int o = 1; o < 32; o <<= 1) {
                     const float u = __shfl_up_sync(0xffffffffu, v, o);
                     if (ln >= o) v += u;
