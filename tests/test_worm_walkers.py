@@ -248,3 +248,31 @@ def test_team_walkers_match_oracle_statistically(pgb, oracle_lib, n):
     n_w, sn_w = nw.mean(), nw.std(ddof=1) / np.sqrt(len(nw))
     assert abs(e_w - eo) <= 4.0 * np.hypot(se_w, se_o), (e_w, se_w, eo, se_o)
     assert abs(n_w - no) <= 4.0 * np.hypot(sn_w, sn_o), (n_w, sn_w, no, sn_o)
+
+
+def test_walker_chain_independent_of_the_mix(pgb):
+    """A walker's chain depends only on its own parameters and stream, not on
+    the walkers beside it.  Walker 0 (N0 = 48, a two-warp team) and walker 1
+    (N0 = 80, a four-warp team) give the same statistics and paths in two
+    mixes that place walker 0 first and then second of its CTA's two-warp
+    teams, one mix with an odd number of two-warp walkers (a CTA with an
+    empty second place) and small walkers beside them."""
+    m, tau, mu = 16, 0.01, -1.0
+    out = []
+    for ns in ([48, 80, 48, 10, 20], [48, 80, 50, 33, 100, 8]):
+        ns = np.array(ns)
+        W = pgb.WormWalkers(ns, m, wl.box_side(ns), 8, tau, LAM, mu=mu, window=-1, seed=21)
+        W.seed_device(21)
+        W.equilibrate(20)
+        W.run(40)
+        st = W.stats()
+        assert np.all(st["error"] == 0)
+        out.append((st, W.path(0), W.path(1)))
+        for w in range(len(ns)):
+            check_path(W.path(w), m)
+        W.close()
+    (sa, a0, a1), (sb, b0, b1) = out
+    for key in ("energy_sum", "n_sum", "samples", "attempted", "accepted", "bead_updates"):
+        assert np.array_equal(sa[key][:2], sb[key][:2]), key
+    for pa, pb in ((a0, b0), (a1, b1)):
+        assert np.array_equal(pa["next"], pb["next"]) and np.array_equal(pa["pos"], pb["pos"])
