@@ -463,7 +463,8 @@ int pgb_plain_worm_run(pgb_ctx* ctx, const pgb_worm_params* wp, int nsteps, int3
 
 /* ---- Device-resident worm walkers -----------------------------------------
  * Independent worm-algorithm paths (grand canonical, or canonical with a
- * particle window), one warp each, advanced by whole PIMC steps on the
+ * particle window), one warp per walker below N0 = 32 and a team of two
+ * (N0 < 64) or four warps above, advanced by whole PIMC steps on the
  * device: the reference's default move list with its attempt probabilities
  * (the same moves as pgb_plain_worm_run), primitive action, FP32 Aziz pairs
  * reduced in double-float, a Philox stream per walker.  They agree with the

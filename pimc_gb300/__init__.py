@@ -459,7 +459,8 @@ class Walkers:
 
 
 class WormWalkers:
-    """Device-resident worm-algorithm walkers, one warp each: the reference's
+    """Device-resident worm-algorithm walkers (one warp per small walker, a
+    team of two or four warps from N0 = 32 and 64): the reference's
     default PIMC move list on independent paths (grand canonical, or
     canonical with a particle window)."""
 

@@ -1,39 +1,44 @@
 // worm_walkers.cu -- device-resident worm-algorithm walkers.
 //
-// One warp owns one walker (an independent grand-canonical or windowed
-// canonical He-4 path) and runs the reference's PIMC step on it entirely on
-// the device: the default move list (centre of mass, staging, open, close,
-// insert, remove, advance/recede head and tail, swap head and tail) with the
+// Each walker (an independent grand-canonical or windowed canonical He-4
+// path) runs the reference's PIMC step entirely on the device: the default
+// move list (centre of mass, bisection or staging, open, close, insert,
+// remove, advance/recede head and tail, swap head and tail) with the
 // reference's attempt probabilities and diagonal/off-diagonal selection
 // (src/pimc.cpp:120-208, src/constants.cpp:191-205), the move semantics of
-// src/move.cpp:1124-1412, 1710-3826, the Path bookkeeping of
+// src/move.cpp:1124-1707, 1710-3826, the Path bookkeeping of
 // src/path.cpp:205-420 and the Worm state of src/worm.cpp:52-118.  The
 // plain form (plain_moves.cu) runs the same moves from the host with FP64
-// device actions and matches the oracle bit for bit; these walkers draw from
-// a Philox stream per walker and evaluate the primitive action in FP32 pair
-// sums reduced in double-float, so they agree with it statistically.
+// device actions and matches the compiled reference step for step; these
+// walkers draw from a Philox stream per walker and evaluate the primitive
+// action in FP32 pair sums reduced in double-float, so they agree with it
+// statistically.
 //
-// Execution model: the move logic runs redundantly and uniformly in all 32
-// lanes (every lane draws the same random numbers and makes the same
-// decisions); scalar state (worm locators, gap, length, counters) lives in
-// registers, identical in every lane; array writes (positions, links,
-// numBeadsAtSlice) are made by lane 0 and published with __syncwarp; pair
-// sums spread a bead's same-slice partners over the lanes.  Links store the
-// partner particle only: next(t, p) is on slice t + 1 and prev on t - 1.
+// Execution model: a small walker is one warp; a walker of N0 >= 32 is a
+// team of two or four warps (kTeamMinN, kTeam4MinN).  The move logic runs
+// redundantly and uniformly in all 32 lanes of the walker's first warp
+// (every lane draws the same random numbers and makes the same decisions);
+// scalar state (worm locators, gap, length, counters) lives in registers,
+// identical in every lane; array writes (positions, links, numBeadsAtSlice)
+// are made by lane 0, or lane-parallel for independent beads, and published
+// with __syncwarp; a team's other warps take their share of every range
+// action, per-bead action and energy sample.  Links store the partner
+// particle only: next(t, p) is on slice t + 1 and prev on t - 1.
 //
 // Latency, not throughput, bounds a walker: a move is a chain of dependent
-// link loads and warp reductions.  So (1) a move walks its range once and
-// caches the beads in shared memory (chain[]), and the actions, saves,
-// restores and centre-of-mass shifts index that cache, lane-parallel where
-// the beads are independent; (2) the pair terms of a lane have no branches
-// (absent partners add zero), so its four partner terms schedule together;
-// (3) the heavy helpers (pair sums, tower sampling, staging positions, bead
-// insertion and deletion, the energy) are not inlined: one copy of each
-// serves all twelve moves, which keeps the kernel's hot code within the
-// instruction cache when the warps of one SM run different moves; (4) one
-// walker per CTA, launched largest first, spreads the largest walkers over
-// the SMs; (5) a staging move's normal deviates come from the lanes together
-// (normals()), in the same order and from the same words as serial draws.
+// link loads, pair sums and warp reductions.  So (1) a move walks its range
+// once and caches the beads in shared memory (chain[]), and the actions,
+// saves, restores and centre-of-mass shifts index that cache; (2) the pair
+// terms of a lane have no branches (absent partners add zero), so its four
+// partner terms schedule together, and a team splits a range by beads, so
+// several beads' load chains are in flight; (3) position chains (staging
+// bridges, free-particle walks) are scans over the lanes, and a worm move's
+// run of new beads is placed at once and evaluated in doubling chunks; (4)
+// the heavy helpers are not inlined: one copy of each serves all twelve
+// moves, which keeps the kernel's code small for the instruction caches;
+// (5) the largest walkers are launched first; (6) a move's normal deviates
+// come from the lanes together (normals()), from the same words as serial
+// draws.
 //
 // Differences from the reference, all documented where they occur:
 //  * the swap pivot is drawn from the pivot slice's beads in index order
