@@ -298,6 +298,31 @@ struct WormWalker {
         if (p >= m.Ne) { err = WERR_LINK; return {-1, -1}; }
         return {b.t == 0 ? m.M - 1 : b.t - 1, p};
     }
+    // The link arrays and extents in registers for the walks along worldlines
+    // (next/prev with the same checks, a bad locator or link reported in
+    // `bad`): a walk reads one link a step and stores each bead to the move
+    // cache, after which the walker's own copy of these fields would be read
+    // again from local memory.
+    struct LinkWalk {
+        const int* nx;
+        const int* pv;
+        int M, Ne;
+        __device__ WB next(WB b, bool& bad) const {
+            if (b.t < 0 || b.t >= M || b.p < 0 || b.p >= Ne) { bad = true; return {-1, -1}; }
+            const int p = nx[(size_t)b.p * M + b.t];
+            if (p < 0) return {-1, -1};
+            if (p >= Ne) { bad = true; return {-1, -1}; }
+            return {b.t + 1 == M ? 0 : b.t + 1, p};
+        }
+        __device__ WB prev(WB b, bool& bad) const {
+            if (b.t < 0 || b.t >= M || b.p < 0 || b.p >= Ne) { bad = true; return {-1, -1}; }
+            const int p = pv[(size_t)b.p * M + b.t];
+            if (p < 0) return {-1, -1};
+            if (p >= Ne) { bad = true; return {-1, -1}; }
+            return {b.t == 0 ? M - 1 : b.t - 1, p};
+        }
+    };
+    __device__ LinkWalk links() const { return LinkWalk{nxt, prv, m.M, m.Ne}; }
     __device__ WB nextN(WB b, int n) { for (int i = 0; i < n && !isXW(b); ++i) b = next(b); return b; }
     __device__ WB prevN(WB b, int n) { for (int i = 0; i < n && !isXW(b); ++i) b = prev(b); return b; }
     // every access checks its bead: a bad locator sets the error word and
@@ -701,9 +726,11 @@ struct WormWalker {
         WB b = nt;
         length = 0;
         const int cap = m.mbar + 1;
+        const LinkWalk lw = links();
+        bool bad = false;
         do {
             ++length;
-            b = next(b);
+            b = lw.next(b, bad);
             if (isXW(b)) { err = WERR_LOOP; break; }
         } while (!eqW(b, nh) && length < cap);
         const float4 rt = P(nt), rh = P(nh);
@@ -855,9 +882,11 @@ struct WormWalker {
         WB b = first;
         int back = 0;
         bool closed = false;
+        const LinkWalk lw = links();
+        bool bad = false;
         for (;;) {
-            const WB pb = prev(b);
-            if (err) return 0;
+            const WB pb = lw.prev(b, bad);
+            if (bad) { err = WERR_LINK; return 0; }
             if (isXW(pb)) break;
             if (eqW(pb, first)) { closed = true; break; }
             if (back + 1 >= m.M) return 0;
@@ -875,8 +904,8 @@ struct WormWalker {
                 if (wl >= m.M) return 0;
                 if (lane == 0) chain[wl] = pack(s);
                 ++wl;
-                const WB ns = next(s);
-                if (err) return 0;
+                const WB ns = lw.next(s, bad);
+                if (bad) { err = WERR_LINK; return 0; }
                 if (isXW(ns)) break;
                 s = ns;
             }
@@ -911,9 +940,13 @@ struct WormWalker {
         sb.p = (int)randInt((uint32_t)(nb(sb.t) - 1));
         const int L = 2 + (int)randInt((uint32_t)(m.mbar - 2));
         WB b = sb;
+        const LinkWalk lw = links();
+        const int* cnts = nbs;
+        bool bad = false;
         for (int k = 0; k < L; ++k) {
-            if (b.p >= nb(b.t)) return 0;
-            const WB nb_ = next(b);
+            if (b.p >= cnts[b.t]) return 0;
+            const WB nb_ = lw.next(b, bad);
+            if (bad) { err = WERR_LINK; return 0; }
             if (isXW(nb_)) return 0;
             if (lane == 0) chain[k] = pack(b);
             b = nb_;
@@ -962,9 +995,13 @@ struct WormWalker {
         sb.p = (int)randInt((uint32_t)(nb(sb.t) - 1));
         if (numActive > kOrigCap) { err = WERR_LOOP; return 0; }
         WB b = sb;
+        const LinkWalk lw = links();
+        const int* cnts = nbs;
+        bool bad = false;
         for (int k = 0; k <= numActive; ++k) {
-            if (b.p >= nb(b.t)) return 0;
-            const WB nx = next(b);
+            if (b.p >= cnts[b.t]) return 0;
+            const WB nx = lw.next(b, bad);
+            if (bad) { err = WERR_LINK; return 0; }
             if (isXW(nx)) return 0;
             if (lane == 0) chain[k] = pack(b);
             b = nx;
@@ -1051,12 +1088,15 @@ struct WormWalker {
     __device__ int collectRun(WB a, WB b, int dir) {
         int cnt = 0;
         WB x = a;
-        for (int g = 0; g <= m.mbar + 1; ++g) {
+        const LinkWalk lw = links();
+        const int cap = m.mbar + 1;
+        bool bad = false;
+        for (int g = 0; g <= cap; ++g) {
             if (isXW(x)) { err = WERR_LINK; break; }
             if (lane == 0) chain[cnt] = pack(x);
             ++cnt;
             if (eqW(x, b)) break;
-            x = dir > 0 ? next(x) : prev(x);
+            x = dir > 0 ? lw.next(x, bad) : lw.prev(x, bad);
         }
         __syncwarp();
         return cnt;
@@ -1461,11 +1501,14 @@ struct WormWalker {
         WB pivot; int3 wind;
         const double SigmaHead = towerNorm(head, pivotSlice, 1, rand(), pivot, wind);
         WB b = pivot;
+        const LinkWalk lw = links();
+        bool bad = false;
         for (int k = 0; k < swapLength; k++) {
-            if (eqW(b, tail) || isXW(b)) return -1;
+            if (eqW(b, tail) || isXW(b)) { if (bad) err = WERR_LINK; return -1; }
             if (lane == 0) chain[swapLength - k] = pack(b);
-            b = prev(b);
+            b = lw.prev(b, bad);
         }
+        if (bad) err = WERR_LINK;
         const WB swp = b;
         if (isXW(swp) || eqW(tail, swp)) return -1;
         if (lane == 0) chain[0] = pack(swp);
@@ -1512,11 +1555,14 @@ struct WormWalker {
         WB pivot; int3 wind;
         const double SigmaTail = towerNorm(tail, pivotSlice, -1, rand(), pivot, wind);
         WB b = pivot;
+        const LinkWalk lw = links();
+        bool bad = false;
         for (int k = 0; k < swapLength; k++) {
-            if (eqW(b, head) || isXW(b)) return -1;
+            if (eqW(b, head) || isXW(b)) { if (bad) err = WERR_LINK; return -1; }
             if (lane == 0) chain[k] = pack(b);
-            b = next(b);
+            b = lw.next(b, bad);
         }
+        if (bad) err = WERR_LINK;
         const WB swp = b;
         if (isXW(swp) || eqW(head, swp)) return -1;
         if (lane == 0) chain[swapLength] = pack(swp);
