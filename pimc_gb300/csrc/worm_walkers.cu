@@ -372,6 +372,9 @@ struct WormWalker {
     // The fields a pair sum reads, copied once per call into registers: the
     // walker itself lives in local memory around the helpers that are not
     // inlined, and reading it there per pair would cost a load each time.
+    // The out-of-line pair loops (teamShare, teamBeadShares, energyShare)
+    // take it by value, so it arrives in their registers; by reference it
+    // would sit in the caller's local memory and every bead would reload it.
     struct PairCtx {
         const float4* pos;
         const int* nbs;
@@ -457,7 +460,7 @@ struct WormWalker {
     // of the dependent load chain of one warp walking it.  Returns the
     // warp's (double-float) sum; ok false for a locator outside the walker's
     // arrays.
-    __device__ __noinline__ static float2 teamShare(const PairCtx& c, const int* ch, int c0, int cnt, int wk, int T,
+    __device__ __noinline__ static float2 teamShare(const PairCtx c, const int* ch, int c0, int cnt, int wk, int T,
                                                     bool& ok) {
         KahanF k;
         if (wk < cnt) {
@@ -511,7 +514,7 @@ struct WormWalker {
     // One warp's share of a team's per-bead actions: the beads of its
     // teamShare share, each reduced on its own and written to part[i] by
     // lane 0
-    __device__ __noinline__ static void teamBeadShares(const PairCtx& c, const int* ch, int c0, int cnt, int wk,
+    __device__ __noinline__ static void teamBeadShares(const PairCtx c, const int* ch, int c0, int cnt, int wk,
                                                        int T, bool& ok, float2* part) {
         if (wk >= cnt) return;
         BeadLoad cur, nx;
@@ -1629,7 +1632,7 @@ struct WormWalker {
     }
     // the energy sums of slices t0, t0 + step, ... below t1 by one warp:
     // (pot, kin) as double-float pairs
-    __device__ __noinline__ static void energyShare(const PairCtx& c, const int* nx_, int t0, int t1, int step,
+    __device__ __noinline__ static void energyShare(const PairCtx c, const int* nx_, int t0, int t1, int step,
                                                     float2& pot_out, float2& kin_out) {
         KahanF pot, kin;
         for (int t = t0; t < t1; t += step) {
