@@ -225,50 +225,56 @@ struct WormWalker {
         return x * sqrtf(-2.0f * logf(r) / r);
     }
     __device__ float randNorm(float mean, float sd) { return mean + randNormZ() * sd; }
-    // word i ahead in the stream (rem = words left in buf)
-    __device__ uint32_t wordAhead(long long i, int rem) const {
-        if (i < rem) {
-            const int q = bidx + (int)i;
-            return q == 0 ? buf.x : q == 1 ? buf.y : q == 2 ? buf.z : buf.w;
-        }
-        const long long j = i - rem;
-        const unsigned long long c = ctr + (unsigned long long)(j >> 2);
-        const uint4 w = philox4x32(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0x574F524Du, 0u), m.key);
-        const int q = (int)(j & 3);
-        return q == 0 ? w.x : q == 1 ? w.y : q == 2 ? w.z : w.w;
-    }
     // the next cnt deviates that cnt calls of randNormZ() would return, made
     // by the lanes together from the same words: lane l tests attempt
     // a = base + l on words 2a and 2a + 1, the accepted attempts in order
     // give the deviates, and the stream then moves past the last attempt
     // used, exactly where the serial draws would leave it
+    // (the stream position is read into registers once: the walker's own
+    // copy lives in local memory)
     __device__ __noinline__ void normals(int cnt, float* out) {
         const int rem = 4 - bidx;
+        const int bi = bidx;
+        const uint4 bf = buf;
+        const unsigned long long c0 = ctr;
+        const uint2 key = m.key;
+        const int ln = lane;
+        auto word = [&](long long i) -> uint32_t {
+            if (i < rem) {
+                const int q = bi + (int)i;
+                return q == 0 ? bf.x : q == 1 ? bf.y : q == 2 ? bf.z : bf.w;
+            }
+            const long long j = i - rem;
+            const unsigned long long c = c0 + (unsigned long long)(j >> 2);
+            const uint4 w = philox4x32(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0x574F524Du, 0u), key);
+            const int q = (int)(j & 3);
+            return q == 0 ? w.x : q == 1 ? w.y : q == 2 ? w.z : w.w;
+        };
         int have = 0;
         long long base = 0, used = 0;
         for (int round = 0; have < cnt && round < 64; ++round, base += 32) {
-            const long long a = base + lane;
-            const float x = 2.0f * ((float)wordAhead(2 * a, rem) * 2.3283064365386963e-10f) - 1.0f;
-            const float y = 2.0f * ((float)wordAhead(2 * a + 1, rem) * 2.3283064365386963e-10f) - 1.0f;
+            const long long a = base + ln;
+            const float x = 2.0f * ((float)word(2 * a) * 2.3283064365386963e-10f) - 1.0f;
+            const float y = 2.0f * ((float)word(2 * a + 1) * 2.3283064365386963e-10f) - 1.0f;
             const float r = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));
             const bool ok = !(r >= 1.0f || r == 0.0f);
             const unsigned mask = __ballot_sync(0xffffffffu, ok);
-            const int rank = __popc(mask & ((1u << lane) - 1u));
+            const int rank = __popc(mask & ((1u << ln) - 1u));
             if (ok && have + rank < cnt) out[have + rank] = x * sqrtf(-2.0f * logf(r) / r);
             const unsigned last = __ballot_sync(0xffffffffu, ok && rank == cnt - have - 1);
             if (last) used = 2 * (base + __ffs(last));
             have += __popc(mask);
         }
         if (have < cnt) {                           // never in practice: 2048 attempts
-            for (int i = have + lane; i < cnt; i += 32) out[i] = 0.0f;
+            for (int i = have + ln; i < cnt; i += 32) out[i] = 0.0f;
             used = 2 * base;
         }
         if (used <= rem) {
             bidx += (int)used;
         } else {
             const long long wb = used - rem, nb = (wb + 3) >> 2;
-            const unsigned long long c = ctr + (unsigned long long)(nb - 1);
-            buf = philox4x32(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0x574F524Du, 0u), m.key);
+            const unsigned long long c = c0 + (unsigned long long)(nb - 1);
+            buf = philox4x32(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0x574F524Du, 0u), key);
             ctr = c + 1;
             bidx = (int)(wb - 4 * (nb - 1));
         }
