@@ -23,11 +23,13 @@ PER_FILE = {
     "fp64_kernels.cu": ["-fmad=false"],
     # FP32 pair and phase kernels: subnormal FP32 values flush to zero, which
     # drops the subnormal handling around rsqrt/ex2/sin/cos (about 6 % of the
-    # walker sweep); FP64 arithmetic is unaffected
+    # canonical walker sweep, 7 % of the worm walkers' step); FP64 arithmetic
+    # is unaffected
     "walkers.cu": ["-ftz=true"],
     "mixed_kernels.cu": ["-ftz=true"],
     "scatter.cu": ["-ftz=true"],
     "isf_static.cu": ["-ftz=true"],
+    "worm_walkers.cu": ["-ftz=true"],
     "path_estimators.cu": ["-fmad=false"],
     "gp.cu": ["-fmad=false"],
 }
