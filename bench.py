@@ -58,9 +58,9 @@ SFU_PER_SM_CLK = 16     # nominal special-function results per SM per clock
 # the workload its bench leg runs (profiles/ holds the summaries)
 NCU_TRAFFIC = {"k_walkers_pipe": 160.4e6, "k_walkers_group": 158.9e6}
 # DRAM bytes of one k_worm_walkers step on the 1024-walker workload, L2 flushed
-# before it (profiles/k_worm_walkers_walkers1024.md): 342.4 MB read + 46.9 MB
+# before it (profiles/k_worm_walkers_walkers1024.md): 344.5 MB read + 47.3 MB
 # written, about the walkers' resident state (396 MB) once
-NCU_TRAFFIC_WORM = 389.4e6
+NCU_TRAFFIC_WORM = 391.9e6
 L2_BYTES = 129 * 1024 * 1024
 
 
