@@ -82,3 +82,33 @@ def test_rank_reductions_over_gloo():
         assert p.exitcode == 0
     got = sorted(q.get(timeout=10) for _ in range(2))
     assert got == [(0, 2.5, 30.0), (1, 2.5, 30.0)]
+
+
+def _bench_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_kaplan_meier_quantiles():
+    """The serving line's time-to-first-bin and completion percentiles:
+    the Kaplan-Meier estimate over right-censored durations, worked by hand.
+    Without censoring it is the empirical quantile; a job censored at t
+    leaves the risk set after the events at t; a quantile the estimate never
+    reaches is None; the jobs at risk where each quantile is reached."""
+    km = _bench_module().km_quantiles
+    # no censoring: S = 3/4, 1/2, 1/4, 0 after 1, 2, 3, 4
+    assert km([1, 2, 3, 4], [True] * 4) == {50: 2.0, 99: 4.0}
+    # one censored job at 2: S = 3/4 after 1, then 3/4 (1 - 1/3) = 1/2 at 3,
+    # then 0 at 4 (one job at risk)
+    out, risk = km([4, 2, 1, 3], [True, False, True, True], with_risk=True)
+    assert out == {50: 3.0, 99: 4.0}
+    assert risk == {50: 2, 99: 1}
+    # the event and a censoring at the same time: the event first (4 at risk)
+    assert km([2, 2, 5, 6], [False, True, False, False], qs=(25,)) == {25: 2.0}
+    # most jobs still waiting when the window closes: the median lies beyond
+    out = km([1, 9, 9, 9, 9], [True, False, False, False, False])
+    assert out == {50: None, 99: None}
+    assert km([], [], qs=(50,)) == {50: None}
